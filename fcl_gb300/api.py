@@ -1,0 +1,378 @@
+"""Python mirror of FCL's proximity-query API for BVHModel<OBBRSS> meshes.
+
+Names, argument meaning and defaults follow FCL 0.7.0:
+  BVHModel.beginModel/addSubModel/endModel  geometry/bvh/BVH_model.h:56-227
+  CollisionRequest / CollisionResult / Contact  narrowphase/collision_request.h:52-106,
+                                                collision_result.h:52-93, contact.h:48-91
+  DistanceRequest / DistanceResult          narrowphase/distance_request.h:52-113,
+                                            distance_result.h
+  CollisionObject                           narrowphase/collision_object.h:50-157
+  collide(o1, o2, request, result)          narrowphase/collision.h:55-66
+  distance(o1, o2, request, result)         narrowphase/distance.h:51-62
+plus the batched entry points collide_batch / distance_batch.  Everything runs
+through the C ABI (include/fclgpu.h) on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native as N
+
+PRECISIONS = {"fp64": N.PLAIN_FP64, "plain": N.PLAIN_FP64, "fp32": N.FP32_RECHECK, "fp32_recheck": N.FP32_RECHECK}
+
+
+def _prec(p) -> int:
+    if isinstance(p, int):
+        return p
+    return PRECISIONS[p]
+
+
+class BVHModel:
+    """BVHModel<OBBRSS<double>>: triangles + vertices, BVH built by endModel()."""
+
+    def __init__(self):
+        self._verts: list[np.ndarray] = []
+        self._tris: list[np.ndarray] = []
+        self._nv = 0
+        self.handle = None
+        self.build_state = "empty"
+
+    # geometry/bvh/BVH_model-inl.h:207-248
+    def beginModel(self, num_tris: int = 0, num_vertices: int = 0) -> int:
+        self._verts, self._tris, self._nv = [], [], 0
+        self.build_state = "begun"
+        return 0
+
+    # BVH_model-inl.h:416-446
+    def addSubModel(self, vertices, triangles=None) -> int:
+        if self.build_state != "begun":
+            return -8  # BVH_ERR_BUILD_OUT_OF_SEQUENCE
+        v = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+        self._verts.append(v)
+        if triangles is not None:
+            t = np.ascontiguousarray(triangles, dtype=np.int64).reshape(-1, 3) + self._nv
+            self._tris.append(t.astype(np.int32))
+        self._nv += v.shape[0]
+        return 0
+
+    def addTriangle(self, p1, p2, p3) -> int:
+        return self.addSubModel(np.array([p1, p2, p3], np.float64), np.array([[0, 1, 2]], np.int32))
+
+    # BVH_model-inl.h:450-517
+    def endModel(self) -> int:
+        if self.build_state != "begun":
+            return -8
+        V = np.concatenate(self._verts) if self._verts else np.zeros((0, 3))
+        T = np.concatenate(self._tris) if self._tris else np.zeros((0, 3), np.int32)
+        if V.shape[0] == 0 or T.shape[0] == 0:
+            raise N.FclGpuError(-5, "endModel", "model with no triangles and vertices")
+        self.vertices = np.ascontiguousarray(V)
+        self.tri_indices = np.ascontiguousarray(T, dtype=np.int32)
+        h = C.c_void_p()
+        N.check(N.lib().fclgpu_mesh_create(self.vertices.ctypes.data, V.shape[0], self.tri_indices.ctypes.data,
+                                           T.shape[0], C.byref(h)), "fclgpu_mesh_create")
+        self.handle = h
+        self.build_state = "processed"
+        return 0
+
+    @classmethod
+    def from_arrays(cls, vertices, triangles) -> "BVHModel":
+        m = cls()
+        m.beginModel()
+        m.addSubModel(vertices, triangles)
+        m.endModel()
+        return m
+
+    def info(self) -> N.MeshInfo:
+        inf = N.MeshInfo()
+        N.check(N.lib().fclgpu_mesh_get_info(self.handle, C.byref(inf)), "fclgpu_mesh_get_info")
+        return inf
+
+    @property
+    def num_tris(self) -> int:
+        return int(self.tri_indices.shape[0])
+
+    @property
+    def num_vertices(self) -> int:
+        return int(self.vertices.shape[0])
+
+    @property
+    def num_bvs(self) -> int:
+        return int(self.info().num_nodes)
+
+    def get_nodes(self):
+        """(nodes (n,30) float64, first_child (n,) int32) in FCL's node order."""
+        n = self.num_bvs
+        out = np.empty((n, 30), np.float64)
+        fc = np.empty(n, np.int32)
+        N.check(N.lib().fclgpu_mesh_get_nodes(self.handle, out.ctypes.data, fc.ctypes.data), "fclgpu_mesh_get_nodes")
+        return out, fc
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.fclgpu_mesh_destroy(h)
+            self.handle = None
+
+
+def transform(R=None, t=None) -> np.ndarray:
+    tf = np.zeros((3, 4))
+    tf[:, :3] = np.eye(3) if R is None else np.asarray(R, np.float64)
+    if t is not None:
+        tf[:, 3] = np.asarray(t, np.float64)
+    return tf
+
+
+@dataclass
+class CollisionObject:
+    geometry: BVHModel
+    tf: np.ndarray = field(default_factory=lambda: transform())
+
+    def setTransform(self, R, t):
+        self.tf = transform(R, t)
+
+
+@dataclass
+class CollisionRequest:
+    num_max_contacts: int = 1
+    enable_contact: bool = False
+    enable_statistics: bool = False
+    precision: str = "fp32"
+
+
+@dataclass
+class Contact:
+    o1: object
+    o2: object
+    b1: int
+    b2: int
+
+    def __lt__(self, other):  # contact-inl.h:98-104
+        if self.b1 == other.b1:
+            return self.b2 < other.b2
+        return self.b1 < other.b1
+
+
+@dataclass
+class CollisionResult:
+    contacts: list = field(default_factory=list)
+    num_bv_tests: int = 0
+    num_leaf_tests: int = 0
+
+    def numContacts(self) -> int:
+        return len(self.contacts)
+
+    def isCollision(self) -> bool:
+        return len(self.contacts) > 0
+
+    def getContact(self, i: int) -> Contact:
+        return self.contacts[i]
+
+    def clear(self):
+        self.contacts = []
+
+
+@dataclass
+class DistanceRequest:
+    enable_nearest_points: bool = False
+    enable_signed_distance: bool = False
+    rel_err: float = 0.0
+    abs_err: float = 0.0
+    enable_statistics: bool = False
+    precision: str = "fp32"
+
+
+@dataclass
+class DistanceResult:
+    min_distance: float = float(np.finfo(np.float64).max)
+    nearest_points: np.ndarray = field(default_factory=lambda: np.zeros((2, 3)))
+    o1: object = None
+    o2: object = None
+    b1: int = -1
+    b2: int = -1
+
+    def clear(self):
+        self.min_distance = float(np.finfo(np.float64).max)
+        self.nearest_points = np.zeros((2, 3))
+        self.o1 = self.o2 = None
+        self.b1 = self.b2 = -1
+
+
+def _unsupported(req):
+    if getattr(req, "enable_contact", False):
+        raise N.FclGpuError(-9, "collide", "enable_contact (contact points/normals) is not on the GPU path")
+    if getattr(req, "enable_signed_distance", False):
+        raise N.FclGpuError(-9, "distance", "enable_signed_distance is not on the GPU path")
+    if getattr(req, "rel_err", 0.0) or getattr(req, "abs_err", 0.0):
+        raise N.FclGpuError(-9, "distance", "rel_err/abs_err must be 0 on the GPU path")
+
+
+def collide(o1: CollisionObject, o2: CollisionObject, request: CollisionRequest, result: CollisionResult) -> int:
+    """fcl::collide for two BVHModel<OBBRSS> objects; appends to result like FCL."""
+    _unsupported(request)
+    if request.num_max_contacts == 0:
+        return 0
+    out = collide_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None], o2.tf[None],
+                        pair_of_query=None, num_max_contacts=request.num_max_contacts, precision=request.precision,
+                        statistics=request.enable_statistics)
+    room = max(0, request.num_max_contacts - len(result.contacts))
+    for b1, b2 in out["contacts"][:room]:
+        result.contacts.append(Contact(o1.geometry, o2.geometry, int(b1), int(b2)))
+    if request.enable_statistics:
+        result.num_bv_tests = int(out["num_bv_tests"][0])
+        result.num_leaf_tests = int(out["num_leaf_tests"][0])
+    return result.numContacts()
+
+
+def distance(o1: CollisionObject, o2: CollisionObject, request: DistanceRequest, result: DistanceResult) -> float:
+    """fcl::distance for two BVHModel<OBBRSS> objects; DistanceResult::update semantics."""
+    _unsupported(request)
+    out = distance_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None], o2.tf[None],
+                         nearest_points=request.enable_nearest_points, precision=request.precision)
+    d = float(out["min_distance"][0])
+    if result.min_distance > d:
+        result.min_distance = d
+        result.o1, result.o2 = o1.geometry, o2.geometry
+        result.b1, result.b2 = int(out["ids"][0, 0]), int(out["ids"][0, 1])
+        if request.enable_nearest_points:
+            result.nearest_points = out["nearest_points"][0].copy()
+    return result.min_distance
+
+
+def _handles(meshes):
+    arr = (C.c_void_p * len(meshes))()
+    for i, m in enumerate(meshes):
+        arr[i] = m.handle.value if isinstance(m.handle, C.c_void_p) else m.handle
+    return arr
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def collide_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, precision="fp32",
+                  statistics=False, contacts=True, stream=None):
+    """Batched fcl::collide.  Host (numpy) inputs use the host entry point (copies in
+    and out); torch CUDA tensors use the device entry point.  Returns a dict with
+    counts, offsets, contacts (total, 2) and optional statistics."""
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    req = N.CollideRequest(int(num_max_contacts), _prec(precision), int(bool(statistics)), 0)
+    hs = _handles(meshes)
+    if _is_torch(tf2):
+        return _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statistics, contacts, stream)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(-1, 12)
+    pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
+    counts = np.zeros(n, np.int32)
+    offsets = np.zeros(n + 1, np.int64)
+    st = [np.zeros(n, np.int64) for _ in range(3)] if statistics else [None] * 3
+    cap = 0
+    while True:
+        buf = np.empty((max(cap, 1), 2), np.int32) if contacts else None
+        res = N.CollideResult(counts.ctypes.data, offsets.ctypes.data, None if buf is None else buf.ctypes.data,
+                              cap, *(None if a is None else a.ctypes.data for a in st), 0)
+        rc = N.lib().fclgpu_collide_batch(hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+                                          None if pq is None else pq.ctypes.data,
+                                          None if tf1a is None else tf1a.ctypes.data, tf2.ctypes.data,
+                                          C.byref(req), C.byref(res), stream)
+        if rc == N.FCLGPU_ERR_CAPACITY and contacts:
+            cap = int(res.total_contacts)
+            continue
+        N.check(rc, "fclgpu_collide_batch")
+        break
+    out = {"counts": counts, "offsets": offsets, "total_contacts": int(res.total_contacts)}
+    if contacts:
+        out["contacts"] = buf[: res.total_contacts]
+    if statistics:
+        out["num_bv_tests"], out["num_leaf_tests"], out["num_rechecks"] = st
+    return out
+
+
+def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statistics, contacts, stream):
+    import torch
+    dev = tf2.device
+    n = tf2.shape[0]
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    offsets = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    st = [torch.zeros(n, dtype=torch.int64, device=dev) for _ in range(3)] if statistics else [None] * 3
+    s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    cap = 0
+    buf = None
+    while True:
+        res = N.CollideResult(counts.data_ptr(), offsets.data_ptr(),
+                              None if buf is None else buf.data_ptr(), cap,
+                              *(None if a is None else a.data_ptr() for a in st), 0)
+        rc = N.lib().fclgpu_collide_batch_device(
+            hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+            None if pair_of_query is None else pair_of_query.data_ptr(),
+            None if tf1 is None else tf1.data_ptr(), tf2.data_ptr(), C.byref(req), C.byref(res), s)
+        if contacts and (rc == N.FCLGPU_ERR_CAPACITY or (rc == 0 and buf is None)):
+            cap = int(res.total_contacts)
+            buf = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=dev)
+            continue
+        N.check(rc, "fclgpu_collide_batch_device")
+        break
+    out = {"counts": counts, "offsets": offsets, "total_contacts": int(res.total_contacts)}
+    if contacts:
+        out["contacts"] = buf[: res.total_contacts]
+    if statistics:
+        out["num_bv_tests"], out["num_leaf_tests"], out["num_rechecks"] = st
+    return out
+
+
+def distance_batch(meshes, pairs, tf1, tf2, pair_of_query=None, nearest_points=True, precision="fp32",
+                   margins=None, statistics=False, stream=None):
+    """Batched fcl::distance.  Returns min_distance, ids (n,2), nearest_points (n,2,3)
+    world frame, optional within_margin (distance <= margin) and statistics."""
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    req = N.DistanceRequest(int(bool(nearest_points)), _prec(precision), int(bool(statistics)), 0)
+    hs = _handles(meshes)
+    if _is_torch(tf2):
+        import torch
+        dev = tf2.device
+        n = tf2.shape[0]
+        d = torch.empty(n, dtype=torch.float64, device=dev)
+        ids = torch.empty((n, 2), dtype=torch.int32, device=dev)
+        pts = torch.zeros((n, 2, 3), dtype=torch.float64, device=dev) if nearest_points else None
+        within = torch.empty(n, dtype=torch.int32, device=dev) if margins is not None else None
+        st = [torch.zeros(n, dtype=torch.int64, device=dev) for _ in range(3)] if statistics else [None] * 3
+        res = N.DistanceResult(d.data_ptr(), ids.data_ptr(), None if pts is None else pts.data_ptr(),
+                               None if margins is None else margins.data_ptr(),
+                               None if within is None else within.data_ptr(),
+                               *(None if a is None else a.data_ptr() for a in st))
+        s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        N.check(N.lib().fclgpu_distance_batch_device(
+            hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+            None if pair_of_query is None else pair_of_query.data_ptr(),
+            None if tf1 is None else tf1.data_ptr(), tf2.data_ptr(), C.byref(req), C.byref(res), s),
+            "fclgpu_distance_batch_device")
+    else:
+        tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+        n = tf2.shape[0]
+        tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(-1, 12)
+        pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
+        mg = None if margins is None else np.ascontiguousarray(margins, np.float64)
+        d = np.empty(n, np.float64)
+        ids = np.empty((n, 2), np.int32)
+        pts = np.zeros((n, 2, 3), np.float64) if nearest_points else None
+        within = np.empty(n, np.int32) if margins is not None else None
+        st = [np.zeros(n, np.int64) for _ in range(3)] if statistics else [None] * 3
+        res = N.DistanceResult(d.ctypes.data, ids.ctypes.data, None if pts is None else pts.ctypes.data,
+                               None if mg is None else mg.ctypes.data, None if within is None else within.ctypes.data,
+                               *(None if a is None else a.ctypes.data for a in st))
+        N.check(N.lib().fclgpu_distance_batch(
+            hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n, None if pq is None else pq.ctypes.data,
+            None if tf1a is None else tf1a.ctypes.data, tf2.ctypes.data, C.byref(req), C.byref(res), stream),
+            "fclgpu_distance_batch")
+    out = {"min_distance": d, "ids": ids}
+    if nearest_points:
+        out["nearest_points"] = pts
+    if margins is not None:
+        out["within_margin"] = within
+    if statistics:
+        out["num_bv_tests"], out["num_leaf_tests"], out["num_rechecks"] = st
+    return out

@@ -1,0 +1,502 @@
+// C ABI of the library (include/fclgpu.h): mesh registry, batched collide and
+// distance entry points, device scratch management and status reporting.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fclgpu.h"
+#include "bvh_build.h"
+#include "kernels.h"
+
+using namespace fclgpu;
+
+struct fclgpu_mesh_s {
+  DevMesh dev;
+  fclgpu_mesh_info info;
+  std::vector<void*> allocations;
+};
+
+namespace {
+
+std::recursive_mutex g_mu;
+int g_device = -1;
+thread_local std::string g_detail;
+
+int fail(int code, const std::string& why) {
+  g_detail = why;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* where) {
+  g_detail = std::string(where) + ": " + cudaGetErrorString(e);
+  return (e == cudaErrorMemoryAllocation) ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
+}
+
+#define CK(expr, where)                              \
+  do {                                               \
+    cudaError_t e_ = (expr);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+  } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) {
+      cudaError_t e = cudaFree(p);
+      if (e != cudaSuccess) return e;
+      p = nullptr;
+      cap = 0;
+    }
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+};
+
+struct Scratch {
+  DevBuf meshes, pairs, ctr, records, counts, offsets, scan_tmp;
+  DevBuf in_pair, in_tf1, in_tf2, in_margin;
+  DevBuf out_contacts, out_nbv, out_nleaf, out_nrc, out_dist, out_ids, out_pts, out_within;
+  int64_t record_hint = 0;
+  int64_t last_nrec = 0;  // records written by the last collide launch
+};
+Scratch g_scratch;
+
+int ensure_init() {
+  if (g_device >= 0) return FCLGPU_OK;
+  int dev = 0;
+  CK(cudaGetDevice(&dev), "cudaGetDevice");
+  g_device = dev;
+  return FCLGPU_OK;
+}
+
+template <class T>
+int upload(DevBuf& b, const T* host, size_t count, cudaStream_t s, const char* what) {
+  CK(b.ensure(sizeof(T) * std::max<size_t>(count, 1)), what);
+  if (count) CK(cudaMemcpyAsync(b.p, host, sizeof(T) * count, cudaMemcpyHostToDevice, s), what);
+  return FCLGPU_OK;
+}
+
+// Common validation + mesh/pair tables.  Returns the traversal stack size needed.
+int prepare_tables(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host, int32_t num_pairs,
+                   cudaStream_t s, int* stack_entries) {
+  if (!meshes || num_meshes <= 0 || !pairs_host || num_pairs <= 0)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "meshes and pairs must be non-empty");
+  std::vector<DevMesh> tab(num_meshes);
+  for (int i = 0; i < num_meshes; ++i) {
+    if (!meshes[i]) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null mesh handle");
+    tab[i] = meshes[i]->dev;
+  }
+  int need = 0;
+  for (int p = 0; p < num_pairs; ++p) {
+    const int a = pairs_host[2 * p], b = pairs_host[2 * p + 1];
+    if (a < 0 || a >= num_meshes || b < 0 || b >= num_meshes)
+      return fail(FCLGPU_ERR_INVALID_ARGUMENT, "pair index out of range");
+    need = std::max(need, tab[a].max_depth + tab[b].max_depth + 2);
+  }
+  if (need > 256) return fail(FCLGPU_ERR_STACK_DEPTH, "BVH pair deeper than 256 levels");
+  *stack_entries = need <= 64 ? 64 : 256;
+  int rc = upload(g_scratch.meshes, tab.data(), tab.size(), s, "upload mesh table");
+  if (rc) return rc;
+  std::vector<int2> pr(num_pairs);
+  for (int p = 0; p < num_pairs; ++p) pr[p] = make_int2(pairs_host[2 * p], pairs_host[2 * p + 1]);
+  rc = upload(g_scratch.pairs, pr.data(), pr.size(), s, "upload pair table");
+  if (rc) return rc;
+  return FCLGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fclgpu_status_string(int status) {
+  switch (status) {
+    case FCLGPU_OK: return "ok";
+    case FCLGPU_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FCLGPU_ERR_CUDA: return "CUDA error";
+    case FCLGPU_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FCLGPU_ERR_CAPACITY: return "output capacity too small";
+    case FCLGPU_ERR_EMPTY_MODEL: return "model has no triangles or vertices";
+    case FCLGPU_ERR_STACK_DEPTH: return "BVH too deep for the traversal stack";
+    case FCLGPU_ERR_DEVICE_STATUS: return "kernel reported an internal error";
+    case FCLGPU_ERR_NOT_INITIALIZED: return "not initialized";
+    case FCLGPU_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* fclgpu_last_error_detail(void) { return g_detail.c_str(); }
+
+int fclgpu_init(int device) {
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int n = 0;
+  CK(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+  if (device < 0 || device >= n) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "no such device");
+  CK(cudaSetDevice(device), "cudaSetDevice");
+  CK(cudaFree(nullptr), "context");
+  g_device = device;
+  return FCLGPU_OK;
+}
+
+int64_t fclgpu_kernel_launch_count(void) { return g_kernel_launches; }
+
+int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out) {
+  if (!out) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (nv <= 0 || nt <= 0 || !verts || !tris) return fail(FCLGPU_ERR_EMPTY_MODEL, "empty model");
+  if (nt > (1 << 29)) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many triangles");
+  for (int64_t i = 0; i < 3 * nt; ++i)
+    if (tris[i] < 0 || tris[i] >= nv) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "triangle index out of range");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+
+  HostBVH bvh;
+  if (build_obbrss(verts, nv, tris, nt, bvh) != 0) return fail(FCLGPU_ERR_EMPTY_MODEL, "empty model");
+  PackedF32 pk;
+  pack_fp32(verts, tris, nt, bvh, pk);
+
+  fclgpu_mesh_s* m = new fclgpu_mesh_s();
+  auto alloc = [&](void** p, size_t bytes, const void* src) -> cudaError_t {
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return e;
+    m->allocations.push_back(*p);
+    return cudaMemcpy(*p, src, bytes, cudaMemcpyHostToDevice);
+  };
+  const size_t nn = bvh.nodes.size();
+  void *p_n64, *p_r64, *p_v64, *p_t, *p_n32, *p_s64, *p_r32, *p_t32;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = alloc(&p_n64, sizeof(NodeD) * nn, bvh.nodes.data());
+  if (e == cudaSuccess) e = alloc(&p_r64, sizeof(RssD) * nn, bvh.rss.data());
+  if (e == cudaSuccess) e = alloc(&p_v64, sizeof(double) * 3 * nv, verts);
+  if (e == cudaSuccess) e = alloc(&p_t, sizeof(int32_t) * 3 * nt, tris);
+  if (e == cudaSuccess) e = alloc(&p_n32, sizeof(float) * pk.nodes32.size(), pk.nodes32.data());
+  if (e == cudaSuccess) e = alloc(&p_s64, sizeof(double) * pk.size64.size(), pk.size64.data());
+  if (e == cudaSuccess) e = alloc(&p_r32, sizeof(float) * pk.rss32.size(), pk.rss32.data());
+  if (e == cudaSuccess) e = alloc(&p_t32, sizeof(float) * pk.tri32.size(), pk.tri32.data());
+  if (e != cudaSuccess) {
+    for (void* p : m->allocations) cudaFree(p);
+    delete m;
+    return cuda_fail(e, "mesh upload");
+  }
+  double vmax = 0.0;
+  for (int64_t i = 0; i < 3 * nv; ++i) vmax = std::max(vmax, std::fabs(verts[i]));
+  DevMesh& d = m->dev;
+  d.nodes64 = (const NodeD*)p_n64;
+  d.rss64 = (const RssD*)p_r64;
+  d.verts64 = (const double*)p_v64;
+  d.tris = (const int32_t*)p_t;
+  d.nodes32 = p_n32;
+  d.size64 = (const double*)p_s64;
+  d.rss32 = p_r32;
+  d.tri32 = p_t32;
+  d.n_nodes = (int32_t)nn;
+  d.n_tris = (int32_t)nt;
+  d.n_verts = (int32_t)nv;
+  d.max_depth = bvh.max_depth;
+  // inflate the magnitude constants slightly so they bound the FP64 values after rounding
+  d.vmax = vmax * (1.0 + 1e-12);
+  d.cmax = pk.cmax * (1.0 + 1e-12);
+  d.rmax = pk.rmax * (1.0 + 1e-12);
+  m->info.num_vertices = nv;
+  m->info.num_tris = nt;
+  m->info.num_nodes = (int64_t)nn;
+  m->info.max_depth = bvh.max_depth;
+  m->info.reserved = 0;
+  m->info.max_abs_coord = vmax;
+  m->info.device_bytes = (int64_t)(nn * (sizeof(NodeD) + sizeof(RssD) + 64 + 8 + 32) + nv * 24 + nt * (12 + 48));
+  *out = m;
+  return FCLGPU_OK;
+}
+
+int fclgpu_mesh_destroy(fclgpu_mesh mesh) {
+  if (!mesh) return FCLGPU_OK;
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  for (void* p : mesh->allocations) cudaFree(p);
+  delete mesh;
+  return FCLGPU_OK;
+}
+
+int fclgpu_mesh_get_info(fclgpu_mesh mesh, fclgpu_mesh_info* info) {
+  if (!mesh || !info) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
+  *info = mesh->info;
+  return FCLGPU_OK;
+}
+
+int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t* first_child) {
+  if (!mesh || !nodes30 || !first_child) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t nn = (size_t)mesh->dev.n_nodes;
+  std::vector<NodeD> nd(nn);
+  std::vector<RssD> rs(nn);
+  CK(cudaMemcpy(nd.data(), mesh->dev.nodes64, sizeof(NodeD) * nn, cudaMemcpyDeviceToHost), "read nodes");
+  CK(cudaMemcpy(rs.data(), mesh->dev.rss64, sizeof(RssD) * nn, cudaMemcpyDeviceToHost), "read rss");
+  for (size_t i = 0; i < nn; ++i) {
+    double* o = nodes30 + 30 * i;
+    for (int k = 0; k < 9; ++k) o[k] = nd[i].axis[k];
+    for (int k = 0; k < 3; ++k) o[9 + k] = nd[i].To[k];
+    for (int k = 0; k < 3; ++k) o[12 + k] = nd[i].ext[k];
+    for (int k = 0; k < 9; ++k) o[15 + k] = nd[i].axis[k];
+    for (int k = 0; k < 3; ++k) o[24 + k] = rs[i].To[k];
+    o[27] = rs[i].l[0];
+    o[28] = rs[i].l[1];
+    o[29] = rs[i].r;
+    first_child[i] = nd[i].child;
+  }
+  return FCLGPU_OK;
+}
+
+int fclgpu_collide_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                                const double* tf2, const fclgpu_collide_request* req, fclgpu_collide_result* res,
+                                void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or counts");
+  if (n >= (int64_t)1 << 31) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "batch too large");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int stack = 64;
+  rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+  if (rc) return rc;
+  res->total_contacts = 0;
+  if (n == 0) {
+    if (res->offsets) CK(cudaMemsetAsync(res->offsets, 0, sizeof(int64_t), s), "offsets");
+    return FCLGPU_OK;
+  }
+  Scratch& S = g_scratch;
+  CK(S.ctr.ensure(sizeof(BatchCounters)), "counters");
+  const int64_t maxc = std::max<int64_t>(req->num_max_contacts, 0);
+  int64_t rec_cap = std::max<int64_t>(S.record_hint, std::min<int64_t>(n * std::max<int64_t>(maxc, 1), 4 * n) + 65536);
+  for (int attempt = 0; attempt < 6; ++attempt) {
+    CK(S.records.ensure(sizeof(int4) * (size_t)rec_cap), "record scratch");
+    rec_cap = (int64_t)(S.records.cap / sizeof(int4));
+    CK(cudaMemsetAsync(S.ctr.p, 0, sizeof(BatchCounters), s), "counters");
+    CollideLaunch L;
+    L.meshes = (const DevMesh*)S.meshes.p;
+    L.pairs = (const int2*)S.pairs.p;
+    L.pair_of_query = pair_of_query;
+    L.tf1 = tf1;
+    L.tf2 = tf2;
+    L.n = n;
+    L.num_max_contacts = (int32_t)std::min<int64_t>(maxc, INT32_MAX);
+    L.want_stats = req->enable_statistics;
+    L.ctr = (BatchCounters*)S.ctr.p;
+    L.records = (int4*)S.records.p;
+    L.record_cap = rec_cap;
+    L.counts = res->counts;
+    L.nbv = res->num_bv_tests;
+    L.nleaf = res->num_leaf_tests;
+    L.nrecheck = res->num_rechecks;
+    const int block = 128;
+    const int grid = collide_grid(req->precision, stack, block);
+    CK(launch_mesh_collide(L, req->precision, stack, grid, block, s), "collide kernel");
+    BatchCounters hc;
+    CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
+    CK(cudaStreamSynchronize(s), "collide kernel");
+    if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
+    if (hc.status & DEV_ERR_RECORDS) {
+      rec_cap = (int64_t)hc.records + 65536;
+      S.record_hint = rec_cap;
+      continue;
+    }
+    const int64_t nrec = (int64_t)hc.records;
+    S.record_hint = std::max<int64_t>(S.record_hint, nrec);
+    S.last_nrec = nrec;
+    if (!res->offsets && !res->contacts) return FCLGPU_OK;
+    int64_t* offsets = res->offsets;
+    if (!offsets) {
+      CK(S.offsets.ensure(sizeof(int64_t) * (size_t)(n + 1)), "offsets scratch");
+      offsets = (int64_t*)S.offsets.p;
+    }
+    CK(S.scan_tmp.ensure(sizeof(int64_t) * (size_t)(2 * ((n + 4095) / 4096) + 4)), "scan scratch");
+    CK(launch_exclusive_scan(res->counts, n, offsets, (int64_t*)S.scan_tmp.p, s), "scan");
+    int64_t total = 0;
+    CK(cudaMemcpyAsync(&total, offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read total");
+    CK(cudaStreamSynchronize(s), "scan");
+    res->total_contacts = total;
+    if (!res->contacts) return FCLGPU_OK;
+    if (total > res->contacts_capacity) return fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
+    CK(launch_scatter_contacts((const int4*)S.records.p, nrec, offsets, res->contacts, s), "scatter");
+    return FCLGPU_OK;
+  }
+  return fail(FCLGPU_ERR_OUT_OF_MEMORY, "contact record scratch kept overflowing");
+}
+
+int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                         int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                         const double* tf2, const fclgpu_collide_request* req, fclgpu_collide_result* res,
+                         void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or counts");
+  cudaStream_t s = (cudaStream_t)stream;
+  Scratch& S = g_scratch;
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);  // held across the device call and the copies
+  {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (pair_of_query) CK(S.in_pair.ensure(4 * nn), "inputs");
+    if (tf1) CK(S.in_tf1.ensure(96 * nn), "inputs");
+    CK(S.in_tf2.ensure(96 * nn), "inputs");
+    CK(S.counts.ensure(4 * nn), "outputs");
+    CK(S.offsets.ensure(8 * (nn + 1)), "outputs");
+    if (res->num_bv_tests) CK(S.out_nbv.ensure(8 * nn), "outputs");
+    if (res->num_leaf_tests) CK(S.out_nleaf.ensure(8 * nn), "outputs");
+    if (res->num_rechecks) CK(S.out_nrc.ensure(8 * nn), "outputs");
+    if (pair_of_query) CK(cudaMemcpyAsync(S.in_pair.p, pair_of_query, 4 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (tf1) CK(cudaMemcpyAsync(S.in_tf1.p, tf1, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    CK(cudaMemcpyAsync(S.in_tf2.p, tf2, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+  }
+  fclgpu_collide_result dr = *res;
+  dr.counts = (int32_t*)S.counts.p;
+  dr.offsets = (int64_t*)S.offsets.p;
+  dr.contacts = nullptr;
+  dr.num_bv_tests = res->num_bv_tests ? (int64_t*)S.out_nbv.p : nullptr;
+  dr.num_leaf_tests = res->num_leaf_tests ? (int64_t*)S.out_nleaf.p : nullptr;
+  dr.num_rechecks = res->num_rechecks ? (int64_t*)S.out_nrc.p : nullptr;
+  // first pass computes counts and offsets; contacts are scattered into device scratch
+  // sized from the total, then copied out
+  int rc = fclgpu_collide_batch_device(meshes, num_meshes, pairs_host, num_pairs, n,
+                                       pair_of_query ? (const int32_t*)S.in_pair.p : nullptr,
+                                       tf1 ? (const double*)S.in_tf1.p : nullptr, (const double*)S.in_tf2.p, req,
+                                       &dr, stream);
+  if (rc) return rc;
+  res->total_contacts = dr.total_contacts;
+  if (res->contacts) {
+    if (dr.total_contacts > res->contacts_capacity) return fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
+    CK(S.out_contacts.ensure(8 * (size_t)std::max<int64_t>(dr.total_contacts, 1)), "contacts scratch");
+    // records of the last launch are still in scratch: scatter them now
+    CK(launch_scatter_contacts((const int4*)S.records.p, S.last_nrec, (const int64_t*)S.offsets.p,
+                               (int32_t*)S.out_contacts.p, s),
+       "scatter");
+    if (dr.total_contacts)
+      CK(cudaMemcpyAsync(res->contacts, S.out_contacts.p, 8 * dr.total_contacts, cudaMemcpyDeviceToHost, s), "d2h");
+  }
+  CK(cudaMemcpyAsync(res->counts, S.counts.p, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->offsets) CK(cudaMemcpyAsync(res->offsets, S.offsets.p, 8 * (n + 1), cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_bv_tests) CK(cudaMemcpyAsync(res->num_bv_tests, S.out_nbv.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_leaf_tests)
+    CK(cudaMemcpyAsync(res->num_leaf_tests, S.out_nleaf.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_rechecks) CK(cudaMemcpyAsync(res->num_rechecks, S.out_nrc.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  CK(cudaStreamSynchronize(s), "collide batch");
+  return FCLGPU_OK;
+}
+
+int fclgpu_distance_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                 int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                                 const double* tf2, const fclgpu_distance_request* req, fclgpu_distance_result* res,
+                                 void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->min_distance)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or min_distance");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int stack = 64;
+  rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+  if (rc) return rc;
+  if (n == 0) return FCLGPU_OK;
+  Scratch& S = g_scratch;
+  CK(S.ctr.ensure(sizeof(BatchCounters)), "counters");
+  CK(cudaMemsetAsync(S.ctr.p, 0, sizeof(BatchCounters), s), "counters");
+  DistanceLaunch L;
+  L.meshes = (const DevMesh*)S.meshes.p;
+  L.pairs = (const int2*)S.pairs.p;
+  L.pair_of_query = pair_of_query;
+  L.tf1 = tf1;
+  L.tf2 = tf2;
+  L.n = n;
+  L.nearest = req->enable_nearest_points;
+  L.want_stats = req->enable_statistics;
+  L.ctr = (BatchCounters*)S.ctr.p;
+  L.dist = res->min_distance;
+  L.ids = res->ids;
+  L.points = res->nearest_points;
+  L.margins = res->margins;
+  L.within = res->within_margin;
+  L.nbv = res->num_bv_tests;
+  L.nleaf = res->num_leaf_tests;
+  L.nrecheck = res->num_rechecks;
+  const int block = 128;
+  const int grid = distance_grid(req->precision, stack, block);
+  CK(launch_mesh_distance(L, req->precision, stack, grid, block, s), "distance kernel");
+  BatchCounters hc;
+  CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
+  CK(cudaStreamSynchronize(s), "distance kernel");
+  if (hc.status) return fail(FCLGPU_ERR_DEVICE_STATUS, "distance kernel status word set");
+  return FCLGPU_OK;
+}
+
+int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                          int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                          const double* tf2, const fclgpu_distance_request* req, fclgpu_distance_result* res,
+                          void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->min_distance)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or min_distance");
+  cudaStream_t s = (cudaStream_t)stream;
+  Scratch& S = g_scratch;
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (pair_of_query) CK(S.in_pair.ensure(4 * nn), "inputs");
+    if (tf1) CK(S.in_tf1.ensure(96 * nn), "inputs");
+    CK(S.in_tf2.ensure(96 * nn), "inputs");
+    if (res->margins) CK(S.in_margin.ensure(8 * nn), "inputs");
+    CK(S.out_dist.ensure(8 * nn), "outputs");
+    if (res->ids) CK(S.out_ids.ensure(8 * nn), "outputs");
+    if (res->nearest_points) CK(S.out_pts.ensure(48 * nn), "outputs");
+    if (res->within_margin) CK(S.out_within.ensure(4 * nn), "outputs");
+    if (res->num_bv_tests) CK(S.out_nbv.ensure(8 * nn), "outputs");
+    if (res->num_leaf_tests) CK(S.out_nleaf.ensure(8 * nn), "outputs");
+    if (res->num_rechecks) CK(S.out_nrc.ensure(8 * nn), "outputs");
+    if (pair_of_query) CK(cudaMemcpyAsync(S.in_pair.p, pair_of_query, 4 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (tf1) CK(cudaMemcpyAsync(S.in_tf1.p, tf1, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    CK(cudaMemcpyAsync(S.in_tf2.p, tf2, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (res->margins) CK(cudaMemcpyAsync(S.in_margin.p, res->margins, 8 * n, cudaMemcpyHostToDevice, s), "h2d");
+  }
+  fclgpu_distance_result dr;
+  dr.min_distance = (double*)S.out_dist.p;
+  dr.ids = res->ids ? (int32_t*)S.out_ids.p : nullptr;
+  dr.nearest_points = res->nearest_points ? (double*)S.out_pts.p : nullptr;
+  dr.margins = res->margins ? (const double*)S.in_margin.p : nullptr;
+  dr.within_margin = res->within_margin ? (int32_t*)S.out_within.p : nullptr;
+  dr.num_bv_tests = res->num_bv_tests ? (int64_t*)S.out_nbv.p : nullptr;
+  dr.num_leaf_tests = res->num_leaf_tests ? (int64_t*)S.out_nleaf.p : nullptr;
+  dr.num_rechecks = res->num_rechecks ? (int64_t*)S.out_nrc.p : nullptr;
+  int rc = fclgpu_distance_batch_device(meshes, num_meshes, pairs_host, num_pairs, n,
+                                        pair_of_query ? (const int32_t*)S.in_pair.p : nullptr,
+                                        tf1 ? (const double*)S.in_tf1.p : nullptr, (const double*)S.in_tf2.p, req,
+                                        &dr, stream);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(res->min_distance, dr.min_distance, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->ids) CK(cudaMemcpyAsync(res->ids, dr.ids, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->nearest_points)
+    CK(cudaMemcpyAsync(res->nearest_points, dr.nearest_points, 48 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->within_margin)
+    CK(cudaMemcpyAsync(res->within_margin, dr.within_margin, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_bv_tests) CK(cudaMemcpyAsync(res->num_bv_tests, dr.num_bv_tests, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_leaf_tests)
+    CK(cudaMemcpyAsync(res->num_leaf_tests, dr.num_leaf_tests, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->num_rechecks) CK(cudaMemcpyAsync(res->num_rechecks, dr.num_rechecks, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  CK(cudaStreamSynchronize(s), "distance batch");
+  return FCLGPU_OK;
+}
+
+}  // extern "C"

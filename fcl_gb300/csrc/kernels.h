@@ -1,0 +1,77 @@
+// Internal launch interface between the C ABI layer and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fclgpu_types.h"
+
+namespace fclgpu {
+
+// Device status word bits (written by kernels, read by the host after a batch).
+enum : uint32_t {
+  DEV_ERR_STACK = 1u,     // traversal stack overflow
+  DEV_ERR_RECORDS = 2u,   // contact record scratch overflow
+};
+
+// Counters shared by one batch launch (device scratch).
+struct BatchCounters {
+  unsigned long long work;      // next query to fetch
+  unsigned long long records;   // contact-record slots reserved
+  unsigned int status;          // DEV_ERR_* bits
+  unsigned int pad;
+};
+
+struct CollideLaunch {
+  const DevMesh* meshes;
+  const int2* pairs;
+  const int32_t* pair_of_query;  // may be null (all queries use pair 0)
+  const double* tf1;             // may be null (identity)
+  const double* tf2;
+  int64_t n;
+  int32_t num_max_contacts;
+  int32_t want_stats;
+  BatchCounters* ctr;
+  int4* records;                 // (query, rank, b1, b2)
+  int64_t record_cap;
+  int32_t* counts;
+  int64_t* nbv;
+  int64_t* nleaf;
+  int64_t* nrecheck;
+};
+
+struct DistanceLaunch {
+  const DevMesh* meshes;
+  const int2* pairs;
+  const int32_t* pair_of_query;
+  const double* tf1;
+  const double* tf2;
+  int64_t n;
+  int32_t nearest;
+  int32_t want_stats;
+  BatchCounters* ctr;
+  double* dist;
+  int32_t* ids;
+  double* points;
+  const double* margins;
+  int32_t* within;
+  int64_t* nbv;
+  int64_t* nleaf;
+  int64_t* nrecheck;
+};
+
+// precision: 0 = plain FP64, 1 = FP32 with FP64 recheck.  stack_entries: 64 or 256.
+cudaError_t launch_mesh_collide(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
+                                cudaStream_t s);
+cudaError_t launch_mesh_distance(const DistanceLaunch& L, int precision, int stack_entries, int grid, int block,
+                                 cudaStream_t s);
+// offsets[0..n] = exclusive scan of counts (int32 -> int64), using tmp (>= 2*ceil(n/4096)+2 int64).
+cudaError_t launch_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, int64_t* tmp, cudaStream_t s);
+// contacts[offsets[q] + rank] = (b1, b2) for every valid record.
+cudaError_t launch_scatter_contacts(const int4* records, int64_t nrec, const int64_t* offsets, int32_t* contacts,
+                                    cudaStream_t s);
+int collide_grid(int precision, int stack_entries, int block);
+int distance_grid(int precision, int stack_entries, int block);
+
+extern int64_t g_kernel_launches;
+
+}  // namespace fclgpu

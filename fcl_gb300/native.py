@@ -1,0 +1,108 @@
+"""ctypes binding of the C ABI in include/fclgpu.h (fcl_gb300/_build/libfclgpu.so).
+
+There is no CPU fallback: if the native library is missing or fails to load, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfclgpu.so")
+
+FCLGPU_OK = 0
+FCLGPU_ERR_CAPACITY = -4
+PLAIN_FP64 = 0
+FP32_RECHECK = 1
+
+
+class FclGpuError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        super().__init__(f"{where}: status {code} ({status_string(code)}) {detail}".strip())
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("num_vertices", C.c_int64), ("num_tris", C.c_int64), ("num_nodes", C.c_int64),
+                ("max_depth", C.c_int32), ("reserved", C.c_int32), ("max_abs_coord", C.c_double),
+                ("device_bytes", C.c_int64)]
+
+
+class CollideRequest(C.Structure):
+    _fields_ = [("num_max_contacts", C.c_int32), ("precision", C.c_int32), ("enable_statistics", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class CollideResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("contacts", C.c_void_p),
+                ("contacts_capacity", C.c_int64), ("num_bv_tests", C.c_void_p), ("num_leaf_tests", C.c_void_p),
+                ("num_rechecks", C.c_void_p), ("total_contacts", C.c_int64)]
+
+
+class DistanceRequest(C.Structure):
+    _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32), ("enable_statistics", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class DistanceResult(C.Structure):
+    _fields_ = [("min_distance", C.c_void_p), ("ids", C.c_void_p), ("nearest_points", C.c_void_p),
+                ("margins", C.c_void_p), ("within_margin", C.c_void_p), ("num_bv_tests", C.c_void_p),
+                ("num_leaf_tests", C.c_void_p), ("num_rechecks", C.c_void_p)]
+
+
+_lib = None
+
+# every function the header declares, with (restype, argtypes)
+_VP = C.c_void_p
+_SIGS = {
+    "fclgpu_status_string": (C.c_char_p, [C.c_int]),
+    "fclgpu_last_error_detail": (C.c_char_p, []),
+    "fclgpu_init": (C.c_int, [C.c_int]),
+    "fclgpu_mesh_create": (C.c_int, [_VP, C.c_int64, _VP, C.c_int64, C.POINTER(C.c_void_p)]),
+    "fclgpu_mesh_destroy": (C.c_int, [_VP]),
+    "fclgpu_mesh_get_info": (C.c_int, [_VP, C.POINTER(MeshInfo)]),
+    "fclgpu_mesh_get_nodes": (C.c_int, [_VP, _VP, _VP]),
+    "fclgpu_collide_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                              C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
+    "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                       C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
+    "fclgpu_distance_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                               C.POINTER(DistanceRequest), C.POINTER(DistanceResult), _VP]),
+    "fclgpu_distance_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                        C.POINTER(DistanceRequest), C.POINTER(DistanceResult), _VP]),
+    "fclgpu_kernel_launch_count": (C.c_int64, []),
+}
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def lib():
+    """Loads the native library (building it first if it is absent)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build as _b
+            _b.build()
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(code: int) -> str:
+    try:
+        return lib().fclgpu_status_string(code).decode()
+    except Exception:  # library not loadable
+        return "?"
+
+
+def check(code: int, where: str) -> None:
+    if code != FCLGPU_OK:
+        detail = lib().fclgpu_last_error_detail()
+        raise FclGpuError(code, where, detail.decode() if detail else "")

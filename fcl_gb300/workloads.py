@@ -1,0 +1,202 @@
+"""Seeded synthetic workloads for the mesh, convex-shape and broadphase queries.
+
+All generators are deterministic for a given seed on one machine (numpy PCG64).
+Meshes are class-I geodesic icospheres (frequency n -> 20 n^2 triangles) scaled to
+ellipsoids and perturbed per vertex; poses are Haar-uniform rotations (normalised
+4-D Gaussian quaternions) with uniform translations.  Transforms are returned as
+(N, 3, 4) float64 arrays [R | t].
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+_ICO_CACHE: dict[int, tuple[np.ndarray, np.ndarray]] = {}
+
+
+def _icosahedron() -> tuple[np.ndarray, np.ndarray]:
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array(
+        [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0],
+         [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    f = np.array(
+        [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
+         [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
+         [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
+         [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]], dtype=np.int64)
+    return v, f
+
+
+def geodesic_sphere(freq: int) -> tuple[np.ndarray, np.ndarray]:
+    """Unit class-I geodesic sphere with 20*freq^2 triangles and 10*freq^2+2 vertices."""
+    if freq in _ICO_CACHE:
+        v, f = _ICO_CACHE[freq]
+        return v.copy(), f.copy()
+    n = int(freq)
+    if n < 1:
+        raise ValueError("freq must be >= 1")
+    iv, ifc = _icosahedron()
+    # grid points (a, b) with a + b <= n on each face; weights (n-a-b, a, b)
+    ab = [(a, b) for a in range(n + 1) for b in range(n + 1 - a)]
+    ab = np.array(ab, dtype=np.int64)
+    local = {(int(a), int(b)): k for k, (a, b) in enumerate(ab)}
+    npts = len(ab)
+    # canonical weight vectors over the 12 icosahedron vertices for de-duplication
+    W = np.zeros((20 * npts, 12), dtype=np.int64)
+    for fi, (i0, i1, i2) in enumerate(ifc):
+        rows = slice(fi * npts, (fi + 1) * npts)
+        W[rows, i0] += n - ab[:, 0] - ab[:, 1]
+        W[rows, i1] += ab[:, 0]
+        W[rows, i2] += ab[:, 1]
+    uniq, inv = np.unique(W, axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    pos = (uniq.astype(np.float64) @ iv) / n
+    pos /= np.linalg.norm(pos, axis=1, keepdims=True)
+    # local triangles (orientation inherited from the face)
+    tl = []
+    for a in range(n):
+        for b in range(n - a):
+            tl.append((local[(a, b)], local[(a + 1, b)], local[(a, b + 1)]))
+            if a + b < n - 1:
+                tl.append((local[(a + 1, b)], local[(a + 1, b + 1)], local[(a, b + 1)]))
+    tl = np.array(tl, dtype=np.int64)
+    tris = np.concatenate([inv[fi * npts + tl] for fi in range(20)], axis=0)
+    # make orientation outward
+    p0, p1, p2 = pos[tris[:, 0]], pos[tris[:, 1]], pos[tris[:, 2]]
+    nrm = np.cross(p1 - p0, p2 - p0)
+    flip = np.einsum("ij,ij->i", nrm, p0 + p1 + p2) < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+    tris = tris.astype(np.int32)
+    _ICO_CACHE[freq] = (pos, tris)
+    return pos.copy(), tris.copy()
+
+
+def perturbed_ellipsoid(freq: int, radii, noise: float, seed: int, scale: float = 1.0):
+    """Icosphere of frequency `freq`, scaled to `radii`, vertices + N(0, noise^2), times scale."""
+    v, f = geodesic_sphere(freq)
+    rng = np.random.default_rng(seed)
+    v = v * np.asarray(radii, dtype=np.float64)[None, :]
+    v = v + rng.normal(0.0, noise, size=v.shape)
+    v = v * scale
+    return np.ascontiguousarray(v, dtype=np.float64), np.ascontiguousarray(f, dtype=np.int32)
+
+
+def haar_rotations(n: int, rng: np.random.Generator) -> np.ndarray:
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def random_poses(n: int, lo, hi, seed: int) -> np.ndarray:
+    """(n, 3, 4) transforms: Haar rotation, translation ~ U[lo, hi]^3."""
+    rng = np.random.default_rng(seed)
+    R = haar_rotations(n, rng)
+    t = rng.uniform(lo, hi, size=(n, 3))
+    tf = np.empty((n, 3, 4))
+    tf[:, :, :3] = R
+    tf[:, :, 3] = t
+    return np.ascontiguousarray(tf)
+
+
+def identity_poses(n: int) -> np.ndarray:
+    tf = np.zeros((n, 3, 4))
+    tf[:, 0, 0] = tf[:, 1, 1] = tf[:, 2, 2] = 1.0
+    return tf
+
+
+# ---------------------------------------------------------------------------------
+# Mesh-pair workloads
+# ---------------------------------------------------------------------------------
+
+@dataclass
+class MeshPairWorkload:
+    """meshes: list of (verts, tris); pairs: (P, 2) mesh indices; queries reference
+    a pair via `pair` and carry tf1 (None = identity) and tf2."""
+    meshes: list
+    pairs: np.ndarray
+    pair: np.ndarray      # (N,) int32
+    tf2: np.ndarray       # (N, 3, 4)
+    tf1: np.ndarray | None = None
+    margin: np.ndarray | None = None   # (N,) tolerance for the distance check
+    name: str = ""
+
+    @property
+    def n(self) -> int:
+        return int(self.pair.shape[0])
+
+
+def config0(n_poses: int = 10000, seed: int = 0, freq: int = 16) -> MeshPairWorkload:
+    """Plain method, 5,120-triangle perturbed ellipsoids, 10,000 poses in [-2,2]^3."""
+    a = perturbed_ellipsoid(freq, (1.0, 0.7, 0.5), 0.01, seed)
+    b = perturbed_ellipsoid(freq, (1.0, 0.7, 0.5), 0.01, seed + 1, scale=0.8)
+    tf2 = random_poses(n_poses, -2.0, 2.0, seed + 7)
+    return MeshPairWorkload(meshes=[a, b], pairs=np.array([[0, 1]], np.int32),
+                            pair=np.zeros(n_poses, np.int32), tf2=tf2, name="c0")
+
+
+def _loguniform_int(rng, lo, hi, size=None):
+    return np.exp(rng.uniform(math.log(lo), math.log(hi), size=size))
+
+
+def mesh_pair_set(n_pairs: int = 64, seed: int = 1, tri_lo: int = 500, tri_hi: int = 200000):
+    """64 mesh pairs: triangle counts log-uniform in [500, 200k] (geodesic frequency
+    round(sqrt(T/20))), radii U[0.5,1.5]^3, N(0, 0.01^2) vertex noise."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for k in range(2 * n_pairs):
+        T = _loguniform_int(rng, tri_lo, tri_hi)
+        freq = max(1, int(round(math.sqrt(T / 20.0))))
+        radii = rng.uniform(0.5, 1.5, size=3)
+        meshes.append(perturbed_ellipsoid(freq, radii, 0.01, seed * 100003 + k))
+    pairs = np.arange(2 * n_pairs, dtype=np.int32).reshape(n_pairs, 2)
+    return meshes, pairs
+
+
+def config1(scale: float = 1.0, seed: int = 1, n_pairs: int = 64, tri_hi: int = 200000,
+            pose_lo: int = 2000, pose_hi: int = 50000) -> MeshPairWorkload:
+    """Exhaustive contacts: per pair log-uniform [2,000, 50,000] poses (times `scale`),
+    translations U[-1.5,1.5]^3."""
+    meshes, pairs = mesh_pair_set(n_pairs, seed, tri_hi=tri_hi)
+    rng = np.random.default_rng(seed + 11)
+    counts = np.maximum(1, np.round(_loguniform_int(rng, pose_lo, pose_hi, size=n_pairs) * scale)).astype(np.int64)
+    pair = np.repeat(np.arange(n_pairs, dtype=np.int32), counts)
+    tf2 = random_poses(int(counts.sum()), -1.5, 1.5, seed + 13)
+    return MeshPairWorkload(meshes=meshes, pairs=pairs, pair=pair, tf2=tf2, name="c1")
+
+
+def config2(total_poses: int = 1_000_000, seed: int = 1, n_pairs: int = 64, tri_hi: int = 200000
+            ) -> MeshPairWorkload:
+    """Distance batch over the same pair set: poses spread in proportion to the
+    exhaustive-contact counts, translations U[1.5,4]^3, margins U[0.01,0.2]."""
+    meshes, pairs = mesh_pair_set(n_pairs, seed, tri_hi=tri_hi)
+    rng = np.random.default_rng(seed + 11)
+    w = _loguniform_int(rng, 2000, 50000, size=n_pairs)
+    counts = np.maximum(1, np.floor(w / w.sum() * total_poses)).astype(np.int64)
+    counts[0] += total_poses - counts.sum()
+    pair = np.repeat(np.arange(n_pairs, dtype=np.int32), counts)
+    tf2 = random_poses(int(counts.sum()), 1.5, 4.0, seed + 17)
+    margin = np.random.default_rng(seed + 19).uniform(0.01, 0.2, size=pair.shape[0])
+    return MeshPairWorkload(meshes=meshes, pairs=pairs, pair=pair, tf2=tf2, margin=margin, name="c2")
+
+
+def subsample(w: MeshPairWorkload, n: int, seed: int = 0) -> MeshPairWorkload:
+    """A uniform random subset of n queries (sorted by original order)."""
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(w.n, size=min(n, w.n), replace=False))
+    return MeshPairWorkload(meshes=w.meshes, pairs=w.pairs, pair=w.pair[idx], tf2=w.tf2[idx],
+                            tf1=None if w.tf1 is None else w.tf1[idx],
+                            margin=None if w.margin is None else w.margin[idx], name=w.name + "_sub")

@@ -1,0 +1,170 @@
+/*
+ * fclgpu.h -- C ABI of the GB300 proximity-query library (one GPU, sm_103a).
+ *
+ * This is the drop-in boundary for FCL 0.7.0's proximity-query hot path.  Plain C:
+ * pointers, sizes and int status codes; no C++ or CUDA types cross it except the
+ * opaque `stream` argument (a cudaStream_t passed as void*, NULL = legacy default
+ * stream).  Every function returns FCLGPU_OK (0) or a negative status; nothing
+ * throws.  fclgpu_status_string() names a status.
+ *
+ * Transforms are 3x4 row-major doubles [R | t] (12 doubles), the rigid part of
+ * fcl::Transform3<double> (common/types.h:67-98).  Triangle indices are int32.
+ *
+ * Reference interfaces replaced (paths inside the FCL repository):
+ *   fclgpu_mesh_create      BVHModel<OBBRSS<double>>::beginModel/addSubModel/endModel
+ *                           (geometry/bvh/BVH_model-inl.h:207-517), MEAN split
+ *   fclgpu_collide_batch*   fcl::collide(...) on BVHModel<OBBRSS> pairs
+ *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
+ *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
+ *                           (narrowphase/distance.h:51-62, distance-inl.h:71-246)
+ */
+#ifndef FCLGPU_H
+#define FCLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCLGPU_API __attribute__((visibility("default")))
+
+/* ---- status codes (FCL returns counts / prints warnings / throws; the C ABI maps
+ *      those to codes: collision-inl.h:113-138, BVH_internal.h:61-72,
+ *      failed_at_this_configuration.h:65-167) --------------------------------------- */
+enum {
+  FCLGPU_OK = 0,
+  FCLGPU_ERR_INVALID_ARGUMENT = -1,
+  FCLGPU_ERR_CUDA = -2,
+  FCLGPU_ERR_OUT_OF_MEMORY = -3,
+  FCLGPU_ERR_CAPACITY = -4,        /* output buffer too small; required size reported */
+  FCLGPU_ERR_EMPTY_MODEL = -5,     /* BVH_ERR_BUILD_EMPTY_MODEL */
+  FCLGPU_ERR_STACK_DEPTH = -6,     /* pair of BVHs deeper than the traversal stack */
+  FCLGPU_ERR_DEVICE_STATUS = -7,   /* a kernel reported an internal error word */
+  FCLGPU_ERR_NOT_INITIALIZED = -8,
+  FCLGPU_ERR_UNSUPPORTED = -9
+};
+
+FCLGPU_API const char* fclgpu_status_string(int status);
+FCLGPU_API const char* fclgpu_last_error_detail(void);
+
+/* Selects the CUDA device for this process (idempotent). */
+FCLGPU_API int fclgpu_init(int device);
+
+/* ---- precision forms ---------------------------------------------------------------
+ * FCLGPU_PLAIN_FP64   : every test in FP64 in the reference's operation order.
+ * FCLGPU_FP32_RECHECK : FP32 traversal and leaf tests with rigorous forward-error
+ *                       bounds; any decision inside its bound is re-decided in FP64
+ *                       (reference order, no FMA), so booleans, contact sets and
+ *                       traversal statistics equal the FP64 form bit for bit.     */
+enum { FCLGPU_PLAIN_FP64 = 0, FCLGPU_FP32_RECHECK = 1 };
+
+/* ---- meshes (BVHModel<OBBRSS<double>>) --------------------------------------------- */
+typedef struct fclgpu_mesh_s* fclgpu_mesh;
+
+typedef struct {
+  int64_t num_vertices;
+  int64_t num_tris;
+  int64_t num_nodes;
+  int32_t max_depth;       /* root depth 0 */
+  int32_t reserved;
+  double max_abs_coord;    /* max |vertex coordinate| */
+  int64_t device_bytes;    /* HBM held by the device mirror */
+} fclgpu_mesh_info;
+
+/* Builds the OBBRSS BVH on the host (FCL's top-down PCA fit, MEAN split) from
+ * nv vertices (3 doubles each) and nt triangles (3 int32 each) and uploads a
+ * device mirror (FP64 nodes and vertices, packed FP32 nodes and triangles). */
+FCLGPU_API int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt,
+                                  fclgpu_mesh* out);
+FCLGPU_API int fclgpu_mesh_destroy(fclgpu_mesh mesh);
+FCLGPU_API int fclgpu_mesh_get_info(fclgpu_mesh mesh, fclgpu_mesh_info* info);
+/* Copies the FP64 BVH back to the host: per node 30 doubles (obb.axis row-major 9,
+ * obb.To 3, obb.extent 3, rss.axis 9, rss.To 3, rss.l 2, rss.r 1) and first_child
+ * (<0: leaf, primitive = -(first_child+1)), in FCL's node order. */
+FCLGPU_API int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t* first_child);
+
+/* ---- batched queries ----------------------------------------------------------------
+ * A batch is n queries over a table of mesh pairs.  Query i tests meshes
+ * (pairs[2*pair_of_query[i]], pairs[2*pair_of_query[i]+1]) at poses tf1[i], tf2[i].
+ * pair_of_query == NULL means every query uses pair 0; tf1 == NULL means tf1 = I.
+ * "_device" entry points take device pointers for per-query arrays and outputs and
+ * are asynchronous on `stream` except where they must read a size back; the plain
+ * entry points take host pointers (pinned or pageable) and copy in and out.       */
+typedef struct {
+  int32_t num_max_contacts;   /* CollisionRequest::num_max_contacts (collision_request.h:58) */
+  int32_t precision;          /* FCLGPU_PLAIN_FP64 or FCLGPU_FP32_RECHECK */
+  int32_t enable_statistics;  /* fill num_bv_tests / num_leaf_tests */
+  int32_t reserved;
+} fclgpu_collide_request;
+
+/* Outputs of a collide batch.  counts[n] (int32) always.  Contacts (b1,b2 triangle
+ * ids, int32 pairs) are written per query in the reference's DFS order, query after
+ * query, at offsets[i] (int64, n+1 entries) when `contacts` is non-NULL; if the total
+ * exceeds contacts_capacity the call returns FCLGPU_ERR_CAPACITY and *total_contacts
+ * holds the size needed.  Optional per-query int64 statistics and FP64-recheck
+ * counts (FP32_RECHECK form). */
+typedef struct {
+  int32_t* counts;
+  int64_t* offsets;
+  int32_t* contacts;
+  int64_t contacts_capacity;
+  int64_t* num_bv_tests;
+  int64_t* num_leaf_tests;
+  int64_t* num_rechecks;
+  int64_t total_contacts;     /* written by the call */
+} fclgpu_collide_result;
+
+FCLGPU_API int fclgpu_collide_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                           const int32_t* pairs_host, int32_t num_pairs,
+                                           int64_t n, const int32_t* pair_of_query,
+                                           const double* tf1, const double* tf2,
+                                           const fclgpu_collide_request* req,
+                                           fclgpu_collide_result* res, void* stream);
+FCLGPU_API int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                    const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+                                    const int32_t* pair_of_query, const double* tf1,
+                                    const double* tf2, const fclgpu_collide_request* req,
+                                    fclgpu_collide_result* res, void* stream);
+
+typedef struct {
+  int32_t enable_nearest_points;  /* DistanceRequest::enable_nearest_points */
+  int32_t precision;
+  int32_t enable_statistics;
+  int32_t reserved;
+} fclgpu_distance_request;
+
+/* min_distance[n] always; ids[2n] (b1,b2); nearest_points[6n] (world frame, p1 then
+ * p2) when requested; optional margins[n] + within_margin[n] give the tolerance
+ * check distance <= margin (int32 0/1). */
+typedef struct {
+  double* min_distance;
+  int32_t* ids;
+  double* nearest_points;
+  const double* margins;
+  int32_t* within_margin;
+  int64_t* num_bv_tests;
+  int64_t* num_leaf_tests;
+  int64_t* num_rechecks;
+} fclgpu_distance_result;
+
+FCLGPU_API int fclgpu_distance_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                            const int32_t* pairs_host, int32_t num_pairs,
+                                            int64_t n, const int32_t* pair_of_query,
+                                            const double* tf1, const double* tf2,
+                                            const fclgpu_distance_request* req,
+                                            fclgpu_distance_result* res, void* stream);
+FCLGPU_API int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                     const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+                                     const int32_t* pair_of_query, const double* tf1,
+                                     const double* tf2, const fclgpu_distance_request* req,
+                                     fclgpu_distance_result* res, void* stream);
+
+/* Number of this library's kernel launches issued since load (for launch accounting). */
+FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FCLGPU_H */

@@ -1,0 +1,238 @@
+// C entry points of the FP64 CPU oracle, loaded by tests/ and by bench.py's CPU
+// baseline through ctypes.  TEST INFRASTRUCTURE ONLY: the shipped library never
+// links or calls this file.
+//
+// Transforms are 3x4 row-major doubles [R | t] (12 per pose).
+#include <atomic>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "oracle_mesh.h"
+
+using namespace oracle;
+
+namespace {
+
+Tf load_tf(const double* p) {
+  Tf f;
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) f.R(r, c) = p[4 * r + c];
+    f.t[r] = p[4 * r + 3];
+  }
+  return f;
+}
+Tf identity_tf() {
+  Tf f;
+  f.R = ident();
+  f.t = mk(0, 0, 0);
+  return f;
+}
+
+template <class F>
+void parallel_for(int64_t n, int nthreads, F fn) {
+  if (nthreads <= 1 || n < 2) {
+    for (int64_t i = 0; i < n; ++i) fn(i, 0);
+    return;
+  }
+  std::atomic<int64_t> next(0);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t)
+    th.emplace_back([&, t]() {
+      for (;;) {
+        int64_t i = next.fetch_add(1);
+        if (i >= n) break;
+        fn(i, t);
+      }
+    });
+  for (auto& x : th) x.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_mesh_create(const double* verts, int nv, const int* tris, int nt) {
+  Mesh* m = new Mesh();
+  m->verts.resize(nv);
+  for (int i = 0; i < nv; ++i) m->verts[i] = mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+  m->tris.resize(nt);
+  for (int i = 0; i < nt; ++i)
+    for (int k = 0; k < 3; ++k) m->tris[i].v[k] = tris[3 * i + k];
+  build_bvh(*m);
+  return m;
+}
+
+void orc_mesh_free(void* h) { delete static_cast<Mesh*>(h); }
+
+int orc_mesh_num_nodes(void* h) { return (int)static_cast<Mesh*>(h)->nodes.size(); }
+
+// Per node: obb.axis (9, row-major), obb.To (3), obb.extent (3), rss.axis (9),
+// rss.To (3), rss.l (2), rss.r (1) = 30 doubles; first_child in a separate array.
+void orc_mesh_get_nodes(void* h, double* out, int* first_child) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  for (size_t i = 0; i < m->nodes.size(); ++i) {
+    const Node& n = m->nodes[i];
+    double* o = out + 30 * i;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) o[3 * r + c] = n.obb.axis(r, c);
+    for (int k = 0; k < 3; ++k) o[9 + k] = n.obb.To[k];
+    for (int k = 0; k < 3; ++k) o[12 + k] = n.obb.extent[k];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) o[15 + 3 * r + c] = n.rss.axis(r, c);
+    for (int k = 0; k < 3; ++k) o[24 + k] = n.rss.To[k];
+    o[27] = n.rss.l[0];
+    o[28] = n.rss.l[1];
+    o[29] = n.rss.r;
+    first_child[i] = n.first_child;
+  }
+}
+
+// Batched fcl::collide over n poses of one mesh pair.  tf1 may be NULL (identity).
+// counts[i] = number of contacts of pose i; contacts (b1,b2) are written pose after
+// pose in the reference's DFS order into out (capacity cap pairs).  Returns the total
+// number of contact pairs (even if it exceeds cap; then out holds only a prefix).
+int64_t orc_collide_batch(void* h1, void* h2, int64_t n, const double* tf1, const double* tf2,
+                          int64_t num_max_contacts, int nthreads, int64_t* counts, int64_t* nbv,
+                          int64_t* nleaf, int* out, int64_t cap) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  std::vector<std::vector<int>> per(n);
+  parallel_for(n, nthreads, [&](int64_t i, int) {
+    Tf a = tf1 ? load_tf(tf1 + 12 * i) : identity_tf();
+    Tf b = load_tf(tf2 + 12 * i);
+    CollideStats st;
+    size_t k = collide_mesh(*m1, a, *m2, b, (size_t)num_max_contacts, per[i], &st);
+    counts[i] = (int64_t)k;
+    if (nbv) nbv[i] = st.num_bv_tests;
+    if (nleaf) nleaf[i] = st.num_leaf_tests;
+  });
+  int64_t total = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t k = counts[i];
+    if (out && total + k <= cap) std::memcpy(out + 2 * total, per[i].data(), sizeof(int) * 2 * k);
+    total += k;
+  }
+  return total;
+}
+
+// Batched fcl::distance over n poses of one mesh pair.  Outputs per pose: dist,
+// (b1,b2), and when nearest != 0 the two world-frame nearest points (6 doubles).
+void orc_distance_batch(void* h1, void* h2, int64_t n, const double* tf1, const double* tf2,
+                        int nearest, int nthreads, double* dist, int* ids, double* pts,
+                        int64_t* nbv, int64_t* nleaf) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  parallel_for(n, nthreads, [&](int64_t i, int) {
+    Tf a = tf1 ? load_tf(tf1 + 12 * i) : identity_tf();
+    Tf b = load_tf(tf2 + 12 * i);
+    DistanceOut o;
+    CollideStats st;
+    distance_mesh(*m1, a, *m2, b, nearest != 0, o, &st);
+    dist[i] = o.min_distance;
+    if (ids) {
+      ids[2 * i] = o.b1;
+      ids[2 * i + 1] = o.b2;
+    }
+    if (pts) {
+      for (int k = 0; k < 3; ++k) {
+        pts[6 * i + k] = o.p1[k];
+        pts[6 * i + 3 + k] = o.p2[k];
+      }
+    }
+    if (nbv) nbv[i] = st.num_bv_tests;
+    if (nleaf) nleaf[i] = st.num_leaf_tests;
+  });
+}
+
+// --- single-primitive entry points used by the known-answer tests -------------------
+
+// RSS given as axis (9 row-major), To (3), l (2), r (1) = 15 doubles.
+static RSS load_rss(const double* p) {
+  RSS r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.axis(i, j) = p[3 * i + j];
+  r.To = mk(p[9], p[10], p[11]);
+  r.l[0] = p[12];
+  r.l[1] = p[13];
+  r.r = p[14];
+  return r;
+}
+static void store_rss(const RSS& r, double* p) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) p[3 * i + j] = r.axis(i, j);
+  p[9] = r.To[0]; p[10] = r.To[1]; p[11] = r.To[2];
+  p[12] = r.l[0]; p[13] = r.l[1]; p[14] = r.r;
+}
+
+void orc_rss_fit3(const double* pts9, double* rss15) {
+  V3 ps[3];
+  for (int i = 0; i < 3; ++i) ps[i] = mk(pts9[3 * i], pts9[3 * i + 1], pts9[3 * i + 2]);
+  RSS r;
+  rss_fit3(ps, r);
+  store_rss(r, rss15);
+}
+
+double orc_rss_member_distance(const double* a15, const double* b15) {
+  return rss_member_distance(load_rss(a15), load_rss(b15));
+}
+
+// rss_distance(R0,T0,b1,b2): tf given as 3x4.
+double orc_rss_distance(const double* tf12, const double* a15, const double* b15) {
+  Tf f = load_tf(tf12);
+  return rss_distance(f.R, f.t, load_rss(a15), load_rss(b15), nullptr, nullptr);
+}
+
+// OBB given as axis (9), To (3), extent (3) = 15 doubles.
+int orc_obb_overlap(const double* tf12, const double* a15, const double* b15) {
+  Tf f = load_tf(tf12);
+  OBB a, b;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      a.axis(i, j) = a15[3 * i + j];
+      b.axis(i, j) = b15[3 * i + j];
+    }
+  a.To = mk(a15[9], a15[10], a15[11]);
+  b.To = mk(b15[9], b15[10], b15[11]);
+  a.extent = mk(a15[12], a15[13], a15[14]);
+  b.extent = mk(b15[12], b15[13], b15[14]);
+  return obb_overlap(f.R, f.t, a, b) ? 1 : 0;
+}
+
+// Triangle pair tests on n pairs: P (9 doubles) and Q (9 doubles) per pair, Q moved
+// by tf (3x4, shared).
+void orc_tri_intersect_batch(int64_t n, const double* P, const double* Q, const double* tf12,
+                             int* out) {
+  Tf f = load_tf(tf12);
+  for (int64_t i = 0; i < n; ++i) {
+    const double* p = P + 9 * i;
+    const double* q = Q + 9 * i;
+    out[i] = tri_intersect(mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8]),
+                           mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), mk(q[6], q[7], q[8]), f.R, f.t)
+                 ? 1 : 0;
+  }
+}
+
+void orc_tri_distance_batch(int64_t n, const double* P, const double* Q, double* dist, double* pts) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3 A[3], B[3];
+    for (int k = 0; k < 3; ++k) {
+      A[k] = mk(P[9 * i + 3 * k], P[9 * i + 3 * k + 1], P[9 * i + 3 * k + 2]);
+      B[k] = mk(Q[9 * i + 3 * k], Q[9 * i + 3 * k + 1], Q[9 * i + 3 * k + 2]);
+    }
+    V3 p, q;
+    dist[i] = tri_distance(A, B, p, q);
+    if (pts)
+      for (int k = 0; k < 3; ++k) {
+        pts[6 * i + k] = p[k];
+        pts[6 * i + 3 + k] = q[k];
+      }
+  }
+}
+
+int orc_hardware_threads() {
+  unsigned n = std::thread::hardware_concurrency();
+  return n ? (int)n : 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// FP64 CPU oracle for the BVHModel<OBBRSS> mesh path: BVH build, OBB/RSS bounding
+// volume tests, triangle leaf tests and the two traversals.
+//
+// TEST INFRASTRUCTURE ONLY (see oracle_math.h).  Every function cites the FCL 0.7.0
+// source it restates (paths relative to the FCL repository).
+#pragma once
+#include <vector>
+#include <cstdint>
+#include "oracle_math.h"
+
+namespace oracle {
+
+// math/bv/OBB.h:62-68
+struct OBB {
+  M3 axis;
+  V3 To;
+  V3 extent;
+};
+// math/bv/RSS.h:70-82
+struct RSS {
+  M3 axis;
+  V3 To;
+  double l[2];
+  double r;
+};
+// geometry/bvh/BV_node.h:51-74, BV_node_base.h:50-76
+struct Node {
+  OBB obb;
+  RSS rss;
+  int first_child;  // <0: leaf, primitive = -(first_child+1)
+  int first_primitive;
+  int num_primitives;
+};
+
+struct Tri {
+  int v[3];
+};
+
+struct Mesh {
+  std::vector<V3> verts;
+  std::vector<Tri> tris;
+  std::vector<Node> nodes;
+  std::vector<unsigned> prim_idx;
+};
+
+// --- BVH build (geometry/bvh/BVH_model-inl.h:450-517, 833-938) -------------------
+void build_bvh(Mesh& m);
+
+// --- point-set RSS fit for three points (math/bv/utility-inl.h:208-230) ----------
+void rss_fit3(const V3 ps[3], RSS& bv);
+
+// --- bounding-volume tests ----------------------------------------------------------
+bool obb_disjoint(const M3& B, const V3& T, const V3& a, const V3& b);          // OBB-inl.h:398-523
+bool obb_overlap(const M3& R0, const V3& T0, const OBB& b1, const OBB& b2);      // OBB-inl.h:383-395
+double rect_distance(const M3& Rab, const V3& Tab, const double a[2], const double b[2],
+                     V3* P, V3* Q);                                              // RSS-inl.h:512-1224
+double rss_distance(const M3& R0, const V3& T0, const RSS& b1, const RSS& b2,
+                    V3* P, V3* Q);                                               // RSS-inl.h:1956-1974
+double rss_member_distance(const RSS& a, const RSS& b);                         // RSS-inl.h:432-446
+inline double obb_size(const OBB& b) { return sqnorm(b.extent); }               // OBB-inl.h:205-209
+
+// --- leaf tests -----------------------------------------------------------------------
+bool tri_intersect(const V3& P1, const V3& P2, const V3& P3, const V3& Q1, const V3& Q2,
+                   const V3& Q3, const M3& R, const V3& T);                      // intersect-inl.h:597-617,727-798
+double tri_distance(const V3 T1[3], const V3 T2[3], V3& P, V3& Q);             // triangle_distance-inl.h:170-394
+
+// --- queries ----------------------------------------------------------------------
+struct CollideStats {
+  int64_t num_bv_tests = 0;
+  int64_t num_leaf_tests = 0;
+};
+
+// fcl::collide for BVHModel<OBBRSS> x BVHModel<OBBRSS> with enable_contact=false.
+// Contacts are appended in the reference's DFS order as (b1, b2) triangle ids.
+size_t collide_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
+                    size_t num_max_contacts, std::vector<int>& contacts, CollideStats* st);
+
+struct DistanceOut {
+  double min_distance;
+  int b1, b2;
+  V3 p1, p2;  // world frame (postprocess maps by tf1)
+};
+// fcl::distance for BVHModel<OBBRSS> pairs with rel_err = abs_err = 0.
+double distance_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
+                     bool nearest_points, DistanceOut& out, CollideStats* st);
+
+}  // namespace oracle

@@ -1,0 +1,173 @@
+"""ctypes front end of the FP64 CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the CPU
+baseline leg of bench.py.  The shipped library never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i64p = C.POINTER(C.c_int64)
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the oracle with its Makefile (g++ -ffp-contract=off)."""
+    out = subprocess.run(["make", "-s", "-C", _HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.orc_mesh_create.restype = C.c_void_p
+        L.orc_mesh_create.argtypes = [_dp, C.c_int, _ip, C.c_int]
+        L.orc_mesh_free.argtypes = [C.c_void_p]
+        L.orc_mesh_num_nodes.argtypes = [C.c_void_p]
+        L.orc_mesh_get_nodes.argtypes = [C.c_void_p, _dp, _ip]
+        L.orc_collide_batch.restype = C.c_int64
+        L.orc_collide_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64, C.c_int,
+                                        _i64p, _i64p, _i64p, _ip, C.c_int64]
+        L.orc_distance_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int, C.c_int,
+                                         _dp, _ip, _dp, _i64p, _i64p]
+        L.orc_rss_fit3.argtypes = [_dp, _dp]
+        L.orc_rss_member_distance.restype = C.c_double
+        L.orc_rss_member_distance.argtypes = [_dp, _dp]
+        L.orc_rss_distance.restype = C.c_double
+        L.orc_rss_distance.argtypes = [_dp, _dp, _dp]
+        L.orc_obb_overlap.argtypes = [_dp, _dp, _dp]
+        L.orc_tri_intersect_batch.argtypes = [C.c_int64, _dp, _dp, _dp, _ip]
+        L.orc_tri_distance_batch.argtypes = [C.c_int64, _dp, _dp, _dp, _dp]
+        L.orc_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _q(a):
+    return a.ctypes.data_as(_i64p)
+
+
+def hardware_threads() -> int:
+    return int(lib().orc_hardware_threads())
+
+
+class Mesh:
+    """BVHModel<OBBRSS> built by the oracle (reference algorithm, MEAN split)."""
+
+    def __init__(self, verts: np.ndarray, tris: np.ndarray):
+        self.verts = np.ascontiguousarray(verts, dtype=np.float64)
+        self.tris = np.ascontiguousarray(tris, dtype=np.int32)
+        self.h = lib().orc_mesh_create(_d(self.verts), self.verts.shape[0], _i(self.tris), self.tris.shape[0])
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_mesh_free(self.h)
+            self.h = None
+
+    def nodes(self):
+        n = lib().orc_mesh_num_nodes(self.h)
+        out = np.empty((n, 30), np.float64)
+        fc = np.empty(n, np.int32)
+        lib().orc_mesh_get_nodes(self.h, _d(out), _i(fc))
+        return out, fc
+
+
+def collide_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None,
+                  num_max_contacts: int = 1, nthreads: int = 1):
+    """Returns (counts, contacts (total,2) int32 in per-pose DFS order, nbv, nleaf)."""
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1p = None if tf1 is None else _d(np.ascontiguousarray(tf1, np.float64).reshape(-1, 12))
+    counts = np.zeros(n, np.int64)
+    nbv = np.zeros(n, np.int64)
+    nleaf = np.zeros(n, np.int64)
+    cap = 1 << 16
+    while True:
+        out = np.empty((cap, 2), np.int32)
+        total = lib().orc_collide_batch(m1.h, m2.h, n, tf1p, _d(tf2), num_max_contacts, nthreads,
+                                        _q(counts), _q(nbv), _q(nleaf), _i(out), cap)
+        if total <= cap:
+            return counts, out[:total].copy(), nbv, nleaf
+        cap = int(total)
+
+
+def distance_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None,
+                   nearest: bool = True, nthreads: int = 1):
+    """Returns (dist, ids (n,2), points (n,2,3) world frame, nbv, nleaf)."""
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(-1, 12)
+    dist = np.empty(n, np.float64)
+    ids = np.empty((n, 2), np.int32)
+    pts = np.zeros((n, 2, 3), np.float64)
+    nbv = np.zeros(n, np.int64)
+    nleaf = np.zeros(n, np.int64)
+    lib().orc_distance_batch(m1.h, m2.h, n, None if tf1a is None else _d(tf1a), _d(tf2), int(nearest),
+                             nthreads, _d(dist), _i(ids), _d(pts), _q(nbv), _q(nleaf))
+    return dist, ids, pts, nbv, nleaf
+
+
+def rss_fit3(pts: np.ndarray) -> np.ndarray:
+    pts = np.ascontiguousarray(pts, np.float64).reshape(9)
+    out = np.empty(15, np.float64)
+    lib().orc_rss_fit3(_d(pts), _d(out))
+    return out
+
+
+def rss_member_distance(a15: np.ndarray, b15: np.ndarray) -> float:
+    a = np.ascontiguousarray(a15, np.float64)
+    b = np.ascontiguousarray(b15, np.float64)
+    return float(lib().orc_rss_member_distance(_d(a), _d(b)))
+
+
+def rss_distance(tf: np.ndarray, a15: np.ndarray, b15: np.ndarray) -> float:
+    tf = np.ascontiguousarray(tf, np.float64).reshape(12)
+    a = np.ascontiguousarray(a15, np.float64)
+    b = np.ascontiguousarray(b15, np.float64)
+    return float(lib().orc_rss_distance(_d(tf), _d(a), _d(b)))
+
+
+def obb_overlap(tf: np.ndarray, a15: np.ndarray, b15: np.ndarray) -> bool:
+    tf = np.ascontiguousarray(tf, np.float64).reshape(12)
+    a = np.ascontiguousarray(a15, np.float64)
+    b = np.ascontiguousarray(b15, np.float64)
+    return bool(lib().orc_obb_overlap(_d(tf), _d(a), _d(b)))
+
+
+def tri_intersect_batch(P: np.ndarray, Q: np.ndarray, tf: np.ndarray) -> np.ndarray:
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 9)
+    Q = np.ascontiguousarray(Q, np.float64).reshape(-1, 9)
+    tf = np.ascontiguousarray(tf, np.float64).reshape(12)
+    out = np.empty(P.shape[0], np.int32)
+    lib().orc_tri_intersect_batch(P.shape[0], _d(P), _d(Q), _d(tf), _i(out))
+    return out.astype(bool)
+
+
+def tri_distance_batch(P: np.ndarray, Q: np.ndarray):
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 9)
+    Q = np.ascontiguousarray(Q, np.float64).reshape(-1, 9)
+    d = np.empty(P.shape[0], np.float64)
+    pts = np.empty((P.shape[0], 2, 3), np.float64)
+    lib().orc_tri_distance_batch(P.shape[0], _d(P), _d(Q), _d(d), _d(pts))
+    return d, pts
