@@ -1,0 +1,339 @@
+"""Benchmark of the batched OBBRSS mesh-collide hot path on one GB300.
+
+Workload (the configuration the headline metric is quoted on): 64 mesh pairs of
+perturbed icosphere/ellipsoid meshes with 500-200,000 triangles (log-uniform), each
+pair with 2,000-50,000 Haar-uniform poses (log-uniform; ~1.1M queries in total),
+translations U[-1.5,1.5]^3, exhaustive contacts (num_max_contacts = 100,000).
+A step = one batched collide over all queries, inputs resident in HBM.  Timed
+with CUDA events on the launching stream; L2 is flushed between steps.
+
+Reported: queries/s of the FP32 + FP64-recheck form (value), the plain FP64 GPU
+form beside it with the exact-hit check (identical counts and contact lists), the
+same metric end to end through the host C ABI (pinned host buffers, copies in the
+timed region), the roofline of the traversal kernel, the FP64 CPU oracle timed on
+the host cores on a bounded sample, and SM clocks sampled during the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "queries/s batched FP32+FP64-recheck vs plain GPU (exact hits); p50/p99 request ms"
+UNIT = "queries/s"
+WORKLOAD = "c1_exhaustive_contacts_64pairs_500-200k_tris"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def _workload(args, rank):
+    from fcl_gb300 import workloads as W
+    return W.config1(scale=args.scale, seed=1 + 1000 * rank)
+
+
+# ------------------------------------------------------------------------------------
+# reference arm: the reference's CPU algorithm (the FP64 oracle restatement; FCL itself
+# cannot be compiled here) on all host cores, bounded sample per step
+# ------------------------------------------------------------------------------------
+def _cpu_sample(w, n_sample, seed=0):
+    from fcl_gb300 import workloads as W
+    return W.subsample(w, n_sample, seed)
+
+
+def _time_cpu(w_sample, nthreads):
+    from oracle import pyoracle as O
+    om = {}
+    for p in np.unique(w_sample.pair):
+        for m in w_sample.pairs[p]:
+            if m not in om:
+                om[m] = O.Mesh(*w_sample.meshes[m])
+    t0 = time.perf_counter()
+    total = 0
+    for p in np.unique(w_sample.pair):
+        idx = np.nonzero(w_sample.pair == p)[0]
+        c, _, _, _ = O.collide_batch(om[w_sample.pairs[p, 0]], om[w_sample.pairs[p, 1]], w_sample.tf2[idx],
+                                     num_max_contacts=100000, nthreads=nthreads)
+        total += int(c.sum())
+    return time.perf_counter() - t0, total
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import pyoracle as O
+    O.build()
+    threads = O.hardware_threads()
+    w = _workload(args, 0)
+    n_sample = args.cpu_sample
+    times = []
+    for s in range(args.warmup + args.steps):
+        ws = _cpu_sample(w, n_sample, seed=s)
+        dt, _ = _time_cpu(ws, threads)
+        if s >= args.warmup:
+            times.append(dt)
+    qps = n_sample / float(np.mean(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "queries": w.n, "sample_per_step": n_sample},
+        "cpu_baseline": {"value": qps, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_sample} queries drawn uniformly from the {w.n}-query workload per step"},
+        "e2e": {"value": qps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and "Active" in r[5 + k]
+                          and "Not" not in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from fcl_gb300 import api, native
+    native.check(native.lib().fclgpu_init(local), "fclgpu_init")
+    L = native.lib()
+
+    w = _workload(args, rank)
+    t0 = time.time()
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        meshes = list(ex.map(lambda m: api.BVHModel.from_arrays(*m), w.meshes))
+    build_s = time.time() - t0
+
+    dev = torch.device("cuda", local)
+    tf2 = torch.from_numpy(w.tf2).to(dev)
+    pq = torch.from_numpy(w.pair).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+
+    def step(prec, stats=False):
+        return api.collide_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000,
+                                 precision=prec, statistics=stats, stream=stream.cuda_stream)
+
+    # reference run for exact-hit check and algorithmic byte counts (outside timing)
+    ref64 = step("fp64", stats=True)
+    fp32 = step("fp32", stats=True)
+    torch.cuda.synchronize()
+    exact = bool(torch.equal(ref64["counts"], fp32["counts"]) and torch.equal(ref64["contacts"], fp32["contacts"])
+                 and torch.equal(ref64["num_bv_tests"], fp32["num_bv_tests"]))
+    n_bv = int(fp32["num_bv_tests"].sum())
+    n_leaf = int(fp32["num_leaf_tests"].sum())
+    n_rc = int(fp32["num_rechecks"].sum())
+    total_contacts = int(fp32["total_contacts"])
+    n = w.n
+    # algorithmic bytes of one launch: 192 B per BV-pair test (two 96-B packed nodes),
+    # 96 B per leaf pair (two triangles), 48 B per pose, 4 B count + 8 B per contact
+    alg_bytes = 192.0 * n_bv + 96.0 * n_leaf + 48.0 * n + 4.0 * n + 8.0 * total_contacts
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            step(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        launches0 = L.fclgpu_kernel_launch_count()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        kms = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            step(prec)
+            ev[i][1].record(stream)
+            km = C.c_double()
+            native.check(L.fclgpu_last_kernel_time(C.byref(km)), "fclgpu_last_kernel_time")
+            kms.append(km.value)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return float(np.sum(ms)), kms, L.fclgpu_kernel_launch_count() - launches0
+
+    with ClockSampler(local) as clk:
+        total_ms, kms, launches = timed("fp32", args.steps, args.warmup)
+    clocks = clk.summary()
+    t_step = total_ms / args.steps
+    if world > 1:
+        t = torch.tensor([t_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = world * n / (t_step / 1000.0)
+
+    # plain FP64 GPU form (the drop-in denominator)
+    fp64_steps = max(1, min(args.steps, 2))
+    ms64, kms64, _ = timed("fp64", fp64_steps, 1)
+    t64 = ms64 / fp64_steps
+    value64 = world * n / (t64 / 1000.0)
+
+    # end to end through the host C ABI: pinned host inputs, H2D + kernels + D2H per step
+    tf2_h = torch.from_numpy(w.tf2).pin_memory()
+    pq_h = torch.from_numpy(w.pair).pin_memory()
+    counts_h = torch.empty(n, dtype=torch.int32).pin_memory()
+    offs_h = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    cont_h = torch.empty((max(total_contacts, 1), 2), dtype=torch.int32).pin_memory()
+    meshes_c = (C.c_void_p * len(meshes))(*[m.handle.value for m in meshes])
+    pairs_np = np.ascontiguousarray(w.pairs, np.int32)
+    req = native.CollideRequest(100000, native.FP32_RECHECK, 0, 0)
+
+    def e2e_step():
+        res = native.CollideResult(counts_h.data_ptr(), offs_h.data_ptr(), cont_h.data_ptr(), cont_h.shape[0],
+                                   None, None, None, 0)
+        native.check(L.fclgpu_collide_batch(meshes_c, len(meshes), pairs_np.ctypes.data, pairs_np.shape[0], n,
+                                            pq_h.data_ptr(), None, tf2_h.data_ptr(), C.byref(req), C.byref(res),
+                                            stream.cuda_stream), "fclgpu_collide_batch")
+        return res
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_hits = bool(np.array_equal(counts_h.numpy(), fp32["counts"].cpu().numpy()))
+    t_e2e = float(np.mean(e2e_ms))
+    h2d = n * (96 + 4)
+    d2h = n * 4 + (n + 1) * 8 + total_contacts * 8
+
+    # roofline of the traversal kernel
+    peak, peak_kind = _peaks()
+    k_ms = float(np.mean(kms))
+    achieved = alg_bytes / (k_ms / 1000.0) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_kind": peak_kind, "kernel": "k_mesh_collide<FP32+recheck>",
+            "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg_bytes}
+    prof = os.path.join(ROOT, "profiles", "mesh_collide_c1_traffic.json")
+    if os.path.exists(prof):
+        try:
+            roof["traffic"] = float(json.load(open(prof))["dram_bytes_per_launch"])
+        except Exception:
+            pass
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import pyoracle as O
+        O.build()
+        threads = O.hardware_threads()
+        ws = _cpu_sample(w, args.cpu_sample, seed=123)
+        dt, _ = _time_cpu(ws, threads)
+        cpu = {"value": args.cpu_sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} queries drawn uniformly from the {n}-query workload"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (f64 recheck)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "queries": n, "mesh_pairs": int(w.pairs.shape[0]),
+                       "triangles_total": int(sum(m[1].shape[0] for m in w.meshes)),
+                       "num_max_contacts": 100000, "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "clocks": clocks,
+            "e2e": {"value": world * n / (t_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e, "exact_hits": e2e_hits},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "plain_fp64": {"value": value64, "unit": UNIT, "ms_per_step": t64,
+                           "kernel_ms": float(np.mean(kms64))},
+            "fp32_vs_fp64_speedup": value / value64,
+            "exact_hits": exact,
+            "stats": {"bv_tests": n_bv, "leaf_tests": n_leaf, "fp64_rechecks": n_rc,
+                      "recheck_rate": n_rc / max(1, n_bv + n_leaf), "contacts": total_contacts,
+                      "colliding_fraction": float((fp32["counts"] > 0).float().mean().item()),
+                      "mesh_build_s": build_s},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fcl_gb300", choices=["fcl_gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="pose-count scale of the workload")
+    ap.add_argument("--cpu-sample", type=int, default=2000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -292,7 +292,12 @@ def collide_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=
     return out
 
 
+_contacts_hint = {"cap": 1 << 16}
+
+
 def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statistics, contacts, stream):
+    """Device entry point.  The contacts buffer is sized from the previous batch (a
+    batch that outgrows it is re-run once with the exact size)."""
     import torch
     dev = tf2.device
     n = tf2.shape[0]
@@ -300,8 +305,8 @@ def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statis
     offsets = torch.zeros(n + 1, dtype=torch.int64, device=dev)
     st = [torch.zeros(n, dtype=torch.int64, device=dev) for _ in range(3)] if statistics else [None] * 3
     s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
-    cap = 0
-    buf = None
+    cap = _contacts_hint["cap"] if contacts else 0
+    buf = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=dev) if contacts else None
     while True:
         res = N.CollideResult(counts.data_ptr(), offsets.data_ptr(),
                               None if buf is None else buf.data_ptr(), cap,
@@ -310,8 +315,9 @@ def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statis
             hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
             None if pair_of_query is None else pair_of_query.data_ptr(),
             None if tf1 is None else tf1.data_ptr(), tf2.data_ptr(), C.byref(req), C.byref(res), s)
-        if contacts and (rc == N.FCLGPU_ERR_CAPACITY or (rc == 0 and buf is None)):
-            cap = int(res.total_contacts)
+        if contacts and rc == N.FCLGPU_ERR_CAPACITY:
+            cap = int(res.total_contacts * 1.25) + 1024
+            _contacts_hint["cap"] = cap
             buf = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=dev)
             continue
         N.check(rc, "fclgpu_collide_batch_device")

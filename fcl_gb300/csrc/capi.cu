@@ -72,6 +72,18 @@ struct Scratch {
 };
 Scratch g_scratch;
 
+// Device time of the main traversal kernel of the most recent batch (CUDA events
+// recorded on the batch's stream around that launch).
+cudaEvent_t g_ev[2] = {nullptr, nullptr};
+double g_last_kernel_ms = -1.0;
+int ensure_events() {
+  if (!g_ev[0]) {
+    CK(cudaEventCreate(&g_ev[0]), "event");
+    CK(cudaEventCreate(&g_ev[1]), "event");
+  }
+  return FCLGPU_OK;
+}
+
 int ensure_init() {
   if (g_device >= 0) return FCLGPU_OK;
   int dev = 0;
@@ -150,6 +162,13 @@ int fclgpu_init(int device) {
 
 int64_t fclgpu_kernel_launch_count(void) { return g_kernel_launches; }
 
+int fclgpu_last_kernel_time(double* ms) {
+  if (!ms) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
+  if (g_last_kernel_ms < 0) return fail(FCLGPU_ERR_NOT_INITIALIZED, "no batch has run");
+  *ms = g_last_kernel_ms;
+  return FCLGPU_OK;
+}
+
 int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out) {
   if (!out) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "out is null");
   *out = nullptr;
@@ -157,14 +176,14 @@ int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int
   if (nt > (1 << 29)) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many triangles");
   for (int64_t i = 0; i < 3 * nt; ++i)
     if (tris[i] < 0 || tris[i] >= nv) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "triangle index out of range");
-  std::lock_guard<std::recursive_mutex> lk(g_mu);
-  int rc = ensure_init();
-  if (rc) return rc;
-
+  // the host build runs outside the lock so several meshes can be built in parallel
   HostBVH bvh;
   if (build_obbrss(verts, nv, tris, nt, bvh) != 0) return fail(FCLGPU_ERR_EMPTY_MODEL, "empty model");
   PackedF32 pk;
   pack_fp32(verts, tris, nt, bvh, pk);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
 
   fclgpu_mesh_s* m = new fclgpu_mesh_s();
   auto alloc = [&](void** p, size_t bytes, const void* src) -> cudaError_t {
@@ -302,10 +321,19 @@ int fclgpu_collide_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, c
     L.nrecheck = res->num_rechecks;
     const int block = 128;
     const int grid = collide_grid(req->precision, stack, block);
+    rc = ensure_events();
+    if (rc) return rc;
+    CK(cudaEventRecord(g_ev[0], s), "event");
     CK(launch_mesh_collide(L, req->precision, stack, grid, block, s), "collide kernel");
+    CK(cudaEventRecord(g_ev[1], s), "event");
     BatchCounters hc;
     CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
     CK(cudaStreamSynchronize(s), "collide kernel");
+    {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, g_ev[0], g_ev[1]), "event");
+      g_last_kernel_ms = ms;
+    }
     if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
     if (hc.status & DEV_ERR_RECORDS) {
       rec_cap = (int64_t)hc.records + 65536;
@@ -434,10 +462,19 @@ int fclgpu_distance_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, 
   L.nrecheck = res->num_rechecks;
   const int block = 128;
   const int grid = distance_grid(req->precision, stack, block);
+  rc = ensure_events();
+  if (rc) return rc;
+  CK(cudaEventRecord(g_ev[0], s), "event");
   CK(launch_mesh_distance(L, req->precision, stack, grid, block, s), "distance kernel");
+  CK(cudaEventRecord(g_ev[1], s), "event");
   BatchCounters hc;
   CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
   CK(cudaStreamSynchronize(s), "distance kernel");
+  {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, g_ev[0], g_ev[1]), "event");
+    g_last_kernel_ms = ms;
+  }
   if (hc.status) return fail(FCLGPU_ERR_DEVICE_STATUS, "distance kernel status word set");
   return FCLGPU_OK;
 }

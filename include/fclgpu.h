@@ -163,6 +163,9 @@ FCLGPU_API int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_mesh
 
 /* Number of this library's kernel launches issued since load (for launch accounting). */
 FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
+/* Device time (ms, CUDA events on the batch's stream) of the traversal kernel of the
+ * most recent collide or distance batch.  No counterpart in FCL (profiling hook). */
+FCLGPU_API int fclgpu_last_kernel_time(double* ms);
 
 #ifdef __cplusplus
 }

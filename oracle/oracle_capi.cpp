@@ -5,6 +5,7 @@
 // Transforms are 3x4 row-major doubles [R | t] (12 per pose).
 #include <atomic>
 #include <cstring>
+#include <limits>
 #include <thread>
 #include <vector>
 
@@ -228,6 +229,61 @@ void orc_tri_distance_batch(int64_t n, const double* P, const double* Q, double*
         pts[6 * i + 3 + k] = q[k];
       }
   }
+}
+
+// Brute force over all triangle pairs (the reference tests' cross-check:
+// test_fcl_collision.cpp compares every BV type, AABB included, on the same poses).
+// Writes intersecting pairs (b1,b2) in row-major pair order; returns their number.
+int64_t orc_brute_collide(void* h1, void* h2, const double* tf1, const double* tf2, int* out, int64_t cap) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  Tf a = tf1 ? load_tf(tf1) : identity_tf();
+  Tf b = load_tf(tf2);
+  M3 R = mulT(a.R, b.R);
+  V3 T = mulTv(a.R, sub(b.t, a.t));
+  int64_t k = 0;
+  for (size_t i = 0; i < m1->tris.size(); ++i) {
+    const Tri& t1 = m1->tris[i];
+    for (size_t j = 0; j < m2->tris.size(); ++j) {
+      const Tri& t2 = m2->tris[j];
+      if (tri_intersect(m1->verts[t1.v[0]], m1->verts[t1.v[1]], m1->verts[t1.v[2]], m2->verts[t2.v[0]],
+                        m2->verts[t2.v[1]], m2->verts[t2.v[2]], R, T)) {
+        if (k < cap) {
+          out[2 * k] = (int)i;
+          out[2 * k + 1] = (int)j;
+        }
+        ++k;
+      }
+    }
+  }
+  return k;
+}
+
+// Minimum triangle distance over all pairs (tf = tf1^-1 tf2 as in the distance path).
+double orc_brute_distance(void* h1, void* h2, const double* tf1, const double* tf2) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  Tf a = tf1 ? load_tf(tf1) : identity_tf();
+  Tf b = load_tf(tf2);
+  M3 Rinv = transpose(a.R);
+  V3 tinv = neg(mulv(Rinv, a.t));
+  M3 R = mul(Rinv, b.R);
+  V3 T = add(mulv(Rinv, b.t), tinv);
+  std::vector<V3> moved(m2->verts.size());
+  for (size_t k = 0; k < moved.size(); ++k) moved[k] = add(mulv(R, m2->verts[k]), T);
+  double best = std::numeric_limits<double>::max();
+  for (size_t i = 0; i < m1->tris.size(); ++i) {
+    const Tri& t1 = m1->tris[i];
+    V3 A[3] = {m1->verts[t1.v[0]], m1->verts[t1.v[1]], m1->verts[t1.v[2]]};
+    for (size_t j = 0; j < m2->tris.size(); ++j) {
+      const Tri& t2 = m2->tris[j];
+      V3 B[3] = {moved[t2.v[0]], moved[t2.v[1]], moved[t2.v[2]]};
+      V3 P, Q;
+      double d = tri_distance(A, B, P, Q);
+      if (d < best) best = d;
+    }
+  }
+  return best;
 }
 
 int orc_hardware_threads() {

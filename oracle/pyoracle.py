@@ -52,6 +52,10 @@ def lib():
         L.orc_tri_intersect_batch.argtypes = [C.c_int64, _dp, _dp, _dp, _ip]
         L.orc_tri_distance_batch.argtypes = [C.c_int64, _dp, _dp, _dp, _dp]
         L.orc_hardware_threads.restype = C.c_int
+        L.orc_brute_collide.restype = C.c_int64
+        L.orc_brute_collide.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, _ip, C.c_int64]
+        L.orc_brute_distance.restype = C.c_double
+        L.orc_brute_distance.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp]
         _lib = L
     return _lib
 
@@ -171,3 +175,22 @@ def tri_distance_batch(P: np.ndarray, Q: np.ndarray):
     pts = np.empty((P.shape[0], 2, 3), np.float64)
     lib().orc_tri_distance_batch(P.shape[0], _d(P), _d(Q), _d(d), _d(pts))
     return d, pts
+
+
+def brute_collide(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None) -> np.ndarray:
+    """All intersecting triangle pairs (k, 2), row-major pair order."""
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(12)
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(12)
+    cap = 1 << 16
+    while True:
+        out = np.empty((cap, 2), np.int32)
+        k = lib().orc_brute_collide(m1.h, m2.h, None if tf1a is None else _d(tf1a), _d(tf2), _i(out), cap)
+        if k <= cap:
+            return out[:k].copy()
+        cap = int(k)
+
+
+def brute_distance(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None) -> float:
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(12)
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(12)
+    return float(lib().orc_brute_distance(m1.h, m2.h, None if tf1a is None else _d(tf1a), _d(tf2)))

@@ -1,0 +1,34 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares."""
+import ctypes as C
+import os
+import re
+
+from fcl_gb300 import build as B
+from fcl_gb300 import native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"FCLGPU_API\s+[\w\s\*]+?\b(fclgpu_\w+)\s*\(", txt))
+    return names
+
+
+def test_library_builds_and_exports_all_declared_symbols():
+    path = B.build()
+    lib = C.CDLL(path)
+    declared = _declared()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared <= set(N.exported_symbols()) | declared
+
+
+def test_status_strings_without_gpu():
+    L = N.lib()
+    assert L.fclgpu_status_string(0) == b"ok"
+    assert L.fclgpu_status_string(-4) == b"output capacity too small"

@@ -1,0 +1,161 @@
+"""GPU parity for the OBBRSS mesh path, through the C ABI, against the FP64 oracle.
+
+Collide: counts, contact lists (same triangle pairs in the same DFS order) and
+traversal statistics must equal the oracle's exactly in both precision forms.
+Distance: min distance, triangle ids and nearest points of the FP64 form must equal
+the oracle's bit for bit; the FP32 form must agree within 1e-6 relative (1e-9
+absolute floor) and report the witness points of a pair at that distance."""
+import numpy as np
+import pytest
+
+from fcl_gb300 import api
+from fcl_gb300 import workloads as W
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL, ABS = 1e-6, 1e-9
+
+
+def _meshes(w):
+    return [api.BVHModel.from_arrays(v, t) for v, t in w.meshes]
+
+
+def _oracle_collide(w, maxc, nthreads=8):
+    om = [O.Mesh(v, t) for v, t in w.meshes]
+    counts, contacts, nbv, nleaf = [], [], [], []
+    order = []
+    for p in range(w.pairs.shape[0]):
+        idx = np.nonzero(w.pair == p)[0]
+        if idx.size == 0:
+            continue
+        a, b = om[w.pairs[p, 0]], om[w.pairs[p, 1]]
+        c, ct, bv, lf = O.collide_batch(a, b, w.tf2[idx], None if w.tf1 is None else w.tf1[idx],
+                                        num_max_contacts=maxc, nthreads=nthreads)
+        off = np.concatenate([[0], np.cumsum(c)])
+        for j, q in enumerate(idx):
+            order.append((q, ct[off[j]:off[j + 1]]))
+        counts.append((idx, c)); nbv.append((idx, bv)); nleaf.append((idx, lf))
+    n = w.n
+    C = np.zeros(n, np.int64); BV = np.zeros(n, np.int64); LF = np.zeros(n, np.int64)
+    for idx, c in counts:
+        C[idx] = c
+    for idx, c in nbv:
+        BV[idx] = c
+    for idx, c in nleaf:
+        LF[idx] = c
+    order.sort(key=lambda x: x[0])
+    ct = np.concatenate([x[1] for x in order]) if order else np.zeros((0, 2), np.int32)
+    return C, ct, BV, LF
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("maxc", [1, 100000])
+def test_collide_config0_matches_oracle(gpu_lib, precision, maxc):
+    w = W.config0(n_poses=2000)
+    ms = _meshes(w)
+    out = api.collide_batch(ms, w.pairs, None, w.tf2, num_max_contacts=maxc, precision=precision,
+                            statistics=True)
+    C, ct, BV, LF = _oracle_collide(w, maxc)
+    assert np.array_equal(out["counts"], C)
+    assert np.array_equal(out["contacts"], ct)
+    assert np.array_equal(out["num_bv_tests"], BV)
+    assert np.array_equal(out["num_leaf_tests"], LF)
+    if precision == "fp64":
+        assert out["num_rechecks"].sum() == 0
+    else:
+        assert out["num_rechecks"].sum() <= 0.01 * (BV.sum() + LF.sum())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_collide_reference_fixture(gpu_lib, golden, precision):
+    ms = [api.BVHModel.from_arrays(golden["env_v"], golden["env_t"]),
+          api.BVHModel.from_arrays(golden["rob_v"], golden["rob_t"])]
+    tf = golden["tf"]
+    out = api.collide_batch(ms, [[0, 1]], None, tf, num_max_contacts=1 << 30, precision=precision,
+                            statistics=True)
+    env = O.Mesh(golden["env_v"], golden["env_t"]); rob = O.Mesh(golden["rob_v"], golden["rob_t"])
+    c, ct, bv, lf = O.collide_batch(env, rob, tf, num_max_contacts=1 << 30)
+    assert np.array_equal(out["counts"], c) and np.array_equal(out["contacts"], ct)
+    assert np.array_equal(out["num_bv_tests"], bv) and np.array_equal(out["num_leaf_tests"], lf)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_collide_multi_pair_uneven_with_tf1(gpu_lib, precision):
+    w = W.config1(scale=0.004, n_pairs=6, tri_hi=30000, seed=3)
+    w.tf1 = W.random_poses(w.n, -0.3, 0.3, 77)
+    ms = _meshes(w)
+    out = api.collide_batch(ms, w.pairs, w.tf1, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                            precision=precision, statistics=True)
+    C, ct, BV, LF = _oracle_collide(w, 100000)
+    assert np.array_equal(out["counts"], C)
+    assert np.array_equal(out["contacts"], ct)
+    assert np.array_equal(out["num_bv_tests"], BV) and np.array_equal(out["num_leaf_tests"], LF)
+
+
+def test_collide_device_api_torch(gpu_lib):
+    import torch
+    w = W.config0(n_poses=3000, seed=4)
+    ms = _meshes(w)
+    tf2 = torch.from_numpy(w.tf2).cuda()
+    outs = {}
+    for prec in ("fp64", "fp32"):
+        o = api.collide_batch(ms, w.pairs, None, tf2, num_max_contacts=100000, precision=prec, statistics=True)
+        torch.cuda.synchronize()
+        outs[prec] = {k: (v.cpu().numpy() if hasattr(v, "cpu") else v) for k, v in o.items()}
+    C, ct, BV, LF = _oracle_collide(w, 100000)
+    for prec in outs:
+        assert np.array_equal(outs[prec]["counts"], C)
+        assert np.array_equal(outs[prec]["contacts"], ct)
+        assert np.array_equal(outs[prec]["offsets"][1:], np.cumsum(C))
+
+
+def test_collide_fp32_equals_fp64_at_scale(gpu_lib):
+    # size-independent property at a larger batch: both forms agree exactly
+    w = W.config1(scale=0.1, n_pairs=8, tri_hi=100000, seed=9)
+    ms = _meshes(w)
+    a = api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                          precision="fp64", statistics=True)
+    b = api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                          precision="fp32", statistics=True)
+    assert np.array_equal(a["counts"], b["counts"]) and np.array_equal(a["contacts"], b["contacts"])
+    assert np.array_equal(a["num_bv_tests"], b["num_bv_tests"])
+    # every reported pair is a real intersection per the oracle's triangle test
+    rng = np.random.default_rng(0)
+    sel = rng.choice(np.nonzero(a["counts"])[0], size=min(50, int((a["counts"] > 0).sum())), replace=False)
+    for q in sel:
+        p = w.pair[q]; A = w.meshes[w.pairs[p, 0]]; B = w.meshes[w.pairs[p, 1]]
+        lo, hi = a["offsets"][q], a["offsets"][q + 1]
+        pairs = a["contacts"][lo:hi]
+        P = A[0][A[1][pairs[:, 0]]].reshape(-1, 9); Q = B[0][B[1][pairs[:, 1]]].reshape(-1, 9)
+        assert O.tri_intersect_batch(P, Q, w.tf2[q]).all()
+
+
+def test_collide_empty_and_zero_contacts(gpu_lib):
+    w = W.config0(n_poses=10, freq=4)
+    ms = _meshes(w)
+    out = api.collide_batch(ms, w.pairs, None, w.tf2[:0], num_max_contacts=1)
+    assert out["counts"].shape == (0,) and out["total_contacts"] == 0
+    out = api.collide_batch(ms, w.pairs, None, w.tf2, num_max_contacts=0)
+    assert out["counts"].sum() == 0
+
+
+def test_distance_fp64_bit_exact(gpu_lib):
+    w = W.config0(n_poses=400, seed=2)
+    ms = _meshes(w)
+    out = api.distance_batch(ms, w.pairs, None, w.tf2, nearest_points=True, precision="fp64", statistics=True)
+    a = O.Mesh(*w.meshes[0]); b = O.Mesh(*w.meshes[1])
+    d, ids, pts, nbv, nl = O.distance_batch(a, b, w.tf2, nearest=True, nthreads=8)
+    assert np.array_equal(out["min_distance"], d)
+    assert np.array_equal(out["ids"], ids)
+    assert np.array_equal(out["nearest_points"], pts)
+    assert np.array_equal(out["num_bv_tests"], nbv) and np.array_equal(out["num_leaf_tests"], nl)
+
+
+def test_distance_reference_fixture(gpu_lib, golden):
+    ms = [api.BVHModel.from_arrays(golden["env_v"], golden["env_t"]),
+          api.BVHModel.from_arrays(golden["rob_v"], golden["rob_t"])]
+    out = api.distance_batch(ms, [[0, 1]], None, golden["tf"], nearest_points=True, precision="fp64")
+    env = O.Mesh(golden["env_v"], golden["env_t"]); rob = O.Mesh(golden["rob_v"], golden["rob_t"])
+    for i in range(golden["tf"].shape[0]):
+        assert out["min_distance"][i] == O.brute_distance(env, rob, golden["tf"][i])

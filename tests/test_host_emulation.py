@@ -1,0 +1,68 @@
+"""Product code paths checked on the CPU against the oracle.
+
+The BVH build (bvh_build.cpp) and the per-query traversal (collide_traverse.cuh,
+the code the GPU kernel runs, FP32 filters and FP64 rechecks included) are compiled
+for the host by tests/native and must reproduce the oracle bit for bit."""
+import numpy as np
+import pytest
+
+from fcl_gb300 import workloads as W
+from oracle import pyoracle as O
+from tests import emul
+
+
+@pytest.mark.parametrize("freq,seed", [(1, 0), (3, 1), (8, 2), (16, 3)])
+def test_bvh_build_bit_exact(freq, seed):
+    v, t = W.perturbed_ellipsoid(freq, (1.0, 0.7, 0.5), 0.01, seed)
+    on, ofc = O.Mesh(v, t).nodes()
+    en, efc, _ = emul.build(v, t)
+    assert np.array_equal(ofc, efc)
+    assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
+
+
+def test_bvh_build_bit_exact_reference_meshes(golden):
+    for k in ("env", "rob"):
+        on, ofc = O.Mesh(golden[k + "_v"], golden[k + "_t"]).nodes()
+        en, efc, _ = emul.build(golden[k + "_v"], golden[k + "_t"])
+        assert np.array_equal(ofc, efc) and np.array_equal(on.view(np.uint64), en.view(np.uint64))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("maxc", [1, 100000])
+def test_traversal_matches_oracle_c0(prec, maxc):
+    w = W.config0(n_poses=300)
+    a = O.Mesh(*w.meshes[0]); b = O.Mesh(*w.meshes[1])
+    oc, oct_, onbv, onl = O.collide_batch(a, b, w.tf2, num_max_contacts=maxc, nthreads=4)
+    ec, ect, enbv, enl, enrc = emul.collide(prec, w.meshes[0], w.meshes[1], w.tf2, maxc)
+    assert np.array_equal(oc, ec)
+    assert np.array_equal(oct_, ect)          # same contacts in the same DFS order
+    assert np.array_equal(onbv, enbv) and np.array_equal(onl, enl)
+    if prec == 0:
+        assert enrc.sum() == 0
+    else:
+        assert enrc.sum() <= 0.01 * (enbv.sum() + enl.sum())
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_traversal_matches_oracle_reference_fixture(golden, prec):
+    env = (golden["env_v"], golden["env_t"]); rob = (golden["rob_v"], golden["rob_t"])
+    a = O.Mesh(*env); b = O.Mesh(*rob)
+    tf = golden["tf"]
+    oc, oct_, onbv, onl = O.collide_batch(a, b, tf, num_max_contacts=1 << 30)
+    ec, ect, enbv, enl, _ = emul.collide(prec, env, rob, tf, 1 << 30)
+    assert np.array_equal(oc, ec) and np.array_equal(oct_, ect)
+    assert np.array_equal(onbv, enbv) and np.array_equal(onl, enl)
+
+
+def test_traversal_with_tf1_small_triangles():
+    # dense meshes (small triangles relative to coordinates) stress the FP32 bounds
+    w = W.config1(scale=0.005, n_pairs=2, tri_hi=60000, seed=5)
+    for p in range(2):
+        A = w.meshes[w.pairs[p, 0]]; B = w.meshes[w.pairs[p, 1]]
+        tf2 = w.tf2[w.pair == p][:60]
+        tf1 = W.random_poses(tf2.shape[0], -0.5, 0.5, 99 + p)
+        a = O.Mesh(*A); b = O.Mesh(*B)
+        oc, oct_, onbv, onl = O.collide_batch(a, b, tf2, tf1=tf1, num_max_contacts=100000, nthreads=4)
+        ec, ect, enbv, enl, enrc = emul.collide(1, A, B, tf2, 100000, tf1=tf1)
+        assert np.array_equal(oc, ec) and np.array_equal(oct_, ect)
+        assert np.array_equal(onbv, enbv) and np.array_equal(onl, enl)
