@@ -46,7 +46,7 @@ def _peaks():
 
 def _workload(args, rank):
     from fcl_gb300 import workloads as W
-    return W.config1(scale=args.scale, seed=1 + 1000 * rank)
+    return W.config1(scale=args.scale, seed=1 + 1000 * rank, n_pairs=args.pairs, tri_hi=args.tri_hi)
 
 
 # ------------------------------------------------------------------------------------
@@ -177,7 +177,7 @@ def run_gpu(args):
 
     def step(prec, stats=False):
         return api.collide_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000,
-                                 precision=prec, statistics=stats, stream=stream.cuda_stream)
+                                 precision=prec, statistics=stats, stream=stream.cuda_stream, budget=args.budget)
 
     # reference run for exact-hit check and algorithmic byte counts (outside timing)
     ref64 = step("fp64", stats=True)
@@ -238,7 +238,7 @@ def run_gpu(args):
 
         def step64():
             return api.collide_batch(meshes, w.pairs, None, tf2_s, pair_of_query=pq_s, num_max_contacts=100000,
-                                     precision="fp64", stream=stream.cuda_stream)
+                                     precision="fp64", stream=stream.cuda_stream, budget=args.budget)
         step64()
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -261,7 +261,7 @@ def run_gpu(args):
     cont_h = torch.empty((max(total_contacts, 1), 2), dtype=torch.int32).pin_memory()
     meshes_c = (C.c_void_p * len(meshes))(*[m.handle.value for m in meshes])
     pairs_np = np.ascontiguousarray(w.pairs, np.int32)
-    req = native.CollideRequest(100000, native.FP32_RECHECK, 0, 0)
+    req = native.CollideRequest(100000, native.FP32_RECHECK, 0, args.budget)
 
     def e2e_step():
         res = native.CollideResult(counts_h.data_ptr(), offs_h.data_ptr(), cont_h.data_ptr(), cont_h.shape[0],
@@ -348,6 +348,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fcl_gb300", choices=["fcl_gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="pose-count scale of the workload")
+    ap.add_argument("--pairs", type=int, default=64, help="mesh pairs (64 in the headline workload)")
+    ap.add_argument("--tri-hi", type=int, default=200000, help="largest triangle count of the mesh set")
+    ap.add_argument("--budget", type=int, default=0, help="BV tests per work item per round (0 = default)")
     ap.add_argument("--cpu-sample", type=int, default=2000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 form")

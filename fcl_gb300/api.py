@@ -254,12 +254,12 @@ def _is_torch(x) -> bool:
 
 
 def collide_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, precision="fp32",
-                  statistics=False, contacts=True, stream=None):
+                  statistics=False, contacts=True, stream=None, budget=0):
     """Batched fcl::collide.  Host (numpy) inputs use the host entry point (copies in
     and out); torch CUDA tensors use the device entry point.  Returns a dict with
     counts, offsets, contacts (total, 2) and optional statistics."""
     pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
-    req = N.CollideRequest(int(num_max_contacts), _prec(precision), int(bool(statistics)), 0)
+    req = N.CollideRequest(int(num_max_contacts), _prec(precision), int(bool(statistics)), int(budget))
     hs = _handles(meshes)
     if _is_torch(tf2):
         return _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statistics, contacts, stream)

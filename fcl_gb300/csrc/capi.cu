@@ -127,6 +127,154 @@ int prepare_tables(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t*
   return FCLGPU_OK;
 }
 
+
+// ---------------------------------------------------------------------------------
+// Collide batch core: budgeted rounds of work items, then the item-tree assembly.
+// ---------------------------------------------------------------------------------
+struct SplitScratch {
+  DevBuf items, own, cstart, ccount, total, rel_start, capped;
+  int64_t item_hint = 0;
+  CollideLaunch last;       // launch description of the last batch (for the scatter)
+  int64_t last_nrec = 0;
+  std::vector<std::pair<int64_t, int64_t>> rounds;
+  std::vector<cudaEvent_t> ev;
+};
+SplitScratch g_split;
+
+int64_t g_default_budget = 4096;
+
+int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
+                 const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
+                 int64_t* nrc, int stack, cudaStream_t s, int64_t* total_out) {
+  Scratch& S = g_scratch;
+  SplitScratch& P = g_split;
+  CK(S.ctr.ensure(sizeof(BatchCounters)), "counters");
+  const int64_t maxc = std::max<int64_t>(req->num_max_contacts, 0);
+  const int64_t budget = req->budget > 0 ? req->budget : g_default_budget;
+  int64_t rec_cap = std::max<int64_t>(S.record_hint, std::min<int64_t>(n * std::max<int64_t>(maxc, 1), 4 * n) + 65536);
+  int64_t item_cap = std::max<int64_t>(P.item_hint, 4 * n + (1 << 20));
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    CK(S.records.ensure(sizeof(int4) * (size_t)rec_cap), "record scratch");
+    rec_cap = (int64_t)(S.records.cap / sizeof(int4));
+    CK(P.items.ensure(sizeof(int4) * (size_t)item_cap), "item scratch");
+    item_cap = (int64_t)(P.items.cap / sizeof(int4));
+    CK(P.own.ensure(4 * (size_t)item_cap), "item scratch");
+    CK(P.cstart.ensure(4 * (size_t)item_cap), "item scratch");
+    CK(P.ccount.ensure(4 * (size_t)item_cap), "item scratch");
+    if (req->enable_statistics) {
+      if (nbv) CK(cudaMemsetAsync(nbv, 0, 8 * n, s), "stats");
+      if (nleaf) CK(cudaMemsetAsync(nleaf, 0, 8 * n, s), "stats");
+      if (nrc) CK(cudaMemsetAsync(nrc, 0, 8 * n, s), "stats");
+    }
+    BatchCounters h0;
+    std::memset(&h0, 0, sizeof(h0));
+    h0.items = (unsigned long long)n;
+    CK(cudaMemcpyAsync(S.ctr.p, &h0, sizeof(h0), cudaMemcpyHostToDevice, s), "counters");
+    CollideLaunch L{};
+    L.meshes = (const DevMesh*)S.meshes.p;
+    L.pairs = (const int2*)S.pairs.p;
+    L.pair_of_query = pair_of_query;
+    L.tf1 = tf1;
+    L.tf2 = tf2;
+    L.n = n;
+    L.num_max_contacts = (int32_t)std::min<int64_t>(maxc, INT32_MAX);
+    L.want_stats = req->enable_statistics;
+    L.ctr = (BatchCounters*)S.ctr.p;
+    L.records = (int4*)S.records.p;
+    L.record_cap = rec_cap;
+    L.counts = counts;
+    L.nbv = nbv;
+    L.nleaf = nleaf;
+    L.nrecheck = nrc;
+    L.items = (int4*)P.items.p;
+    L.item_cap = item_cap;
+    L.budget = budget;
+    L.own = (int32_t*)P.own.p;
+    L.child_start = (int32_t*)P.cstart.p;
+    L.child_count = (int32_t*)P.ccount.p;
+    const int block = 128;
+    const int grid = collide_round_grid(req->precision, stack, block);
+    P.rounds.clear();
+    int64_t lo = 0, hi = n;
+    bool retry = false;
+    double kernel_ms = 0.0;
+    BatchCounters hc;
+    for (int round = 0; round < 100000 && hi > lo; ++round) {
+      L.item_lo = lo;
+      L.item_hi = hi;
+      P.rounds.emplace_back(lo, hi);
+      if (P.ev.size() < 2) {
+        for (int k = 0; k < 2; ++k) {
+          cudaEvent_t e;
+          CK(cudaEventCreate(&e), "event");
+          P.ev.push_back(e);
+        }
+      }
+      CK(cudaMemsetAsync(&L.ctr->work, 0, sizeof(unsigned long long), s), "counters");
+      CK(cudaEventRecord(P.ev[0], s), "event");
+      CK(launch_collide_round(L, req->precision, stack, grid, block, s), "collide round");
+      CK(cudaEventRecord(P.ev[1], s), "event");
+      CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
+      CK(cudaStreamSynchronize(s), "collide round");
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]), "event");
+      kernel_ms += ms;
+      if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
+      if (hc.status & (DEV_ERR_RECORDS | DEV_ERR_ITEMS)) {
+        if (hc.status & DEV_ERR_RECORDS) rec_cap = std::max<int64_t>(rec_cap * 2, (int64_t)hc.records + 65536);
+        if (hc.status & DEV_ERR_ITEMS) item_cap = std::max<int64_t>(item_cap * 2, (int64_t)hc.items + 65536);
+        if (item_cap > 0x7fffffffll) return fail(FCLGPU_ERR_OUT_OF_MEMORY, "work items exceed 2^31");
+        S.record_hint = rec_cap;
+        P.item_hint = item_cap;
+        retry = true;
+        break;
+      }
+      lo = hi;
+      hi = (int64_t)hc.items;
+    }
+    if (retry) continue;
+    g_last_kernel_ms = kernel_ms;
+    const int64_t nitems = hi;
+    S.record_hint = std::max<int64_t>(S.record_hint, (int64_t)hc.records);
+    P.item_hint = std::max<int64_t>(P.item_hint, nitems);
+    P.last_nrec = (int64_t)hc.records;
+    // assembly: totals bottom-up, counts and offsets, starts top-down
+    CK(P.total.ensure(8 * (size_t)std::max<int64_t>(nitems, 1)), "item scratch");
+    CK(P.rel_start.ensure(8 * (size_t)std::max<int64_t>(nitems, 1)), "item scratch");
+    CK(P.capped.ensure(4 * (size_t)std::max<int64_t>(n, 1)), "item scratch");
+    int64_t* tot = (int64_t*)P.total.p;
+    for (size_t r = P.rounds.size(); r-- > 0;)
+      CK(launch_item_totals(L, P.rounds[r].first, P.rounds[r].second, tot, s), "item totals");
+    CK(launch_item_counts(L, tot, (int32_t*)P.capped.p, s), "item counts");
+    CK(S.scan_tmp.ensure(sizeof(int64_t) * (size_t)(2 * ((n + 4095) / 4096) + 4)), "scan scratch");
+    CK(launch_exclusive_scan(counts, n, offsets, (int64_t*)S.scan_tmp.p, s), "scan");
+    for (size_t r = 0; r < P.rounds.size(); ++r)
+      CK(launch_item_starts(L, P.rounds[r].first, P.rounds[r].second, tot, (int64_t*)P.rel_start.p, s),
+         "item starts");
+    int64_t total = 0;
+    CK(cudaMemcpyAsync(&total, offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read total");
+    CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
+    CK(cudaStreamSynchronize(s), "assembly");
+    if (req->enable_statistics && hc.capped_split > 0) {
+      // queries split across items and capped at num_max_contacts ran past FCL's stop
+      // point; their statistics come from an exact serial traversal
+      CK(cudaMemsetAsync(&L.ctr->work, 0, sizeof(unsigned long long), s), "counters");
+      CK(launch_collide_stats(L, (const int32_t*)P.capped.p, (int64_t)hc.capped_split, req->precision, stack, s),
+         "stats pass");
+    }
+    P.last = L;
+    *total_out = total;
+    return FCLGPU_OK;
+  }
+  return fail(FCLGPU_ERR_OUT_OF_MEMORY, "batch scratch kept overflowing");
+}
+
+int collide_scatter(const int64_t* offsets, int32_t* contacts, cudaStream_t s) {
+  CK(launch_scatter_items(g_split.last, g_split.last_nrec, (const int64_t*)g_split.rel_start.p, offsets, contacts, s),
+     "scatter");
+  return FCLGPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -295,72 +443,19 @@ int fclgpu_collide_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, c
     if (res->offsets) CK(cudaMemsetAsync(res->offsets, 0, sizeof(int64_t), s), "offsets");
     return FCLGPU_OK;
   }
-  Scratch& S = g_scratch;
-  CK(S.ctr.ensure(sizeof(BatchCounters)), "counters");
-  const int64_t maxc = std::max<int64_t>(req->num_max_contacts, 0);
-  int64_t rec_cap = std::max<int64_t>(S.record_hint, std::min<int64_t>(n * std::max<int64_t>(maxc, 1), 4 * n) + 65536);
-  for (int attempt = 0; attempt < 6; ++attempt) {
-    CK(S.records.ensure(sizeof(int4) * (size_t)rec_cap), "record scratch");
-    rec_cap = (int64_t)(S.records.cap / sizeof(int4));
-    CK(cudaMemsetAsync(S.ctr.p, 0, sizeof(BatchCounters), s), "counters");
-    CollideLaunch L;
-    L.meshes = (const DevMesh*)S.meshes.p;
-    L.pairs = (const int2*)S.pairs.p;
-    L.pair_of_query = pair_of_query;
-    L.tf1 = tf1;
-    L.tf2 = tf2;
-    L.n = n;
-    L.num_max_contacts = (int32_t)std::min<int64_t>(maxc, INT32_MAX);
-    L.want_stats = req->enable_statistics;
-    L.ctr = (BatchCounters*)S.ctr.p;
-    L.records = (int4*)S.records.p;
-    L.record_cap = rec_cap;
-    L.counts = res->counts;
-    L.nbv = res->num_bv_tests;
-    L.nleaf = res->num_leaf_tests;
-    L.nrecheck = res->num_rechecks;
-    const int block = 128;
-    const int grid = collide_grid(req->precision, stack, block);
-    rc = ensure_events();
-    if (rc) return rc;
-    CK(cudaEventRecord(g_ev[0], s), "event");
-    CK(launch_mesh_collide(L, req->precision, stack, grid, block, s), "collide kernel");
-    CK(cudaEventRecord(g_ev[1], s), "event");
-    BatchCounters hc;
-    CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
-    CK(cudaStreamSynchronize(s), "collide kernel");
-    {
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, g_ev[0], g_ev[1]), "event");
-      g_last_kernel_ms = ms;
-    }
-    if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
-    if (hc.status & DEV_ERR_RECORDS) {
-      rec_cap = (int64_t)hc.records + 65536;
-      S.record_hint = rec_cap;
-      continue;
-    }
-    const int64_t nrec = (int64_t)hc.records;
-    S.record_hint = std::max<int64_t>(S.record_hint, nrec);
-    S.last_nrec = nrec;
-    if (!res->offsets && !res->contacts) return FCLGPU_OK;
-    int64_t* offsets = res->offsets;
-    if (!offsets) {
-      CK(S.offsets.ensure(sizeof(int64_t) * (size_t)(n + 1)), "offsets scratch");
-      offsets = (int64_t*)S.offsets.p;
-    }
-    CK(S.scan_tmp.ensure(sizeof(int64_t) * (size_t)(2 * ((n + 4095) / 4096) + 4)), "scan scratch");
-    CK(launch_exclusive_scan(res->counts, n, offsets, (int64_t*)S.scan_tmp.p, s), "scan");
-    int64_t total = 0;
-    CK(cudaMemcpyAsync(&total, offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read total");
-    CK(cudaStreamSynchronize(s), "scan");
-    res->total_contacts = total;
-    if (!res->contacts) return FCLGPU_OK;
-    if (total > res->contacts_capacity) return fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
-    CK(launch_scatter_contacts((const int4*)S.records.p, nrec, offsets, res->contacts, s), "scatter");
-    return FCLGPU_OK;
+  int64_t* offsets = res->offsets;
+  if (!offsets) {
+    CK(g_scratch.offsets.ensure(sizeof(int64_t) * (size_t)(n + 1)), "offsets scratch");
+    offsets = (int64_t*)g_scratch.offsets.p;
   }
-  return fail(FCLGPU_ERR_OUT_OF_MEMORY, "contact record scratch kept overflowing");
+  int64_t total = 0;
+  rc = collide_core(n, pair_of_query, tf1, tf2, req, res->counts, offsets, res->num_bv_tests,
+                    res->num_leaf_tests, res->num_rechecks, stack, s, &total);
+  if (rc) return rc;
+  res->total_contacts = total;
+  if (!res->contacts) return FCLGPU_OK;
+  if (total > res->contacts_capacity) return fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
+  return collide_scatter(offsets, res->contacts, s);
 }
 
 int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
@@ -406,10 +501,9 @@ int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const in
   if (res->contacts) {
     if (dr.total_contacts > res->contacts_capacity) return fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
     CK(S.out_contacts.ensure(8 * (size_t)std::max<int64_t>(dr.total_contacts, 1)), "contacts scratch");
-    // records of the last launch are still in scratch: scatter them now
-    CK(launch_scatter_contacts((const int4*)S.records.p, S.last_nrec, (const int64_t*)S.offsets.p,
-                               (int32_t*)S.out_contacts.p, s),
-       "scatter");
+    // records of the batch are still in scratch: scatter them now
+    rc = collide_scatter((const int64_t*)S.offsets.p, (int32_t*)S.out_contacts.p, s);
+    if (rc) return rc;
     if (dr.total_contacts)
       CK(cudaMemcpyAsync(res->contacts, S.out_contacts.p, 8 * dr.total_contacts, cudaMemcpyDeviceToHost, s), "d2h");
   }

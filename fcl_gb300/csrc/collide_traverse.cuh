@@ -88,6 +88,120 @@ bool bv_overlap64(const DevMesh& A, const DevMesh& B, int b1, int b2, const M3<d
   return obb_overlap64(R, T, na, nb);
 }
 
+// Per-item traversal with a test budget, used by the work-splitting batch.
+//
+// An item is a query plus a starting BV pair.  The item runs FCL's DFS from that pair
+// until it is exhausted or `budget` BV tests have been spent.  In the second case the
+// unfinished frontier -- the current pair, then the stacked siblings from the top of
+// the stack down -- is exactly the rest of the item's DFS order, split into
+// contiguous pieces; the caller writes it out as new items in that order.  The
+// item's own contacts are a prefix of its DFS-order output, so the batch output is
+// rebuilt as: own contacts, then the children's outputs in order.
+// Sink interface: push(item, rank, b1, b2) appends a contact; dump(item, qi, cur,
+// stk, sp) writes the frontier (cur, stk[sp-1], ..., stk[0]) as child items of `item`.
+template <int PREC, int STACK, class Sink>
+FCLG_HD int collide_item(const CollideLaunch& L, long long qi, int sb1, int sb2, long long item, long long budget,
+                         int maxc, Sink& sink, QueryStats& st) {
+  const int pi = L.pair_of_query ? FCLG_LDG(L.pair_of_query + qi) : 0;
+  const int2 mp = L.pairs[pi];
+  const DevMesh A = L.meshes[mp.x];
+  const DevMesh B = L.meshes[mp.y];
+  M3<double> R;
+  V3<double> T;
+  double ta[12];
+  query_transform_collide(L.tf1, L.tf2, qi, R, T, ta);
+  QueryF32 qf;
+  if (PREC == 1) make_query_f32(R, T, A.cmax, B.cmax, A.vmax, B.vmax, qf);
+  int ncont = 0;
+  st.nbv = st.nleaf = st.nrecheck = 0;
+  st.status = 0;
+  if (maxc <= 0) return 0;
+  int2 stk[STACK];
+  int sp = 0;
+  int b1 = sb1, b2 = sb2;
+  for (;;) {
+    if (st.nbv >= budget) {
+      sink.dump(item, qi, make_int2(b1, b2), stk, sp);
+      break;
+    }
+    int c1, c2;
+    bool overlap;
+    if (PREC == 0) {
+      NodeD na, nb;
+      load_nodeD(A.nodes64 + b1, na);
+      load_nodeD(B.nodes64 + b2, nb);
+      c1 = na.child;
+      c2 = nb.child;
+      overlap = obb_overlap64(R, T, na, nb);
+    } else {
+      const float4* pa = reinterpret_cast<const float4*>(A.nodes32) + 4 * (long long)b1;
+      const float4* pb = reinterpret_cast<const float4*>(B.nodes32) + 4 * (long long)b2;
+      const float4 a0 = FCLG_LDG(pa), a1 = FCLG_LDG(pa + 1), a2 = FCLG_LDG(pa + 2), ea = FCLG_LDG(pa + 3);
+      const float4 x0 = FCLG_LDG(pb), x1 = FCLG_LDG(pb + 1), x2 = FCLG_LDG(pb + 2), eb = FCLG_LDG(pb + 3);
+      c1 = FCLG_F2I(ea.w);
+      c2 = FCLG_F2I(eb.w);
+      int r = obb_overlap_f32(qf, a0, a1, a2, ea, x0, x1, x2, eb);
+      if (r == F_UNSURE) {
+        ++st.nrecheck;
+        r = bv_overlap64(A, B, b1, b2, R, T) ? F_TRUE : F_FALSE;
+      }
+      overlap = (r == F_TRUE);
+    }
+    ++st.nbv;
+    if (overlap) {
+      const bool l1 = c1 < 0, l2 = c2 < 0;
+      if (l1 && l2) {
+        ++st.nleaf;
+        const int p1 = -(c1 + 1), p2 = -(c2 + 1);
+        bool hit;
+        if (PREC == 0) {
+          hit = leaf_collide64(A, B, p1, p2, R, T);
+        } else {
+          const float4* ta4 = reinterpret_cast<const float4*>(A.tri32) + 3 * (long long)p1;
+          const float4* tb4 = reinterpret_cast<const float4*>(B.tri32) + 3 * (long long)p2;
+          int r = tri_intersect_f32(qf, FCLG_LDG(ta4), FCLG_LDG(ta4 + 1), FCLG_LDG(ta4 + 2), FCLG_LDG(tb4),
+                                    FCLG_LDG(tb4 + 1), FCLG_LDG(tb4 + 2));
+          if (r == F_UNSURE) {
+            ++st.nrecheck;
+            r = leaf_collide64(A, B, p1, p2, R, T) ? F_TRUE : F_FALSE;
+          }
+          hit = (r == F_TRUE);
+        }
+        if (hit) {
+          sink.push((int)item, ncont, p1, p2);
+          ++ncont;
+          if (ncont >= maxc) break;
+        }
+      } else {
+        bool first_over_second;
+        if (l2)
+          first_over_second = true;
+        else if (l1)
+          first_over_second = false;
+        else
+          first_over_second = FCLG_LDG(A.size64 + b1) > FCLG_LDG(B.size64 + b2);
+        if (sp >= STACK) {
+          st.status |= DEV_ERR_STACK;
+          break;
+        }
+        if (first_over_second) {
+          stk[sp++] = make_int2(c1 + 1, b2);
+          b1 = c1;
+        } else {
+          stk[sp++] = make_int2(b1, c2 + 1);
+          b2 = c2;
+        }
+        continue;
+      }
+    }
+    if (sp == 0) break;
+    const int2 e = stk[--sp];
+    b1 = e.x;
+    b2 = e.y;
+  }
+  return ncont;
+}
+
 // Runs query qi; contacts go to sink.push(qi, rank, b1, b2).  Returns the number of
 // contacts.
 template <int PREC, int STACK, class Sink>

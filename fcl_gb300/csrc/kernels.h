@@ -11,6 +11,7 @@ namespace fclgpu {
 enum : uint32_t {
   DEV_ERR_STACK = 1u,     // traversal stack overflow
   DEV_ERR_RECORDS = 2u,   // contact record scratch overflow
+  DEV_ERR_ITEMS = 4u,     // work-item scratch overflow
 };
 
 // Counters shared by one batch launch (device scratch).
@@ -19,6 +20,8 @@ struct BatchCounters {
   unsigned long long records;   // contact-record slots reserved
   unsigned int status;          // DEV_ERR_* bits
   unsigned int pad;
+  unsigned long long items;     // items allocated so far (split batches; starts at n)
+  unsigned long long capped_split;
 };
 
 struct CollideLaunch {
@@ -31,13 +34,37 @@ struct CollideLaunch {
   int32_t num_max_contacts;
   int32_t want_stats;
   BatchCounters* ctr;
-  int4* records;                 // (query, rank, b1, b2)
+  int4* records;                 // (item, rank, b1, b2)
   int64_t record_cap;
   int32_t* counts;
   int64_t* nbv;
   int64_t* nleaf;
   int64_t* nrecheck;
+  // work splitting: items [item_lo, item_hi) run this round; item i < n is query i
+  // at the root pair, later items are items[i] = (query, b1, b2, -)
+  int4* items;
+  int64_t item_cap;
+  int64_t item_lo, item_hi;
+  int64_t budget;                // BV tests per item per round
+  int32_t* own;                  // per item: contacts found by the item itself
+  int32_t* child_start;          // per item: id of its first child item
+  int32_t* child_count;          // per item: number of child items (0 = finished)
 };
+
+cudaError_t launch_collide_round(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
+                                 cudaStream_t s);
+cudaError_t launch_item_totals(const CollideLaunch& L, int64_t lo, int64_t hi, int64_t* total, cudaStream_t s);
+// counts[q] = min(total[q], num_max_contacts); queries that were split and reached the
+// cap are listed in capped[] (their statistics need the exact serial pass).
+cudaError_t launch_item_counts(const CollideLaunch& L, const int64_t* total, int32_t* capped, cudaStream_t s);
+cudaError_t launch_item_starts(const CollideLaunch& L, int64_t lo, int64_t hi, const int64_t* total,
+                               int64_t* rel_start, cudaStream_t s);
+cudaError_t launch_scatter_items(const CollideLaunch& L, int64_t nrec, const int64_t* rel_start,
+                                 const int64_t* offsets, int32_t* contacts, cudaStream_t s);
+// Serial exact traversal of the listed queries, statistics only (counts untouched).
+cudaError_t launch_collide_stats(const CollideLaunch& L, const int32_t* list, int64_t nlist, int precision,
+                                 int stack_entries, cudaStream_t s);
+int collide_round_grid(int precision, int stack_entries, int block);
 
 struct DistanceLaunch {
   const DevMesh* meshes;

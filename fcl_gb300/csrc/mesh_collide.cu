@@ -76,6 +76,160 @@ __global__ void __launch_bounds__(128) k_mesh_collide(const CollideLaunch L) {
 }
 
 // ---------------------------------------------------------------------------------
+// Work-splitting rounds.  Items [item_lo, item_hi) run with a BV-test budget; an
+// item that exhausts it writes its frontier as child items (contiguous ids, DFS
+// order) for the next round.
+// ---------------------------------------------------------------------------------
+struct SplitSink : ContactSink {
+  int4* items;
+  long long item_cap;
+  unsigned long long* item_ctr;
+  int32_t* child_start;
+  int32_t* child_count;
+  bool dumped;
+
+  __device__ __forceinline__ void dump(long long item, long long qi, int2 cur, const int2* stk, int sp) {
+    const int k = 1 + sp;
+    const long long b = (long long)atomicAdd(item_ctr, (unsigned long long)k);
+    if (b + k > item_cap || b + k > 0x7fffffffll) {
+      atomicOr(status, DEV_ERR_ITEMS);
+      return;
+    }
+    items[b] = make_int4((int)qi, cur.x, cur.y, 0);
+    for (int j = 0; j < sp; ++j) {
+      const int2 e = stk[sp - 1 - j];
+      items[b + 1 + j] = make_int4((int)qi, e.x, e.y, 0);
+    }
+    child_start[item] = (int32_t)b;
+    child_count[item] = k;
+    dumped = true;
+  }
+};
+
+template <int PREC, int STACK>
+__global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
+  SplitSink sink;
+  sink.rec = L.records;
+  sink.cap = L.record_cap;
+  sink.ctr = &L.ctr->records;
+  sink.status = &L.ctr->status;
+  sink.base = -1;
+  sink.used = 0;
+  sink.items = L.items;
+  sink.item_cap = L.item_cap;
+  sink.item_ctr = &L.ctr->items;
+  sink.child_start = L.child_start;
+  sink.child_count = L.child_count;
+  const long long span = L.item_hi - L.item_lo;
+  for (;;) {
+    const long long k = (long long)atomicAdd(&L.ctr->work, 1ull);
+    if (k >= span) break;
+    const long long item = L.item_lo + k;
+    long long qi;
+    int b1, b2;
+    if (item < L.n) {
+      qi = item;
+      b1 = b2 = 0;
+    } else {
+      const int4 it = L.items[item];
+      qi = it.x;
+      b1 = it.y;
+      b2 = it.z;
+    }
+    sink.dumped = false;
+    QueryStats st;
+    const int ncont = collide_item<PREC, STACK>(L, qi, b1, b2, item, L.budget, L.num_max_contacts, sink, st);
+    if (st.status) atomicOr(&L.ctr->status, st.status);
+    L.own[item] = ncont;
+    if (!sink.dumped) L.child_count[item] = 0;
+    if (L.want_stats) {
+      if (L.nbv) atomicAdd((unsigned long long*)(L.nbv + qi), (unsigned long long)st.nbv);
+      if (L.nleaf) atomicAdd((unsigned long long*)(L.nleaf + qi), (unsigned long long)st.nleaf);
+      if (L.nrecheck) atomicAdd((unsigned long long*)(L.nrecheck + qi), (unsigned long long)st.nrecheck);
+    }
+  }
+  sink.flush();
+}
+
+// total[i] = own[i] + sum of the totals of its children (children are in a later
+// round, whose totals are already known when rounds are processed last to first).
+__global__ void k_item_totals(const CollideLaunch L, long long lo, long long hi, long long* total) {
+  const long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  long long t = L.own[i];
+  const int c = L.child_count[i];
+  if (c > 0) {
+    const long long s = L.child_start[i];
+    for (int j = 0; j < c; ++j) t += total[s + j];
+  }
+  total[i] = t;
+}
+
+__global__ void k_item_counts(const CollideLaunch L, const long long* total, int32_t* capped,
+                              unsigned long long* ncapped) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.n) return;
+  const long long t = total[q];
+  const long long m = L.num_max_contacts;
+  L.counts[q] = (int32_t)(t < m ? t : m);
+  if (t >= m && L.child_count[q] > 0 && capped) {
+    const unsigned long long k = atomicAdd(ncapped, 1ull);
+    capped[k] = (int32_t)q;
+  }
+}
+
+// rel_start of the children of round items [lo, hi): the position of the child's
+// first contact inside its query's DFS-order contact list.
+__global__ void k_item_starts(const CollideLaunch L, long long lo, long long hi, const long long* total,
+                              long long* rel_start) {
+  const long long i = lo + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hi) return;
+  if (i < L.n) rel_start[i] = 0;
+  const int c = L.child_count[i];
+  if (c <= 0) return;
+  long long run = rel_start[i] + L.own[i];
+  const long long s = L.child_start[i];
+  for (int j = 0; j < c; ++j) {
+    rel_start[s + j] = run;
+    run += total[s + j];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scatter_items(const CollideLaunch L, long long nrec,
+                                                       const long long* rel_start, const long long* offsets,
+                                                       int32_t* contacts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nrec; i += stride) {
+    const int4 r = L.records[i];
+    if (r.x < 0) continue;
+    const long long item = r.x;
+    const long long q = item < L.n ? item : (long long)L.items[item].x;
+    const long long pos = rel_start[item] + r.y;
+    if (pos >= L.num_max_contacts) continue;
+    reinterpret_cast<int2*>(contacts)[offsets[q] + pos] = make_int2(r.z, r.w);
+  }
+}
+
+struct NullSink {
+  FCLG_HD void push(int, int, int, int) {}
+};
+
+template <int PREC, int STACK>
+__global__ void __launch_bounds__(128) k_collide_stats(const CollideLaunch L, const int32_t* list, long long nlist) {
+  NullSink sink;
+  for (;;) {
+    const long long k = (long long)atomicAdd(&L.ctr->work, 1ull);
+    if (k >= nlist) break;
+    const long long qi = list[k];
+    QueryStats st;
+    collide_query<PREC, STACK>(L, qi, sink, st);
+    if (L.nbv) L.nbv[qi] = st.nbv;
+    if (L.nleaf) L.nleaf[qi] = st.nleaf;
+    if (L.nrecheck) L.nrecheck[qi] = st.nrecheck;
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // Exclusive scan of int32 counts into int64 offsets (three passes over 4096-tiles).
 // ---------------------------------------------------------------------------------
 constexpr int kScanBlock = 1024;
@@ -216,6 +370,97 @@ cudaError_t launch_scatter_contacts(const int4* records, int64_t nrec, const int
                                                       contacts);
   ++g_kernel_launches;
   return cudaGetLastError();
+}
+
+cudaError_t launch_collide_round(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
+                                 cudaStream_t s) {
+  ++g_kernel_launches;
+  if (precision == 0) {
+    if (stack_entries <= 64)
+      k_collide_round<0, 64><<<grid, block, 0, s>>>(L);
+    else
+      k_collide_round<0, 256><<<grid, block, 0, s>>>(L);
+  } else {
+    if (stack_entries <= 64)
+      k_collide_round<1, 64><<<grid, block, 0, s>>>(L);
+    else
+      k_collide_round<1, 256><<<grid, block, 0, s>>>(L);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_item_totals(const CollideLaunch& L, int64_t lo, int64_t hi, int64_t* total, cudaStream_t s) {
+  if (hi <= lo) return cudaSuccess;
+  const long long nb = (hi - lo + 255) / 256;
+  k_item_totals<<<(unsigned)nb, 256, 0, s>>>(L, lo, hi, reinterpret_cast<long long*>(total));
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_item_counts(const CollideLaunch& L, const int64_t* total, int32_t* capped, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  const long long nb = (L.n + 255) / 256;
+  k_item_counts<<<(unsigned)nb, 256, 0, s>>>(L, reinterpret_cast<const long long*>(total), capped,
+                                             &L.ctr->capped_split);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_item_starts(const CollideLaunch& L, int64_t lo, int64_t hi, const int64_t* total,
+                               int64_t* rel_start, cudaStream_t s) {
+  if (hi <= lo) return cudaSuccess;
+  const long long nb = (hi - lo + 255) / 256;
+  k_item_starts<<<(unsigned)nb, 256, 0, s>>>(L, lo, hi, reinterpret_cast<const long long*>(total),
+                                             reinterpret_cast<long long*>(rel_start));
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_items(const CollideLaunch& L, int64_t nrec, const int64_t* rel_start,
+                                 const int64_t* offsets, int32_t* contacts, cudaStream_t s) {
+  if (nrec <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long blocks = (nrec + 255) / 256;
+  if (blocks > (long long)sms * 8) blocks = (long long)sms * 8;
+  k_scatter_items<<<(unsigned)blocks, 256, 0, s>>>(L, nrec, reinterpret_cast<const long long*>(rel_start),
+                                                   reinterpret_cast<const long long*>(offsets), contacts);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_collide_stats(const CollideLaunch& L, const int32_t* list, int64_t nlist, int precision,
+                                 int stack_entries, cudaStream_t s) {
+  if (nlist <= 0) return cudaSuccess;
+  const int grid = collide_grid(precision, stack_entries, 128);
+  ++g_kernel_launches;
+  if (precision == 0) {
+    if (stack_entries <= 64)
+      k_collide_stats<0, 64><<<grid, 128, 0, s>>>(L, list, nlist);
+    else
+      k_collide_stats<0, 256><<<grid, 128, 0, s>>>(L, list, nlist);
+  } else {
+    if (stack_entries <= 64)
+      k_collide_stats<1, 64><<<grid, 128, 0, s>>>(L, list, nlist);
+    else
+      k_collide_stats<1, 256><<<grid, 128, 0, s>>>(L, list, nlist);
+  }
+  return cudaGetLastError();
+}
+
+int collide_round_grid(int precision, int stack_entries, int block) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const void* k;
+  if (precision == 0)
+    k = stack_entries <= 64 ? (const void*)k_collide_round<0, 64> : (const void*)k_collide_round<0, 256>;
+  else
+    k = stack_entries <= 64 ? (const void*)k_collide_round<1, 64> : (const void*)k_collide_round<1, 256>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
 }
 
 int collide_grid(int precision, int stack_entries, int block) {

@@ -31,7 +31,7 @@ class MeshInfo(C.Structure):
 
 class CollideRequest(C.Structure):
     _fields_ = [("num_max_contacts", C.c_int32), ("precision", C.c_int32), ("enable_statistics", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("budget", C.c_int32)]
 
 
 class CollideResult(C.Structure):

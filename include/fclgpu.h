@@ -96,7 +96,8 @@ typedef struct {
   int32_t num_max_contacts;   /* CollisionRequest::num_max_contacts (collision_request.h:58) */
   int32_t precision;          /* FCLGPU_PLAIN_FP64 or FCLGPU_FP32_RECHECK */
   int32_t enable_statistics;  /* fill num_bv_tests / num_leaf_tests */
-  int32_t reserved;
+  int32_t budget;             /* BV tests per work item per round before its frontier is
+                                 re-queued (work splitting); 0 = library default */
 } fclgpu_collide_request;
 
 /* Outputs of a collide batch.  counts[n] (int32) always.  Contacts (b1,b2 triangle

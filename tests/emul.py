@@ -45,3 +45,22 @@ def collide(prec, a, b, tf2, maxc, tf1=None):
                             C.c_int64(cap), _p(nbv), _p(nl), _p(nrc))
     assert 0 <= tot <= cap
     return counts, out[:tot], nbv, nl, nrc
+
+
+def collide_split(prec, a, b, tf2, maxc, budget, tf1=None):
+    n = tf2.shape[0]
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(n, 12)
+    counts = np.zeros(n, np.int32)
+    cap = 1 << 22
+    out = np.empty((cap, 2), np.int32)
+    nbv = np.zeros(n, np.int64); nl = np.zeros(n, np.int64); ni = C.c_int64()
+    av, at = [np.ascontiguousarray(x) for x in a]
+    bv, bt = [np.ascontiguousarray(x) for x in b]
+    lib().emu_collide_split.restype = C.c_int64
+    tot = lib().emu_collide_split(C.c_int(prec), _p(av), C.c_int64(av.shape[0]), _p(at), C.c_int64(at.shape[0]),
+                                  _p(bv), C.c_int64(bv.shape[0]), _p(bt), C.c_int64(bt.shape[0]), C.c_int64(n),
+                                  None if tf1a is None else _p(tf1a), _p(tf2), C.c_int(maxc), C.c_int64(budget),
+                                  _p(counts), _p(out), C.c_int64(cap), _p(nbv), _p(nl), C.byref(ni))
+    assert 0 <= tot <= cap
+    return counts, out[:tot], nbv, nl, ni.value

@@ -52,9 +52,110 @@ struct VecSink {
   }
 };
 
+// Host stand-in for the device split sink: contacts are (item, rank, b1, b2).
+struct SplitHostSink {
+  std::vector<int4>* rec;
+  std::vector<int4>* items;
+  std::vector<int>* cstart;
+  std::vector<int>* ccount;
+  bool dumped;
+  void push(int item, int rank, int b1, int b2) { rec->push_back(make_int4(item, rank, b1, b2)); }
+  void dump(long long item, long long qi, int2 cur, const int2* stk, int sp) {
+    const int b = (int)items->size();
+    items->push_back(make_int4((int)qi, cur.x, cur.y, 0));
+    for (int j = 0; j < sp; ++j) items->push_back(make_int4((int)qi, stk[sp - 1 - j].x, stk[sp - 1 - j].y, 0));
+    (*cstart)[item] = b;
+    (*ccount)[item] = 1 + sp;
+    dumped = true;
+  }
+};
+
 }  // namespace
 
 extern "C" {
+
+// Work-splitting batch on the host: same rounds, frontier dumps and item-tree
+// assembly as the GPU path (budget = BV tests per item per round).
+int64_t emu_collide_split(int prec, const double* v1, int64_t nv1, const int32_t* t1, int64_t nt1, const double* v2,
+                          int64_t nv2, const int32_t* t2, int64_t nt2, int64_t n, const double* tf1,
+                          const double* tf2, int maxc, int64_t budget, int32_t* counts, int32_t* out, int64_t cap,
+                          int64_t* nbv, int64_t* nleaf, int64_t* nitems_out) {
+  HostMesh A, B;
+  make_mesh(v1, nv1, t1, nt1, A);
+  make_mesh(v2, nv2, t2, nt2, B);
+  DevMesh tab[2] = {A.view, B.view};
+  int2 pair = make_int2(0, 1);
+  CollideLaunch L{};
+  L.meshes = tab;
+  L.pairs = &pair;
+  L.tf1 = tf1;
+  L.tf2 = tf2;
+  L.n = n;
+  L.num_max_contacts = maxc;
+  std::vector<int4> rec, items((size_t)n);
+  for (int64_t q = 0; q < n; ++q) items[q] = make_int4((int)q, 0, 0, 0);
+  std::vector<int> own, cstart, ccount;
+  std::vector<std::pair<int64_t, int64_t>> rounds;
+  for (int64_t q = 0; q < n; ++q) nbv[q] = nleaf[q] = 0;
+  int64_t lo = 0, hi = n;
+  while (hi > lo) {
+    rounds.emplace_back(lo, hi);
+    own.resize(items.size() + 70 * (hi - lo));
+    cstart.resize(own.size());
+    ccount.resize(own.size());
+    for (int64_t it = lo; it < hi; ++it) {
+      const int4 w = items[it];
+      SplitHostSink sink{&rec, &items, &cstart, &ccount, false};
+      QueryStats st;
+      int k = prec == 0 ? collide_item<0, 256>(L, w.x, w.y, w.z, it, budget, maxc, sink, st)
+                        : collide_item<1, 256>(L, w.x, w.y, w.z, it, budget, maxc, sink, st);
+      if (st.status) return -1;
+      own[it] = k;
+      if (!sink.dumped) ccount[it] = 0;
+      nbv[w.x] += st.nbv;
+      nleaf[w.x] += st.nleaf;
+      own.resize(std::max(own.size(), items.size() + 70));
+      cstart.resize(own.size());
+      ccount.resize(own.size());
+    }
+    lo = hi;
+    hi = (int64_t)items.size();
+  }
+  const int64_t ni = (int64_t)items.size();
+  std::vector<int64_t> total(ni), rel(ni, 0);
+  for (size_t r = rounds.size(); r-- > 0;)
+    for (int64_t i = rounds[r].first; i < rounds[r].second; ++i) {
+      int64_t t = own[i];
+      for (int j = 0; j < ccount[i]; ++j) t += total[cstart[i] + j];
+      total[i] = t;
+    }
+  std::vector<int64_t> off(n + 1, 0);
+  for (int64_t q = 0; q < n; ++q) {
+    counts[q] = (int32_t)std::min<int64_t>(total[q], maxc);
+    off[q + 1] = off[q] + counts[q];
+  }
+  for (size_t r = 0; r < rounds.size(); ++r)
+    for (int64_t i = rounds[r].first; i < rounds[r].second; ++i) {
+      int64_t run = rel[i] + own[i];
+      for (int j = 0; j < ccount[i]; ++j) {
+        rel[cstart[i] + j] = run;
+        run += total[cstart[i] + j];
+      }
+    }
+  const int64_t tot = off[n];
+  for (const int4& r : rec) {
+    const int64_t q = items[r.x].x;
+    const int64_t pos = rel[r.x] + r.y;
+    if (pos >= maxc) continue;
+    const int64_t o = off[q] + pos;
+    if (o < cap) {
+      out[2 * o] = r.z;
+      out[2 * o + 1] = r.w;
+    }
+  }
+  *nitems_out = ni;
+  return tot;
+}
 
 int emu_build(const double* v, int64_t nv, const int32_t* t, int64_t nt, double* nodes30, int32_t* fc,
               int32_t* max_depth) {

@@ -66,3 +66,21 @@ def test_traversal_with_tf1_small_triangles():
         ec, ect, enbv, enl, enrc = emul.collide(1, A, B, tf2, 100000, tf1=tf1)
         assert np.array_equal(oc, ec) and np.array_equal(oct_, ect)
         assert np.array_equal(onbv, enbv) and np.array_equal(onl, enl)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("budget", [3, 64, 1000])
+def test_work_splitting_rebuilds_dfs_order(prec, budget):
+    """Budgeted items + frontier re-queueing + item-tree assembly give the reference's
+    contact list (same pairs, same DFS order) for any budget; statistics are equal
+    whenever the num_max_contacts cap is not what stopped the traversal."""
+    w = W.config0(n_poses=200, seed=8)
+    a = O.Mesh(*w.meshes[0]); b = O.Mesh(*w.meshes[1])
+    for maxc in (1, 7, 100000):
+        oc, oct_, onbv, onl = O.collide_batch(a, b, w.tf2, num_max_contacts=maxc, nthreads=4)
+        c, ct, nbv, nl, _ = emul.collide_split(prec, w.meshes[0], w.meshes[1], w.tf2, maxc, budget)
+        assert np.array_equal(c, oc)
+        assert np.array_equal(ct, oct_)
+        uncapped = oc < maxc
+        assert np.array_equal(nbv[uncapped], onbv[uncapped])
+        assert np.array_equal(nl[uncapped], onl[uncapped])
