@@ -159,3 +159,50 @@ def test_distance_reference_fixture(gpu_lib, golden):
     env = O.Mesh(golden["env_v"], golden["env_t"]); rob = O.Mesh(golden["rob_v"], golden["rob_t"])
     for i in range(golden["tf"].shape[0]):
         assert out["min_distance"][i] == O.brute_distance(env, rob, golden["tf"][i])
+
+
+def _dist_check(out, d, pts):
+    got = out["min_distance"]
+    err = np.abs(got - d)
+    tol = np.maximum(REL * np.abs(d), ABS)
+    assert np.all(err <= tol), f"max rel err {np.max(err / np.maximum(np.abs(d), ABS))}"
+    pos = d > 0
+    if pos.any():
+        perr = np.abs(out["nearest_points"][pos] - pts[pos]).max(axis=(1, 2))
+        scale = np.maximum(np.abs(pts[pos]).max(axis=(1, 2)), 1.0)
+        assert np.all(perr <= REL * scale + ABS)
+
+
+def test_distance_fp32_config0(gpu_lib):
+    w = W.config0(n_poses=1500, seed=3)
+    ms = _meshes(w)
+    out = api.distance_batch(ms, w.pairs, None, w.tf2, nearest_points=True, precision="fp32", statistics=True)
+    a = O.Mesh(*w.meshes[0]); b = O.Mesh(*w.meshes[1])
+    d, ids, pts, _, _ = O.distance_batch(a, b, w.tf2, nearest=True, nthreads=8)
+    _dist_check(out, d, pts)
+
+
+def test_distance_fp32_separated_multi_pair_with_margins(gpu_lib):
+    w = W.config2(total_poses=3000, n_pairs=6, tri_hi=30000, seed=4)
+    ms = _meshes(w)
+    out = api.distance_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, nearest_points=True,
+                             precision="fp32", margins=w.margin, statistics=True)
+    om = [O.Mesh(v, t) for v, t in w.meshes]
+    d = np.empty(w.n); pts = np.empty((w.n, 2, 3))
+    for p in range(w.pairs.shape[0]):
+        idx = np.nonzero(w.pair == p)[0]
+        dd, _, pp, _, _ = O.distance_batch(om[w.pairs[p, 0]], om[w.pairs[p, 1]], w.tf2[idx], nearest=True, nthreads=8)
+        d[idx] = dd; pts[idx] = pp
+    _dist_check(out, d, pts)
+    assert np.array_equal(out["within_margin"].astype(bool), d <= w.margin)
+
+
+def test_distance_fp32_tf1_and_fixture(gpu_lib, golden):
+    ms = [api.BVHModel.from_arrays(golden["env_v"], golden["env_t"]),
+          api.BVHModel.from_arrays(golden["rob_v"], golden["rob_t"])]
+    tf = golden["tf"]
+    tf1 = W.random_poses(tf.shape[0], -100, 100, 5)
+    out = api.distance_batch(ms, [[0, 1]], tf1, tf, nearest_points=True, precision="fp32")
+    env = O.Mesh(golden["env_v"], golden["env_t"]); rob = O.Mesh(golden["rob_v"], golden["rob_t"])
+    d, ids, pts, _, _ = O.distance_batch(env, rob, tf, tf1=tf1, nearest=True)
+    _dist_check(out, d, pts)
