@@ -382,3 +382,80 @@ def distance_batch(meshes, pairs, tf1, tf2, pair_of_query=None, nearest_points=T
     if statistics:
         out["num_bv_tests"], out["num_leaf_tests"], out["num_rechecks"] = st
     return out
+
+
+# ---------------------------------------------------------------------------------
+# Convex shapes (fcl::Box, Sphere, Capsule, Cylinder, Cone, Convex) with FCL's own
+# GJK/EPA solver (GJKSolver_indep) and its closed-form pairs.
+# ---------------------------------------------------------------------------------
+class ShapeSet:
+    """A device-resident set of convex shapes.  types/params/voff/vcnt/verts follow
+    fcl_gb300.workloads.ShapeSet (params: box sides; sphere r; capsule/cylinder/cone
+    r, lz; convex vertices [voff, voff+vcnt) of verts)."""
+
+    def __init__(self, types, params, voff=None, vcnt=None, verts=None):
+        types = np.ascontiguousarray(types, np.int32)
+        n = types.shape[0]
+        params = np.ascontiguousarray(params, np.float64).reshape(n, 3)
+        voff = np.zeros(n, np.int32) if voff is None else np.asarray(voff, np.int32)
+        vcnt = np.zeros(n, np.int32) if vcnt is None else np.asarray(vcnt, np.int32)
+        verts = np.zeros((0, 3)) if verts is None else np.ascontiguousarray(verts, np.float64).reshape(-1, 3)
+        arr = (N.Shape * n)()
+        for i in range(n):
+            arr[i].type = int(types[i])
+            arr[i].vertex_offset = int(voff[i])
+            arr[i].vertex_count = int(vcnt[i])
+            for k in range(3):
+                arr[i].params[k] = float(params[i, k])
+        self._verts = verts if verts.shape[0] else np.zeros((1, 3))
+        h = C.c_void_p()
+        N.check(N.lib().fclgpu_shapeset_create(arr, n, self._verts.ctypes.data, verts.shape[0], C.byref(h)),
+                "fclgpu_shapeset_create")
+        self.handle = h
+        self.n = n
+
+    @classmethod
+    def from_workload(cls, s) -> "ShapeSet":
+        return cls(s.type, s.params, s.voff, s.vcnt, s.verts)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.fclgpu_shapeset_destroy(h)
+            self.handle = None
+
+
+def shape_batch(shapes: ShapeSet, ia, ib, tf1, tf2, stream=None):
+    """Batched fcl::collide (with contact) then, for separated pairs, fcl::distance.
+    numpy inputs use the host entry point, torch CUDA tensors the device one."""
+    if _is_torch(tf2):
+        import torch
+        dev = tf2.device
+        n = tf2.shape[0]
+        out = dict(hit=torch.zeros(n, dtype=torch.int32, device=dev),
+                   normal=torch.zeros((n, 3), dtype=torch.float64, device=dev),
+                   point=torch.zeros((n, 3), dtype=torch.float64, device=dev),
+                   depth=torch.zeros(n, dtype=torch.float64, device=dev),
+                   dist=torch.zeros(n, dtype=torch.float64, device=dev),
+                   p1=torch.zeros((n, 3), dtype=torch.float64, device=dev),
+                   p2=torch.zeros((n, 3), dtype=torch.float64, device=dev),
+                   status=torch.zeros((n, 2), dtype=torch.int32, device=dev))
+        res = N.ShapeResult(*(out[k].data_ptr() for k in ("hit", "normal", "point", "depth", "dist", "p1", "p2",
+                                                           "status")))
+        s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        N.check(N.lib().fclgpu_shape_batch_device(shapes.handle, n, ia.data_ptr(), ib.data_ptr(), tf1.data_ptr(),
+                                                  tf2.data_ptr(), C.byref(res), s), "fclgpu_shape_batch_device")
+        return out
+    ia = np.ascontiguousarray(ia, np.int32)
+    ib = np.ascontiguousarray(ib, np.int32)
+    n = ia.shape[0]
+    tf1 = np.ascontiguousarray(tf1, np.float64).reshape(n, 12)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)
+    out = dict(hit=np.zeros(n, np.int32), normal=np.zeros((n, 3)), point=np.zeros((n, 3)), depth=np.zeros(n),
+               dist=np.zeros(n), p1=np.zeros((n, 3)), p2=np.zeros((n, 3)), status=np.zeros((n, 2), np.int32))
+    res = N.ShapeResult(*(out[k].ctypes.data for k in ("hit", "normal", "point", "depth", "dist", "p1", "p2",
+                                                       "status")))
+    N.check(N.lib().fclgpu_shape_batch(shapes.handle, n, ia.ctypes.data, ib.ctypes.data, tf1.ctypes.data,
+                                       tf2.ctypes.data, C.byref(res), stream), "fclgpu_shape_batch")
+    out["hit"] = out["hit"].astype(bool)
+    return out

@@ -1,0 +1,195 @@
+// C ABI for convex shape sets and batched shape-pair queries (include/fclgpu.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fclgpu.h"
+#include "shapes.h"
+
+using namespace fclgpu;
+
+struct fclgpu_shapeset_s {
+  DevShape* shapes = nullptr;
+  double* verts = nullptr;
+  int32_t n = 0;
+  int64_t nv = 0;
+};
+
+namespace {
+
+std::mutex g_mu;
+thread_local std::string g_err;
+
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+    if (e == cudaSuccess) cap = std::max<size_t>(bytes, 256);
+    return e;
+  }
+};
+Buf g_ctr, g_ia, g_ib, g_tf1, g_tf2, g_hit, g_nrm, g_pt, g_dep, g_dist, g_p1, g_p2, g_st;
+cudaEvent_t g_ev[2] = {nullptr, nullptr};
+
+int cfail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
+}
+#define CKS(expr, where)                          \
+  do {                                            \
+    cudaError_t e_ = (expr);                      \
+    if (e_ != cudaSuccess) return cfail(e_, where); \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* verts, int64_t nv,
+                           fclgpu_shapeset* out) {
+  if (!out || n <= 0 || !shapes || (nv > 0 && !verts)) return FCLGPU_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::vector<DevShape> h(n);
+  for (int i = 0; i < n; ++i) {
+    const fclgpu_shape& s = shapes[i];
+    if (s.type < FCLGPU_SHAPE_BOX || s.type > FCLGPU_SHAPE_CONVEX) return FCLGPU_ERR_INVALID_ARGUMENT;
+    if (s.type == FCLGPU_SHAPE_CONVEX &&
+        (s.vertex_count <= 0 || s.vertex_offset < 0 || s.vertex_offset + (int64_t)s.vertex_count > nv))
+      return FCLGPU_ERR_INVALID_ARGUMENT;
+    h[i].type = s.type;
+    h[i].voff = s.vertex_offset;
+    h[i].vcnt = s.vertex_count;
+    h[i].pad = 0;
+    for (int k = 0; k < 3; ++k) h[i].p[k] = s.params[k];
+  }
+  fclgpu_shapeset_s* ss = new fclgpu_shapeset_s();
+  cudaError_t e = cudaMalloc(&ss->shapes, sizeof(DevShape) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(ss->shapes, h.data(), sizeof(DevShape) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&ss->verts, sizeof(double) * 3 * std::max<int64_t>(nv, 1));
+  if (e == cudaSuccess && nv > 0) e = cudaMemcpy(ss->verts, verts, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (ss->shapes) cudaFree(ss->shapes);
+    if (ss->verts) cudaFree(ss->verts);
+    delete ss;
+    return cfail(e, "shapeset upload");
+  }
+  ss->n = n;
+  ss->nv = nv;
+  *out = ss;
+  return FCLGPU_OK;
+}
+
+int fclgpu_shapeset_destroy(fclgpu_shapeset s) {
+  if (!s) return FCLGPU_OK;
+  cudaFree(s->shapes);
+  cudaFree(s->verts);
+  delete s;
+  return FCLGPU_OK;
+}
+
+int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
+                              const double* tf1, const double* tf2, fclgpu_shape_result* res, void* stream) {
+  if (!set || !res || n < 0 || (n > 0 && (!ia || !ib || !tf1 || !tf2 || !res->hit || !res->distance)))
+    return FCLGPU_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FCLGPU_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  CKS(g_ctr.ensure(sizeof(BatchCounters)), "counters");
+  CKS(cudaMemsetAsync(g_ctr.p, 0, sizeof(BatchCounters), s), "counters");
+  // optional outputs default to scratch
+  const size_t nn = (size_t)n;
+  CKS(g_nrm.ensure(24 * nn), "scratch");
+  CKS(g_pt.ensure(24 * nn), "scratch");
+  CKS(g_dep.ensure(8 * nn), "scratch");
+  CKS(g_p1.ensure(24 * nn), "scratch");
+  CKS(g_p2.ensure(24 * nn), "scratch");
+  ShapeLaunch L;
+  L.shapes = set->shapes;
+  L.verts = set->verts;
+  L.ia = ia;
+  L.ib = ib;
+  L.tf1 = tf1;
+  L.tf2 = tf2;
+  L.n = n;
+  L.ctr = (BatchCounters*)g_ctr.p;
+  L.hit = res->hit;
+  L.normal = res->normal ? res->normal : (double*)g_nrm.p;
+  L.point = res->point ? res->point : (double*)g_pt.p;
+  L.depth = res->depth ? res->depth : (double*)g_dep.p;
+  L.dist = res->distance;
+  L.p1 = res->p1 ? res->p1 : (double*)g_p1.p;
+  L.p2 = res->p2 ? res->p2 : (double*)g_p2.p;
+  L.status = res->status;
+  if (!g_ev[0]) {
+    CKS(cudaEventCreate(&g_ev[0]), "event");
+    CKS(cudaEventCreate(&g_ev[1]), "event");
+  }
+  const int block = 128;
+  CKS(cudaEventRecord(g_ev[0], s), "event");
+  CKS(launch_shape_batch(L, shape_grid(block), block, s), "shape kernel");
+  CKS(cudaEventRecord(g_ev[1], s), "event");
+  CKS(cudaStreamSynchronize(s), "shape kernel");
+  float ms = 0.f;
+  CKS(cudaEventElapsedTime(&ms, g_ev[0], g_ev[1]), "event");
+  g_last_shape_ms = ms;
+  return FCLGPU_OK;
+}
+
+int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib, const double* tf1,
+                       const double* tf2, fclgpu_shape_result* res, void* stream) {
+  if (!set || !res || n < 0 || (n > 0 && (!ia || !ib || !tf1 || !tf2 || !res->hit || !res->distance)))
+    return FCLGPU_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FCLGPU_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nn = (size_t)n;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    CKS(g_ia.ensure(4 * nn), "inputs");
+    CKS(g_ib.ensure(4 * nn), "inputs");
+    CKS(g_tf1.ensure(96 * nn), "inputs");
+    CKS(g_tf2.ensure(96 * nn), "inputs");
+    CKS(g_hit.ensure(4 * nn), "outputs");
+    CKS(g_dist.ensure(8 * nn), "outputs");
+    CKS(g_st.ensure(8 * nn), "outputs");
+    CKS(cudaMemcpyAsync(g_ia.p, ia, 4 * nn, cudaMemcpyHostToDevice, s), "h2d");
+    CKS(cudaMemcpyAsync(g_ib.p, ib, 4 * nn, cudaMemcpyHostToDevice, s), "h2d");
+    CKS(cudaMemcpyAsync(g_tf1.p, tf1, 96 * nn, cudaMemcpyHostToDevice, s), "h2d");
+    CKS(cudaMemcpyAsync(g_tf2.p, tf2, 96 * nn, cudaMemcpyHostToDevice, s), "h2d");
+  }
+  fclgpu_shape_result d{};
+  d.hit = (int32_t*)g_hit.p;
+  d.distance = (double*)g_dist.p;
+  d.status = res->status ? (int32_t*)g_st.p : nullptr;
+  // optional per-pair vectors land in scratch owned by the device entry point
+  int rc = fclgpu_shape_batch_device(set, n, (const int32_t*)g_ia.p, (const int32_t*)g_ib.p,
+                                     (const double*)g_tf1.p, (const double*)g_tf2.p, &d, stream);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_mu);
+  CKS(cudaMemcpyAsync(res->hit, g_hit.p, 4 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  CKS(cudaMemcpyAsync(res->distance, g_dist.p, 8 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->normal) CKS(cudaMemcpyAsync(res->normal, g_nrm.p, 24 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->point) CKS(cudaMemcpyAsync(res->point, g_pt.p, 24 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->depth) CKS(cudaMemcpyAsync(res->depth, g_dep.p, 8 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->p1) CKS(cudaMemcpyAsync(res->p1, g_p1.p, 24 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->p2) CKS(cudaMemcpyAsync(res->p2, g_p2.p, 24 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  if (res->status) CKS(cudaMemcpyAsync(res->status, g_st.p, 8 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  CKS(cudaStreamSynchronize(s), "shape batch");
+  return FCLGPU_OK;
+}
+
+int fclgpu_last_shape_kernel_time(double* ms) {
+  if (!ms) return FCLGPU_ERR_INVALID_ARGUMENT;
+  *ms = fclgpu::g_last_shape_ms;
+  return FCLGPU_OK;
+}
+
+}  // extern "C"

@@ -100,5 +100,6 @@ int collide_grid(int precision, int stack_entries, int block);
 int distance_grid(int precision, int stack_entries, int block);
 
 extern int64_t g_kernel_launches;
+extern double g_last_shape_ms;
 
 }  // namespace fclgpu

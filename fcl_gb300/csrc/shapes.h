@@ -1,0 +1,30 @@
+// Launch interface of the convex shape-pair batch.
+#pragma once
+#include "gjk_epa.cuh"
+#include "kernels.h"
+
+namespace fclgpu {
+
+struct ShapeLaunch {
+  const DevShape* shapes;
+  const double* verts;   // convex vertex pool
+  const int32_t* ia;
+  const int32_t* ib;
+  const double* tf1;
+  const double* tf2;
+  int64_t n;
+  BatchCounters* ctr;
+  int32_t* hit;
+  double* normal;
+  double* point;
+  double* depth;
+  double* dist;
+  double* p1;
+  double* p2;
+  int32_t* status;
+};
+
+cudaError_t launch_shape_batch(const ShapeLaunch& L, int grid, int block, cudaStream_t s);
+int shape_grid(int block);
+
+}  // namespace fclgpu

@@ -73,7 +73,22 @@ _SIGS = {
                                         C.POINTER(DistanceRequest), C.POINTER(DistanceResult), _VP]),
     "fclgpu_kernel_launch_count": (C.c_int64, []),
     "fclgpu_last_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
+    "fclgpu_shapeset_create": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, C.POINTER(C.c_void_p)]),
+    "fclgpu_shapeset_destroy": (C.c_int, [_VP]),
+    "fclgpu_shape_batch_device": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "fclgpu_shape_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "fclgpu_last_shape_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
 }
+
+
+class Shape(C.Structure):
+    _fields_ = [("type", C.c_int32), ("vertex_offset", C.c_int32), ("vertex_count", C.c_int32),
+                ("reserved", C.c_int32), ("params", C.c_double * 3)]
+
+
+class ShapeResult(C.Structure):
+    _fields_ = [("hit", C.c_void_p), ("normal", C.c_void_p), ("point", C.c_void_p), ("depth", C.c_void_p),
+                ("distance", C.c_void_p), ("p1", C.c_void_p), ("p2", C.c_void_p), ("status", C.c_void_p)]
 
 
 def exported_symbols() -> list[str]:

@@ -200,3 +200,83 @@ def subsample(w: MeshPairWorkload, n: int, seed: int = 0) -> MeshPairWorkload:
     return MeshPairWorkload(meshes=w.meshes, pairs=w.pairs, pair=w.pair[idx], tf2=w.tf2[idx],
                             tf1=None if w.tf1 is None else w.tf1[idx],
                             margin=None if w.margin is None else w.margin[idx], name=w.name + "_sub")
+
+
+# ---------------------------------------------------------------------------------
+# Convex shape pairs (GJK/EPA batch)
+# ---------------------------------------------------------------------------------
+BOX, SPHERE, CAPSULE, CYLINDER, CONE, CONVEX = 0, 1, 2, 3, 4, 5
+
+
+@dataclass
+class ShapeSet:
+    """Shapes as arrays: type[n], params[n,3] (box sides; sphere r; capsule/cylinder/
+    cone r, lz), convex vertex ranges voff/vcnt into verts[m,3]."""
+    type: np.ndarray
+    params: np.ndarray
+    voff: np.ndarray
+    vcnt: np.ndarray
+    verts: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.type.shape[0])
+
+
+def random_shapes(n: int, seed: int) -> ShapeSet:
+    """Box sides U[0.1,1]; Sphere r U[0.05,0.5]; Capsule/Cylinder/Cone r U[0.05,0.3],
+    lz U[0.1,1]; Convex = hull of 32-256 points uniform in the unit ball scaled U[0.2,1]."""
+    from scipy.spatial import ConvexHull
+    rng = np.random.default_rng(seed)
+    typ = rng.integers(0, 6, size=n).astype(np.int32)
+    params = np.zeros((n, 3))
+    voff = np.zeros(n, np.int32)
+    vcnt = np.zeros(n, np.int32)
+    verts = []
+    off = 0
+    for i in range(n):
+        t = typ[i]
+        if t == BOX:
+            params[i] = rng.uniform(0.1, 1.0, 3)
+        elif t == SPHERE:
+            params[i, 0] = rng.uniform(0.05, 0.5)
+        elif t in (CAPSULE, CYLINDER, CONE):
+            params[i, 0] = rng.uniform(0.05, 0.3)
+            params[i, 1] = rng.uniform(0.1, 1.0)
+        else:
+            m = int(rng.integers(32, 257))
+            d = rng.normal(size=(m, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            pts = d * rng.uniform(0, 1, size=(m, 1)) ** (1.0 / 3.0) * rng.uniform(0.2, 1.0)
+            hv = pts[np.sort(ConvexHull(pts).vertices)]
+            voff[i] = off
+            vcnt[i] = hv.shape[0]
+            off += hv.shape[0]
+            verts.append(hv)
+    V = np.concatenate(verts) if verts else np.zeros((0, 3))
+    return ShapeSet(typ, params, voff, vcnt, np.ascontiguousarray(V))
+
+
+@dataclass
+class ShapePairWorkload:
+    shapes: ShapeSet
+    ia: np.ndarray
+    ib: np.ndarray
+    tf1: np.ndarray
+    tf2: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.ia.shape[0])
+
+
+def config3(n_pairs: int = 4_000_000, n_shapes: int = 4096, seed: int = 3) -> ShapePairWorkload:
+    """Convex GJK/EPA batch: pairs of random shapes, both posed by a Haar rotation and
+    a translation in [-1,1]^3."""
+    shapes = random_shapes(n_shapes, seed)
+    rng = np.random.default_rng(seed + 1)
+    ia = rng.integers(0, n_shapes, size=n_pairs).astype(np.int32)
+    ib = rng.integers(0, n_shapes, size=n_pairs).astype(np.int32)
+    tf1 = random_poses(n_pairs, -1.0, 1.0, seed + 2)
+    tf2 = random_poses(n_pairs, -1.0, 1.0, seed + 3)
+    return ShapePairWorkload(shapes, ia, ib, tf1, tf2)

@@ -168,6 +168,59 @@ FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
  * most recent collide or distance batch.  No counterpart in FCL (profiling hook). */
 FCLGPU_API int fclgpu_last_kernel_time(double* ms);
 
+/* ---- convex shapes (fcl::Box/Sphere/Capsule/Cylinder/Cone/Convex, geometry/shape/*.h) --
+ * GJK/EPA of FCL's own solver (GJKSolver_indep, narrowphase/detail/gjk_solver_indep.h)
+ * with its closed-form pairs; replaces fcl::collide / fcl::distance on shape pairs
+ * (collision_func_matrix-inl.h:278-311, distance_func_matrix-inl.h:207-226). */
+enum {
+  FCLGPU_SHAPE_BOX = 0,       /* params: side x, y, z */
+  FCLGPU_SHAPE_SPHERE = 1,    /* params: radius */
+  FCLGPU_SHAPE_CAPSULE = 2,   /* params: radius, lz */
+  FCLGPU_SHAPE_CYLINDER = 3,  /* params: radius, lz */
+  FCLGPU_SHAPE_CONE = 4,      /* params: radius, lz */
+  FCLGPU_SHAPE_CONVEX = 5     /* vertices [vertex_offset, +vertex_count) of the pool */
+};
+
+typedef struct {
+  int32_t type;
+  int32_t vertex_offset;
+  int32_t vertex_count;
+  int32_t reserved;
+  double params[3];
+} fclgpu_shape;
+
+typedef struct fclgpu_shapeset_s* fclgpu_shapeset;
+
+/* Uploads n shapes and the convex vertex pool (nv vertices, 3 doubles each). */
+FCLGPU_API int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* verts, int64_t nv,
+                                      fclgpu_shapeset* out);
+FCLGPU_API int fclgpu_shapeset_destroy(fclgpu_shapeset set);
+
+/* Per pair i (shapes ia[i], ib[i] at tf1[i], tf2[i]): hit = fcl::collide with contact;
+ * when hit, normal / point / depth are the contact (depth is FCL's ContactPoint
+ * penetration_depth: positive for closed forms, -epa.depth for GJK/EPA); when not hit,
+ * distance and the world-frame witness points p1, p2 are fcl::distance's (-1 if the
+ * solver failed).  status[2i] = GJK status, status[2i+1] = EPA status (-1 = not run).
+ * hit and distance are required; other outputs may be NULL. */
+typedef struct {
+  int32_t* hit;
+  double* normal;
+  double* point;
+  double* depth;
+  double* distance;
+  double* p1;
+  double* p2;
+  int32_t* status;
+} fclgpu_shape_result;
+
+FCLGPU_API int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
+                                         const double* tf1, const double* tf2, fclgpu_shape_result* res,
+                                         void* stream);
+FCLGPU_API int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
+                                  const double* tf1, const double* tf2, fclgpu_shape_result* res, void* stream);
+/* Device time (ms) of the most recent shape-pair kernel.  No counterpart in FCL. */
+FCLGPU_API int fclgpu_last_shape_kernel_time(double* ms);
+
 #ifdef __cplusplus
 }
 #endif

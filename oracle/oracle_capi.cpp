@@ -292,3 +292,60 @@ int orc_hardware_threads() {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Convex shape pairs (GJKSolver_indep semantics, see oracle_gjk.cpp)
+// ---------------------------------------------------------------------------------
+#include "oracle_gjk.h"
+
+extern "C" {
+
+// Shapes: type[ns], params[3*ns], voff[ns], vcnt[ns] into verts[3*nv] (convex only).
+// Queries: ia[n], ib[n], tf1[12n], tf2[12n].  Outputs: hit[n], normal[3n], point[3n],
+// depth[n], dist[n], p1[3n], p2[3n], status[2n] (gjk, epa).
+void orc_shape_batch(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                     const double* verts, int64_t n, const int* ia, const int* ib, const double* tf1,
+                     const double* tf2, int nthreads, int* hit, double* normal, double* point, double* depth,
+                     double* dist, double* p1, double* p2, int* status) {
+  std::vector<V3> vv;
+  int nv = 0;
+  for (int i = 0; i < ns; ++i) nv = std::max(nv, voff[i] + vcnt[i]);
+  vv.resize(nv);
+  for (int i = 0; i < nv; ++i) vv[i] = mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+  std::vector<Shape> sh(ns);
+  for (int i = 0; i < ns; ++i) {
+    sh[i].type = type[i];
+    for (int k = 0; k < 3; ++k) sh[i].p[k] = params[3 * i + k];
+    sh[i].verts = vv.data() + voff[i];
+    sh[i].nverts = vcnt[i];
+  }
+  parallel_for(n, nthreads, [&](int64_t q, int) {
+    ShapeResult r;
+    shape_pair(sh[ia[q]], load_tf(tf1 + 12 * q), sh[ib[q]], load_tf(tf2 + 12 * q), r);
+    hit[q] = r.collide ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+      normal[3 * q + k] = r.normal[k];
+      point[3 * q + k] = r.point[k];
+      p1[3 * q + k] = r.p1[k];
+      p2[3 * q + k] = r.p2[k];
+    }
+    depth[q] = r.depth;
+    dist[q] = r.distance;
+    status[2 * q] = r.gjk_status;
+    status[2 * q + 1] = r.epa_status;
+  });
+}
+
+// Origin projections (math/detail/project-inl.h:183-306) for the known-answer tests.
+// k = 2, 3 or 4 points (3k doubles); out: encode, sqr_distance, parameterization[4].
+void orc_project_origin(int k, const double* pts, int* encode, double* out5) {
+  V3 v[4];
+  for (int i = 0; i < k; ++i) v[i] = mk(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+  ProjectResult r = k == 2 ? project_line(v[0], v[1]) : (k == 3 ? project_triangle(v[0], v[1], v[2])
+                                                                : project_tetra(v[0], v[1], v[2], v[3]));
+  *encode = (int)r.encode;
+  out5[0] = r.sqr_distance;
+  for (int i = 0; i < 4; ++i) out5[1 + i] = r.parameterization[i];
+}
+
+}  // extern "C"

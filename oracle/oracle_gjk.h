@@ -1,0 +1,50 @@
+// FP64 CPU oracle for convex shape pairs: FCL's own GJK/EPA (GST_INDEP solver) and
+// the closed-form pairs its dispatch prefers.  TEST INFRASTRUCTURE ONLY.
+#pragma once
+#include <vector>
+
+#include "oracle_math.h"
+
+namespace oracle {
+
+// geometry/shape/*.h (Box side, Sphere radius, Capsule/Cylinder/Cone radius + lz,
+// Convex vertex list)
+enum ShapeType { SH_BOX = 0, SH_SPHERE = 1, SH_CAPSULE = 2, SH_CYLINDER = 3, SH_CONE = 4, SH_CONVEX = 5 };
+
+struct Shape {
+  int type;
+  double p[3];             // box: side[3]; sphere: radius; capsule/cylinder/cone: radius, lz
+  const V3* verts = nullptr;  // convex
+  int nverts = 0;
+};
+
+struct ShapeResult {
+  bool collide;
+  V3 normal, point;  // contact (only when collide)
+  double depth;      // penetration depth (>= 0) when collide
+  double distance;   // when not colliding (GJK / closed form), -1 when that failed
+  V3 p1, p2;         // world-frame witness points when not colliding
+  int gjk_status, epa_status;
+};
+
+// fcl::collide + fcl::distance for one convex pair with GJKSolver_indep.
+void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
+
+// Pure GJK/EPA without closed-form dispatch (used to check the device solver).
+bool gjk_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, V3* normal, V3* point,
+                   double* depth, int* gjk_status, int* epa_status);
+bool gjk_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, double* dist, V3* p1, V3* p2,
+                  int* gjk_status);
+
+// Simplex projections (math/detail/project-inl.h:183-320), exposed for the
+// known-answer tests of test_fcl_simple.cpp.
+struct ProjectResult {
+  double parameterization[4] = {0, 0, 0, 0};
+  double sqr_distance = -1;
+  unsigned encode = 0;
+};
+ProjectResult project_line(const V3& a, const V3& b);
+ProjectResult project_triangle(const V3& a, const V3& b, const V3& c);
+ProjectResult project_tetra(const V3& a, const V3& b, const V3& c, const V3& d);
+
+}  // namespace oracle

@@ -194,3 +194,41 @@ def brute_distance(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None =
     tf2 = np.ascontiguousarray(tf2, np.float64).reshape(12)
     tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(12)
     return float(lib().orc_brute_distance(m1.h, m2.h, None if tf1a is None else _d(tf1a), _d(tf2)))
+
+
+def shape_batch(shapes, ia, ib, tf1, tf2, nthreads: int = 1):
+    """GJKSolver_indep collide (+ EPA contact) and, for separated pairs, distance.
+    Returns dict: hit, normal, point, depth, dist, p1, p2, status (n,2)."""
+    L = lib()
+    if not hasattr(L, "_shape_sig"):
+        L.orc_shape_batch.argtypes = [C.c_int, _ip, _dp, _ip, _ip, _dp, C.c_int64, _ip, _ip, _dp, _dp, C.c_int,
+                                      _ip, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+        L._shape_sig = True
+    t = np.ascontiguousarray(shapes.type, np.int32)
+    pr = np.ascontiguousarray(shapes.params, np.float64)
+    vo = np.ascontiguousarray(shapes.voff, np.int32)
+    vc = np.ascontiguousarray(shapes.vcnt, np.int32)
+    vv = np.ascontiguousarray(shapes.verts, np.float64).reshape(-1, 3)
+    if vv.shape[0] == 0:
+        vv = np.zeros((1, 3))
+    ia = np.ascontiguousarray(ia, np.int32); ib = np.ascontiguousarray(ib, np.int32)
+    n = ia.shape[0]
+    tf1 = np.ascontiguousarray(tf1, np.float64).reshape(n, 12)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)
+    out = dict(hit=np.zeros(n, np.int32), normal=np.zeros((n, 3)), point=np.zeros((n, 3)), depth=np.zeros(n),
+               dist=np.zeros(n), p1=np.zeros((n, 3)), p2=np.zeros((n, 3)), status=np.zeros((n, 2), np.int32))
+    L.orc_shape_batch(t.shape[0], _i(t), _d(pr), _i(vo), _i(vc), _d(vv), n, _i(ia), _i(ib), _d(tf1), _d(tf2),
+                      nthreads, _i(out["hit"]), _d(out["normal"]), _d(out["point"]), _d(out["depth"]),
+                      _d(out["dist"]), _d(out["p1"]), _d(out["p2"]), _i(out["status"]))
+    out["hit"] = out["hit"].astype(bool)
+    return out
+
+
+def project_origin(pts):
+    L = lib()
+    L.orc_project_origin.argtypes = [C.c_int, _dp, _ip, _dp]
+    pts = np.ascontiguousarray(pts, np.float64)
+    enc = C.c_int()
+    out = np.zeros(5)
+    L.orc_project_origin(pts.shape[0], _d(pts), C.byref(enc), _d(out))
+    return enc.value, out[0], out[1:]
