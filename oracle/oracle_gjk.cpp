@@ -16,7 +16,7 @@ inline V3 normalized(const V3& v) {
   double n = norm(v);
   return mk(v[0] / n, v[1] / n, v[2] / n);
 }
-const double kTol = std::pow(std::numeric_limits<double>::epsilon(), 7.0 / 8.0);  // constants.h:145-148
+const double kTol = 2.0097183471152322e-14;  // std::pow(eps, 7/8) = 2^-45.5 (math/constants.h:164-167)
 
 // narrowphase/detail/convexity_based_algorithm/minkowski_diff-inl.h:65-206
 V3 get_support(const Shape& s, const V3& dir) {

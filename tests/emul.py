@@ -64,3 +64,24 @@ def collide_split(prec, a, b, tf2, maxc, budget, tf1=None):
                                   _p(counts), _p(out), C.c_int64(cap), _p(nbv), _p(nl), C.byref(ni))
     assert 0 <= tot <= cap
     return counts, out[:tot], nbv, nl, ni.value
+
+
+def shape_batch(shapes, ia, ib, tf1, tf2):
+    t = np.ascontiguousarray(shapes.type, np.int32)
+    pr = np.ascontiguousarray(shapes.params, np.float64)
+    vo = np.ascontiguousarray(shapes.voff, np.int32)
+    vc = np.ascontiguousarray(shapes.vcnt, np.int32)
+    vv = np.ascontiguousarray(shapes.verts, np.float64).reshape(-1, 3)
+    if vv.shape[0] == 0:
+        vv = np.zeros((1, 3))
+    ia = np.ascontiguousarray(ia, np.int32); ib = np.ascontiguousarray(ib, np.int32)
+    n = ia.shape[0]
+    tf1 = np.ascontiguousarray(tf1, np.float64).reshape(n, 12)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)
+    out = dict(hit=np.zeros(n, np.int32), normal=np.zeros((n, 3)), point=np.zeros((n, 3)), depth=np.zeros(n),
+               dist=np.zeros(n), p1=np.zeros((n, 3)), p2=np.zeros((n, 3)), status=np.zeros((n, 2), np.int32))
+    lib().emu_shape_batch(C.c_int(t.shape[0]), _p(t), _p(pr), _p(vo), _p(vc), _p(vv), C.c_int64(n), _p(ia), _p(ib),
+                          _p(tf1), _p(tf2), *(_p(out[k]) for k in ("hit", "normal", "point", "depth", "dist", "p1",
+                                                                    "p2", "status")))
+    out["hit"] = out["hit"].astype(bool)
+    return out

@@ -6,6 +6,7 @@
 
 #include "bvh_build.h"
 #include "collide_traverse.cuh"
+#include "shape_pair.cuh"
 
 using namespace fclgpu;
 
@@ -215,6 +216,41 @@ int64_t emu_collide(int prec, const double* v1, int64_t nv1, const int32_t* t1, 
   const int64_t total = (int64_t)all.size() / 2;
   for (int64_t i = 0; i < std::min(total, cap) * 2; ++i) out[i] = all[i];
   return total;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Host run of the device shape-pair query (shape_pair.cuh) over n pairs.
+void emu_shape_batch(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                     const double* verts, int64_t n, const int* ia, const int* ib, const double* tf1,
+                     const double* tf2, int* hit, double* normal, double* point, double* depth, double* dist,
+                     double* p1, double* p2, int* status) {
+  std::vector<DevShape> sh(ns);
+  for (int i = 0; i < ns; ++i) {
+    sh[i].type = type[i];
+    sh[i].voff = voff[i];
+    sh[i].vcnt = vcnt[i];
+    sh[i].pad = 0;
+    for (int k = 0; k < 3; ++k) sh[i].p[k] = params[3 * i + k];
+  }
+  for (int64_t q = 0; q < n; ++q) {
+    PairOut o;
+    shape_pair_query(sh[ia[q]], sh[ib[q]], verts, tf1 + 12 * q, tf2 + 12 * q, o);
+    hit[q] = o.hit;
+    const D3v* v[4] = {&o.normal, &o.point, &o.p1, &o.p2};
+    double* d[4] = {normal, point, p1, p2};
+    for (int k = 0; k < 4; ++k) {
+      d[k][3 * q] = v[k]->x;
+      d[k][3 * q + 1] = v[k]->y;
+      d[k][3 * q + 2] = v[k]->z;
+    }
+    depth[q] = o.depth;
+    dist[q] = o.dist;
+    status[2 * q] = o.gstat;
+    status[2 * q + 1] = o.estat;
+  }
 }
 
 }  // extern "C"

@@ -88,3 +88,10 @@ def test_random_batch_consistency():
     # separated pairs: witness distance equals the reported distance
     d = np.linalg.norm(r["p1"][sep][ok] - r["p2"][sep][ok], axis=1)
     assert np.allclose(d, r["dist"][sep][ok], rtol=1e-6, atol=1e-9)
+
+
+def test_gjk_tolerance_constant():
+    # FCL's gjk_default_tolerance = std::pow(eps, 7/8) (math/constants.h:145-167);
+    # the oracle and the device code use this literal
+    import math
+    assert math.pow(np.finfo(np.float64).eps, 7.0 / 8.0) == 2.0097183471152322e-14
