@@ -12,11 +12,12 @@
 // The FP32 form (PREC 1) traverses with FP32 RSS distances widened by a slack
 // (2^-12 relative + 64u times the coordinate scale) as pruning lower bounds, and FP32
 // triangle distances (points taken relative to the first vertex, offset in
-// float-float) as intervals [d - E, d + E].  Every leaf whose interval can still
-// hold the minimum is kept as a candidate; at the end each candidate is re-evaluated
-// with the exact FP64 triangle distance in visit order with the strict "<" update,
-// so the reported distance, triangle ids and witness points are the FP64 values of
-// the winning pair.  A query whose candidate list overflows is re-run in FP64.
+// float-float) with a slack E = 2^-18 d + 128u times the pair's coordinate scale.  A
+// leaf whose FP32 interval can still reach the best distance so far -- and every
+// leaf near contact, where triDistance switches branches -- is re-evaluated at once
+// with the exact FP64 triangle distance and the strict "<" update, in visit order,
+// so the reported distance, triangle ids and witness points are FP64 values of the
+// winning pair, and the pruning bound is the exact best.
 #include "filter32.cuh"
 #include "geom.cuh"
 #include "kernels.h"
@@ -24,8 +25,6 @@
 namespace fclgpu {
 
 namespace {
-
-constexpr int kCand = 16;
 
 struct DStack {
   int b1, b2;
@@ -249,11 +248,6 @@ __device__ __forceinline__ float rss_distance_f32(const QueryF32& q, const DevMe
                              v3(r2a.x, r2a.y, r2a.z), l2, r2a.w);
 }
 
-struct Cand {
-  int p1, p2;
-  float lb;
-};
-
 template <int STACK>
 __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, int prec) {
   for (;;) {
@@ -276,21 +270,29 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
       const float u = FCLG_U32;
       const float tau = fmaxf(fabsf(qf.T[0]), fmaxf(fabsf(qf.T[1]), fabsf(qf.T[2])));
       const float rss_abs = 64.f * u * (float)(A.rmax + B.rmax) + 64.f * u * 1.7321f * tau;
-      const float rel = 2.44140625e-4f;  // 2^-12
-      Cand cand[kCand];
-      int nc = 0;
-      bool overflow = false;
-      float best_up = 3.0e38f;
+      const float rel = 3.814697265625e-6f;  // 2^-18 of the distance
       long long nbv = 0, nleaf = 0, nrc64 = 0;
+      // exact FP64 best so far (strict "<" in visit order, as DistanceResult::update);
+      // best_up is a float upper bound of it used for pruning
+      o.d = 1.7976931348623157e308;
+      o.id1 = o.id2 = 0;
+      o.P = o.Q = v3(0.0, 0.0, 0.0);
+      float best_up = 3.0e38f;
+      auto exact_leaf = [&](int p1, int p2) {
+        V3<double> P, Q;
+        const double d64 = leaf_distance64(A, B, p1, p2, R, T, P, Q);
+        ++nrc64;
+        if (o.d > d64) {
+          o.d = d64;
+          o.id1 = p1;
+          o.id2 = p2;
+          o.P = P;
+          o.Q = Q;
+          best_up = (float)d64 * (1.f + 2.f * u) + 1e-37f;
+        }
+      };
       // preprocess pair (triangle 0, triangle 0)
-      {
-        float sc;
-        const float d = tri_distance_f32(qf, reinterpret_cast<const float4*>(A.tri32),
-                                         reinterpret_cast<const float4*>(B.tri32), sc);
-        const float E = rel * d + 128.f * u * sc + qf.dabs * 2.f;
-        cand[nc++] = Cand{0, 0, d - E};
-        best_up = d + E;
-      }
+      exact_leaf(0, 0);
       FStack stk[STACK];
       int sp = 0;
       int b1 = 0, b2 = 0;
@@ -303,33 +305,13 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
           ++nleaf;
           const int p1 = -(c1 + 1), p2 = -(c2 + 1);
           float sc;
-          float d = tri_distance_f32(qf, reinterpret_cast<const float4*>(A.tri32) + 3 * (long long)p1,
-                                     reinterpret_cast<const float4*>(B.tri32) + 3 * (long long)p2, sc);
-          float E = rel * d + 128.f * u * sc + qf.dabs * 2.f;
-          if (d <= 3.90625e-3f * sc) {
-            // near contact triDistance switches between its edge/face and overlap
-            // branches; take the exact FP64 value for this pair
-            V3<double> P, Q;
-            const double d64 = leaf_distance64(A, B, p1, p2, R, T, P, Q);
-            ++nrc64;
-            d = (float)d64;
-            E = 4.f * u * d + 1e-30f;
-          }
-          const float lo = d - E, hi = d + E;
-          if (lo <= best_up) {
-            if (hi < best_up) {
-              best_up = hi;
-              // drop candidates that can no longer hold the minimum
-              int k = 0;
-              for (int j = 0; j < nc; ++j)
-                if (cand[j].lb <= best_up) cand[k++] = cand[j];
-              nc = k;
-            }
-            if (nc < kCand)
-              cand[nc++] = Cand{p1, p2, lo};
-            else
-              overflow = true;
-          }
+          const float d = tri_distance_f32(qf, reinterpret_cast<const float4*>(A.tri32) + 3 * (long long)p1,
+                                           reinterpret_cast<const float4*>(B.tri32) + 3 * (long long)p2, sc);
+          const float E = rel * d + 128.f * u * sc + qf.dabs * 2.f;
+          // near contact triDistance switches between its edge/face and overlap
+          // branches, so such pairs always take the exact value; otherwise only a
+          // pair whose FP32 interval can still reach the best is re-evaluated
+          if (d <= 3.90625e-3f * sc || d - E <= best_up) exact_leaf(p1, p2);
         } else {
           int a1, a2, e1, e2;
           if (first_over_second(A, B, b1, b2, l1, l2)) {
@@ -339,8 +321,8 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
           }
           float d1 = rss_distance_f32(qf, A, B, a1, a2);
           float d2 = rss_distance_f32(qf, A, B, e1, e2);
-          d1 = d1 - (rel * d1 + rss_abs);
-          d2 = d2 - (rel * d2 + rss_abs);
+          d1 = d1 - (2.44140625e-4f * d1 + rss_abs);
+          d2 = d2 - (2.44140625e-4f * d2 + rss_abs);
           nbv += 2;
           if (sp >= STACK) {
             atomicOr(&L.ctr->status, DEV_ERR_STACK);
@@ -374,30 +356,10 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
         }
         if (!found) break;
       }
-      if (overflow) {
-        exact = true;  // re-run this query in FP64
-      } else {
-        // FP64 finish over the candidates in visit order, strict "<"
-        o.d = 1.7976931348623157e308;
-        o.id1 = o.id2 = 0;
-        o.P = o.Q = v3(0.0, 0.0, 0.0);
-        for (int j = 0; j < nc; ++j) {
-          if (cand[j].lb > best_up) continue;
-          V3<double> P, Q;
-          const double d = leaf_distance64(A, B, cand[j].p1, cand[j].p2, R, T, P, Q);
-          if (o.d > d) {
-            o.d = d;
-            o.id1 = cand[j].p1;
-            o.id2 = cand[j].p2;
-            o.P = P;
-            o.Q = Q;
-          }
-        }
-        o.nbv = nbv;
-        o.nleaf = nleaf;
-        o.nrc = nrc64;
-        o.status = 0;
-      }
+      o.nbv = nbv;
+      o.nleaf = nleaf;
+      o.nrc = nrc64;
+      o.status = 0;
     }
     if (exact) {
       distance_query_fp64<STACK>(A, B, R, T, o);
