@@ -17,11 +17,7 @@
 
 using namespace fclgpu;
 
-struct fclgpu_mesh_s {
-  DevMesh dev;
-  fclgpu_mesh_info info;
-  std::vector<void*> allocations;
-};
+#include "mesh_handle.h"
 
 namespace {
 

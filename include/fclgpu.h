@@ -162,6 +162,21 @@ FCLGPU_API int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_mesh
                                      const double* tf2, const fclgpu_distance_request* req,
                                      fclgpu_distance_result* res, void* stream);
 
+/* Same query and outputs as fclgpu_distance_batch_device (device pointers), but the
+ * call allocates no memory: for callers that cannot allocate GPU memory at query time
+ * (deadline-bound control loops, processes whose HBM is owned by another allocator,
+ * work issued during stream capture).  Its scratch is a fixed array inside the
+ * library, shared by all calls: at most 64 meshes and 256 pairs per call (larger
+ * requests return FCLGPU_ERR_INVALID_ARGUMENT), and calls that overlap on the GPU
+ * race, so serialise them.  The first call on a device looks the array up and should
+ * come before any stream capture.  No counterpart in FCL. */
+FCLGPU_API int fclgpu_distance_batch_noalloc(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                             const int32_t* pairs_host, int32_t num_pairs,
+                                             int64_t n, const int32_t* pair_of_query,
+                                             const double* tf1, const double* tf2,
+                                             const fclgpu_distance_request* req,
+                                             fclgpu_distance_result* res, void* stream);
+
 /* Number of this library's kernel launches issued since load (for launch accounting). */
 FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
 /* Device time (ms, CUDA events on the batch's stream) of the traversal kernel of the
