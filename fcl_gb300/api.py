@@ -459,3 +459,128 @@ def shape_batch(shapes: ShapeSet, ia, ib, tf1, tf2, stream=None):
                                        tf2.ctypes.data, C.byref(res), stream), "fclgpu_shape_batch")
     out["hit"] = out["hit"].astype(bool)
     return out
+
+
+# ------------------------------------------------------------------ broadphase ----
+
+class DynamicAABBTreeCollisionManager:
+    """Device broadphase in the place of FCL's DynamicAABBTreeCollisionManager
+    (broadphase/broadphase_dynamic_AABB_tree.h:56-157).
+
+    Geometry comes from a registry, as CollisionObject's shared geometry does: a
+    ShapeSet and a list of BVHModels.  Scene and query objects are geometry refs
+    (n, 2) int32 rows (kind, index) -- kind 0 = shape set entry, 1 = mesh -- with
+    3x4 poses.  registerObjects + setup build the device tree; update() takes new
+    poses.  collide_batch / distance_batch run manager.collide(obj, ...,
+    DefaultCollisionFunction) and manager.distance(obj, ..., DefaultDistanceFunction)
+    for every query object (torch CUDA tensors stay on the device, numpy arrays go
+    through the host entry points)."""
+
+    def __init__(self, shapes: "ShapeSet | None" = None, meshes=()):
+        self.shapes = shapes
+        self.meshes = list(meshes)
+        self.handle = None
+        self._refs = None
+        self._tf = None
+
+    def registerObjects(self, refs, tf) -> None:
+        self._refs = np.ascontiguousarray(refs, np.int32).reshape(-1, 2)
+        self._tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+        self.setup()
+
+    def setup(self) -> None:
+        self._release()
+        n = self._refs.shape[0]
+        hs = (C.c_void_p * max(1, len(self.meshes)))(*[m.handle.value for m in self.meshes])
+        h = C.c_void_p()
+        N.check(N.lib().fclgpu_broadphase_create(self.shapes.handle if self.shapes is not None else None,
+                                                 hs if self.meshes else None, len(self.meshes),
+                                                 self._refs.ctypes.data, n, self._tf.ctypes.data, C.byref(h)),
+                "fclgpu_broadphase_create")
+        self.handle = h
+
+    def size(self) -> int:
+        return 0 if self._refs is None else int(self._refs.shape[0])
+
+    def update(self, tf, stream=None) -> None:
+        """New poses of every scene object (numpy on the host or a CUDA tensor)."""
+        if _is_torch(tf):
+            N.check(N.lib().fclgpu_broadphase_update(self.handle, tf.data_ptr(), 1, stream), "fclgpu_broadphase_update")
+            return
+        self._tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+        N.check(N.lib().fclgpu_broadphase_update(self.handle, self._tf.ctypes.data, 0, stream),
+                "fclgpu_broadphase_update")
+
+    def getAABBs(self) -> np.ndarray:
+        out = np.zeros((self.size(), 6))
+        N.check(N.lib().fclgpu_broadphase_get_aabbs(self.handle, out.ctypes.data), "fclgpu_broadphase_get_aabbs")
+        return out
+
+    def collide_batch(self, refs, tf, num_max_contacts: int = 1, precision: str = "fp32", stream=None):
+        req = N.BpCollideRequest(num_max_contacts, _prec(precision), 0)
+        if _is_torch(tf):
+            import torch
+            dev = tf.device
+            n = tf.shape[0]
+            out = dict(num_contacts=torch.empty(n, dtype=torch.int64, device=dev),
+                       num_objects=torch.empty(n, dtype=torch.int32, device=dev),
+                       first_object=torch.empty(n, dtype=torch.int32, device=dev))
+            res = N.BpCollideResult(out["num_contacts"].data_ptr(), out["num_objects"].data_ptr(),
+                                    out["first_object"].data_ptr(), 0, 0)
+            s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+            N.check(N.lib().fclgpu_broadphase_collide_device(self.handle, refs.data_ptr(), n, tf.data_ptr(),
+                                                             C.byref(req), C.byref(res), s),
+                    "fclgpu_broadphase_collide_device")
+        else:
+            refs = np.ascontiguousarray(refs, np.int32).reshape(-1, 2)
+            tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+            n = refs.shape[0]
+            out = dict(num_contacts=np.zeros(n, np.int64), num_objects=np.zeros(n, np.int32),
+                       first_object=np.zeros(n, np.int32))
+            res = N.BpCollideResult(out["num_contacts"].ctypes.data, out["num_objects"].ctypes.data,
+                                    out["first_object"].ctypes.data, 0, 0)
+            N.check(N.lib().fclgpu_broadphase_collide(self.handle, refs.ctypes.data, n, tf.ctypes.data, C.byref(req),
+                                                      C.byref(res), stream), "fclgpu_broadphase_collide")
+        out["total_candidates"] = res.total_candidates
+        out["node_visits"] = res.total_node_visits
+        return out
+
+    def distance_batch(self, refs, tf, nearest_points: bool = True, precision: str = "fp32", stream=None):
+        req = N.BpDistanceRequest(int(nearest_points), _prec(precision))
+        if _is_torch(tf):
+            import torch
+            dev = tf.device
+            n = tf.shape[0]
+            out = dict(min_distance=torch.empty(n, dtype=torch.float64, device=dev),
+                       object=torch.empty(n, dtype=torch.int32, device=dev),
+                       ids=torch.empty((n, 2), dtype=torch.int32, device=dev),
+                       nearest_points=torch.zeros((n, 2, 3), dtype=torch.float64, device=dev))
+            res = N.BpDistanceResult(out["min_distance"].data_ptr(), out["object"].data_ptr(), out["ids"].data_ptr(),
+                                     out["nearest_points"].data_ptr(), 0, 0)
+            s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+            N.check(N.lib().fclgpu_broadphase_distance_device(self.handle, refs.data_ptr(), n, tf.data_ptr(),
+                                                              C.byref(req), C.byref(res), s),
+                    "fclgpu_broadphase_distance_device")
+        else:
+            refs = np.ascontiguousarray(refs, np.int32).reshape(-1, 2)
+            tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+            n = refs.shape[0]
+            out = dict(min_distance=np.zeros(n), object=np.zeros(n, np.int32), ids=np.zeros((n, 2), np.int32),
+                       nearest_points=np.zeros((n, 2, 3)))
+            res = N.BpDistanceResult(out["min_distance"].ctypes.data, out["object"].ctypes.data,
+                                     out["ids"].ctypes.data, out["nearest_points"].ctypes.data, 0, 0)
+            N.check(N.lib().fclgpu_broadphase_distance(self.handle, refs.ctypes.data, n, tf.ctypes.data,
+                                                       C.byref(req), C.byref(res), stream),
+                    "fclgpu_broadphase_distance")
+        out["total_candidates"] = res.total_candidates
+        out["node_visits"] = res.total_node_visits
+        return out
+
+    def _release(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.fclgpu_broadphase_destroy(h)
+        self.handle = None
+
+    def __del__(self):
+        self._release()

@@ -1,0 +1,128 @@
+// Device broadphase: a linear BVH (LBVH) over scene-object AABBs, rebuilt on the
+// device from Morton codes, queried per query object; plus the record types the
+// C ABI layer (capi_broadphase.cu) hands to the kernels (broadphase.cu).
+//
+// The tree replaces FCL's DynamicAABBTreeCollisionManager tree
+// (broadphase/broadphase_dynamic_AABB_tree-inl.h, broadphase/detail/hierarchy_tree-inl.h).
+// Its structure differs from FCL's (Morton order instead of median splits), so every
+// result it returns is one that does not depend on traversal order: candidate sets,
+// contact totals, collision booleans and minimum distances.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fclgpu_types.h"
+#include "gjk_epa.cuh"
+
+namespace fclgpu {
+
+enum : int32_t { GEOM_SHAPE = 0, GEOM_MESH = 1 };
+
+// One geometry of the registry the scene and the queries draw from: its kind, index
+// (into the shape set or the mesh table) and CollisionGeometry::aabb_local /
+// aabb_center / aabb_radius (geometry/collision_geometry.h:104-113).
+struct GeomRec {
+  int32_t kind;
+  int32_t index;
+  int32_t pad[2];
+  double lo[3], hi[3];
+  double center[3];
+  double radius;
+  double ref[3];  // a point of the geometry (mesh: its first vertex) for distance upper bounds
+};
+
+// LBVH internal node: both children's FP32 boxes (rounded outward from the FP64
+// object AABBs) and their indices; child >= 0 is an internal node, child < 0 is the
+// leaf of scene object ~child.  64 bytes, loaded as four float4.
+struct __align__(16) BpNode {
+  float lo0[3];
+  int32_t c0;
+  float hi0[3];
+  int32_t c1;
+  float lo1[3];
+  int32_t pad0;
+  float hi1[3];
+  int32_t pad1;
+};
+
+struct BpSceneView {
+  const GeomRec* geoms;
+  const DevShape* shapes;
+  const double* sverts;
+  const DevMesh* meshes;
+  int32_t n;         // scene objects
+  int32_t root;      // node index, or ~object when n == 1
+  const int32_t* gid;
+  const double* tf;      // 12 per object
+  const double* aabb64;  // 6 per object (min, max), FCL's CollisionObject::getAABB()
+  const BpNode* nodes;
+};
+
+// ---------------------------------------------------------------- build ----
+// World AABBs (CollisionObject::computeAABB, collision_object-inl.h:116-131) of n
+// objects, FP64 (6 per object) and rounded outward to FP32 (6 per object).
+cudaError_t launch_world_aabbs(const GeomRec* geoms, int64_t n, const int32_t* gid, const double* tf,
+                               double* aabb64, float* aabb32, cudaStream_t s);
+// LBVH over n >= 2 leaves.  scratch holds at least bp_build_scratch_bytes(n) bytes.
+size_t bp_build_scratch_bytes(int64_t n);
+cudaError_t launch_lbvh_build(int32_t n, const float* aabb32, BpNode* nodes, void* scratch, cudaStream_t s);
+
+// ---------------------------------------------------------------- queries ----
+struct BpQueryView {
+  int64_t nq;
+  const int32_t* gid;   // geometry id per query
+  const double* tf;     // 12 per query
+  const double* aabb64; // 6 per query
+  const float* aabb32;  // 6 per query
+};
+
+enum : uint32_t { BP_ERR_STACK = 1u, BP_ERR_REF = 2u };
+
+// Geometry refs (kind, index) of nq queries -> registry ids (shapes first, then meshes);
+// an out-of-range ref sets BP_ERR_REF.
+cudaError_t launch_bp_query_gids(const int2* refs, int64_t nq, int32_t ns, int32_t nm, int32_t* gid,
+                                 unsigned* status, cudaStream_t s);
+
+// Candidate pass: scene objects whose FP64 AABB overlaps the query's (exactly the
+// pairs FCL's collisionRecurse hands to its callback).  counts_only: write counts[q];
+// else write (query, object) pairs at offsets[q].
+cudaError_t launch_bp_overlap(const BpSceneView& S, const BpQueryView& Q, int32_t* counts, const int64_t* offsets,
+                              int2* pairs, int64_t* node_visits, unsigned* status, cudaStream_t s);
+// Distance upper bound per query: min over visited objects of |p_obj - p_query| for
+// one point of each geometry, visiting nearest-first with pruning by the FP32 lower
+// bound.  Then the candidate pass: objects whose FP64 AABB distance is below it.
+cudaError_t launch_bp_dist_bound(const BpSceneView& S, const BpQueryView& Q, double* ub, unsigned* status,
+                                 cudaStream_t s);
+cudaError_t launch_bp_dist_candidates(const BpSceneView& S, const BpQueryView& Q, const double* ub, int32_t* counts,
+                                      const int64_t* offsets, int2* pairs, int64_t* node_visits, unsigned* status,
+                                      cudaStream_t s);
+
+// Narrowphase of candidate pairs.  kind[i] = 0 shape-shape, 1 mesh-mesh, 2 mixed.
+cudaError_t launch_bp_classify(const BpSceneView& S, const BpQueryView& Q, const int2* pairs, int64_t n,
+                               int32_t* kind, cudaStream_t s);
+// Shape-shape pairs (kind 0) in place: collide -> hit[i]; distance -> dist/points.
+cudaError_t launch_bp_shape_narrow(const BpSceneView& S, const BpQueryView& Q, const int2* pairs, int64_t n,
+                                   const int32_t* kind, int mode, int32_t* hit, double* dist, double* pts,
+                                   cudaStream_t s);
+// Gathers of the mesh-mesh pairs (kind 1): per listed pair, the mesh-pair index
+// (scene mesh * nm + query mesh) and both transforms.
+cudaError_t launch_bp_gather_mesh(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
+                                  const int64_t* list, int64_t nlist, int32_t nm, int32_t* pair_index, double* tf1,
+                                  double* tf2, cudaStream_t s);
+cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, int64_t* list, unsigned long long* count,
+                           cudaStream_t s);
+// Scatter mesh results back to candidate slots.
+cudaError_t launch_bp_scatter_hits(const int64_t* list, int64_t nlist, const int32_t* counts, int32_t* hit,
+                                   cudaStream_t s);
+cudaError_t launch_bp_scatter_dist(const int64_t* list, int64_t nlist, const double* d, const int32_t* ids,
+                                   const double* pts, double* dist, int32_t* b12, double* outpts, cudaStream_t s);
+
+// Per-query reductions over the candidate segments [offsets[q], offsets[q+1]).
+cudaError_t launch_bp_reduce_collide(int64_t nq, const int64_t* offsets, const int2* pairs, const int32_t* hit,
+                                     int64_t max_contacts, int64_t* num_contacts, int32_t* num_objects,
+                                     int32_t* first_object, cudaStream_t s);
+cudaError_t launch_bp_reduce_distance(int64_t nq, const int64_t* offsets, const int2* pairs, const double* dist,
+                                      const int32_t* b12, const double* pts, double* min_distance, int32_t* object,
+                                      int32_t* ids, double* nearest, cudaStream_t s);
+
+}  // namespace fclgpu

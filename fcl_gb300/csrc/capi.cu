@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -18,6 +19,10 @@
 using namespace fclgpu;
 
 #include "mesh_handle.h"
+
+namespace fclgpu {
+void set_error_detail(const std::string& what);
+}
 
 namespace {
 
@@ -273,6 +278,8 @@ int collide_scatter(const int64_t* offsets, int32_t* contacts, cudaStream_t s) {
 
 }  // namespace
 
+void fclgpu::set_error_detail(const std::string& what) { g_detail = what; }
+
 extern "C" {
 
 const char* fclgpu_status_string(int status) {
@@ -371,6 +378,32 @@ int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int
   d.vmax = vmax * (1.0 + 1e-12);
   d.cmax = pk.cmax * (1.0 + 1e-12);
   d.rmax = pk.rmax * (1.0 + 1e-12);
+  {
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::numeric_limits<double>::max();
+      hi[k] = -std::numeric_limits<double>::max();
+    }
+    for (int64_t i = 0; i < nv; ++i)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], verts[3 * i + k]);
+        hi[k] = std::max(hi[k], verts[3 * i + k]);
+      }
+    double c[3], r = 0;
+    for (int k = 0; k < 3; ++k) c[k] = (lo[k] + hi[k]) * 0.5;
+    for (int64_t i = 0; i < nv; ++i) {
+      const double dx = c[0] - verts[3 * i], dy = c[1] - verts[3 * i + 1], dz = c[2] - verts[3 * i + 2];
+      const double q = (dx * dx + dy * dy) + dz * dz;
+      if (q > r) r = q;
+    }
+    for (int k = 0; k < 3; ++k) {
+      m->aabb_local[k] = lo[k];
+      m->aabb_local[3 + k] = hi[k];
+      m->aabb_center[k] = c[k];
+      m->first_vertex[k] = verts[k];
+    }
+    m->aabb_radius = std::sqrt(r);
+  }
   m->info.num_vertices = nv;
   m->info.num_tris = nt;
   m->info.num_nodes = (int64_t)nn;

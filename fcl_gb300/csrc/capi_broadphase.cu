@@ -1,0 +1,574 @@
+// C ABI of the device broadphase (include/fclgpu.h): scene registration and update,
+// batched per-object collide and distance queries with FCL's default callbacks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fclgpu.h"
+#include "broadphase.h"
+#include "kernels.h"
+#include "mesh_handle.h"
+#include "shape_pair.cuh"
+#include "shapeset_handle.h"
+
+using namespace fclgpu;
+
+struct fclgpu_broadphase_s {
+  fclgpu_shapeset shapes = nullptr;
+  std::vector<fclgpu_mesh> meshes;
+  std::vector<int32_t> mesh_pairs;  // nm x nm table, pair p = a * nm + b -> (a, b)
+  int32_t ns = 0, nm = 0, n = 0, root = -1;
+  GeomRec* geoms = nullptr;
+  int32_t* gid = nullptr;
+  double* tf = nullptr;
+  double* aabb64 = nullptr;
+  float* aabb32 = nullptr;
+  BpNode* nodes = nullptr;
+  void* build_scratch = nullptr;
+};
+
+namespace {
+
+std::mutex g_bp_mu;
+
+int bp_fail(int code, const std::string& why) {
+  set_error_detail(why);
+  return code;
+}
+int bp_cuda(cudaError_t e, const char* where) {
+  set_error_detail(std::string(where) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
+}
+#define CKB(expr, where)                            \
+  do {                                              \
+    cudaError_t e_ = (expr);                        \
+    if (e_ != cudaSuccess) return bp_cuda(e_, where); \
+  } while (0)
+#define RCB(expr)         \
+  do {                    \
+    int r_ = (expr);      \
+    if (r_) return r_;    \
+  } while (0)
+
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// query-side scratch (one set, calls are serialised by g_bp_mu)
+struct BpScratch {
+  Buf ctr, qgid, q64, q32, counts, offsets, scan_tmp, ub;
+  Buf pairs, kind, hit, dist, b12, pts, list;
+  Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
+  Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
+};
+BpScratch g_bs;
+
+// device counters block
+struct BpCounters {
+  unsigned status;
+  unsigned pad;
+  unsigned long long list_count;
+  int64_t visits;
+};
+
+// Shape::computeLocalAABB per type, in FCL's operation order (see oracle restatement)
+void shape_record(const DevShape& s, const double* verts, GeomRec& g) {
+  g.kind = GEOM_SHAPE;
+  for (int k = 0; k < 3; ++k) g.ref[k] = 0.0;
+  double d[3];
+  switch (s.type) {
+    case FCLGPU_SHAPE_BOX:  // box-inl.h:80-88: 0.5 * side
+      for (int k = 0; k < 3; ++k) d[k] = 0.5 * s.p[k];
+      break;
+    case FCLGPU_SHAPE_SPHERE:  // sphere-inl.h:62-69
+      d[0] = d[1] = d[2] = s.p[0];
+      break;
+    case FCLGPU_SHAPE_CAPSULE:  // capsule-inl.h:64-72
+      d[0] = d[1] = s.p[0];
+      d[2] = 0.5 * s.p[1] + s.p[0];
+      break;
+    case FCLGPU_SHAPE_CYLINDER:  // cylinder-inl.h:64-72
+    case FCLGPU_SHAPE_CONE:      // cone-inl.h:64-72
+      d[0] = d[1] = s.p[0];
+      d[2] = 0.5 * s.p[1];
+      break;
+    default: {  // convex-inl.h:86-96
+      double lo[3], hi[3];
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::numeric_limits<double>::max();
+        hi[k] = -std::numeric_limits<double>::max();
+      }
+      for (int i = 0; i < s.vcnt; ++i)
+        for (int k = 0; k < 3; ++k) {
+          lo[k] = std::min(lo[k], verts[3 * (s.voff + i) + k]);
+          hi[k] = std::max(hi[k], verts[3 * (s.voff + i) + k]);
+        }
+      double m[3];
+      for (int k = 0; k < 3; ++k) {
+        g.lo[k] = lo[k];
+        g.hi[k] = hi[k];
+        g.center[k] = (lo[k] + hi[k]) * 0.5;
+        m[k] = lo[k] - g.center[k];
+        g.ref[k] = verts[3 * s.voff + k];
+      }
+      g.radius = std::sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]);
+      return;
+    }
+  }
+  double m[3];
+  for (int k = 0; k < 3; ++k) {
+    g.hi[k] = d[k];
+    g.lo[k] = -d[k];
+    g.center[k] = (g.lo[k] + g.hi[k]) * 0.5;
+    m[k] = g.lo[k] - g.center[k];
+  }
+  g.radius = s.type == FCLGPU_SHAPE_SPHERE ? s.p[0] : std::sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]);
+}
+
+BpSceneView scene_view(const fclgpu_broadphase_s* bp) {
+  BpSceneView S;
+  S.geoms = bp->geoms;
+  S.shapes = bp->shapes ? bp->shapes->shapes : nullptr;
+  S.sverts = bp->shapes ? bp->shapes->verts : nullptr;
+  S.meshes = nullptr;
+  S.n = bp->n;
+  S.root = bp->root;
+  S.gid = bp->gid;
+  S.tf = bp->tf;
+  S.aabb64 = bp->aabb64;
+  S.nodes = bp->nodes;
+  return S;
+}
+
+// AABBs + tree for the current poses
+int rebuild(fclgpu_broadphase_s* bp, cudaStream_t s) {
+  if (bp->n == 0) return FCLGPU_OK;
+  CKB(launch_world_aabbs(bp->geoms, bp->n, bp->gid, bp->tf, bp->aabb64, bp->aabb32, s), "world aabbs");
+  if (bp->n >= 2) {
+    CKB(launch_lbvh_build(bp->n, bp->aabb32, bp->nodes, bp->build_scratch, s), "lbvh build");
+    bp->root = 0;
+  } else {
+    bp->root = ~0;
+  }
+  CKB(cudaStreamSynchronize(s), "broadphase build");
+  return FCLGPU_OK;
+}
+
+void free_bp(fclgpu_broadphase_s* bp) {
+  for (void* p : {(void*)bp->geoms, (void*)bp->gid, (void*)bp->tf, (void*)bp->aabb64, (void*)bp->aabb32,
+                  (void*)bp->nodes, bp->build_scratch})
+    if (p) cudaFree(p);
+  delete bp;
+}
+
+// Query preparation: registry ids, world AABBs.
+int prepare_queries(const fclgpu_broadphase_s* bp, const fclgpu_geometry_ref* refs, int64_t nq, const double* tf,
+                    BpQueryView& Q, BpCounters* dctr, cudaStream_t s) {
+  CKB(g_bs.qgid.ensure(4 * nq), "query scratch");
+  CKB(g_bs.q64.ensure(48 * nq), "query scratch");
+  CKB(g_bs.q32.ensure(24 * nq), "query scratch");
+  CKB(launch_bp_query_gids(reinterpret_cast<const int2*>(refs), nq, bp->ns, bp->nm, g_bs.qgid.as<int32_t>(),
+                           &dctr->status, s),
+      "query refs");
+  CKB(launch_world_aabbs(bp->geoms, nq, g_bs.qgid.as<int32_t>(), tf, g_bs.q64.as<double>(), g_bs.q32.as<float>(), s),
+      "query aabbs");
+  Q.nq = nq;
+  Q.gid = g_bs.qgid.as<int32_t>();
+  Q.tf = tf;
+  Q.aabb64 = g_bs.q64.as<double>();
+  Q.aabb32 = g_bs.q32.as<float>();
+  return FCLGPU_OK;
+}
+
+int check_status(const BpCounters& c) {
+  if (c.status & BP_ERR_REF) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "query geometry ref out of range");
+  if (c.status & BP_ERR_STACK) return bp_fail(FCLGPU_ERR_STACK_DEPTH, "broadphase traversal stack overflow");
+  if (c.status) return bp_fail(FCLGPU_ERR_DEVICE_STATUS, "broadphase status word set");
+  return FCLGPU_OK;
+}
+
+// counts -> offsets -> total; returns the total through *total (host sync)
+int scan_counts(int64_t nq, BpCounters* dctr, BpCounters* hctr, int64_t* total, cudaStream_t s) {
+  CKB(g_bs.offsets.ensure(8 * (nq + 1)), "offsets");
+  CKB(g_bs.scan_tmp.ensure(8 * ((nq + 4095) / 4096 + 2)), "scan scratch");
+  CKB(launch_exclusive_scan(g_bs.counts.as<int32_t>(), nq, g_bs.offsets.as<int64_t>(), g_bs.scan_tmp.as<int64_t>(),
+                            s),
+      "scan");
+  CKB(cudaMemcpyAsync(total, g_bs.offsets.as<int64_t>() + nq, 8, cudaMemcpyDeviceToHost, s), "read total");
+  CKB(cudaMemcpyAsync(hctr, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
+  CKB(cudaStreamSynchronize(s), "candidate pass");
+  return check_status(*hctr);
+}
+
+int ensure_pair_buffers(int64_t total) {
+  const size_t t = (size_t)std::max<int64_t>(total, 1);
+  CKB(g_bs.pairs.ensure(8 * t), "pairs");
+  CKB(g_bs.kind.ensure(4 * t), "pairs");
+  CKB(g_bs.list.ensure(8 * t), "pairs");
+  return FCLGPU_OK;
+}
+
+// list of candidates of one kind; returns its length (host sync)
+int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cudaStream_t s) {
+  CKB(cudaMemsetAsync(&dctr->list_count, 0, 8, s), "list");
+  CKB(launch_bp_list(g_bs.kind.as<int32_t>(), total, want, g_bs.list.as<int64_t>(), &dctr->list_count, s), "list");
+  unsigned long long c = 0;
+  CKB(cudaMemcpyAsync(&c, &dctr->list_count, 8, cudaMemcpyDeviceToHost, s), "list");
+  CKB(cudaStreamSynchronize(s), "list");
+  *nlist = (int64_t)c;
+  return FCLGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fclgpu_broadphase_create(fclgpu_shapeset shapes, const fclgpu_mesh* meshes, int32_t num_meshes,
+                             const fclgpu_geometry_ref* objects, int32_t num_objects, const double* tf,
+                             fclgpu_broadphase* out) {
+  if (!out) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (num_meshes < 0 || num_objects < 0 || (num_meshes > 0 && !meshes) || (num_objects > 0 && (!objects || !tf)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "bad broadphase arguments");
+  const int32_t ns = shapes ? shapes->n : 0;
+  for (int32_t i = 0; i < num_meshes; ++i)
+    if (!meshes[i]) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null mesh handle");
+  if ((int64_t)num_meshes * num_meshes > (1 << 22)) return bp_fail(FCLGPU_ERR_UNSUPPORTED, "too many meshes");
+  std::vector<int32_t> gid(num_objects);
+  for (int32_t i = 0; i < num_objects; ++i) {
+    const fclgpu_geometry_ref r = objects[i];
+    if (r.kind == FCLGPU_GEOM_SHAPE && r.index >= 0 && r.index < ns)
+      gid[i] = r.index;
+    else if (r.kind == FCLGPU_GEOM_MESH && r.index >= 0 && r.index < num_meshes)
+      gid[i] = ns + r.index;
+    else
+      return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "scene geometry ref out of range");
+  }
+  std::vector<GeomRec> geoms(ns + num_meshes);
+  for (int32_t i = 0; i < ns; ++i) {
+    std::memset(&geoms[i], 0, sizeof(GeomRec));
+    shape_record(shapes->host[i], shapes->host_verts.data(), geoms[i]);
+    geoms[i].index = i;
+  }
+  for (int32_t i = 0; i < num_meshes; ++i) {
+    GeomRec& g = geoms[ns + i];
+    std::memset(&g, 0, sizeof(GeomRec));
+    g.kind = GEOM_MESH;
+    g.index = i;
+    for (int k = 0; k < 3; ++k) {
+      g.lo[k] = meshes[i]->aabb_local[k];
+      g.hi[k] = meshes[i]->aabb_local[3 + k];
+      g.center[k] = meshes[i]->aabb_center[k];
+      g.ref[k] = meshes[i]->first_vertex[k];
+    }
+    g.radius = meshes[i]->aabb_radius;
+  }
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  fclgpu_broadphase_s* bp = new fclgpu_broadphase_s();
+  bp->shapes = shapes;
+  bp->meshes.assign(meshes, meshes + num_meshes);
+  bp->ns = ns;
+  bp->nm = num_meshes;
+  bp->n = num_objects;
+  bp->mesh_pairs.resize(2 * (size_t)num_meshes * num_meshes);
+  for (int32_t a = 0; a < num_meshes; ++a)
+    for (int32_t b = 0; b < num_meshes; ++b) {
+      bp->mesh_pairs[2 * ((size_t)a * num_meshes + b)] = a;
+      bp->mesh_pairs[2 * ((size_t)a * num_meshes + b) + 1] = b;
+    }
+  const size_t n = (size_t)std::max(num_objects, 1);
+  cudaError_t e = cudaMalloc(&bp->geoms, sizeof(GeomRec) * std::max<size_t>(geoms.size(), 1));
+  if (e == cudaSuccess) e = cudaMalloc(&bp->gid, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&bp->tf, 96 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&bp->aabb64, 48 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&bp->aabb32, 24 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&bp->nodes, sizeof(BpNode) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&bp->build_scratch, bp_build_scratch_bytes((int64_t)n));
+  if (e == cudaSuccess && !geoms.empty())
+    e = cudaMemcpy(bp->geoms, geoms.data(), sizeof(GeomRec) * geoms.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && num_objects > 0) e = cudaMemcpy(bp->gid, gid.data(), 4 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && num_objects > 0) e = cudaMemcpy(bp->tf, tf, 96 * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    free_bp(bp);
+    return bp_cuda(e, "broadphase upload");
+  }
+  const int rc = rebuild(bp, nullptr);
+  if (rc) {
+    free_bp(bp);
+    return rc;
+  }
+  *out = bp;
+  return FCLGPU_OK;
+}
+
+int fclgpu_broadphase_update(fclgpu_broadphase bp, const double* tf, int32_t tf_on_device, void* stream) {
+  if (!bp || (bp->n > 0 && !tf)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "bad update arguments");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (bp->n > 0)
+    CKB(cudaMemcpyAsync(bp->tf, tf, 96 * (size_t)bp->n, tf_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                        s),
+        "update poses");
+  return rebuild(bp, s);
+}
+
+int fclgpu_broadphase_destroy(fclgpu_broadphase bp) {
+  if (!bp) return FCLGPU_OK;
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaDeviceSynchronize();
+  free_bp(bp);
+  return FCLGPU_OK;
+}
+
+int fclgpu_broadphase_get_aabbs(fclgpu_broadphase bp, double* aabb6) {
+  if (!bp || (bp->n > 0 && !aabb6)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  if (bp->n > 0) CKB(cudaMemcpy(aabb6, bp->aabb64, 48 * (size_t)bp->n, cudaMemcpyDeviceToHost), "read aabbs");
+  return FCLGPU_OK;
+}
+
+int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                     const double* tf, const fclgpu_broadphase_collide_request* req,
+                                     fclgpu_broadphase_collide_result* res, void* stream) {
+  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->num_contacts)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase collide argument");
+  if (req->num_max_contacts < 1) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_contacts must be >= 1");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (nq >= ((int64_t)1 << 31)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many queries");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_candidates = 0;
+  res->total_node_visits = 0;
+  if (nq == 0) return FCLGPU_OK;
+  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
+  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
+  BpQueryView Q;
+  RCB(prepare_queries(bp, queries, nq, tf, Q, dctr, s));
+  const BpSceneView S = scene_view(bp);
+  CKB(g_bs.counts.ensure(4 * nq), "counts");
+  CKB(launch_bp_overlap(S, Q, g_bs.counts.as<int32_t>(), nullptr, nullptr, &dctr->visits, &dctr->status, s),
+      "overlap count");
+  BpCounters hc;
+  int64_t total = 0;
+  RCB(scan_counts(nq, dctr, &hc, &total, s));
+  res->total_candidates = total;
+  res->total_node_visits = hc.visits;
+  RCB(ensure_pair_buffers(total));
+  CKB(g_bs.hit.ensure(4 * (size_t)std::max<int64_t>(total, 1)), "hits");
+  const int64_t* off = g_bs.offsets.as<int64_t>();
+  int2* pairs = g_bs.pairs.as<int2>();
+  int32_t* hit = g_bs.hit.as<int32_t>();
+  if (total > 0) {
+    CKB(launch_bp_overlap(S, Q, nullptr, off, pairs, nullptr, &dctr->status, s), "overlap write");
+    CKB(launch_bp_classify(S, Q, pairs, total, g_bs.kind.as<int32_t>(), s), "classify");
+    CKB(cudaMemsetAsync(hit, 0, 4 * (size_t)total, s), "hits");
+    CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_INTERSECT, hit, nullptr, nullptr,
+                               s),
+        "shape narrowphase");
+    int64_t nmixed = 0;
+    RCB(list_kind(total, 2, dctr, &nmixed, s));
+    if (nmixed > 0) return bp_fail(FCLGPU_ERR_UNSUPPORTED, "mesh-shape pairs are not supported by the broadphase");
+    int64_t nl = 0;
+    RCB(list_kind(total, 1, dctr, &nl, s));
+    if (nl > 0) {
+      CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
+      CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_tf2.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_counts.ensure(4 * nl), "mesh scratch");
+      CKB(launch_bp_gather_mesh(S, Q, pairs, g_bs.list.as<int64_t>(), nl, bp->nm, g_bs.m_pair.as<int32_t>(),
+                                g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
+          "mesh gather");
+      fclgpu_collide_request mr = {(int32_t)std::min<int64_t>(req->num_max_contacts, INT32_MAX), req->precision, 0,
+                                   0};
+      fclgpu_collide_result mres = {g_bs.m_counts.as<int32_t>(), nullptr, nullptr, 0, nullptr, nullptr, nullptr, 0};
+      const int rc = fclgpu_collide_batch_device(bp->meshes.data(), bp->nm, bp->mesh_pairs.data(), bp->nm * bp->nm,
+                                                 nl, g_bs.m_pair.as<int32_t>(), g_bs.m_tf1.as<double>(),
+                                                 g_bs.m_tf2.as<double>(), &mr, &mres, stream);
+      if (rc) return rc;
+      CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.m_counts.as<int32_t>(), hit, s), "mesh scatter");
+    }
+  }
+  CKB(launch_bp_reduce_collide(nq, off, pairs, hit, req->num_max_contacts, res->num_contacts, res->num_objects,
+                               res->first_object, s),
+      "reduce");
+  CKB(cudaMemcpyAsync(&hc, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
+  CKB(cudaStreamSynchronize(s), "broadphase collide");
+  return check_status(hc);
+}
+
+int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                      const double* tf, const fclgpu_broadphase_distance_request* req,
+                                      fclgpu_broadphase_distance_result* res, void* stream) {
+  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->min_distance)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase distance argument");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (nq >= ((int64_t)1 << 31)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many queries");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_candidates = 0;
+  res->total_node_visits = 0;
+  if (nq == 0) return FCLGPU_OK;
+  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
+  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
+  BpQueryView Q;
+  RCB(prepare_queries(bp, queries, nq, tf, Q, dctr, s));
+  const BpSceneView S = scene_view(bp);
+  CKB(g_bs.ub.ensure(8 * nq), "bounds");
+  CKB(g_bs.counts.ensure(4 * nq), "counts");
+  CKB(launch_bp_dist_bound(S, Q, g_bs.ub.as<double>(), &dctr->status, s), "distance bound");
+  CKB(launch_bp_dist_candidates(S, Q, g_bs.ub.as<double>(), g_bs.counts.as<int32_t>(), nullptr, nullptr,
+                                &dctr->visits, &dctr->status, s),
+      "distance count");
+  BpCounters hc;
+  int64_t total = 0;
+  RCB(scan_counts(nq, dctr, &hc, &total, s));
+  res->total_candidates = total;
+  res->total_node_visits = hc.visits;
+  RCB(ensure_pair_buffers(total));
+  const size_t t = (size_t)std::max<int64_t>(total, 1);
+  CKB(g_bs.dist.ensure(8 * t), "distances");
+  CKB(g_bs.b12.ensure(8 * t), "distances");
+  CKB(g_bs.pts.ensure(48 * t), "distances");
+  const int64_t* off = g_bs.offsets.as<int64_t>();
+  int2* pairs = g_bs.pairs.as<int2>();
+  double* dist = g_bs.dist.as<double>();
+  int32_t* b12 = g_bs.b12.as<int32_t>();
+  double* pts = g_bs.pts.as<double>();
+  if (total > 0) {
+    CKB(launch_bp_dist_candidates(S, Q, g_bs.ub.as<double>(), nullptr, off, pairs, nullptr, &dctr->status, s),
+        "distance write");
+    CKB(launch_bp_classify(S, Q, pairs, total, g_bs.kind.as<int32_t>(), s), "classify");
+    CKB(cudaMemsetAsync(b12, 0xff, 8 * (size_t)total, s), "ids");
+    CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_DISTANCE, nullptr, dist, pts, s),
+        "shape narrowphase");
+    int64_t nmixed = 0;
+    RCB(list_kind(total, 2, dctr, &nmixed, s));
+    if (nmixed > 0) return bp_fail(FCLGPU_ERR_UNSUPPORTED, "mesh-shape pairs are not supported by the broadphase");
+    int64_t nl = 0;
+    RCB(list_kind(total, 1, dctr, &nl, s));
+    if (nl > 0) {
+      CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
+      CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_tf2.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_dist.ensure(8 * nl), "mesh scratch");
+      CKB(g_bs.m_ids.ensure(8 * nl), "mesh scratch");
+      CKB(g_bs.m_pts.ensure(48 * nl), "mesh scratch");
+      CKB(launch_bp_gather_mesh(S, Q, pairs, g_bs.list.as<int64_t>(), nl, bp->nm, g_bs.m_pair.as<int32_t>(),
+                                g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
+          "mesh gather");
+      fclgpu_distance_request mr = {1, req->precision, 0, 0};
+      fclgpu_distance_result mres = {g_bs.m_dist.as<double>(), g_bs.m_ids.as<int32_t>(), g_bs.m_pts.as<double>(),
+                                     nullptr, nullptr, nullptr, nullptr, nullptr};
+      const int rc = fclgpu_distance_batch_device(bp->meshes.data(), bp->nm, bp->mesh_pairs.data(),
+                                                  bp->nm * bp->nm, nl, g_bs.m_pair.as<int32_t>(),
+                                                  g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), &mr, &mres,
+                                                  stream);
+      if (rc) return rc;
+      CKB(launch_bp_scatter_dist(g_bs.list.as<int64_t>(), nl, g_bs.m_dist.as<double>(), g_bs.m_ids.as<int32_t>(),
+                                 g_bs.m_pts.as<double>(), dist, b12, pts, s),
+          "mesh scatter");
+    }
+  }
+  CKB(launch_bp_reduce_distance(nq, off, pairs, dist, b12, pts, res->min_distance, res->object, res->ids,
+                                req->enable_nearest_points ? res->nearest_points : nullptr, s),
+      "reduce");
+  CKB(cudaMemcpyAsync(&hc, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
+  CKB(cudaStreamSynchronize(s), "broadphase distance");
+  return check_status(hc);
+}
+
+int fclgpu_broadphase_collide(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq, const double* tf,
+                              const fclgpu_broadphase_collide_request* req, fclgpu_broadphase_collide_result* res,
+                              void* stream) {
+  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->num_contacts)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase collide argument");
+  if (nq == 0) return fclgpu_broadphase_collide_device(bp, queries, 0, tf, req, res, stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf refs, tfd, nc, no, fo;  // per-call staging (the device entry point owns the shared scratch)
+  CKB(refs.ensure(8 * nq), "staging");
+  CKB(tfd.ensure(96 * nq), "staging");
+  CKB(nc.ensure(8 * nq), "staging");
+  CKB(no.ensure(4 * nq), "staging");
+  CKB(fo.ensure(4 * nq), "staging");
+  CKB(cudaMemcpyAsync(refs.p, queries, 8 * nq, cudaMemcpyHostToDevice, s), "h2d");
+  CKB(cudaMemcpyAsync(tfd.p, tf, 96 * nq, cudaMemcpyHostToDevice, s), "h2d");
+  fclgpu_broadphase_collide_result dr = {nc.as<int64_t>(), no.as<int32_t>(), fo.as<int32_t>(), 0, 0};
+  int rc = fclgpu_broadphase_collide_device(bp, refs.as<fclgpu_geometry_ref>(), nq, tfd.as<double>(), req, &dr,
+                                            stream);
+  if (rc == FCLGPU_OK) {
+    res->total_candidates = dr.total_candidates;
+    res->total_node_visits = dr.total_node_visits;
+    cudaError_t e = cudaMemcpyAsync(res->num_contacts, nc.p, 8 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && res->num_objects)
+      e = cudaMemcpyAsync(res->num_objects, no.p, 4 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && res->first_object)
+      e = cudaMemcpyAsync(res->first_object, fo.p, 4 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = bp_cuda(e, "d2h");
+  }
+  for (Buf* b : {&refs, &tfd, &nc, &no, &fo}) cudaFree(b->p);
+  return rc;
+}
+
+int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                               const double* tf, const fclgpu_broadphase_distance_request* req,
+                               fclgpu_broadphase_distance_result* res, void* stream) {
+  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->min_distance)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase distance argument");
+  if (nq == 0) return fclgpu_broadphase_distance_device(bp, queries, 0, tf, req, res, stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf refs, tfd, d, ob, ids, pts;
+  CKB(refs.ensure(8 * nq), "staging");
+  CKB(tfd.ensure(96 * nq), "staging");
+  CKB(d.ensure(8 * nq), "staging");
+  CKB(ob.ensure(4 * nq), "staging");
+  CKB(ids.ensure(8 * nq), "staging");
+  CKB(pts.ensure(48 * nq), "staging");
+  CKB(cudaMemcpyAsync(refs.p, queries, 8 * nq, cudaMemcpyHostToDevice, s), "h2d");
+  CKB(cudaMemcpyAsync(tfd.p, tf, 96 * nq, cudaMemcpyHostToDevice, s), "h2d");
+  fclgpu_broadphase_distance_result dr = {d.as<double>(), ob.as<int32_t>(), ids.as<int32_t>(), pts.as<double>(), 0,
+                                          0};
+  int rc = fclgpu_broadphase_distance_device(bp, refs.as<fclgpu_geometry_ref>(), nq, tfd.as<double>(), req, &dr,
+                                             stream);
+  if (rc == FCLGPU_OK) {
+    res->total_candidates = dr.total_candidates;
+    res->total_node_visits = dr.total_node_visits;
+    cudaError_t e = cudaMemcpyAsync(res->min_distance, d.p, 8 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && res->object) e = cudaMemcpyAsync(res->object, ob.p, 4 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && res->ids) e = cudaMemcpyAsync(res->ids, ids.p, 8 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && res->nearest_points && req->enable_nearest_points)
+      e = cudaMemcpyAsync(res->nearest_points, pts.p, 48 * nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = bp_cuda(e, "d2h");
+  }
+  for (Buf* b : {&refs, &tfd, &d, &ob, &ids, &pts}) cudaFree(b->p);
+  return rc;
+}
+
+}  // extern "C"

@@ -9,20 +9,13 @@
 
 #include "../../include/fclgpu.h"
 #include "shapes.h"
+#include "shapeset_handle.h"
 
 using namespace fclgpu;
-
-struct fclgpu_shapeset_s {
-  DevShape* shapes = nullptr;
-  double* verts = nullptr;
-  int32_t n = 0;
-  int64_t nv = 0;
-};
 
 namespace {
 
 std::mutex g_mu;
-thread_local std::string g_err;
 
 struct Buf {
   void* p = nullptr;
@@ -41,7 +34,7 @@ Buf g_ctr, g_ia, g_ib, g_tf1, g_tf2, g_hit, g_nrm, g_pt, g_dep, g_dist, g_p1, g_
 cudaEvent_t g_ev[2] = {nullptr, nullptr};
 
 int cfail(cudaError_t e, const char* where) {
-  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  set_error_detail(std::string(where) + ": " + cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
 }
 #define CKS(expr, where)                          \
@@ -84,6 +77,8 @@ int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* 
   }
   ss->n = n;
   ss->nv = nv;
+  ss->host = h;
+  if (nv > 0) ss->host_verts.assign(verts, verts + 3 * nv);
   *out = ss;
   return FCLGPU_OK;
 }

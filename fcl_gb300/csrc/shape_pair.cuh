@@ -379,8 +379,13 @@ FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1
 }
 
 // One pair: shapes a, b (with the vertex pool) at tf1, tf2 (3x4 row-major).
+enum { PAIR_INTERSECT = 1, PAIR_DISTANCE = 2, PAIR_BOTH = 3 };
+
+// mode PAIR_INTERSECT: fcl::collide only; PAIR_DISTANCE: fcl::distance only (dist = -1
+// when the distance dispatch finds the pair intersecting); PAIR_BOTH: collide, then
+// distance when the pair does not collide.
 FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const double* verts, const double* tf1p,
-                              const double* tf2p, PairOut& o) {
+                              const double* tf2p, PairOut& o, int mode = PAIR_BOTH) {
   ShapeRef A, B;
   A.s = sa;
   B.s = sb;
@@ -396,8 +401,9 @@ FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const doub
   o.gstat = o.estat = -1;
   SimplexVert V[kSimplexSlots];
   const int a = A.s.type, b = B.s.type;
-  bool hit;
-  if (a == SHAPE_SPHERE && b == SHAPE_SPHERE) {
+  bool hit = false;
+  if (!(mode & PAIR_INTERSECT)) {
+  } else if (a == SHAPE_SPHERE && b == SHAPE_SPHERE) {
     hit = sphere_sphere_intersect(A.s.p[0], t1, B.s.p[0], t2, o);
   } else if (a == SHAPE_SPHERE && b == SHAPE_CAPSULE) {
     hit = sphere_capsule_intersect(A.s.p[0], t1, B.s.p[0], B.s.p[1], R2, t2, o);
@@ -420,7 +426,7 @@ FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const doub
     hit = o.hit != 0;
   }
   o.hit = hit ? 1 : 0;
-  if (!hit) {
+  if (!hit && (mode & PAIR_DISTANCE)) {
     if (a == SHAPE_SPHERE && b == SHAPE_SPHERE) {
       sphere_sphere_distance(A.s.p[0], t1, B.s.p[0], t2, o);
     } else if (a == SHAPE_SPHERE && b == SHAPE_CAPSULE) {

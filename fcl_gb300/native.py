@@ -51,6 +51,31 @@ class DistanceResult(C.Structure):
                 ("num_leaf_tests", C.c_void_p), ("num_rechecks", C.c_void_p)]
 
 
+class GeometryRef(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32)]
+
+
+class BpCollideRequest(C.Structure):
+    _fields_ = [("num_max_contacts", C.c_int64), ("precision", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BpCollideResult(C.Structure):
+    _fields_ = [("num_contacts", C.c_void_p), ("num_objects", C.c_void_p), ("first_object", C.c_void_p),
+                ("total_candidates", C.c_int64), ("total_node_visits", C.c_int64)]
+
+
+class BpDistanceRequest(C.Structure):
+    _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32)]
+
+
+class BpDistanceResult(C.Structure):
+    _fields_ = [("min_distance", C.c_void_p), ("object", C.c_void_p), ("ids", C.c_void_p),
+                ("nearest_points", C.c_void_p), ("total_candidates", C.c_int64), ("total_node_visits", C.c_int64)]
+
+
+GEOM_SHAPE = 0
+GEOM_MESH = 1
+
 _lib = None
 
 # every function the header declares, with (restype, argtypes)
@@ -80,6 +105,18 @@ _SIGS = {
     "fclgpu_shape_batch_device": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_shape_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_last_shape_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
+    "fclgpu_broadphase_create": (C.c_int, [_VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.POINTER(C.c_void_p)]),
+    "fclgpu_broadphase_update": (C.c_int, [_VP, _VP, C.c_int32, _VP]),
+    "fclgpu_broadphase_destroy": (C.c_int, [_VP]),
+    "fclgpu_broadphase_get_aabbs": (C.c_int, [_VP, _VP]),
+    "fclgpu_broadphase_collide_device": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpCollideRequest),
+                                                   C.POINTER(BpCollideResult), _VP]),
+    "fclgpu_broadphase_collide": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpCollideRequest),
+                                            C.POINTER(BpCollideResult), _VP]),
+    "fclgpu_broadphase_distance_device": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
+                                                    C.POINTER(BpDistanceResult), _VP]),
+    "fclgpu_broadphase_distance": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
+                                             C.POINTER(BpDistanceResult), _VP]),
 }
 
 

@@ -280,3 +280,165 @@ def config3(n_pairs: int = 4_000_000, n_shapes: int = 4096, seed: int = 3) -> Sh
     tf1 = random_poses(n_pairs, -1.0, 1.0, seed + 2)
     tf2 = random_poses(n_pairs, -1.0, 1.0, seed + 3)
     return ShapePairWorkload(shapes, ia, ib, tf1, tf2)
+
+
+# ---------------------------------------------------------------------------------
+# Broadphase scene and motion-checking requests
+# ---------------------------------------------------------------------------------
+
+def concat_shapes(a: ShapeSet, b: ShapeSet) -> ShapeSet:
+    """Shape set with a's shapes first, then b's (convex vertex offsets of b shifted)."""
+    na_v = a.verts.shape[0]
+    voff_b = np.where(b.type == CONVEX, b.voff + na_v, 0).astype(np.int32)
+    return ShapeSet(np.concatenate([a.type, b.type]).astype(np.int32), np.concatenate([a.params, b.params]),
+                    np.concatenate([a.voff, voff_b]).astype(np.int32),
+                    np.concatenate([a.vcnt, b.vcnt]).astype(np.int32),
+                    np.ascontiguousarray(np.concatenate([a.verts.reshape(-1, 3), b.verts.reshape(-1, 3)])))
+
+
+@dataclass
+class Robot:
+    """A serial chain: joint i turns about a coordinate axis of the frame left by
+    link i-1 (axis 0/1/2 = x/y/z), then link i extends by `offset[i]`.  Link i's
+    geometry (`link_refs[i]`, kind/index into the registry) sits at `geom_tf[i]`
+    (3x4) in the joint frame."""
+    axis: np.ndarray        # (L,) int32
+    offset: np.ndarray      # (L, 3)
+    link_refs: np.ndarray   # (L, 2) int32
+    geom_tf: np.ndarray     # (L, 3, 4)
+
+    @property
+    def n_links(self) -> int:
+        return int(self.axis.shape[0])
+
+
+@dataclass
+class SceneWorkload:
+    """Registry (shapes, meshes) shared by scene and robot; scene objects as refs + poses."""
+    shapes: ShapeSet
+    meshes: list
+    refs: np.ndarray   # (N, 2) int32
+    tf: np.ndarray     # (N, 3, 4)
+    robot: Robot
+
+    @property
+    def n(self) -> int:
+        return int(self.refs.shape[0])
+
+
+def _rot_y90() -> np.ndarray:
+    # maps the local z axis (capsule axis) onto x
+    return np.array([[0.0, 0.0, 1.0], [0.0, 1.0, 0.0], [-1.0, 0.0, 0.0]])
+
+
+def scene4(n_objects: int | None = None, seed: int = 4, box: float = 20.0, n_shape_geoms: int = 1024,
+           n_mesh_geoms: int = 16, mesh_fraction: float = 0.25, tri_lo: int = 500, tri_hi: int = 5000,
+           n_links: int = 20, mesh_links: bool = True, link_tris: int = 2000) -> SceneWorkload:
+    """Serving scene: N ~ logU[1000, 50000] objects (or n_objects), each a random convex
+    primitive (the convex-pair recipe) or, with probability mesh_fraction, one of
+    n_mesh_geoms perturbed icospheres of logU[tri_lo, tri_hi] triangles (radii
+    U[0.3, 1.0]^3); Haar rotations, positions U[0, box]^3.  The robot has n_links
+    links of length U[0.25, 0.4]; even links are capsules (r 0.06), odd links (when
+    mesh_links) ellipsoid meshes of link_tris triangles along the link."""
+    rng = np.random.default_rng(seed)
+    if n_objects is None:
+        n_objects = int(_loguniform_int(rng, 1000, 50000))
+    scene_shapes = random_shapes(n_shape_geoms, seed + 1)
+    meshes = []
+    if mesh_fraction > 0:
+        for k in range(n_mesh_geoms):
+            T = _loguniform_int(rng, tri_lo, tri_hi)
+            freq = max(1, int(round(math.sqrt(T / 20.0))))
+            meshes.append(perturbed_ellipsoid(freq, rng.uniform(0.3, 1.0, size=3), 0.01, seed * 7919 + k))
+    # robot link geometries
+    lengths = rng.uniform(0.25, 0.4, size=n_links)
+    link_types, link_params = [], []
+    link_refs = np.zeros((n_links, 2), np.int32)
+    geom_tf = np.zeros((n_links, 3, 4))
+    freq_link = max(1, int(round(math.sqrt(link_tris / 20.0))))
+    for i in range(n_links):
+        L = lengths[i]
+        geom_tf[i, :, 3] = (L / 2, 0.0, 0.0)
+        if mesh_links and i % 2 == 1:
+            link_refs[i] = (1, len(meshes))
+            meshes.append(perturbed_ellipsoid(freq_link, (L / 2, 0.08, 0.08), 0.002, seed * 104729 + i))
+            geom_tf[i, :, :3] = np.eye(3)
+        else:
+            link_refs[i] = (0, n_shape_geoms + len(link_types))
+            link_types.append(CAPSULE)
+            link_params.append((0.06, L, 0.0))
+            geom_tf[i, :, :3] = _rot_y90()
+    robot_shapes = ShapeSet(np.array(link_types, np.int32), np.array(link_params, np.float64).reshape(-1, 3),
+                            np.zeros(len(link_types), np.int32), np.zeros(len(link_types), np.int32),
+                            np.zeros((0, 3)))
+    shapes = concat_shapes(scene_shapes, robot_shapes)
+    n_scene_meshes = n_mesh_geoms if mesh_fraction > 0 else 0
+    is_mesh = rng.uniform(size=n_objects) < mesh_fraction if n_scene_meshes else np.zeros(n_objects, bool)
+    refs = np.zeros((n_objects, 2), np.int32)
+    refs[:, 0] = is_mesh.astype(np.int32)
+    refs[:, 1] = np.where(is_mesh, rng.integers(0, max(1, n_scene_meshes), size=n_objects),
+                          rng.integers(0, n_shape_geoms, size=n_objects))
+    tf = np.empty((n_objects, 3, 4))
+    tf[:, :, :3] = haar_rotations(n_objects, rng)
+    tf[:, :, 3] = rng.uniform(0.0, box, size=(n_objects, 3))
+    axis = np.array([2 if i % 2 == 0 else 1 for i in range(n_links)], np.int32)
+    offset = np.zeros((n_links, 3))
+    offset[:, 0] = lengths
+    robot = Robot(axis, offset, link_refs, geom_tf)
+    return SceneWorkload(shapes, meshes, refs, np.ascontiguousarray(tf), robot)
+
+
+def joint_rotation(axis: int, q: np.ndarray) -> np.ndarray:
+    c, s = np.cos(q), np.sin(q)
+    R = np.zeros(q.shape + (3, 3))
+    if axis == 0:
+        R[..., 0, 0] = 1; R[..., 1, 1] = c; R[..., 1, 2] = -s; R[..., 2, 1] = s; R[..., 2, 2] = c
+    elif axis == 1:
+        R[..., 0, 0] = c; R[..., 0, 2] = s; R[..., 1, 1] = 1; R[..., 2, 0] = -s; R[..., 2, 2] = c
+    else:
+        R[..., 0, 0] = c; R[..., 0, 1] = -s; R[..., 1, 0] = s; R[..., 1, 1] = c; R[..., 2, 2] = 1
+    return R
+
+
+def robot_fk(robot: Robot, base: np.ndarray, q: np.ndarray) -> np.ndarray:
+    """World poses (K, L, 3, 4) of the link geometries for joint angles q (K, L)."""
+    q = np.asarray(q, np.float64)
+    K, L = q.shape
+    R = np.broadcast_to(base[:3, :3], (K, 3, 3)).copy()
+    t = np.broadcast_to(base[:3, 3], (K, 3)).copy()
+    out = np.empty((K, L, 3, 4))
+    for i in range(L):
+        R = R @ joint_rotation(int(robot.axis[i]), q[:, i])
+        G = robot.geom_tf[i]
+        out[:, i, :, :3] = R @ G[:, :3]
+        out[:, i, :, 3] = t + R @ G[:, 3]
+        t = t + R @ robot.offset[i]
+    return out
+
+
+@dataclass
+class MotionRequest:
+    base: np.ndarray   # (3, 4)
+    q: np.ndarray      # (K, L) joint angles per waypoint
+
+
+def motion_requests(w: SceneWorkload, n_requests: int, seed: int = 5, k_lo: int = 10, k_hi: int = 500,
+                    sigma: float = 0.05) -> list:
+    """Requests: base pose uniform in the scene box (Haar rotation), K ~ logU[k_lo,
+    k_hi] waypoints of a joint-space random walk with step N(0, sigma^2) from a start
+    uniform in [-pi, pi]^L."""
+    rng = np.random.default_rng(seed)
+    box = float(w.tf[:, :, 3].max()) if w.n else 20.0
+    out = []
+    L = w.robot.n_links
+    for _ in range(n_requests):
+        K = int(_loguniform_int(rng, k_lo, k_hi + 1))
+        K = max(k_lo, min(k_hi, K))
+        base = np.zeros((3, 4))
+        base[:, :3] = haar_rotations(1, rng)[0]
+        base[:, 3] = rng.uniform(0.0, box, size=3)
+        q0 = rng.uniform(-math.pi, math.pi, size=L)
+        q = q0[None, :] + np.cumsum(rng.normal(0.0, sigma, size=(K, L)), axis=0)
+        q[0] = q0
+        out.append(MotionRequest(base, np.ascontiguousarray(q)))
+    return out

@@ -236,6 +236,103 @@ FCLGPU_API int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t*
 /* Device time (ms) of the most recent shape-pair kernel.  No counterpart in FCL. */
 FCLGPU_API int fclgpu_last_shape_kernel_time(double* ms);
 
+/* ---- broadphase -------------------------------------------------------------------
+ * Replaces DynamicAABBTreeCollisionManager<double> (broadphase/
+ * broadphase_dynamic_AABB_tree.h:56-157, -inl.h:727-1009) behind
+ * BroadPhaseCollisionManager's registerObjects/setup/update and the per-object
+ * collide(obj, cdata, DefaultCollisionFunction) / distance(obj, cdata,
+ * DefaultDistanceFunction) queries (broadphase_collision_manager.h:65-122,
+ * default_broadphase_callbacks.h:88-106, 195-215), batched over many query objects.
+ *
+ * Geometry is referenced, as CollisionObject's shared_ptr<CollisionGeometry> is
+ * (narrowphase/collision_object.h:143-144): the broadphase keeps the shape set and the
+ * mesh table it was created with, and scene objects and query objects name a
+ * geometry by (kind, index).  World AABBs follow CollisionObject::computeAABB
+ * (collision_object-inl.h:116-131) bit for bit.  The device tree is an LBVH rebuilt from
+ * Morton codes; its shape differs from FCL's, so the results reported are the ones
+ * that do not depend on traversal order (see the result structs). */
+enum { FCLGPU_GEOM_SHAPE = 0, FCLGPU_GEOM_MESH = 1 };
+
+typedef struct {
+  int32_t kind;   /* FCLGPU_GEOM_SHAPE: index into the shape set; FCLGPU_GEOM_MESH: into meshes[] */
+  int32_t index;
+} fclgpu_geometry_ref;
+
+typedef struct fclgpu_broadphase_s* fclgpu_broadphase;
+
+/* registerObjects + setup: num_objects scene objects (geometry refs and poses, host
+ * arrays).  shapes may be NULL when no shape is referenced; meshes may be NULL when
+ * num_meshes is 0.  The shape set and meshes must outlive the broadphase. */
+FCLGPU_API int fclgpu_broadphase_create(fclgpu_shapeset shapes, const fclgpu_mesh* meshes, int32_t num_meshes,
+                                        const fclgpu_geometry_ref* objects, int32_t num_objects, const double* tf,
+                                        fclgpu_broadphase* out);
+/* update(): new poses for every scene object (tf: num_objects x 12 doubles, a device
+ * pointer when tf_on_device != 0); AABBs are recomputed and the tree rebuilt. */
+FCLGPU_API int fclgpu_broadphase_update(fclgpu_broadphase bp, const double* tf, int32_t tf_on_device, void* stream);
+FCLGPU_API int fclgpu_broadphase_destroy(fclgpu_broadphase bp);
+/* CollisionObject::getAABB() of every scene object: 6 doubles (min, max) each. */
+FCLGPU_API int fclgpu_broadphase_get_aabbs(fclgpu_broadphase bp, double* aabb6);
+
+typedef struct {
+  int64_t num_max_contacts; /* CollisionRequest::num_max_contacts (>= 1) */
+  int32_t precision;        /* mesh-mesh narrowphase form (FCLGPU_PLAIN_FP64 / FCLGPU_FP32_RECHECK) */
+  int32_t reserved;
+} fclgpu_broadphase_collide_request;
+
+/* Per query q: num_contacts[q] = DefaultCollisionData::result.numContacts() after
+ * manager.collide(query, DefaultCollisionFunction), which is min(num_max_contacts,
+ * sum over colliding scene objects of their contacts); num_objects[q] = number of
+ * scene objects in collision with the query and first_object[q] = the smallest such
+ * object index (-1 if none) -- both exhaustive, an extension that does not depend on
+ * the order FCL's callback would meet the objects in.  Outputs may be NULL except
+ * num_contacts.  The totals are filled on return. */
+typedef struct {
+  int64_t* num_contacts;
+  int32_t* num_objects;
+  int32_t* first_object;
+  int64_t total_candidates;  /* (query, object) pairs with overlapping AABBs */
+  int64_t total_node_visits; /* tree nodes loaded */
+} fclgpu_broadphase_collide_result;
+
+/* queries: nq geometry refs, tf: nq x 12 doubles.  _device: every pointer (queries,
+ * tf and the result arrays) is a device pointer; the plain form takes host pointers. */
+FCLGPU_API int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                                const double* tf, const fclgpu_broadphase_collide_request* req,
+                                                fclgpu_broadphase_collide_result* res, void* stream);
+FCLGPU_API int fclgpu_broadphase_collide(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                         const double* tf, const fclgpu_broadphase_collide_request* req,
+                                         fclgpu_broadphase_collide_result* res, void* stream);
+
+typedef struct {
+  int32_t enable_nearest_points;
+  int32_t precision; /* mesh-mesh narrowphase form */
+} fclgpu_broadphase_distance_request;
+
+/* Per query q: min_distance[q] = DefaultDistanceData::result.min_distance after
+ * manager.distance(query, DefaultDistanceFunction) for a query in no contact (the
+ * minimum over scene objects; ties go to the smaller object index); object[q] = that
+ * scene object, ids[2q..2q+1] = its (b1, b2) triangle ids (-1 for shapes),
+ * nearest_points[6q..6q+5] = the world-frame witnesses on the object and on the
+ * query.  A query in contact reports a value <= 0 (FCL reports the first contact its
+ * traversal meets, -1 for shape pairs, 0 for mesh pairs).  DBL_MAX for an empty
+ * scene.  Outputs other than min_distance may be NULL. */
+typedef struct {
+  double* min_distance;
+  int32_t* object;
+  int32_t* ids;
+  double* nearest_points;
+  int64_t total_candidates;  /* (query, object) pairs evaluated by the narrowphase */
+  int64_t total_node_visits;
+} fclgpu_broadphase_distance_result;
+
+FCLGPU_API int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries,
+                                                 int64_t nq, const double* tf,
+                                                 const fclgpu_broadphase_distance_request* req,
+                                                 fclgpu_broadphase_distance_result* res, void* stream);
+FCLGPU_API int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                          const double* tf, const fclgpu_broadphase_distance_request* req,
+                                          fclgpu_broadphase_distance_result* res, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

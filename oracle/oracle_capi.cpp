@@ -9,6 +9,7 @@
 #include <thread>
 #include <vector>
 
+#include "oracle_broadphase.h"
 #include "oracle_mesh.h"
 
 using namespace oracle;
@@ -346,6 +347,169 @@ void orc_project_origin(int k, const double* pts, int* encode, double* out5) {
   *encode = (int)r.encode;
   out5[0] = r.sqr_distance;
   for (int i = 0; i < 4; ++i) out5[1 + i] = r.parameterization[i];
+}
+
+// ------------------------------------------------------------------ broadphase ----
+// A geometry registry: ids [0, ns) are convex shapes, [ns, ns + nm) meshes created by
+// orc_mesh_create.  Scenes and queries name geometries by id.
+struct OrcGeoms {
+  std::vector<V3> verts;
+  std::vector<BpGeom> g;
+};
+struct OrcScene {
+  const OrcGeoms* geoms;
+  std::vector<BpObject> objs;
+  DynTree tree;
+};
+
+static BpObject make_object(const OrcGeoms& G, int gid, const double* tf) {
+  BpObject o;
+  o.geom = &G.g[gid];
+  o.tf = load_tf(tf);
+  o.aabb = compute_aabb(*o.geom, o.tf);
+  return o;
+}
+
+void* orc_geoms_create(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                       const double* verts, int nm, void* const* meshes) {
+  OrcGeoms* G = new OrcGeoms();
+  int nv = 0;
+  for (int i = 0; i < ns; ++i) nv = std::max(nv, voff[i] + vcnt[i]);
+  G->verts.resize(nv);
+  for (int i = 0; i < nv; ++i) G->verts[i] = mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+  G->g.resize(ns + nm);
+  for (int i = 0; i < ns; ++i) {
+    BpGeom& g = G->g[i];
+    g.kind = 0;
+    g.shape.type = type[i];
+    for (int k = 0; k < 3; ++k) g.shape.p[k] = params[3 * i + k];
+    g.shape.verts = G->verts.data() + voff[i];
+    g.shape.nverts = vcnt[i];
+    compute_local_aabb(g);
+  }
+  for (int i = 0; i < nm; ++i) {
+    BpGeom& g = G->g[ns + i];
+    g.kind = 1;
+    g.mesh = static_cast<const Mesh*>(meshes[i]);
+    compute_local_aabb(g);
+  }
+  return G;
+}
+
+void orc_geoms_free(void* h) { delete static_cast<OrcGeoms*>(h); }
+
+// Per geometry: aabb_local min (3), max (3), aabb_center (3), aabb_radius.
+void orc_geoms_local(void* h, double* out10) {
+  const OrcGeoms* G = static_cast<OrcGeoms*>(h);
+  for (size_t i = 0; i < G->g.size(); ++i) {
+    const BpGeom& g = G->g[i];
+    for (int k = 0; k < 3; ++k) {
+      out10[10 * i + k] = g.local.mn[k];
+      out10[10 * i + 3 + k] = g.local.mx[k];
+      out10[10 * i + 6 + k] = g.center[k];
+    }
+    out10[10 * i + 9] = g.radius;
+  }
+}
+
+void* orc_scene_create(void* geoms, int n, const int* gid, const double* tf) {
+  OrcScene* S = new OrcScene();
+  S->geoms = static_cast<OrcGeoms*>(geoms);
+  S->objs.resize(n);
+  std::vector<AABB> bv(n);
+  for (int i = 0; i < n; ++i) {
+    S->objs[i] = make_object(*S->geoms, gid[i], tf + 12 * i);
+    bv[i] = S->objs[i].aabb;
+  }
+  S->tree.build(bv);
+  return S;
+}
+
+void orc_scene_free(void* h) { delete static_cast<OrcScene*>(h); }
+
+int orc_scene_num_tree_nodes(void* h) { return (int)static_cast<OrcScene*>(h)->tree.nodes.size(); }
+
+// World AABBs of n objects (geometry ids + poses), 6 doubles each (min, max).
+void orc_world_aabbs(void* geoms, int64_t n, const int* gid, const double* tf, double* out6) {
+  const OrcGeoms* G = static_cast<OrcGeoms*>(geoms);
+  for (int64_t i = 0; i < n; ++i) {
+    const AABB b = compute_aabb(G->g[gid[i]], load_tf(tf + 12 * i));
+    for (int k = 0; k < 3; ++k) {
+      out6[6 * i + k] = b.mn[k];
+      out6[6 * i + 3 + k] = b.mx[k];
+    }
+  }
+}
+
+// Exact AABB-overlap candidates of each query, brute force, in object order.
+// Returns the total; writes object ids while they fit in cap.
+int64_t orc_scene_candidates(void* h, int64_t nq, const int* qgid, const double* qtf, int64_t* counts, int* out,
+                             int64_t cap) {
+  const OrcScene* S = static_cast<OrcScene*>(h);
+  int64_t total = 0;
+  for (int64_t q = 0; q < nq; ++q) {
+    const BpObject Q = make_object(*S->geoms, qgid[q], qtf + 12 * q);
+    int64_t c = 0;
+    for (int i = 0; i < (int)S->objs.size(); ++i)
+      if (aabb_overlap(S->objs[i].aabb, Q.aabb)) {
+        if (out && total < cap) out[total] = i;
+        ++total;
+        ++c;
+      }
+    counts[q] = c;
+  }
+  return total;
+}
+
+// manager.collide(query, DefaultCollisionFunction) per query with
+// request.num_max_contacts = max_contacts; use_tree selects the dynamic AABB tree
+// manager, else the naive one.  Per query: total contacts, number of scene objects
+// that reported contact; their ids (callback order) go to hits while they fit.
+int64_t orc_scene_collide(void* h, int64_t nq, const int* qgid, const double* qtf, int64_t max_contacts,
+                          int use_tree, int nthreads, int64_t* num_contacts, int* num_hits, int* hits,
+                          int64_t cap, int64_t* narrow_calls) {
+  const OrcScene* S = static_cast<OrcScene*>(h);
+  std::vector<std::vector<int>> per(nq);
+  parallel_for(nq, nthreads, [&](int64_t q, int) {
+    const BpObject Q = make_object(*S->geoms, qgid[q], qtf + 12 * q);
+    BpCollideOut o;
+    bp_collide(S->objs, use_tree ? &S->tree : nullptr, Q, max_contacts, o);
+    num_contacts[q] = o.num_contacts;
+    num_hits[q] = (int)o.hit_objects.size();
+    if (narrow_calls) narrow_calls[q] = o.narrow_calls;
+    per[q] = std::move(o.hit_objects);
+  });
+  int64_t total = 0;
+  for (int64_t q = 0; q < nq; ++q)
+    for (int id : per[q]) {
+      if (hits && total < cap) hits[total] = id;
+      ++total;
+    }
+  return total;
+}
+
+// manager.distance(query, DefaultDistanceFunction) per query.  Outputs: min distance,
+// scene object, (b1, b2) triangle ids (-1 for shapes), world witnesses (6 doubles).
+void orc_scene_distance(void* h, int64_t nq, const int* qgid, const double* qtf, int use_tree, int nthreads,
+                        double* dist, int* obj, int* b12, double* pts, int64_t* narrow_calls) {
+  const OrcScene* S = static_cast<OrcScene*>(h);
+  parallel_for(nq, nthreads, [&](int64_t q, int) {
+    const BpObject Q = make_object(*S->geoms, qgid[q], qtf + 12 * q);
+    BpDistanceOut o;
+    bp_distance(S->objs, use_tree ? &S->tree : nullptr, Q, o);
+    dist[q] = o.min_distance;
+    if (obj) obj[q] = o.object;
+    if (b12) {
+      b12[2 * q] = o.b1;
+      b12[2 * q + 1] = o.b2;
+    }
+    if (pts)
+      for (int k = 0; k < 3; ++k) {
+        pts[6 * q + k] = o.p1[k];
+        pts[6 * q + 3 + k] = o.p2[k];
+      }
+    if (narrow_calls) narrow_calls[q] = o.narrow_calls;
+  });
 }
 
 }  // extern "C"

@@ -1037,15 +1037,9 @@ bool gjk_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2
 // distance) restricted to Box/Sphere/Capsule/Cylinder/Cone/Convex.  Box-box
 // intersection has a closed form in FCL (boxBoxIntersect); it is not restated here
 // and box pairs go through GJK/EPA (documented gap).
-void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
-  r.collide = false;
-  r.normal = r.point = r.p1 = r.p2 = mk(0, 0, 0);
-  r.depth = 0;
-  r.distance = -1;
-  r.gjk_status = r.epa_status = -1;
+bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
   const int a = s1.type, b = s2.type;
   bool hit;
-  // --- intersect
   if (a == SH_SPHERE && b == SH_SPHERE) {
     hit = sphere_sphere_intersect(s1, tf1, s2, tf2, r);
   } else if (a == SH_SPHERE && b == SH_CAPSULE) {
@@ -1068,9 +1062,11 @@ void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, 
     // 0.7.0 reports for this solver); it is returned as is
     hit = gjk_intersect(s1, tf1, s2, tf2, &r.normal, &r.point, &r.depth, &r.gjk_status, &r.epa_status);
   }
-  r.collide = hit;
-  if (hit) return;
-  // --- distance
+  return hit;
+}
+
+void shape_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
+  const int a = s1.type, b = s2.type;
   if (a == SH_SPHERE && b == SH_SPHERE) {
     sphere_sphere_distance(s1, tf1, s2, tf2, &r.distance, &r.p1, &r.p2);
   } else if (a == SH_SPHERE && b == SH_CAPSULE) {
@@ -1090,6 +1086,16 @@ void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, 
   } else {
     gjk_distance(s1, tf1, s2, tf2, &r.distance, &r.p1, &r.p2, &r.gjk_status);
   }
+}
+
+void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
+  r.collide = false;
+  r.normal = r.point = r.p1 = r.p2 = mk(0, 0, 0);
+  r.depth = 0;
+  r.distance = -1;
+  r.gjk_status = r.epa_status = -1;
+  r.collide = shape_intersect(s1, tf1, s2, tf2, r);
+  if (!r.collide) shape_distance(s1, tf1, s2, tf2, r);
 }
 
 }  // namespace oracle

@@ -29,6 +29,11 @@ struct ShapeResult {
 
 // fcl::collide + fcl::distance for one convex pair with GJKSolver_indep.
 void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
+// The two halves of shape_pair: the intersect dispatch (gjk_solver_indep-inl.h:182-200;
+// fills normal/point/depth/statuses when it returns true) and the distance dispatch
+// (gjk_solver_indep-inl.h:686-708; distance -1 when the pair intersects).
+bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
+void shape_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
 
 // Pure GJK/EPA without closed-form dispatch (used to check the device solver).
 bool gjk_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, V3* normal, V3* point,

@@ -232,3 +232,125 @@ def project_origin(pts):
     out = np.zeros(5)
     L.orc_project_origin(pts.shape[0], _d(pts), C.byref(enc), _d(out))
     return enc.value, out[0], out[1:]
+
+
+# ------------------------------------------------------------------ broadphase ----
+
+def _bp_sigs(L):
+    if getattr(L, "_bp_sig", False):
+        return
+    vp = C.c_void_p
+    L.orc_geoms_create.restype = vp
+    L.orc_geoms_create.argtypes = [C.c_int, _ip, _dp, _ip, _ip, _dp, C.c_int, C.POINTER(C.c_void_p)]
+    L.orc_geoms_free.argtypes = [vp]
+    L.orc_geoms_local.argtypes = [vp, _dp]
+    L.orc_scene_create.restype = vp
+    L.orc_scene_create.argtypes = [vp, C.c_int, _ip, _dp]
+    L.orc_scene_free.argtypes = [vp]
+    L.orc_scene_num_tree_nodes.restype = C.c_int
+    L.orc_scene_num_tree_nodes.argtypes = [vp]
+    L.orc_world_aabbs.argtypes = [vp, C.c_int64, _ip, _dp, _dp]
+    L.orc_scene_candidates.restype = C.c_int64
+    L.orc_scene_candidates.argtypes = [vp, C.c_int64, _ip, _dp, _i64p, _ip, C.c_int64]
+    L.orc_scene_collide.restype = C.c_int64
+    L.orc_scene_collide.argtypes = [vp, C.c_int64, _ip, _dp, C.c_int64, C.c_int, C.c_int, _i64p, _ip, _ip,
+                                    C.c_int64, _i64p]
+    L.orc_scene_distance.argtypes = [vp, C.c_int64, _ip, _dp, C.c_int, C.c_int, _dp, _ip, _ip, _dp, _i64p]
+    L._bp_sig = True
+
+
+class Geoms:
+    """Geometry registry for the broadphase: ids [0, ns) are the shapes of a
+    ShapeSet-like object (type, params, voff, vcnt, verts), ids [ns, ns + nm) the meshes."""
+
+    def __init__(self, shapes=None, meshes=()):
+        L = lib()
+        _bp_sigs(L)
+        if shapes is None:
+            t = np.zeros(0, np.int32); pr = np.zeros((0, 3)); vo = np.zeros(0, np.int32); vc = np.zeros(0, np.int32)
+            vv = np.zeros((1, 3))
+        else:
+            t = np.ascontiguousarray(shapes.type, np.int32)
+            pr = np.ascontiguousarray(shapes.params, np.float64)
+            vo = np.ascontiguousarray(shapes.voff, np.int32)
+            vc = np.ascontiguousarray(shapes.vcnt, np.int32)
+            vv = np.ascontiguousarray(shapes.verts, np.float64).reshape(-1, 3)
+            if vv.shape[0] == 0:
+                vv = np.zeros((1, 3))
+        self._keep = (t, pr, vo, vc, vv, list(meshes))
+        self.ns, self.nm = t.shape[0], len(meshes)
+        mh = (C.c_void_p * max(1, self.nm))(*[m.h for m in meshes])
+        self.h = L.orc_geoms_create(self.ns, _i(t), _d(pr), _i(vo), _i(vc), _d(vv), self.nm, mh)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_geoms_free(self.h)
+            self.h = None
+
+    def local(self):
+        """Per geometry: aabb_local min, max, aabb_center, aabb_radius (10 doubles)."""
+        out = np.zeros((self.ns + self.nm, 10))
+        lib().orc_geoms_local(self.h, _d(out))
+        return out
+
+    def world_aabbs(self, gid, tf):
+        gid = np.ascontiguousarray(gid, np.int32)
+        tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+        out = np.zeros((gid.shape[0], 6))
+        lib().orc_world_aabbs(self.h, gid.shape[0], _i(gid), _d(tf), _d(out))
+        return out
+
+
+class Scene:
+    """A broadphase manager over scene objects (geometry ids + 3x4 poses): the dynamic
+    AABB tree manager (use_tree=True) or the naive one, with FCL's default callbacks."""
+
+    def __init__(self, geoms: Geoms, gid, tf):
+        self.geoms = geoms
+        self.gid = np.ascontiguousarray(gid, np.int32)
+        self.tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+        self.h = lib().orc_scene_create(geoms.h, self.gid.shape[0], _i(self.gid), _d(self.tf))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_scene_free(self.h)
+            self.h = None
+
+    def num_tree_nodes(self) -> int:
+        return int(lib().orc_scene_num_tree_nodes(self.h))
+
+    def candidates(self, qgid, qtf):
+        """Exact AABB-overlap scene objects per query: (counts, flat ids in object order)."""
+        qgid = np.ascontiguousarray(qgid, np.int32)
+        qtf = np.ascontiguousarray(qtf, np.float64).reshape(-1, 12)
+        n = qgid.shape[0]
+        counts = np.zeros(n, np.int64)
+        total = lib().orc_scene_candidates(self.h, n, _i(qgid), _d(qtf), _q(counts), None, 0)
+        ids = np.zeros(max(1, total), np.int32)
+        lib().orc_scene_candidates(self.h, n, _i(qgid), _d(qtf), _q(counts), _i(ids), total)
+        return counts, ids[:total]
+
+    def collide(self, qgid, qtf, max_contacts: int = 1, use_tree: bool = True, nthreads: int = 1):
+        qgid = np.ascontiguousarray(qgid, np.int32)
+        qtf = np.ascontiguousarray(qtf, np.float64).reshape(-1, 12)
+        n = qgid.shape[0]
+        nc = np.zeros(n, np.int64); nh = np.zeros(n, np.int32); calls = np.zeros(n, np.int64)
+        cap = max(1, 64 * n)
+        hits = np.zeros(cap, np.int32)
+        total = lib().orc_scene_collide(self.h, n, _i(qgid), _d(qtf), max_contacts, int(use_tree), nthreads,
+                                        _q(nc), _i(nh), _i(hits), cap, _q(calls))
+        if total > cap:
+            hits = np.zeros(total, np.int32)
+            lib().orc_scene_collide(self.h, n, _i(qgid), _d(qtf), max_contacts, int(use_tree), nthreads,
+                                    _q(nc), _i(nh), _i(hits), total, _q(calls))
+        return dict(num_contacts=nc, num_hits=nh, hits=hits[:total], narrow_calls=calls)
+
+    def distance(self, qgid, qtf, use_tree: bool = True, nthreads: int = 1):
+        qgid = np.ascontiguousarray(qgid, np.int32)
+        qtf = np.ascontiguousarray(qtf, np.float64).reshape(-1, 12)
+        n = qgid.shape[0]
+        out = dict(dist=np.zeros(n), obj=np.zeros(n, np.int32), b12=np.zeros((n, 2), np.int32),
+                   pts=np.zeros((n, 2, 3)), narrow_calls=np.zeros(n, np.int64))
+        lib().orc_scene_distance(self.h, n, _i(qgid), _d(qtf), int(use_tree), nthreads, _d(out["dist"]),
+                                 _i(out["obj"]), _i(out["b12"]), _d(out["pts"]), _q(out["narrow_calls"]))
+        return out
