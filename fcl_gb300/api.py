@@ -584,3 +584,70 @@ class DynamicAABBTreeCollisionManager:
 
     def __del__(self):
         self._release()
+
+
+# ------------------------------------------------------------- request loop ----
+
+class MotionServer:
+    """Continuous-batching loop of motion-checking requests over a resident
+    broadphase scene (fclgpu_server_*).  robot: workloads.Robot-like (axis, offset,
+    link_refs, geom_tf).  submit() queues a request (base 3x4, q (K, L)) and returns
+    its id; wait(id) returns its result dict."""
+
+    def __init__(self, scene: DynamicAABBTreeCollisionManager, robot, max_waypoints_per_step: int = 4096,
+                 memory_budget_bytes: int = 0, precision: str = "fp32", clearance: bool = True):
+        self.scene = scene
+        self.L = int(robot.axis.shape[0])
+        self._axis = np.ascontiguousarray(robot.axis, np.int32)
+        self._off = np.ascontiguousarray(robot.offset, np.float64).reshape(self.L, 3)
+        self._refs = np.ascontiguousarray(robot.link_refs, np.int32).reshape(self.L, 2)
+        self._gtf = np.ascontiguousarray(robot.geom_tf, np.float64).reshape(self.L, 12)
+        desc = N.RobotDesc(self.L, self._axis.ctypes.data, self._off.ctypes.data, self._refs.ctypes.data,
+                           self._gtf.ctypes.data)
+        cfg = N.ServerConfig(max_waypoints_per_step, memory_budget_bytes, _prec(precision), int(clearance))
+        h = C.c_void_p()
+        N.check(N.lib().fclgpu_server_create(scene.handle, C.byref(desc), C.byref(cfg), C.byref(h)),
+                "fclgpu_server_create")
+        self.handle = h
+
+    def submit(self, base, q) -> int:
+        base = np.ascontiguousarray(base, np.float64).reshape(12)
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, self.L)
+        rid = C.c_int64()
+        N.check(N.lib().fclgpu_server_submit(self.handle, base.ctypes.data, q.ctypes.data, q.shape[0],
+                                             C.byref(rid)), "fclgpu_server_submit")
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout_ms: float = -1.0):
+        r = N.MotionResult()
+        rc = N.lib().fclgpu_server_wait(self.handle, rid, timeout_ms, C.byref(r))
+        if rc == N.FCLGPU_ERR_PENDING:
+            return None
+        N.check(rc, "fclgpu_server_wait")
+        return dict(first_colliding_waypoint=r.first_colliding_waypoint, min_clearance=r.min_clearance,
+                    clearance_waypoint=r.clearance_waypoint, clearance_link=r.clearance_link,
+                    clearance_object=r.clearance_object, latency_ms=r.latency_ms, queue_ms=r.queue_ms,
+                    num_steps=r.num_steps)
+
+    def stats(self):
+        s = N.ServerStats()
+        N.check(N.lib().fclgpu_server_get_stats(self.handle, C.byref(s)), "fclgpu_server_get_stats")
+        return {k: getattr(s, k) for k, _ in N.ServerStats._fields_}
+
+    def link_poses(self, base, q) -> np.ndarray:
+        """(K, L, 3, 4) link-geometry poses as the loop computes them."""
+        base = np.ascontiguousarray(base, np.float64).reshape(12)
+        q = np.ascontiguousarray(q, np.float64).reshape(-1, self.L)
+        out = np.zeros((q.shape[0], self.L, 3, 4))
+        N.check(N.lib().fclgpu_server_link_poses(self.handle, base.ctypes.data, q.ctypes.data, q.shape[0],
+                                                 out.ctypes.data), "fclgpu_server_link_poses")
+        return out
+
+    def close(self):
+        h = getattr(self, "handle", None)
+        if h is not None and N._lib is not None:
+            N._lib.fclgpu_server_destroy(h)
+        self.handle = None
+
+    def __del__(self):
+        self.close()

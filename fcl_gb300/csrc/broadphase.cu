@@ -505,8 +505,10 @@ __device__ double pair_upper_bound(const BpSceneView& S, const BpQueryView& Q, i
   const double* tq = Q.tf + 12 * q;
   D3v pa = geom_point(S, go, to);
   D3v pb = geom_point(S, gq, tq);
-  double best = d3len(pa - pb);
-  const D3v dir = pb - pa;
+  const double best = d3len(pa - pb);
+  if (!(best > 0)) return best;
+  // the support functions (minkowski_diff-inl.h:65-265) take unit directions
+  const D3v dir = d3scale(pb - pa, 1.0 / best);
   if (go.kind == GEOM_SHAPE) pa = geom_support(S, go, to, dir);
   if (gq.kind == GEOM_SHAPE) pb = geom_support(S, gq, tq, d3neg(dir));
   return fmin(best, d3len(pa - pb));

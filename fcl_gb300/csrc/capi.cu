@@ -294,6 +294,7 @@ const char* fclgpu_status_string(int status) {
     case FCLGPU_ERR_DEVICE_STATUS: return "kernel reported an internal error";
     case FCLGPU_ERR_NOT_INITIALIZED: return "not initialized";
     case FCLGPU_ERR_UNSUPPORTED: return "unsupported";
+    case FCLGPU_ERR_PENDING: return "request not finished";
     default: return "unknown status";
   }
 }

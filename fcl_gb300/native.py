@@ -73,8 +73,31 @@ class BpDistanceResult(C.Structure):
                 ("nearest_points", C.c_void_p), ("total_candidates", C.c_int64), ("total_node_visits", C.c_int64)]
 
 
+class RobotDesc(C.Structure):
+    _fields_ = [("num_links", C.c_int32), ("joint_axis", C.c_void_p), ("link_offset", C.c_void_p),
+                ("link_geometry", C.c_void_p), ("link_geometry_tf", C.c_void_p)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("max_waypoints_per_step", C.c_int64), ("memory_budget_bytes", C.c_int64),
+                ("precision", C.c_int32), ("compute_clearance", C.c_int32)]
+
+
+class MotionResult(C.Structure):
+    _fields_ = [("first_colliding_waypoint", C.c_int32), ("clearance_waypoint", C.c_int32),
+                ("clearance_link", C.c_int32), ("clearance_object", C.c_int32), ("min_clearance", C.c_double),
+                ("latency_ms", C.c_double), ("queue_ms", C.c_double), ("num_steps", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("waypoints", C.c_int64), ("queries", C.c_int64), ("candidates", C.c_int64),
+                ("busy_ms", C.c_double), ("max_step_waypoints", C.c_int64)]
+
+
 GEOM_SHAPE = 0
 GEOM_MESH = 1
+FCLGPU_ERR_PENDING = -10
 
 _lib = None
 
@@ -117,6 +140,12 @@ _SIGS = {
                                                     C.POINTER(BpDistanceResult), _VP]),
     "fclgpu_broadphase_distance": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
                                              C.POINTER(BpDistanceResult), _VP]),
+    "fclgpu_server_create": (C.c_int, [_VP, C.POINTER(RobotDesc), C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "fclgpu_server_submit": (C.c_int, [_VP, _VP, _VP, C.c_int32, C.POINTER(C.c_int64)]),
+    "fclgpu_server_wait": (C.c_int, [_VP, C.c_int64, C.c_double, C.POINTER(MotionResult)]),
+    "fclgpu_server_get_stats": (C.c_int, [_VP, C.POINTER(ServerStats)]),
+    "fclgpu_server_link_poses": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP]),
+    "fclgpu_server_destroy": (C.c_int, [_VP]),
 }
 
 

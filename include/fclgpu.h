@@ -43,7 +43,8 @@ enum {
   FCLGPU_ERR_STACK_DEPTH = -6,     /* pair of BVHs deeper than the traversal stack */
   FCLGPU_ERR_DEVICE_STATUS = -7,   /* a kernel reported an internal error word */
   FCLGPU_ERR_NOT_INITIALIZED = -8,
-  FCLGPU_ERR_UNSUPPORTED = -9
+  FCLGPU_ERR_UNSUPPORTED = -9,
+  FCLGPU_ERR_PENDING = -10          /* a served request has not finished yet */
 };
 
 FCLGPU_API const char* fclgpu_status_string(int status);
@@ -332,6 +333,73 @@ FCLGPU_API int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fcl
 FCLGPU_API int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
                                           const double* tf, const fclgpu_broadphase_distance_request* req,
                                           fclgpu_broadphase_distance_result* res, void* stream);
+
+/* ---- motion-checking request loop --------------------------------------------------
+ * No counterpart in FCL: a serving loop over a resident broadphase scene.  A request
+ * is a serial robot swept along K waypoints; each link geometry at each waypoint is
+ * one broadphase query (manager.collide with num_max_contacts = 1 and, when
+ * clearance is on, manager.distance).  The loop runs on its own thread and stream:
+ * requests are queued by fclgpu_server_submit from any thread, admitted into the
+ * next step while the step's estimated device footprint fits the free-memory budget,
+ * and processed in waypoint chunks shared fairly among the admitted requests, so
+ * requests arriving while others run join the next launch (continuous batching).
+ * A request's result depends only on its own queries. */
+typedef struct {
+  int32_t num_links;
+  const int32_t* joint_axis;                 /* per link: 0 = x, 1 = y, 2 = z of the previous link frame */
+  const double* link_offset;                 /* per link: 3 doubles, the link's translation after its joint */
+  const fclgpu_geometry_ref* link_geometry;  /* per link: geometry in the scene's registry */
+  const double* link_geometry_tf;            /* per link: 12 doubles, geometry pose in the joint frame */
+} fclgpu_robot_desc;
+
+typedef struct {
+  int64_t max_waypoints_per_step; /* 0 = 4096 */
+  int64_t memory_budget_bytes;    /* 0 = half of the free device memory, read at every step */
+  int32_t precision;              /* mesh-mesh narrowphase form */
+  int32_t compute_clearance;      /* 1 = also report the minimum clearance */
+} fclgpu_server_config;
+
+typedef struct {
+  int32_t first_colliding_waypoint; /* smallest waypoint with any link in collision, -1 if none */
+  int32_t clearance_waypoint;       /* argmin of the clearance (ties: smallest waypoint, then link) */
+  int32_t clearance_link;
+  int32_t clearance_object;
+  double min_clearance;             /* min over waypoints and links of the broadphase distance (<= 0 in contact) */
+  double latency_ms;                /* submit -> result ready */
+  double queue_ms;                  /* submit -> first step that included the request */
+  int32_t num_steps;                /* loop steps that processed its waypoints */
+  int32_t reserved;
+} fclgpu_motion_result;
+
+typedef struct {
+  int64_t steps;
+  int64_t waypoints;
+  int64_t queries;
+  int64_t candidates;
+  double busy_ms;          /* wall time spent in steps */
+  int64_t max_step_waypoints;
+} fclgpu_server_stats;
+
+typedef struct fclgpu_server_s* fclgpu_server;
+
+/* The scene must outlive the server.  The robot description is copied. */
+FCLGPU_API int fclgpu_server_create(fclgpu_broadphase scene, const fclgpu_robot_desc* robot,
+                                    const fclgpu_server_config* cfg, fclgpu_server* out);
+/* Queues a request: base pose (12 doubles) and num_waypoints x num_links joint angles
+ * (host arrays, copied).  Thread-safe; returns at once with the request id. */
+FCLGPU_API int fclgpu_server_submit(fclgpu_server srv, const double* base_tf, const double* q,
+                                    int32_t num_waypoints, int64_t* request_id);
+/* Waits up to timeout_ms (< 0: forever) for a request; FCLGPU_OK fills *out and
+ * retires the id, FCLGPU_ERR_PENDING means it has not finished. */
+FCLGPU_API int fclgpu_server_wait(fclgpu_server srv, int64_t request_id, double timeout_ms,
+                                  fclgpu_motion_result* out);
+FCLGPU_API int fclgpu_server_get_stats(fclgpu_server srv, fclgpu_server_stats* out);
+/* The link-geometry poses the loop computes for one request (num_waypoints x
+ * num_links x 12 doubles, host), for checking results against another engine. */
+FCLGPU_API int fclgpu_server_link_poses(fclgpu_server srv, const double* base_tf, const double* q,
+                                        int32_t num_waypoints, double* out_tf);
+/* Stops the loop after its current step; unfinished requests are dropped. */
+FCLGPU_API int fclgpu_server_destroy(fclgpu_server srv);
 
 #ifdef __cplusplus
 }

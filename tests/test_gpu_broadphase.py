@@ -53,7 +53,7 @@ def _check_distance(mgr, S, qrefs, qtf, gid_q):
 
 
 def test_broadphase_shapes_match_oracle(gpu_lib):
-    shapes, refs, tf, qrefs, qtf = _shape_scene(4000, 3000, 11)
+    shapes, refs, tf, qrefs, qtf = _shape_scene(4000, 3000, 11, box=14.0)
     ss = api.ShapeSet.from_workload(shapes)
     mgr = api.DynamicAABBTreeCollisionManager(ss)
     mgr.registerObjects(refs, tf)
@@ -64,7 +64,7 @@ def test_broadphase_shapes_match_oracle(gpu_lib):
     g = _check_collide(mgr, S, qrefs, qtf, qrefs[:, 1])
     counts, _ = S.candidates(qrefs[:, 1], qtf)
     assert g["total_candidates"] == counts.sum()
-    assert 0.2 < (g["num_contacts"] > 0).mean() < 0.95
+    assert 0.2 < (g["num_contacts"] > 0).mean() < 0.99
     _check_distance(mgr, S, qrefs, qtf, qrefs[:, 1])
 
 

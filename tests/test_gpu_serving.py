@@ -1,0 +1,61 @@
+"""The motion-checking request loop: per-request results against the oracle's broadphase
+managers, and the same result alone as in a mix of concurrent requests."""
+import numpy as np
+import pytest
+
+from fcl_gb300 import api
+from fcl_gb300 import workloads as W
+from oracle import pyoracle as P
+
+pytestmark = pytest.mark.gpu
+
+REL, ABS = 1e-6, 1e-9
+
+
+def _expected(S, robot, poses):
+    """First colliding waypoint and clearance from per-query oracle results."""
+    K, L = poses.shape[:2]
+    qg = np.tile(robot.link_refs[:, 1], K).astype(np.int32)
+    tf = poses.reshape(K * L, 12)
+    c = S.collide(qg, tf, max_contacts=1, use_tree=True, nthreads=8)
+    d = S.distance(qg, tf, use_tree=True, nthreads=8)
+    hit = (c["num_contacts"].reshape(K, L) > 0).any(1)
+    first = int(np.argmax(hit)) if hit.any() else -1
+    dist = d["dist"].reshape(K, L)
+    k, i = np.unravel_index(np.argmin(dist), dist.shape)  # first minimum in (waypoint, link) order
+    return first, float(dist[k, i]), int(k), int(i)
+
+
+def test_serving_matches_oracle_alone_and_in_mix(gpu_lib):
+    w = W.scene4(n_objects=3000, seed=4, box=12.0, n_shape_geoms=256, mesh_fraction=0.0, mesh_links=False)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    mgr = api.DynamicAABBTreeCollisionManager(ss)
+    mgr.registerObjects(w.refs, w.tf)
+    reqs = W.motion_requests(w, 10, seed=6, k_lo=10, k_hi=60)
+    srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=64)
+    G = P.Geoms(w.shapes)
+    S = P.Scene(G, w.refs[:, 1], w.tf)
+    # link poses: the loop's forward kinematics agrees with the numpy definition
+    poses = [srv.link_poses(r.base, r.q) for r in reqs]
+    for r, p in zip(reqs, poses):
+        np.testing.assert_allclose(p, W.robot_fk(w.robot, r.base, r.q), rtol=0, atol=1e-12)
+    exp = [_expected(S, w.robot, p) for p in poses]
+    # all requests in flight together (chunks of different requests share steps)
+    ids = [srv.submit(r.base, r.q) for r in reqs]
+    mix = [srv.wait(i) for i in ids]
+    assert srv.stats()["steps"] < sum(r.q.shape[0] for r in reqs) / 8
+    for (first, clr, k, i), got in zip(exp, mix):
+        assert got["first_colliding_waypoint"] == first
+        if clr > 0:
+            assert abs(got["min_clearance"] - clr) <= max(REL * abs(clr), ABS)
+            assert (got["clearance_waypoint"], got["clearance_link"]) == (k, i)
+        else:
+            assert got["min_clearance"] <= 0
+    assert any(e[0] >= 0 for e in exp) and any(e[0] < 0 for e in exp)
+    # each request alone returns what it returned in the mix
+    for r, m in zip(reqs[:4], mix[:4]):
+        alone = srv.wait(srv.submit(r.base, r.q))
+        for key in ("first_colliding_waypoint", "min_clearance", "clearance_waypoint", "clearance_link",
+                    "clearance_object"):
+            assert alone[key] == m[key], key
+    srv.close()
