@@ -234,7 +234,11 @@ int64_t narrow_collide(const BpObject& o1, const BpObject& o2, int64_t max_conta
     std::vector<int> contacts;
     return (int64_t)collide_mesh(*g1.mesh, o1.tf, *g2.mesh, o2.tf, (size_t)(max_contacts - cur), contacts, nullptr);
   }
-  return 0;  // mesh-shape pairs are not part of this oracle
+  // BVHShapeCollider; a shape first is swapped to mesh first (collision-inl.h:100-111)
+  const BpObject& om = g1.kind == 1 ? o1 : o2;
+  const BpObject& os = g1.kind == 1 ? o2 : o1;
+  return (int64_t)collide_mesh_shape(*om.geom->mesh, om.tf, os.geom->shape, os.tf, (size_t)(max_contacts - cur),
+                                     nullptr, nullptr);
 }
 
 // fcl::distance(o1, o2, request, result) accumulating into one DistanceResult:
@@ -260,9 +264,16 @@ void narrow_distance(const BpObject& o1, int obj_index, const BpObject& o2, BpDi
     }
     return;
   }
-  if (g1.kind == 1 && g2.kind == 1) {
+  {
     DistanceOut d;
-    distance_mesh(*g1.mesh, o1.tf, *g2.mesh, o2.tf, true, d, nullptr);
+    if (g1.kind == 1 && g2.kind == 1) {
+      distance_mesh(*g1.mesh, o1.tf, *g2.mesh, o2.tf, true, d, nullptr);
+    } else {
+      // BVHShapeDistancer; a shape first is swapped to mesh first (distance-inl.h:117-126)
+      const BpObject& om = g1.kind == 1 ? o1 : o2;
+      const BpObject& os = g1.kind == 1 ? o2 : o1;
+      distance_mesh_shape(*om.geom->mesh, om.tf, os.geom->shape, os.tf, d, nullptr);
+    }
     if (out.min_distance > d.min_distance) {
       out.min_distance = d.min_distance;
       out.object = obj_index;

@@ -9,6 +9,7 @@
 #include <vector>
 #include "oracle_gjk.h"
 #include "oracle_mesh.h"
+#include "oracle_meshshape.h"
 
 namespace oracle {
 

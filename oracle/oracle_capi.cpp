@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "oracle_broadphase.h"
+#include "oracle_meshshape.h"
 #include "oracle_mesh.h"
 
 using namespace oracle;
@@ -510,6 +511,81 @@ void orc_scene_distance(void* h, int64_t nq, const int* qgid, const double* qtf,
       }
     if (narrow_calls) narrow_calls[q] = o.narrow_calls;
   });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// fcl::collide / fcl::distance of one mesh against a convex shape per query: mesh
+// handle h, shape ids into the registry g, poses tfm (mesh) and tfs (shape).  Outputs
+// per query: collide -> counts (contacts, at most max_contacts); distance -> dist,
+// tri (b1), pts (mesh point, shape point: 6 doubles).  nbv / nleaf optional.
+void orc_mesh_shape_batch(void* h, void* g, int64_t n, const int* sid, const double* tfm, const double* tfs,
+                          int64_t max_contacts, int mode, int nthreads, int64_t* counts, double* dist, int* tri,
+                          double* pts, int64_t* nbv, int64_t* nleaf) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  const OrcGeoms* G = static_cast<OrcGeoms*>(g);
+  parallel_for(n, nthreads, [&](int64_t q, int) {
+    const Shape& s = G->g[sid[q]].shape;
+    const Tf a = load_tf(tfm + 12 * q), b = load_tf(tfs + 12 * q);
+    CollideStats st;
+    if (mode == 0) {
+      counts[q] = (int64_t)collide_mesh_shape(*m, a, s, b, (size_t)max_contacts, nullptr, &st);
+    } else {
+      DistanceOut o;
+      distance_mesh_shape(*m, a, s, b, o, &st);
+      dist[q] = o.min_distance;
+      tri[q] = o.b1;
+      for (int k = 0; k < 3; ++k) {
+        pts[6 * q + k] = o.p1[k];
+        pts[6 * q + 3 + k] = o.p2[k];
+      }
+    }
+    if (nbv) nbv[q] = st.num_bv_tests;
+    if (nleaf) nleaf[q] = st.num_leaf_tests;
+  });
+}
+
+// Brute force over every triangle of the mesh (for the traversal tests): collide ->
+// number of intersecting triangles; distance -> min over triangles.
+void orc_mesh_shape_brute(void* h, void* g, int sid, const double* tfm, const double* tfs, int64_t* count,
+                          double* dist) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  const OrcGeoms* G = static_cast<OrcGeoms*>(g);
+  const Shape& s = G->g[sid].shape;
+  const Tf a = load_tf(tfm), b = load_tf(tfs);
+  int64_t c = 0;
+  double best = std::numeric_limits<double>::max();
+  for (const Tri& t : m->tris) {
+    const V3 &p1 = m->verts[t.v[0]], &p2 = m->verts[t.v[1]], &p3 = m->verts[t.v[2]];
+    if (shape_triangle_intersect(s, b, p1, p2, p3, a)) ++c;
+    double d;
+    V3 ps, pt;
+    shape_triangle_distance(s, b, p1, p2, p3, a, d, ps, pt);
+    if (d < best) best = d;
+  }
+  *count = c;
+  *dist = best;
+}
+
+// computeBV<OBBRSS>(shape, tf): obb axis (9, row-major), To, extent, rss axis, To, l[2], r (30).
+void orc_shape_obbrss(void* g, int sid, const double* tf, double* out30) {
+  const OrcGeoms* G = static_cast<OrcGeoms*>(g);
+  OBB o;
+  RSS r;
+  shape_obbrss(G->g[sid].shape, load_tf(tf), o, r);
+  int k = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out30[k++] = o.axis(i, j);
+  for (int i = 0; i < 3; ++i) out30[k++] = o.To[i];
+  for (int i = 0; i < 3; ++i) out30[k++] = o.extent[i];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out30[k++] = r.axis(i, j);
+  for (int i = 0; i < 3; ++i) out30[k++] = r.To[i];
+  out30[k++] = r.l[0];
+  out30[k++] = r.l[1];
+  out30[k++] = r.r;
 }
 
 }  // extern "C"

@@ -69,6 +69,13 @@ V3 get_support(const Shape& s, const V3& dir) {
       }
       return bestv;
     }
+    case SH_TRIANGLE: {  // TriangleP (minkowski_diff-inl.h:78-97)
+      const double dota = dot(dir, s.verts[0]);
+      const double dotb = dot(dir, s.verts[1]);
+      const double dotc = dot(dir, s.verts[2]);
+      if (dota > dotb) return (dotc > dota) ? s.verts[2] : s.verts[0];
+      return (dotc > dotb) ? s.verts[2] : s.verts[1];
+    }
   }
   return mk(0, 0, 0);
 }

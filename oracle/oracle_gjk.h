@@ -9,7 +9,8 @@ namespace oracle {
 
 // geometry/shape/*.h (Box side, Sphere radius, Capsule/Cylinder/Cone radius + lz,
 // Convex vertex list)
-enum ShapeType { SH_BOX = 0, SH_SPHERE = 1, SH_CAPSULE = 2, SH_CYLINDER = 3, SH_CONE = 4, SH_CONVEX = 5 };
+enum ShapeType { SH_BOX = 0, SH_SPHERE = 1, SH_CAPSULE = 2, SH_CYLINDER = 3, SH_CONE = 4, SH_CONVEX = 5,
+                 SH_TRIANGLE = 6 /* TriangleP: verts[0..2], used by the mesh-shape leaves */ };
 
 struct Shape {
   int type;

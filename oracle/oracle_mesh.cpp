@@ -43,7 +43,7 @@ static void covariance(const Mesh& m, const unsigned* idx, int n, M3& M) {
 
 // math/geometry-inl.h:477-558 (eigen_old: cyclic Jacobi); vout = v^T, i.e. column k
 // of vout is row k of v.
-static void eigen_old(const M3& m, V3& dout, M3& vout) {
+void eigen_old(const M3& m, V3& dout, M3& vout) {
   M3 R = m;
   const int n = 3;
   int j, iq, ip, i;
@@ -129,7 +129,7 @@ static void eigen_old(const M3& m, V3& dout, M3& vout) {
 }
 
 // math/geometry-inl.h:563-598
-static void axis_from_eigen(const M3& eigenV, const V3& eigenS, M3& axis) {
+void axis_from_eigen(const M3& eigenV, const V3& eigenS, M3& axis) {
   int mn, mid, mx;
   if (eigenS[0] > eigenS[1]) { mx = 0; mn = 1; }
   else { mn = 0; mx = 1; }
@@ -165,7 +165,7 @@ static void extent_and_center(const Mesh& m, const unsigned* idx, int n, const M
 
 // math/geometry-inl.h:709-990 (getRadiusAndOriginAndRectangleSize) over an already
 // projected point list P (P[i] = (axis.col(k).dot(p))_k).
-static void rss_from_projected(const std::vector<V3>& P, const M3& axis, V3& origin, double l[2],
+void rss_from_projected(const std::vector<V3>& P, const M3& axis, V3& origin, double l[2],
                                double& r) {
   const int size_P = (int)P.size();
   double minx, maxx, miny, maxy, minz, maxz;

@@ -84,4 +84,10 @@ struct DistanceOut {
 double distance_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
                      bool nearest_points, DistanceOut& out, CollideStats* st);
 
+// --- fit helpers shared with the mesh-shape oracle ---------------------------------
+void eigen_old(const M3& m, V3& dout, M3& vout);                            // math/geometry-inl.h:477-558
+void axis_from_eigen(const M3& eigenV, const V3& eigenS, M3& axis);          // math/geometry-inl.h:294-318
+void rss_from_projected(const std::vector<V3>& P, const M3& axis, V3& origin, double l[2],
+                        double& r);                                          // math/geometry-inl.h:709-990
+
 }  // namespace oracle

@@ -354,3 +354,63 @@ class Scene:
         lib().orc_scene_distance(self.h, n, _i(qgid), _d(qtf), int(use_tree), nthreads, _d(out["dist"]),
                                  _i(out["obj"]), _i(out["b12"]), _d(out["pts"]), _q(out["narrow_calls"]))
         return out
+
+
+# ------------------------------------------------------------------ mesh-shape ----
+
+def _ms_sigs(L):
+    if getattr(L, "_ms_sig", False):
+        return
+    vp = C.c_void_p
+    L.orc_mesh_shape_batch.argtypes = [vp, vp, C.c_int64, _ip, _dp, _dp, C.c_int64, C.c_int, C.c_int, _i64p, _dp,
+                                       _ip, _dp, _i64p, _i64p]
+    L.orc_mesh_shape_brute.argtypes = [vp, vp, C.c_int, _dp, _dp, _i64p, _dp]
+    L.orc_shape_obbrss.argtypes = [vp, C.c_int, _dp, _dp]
+    L._ms_sig = True
+
+
+def mesh_shape_collide(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, max_contacts: int = 1, nthreads: int = 1):
+    """fcl::collide(mesh, shape) per query -> (counts, num_bv_tests, num_leaf_tests)."""
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    sid = np.ascontiguousarray(sid, np.int32)
+    n = sid.shape[0]
+    tfm = np.ascontiguousarray(tfm, np.float64).reshape(n, 12)
+    tfs = np.ascontiguousarray(tfs, np.float64).reshape(n, 12)
+    counts = np.zeros(n, np.int64); nbv = np.zeros(n, np.int64); nleaf = np.zeros(n, np.int64)
+    dummy_d = np.zeros(1); dummy_i = np.zeros(1, np.int32)
+    L.orc_mesh_shape_batch(mesh.h, geoms.h, n, _i(sid), _d(tfm), _d(tfs), max_contacts, 0, nthreads, _q(counts),
+                           _d(dummy_d), _i(dummy_i), _d(dummy_d), _q(nbv), _q(nleaf))
+    return counts, nbv, nleaf
+
+
+def mesh_shape_distance(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, nthreads: int = 1):
+    """fcl::distance(mesh, shape) per query -> dict(dist, tri, pts (n,2,3), nbv, nleaf)."""
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    sid = np.ascontiguousarray(sid, np.int32)
+    n = sid.shape[0]
+    tfm = np.ascontiguousarray(tfm, np.float64).reshape(n, 12)
+    tfs = np.ascontiguousarray(tfs, np.float64).reshape(n, 12)
+    out = dict(dist=np.zeros(n), tri=np.zeros(n, np.int32), pts=np.zeros((n, 2, 3)), nbv=np.zeros(n, np.int64),
+               nleaf=np.zeros(n, np.int64))
+    dummy = np.zeros(1, np.int64)
+    L.orc_mesh_shape_batch(mesh.h, geoms.h, n, _i(sid), _d(tfm), _d(tfs), 0, 1, nthreads, _q(dummy),
+                           _d(out["dist"]), _i(out["tri"]), _d(out["pts"]), _q(out["nbv"]), _q(out["nleaf"]))
+    return out
+
+
+def mesh_shape_brute(mesh: Mesh, geoms: Geoms, sid: int, tfm, tfs):
+    """(number of intersecting triangles, min triangle distance) over every triangle."""
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    tfm = np.ascontiguousarray(tfm, np.float64).reshape(12)
+    tfs = np.ascontiguousarray(tfs, np.float64).reshape(12)
+    c = C.c_int64(); d = C.c_double()
+    L.orc_mesh_shape_brute(mesh.h, geoms.h, sid, _d(tfm), _d(tfs), C.byref(c), C.byref(d))
+    return int(c.value), float(d.value)
+
+
+def shape_obbrss(geoms: Geoms, sid: int, tf):
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    tf = np.ascontiguousarray(tf, np.float64).reshape(12)
+    out = np.zeros(30)
+    L.orc_shape_obbrss(geoms.h, sid, _d(tf), _d(out))
+    return out

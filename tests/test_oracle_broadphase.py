@@ -111,3 +111,28 @@ def test_candidates_are_exact_aabb_overlaps():
     for q in range(50):
         ov = ~((A[:, :3] > Q[q, 3:]).any(1) | (A[:, 3:] < Q[q, :3]).any(1))
         np.testing.assert_array_equal(np.nonzero(ov)[0], seg[q])
+
+
+def test_tree_manager_matches_naive_manager_mixed():
+    shapes = W.random_shapes(32, 12)
+    meshes = [P.Mesh(*W.perturbed_ellipsoid(4, (0.6, 0.4, 0.3), 0.01, k)) for k in range(2)]
+    G = P.Geoms(shapes, meshes)
+    rng = np.random.default_rng(13)
+    n = 120
+    gid = np.where(rng.uniform(size=n) < 0.3, 32 + rng.integers(0, 2, size=n), rng.integers(0, 32, size=n))
+    gid = gid.astype(np.int32)
+    tf = W.random_poses(n, 0.0, 4.0, 14)
+    S = P.Scene(G, gid, tf)
+    qg = np.where(rng.uniform(size=60) < 0.5, 32 + rng.integers(0, 2, size=60), rng.integers(0, 32, size=60))
+    qg = qg.astype(np.int32)
+    qtf = W.random_poses(60, 0.0, 4.0, 15)
+    for M in (1, 100000):
+        a = S.collide(qg, qtf, max_contacts=M, use_tree=True)
+        b = S.collide(qg, qtf, max_contacts=M, use_tree=False)
+        np.testing.assert_array_equal(a["num_contacts"], b["num_contacts"])
+    assert (a["num_contacts"] > 0).any()
+    da = S.distance(qg, qtf, use_tree=True)
+    db = S.distance(qg, qtf, use_tree=False)
+    sep = db["dist"] > 0
+    np.testing.assert_array_equal(da["dist"] <= 0, db["dist"] <= 0)
+    np.testing.assert_array_equal(da["dist"][sep], db["dist"][sep])
