@@ -651,3 +651,31 @@ class MotionServer:
 
     def __del__(self):
         self.close()
+
+
+# ---------------------------------------------------------------- mesh x shape ----
+
+def mesh_shape_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_shape, mode: str = "collide",
+                     num_max_contacts: int = 1, statistics: bool = False, stream=None):
+    """fcl::collide / fcl::distance of BVHModel<OBBRSS> meshes against convex shapes,
+    one (mesh, shape) pair per row.  mode "collide" -> counts; "distance" ->
+    min_distance, tri, nearest_points (mesh point, shape point).  Host numpy inputs."""
+    hs = _handles(meshes)
+    m = 0 if mode == "collide" else 1
+    mesh_idx = np.ascontiguousarray(mesh_idx, np.int32)
+    shape_idx = np.ascontiguousarray(shape_idx, np.int32)
+    n = mesh_idx.shape[0]
+    tf_mesh = np.ascontiguousarray(tf_mesh, np.float64).reshape(n, 12)
+    tf_shape = np.ascontiguousarray(tf_shape, np.float64).reshape(n, 12)
+    out = dict(counts=np.zeros(n, np.int32), min_distance=np.zeros(n), tri=np.zeros(n, np.int32),
+               nearest_points=np.zeros((n, 2, 3)), num_bv_tests=np.zeros(n, np.int64),
+               num_leaf_tests=np.zeros(n, np.int64))
+    req = N.MeshShapeRequest(m, 0, num_max_contacts)
+    res = N.MeshShapeResult(out["counts"].ctypes.data, out["min_distance"].ctypes.data, out["tri"].ctypes.data,
+                            out["nearest_points"].ctypes.data,
+                            out["num_bv_tests"].ctypes.data if statistics else None,
+                            out["num_leaf_tests"].ctypes.data if statistics else None)
+    N.check(N.lib().fclgpu_mesh_shape_batch(hs, len(meshes), shapes.handle, n, mesh_idx.ctypes.data,
+                                            shape_idx.ctypes.data, tf_mesh.ctypes.data, tf_shape.ctypes.data,
+                                            C.byref(req), C.byref(res), stream), "fclgpu_mesh_shape_batch")
+    return out

@@ -657,6 +657,38 @@ __global__ void k_bp_gather_mesh(BpSceneView S, BpQueryView Q, const int2* pairs
   }
 }
 
+__global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pairs, const int64_t* list, long long nl,
+                                  int32_t* mesh_idx, int32_t* shape_idx, double* tfm, double* tfs) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
+    const int2 p = pairs[list[j]];
+    const GeomRec& go = S.geoms[S.gid[p.y]];
+    const GeomRec& gq = S.geoms[Q.gid[p.x]];
+    const bool obj_is_mesh = go.kind == GEOM_MESH;
+    mesh_idx[j] = obj_is_mesh ? go.index : gq.index;
+    shape_idx[j] = obj_is_mesh ? gq.index : go.index;
+    const double* a = obj_is_mesh ? S.tf + 12 * (long long)p.y : Q.tf + 12 * (long long)p.x;
+    const double* b = obj_is_mesh ? Q.tf + 12 * (long long)p.x : S.tf + 12 * (long long)p.y;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      tfm[12 * j + k] = a[k];
+      tfs[12 * j + k] = b[k];
+    }
+  }
+}
+
+__global__ void k_bp_scatter_mixed_dist(const int64_t* list, long long nl, const double* d, const int32_t* tri,
+                                        const double* pts, double* dist, int32_t* b12, double* outpts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
+    const long long i = list[j];
+    dist[i] = d[j];
+    b12[2 * i] = tri[j];
+    b12[2 * i + 1] = -1;
+    for (int k = 0; k < 6; ++k) outpts[6 * i + k] = pts[6 * j + k];
+  }
+}
+
 __global__ void k_bp_scatter_hits(const int64_t* list, long long nl, const int32_t* counts, int32_t* hit) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) hit[list[j]] = counts[j];
@@ -842,6 +874,24 @@ cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, int64_t
                            cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_bp_list<<<grid_for(n, 256), 256, 0, s>>>(kind, n, want, list, count);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
+                                   const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
+                                   double* tfm, double* tfs, cudaStream_t s) {
+  if (nlist <= 0) return cudaSuccess;
+  k_bp_gather_mixed<<<grid_for(nlist, 256), 256, 0, s>>>(S, Q, pairs, list, nlist, mesh_idx, shape_idx, tfm, tfs);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_scatter_mixed_dist(const int64_t* list, int64_t nlist, const double* d, const int32_t* tri,
+                                         const double* pts, double* dist, int32_t* b12, double* outpts,
+                                         cudaStream_t s) {
+  if (nlist <= 0) return cudaSuccess;
+  k_bp_scatter_mixed_dist<<<grid_for(nlist, 256), 256, 0, s>>>(list, nlist, d, tri, pts, dist, b12, outpts);
   ++g_kernel_launches;
   return cudaGetLastError();
 }

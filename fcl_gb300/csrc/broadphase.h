@@ -111,6 +111,15 @@ cudaError_t launch_bp_gather_mesh(const BpSceneView& S, const BpQueryView& Q, co
                                   double* tf2, cudaStream_t s);
 cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, int64_t* list, unsigned long long* count,
                            cudaStream_t s);
+// Mixed pairs (kind 2): FCL calls BVH-shape with the mesh first whichever object is
+// the mesh (collision-inl.h:100-111, distance-inl.h:117-126); gather (mesh, shape)
+// indices and poses in that order.
+cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
+                                   const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
+                                   double* tfm, double* tfs, cudaStream_t s);
+cudaError_t launch_bp_scatter_mixed_dist(const int64_t* list, int64_t nlist, const double* d, const int32_t* tri,
+                                         const double* pts, double* dist, int32_t* b12, double* outpts,
+                                         cudaStream_t s);
 // Scatter mesh results back to candidate slots.
 cudaError_t launch_bp_scatter_hits(const int64_t* list, int64_t nlist, const int32_t* counts, int32_t* hit,
                                    cudaStream_t s);

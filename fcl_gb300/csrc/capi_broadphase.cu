@@ -15,6 +15,7 @@
 #include "broadphase.h"
 #include "kernels.h"
 #include "mesh_handle.h"
+#include "mesh_shape.h"
 #include "shape_pair.cuh"
 #include "shapeset_handle.h"
 
@@ -32,6 +33,8 @@ struct fclgpu_broadphase_s {
   float* aabb32 = nullptr;
   BpNode* nodes = nullptr;
   void* build_scratch = nullptr;
+  DevMesh* dmeshes = nullptr;  // device table of the meshes, for mesh-shape pairs
+  int max_depth = 0;
 };
 
 namespace {
@@ -81,6 +84,7 @@ struct BpScratch {
   Buf ctr, qgid, q64, q32, counts, offsets, scan_tmp, ub;
   Buf pairs, kind, hit, dist, b12, pts, list;
   Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
+  Buf x_midx, x_sidx, x_counts, x_tri;
   Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
 };
 BpScratch g_bs;
@@ -178,7 +182,7 @@ int rebuild(fclgpu_broadphase_s* bp, cudaStream_t s) {
 
 void free_bp(fclgpu_broadphase_s* bp) {
   for (void* p : {(void*)bp->geoms, (void*)bp->gid, (void*)bp->tf, (void*)bp->aabb64, (void*)bp->aabb32,
-                  (void*)bp->nodes, bp->build_scratch})
+                  (void*)bp->nodes, bp->build_scratch, (void*)bp->dmeshes})
     if (p) cudaFree(p);
   delete bp;
 }
@@ -238,6 +242,56 @@ int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cud
   CKB(cudaMemcpyAsync(&c, &dctr->list_count, 8, cudaMemcpyDeviceToHost, s), "list");
   CKB(cudaStreamSynchronize(s), "list");
   *nlist = (int64_t)c;
+  return FCLGPU_OK;
+}
+
+// Mesh-shape candidates (kind 2): BVH-shape collide (mode 0, contacts into hit) or
+// distance (mode 1, into the distance slots), mesh first as FCL calls it.
+int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQueryView& Q, int64_t total, int mode,
+              int64_t max_contacts, BpCounters* dctr, cudaStream_t s) {
+  int64_t nl = 0;
+  RCB(list_kind(total, 2, dctr, &nl, s));
+  if (nl == 0) return FCLGPU_OK;
+  if (!bp->shapes || !bp->dmeshes) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "mesh-shape pair without registry");
+  CKB(g_bs.x_midx.ensure(4 * nl), "mixed scratch");
+  CKB(g_bs.x_sidx.ensure(4 * nl), "mixed scratch");
+  CKB(g_bs.m_tf1.ensure(96 * nl), "mixed scratch");
+  CKB(g_bs.m_tf2.ensure(96 * nl), "mixed scratch");
+  CKB(g_bs.x_counts.ensure(4 * nl), "mixed scratch");
+  CKB(g_bs.m_dist.ensure(8 * nl), "mixed scratch");
+  CKB(g_bs.x_tri.ensure(4 * nl), "mixed scratch");
+  CKB(g_bs.m_pts.ensure(48 * nl), "mixed scratch");
+  CKB(launch_bp_gather_mixed(S, Q, g_bs.pairs.as<int2>(), g_bs.list.as<int64_t>(), nl, g_bs.x_midx.as<int32_t>(),
+                             g_bs.x_sidx.as<int32_t>(), g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
+      "mixed gather");
+  MeshShapeLaunch L;
+  L.meshes = bp->dmeshes;
+  L.shapes = bp->shapes->shapes;
+  L.sverts = bp->shapes->verts;
+  L.n = nl;
+  L.mesh_idx = g_bs.x_midx.as<int32_t>();
+  L.shape_idx = g_bs.x_sidx.as<int32_t>();
+  L.tfm = g_bs.m_tf1.as<double>();
+  L.tfs = g_bs.m_tf2.as<double>();
+  L.mode = mode;
+  L.max_contacts = (int32_t)std::min<int64_t>(max_contacts, INT32_MAX);
+  L.counts = g_bs.x_counts.as<int32_t>();
+  L.dist = g_bs.m_dist.as<double>();
+  L.tri = g_bs.x_tri.as<int32_t>();
+  L.pts = g_bs.m_pts.as<double>();
+  L.nbv = nullptr;
+  L.nleaf = nullptr;
+  L.status = &dctr->status;
+  CKB(launch_mesh_shape(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+  if (mode == 0) {
+    CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.x_counts.as<int32_t>(), g_bs.hit.as<int32_t>(), s),
+        "mixed scatter");
+  } else {
+    CKB(launch_bp_scatter_mixed_dist(g_bs.list.as<int64_t>(), nl, g_bs.m_dist.as<double>(), g_bs.x_tri.as<int32_t>(),
+                                     g_bs.m_pts.as<double>(), g_bs.dist.as<double>(), g_bs.b12.as<int32_t>(),
+                                     g_bs.pts.as<double>(), s),
+        "mixed scatter");
+  }
   return FCLGPU_OK;
 }
 
@@ -310,6 +364,16 @@ int fclgpu_broadphase_create(fclgpu_shapeset shapes, const fclgpu_mesh* meshes, 
     e = cudaMemcpy(bp->geoms, geoms.data(), sizeof(GeomRec) * geoms.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && num_objects > 0) e = cudaMemcpy(bp->gid, gid.data(), 4 * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && num_objects > 0) e = cudaMemcpy(bp->tf, tf, 96 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && num_meshes > 0) {
+    std::vector<DevMesh> table(num_meshes);
+    for (int32_t i = 0; i < num_meshes; ++i) {
+      table[i] = meshes[i]->dev;
+      bp->max_depth = std::max(bp->max_depth, (int)meshes[i]->dev.max_depth);
+    }
+    e = cudaMalloc(&bp->dmeshes, sizeof(DevMesh) * num_meshes);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(bp->dmeshes, table.data(), sizeof(DevMesh) * num_meshes, cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     free_bp(bp);
     return bp_cuda(e, "broadphase upload");
@@ -389,9 +453,7 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
     CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_INTERSECT, hit, nullptr, nullptr,
                                s),
         "shape narrowphase");
-    int64_t nmixed = 0;
-    RCB(list_kind(total, 2, dctr, &nmixed, s));
-    if (nmixed > 0) return bp_fail(FCLGPU_ERR_UNSUPPORTED, "mesh-shape pairs are not supported by the broadphase");
+    RCB(run_mixed(bp, S, Q, total, 0, req->num_max_contacts, dctr, s));
     int64_t nl = 0;
     RCB(list_kind(total, 1, dctr, &nl, s));
     if (nl > 0) {
@@ -467,9 +529,7 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
     CKB(cudaMemsetAsync(b12, 0xff, 8 * (size_t)total, s), "ids");
     CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_DISTANCE, nullptr, dist, pts, s),
         "shape narrowphase");
-    int64_t nmixed = 0;
-    RCB(list_kind(total, 2, dctr, &nmixed, s));
-    if (nmixed > 0) return bp_fail(FCLGPU_ERR_UNSUPPORTED, "mesh-shape pairs are not supported by the broadphase");
+    RCB(run_mixed(bp, S, Q, total, 1, 0, dctr, s));
     int64_t nl = 0;
     RCB(list_kind(total, 1, dctr, &nl, s));
     if (nl > 0) {

@@ -12,7 +12,8 @@
 
 namespace fclgpu {
 
-enum : int { SHAPE_BOX = 0, SHAPE_SPHERE = 1, SHAPE_CAPSULE = 2, SHAPE_CYLINDER = 3, SHAPE_CONE = 4, SHAPE_CONVEX = 5 };
+enum : int { SHAPE_BOX = 0, SHAPE_SPHERE = 1, SHAPE_CAPSULE = 2, SHAPE_CYLINDER = 3, SHAPE_CONE = 4, SHAPE_CONVEX = 5,
+             SHAPE_TRIANGLE = 6 /* TriangleP: 9 doubles at verts + 3 * voff (mesh-shape leaves) */ };
 
 struct DevShape {
   int type;
@@ -90,6 +91,13 @@ FCLG_HD D3v shape_support(const ShapeRef& sh, const D3v& dir) {
         }
       }
       return bestv;
+    }
+    case SHAPE_TRIANGLE: {  // TriangleP (minkowski_diff-inl.h:78-97)
+      const double* V = sh.verts + 3 * (long long)s.voff;
+      const D3v a = v3(V[0], V[1], V[2]), b = v3(V[3], V[4], V[5]), c = v3(V[6], V[7], V[8]);
+      const double dota = dot(dir, a), dotb = dot(dir, b), dotc = dot(dir, c);
+      if (dota > dotb) return (dotc > dota) ? c : a;
+      return (dotc > dotb) ? c : b;
     }
   }
   return v3(0.0, 0.0, 0.0);

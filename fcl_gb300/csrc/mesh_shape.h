@@ -1,0 +1,33 @@
+// Launch interface of the batched mesh-shape kernel (mesh_shape.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fclgpu_types.h"
+#include "gjk_epa.cuh"
+
+namespace fclgpu {
+
+struct MeshShapeLaunch {
+  const DevMesh* meshes;
+  const DevShape* shapes;
+  const double* sverts;
+  int64_t n;
+  const int32_t* mesh_idx;
+  const int32_t* shape_idx;
+  const double* tfm;  // 12 per pair: the mesh's pose
+  const double* tfs;  // 12 per pair: the shape's pose
+  int32_t mode;       // 0 collide, 1 distance
+  int32_t max_contacts;
+  int32_t* counts;
+  double* dist;
+  int32_t* tri;
+  double* pts;        // 6 per pair: point on the mesh, point on the shape
+  int64_t* nbv;
+  int64_t* nleaf;
+  unsigned* status;
+};
+
+cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s);
+
+}  // namespace fclgpu

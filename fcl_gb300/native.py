@@ -95,6 +95,15 @@ class ServerStats(C.Structure):
                 ("busy_ms", C.c_double), ("max_step_waypoints", C.c_int64)]
 
 
+class MeshShapeRequest(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("reserved", C.c_int32), ("num_max_contacts", C.c_int64)]
+
+
+class MeshShapeResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("min_distance", C.c_void_p), ("tri", C.c_void_p),
+                ("nearest_points", C.c_void_p), ("num_bv_tests", C.c_void_p), ("num_leaf_tests", C.c_void_p)]
+
+
 GEOM_SHAPE = 0
 GEOM_MESH = 1
 FCLGPU_ERR_PENDING = -10
@@ -146,6 +155,10 @@ _SIGS = {
     "fclgpu_server_get_stats": (C.c_int, [_VP, C.POINTER(ServerStats)]),
     "fclgpu_server_link_poses": (C.c_int, [_VP, _VP, _VP, C.c_int32, _VP]),
     "fclgpu_server_destroy": (C.c_int, [_VP]),
+    "fclgpu_mesh_shape_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, _VP, _VP, _VP, _VP,
+                                                 C.POINTER(MeshShapeRequest), C.POINTER(MeshShapeResult), _VP]),
+    "fclgpu_mesh_shape_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, _VP, _VP, _VP, _VP,
+                                          C.POINTER(MeshShapeRequest), C.POINTER(MeshShapeResult), _VP]),
 }
 
 

@@ -237,6 +237,49 @@ FCLGPU_API int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t*
 /* Device time (ms) of the most recent shape-pair kernel.  No counterpart in FCL. */
 FCLGPU_API int fclgpu_last_shape_kernel_time(double* ms);
 
+/* ---- mesh x convex shape ------------------------------------------------------------
+ * fcl::collide / fcl::distance of a BVHModel<OBBRSS> against a convex shape with
+ * GJKSolver_indep (narrowphase/detail/collision_func_matrix-inl.h:378-425, 502-523;
+ * distance_func_matrix-inl.h BVHShapeDistancer; traversal nodes
+ * mesh_shape_collision_traversal_node-inl.h and mesh_shape_distance_traversal_node-inl.h):
+ * the shape's OBBRSS is fitted to its bound vertices, the mesh BVH is traversed against
+ * it, and the leaves run shapeTriangleIntersect / shapeTriangleDistance (sphere-triangle
+ * closed forms, GJK/EPA otherwise).  FP64.  Pair i: meshes[mesh_idx[i]] at tf_mesh[i]
+ * and shape shape_idx[i] of the set at tf_shape[i].  (fcl::collide(shape, mesh) is the
+ * same call: FCL swaps the arguments.) */
+enum { FCLGPU_MESH_SHAPE_COLLIDE = 0, FCLGPU_MESH_SHAPE_DISTANCE = 1 };
+
+typedef struct {
+  int32_t mode;              /* FCLGPU_MESH_SHAPE_COLLIDE or _DISTANCE */
+  int32_t reserved;
+  int64_t num_max_contacts;  /* collide: CollisionRequest::num_max_contacts (>= 1) */
+} fclgpu_mesh_shape_request;
+
+/* collide: counts[i] = contacts (<= num_max_contacts).  distance: min_distance[i],
+ * tri[i] = the mesh triangle of the minimum (DistanceResult b1), nearest_points[6i..6i+5]
+ * = the point on the mesh then the point on the shape, in the frames FCL returns them in
+ * (world frame from GJK; for a sphere, the sphere point in the sphere's frame and the
+ * triangle point in the mesh's frame), -1 if the pair intersects.  Statistics optional. */
+typedef struct {
+  int32_t* counts;
+  double* min_distance;
+  int32_t* tri;
+  double* nearest_points;
+  int64_t* num_bv_tests;
+  int64_t* num_leaf_tests;
+} fclgpu_mesh_shape_result;
+
+FCLGPU_API int fclgpu_mesh_shape_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, fclgpu_shapeset shapes,
+                                              int64_t n, const int32_t* mesh_idx, const int32_t* shape_idx,
+                                              const double* tf_mesh, const double* tf_shape,
+                                              const fclgpu_mesh_shape_request* req, fclgpu_mesh_shape_result* res,
+                                              void* stream);
+FCLGPU_API int fclgpu_mesh_shape_batch(const fclgpu_mesh* meshes, int32_t num_meshes, fclgpu_shapeset shapes,
+                                       int64_t n, const int32_t* mesh_idx, const int32_t* shape_idx,
+                                       const double* tf_mesh, const double* tf_shape,
+                                       const fclgpu_mesh_shape_request* req, fclgpu_mesh_shape_result* res,
+                                       void* stream);
+
 /* ---- broadphase -------------------------------------------------------------------
  * Replaces DynamicAABBTreeCollisionManager<double> (broadphase/
  * broadphase_dynamic_AABB_tree.h:56-157, -inl.h:727-1009) behind

@@ -1,0 +1,93 @@
+"""Device BVHModel<OBBRSS> x convex shape (collide and distance) against the FP64
+oracle: same traversal (identical statistics), same results."""
+import numpy as np
+import pytest
+
+from fcl_gb300 import api
+from fcl_gb300 import workloads as W
+from oracle import pyoracle as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(seed, n=3000):
+    vt = [W.perturbed_ellipsoid(f, r, 0.01, seed + k) for k, (f, r) in
+          enumerate([(6, (0.8, 0.6, 0.5)), (10, (0.5, 0.9, 0.4))])]
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in vt]
+    om = [P.Mesh(v, t) for v, t in vt]
+    shapes = W.random_shapes(64, seed + 5)
+    ss = api.ShapeSet.from_workload(shapes)
+    G = P.Geoms(shapes)
+    rng = np.random.default_rng(seed)
+    midx = rng.integers(0, 2, size=n).astype(np.int32)
+    sidx = rng.integers(0, 64, size=n).astype(np.int32)
+    tfm = W.random_poses(n, -0.3, 0.3, seed + 1)
+    tfs = W.random_poses(n, -1.3, 1.3, seed + 2)
+    return meshes, om, ss, G, midx, sidx, tfm, tfs
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mesh_shape_collide_matches_oracle(gpu_lib, seed):
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(seed)
+    for M in (1, 100000):
+        g = api.mesh_shape_batch(meshes, ss, midx, sidx, tfm, tfs, mode="collide", num_max_contacts=M,
+                                 statistics=True)
+        for k in range(2):
+            sel = midx == k
+            c, nbv, nleaf = P.mesh_shape_collide(om[k], G, sidx[sel], tfm[sel], tfs[sel], max_contacts=M,
+                                                 nthreads=8)
+            np.testing.assert_array_equal(g["counts"][sel], c)
+            np.testing.assert_array_equal(g["num_bv_tests"][sel], nbv)
+            np.testing.assert_array_equal(g["num_leaf_tests"][sel], nleaf)
+    assert 0.1 < (g["counts"] > 0).mean() < 0.9
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mesh_shape_distance_matches_oracle(gpu_lib, seed):
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(seed, n=2000)
+    g = api.mesh_shape_batch(meshes, ss, midx, sidx, tfm, tfs, mode="distance", statistics=True)
+    for k in range(2):
+        sel = midx == k
+        o = P.mesh_shape_distance(om[k], G, sidx[sel], tfm[sel], tfs[sel], nthreads=8)
+        # same FP64 operations in the same order: identical values, triangles, witnesses
+        np.testing.assert_array_equal(g["min_distance"][sel], o["dist"])
+        np.testing.assert_array_equal(g["tri"][sel], o["tri"])
+        np.testing.assert_array_equal(g["nearest_points"][sel], o["pts"])
+        np.testing.assert_array_equal(g["num_bv_tests"][sel], o["nbv"])
+
+
+def test_broadphase_mixed_scene_matches_oracle(gpu_lib):
+    shapes = W.random_shapes(64, 21)
+    vt = [W.perturbed_ellipsoid(f, r, 0.01, 30 + k) for k, (f, r) in
+          enumerate([(5, (0.6, 0.4, 0.3)), (7, (0.5, 0.5, 0.5)), (4, (0.8, 0.3, 0.3))])]
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in vt]
+    om = [P.Mesh(v, t) for v, t in vt]
+    ss = api.ShapeSet.from_workload(shapes)
+    rng = np.random.default_rng(22)
+    n, nq = 600, 400
+    kind = (rng.uniform(size=n) < 0.3).astype(np.int32)
+    refs = np.stack([kind, np.where(kind == 1, rng.integers(0, 3, size=n), rng.integers(0, 64, size=n))], 1)
+    refs = refs.astype(np.int32)
+    tf = W.random_poses(n, 0.0, 8.0, 23)
+    qk = (rng.uniform(size=nq) < 0.5).astype(np.int32)
+    qrefs = np.stack([qk, np.where(qk == 1, rng.integers(0, 3, size=nq), rng.integers(0, 64, size=nq))], 1)
+    qrefs = qrefs.astype(np.int32)
+    qtf = W.random_poses(nq, 0.0, 8.0, 24)
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(refs, tf)
+    G = P.Geoms(shapes, om)
+    gid = np.where(refs[:, 0] == 1, 64 + refs[:, 1], refs[:, 1]).astype(np.int32)
+    qgid = np.where(qrefs[:, 0] == 1, 64 + qrefs[:, 1], qrefs[:, 1]).astype(np.int32)
+    S = P.Scene(G, gid, tf)
+    np.testing.assert_array_equal(mgr.getAABBs(), G.world_aabbs(gid, tf))
+    for M in (1, 100000):
+        g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M)
+        o = S.collide(qgid, qtf, max_contacts=M, use_tree=True, nthreads=8)
+        np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
+    assert (g["num_contacts"] > 0).any()
+    d = mgr.distance_batch(qrefs, qtf)
+    o = S.distance(qgid, qtf, use_tree=True, nthreads=8)
+    np.testing.assert_array_equal(d["min_distance"] <= 0, o["dist"] <= 0)
+    sep = o["dist"] > 0
+    r = o["dist"][sep]
+    assert np.all(np.abs(d["min_distance"][sep] - r) <= np.maximum(1e-6 * np.abs(r), 1e-9))

@@ -59,3 +59,36 @@ def test_serving_matches_oracle_alone_and_in_mix(gpu_lib):
                     "clearance_object"):
             assert alone[key] == m[key], key
     srv.close()
+
+
+def test_serving_with_mesh_links_and_mesh_objects(gpu_lib):
+    # the full request shape: capsule and 2,000-triangle mesh links against a scene of
+    # primitives and perturbed icospheres (mesh-mesh, mesh-shape and shape-shape pairs)
+    w = W.scene4(n_objects=800, seed=8, box=8.0, n_shape_geoms=128, n_mesh_geoms=6, mesh_fraction=0.25,
+                 tri_lo=500, tri_hi=1500)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in w.meshes]
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(w.refs, w.tf)
+    reqs = W.motion_requests(w, 5, seed=9, k_lo=10, k_hi=25)
+    srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=32)
+    om = [P.Mesh(v, t) for v, t in w.meshes]
+    G = P.Geoms(w.shapes, om)
+    ns = w.shapes.n
+    gid = np.where(w.refs[:, 0] == 1, ns + w.refs[:, 1], w.refs[:, 1]).astype(np.int32)
+    S = P.Scene(G, gid, w.tf)
+    link_gid = np.where(w.robot.link_refs[:, 0] == 1, ns + w.robot.link_refs[:, 1], w.robot.link_refs[:, 1])
+
+    class _R:  # link refs as registry ids for _expected
+        link_refs = np.stack([np.zeros_like(link_gid), link_gid], 1)
+
+    exp = [_expected(S, _R, srv.link_poses(r.base, r.q)) for r in reqs]
+    ids = [srv.submit(r.base, r.q) for r in reqs]
+    got = [srv.wait(i) for i in ids]
+    for (first, clr, k, i), g in zip(exp, got):
+        assert g["first_colliding_waypoint"] == first
+        if clr > 0:
+            assert abs(g["min_clearance"] - clr) <= max(REL * abs(clr), ABS)
+        else:
+            assert g["min_clearance"] <= 0
+    srv.close()
