@@ -104,6 +104,77 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------
+# serving: motion-checking requests against a resident broadphase scene
+# ------------------------------------------------------------------------------------
+def _serving_expected_cpu(w, reqs, threads):
+    """The reference's CPU path for the same requests: dynamic AABB tree manager with
+    the default callbacks (collide, num_max_contacts = 1, then distance) per link and
+    waypoint on the host cores.  Returns requests/s."""
+    from fcl_gb300 import workloads as W
+    from oracle import pyoracle as O
+    om = [O.Mesh(v, t) for v, t in w.meshes]
+    G = O.Geoms(w.shapes, om)
+    ns = w.shapes.n
+    gid = np.where(w.refs[:, 0] == 1, ns + w.refs[:, 1], w.refs[:, 1]).astype(np.int32)
+    S = O.Scene(G, gid, w.tf)
+    lg = np.where(w.robot.link_refs[:, 0] == 1, ns + w.robot.link_refs[:, 1], w.robot.link_refs[:, 1])
+    t0 = time.perf_counter()
+    for r in reqs:
+        poses = W.robot_fk(w.robot, r.base, r.q)
+        K, L = poses.shape[:2]
+        qg = np.tile(lg, K).astype(np.int32)
+        tf = poses.reshape(K * L, 12)
+        S.collide(qg, tf, max_contacts=1, use_tree=True, nthreads=threads)
+        S.distance(qg, tf, use_tree=True, nthreads=threads)
+    return len(reqs) / (time.perf_counter() - t0)
+
+
+def run_serving(args):
+    from fcl_gb300 import api
+    from fcl_gb300 import serving as SV
+    from fcl_gb300 import workloads as W
+    t0 = time.perf_counter()
+    w = W.scene4(n_objects=args.serve_objects or None, seed=4)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in w.meshes]
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(w.refs, w.tf)
+    setup_s = time.perf_counter() - t0
+    reqs = W.motion_requests(w, args.serve_requests + 80, seed=5)
+    srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=args.serve_step)
+    SV.run_burst(srv, reqs[:16])  # warm-up
+    burst = SV.run_burst(srv, reqs[16:80])
+    rate = args.serve_rate if args.serve_rate > 0 else 0.7 * burst["requests_per_s"]
+    with ClockSampler(0) as cs:
+        load = SV.run_poisson(srv, reqs[80:], rate, seed=6)
+    st = srv.stats()
+    srv.close()
+    out = {
+        "workload": f"scene of {w.n} objects (primitives and 500-5000-tri icospheres, 25% meshes) in a 20^3 box; "
+                    f"20-link robot (10 capsules, 10 x 2000-tri meshes); K ~ logU[10,500] waypoints",
+        "objects": w.n, "links": w.robot.n_links,
+        "capacity_requests_per_s": burst["requests_per_s"],
+        "arrival_rate_per_s": rate, "requests": load["requests"],
+        "throughput_requests_per_s": load["throughput_requests_per_s"],
+        "p50_ms": load["p50_ms"], "p99_ms": load["p99_ms"], "mean_ms": load["mean_ms"], "max_ms": load["max_ms"],
+        "waypoints": int(sum(r.q.shape[0] for r in reqs[80:])),
+        "engine": {k: st[k] for k in ("steps", "waypoints", "queries", "candidates", "busy_ms",
+                                      "max_step_waypoints")},
+        "scene_setup_s": setup_s, "clocks": cs.summary(),
+    }
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        O.build()
+        threads = O.hardware_threads()
+        sample = reqs[80:80 + args.serve_cpu_sample]
+        out["cpu_baseline"] = {"value": _serving_expected_cpu(w, sample, threads), "unit": "requests/s",
+                               "cores": threads, "kind": "port",
+                               "sample": f"{len(sample)} of the requests, dynamic AABB tree manager "
+                                         "(collide + distance per link and waypoint)"}
+    return out
+
+
+# ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
 class ClockSampler:
@@ -336,6 +407,8 @@ def run_gpu(args):
                       "colliding_fraction": float((fp32["counts"] > 0).float().mean().item()),
                       "mesh_build_s": build_s},
         }
+        if world == 1 and not args.no_serving:
+            line["serving"] = run_serving(args)
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -357,6 +430,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host end-to-end measurement")
     ap.add_argument("--fp64-scale", type=float, default=0.1,
                     help="fraction of the queries the plain FP64 form is timed on")
+    ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
+    ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
+    ap.add_argument("--serve-requests", type=int, default=200, help="requests in the Poisson run")
+    ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.7 x measured capacity)")
+    ap.add_argument("--serve-step", type=int, default=4096, help="waypoints per loop step")
+    ap.add_argument("--serve-cpu-sample", type=int, default=4, help="requests timed on the CPU baseline")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

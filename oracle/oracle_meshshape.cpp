@@ -308,9 +308,10 @@ bool shape_triangle_distance(const Shape& s, const Tf& tfs, const V3& P1, const 
       pt = apply(isometry_inverse(tfm), project_p);
       return true;
     }
-    // FCL leaves the distance unset here; the oracle reports -1, the value of the
-    // witness-free branch
+    // FCL leaves the distance and the witnesses unset here; the oracle reports -1 (the
+    // value of the witness-free branch) and zero witnesses
     d = -1;
+    ps = pt = mk(0, 0, 0);
     return false;
   }
   const V3 tv[3] = {P1, P2, P3};
