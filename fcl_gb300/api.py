@@ -516,8 +516,11 @@ class DynamicAABBTreeCollisionManager:
         N.check(N.lib().fclgpu_broadphase_get_aabbs(self.handle, out.ctypes.data), "fclgpu_broadphase_get_aabbs")
         return out
 
-    def collide_batch(self, refs, tf, num_max_contacts: int = 1, precision: str = "fp32", stream=None):
-        req = N.BpCollideRequest(num_max_contacts, _prec(precision), 0)
+    def collide_batch(self, refs, tf, num_max_contacts: int = 1, precision: str = "fp32", exhaustive: bool = False,
+                      stream=None):
+        """exhaustive=False stops a query at num_max_contacts like FCL's default callback
+        (num_objects / first_object then cover the evaluated pairs); True evaluates all."""
+        req = N.BpCollideRequest(num_max_contacts, _prec(precision), int(exhaustive))
         if _is_torch(tf):
             import torch
             dev = tf.device

@@ -637,10 +637,21 @@ __global__ void __launch_bounds__(128) k_bp_shape_narrow(BpSceneView S, BpQueryV
   }
 }
 
-__global__ void k_bp_list(const int32_t* kind, long long n, int32_t want, int64_t* list, unsigned long long* count) {
+__global__ void k_bp_list(const int32_t* kind, long long n, int32_t want, const int2* pairs, const int32_t* qdone,
+                          int64_t* list, unsigned long long* count) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    if (kind[i] == want) list[atomicAdd(count, 1ull)] = i;
+    if (kind[i] == want && !(qdone && qdone[pairs[i].x])) list[atomicAdd(count, 1ull)] = i;
+}
+
+__global__ void k_bp_query_done(long long nq, const int64_t* off, const int32_t* hit, long long maxc,
+                                int32_t* qdone) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    long long total = 0;
+    for (long long i = off[q]; i < off[q + 1]; ++i) total += hit[i];
+    qdone[q] = total >= maxc ? 1 : 0;
+  }
 }
 
 __global__ void k_bp_gather_mesh(BpSceneView S, BpQueryView Q, const int2* pairs, const int64_t* list, long long nl,
@@ -870,10 +881,18 @@ cudaError_t launch_bp_gather_mesh(const BpSceneView& S, const BpQueryView& Q, co
   return cudaGetLastError();
 }
 
-cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, int64_t* list, unsigned long long* count,
-                           cudaStream_t s) {
+cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, const int2* pairs, const int32_t* qdone,
+                           int64_t* list, unsigned long long* count, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_bp_list<<<grid_for(n, 256), 256, 0, s>>>(kind, n, want, list, count);
+  k_bp_list<<<grid_for(n, 256), 256, 0, s>>>(kind, n, want, pairs, qdone, list, count);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32_t* hit, int64_t max_contacts,
+                                 int32_t* qdone, cudaStream_t s) {
+  if (nq <= 0) return cudaSuccess;
+  k_bp_query_done<<<grid_for(nq, 256), 256, 0, s>>>(nq, offsets, hit, max_contacts, qdone);
   ++g_kernel_launches;
   return cudaGetLastError();
 }

@@ -109,8 +109,12 @@ cudaError_t launch_bp_shape_narrow(const BpSceneView& S, const BpQueryView& Q, c
 cudaError_t launch_bp_gather_mesh(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
                                   const int64_t* list, int64_t nlist, int32_t nm, int32_t* pair_index, double* tf1,
                                   double* tf2, cudaStream_t s);
-cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, int64_t* list, unsigned long long* count,
-                           cudaStream_t s);
+// Candidates of one kind; with qdone, only those whose query is not yet done.
+cudaError_t launch_bp_list(const int32_t* kind, int64_t n, int32_t want, const int2* pairs, const int32_t* qdone,
+                           int64_t* list, unsigned long long* count, cudaStream_t s);
+// qdone[q] = 1 when the contacts found so far for query q reach max_contacts.
+cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32_t* hit, int64_t max_contacts,
+                                 int32_t* qdone, cudaStream_t s);
 // Mixed pairs (kind 2): FCL calls BVH-shape with the mesh first whichever object is
 // the mesh (collision-inl.h:100-111, distance-inl.h:117-126); gather (mesh, shape)
 // indices and poses in that order.

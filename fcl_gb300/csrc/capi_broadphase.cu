@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -84,10 +85,32 @@ struct BpScratch {
   Buf ctr, qgid, q64, q32, counts, offsets, scan_tmp, ub;
   Buf pairs, kind, hit, dist, b12, pts, list;
   Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
-  Buf x_midx, x_sidx, x_counts, x_tri;
+  Buf x_midx, x_sidx, x_counts, x_tri, qdone;
   Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
 };
 BpScratch g_bs;
+
+// Phase times of the most recent collide (row 0) and distance (row 1) call, ms:
+// [0] query prep + candidate passes, [1] shape-shape pairs, [2] mesh-shape pairs,
+// [3] mesh-mesh pairs, [4] reduction; [5] candidates, [6] mesh-shape and [7] mesh-mesh
+// pairs evaluated.
+double g_phase[2][8];
+int64_t g_last_mixed = 0;
+
+struct PhaseClock {
+  int row;
+  cudaStream_t s;
+  std::chrono::steady_clock::time_point t;
+  PhaseClock(int r, cudaStream_t st) : row(r), s(st), t(std::chrono::steady_clock::now()) {
+    for (int k = 0; k < 8; ++k) g_phase[r][k] = 0.0;
+  }
+  void tick(int k) {
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    g_phase[row][k] += std::chrono::duration<double, std::milli>(now - t).count();
+    t = now;
+  }
+};
 
 // device counters block
 struct BpCounters {
@@ -235,9 +258,12 @@ int ensure_pair_buffers(int64_t total) {
 }
 
 // list of candidates of one kind; returns its length (host sync)
-int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cudaStream_t s) {
+int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cudaStream_t s,
+              const int32_t* qdone = nullptr) {
   CKB(cudaMemsetAsync(&dctr->list_count, 0, 8, s), "list");
-  CKB(launch_bp_list(g_bs.kind.as<int32_t>(), total, want, g_bs.list.as<int64_t>(), &dctr->list_count, s), "list");
+  CKB(launch_bp_list(g_bs.kind.as<int32_t>(), total, want, g_bs.pairs.as<int2>(), qdone, g_bs.list.as<int64_t>(),
+                     &dctr->list_count, s),
+      "list");
   unsigned long long c = 0;
   CKB(cudaMemcpyAsync(&c, &dctr->list_count, 8, cudaMemcpyDeviceToHost, s), "list");
   CKB(cudaStreamSynchronize(s), "list");
@@ -248,9 +274,10 @@ int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cud
 // Mesh-shape candidates (kind 2): BVH-shape collide (mode 0, contacts into hit) or
 // distance (mode 1, into the distance slots), mesh first as FCL calls it.
 int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQueryView& Q, int64_t total, int mode,
-              int64_t max_contacts, BpCounters* dctr, cudaStream_t s) {
+              int64_t max_contacts, BpCounters* dctr, cudaStream_t s, const int32_t* qdone = nullptr) {
   int64_t nl = 0;
-  RCB(list_kind(total, 2, dctr, &nl, s));
+  RCB(list_kind(total, 2, dctr, &nl, s, qdone));
+  g_last_mixed = nl;
   if (nl == 0) return FCLGPU_OK;
   if (!bp->shapes || !bp->dmeshes) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "mesh-shape pair without registry");
   CKB(g_bs.x_midx.ensure(4 * nl), "mixed scratch");
@@ -282,7 +309,7 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
   L.nbv = nullptr;
   L.nleaf = nullptr;
   L.status = &dctr->status;
-  CKB(launch_mesh_shape(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+  CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
   if (mode == 0) {
     CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.x_counts.as<int32_t>(), g_bs.hit.as<int32_t>(), s),
         "mixed scatter");
@@ -427,6 +454,8 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
   res->total_candidates = 0;
   res->total_node_visits = 0;
   if (nq == 0) return FCLGPU_OK;
+  PhaseClock pc(0, s);
+  g_last_mixed = 0;
   CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
   BpCounters* dctr = g_bs.ctr.as<BpCounters>();
   CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
@@ -441,6 +470,7 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
   RCB(scan_counts(nq, dctr, &hc, &total, s));
   res->total_candidates = total;
   res->total_node_visits = hc.visits;
+  g_phase[0][5] = (double)total;
   RCB(ensure_pair_buffers(total));
   CKB(g_bs.hit.ensure(4 * (size_t)std::max<int64_t>(total, 1)), "hits");
   const int64_t* off = g_bs.offsets.as<int64_t>();
@@ -450,12 +480,27 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
     CKB(launch_bp_overlap(S, Q, nullptr, off, pairs, nullptr, &dctr->status, s), "overlap write");
     CKB(launch_bp_classify(S, Q, pairs, total, g_bs.kind.as<int32_t>(), s), "classify");
     CKB(cudaMemsetAsync(hit, 0, 4 * (size_t)total, s), "hits");
+    pc.tick(0);
     CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_INTERSECT, hit, nullptr, nullptr,
                                s),
         "shape narrowphase");
-    RCB(run_mixed(bp, S, Q, total, 0, req->num_max_contacts, dctr, s));
+    pc.tick(1);
+    // without exhaustive evaluation a query stops once it has num_max_contacts
+    // contacts, as DefaultCollisionFunction stops FCL's traversal: cheaper pair kinds
+    // run first and later kinds skip finished queries
+    int32_t* qdone = nullptr;
+    if (!req->exhaustive) {
+      CKB(g_bs.qdone.ensure(4 * nq), "query flags");
+      qdone = g_bs.qdone.as<int32_t>();
+      CKB(launch_bp_query_done(nq, off, hit, req->num_max_contacts, qdone, s), "query flags");
+    }
+    RCB(run_mixed(bp, S, Q, total, 0, req->num_max_contacts, dctr, s, qdone));
+    g_phase[0][6] = (double)g_last_mixed;
+    pc.tick(2);
+    if (qdone) CKB(launch_bp_query_done(nq, off, hit, req->num_max_contacts, qdone, s), "query flags");
     int64_t nl = 0;
-    RCB(list_kind(total, 1, dctr, &nl, s));
+    RCB(list_kind(total, 1, dctr, &nl, s, qdone));
+    g_phase[0][7] = (double)nl;
     if (nl > 0) {
       CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
       CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
@@ -473,12 +518,14 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
       if (rc) return rc;
       CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.m_counts.as<int32_t>(), hit, s), "mesh scatter");
     }
+    pc.tick(3);
   }
   CKB(launch_bp_reduce_collide(nq, off, pairs, hit, req->num_max_contacts, res->num_contacts, res->num_objects,
                                res->first_object, s),
       "reduce");
   CKB(cudaMemcpyAsync(&hc, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
   CKB(cudaStreamSynchronize(s), "broadphase collide");
+  pc.tick(4);
   return check_status(hc);
 }
 
@@ -495,6 +542,8 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
   res->total_candidates = 0;
   res->total_node_visits = 0;
   if (nq == 0) return FCLGPU_OK;
+  PhaseClock pc(1, s);
+  g_last_mixed = 0;
   CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
   BpCounters* dctr = g_bs.ctr.as<BpCounters>();
   CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
@@ -512,6 +561,7 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
   RCB(scan_counts(nq, dctr, &hc, &total, s));
   res->total_candidates = total;
   res->total_node_visits = hc.visits;
+  g_phase[1][5] = (double)total;
   RCB(ensure_pair_buffers(total));
   const size_t t = (size_t)std::max<int64_t>(total, 1);
   CKB(g_bs.dist.ensure(8 * t), "distances");
@@ -527,11 +577,16 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
         "distance write");
     CKB(launch_bp_classify(S, Q, pairs, total, g_bs.kind.as<int32_t>(), s), "classify");
     CKB(cudaMemsetAsync(b12, 0xff, 8 * (size_t)total, s), "ids");
+    pc.tick(0);
     CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_DISTANCE, nullptr, dist, pts, s),
         "shape narrowphase");
+    pc.tick(1);
     RCB(run_mixed(bp, S, Q, total, 1, 0, dctr, s));
+    g_phase[1][6] = (double)g_last_mixed;
+    pc.tick(2);
     int64_t nl = 0;
     RCB(list_kind(total, 1, dctr, &nl, s));
+    g_phase[1][7] = (double)nl;
     if (nl > 0) {
       CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
       CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
@@ -554,12 +609,14 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
                                  g_bs.m_pts.as<double>(), dist, b12, pts, s),
           "mesh scatter");
     }
+    pc.tick(3);
   }
   CKB(launch_bp_reduce_distance(nq, off, pairs, dist, b12, pts, res->min_distance, res->object, res->ids,
                                 req->enable_nearest_points ? res->nearest_points : nullptr, s),
       "reduce");
   CKB(cudaMemcpyAsync(&hc, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
   CKB(cudaStreamSynchronize(s), "broadphase distance");
+  pc.tick(4);
   return check_status(hc);
 }
 
@@ -629,6 +686,14 @@ int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* 
   }
   for (Buf* b : {&refs, &tfd, &d, &ob, &ids, &pts}) cudaFree(b->p);
   return rc;
+}
+
+int fclgpu_broadphase_last_phase_ms(double* out16) {
+  if (!out16) return FCLGPU_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  for (int r = 0; r < 2; ++r)
+    for (int k = 0; k < 8; ++k) out16[8 * r + k] = g_phase[r][k];
+  return FCLGPU_OK;
 }
 
 }  // extern "C"

@@ -179,7 +179,7 @@ FCLG_HD int collide_item(const CollideLaunch& L, long long qi, int sb1, int sb2,
         else if (l1)
           first_over_second = false;
         else
-          first_over_second = FCLG_LDG(A.size64 + b1) > FCLG_LDG(B.size64 + b2);
+          first_over_second = size_key(A, b1) > size_key(B, b2);
         if (sp >= STACK) {
           st.status |= DEV_ERR_STACK;
           break;
@@ -281,7 +281,7 @@ FCLG_HD int collide_query(const CollideLaunch& L, long long qi, Sink& sink, Quer
         else if (l1)
           first_over_second = false;
         else
-          first_over_second = FCLG_LDG(A.size64 + b1) > FCLG_LDG(B.size64 + b2);
+          first_over_second = size_key(A, b1) > size_key(B, b2);
         if (sp >= STACK) {
           st.status |= DEV_ERR_STACK;
           break;

@@ -7,6 +7,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 #include "fclgpu_types.h"
 
@@ -757,6 +758,20 @@ FCLG_HD S tri_distance(const V3<S> T1[3], const V3<S> T2[3], V3<S>& P, V3<S>& Q)
     return sqrt(mindd);
   }
   return 0;
+}
+
+// OBB::size() of node b (OBB-inl.h:205-209, extent.squaredNorm(), stored in FP64) as the
+// bit pattern of the non-negative double: the integer order equals the FP64 order, so
+// firstOverSecond's comparison runs on the integer pipes instead of the 1/64-rate FP64
+// pipe.
+FCLG_HD long long size_key(const DevMesh& m, int b) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(reinterpret_cast<const long long*>(m.size64) + b);
+#else
+  long long k;
+  memcpy(&k, m.size64 + b, sizeof(k));
+  return k;
+#endif
 }
 
 }  // namespace fclgpu

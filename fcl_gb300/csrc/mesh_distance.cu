@@ -95,7 +95,7 @@ __device__ __forceinline__ bool first_over_second(const DevMesh& A, const DevMes
                                                   bool l2) {
   if (l2) return true;
   if (l1) return false;
-  return __ldg(A.size64 + b1) > __ldg(B.size64 + b2);
+  return size_key(A, b1) > size_key(B, b2);
 }
 
 // FCL's distance traversal in FP64 (the reference's operation order).

@@ -59,7 +59,187 @@ __global__ void __launch_bounds__(128) k_mesh_shape(MeshShapeLaunch L) {
   }
 }
 
+// ------------------------------------------------------------------ split form ----
+
+struct PairGeom {
+  DevMesh m;
+  ShapeRef A;
+  M3<double> Rm, Rs;
+  D3v tm, ts;
+};
+
+__device__ __forceinline__ void pair_geom(const MeshShapeLaunch& L, long long i, PairGeom& g) {
+  g.m = L.meshes[L.mesh_idx[i]];
+  g.A.s = L.shapes[L.shape_idx[i]];
+  g.A.verts = L.sverts;
+  load_tf(L.tfm + 12 * i, g.Rm, g.tm);
+  load_tf(L.tfs + 12 * i, g.Rs, g.ts);
+}
+
+// leaves of each pair: count pass (offsets == null) or write pass
+template <int STACK>
+__global__ void __launch_bounds__(128) k_ms_collect(MeshShapeLaunch L, int32_t* counts, const int64_t* offsets,
+                                                    int32_t* leaf_pair, int32_t* leaf_prim, double* leaf_lb,
+                                                    double* ub) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += stride) {
+    PairGeom g;
+    pair_geom(L, i, g);
+    ShapeBV bv;
+    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
+    const long long base = offsets ? offsets[i] : 0;
+    int cnt = 0;
+    auto emit = [&](int prim, double lb) {
+      if (offsets) {
+        leaf_pair[base + cnt] = (int32_t)i;
+        leaf_prim[base + cnt] = prim;
+        if (leaf_lb) leaf_lb[base + cnt] = lb;
+      }
+      ++cnt;
+    };
+    int st;
+    if (L.mode == 0) {
+      st = mesh_shape_collect_collide<STACK>(g.m, g.Rm, g.tm, bv, emit);
+    } else {
+      double u = DBL_MAX;
+      st = mesh_shape_collect_distance<STACK>(g.m, g.Rm, g.tm, g.A, g.Rs, g.ts, bv, &u, emit);
+      if (ub) ub[i] = u;
+    }
+    if (st) atomicOr(L.status, 1u);
+    if (counts) counts[i] = cnt;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_ms_leaf_tests(MeshShapeLaunch L, long long nl, const int32_t* leaf_pair,
+                                                       const int32_t* leaf_prim, const double* leaf_lb,
+                                                       const double* ub, int32_t* hit, double* dist, double* pts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
+    const long long i = leaf_pair[j];
+    if (L.mode == 1 && leaf_lb[j] > ub[i]) {  // cannot hold the minimum
+      dist[j] = DBL_MAX;
+      continue;
+    }
+    PairGeom g;
+    pair_geom(L, i, g);
+    double P[9];
+    load_tri_local(g.m, leaf_prim[j], P);
+    SimplexVert V[kSimplexSlots];
+    if (L.mode == 0) {
+      EpaState epa;
+      hit[j] = shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa) ? 1 : 0;
+    } else {
+      double d;
+      D3v ps, pt;
+      shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+      dist[j] = d;
+      double* p = pts + 6 * j;
+      p[0] = pt.x;
+      p[1] = pt.y;
+      p[2] = pt.z;
+      p[3] = ps.x;
+      p[4] = ps.y;
+      p[5] = ps.z;
+    }
+  }
+}
+
+// per pair: contacts = min(max_contacts, intersecting leaves); distance = the first
+// minimum in collection order (the seed triangle first, as FCL's strict update)
+__global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t* leaf_prim, const int32_t* hit,
+                            const double* dist, const double* pts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += stride) {
+    if (L.mode == 0) {
+      long long c = 0;
+      for (long long j = off[i]; j < off[i + 1]; ++j) c += hit[j];
+      L.counts[i] = (int32_t)(c < L.max_contacts ? c : L.max_contacts);
+    } else {
+      double best = DBL_MAX;
+      long long bj = -1;
+      for (long long j = off[i]; j < off[i + 1]; ++j)
+        if (best > dist[j]) {
+          best = dist[j];
+          bj = j;
+        }
+      L.dist[i] = best;
+      if (L.tri) L.tri[i] = bj >= 0 ? leaf_prim[bj] : -1;
+      if (L.pts)
+        for (int k = 0; k < 6; ++k) L.pts[6 * i + k] = bj >= 0 ? pts[6 * bj + k] : 0.0;
+    }
+  }
+}
+
+int grid128(long long n) { return (int)std::min<long long>(std::max<long long>((n + 127) / 128, 1), 152 * 32); }
+
 }  // namespace
+
+cudaError_t launch_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, int64_t* tmp, cudaStream_t s);
+
+namespace {
+struct SplitScratch {
+  void* p[8] = {nullptr};
+  size_t cap[8] = {0};
+  cudaError_t ensure(int k, size_t bytes) {
+    if (bytes <= cap[k]) return cudaSuccess;
+    if (p[k]) cudaFree(p[k]);
+    p[k] = nullptr;
+    cap[k] = 0;
+    const size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+    cudaError_t e = cudaMalloc(&p[k], want);
+    if (e == cudaSuccess) cap[k] = want;
+    return e;
+  }
+};
+SplitScratch g_split_ms;
+std::mutex g_split_mu;
+}  // namespace
+
+cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  std::lock_guard<std::mutex> lk(g_split_mu);
+  SplitScratch& S = g_split_ms;
+  const long long n = L.n;
+  cudaError_t e;
+  if ((e = S.ensure(0, 4 * n)) || (e = S.ensure(1, 8 * (n + 1))) || (e = S.ensure(2, 8 * ((n + 4095) / 4096 + 2))) ||
+      (e = S.ensure(3, 8 * n)))
+    return e;
+  int32_t* counts = (int32_t*)S.p[0];
+  int64_t* off = (int64_t*)S.p[1];
+  double* ub = (double*)S.p[3];
+  const bool big = stack_entries > 64;
+  if (big)
+    k_ms_collect<256><<<grid128(n), 128, 0, s>>>(L, counts, nullptr, nullptr, nullptr, nullptr, ub);
+  else
+    k_ms_collect<64><<<grid128(n), 128, 0, s>>>(L, counts, nullptr, nullptr, nullptr, nullptr, ub);
+  ++g_kernel_launches;
+  if ((e = cudaGetLastError())) return e;
+  if ((e = launch_exclusive_scan(counts, n, off, (int64_t*)S.p[2], s))) return e;
+  int64_t nl = 0;
+  if ((e = cudaMemcpyAsync(&nl, off + n, 8, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) return e;
+  if (nl > 0) {
+    if ((e = S.ensure(4, 4 * nl)) || (e = S.ensure(5, 4 * nl)) || (e = S.ensure(6, 8 * nl)) ||
+        (e = S.ensure(7, (L.mode == 0 ? 4 : 56) * nl)))
+      return e;
+    int32_t* leaf_pair = (int32_t*)S.p[4];
+    int32_t* leaf_prim = (int32_t*)S.p[5];
+    double* leaf_lb = (double*)S.p[6];
+    int32_t* hit = (int32_t*)S.p[7];
+    double* dist = (double*)S.p[7];
+    double* pts = dist + nl;
+    if (big)
+      k_ms_collect<256><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
+    else
+      k_ms_collect<64><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
+    k_ms_leaf_tests<<<grid128(nl), 128, 0, s>>>(L, nl, leaf_pair, leaf_prim, leaf_lb, ub, hit, dist, pts);
+    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, leaf_prim, hit, dist, pts);
+    g_kernel_launches += 3;
+  } else {
+    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, nullptr, nullptr, nullptr, nullptr);
+    ++g_kernel_launches;
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
   if (L.n <= 0) return cudaSuccess;
@@ -158,7 +338,8 @@ int fclgpu_mesh_shape_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes
   L.nbv = res->num_bv_tests;
   L.nleaf = res->num_leaf_tests;
   L.status = static_cast<unsigned*>(g_ms_status.p);
-  e = launch_mesh_shape(L, depth + 2, s);
+  // statistics need the serial traversal; otherwise the leaf tests run one per thread
+  e = (L.nbv || L.nleaf) ? launch_mesh_shape(L, depth + 2, s) : run_mesh_shape_split(L, depth + 2, s);
   unsigned st = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&st, g_ms_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

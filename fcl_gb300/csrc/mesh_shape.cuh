@@ -618,6 +618,114 @@ FCLG_HD void load_tri_local(const DevMesh& m, int prim, double* P) {
   }
 }
 
+// ------------------------------------------------- leaf collection (split form) ----
+// The split form runs the BVH part of a pair on one thread and hands the leaf tests
+// (GJK/EPA in FP64, the expensive part) to one thread each.  The set of leaves it
+// collects makes the result equal to the serial traversal's:
+//  * collide: every leaf whose OBB overlaps the shape's; the contact count is
+//    min(max_contacts, intersecting leaves), which is what the serial DFS returns
+//    whether or not it stops early;
+//  * distance: the first triangle (FCL's preprocess seed), then every leaf whose RSS
+//    lower bound does not exceed an upper bound of the pair's distance (the distance
+//    from each visited triangle's centroid to the shape's support point toward it);
+//    the minimiser is always among them.
+
+// a point of the shape's surface toward world point c (support along the unit
+// direction from the shape's origin), and its distance to c
+FCLG_HD double shape_point_ub(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const D3v& c) {
+  const D3v d = c - ts;
+  const double len = d3norm(d);
+  if (!(len > 0)) return 0.0;
+  const D3v ld = mulTv(Rs, d3scale(d, 1.0 / len));
+  const D3v p = mulv(Rs, shape_support(A, ld)) + ts;
+  return d3norm(p - c);
+}
+
+template <int STACK, class Emit>
+FCLG_HD int mesh_shape_collect_collide(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeBV& bv,
+                                       Emit emit) {
+  int stack[STACK];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const int b = stack[--sp];
+    const NodeD nd = m.nodes64[b];
+    if (!obb_overlap64(Rm, tm, bv.obb, nd)) continue;
+    if (nd.child < 0) {
+      emit(-(nd.child + 1), 0.0);
+      continue;
+    }
+    if (sp + 2 > STACK) return 1;
+    stack[sp++] = nd.child + 1;
+    stack[sp++] = nd.child;
+  }
+  return 0;
+}
+
+template <int STACK, class Emit>
+FCLG_HD int mesh_shape_collect_distance(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeRef& A,
+                                        const M3<double>& Rs, const D3v& ts, const ShapeBV& bv, double* ub_out,
+                                        Emit emit) {
+  M3<double> Ab;
+  for (int i = 0; i < 9; ++i) Ab.m[i] = bv.obb.axis[i];
+  const D3v Tob = v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]);
+  auto tri_ub = [&](int prim) {
+    double P[9];
+    load_tri_local(m, prim, P);
+    const D3v c = mulv(Rm, v3((P[0] + P[3] + P[6]) / 3.0, (P[1] + P[4] + P[7]) / 3.0, (P[2] + P[5] + P[8]) / 3.0)) + tm;
+    return shape_point_ub(A, Rs, ts, c);
+  };
+  auto bvd = [&](int b) {
+    const NodeD nd = m.nodes64[b];
+    const RssD& rs = m.rss64[b];
+    M3<double> A2;
+    for (int i = 0; i < 9; ++i) A2.m[i] = nd.axis[i];
+    return rss_distance<double>(Rm, tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
+  };
+  double ub = tri_ub(0);
+  emit(0, -1.0);  // the seed triangle is always evaluated
+  int stack[STACK];
+  double sd[STACK];
+  int sp = 0;
+  stack[sp] = 0;
+  sd[sp] = -1.0;
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    const int b = stack[sp];
+    const double lb = sd[sp];
+    if (lb > ub) continue;
+    const int child = m.nodes64[b].child;
+    if (child < 0) {
+      const int prim = -(child + 1);
+      if (prim != 0) {
+        emit(prim, lb);
+        ub = fmin(ub, tri_ub(prim));
+      }
+      continue;
+    }
+    const double d1 = bvd(child), d2 = bvd(child + 1);
+    if (sp + 2 > STACK) return 1;
+    if (d2 < d1) {
+      stack[sp] = child;
+      sd[sp] = d1;
+      ++sp;
+      stack[sp] = child + 1;
+      sd[sp] = d2;
+      ++sp;
+    } else {
+      stack[sp] = child + 1;
+      sd[sp] = d2;
+      ++sp;
+      stack[sp] = child;
+      sd[sp] = d1;
+      ++sp;
+    }
+  }
+  *ub_out = ub;
+  return 0;
+}
+
 template <int STACK>
 FCLG_HD void mesh_shape_collide(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeRef& A,
                                 const M3<double>& Rs, const D3v& ts, int max_contacts, MeshShapeOut& o) {

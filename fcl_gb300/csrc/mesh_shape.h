@@ -28,6 +28,10 @@ struct MeshShapeLaunch {
   unsigned* status;
 };
 
+// One thread per pair runs the whole FCL traversal (exact statistics).
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s);
+// Split form: BVH traversal per pair, then one thread per leaf test, then a per-pair
+// reduction; same results, no statistics (nbv / nleaf ignored).  Synchronises s once.
+cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s);
 
 }  // namespace fclgpu

@@ -92,6 +92,26 @@ cudaError_t launch_robot_fk(const RobotDev& rb, int64_t W, const double* q, cons
   return cudaGetLastError();
 }
 
+// Queries with no contact, compacted for the clearance pass (a query in contact has
+// clearance 0 and needs no distance query).
+__global__ void k_free_queries(long long nq, const int64_t* nc, const int2* refs, const double* tf, int2* orefs,
+                               double* otf, int32_t* map, unsigned long long* count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq || nc[i] != 0) return;
+  const unsigned long long j = atomicAdd(count, 1ull);
+  orefs[j] = refs[i];
+  for (int k = 0; k < 12; ++k) otf[12 * j + k] = tf[12 * i + k];
+  map[j] = (int32_t)i;
+}
+
+__global__ void k_scatter_clearance(long long nfree, const int32_t* map, const double* d, const int32_t* o,
+                                    double* dist, int32_t* obj) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nfree) return;
+  dist[map[j]] = d[j];
+  obj[map[j]] = o[j];
+}
+
 using Clock = std::chrono::steady_clock;
 
 struct Request {
@@ -137,6 +157,12 @@ struct fclgpu_server_s {
   int64_t* d_nc = nullptr;
   double* d_dist = nullptr;
   int32_t* d_obj = nullptr;
+  int2* d_frefs = nullptr;   // compacted contact-free queries
+  double* d_ftf = nullptr;
+  int32_t* d_fmap = nullptr;
+  double* d_fdist = nullptr;
+  int32_t* d_fobj = nullptr;
+  unsigned long long* d_fcount = nullptr;
   // pinned host staging
   double* h_q = nullptr;
   int32_t* h_slot = nullptr;
@@ -213,12 +239,31 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
   if (rc) return rc;
   int64_t cand = cres.total_candidates;
   if (s->cfg.compute_clearance) {
-    fclgpu_broadphase_distance_request dreq = {0, s->cfg.precision};
-    fclgpu_broadphase_distance_result dres = {s->d_dist, s->d_obj, nullptr, nullptr, 0, 0};
-    rc = fclgpu_broadphase_distance_device(s->scene, reinterpret_cast<const fclgpu_geometry_ref*>(s->d_qrefs), nq,
-                                           s->d_qtf, &dreq, &dres, st);
-    if (rc) return rc;
-    cand = std::max<int64_t>(cand, dres.total_candidates);
+    // queries in contact have clearance 0; the rest go through the distance pass
+    if (cudaMemsetAsync(s->d_dist, 0, 8 * nq, st) != cudaSuccess ||
+        cudaMemsetAsync(s->d_obj, 0xff, 4 * nq, st) != cudaSuccess ||
+        cudaMemsetAsync(s->d_fcount, 0, 8, st) != cudaSuccess)
+      return FCLGPU_ERR_CUDA;
+    k_free_queries<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(nq, s->d_nc, s->d_qrefs, s->d_qtf, s->d_frefs,
+                                                                 s->d_ftf, s->d_fmap, s->d_fcount);
+    ++g_kernel_launches;
+    unsigned long long nfree = 0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&nfree, s->d_fcount, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return FCLGPU_ERR_CUDA;
+    if (nfree > 0) {
+      fclgpu_broadphase_distance_request dreq = {0, s->cfg.precision};
+      fclgpu_broadphase_distance_result dres = {s->d_fdist, s->d_fobj, nullptr, nullptr, 0, 0};
+      rc = fclgpu_broadphase_distance_device(s->scene, reinterpret_cast<const fclgpu_geometry_ref*>(s->d_frefs),
+                                             (int64_t)nfree, s->d_ftf, &dreq, &dres, st);
+      if (rc) return rc;
+      cand = std::max<int64_t>(cand, dres.total_candidates);
+      k_scatter_clearance<<<(unsigned)((nfree + 255) / 256), 256, 0, st>>>((long long)nfree, s->d_fmap, s->d_fdist,
+                                                                           s->d_fobj, s->d_dist, s->d_obj);
+      ++g_kernel_launches;
+      if (cudaGetLastError() != cudaSuccess) return FCLGPU_ERR_CUDA;
+    }
     if (cudaMemcpyAsync(s->h_dist, s->d_dist, 8 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(s->h_obj, s->d_obj, 4 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return FCLGPU_ERR_CUDA;
@@ -324,7 +369,8 @@ void worker_loop(fclgpu_server_s* s) {
 void free_server(fclgpu_server_s* s) {
   for (void* p : {(void*)s->d_axis, (void*)s->d_offset, (void*)s->d_gtf, (void*)s->d_refs, (void*)s->d_q,
                   (void*)s->d_slot, (void*)s->d_bases, (void*)s->d_qtf, (void*)s->d_qrefs, (void*)s->d_nc,
-                  (void*)s->d_dist, (void*)s->d_obj})
+                  (void*)s->d_dist, (void*)s->d_obj, (void*)s->d_frefs, (void*)s->d_ftf, (void*)s->d_fmap,
+                  (void*)s->d_fdist, (void*)s->d_fobj, (void*)s->d_fcount})
     if (p) cudaFree(p);
   for (void* p : {(void*)s->h_q, (void*)s->h_slot, (void*)s->h_bases, (void*)s->h_nc, (void*)s->h_dist,
                   (void*)s->h_obj})
@@ -382,6 +428,12 @@ int fclgpu_server_create(fclgpu_broadphase scene, const fclgpu_robot_desc* robot
   dm((void**)&s->d_nc, 8 * nq);
   dm((void**)&s->d_dist, 8 * nq);
   dm((void**)&s->d_obj, 4 * nq);
+  dm((void**)&s->d_frefs, 8 * nq);
+  dm((void**)&s->d_ftf, 96 * nq);
+  dm((void**)&s->d_fmap, 4 * nq);
+  dm((void**)&s->d_fdist, 8 * nq);
+  dm((void**)&s->d_fobj, 4 * nq);
+  dm((void**)&s->d_fcount, 8);
   hm((void**)&s->h_q, 8 * nq);
   hm((void**)&s->h_slot, 4 * W);
   hm((void**)&s->h_bases, 96 * W);

@@ -56,7 +56,7 @@ class GeometryRef(C.Structure):
 
 
 class BpCollideRequest(C.Structure):
-    _fields_ = [("num_max_contacts", C.c_int64), ("precision", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("num_max_contacts", C.c_int64), ("precision", C.c_int32), ("exhaustive", C.c_int32)]
 
 
 class BpCollideResult(C.Structure):
@@ -149,6 +149,7 @@ _SIGS = {
                                                     C.POINTER(BpDistanceResult), _VP]),
     "fclgpu_broadphase_distance": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
                                              C.POINTER(BpDistanceResult), _VP]),
+    "fclgpu_broadphase_last_phase_ms": (C.c_int, [_VP]),
     "fclgpu_server_create": (C.c_int, [_VP, C.POINTER(RobotDesc), C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
     "fclgpu_server_submit": (C.c_int, [_VP, _VP, _VP, C.c_int32, C.POINTER(C.c_int64)]),
     "fclgpu_server_wait": (C.c_int, [_VP, C.c_int64, C.c_double, C.POINTER(MotionResult)]),

@@ -17,6 +17,10 @@
  *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
  *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/distance.h:51-62, distance-inl.h:71-246)
+ *   fclgpu_shape_batch*     fcl::collide / fcl::distance on convex shapes (GJKSolver_indep)
+ *   fclgpu_mesh_shape_batch*  fcl::collide / fcl::distance, BVHModel<OBBRSS> x convex shape
+ *   fclgpu_broadphase_*     DynamicAABBTreeCollisionManager<double> with the default callbacks
+ *                           (broadphase/broadphase_dynamic_AABB_tree-inl.h:727-1009)
  */
 #ifndef FCLGPU_H
 #define FCLGPU_H
@@ -320,16 +324,19 @@ FCLGPU_API int fclgpu_broadphase_get_aabbs(fclgpu_broadphase bp, double* aabb6);
 typedef struct {
   int64_t num_max_contacts; /* CollisionRequest::num_max_contacts (>= 1) */
   int32_t precision;        /* mesh-mesh narrowphase form (FCLGPU_PLAIN_FP64 / FCLGPU_FP32_RECHECK) */
-  int32_t reserved;
+  int32_t exhaustive;       /* 1: evaluate every candidate pair; 0: like FCL's callback, stop a
+                               query once it has num_max_contacts contacts (shape pairs are
+                               evaluated first, then mesh-shape, then mesh-mesh pairs) */
 } fclgpu_broadphase_collide_request;
 
 /* Per query q: num_contacts[q] = DefaultCollisionData::result.numContacts() after
  * manager.collide(query, DefaultCollisionFunction), which is min(num_max_contacts,
  * sum over colliding scene objects of their contacts); num_objects[q] = number of
- * scene objects in collision with the query and first_object[q] = the smallest such
- * object index (-1 if none) -- both exhaustive, an extension that does not depend on
- * the order FCL's callback would meet the objects in.  Outputs may be NULL except
- * num_contacts.  The totals are filled on return. */
+ * scene objects found in collision with the query and first_object[q] = the smallest
+ * such object index (-1 if none).  With exhaustive = 1 both cover every object, an
+ * extension that does not depend on the order FCL's callback would meet the objects in;
+ * with exhaustive = 0 they cover the pairs evaluated before the query stopped.  Outputs
+ * may be NULL except num_contacts.  The totals are filled on return. */
 typedef struct {
   int64_t* num_contacts;
   int32_t* num_objects;
@@ -376,6 +383,11 @@ FCLGPU_API int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fcl
 FCLGPU_API int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
                                           const double* tf, const fclgpu_broadphase_distance_request* req,
                                           fclgpu_broadphase_distance_result* res, void* stream);
+/* Wall-clock phases of the most recent broadphase collide (out16[0..7]) and distance
+ * (out16[8..15]) call: [0] query setup and candidate passes, [1] shape-shape pairs,
+ * [2] mesh-shape pairs, [3] mesh-mesh pairs, [4] reduction (ms); [5] candidate pairs,
+ * [6] mesh-shape and [7] mesh-mesh pairs evaluated.  No counterpart in FCL. */
+FCLGPU_API int fclgpu_broadphase_last_phase_ms(double* out16);
 
 /* ---- motion-checking request loop --------------------------------------------------
  * No counterpart in FCL: a serving loop over a resident broadphase scene.  A request

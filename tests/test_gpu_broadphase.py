@@ -26,8 +26,11 @@ def _shape_scene(n, nq, seed, box=10.0, n_geoms=256):
 
 def _check_collide(mgr, S, qrefs, qtf, gid_q, nq_checks=None):
     for M in (1, 100000):
-        g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M)
         o = S.collide(gid_q, qtf, max_contacts=M, use_tree=True, nthreads=8)
+        # FCL-like early stop and exhaustive evaluation report the same contact totals
+        g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M, exhaustive=False)
+        np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
+        g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M, exhaustive=True)
         np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
         if M > 1:
             np.testing.assert_array_equal(g["num_objects"], o["num_hits"])

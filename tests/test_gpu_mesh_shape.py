@@ -81,9 +81,10 @@ def test_broadphase_mixed_scene_matches_oracle(gpu_lib):
     S = P.Scene(G, gid, tf)
     np.testing.assert_array_equal(mgr.getAABBs(), G.world_aabbs(gid, tf))
     for M in (1, 100000):
-        g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M)
         o = S.collide(qgid, qtf, max_contacts=M, use_tree=True, nthreads=8)
-        np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
+        for ex in (False, True):
+            g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M, exhaustive=ex)
+            np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
     assert (g["num_contacts"] > 0).any()
     d = mgr.distance_batch(qrefs, qtf)
     o = S.distance(qgid, qtf, use_tree=True, nthreads=8)
@@ -91,3 +92,22 @@ def test_broadphase_mixed_scene_matches_oracle(gpu_lib):
     sep = o["dist"] > 0
     r = o["dist"][sep]
     assert np.all(np.abs(d["min_distance"][sep] - r) <= np.maximum(1e-6 * np.abs(r), 1e-9))
+
+
+@pytest.mark.parametrize("seed", [2])
+def test_mesh_shape_split_form_matches_oracle(gpu_lib, seed):
+    # without statistics the leaf tests run one per thread; results stay the oracle's
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(seed, n=2500)
+    for M in (1, 100000):
+        g = api.mesh_shape_batch(meshes, ss, midx, sidx, tfm, tfs, mode="collide", num_max_contacts=M)
+        for k in range(2):
+            sel = midx == k
+            c, _, _ = P.mesh_shape_collide(om[k], G, sidx[sel], tfm[sel], tfs[sel], max_contacts=M, nthreads=8)
+            np.testing.assert_array_equal(g["counts"][sel], c)
+    g = api.mesh_shape_batch(meshes, ss, midx, sidx, tfm, tfs, mode="distance")
+    for k in range(2):
+        sel = midx == k
+        o = P.mesh_shape_distance(om[k], G, sidx[sel], tfm[sel], tfs[sel], nthreads=8)
+        np.testing.assert_array_equal(g["min_distance"][sel], o["dist"])
+        np.testing.assert_array_equal(g["tri"][sel], o["tri"])
+        np.testing.assert_array_equal(g["nearest_points"][sel], o["pts"])
