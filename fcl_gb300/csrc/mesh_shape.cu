@@ -170,6 +170,54 @@ __global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t
   }
 }
 
+// Collide in rounds: each unfinished pair tests its next kChunk leaves (in DFS order),
+// then stops once it has max_contacts contacts -- the serial DFS's early stop, kept
+// to a chunk's granularity so that colliding pairs do not test (and run EPA on) every
+// overlapping triangle.
+constexpr int kChunk = 16;
+
+__global__ void __launch_bounds__(128) k_ms_chunk_tests(MeshShapeLaunch L, const int32_t* act, long long nact,
+                                                        const int64_t* cur, const int64_t* off,
+                                                        const int32_t* leaf_prim, int32_t* hit) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nact * kChunk; t += stride) {
+    const long long i = act[t / kChunk];
+    const long long j = cur[i] + t % kChunk;
+    if (j >= off[i + 1]) continue;
+    PairGeom g;
+    pair_geom(L, i, g);
+    double P[9];
+    load_tri_local(g.m, leaf_prim[j], P);
+    SimplexVert V[kSimplexSlots];
+    EpaState epa;
+    hit[j] = shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa) ? 1 : 0;
+  }
+}
+
+__global__ void k_ms_chunk_update(MeshShapeLaunch L, const int32_t* act, long long nact, int64_t* cur,
+                                  const int64_t* off, const int32_t* hit, int32_t* next, unsigned long long* nnext) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
+    const long long i = act[a];
+    const long long end = off[i + 1];
+    const long long j1 = cur[i] + kChunk < end ? cur[i] + kChunk : end;
+    int c = L.counts[i];
+    for (long long j = cur[i]; j < j1 && c < L.max_contacts; ++j) c += hit[j];
+    L.counts[i] = c;
+    cur[i] = j1;
+    if (c < L.max_contacts && j1 < end) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
+  }
+}
+
+__global__ void k_ms_iota(int32_t* a, long long n, int64_t* cur, const int64_t* off, int32_t* counts) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    a[i] = (int32_t)i;
+    cur[i] = off[i];
+    counts[i] = 0;
+  }
+}
+
 int grid128(long long n) { return (int)std::min<long long>(std::max<long long>((n + 127) / 128, 1), 152 * 32); }
 
 }  // namespace
@@ -178,8 +226,8 @@ cudaError_t launch_exclusive_scan(const int32_t* counts, int64_t n, int64_t* off
 
 namespace {
 struct SplitScratch {
-  void* p[8] = {nullptr};
-  size_t cap[8] = {0};
+  void* p[12] = {nullptr};
+  size_t cap[12] = {0};
   cudaError_t ensure(int k, size_t bytes) {
     if (bytes <= cap[k]) return cudaSuccess;
     if (p[k]) cudaFree(p[k]);
@@ -231,9 +279,35 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
       k_ms_collect<256><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
     else
       k_ms_collect<64><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
-    k_ms_leaf_tests<<<grid128(nl), 128, 0, s>>>(L, nl, leaf_pair, leaf_prim, leaf_lb, ub, hit, dist, pts);
-    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, leaf_prim, hit, dist, pts);
-    g_kernel_launches += 3;
+    ++g_kernel_launches;
+    if (L.mode == 0) {
+      if ((e = S.ensure(8, 4 * n)) || (e = S.ensure(9, 4 * n)) || (e = S.ensure(10, 8))) return e;
+      int32_t* act = (int32_t*)S.p[8];
+      int32_t* next = (int32_t*)S.p[9];
+      unsigned long long* nnext = (unsigned long long*)S.p[10];
+      int64_t* cur = (int64_t*)S.p[3];
+      k_ms_iota<<<grid128(n), 128, 0, s>>>(act, n, cur, off, L.counts);
+      ++g_kernel_launches;
+      long long nact = n;
+      while (nact > 0) {
+        if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
+        k_ms_chunk_tests<<<grid128(nact * kChunk), 128, 0, s>>>(L, act, nact, cur, off, leaf_prim, hit);
+        k_ms_chunk_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, cur, off, hit, next, nnext);
+        g_kernel_launches += 2;
+        unsigned long long nn = 0;
+        if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+          return e;
+        nact = (long long)nn;
+        int32_t* t = act;
+        act = next;
+        next = t;
+      }
+    } else {
+      k_ms_leaf_tests<<<grid128(nl), 128, 0, s>>>(L, nl, leaf_pair, leaf_prim, leaf_lb, ub, hit, dist, pts);
+      k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, leaf_prim, hit, dist, pts);
+      g_kernel_launches += 2;
+    }
   } else {
     k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, nullptr, nullptr, nullptr, nullptr);
     ++g_kernel_launches;

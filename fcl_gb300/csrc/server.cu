@@ -24,6 +24,9 @@ namespace fclgpu {
 namespace {
 
 constexpr int kMaxLinks = 64;
+// waypoints of one request per step: a request that collides early stops after its
+// first chunk, and long requests share the step with the others
+constexpr int kRequestChunk = 64;
 
 struct RobotDev {
   int32_t L;
@@ -92,24 +95,14 @@ cudaError_t launch_robot_fk(const RobotDev& rb, int64_t W, const double* q, cons
   return cudaGetLastError();
 }
 
-// Queries with no contact, compacted for the clearance pass (a query in contact has
-// clearance 0 and needs no distance query).
-__global__ void k_free_queries(long long nq, const int64_t* nc, const int2* refs, const double* tf, int2* orefs,
-                               double* otf, int32_t* map, unsigned long long* count) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nq || nc[i] != 0) return;
-  const unsigned long long j = atomicAdd(count, 1ull);
+// The queries listed in idx, compacted for the clearance pass.
+__global__ void k_gather_queries(long long n, const int32_t* idx, const int2* refs, const double* tf, int2* orefs,
+                                 double* otf) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const long long i = idx[j];
   orefs[j] = refs[i];
   for (int k = 0; k < 12; ++k) otf[12 * j + k] = tf[12 * i + k];
-  map[j] = (int32_t)i;
-}
-
-__global__ void k_scatter_clearance(long long nfree, const int32_t* map, const double* d, const int32_t* o,
-                                    double* dist, int32_t* obj) {
-  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nfree) return;
-  dist[map[j]] = d[j];
-  obj[map[j]] = o[j];
 }
 
 using Clock = std::chrono::steady_clock;
@@ -170,6 +163,7 @@ struct fclgpu_server_s {
   int64_t* h_nc = nullptr;
   double* h_dist = nullptr;
   int32_t* h_obj = nullptr;
+  int32_t* h_fidx = nullptr;
   cudaStream_t stream = nullptr;
   // queue
   std::mutex mu;
@@ -238,66 +232,81 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
                                             s->d_qtf, &creq, &cres, st);
   if (rc) return rc;
   int64_t cand = cres.total_candidates;
-  if (s->cfg.compute_clearance) {
-    // queries in contact have clearance 0; the rest go through the distance pass
-    if (cudaMemsetAsync(s->d_dist, 0, 8 * nq, st) != cudaSuccess ||
-        cudaMemsetAsync(s->d_obj, 0xff, 4 * nq, st) != cudaSuccess ||
-        cudaMemsetAsync(s->d_fcount, 0, 8, st) != cudaSuccess)
-      return FCLGPU_ERR_CUDA;
-    k_free_queries<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(nq, s->d_nc, s->d_qrefs, s->d_qtf, s->d_frefs,
-                                                                 s->d_ftf, s->d_fmap, s->d_fcount);
-    ++g_kernel_launches;
-    unsigned long long nfree = 0;
-    if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(&nfree, s->d_fcount, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return FCLGPU_ERR_CUDA;
-    if (nfree > 0) {
-      fclgpu_broadphase_distance_request dreq = {0, s->cfg.precision};
-      fclgpu_broadphase_distance_result dres = {s->d_fdist, s->d_fobj, nullptr, nullptr, 0, 0};
-      rc = fclgpu_broadphase_distance_device(s->scene, reinterpret_cast<const fclgpu_geometry_ref*>(s->d_frefs),
-                                             (int64_t)nfree, s->d_ftf, &dreq, &dres, st);
-      if (rc) return rc;
-      cand = std::max<int64_t>(cand, dres.total_candidates);
-      k_scatter_clearance<<<(unsigned)((nfree + 255) / 256), 256, 0, st>>>((long long)nfree, s->d_fmap, s->d_fdist,
-                                                                           s->d_fobj, s->d_dist, s->d_obj);
-      ++g_kernel_launches;
-      if (cudaGetLastError() != cudaSuccess) return FCLGPU_ERR_CUDA;
-    }
-    if (cudaMemcpyAsync(s->h_dist, s->d_dist, 8 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(s->h_obj, s->d_obj, 4 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-      return FCLGPU_ERR_CUDA;
-  }
   if (cudaMemcpyAsync(s->h_nc, s->d_nc, 8 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return FCLGPU_ERR_CUDA;
-  s->cand_per_query = 0.5 * s->cand_per_query + 0.5 * std::max(1.0, (double)cand / (double)std::max<int64_t>(nq, 1));
-  s->stats.queries += nq;
-  s->stats.candidates += cand;
-  // per-request reduction (order independent: min waypoint; clearance ties by (waypoint, link))
+  // first colliding waypoint (and its smallest link) per request
   w = 0;
   for (const Chunk& ch : chunks) {
     fclgpu_motion_result& r = ch.r->res;
-    for (int32_t k = ch.k0; k < ch.k1; ++k, ++w) {
-      for (int i = 0; i < L; ++i) {
-        const int64_t qi = w * L + i;
-        if (s->h_nc[qi] > 0 && (r.first_colliding_waypoint < 0 || k < r.first_colliding_waypoint))
+    for (int32_t k = ch.k0; k < ch.k1; ++k, ++w)
+      for (int i = 0; i < L; ++i)
+        if (s->h_nc[w * L + i] > 0 && (r.first_colliding_waypoint < 0 || k < r.first_colliding_waypoint)) {
           r.first_colliding_waypoint = k;
-        if (s->cfg.compute_clearance) {
-          const double d = s->h_dist[qi];
-          const bool better = d < r.min_clearance ||
-                              (d == r.min_clearance && (k < r.clearance_waypoint ||
-                                                        (k == r.clearance_waypoint && i < r.clearance_link)));
-          if (better) {
-            r.min_clearance = d;
-            r.clearance_waypoint = k;
-            r.clearance_link = i;
-            r.clearance_object = s->h_obj[qi];
-          }
+          r.clearance_link = i;
         }
+  }
+  if (s->cfg.compute_clearance) {
+    // a request in contact has clearance 0; the queries of the others go through
+    // the distance pass
+    int64_t nfree = 0;
+    w = 0;
+    for (const Chunk& ch : chunks) {
+      const int32_t n = ch.k1 - ch.k0;
+      if (ch.r->res.first_colliding_waypoint < 0)
+        for (int64_t qi = w * L; qi < (w + n) * L; ++qi) s->h_fidx[nfree++] = (int32_t)qi;
+      w += n;
+    }
+    if (nfree > 0) {
+      if (cudaMemcpyAsync(s->d_fmap, s->h_fidx, 4 * nfree, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return FCLGPU_ERR_CUDA;
+      k_gather_queries<<<(unsigned)((nfree + 255) / 256), 256, 0, st>>>(nfree, s->d_fmap, s->d_qrefs, s->d_qtf,
+                                                                        s->d_frefs, s->d_ftf);
+      ++g_kernel_launches;
+      if (cudaGetLastError() != cudaSuccess) return FCLGPU_ERR_CUDA;
+      fclgpu_broadphase_distance_request dreq = {0, s->cfg.precision};
+      fclgpu_broadphase_distance_result dres = {s->d_fdist, s->d_fobj, nullptr, nullptr, 0, 0};
+      rc = fclgpu_broadphase_distance_device(s->scene, reinterpret_cast<const fclgpu_geometry_ref*>(s->d_frefs),
+                                             nfree, s->d_ftf, &dreq, &dres, st);
+      if (rc) return rc;
+      cand = std::max<int64_t>(cand, dres.total_candidates);
+      if (cudaMemcpyAsync(s->h_dist, s->d_fdist, 8 * nfree, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaMemcpyAsync(s->h_obj, s->d_fobj, 4 * nfree, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return FCLGPU_ERR_CUDA;
+    }
+    // clearance: minimum over the contact-free queries (ties: smallest waypoint, then
+    // link); 0 at the first contact
+    int64_t f = 0;
+    w = 0;
+    for (const Chunk& ch : chunks) {
+      fclgpu_motion_result& r = ch.r->res;
+      const int32_t n = ch.k1 - ch.k0;
+      if (r.first_colliding_waypoint >= 0) {
+        r.min_clearance = 0.0;
+        r.clearance_waypoint = r.first_colliding_waypoint;
+        r.clearance_object = -1;
+      } else {
+        for (int32_t k = ch.k0; k < ch.k1; ++k)
+          for (int i = 0; i < L; ++i, ++f) {
+            const double d = s->h_dist[f];
+            const bool better = d < r.min_clearance ||
+                                (d == r.min_clearance && (k < r.clearance_waypoint ||
+                                                          (k == r.clearance_waypoint && i < r.clearance_link)));
+            if (better) {
+              r.min_clearance = d;
+              r.clearance_waypoint = k;
+              r.clearance_link = i;
+              r.clearance_object = s->h_obj[f];
+            }
+          }
       }
+      w += n;
     }
   }
+  s->cand_per_query = 0.5 * s->cand_per_query + 0.5 * std::max(1.0, (double)cand / (double)std::max<int64_t>(nq, 1));
+  s->stats.queries += nq;
+  s->stats.candidates += cand;
   return FCLGPU_OK;
 }
 
@@ -323,7 +332,7 @@ void worker_loop(fclgpu_server_s* s) {
         if (left <= 0) break;
         const int64_t share = std::max<int64_t>(1, left / (int64_t)remaining);
         --remaining;
-        const int32_t n = (int32_t)std::min<int64_t>(share, r->K - r->next_wp);
+        const int32_t n = (int32_t)std::min<int64_t>(std::min<int64_t>(share, kRequestChunk), r->K - r->next_wp);
         if (n <= 0) continue;
         chunks.push_back(Chunk{r, r->next_wp, r->next_wp + n});
         r->next_wp += n;
@@ -352,7 +361,9 @@ void worker_loop(fclgpu_server_s* s) {
       }
       std::vector<Request*> keep;
       for (Request* r : s->active) {
-        if (r->done_wp >= r->K || rc) {
+        // a request ends at its first contact: later waypoints change neither its
+        // first colliding waypoint nor its clearance (0)
+        if (r->done_wp >= r->K || r->res.first_colliding_waypoint >= 0 || rc) {
           r->done = true;
           r->res.reserved = rc;
           r->res.latency_ms = ms_between(r->submit, t1);
@@ -373,7 +384,7 @@ void free_server(fclgpu_server_s* s) {
                   (void*)s->d_fdist, (void*)s->d_fobj, (void*)s->d_fcount})
     if (p) cudaFree(p);
   for (void* p : {(void*)s->h_q, (void*)s->h_slot, (void*)s->h_bases, (void*)s->h_nc, (void*)s->h_dist,
-                  (void*)s->h_obj})
+                  (void*)s->h_obj, (void*)s->h_fidx})
     if (p) cudaFreeHost(p);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -440,6 +451,7 @@ int fclgpu_server_create(fclgpu_broadphase scene, const fclgpu_robot_desc* robot
   hm((void**)&s->h_nc, 8 * nq);
   hm((void**)&s->h_dist, 8 * nq);
   hm((void**)&s->h_obj, 4 * nq);
+  hm((void**)&s->h_fidx, 4 * nq);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_axis, s->axis.data(), 4 * L, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_offset, s->offset.data(), 24 * L, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->d_gtf, s->gtf.data(), 96 * L, cudaMemcpyHostToDevice);

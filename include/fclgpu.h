@@ -414,12 +414,16 @@ typedef struct {
   int32_t compute_clearance;      /* 1 = also report the minimum clearance */
 } fclgpu_server_config;
 
+/* A request stops at its first contact (waypoints are checked in order, in chunks):
+ * then min_clearance = 0 at (first colliding waypoint, its smallest colliding link).
+ * Otherwise min_clearance is the minimum over every waypoint and link of the
+ * broadphase distance, with its waypoint, link and scene object. */
 typedef struct {
   int32_t first_colliding_waypoint; /* smallest waypoint with any link in collision, -1 if none */
   int32_t clearance_waypoint;       /* argmin of the clearance (ties: smallest waypoint, then link) */
   int32_t clearance_link;
-  int32_t clearance_object;
-  double min_clearance;             /* min over waypoints and links of the broadphase distance (<= 0 in contact) */
+  int32_t clearance_object;         /* -1 for a request in contact */
+  double min_clearance;             /* 0 for a request in contact */
   double latency_ms;                /* submit -> result ready */
   double queue_ms;                  /* submit -> first step that included the request */
   int32_t num_steps;                /* loop steps that processed its waypoints */
