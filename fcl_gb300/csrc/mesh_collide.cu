@@ -151,6 +151,241 @@ __global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
   sink.flush();
 }
 
+// ---------------------------------------------------------------------------------
+// FP32 form with warp-batched leaf tests.  Each lane runs its item's DFS (BV tests,
+// the common case), but a leaf pair whose boxes overlap is not tested at once: it
+// goes to the warp's queue in shared memory, and whenever 32 are queued all lanes test
+// one each.  Without the queue nearly every warp step carried some lane's leaf test
+// (about one step in eleven is a leaf for each lane) and the other 31 lanes waited.
+// A lane's queued leaves keep its DFS order, so the contact ranks it receives are its
+// DFS-order ranks.  A lane learns of its contacts only when its leaves are tested, so
+// an item capped at num_max_contacts can run past FCL's stop point: the extra contacts
+// land past the cap and are dropped by the assembly, and such queries take their
+// statistics from the exact serial pass.
+// ---------------------------------------------------------------------------------
+constexpr int kWbWarps = 4;
+constexpr int kWbQueue = 64;  // >= 31 left over + 32 appended in one step
+constexpr int kWbSteps = 8;   // DFS steps a lane runs between two warp synchronisations
+
+struct WbCtx {
+  QueryF32 qf;
+  const float4* tri_a;
+  const float4* tri_b;
+  long long qi;
+  long long item;
+  int pair;
+  int ncont;    // contacts recorded for the lane's item
+  int pending;  // queued leaf pairs of the lane's item
+  int nrecheck;
+};
+
+template <int STACK>
+__global__ void __launch_bounds__(128) k_collide_round_wb(const CollideLaunch L) {
+  __shared__ WbCtx ctx[kWbWarps][32];
+  __shared__ int3 queue[kWbWarps][kWbQueue];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1u;
+  SplitSink sink;
+  sink.rec = L.records;
+  sink.cap = L.record_cap;
+  sink.ctr = &L.ctr->records;
+  sink.status = &L.ctr->status;
+  sink.base = -1;
+  sink.used = 0;
+  sink.items = L.items;
+  sink.item_cap = L.item_cap;
+  sink.item_ctr = &L.ctr->items;
+  sink.child_start = L.child_start;
+  sink.child_count = L.child_count;
+  const long long span = L.item_hi - L.item_lo;
+  WbCtx& me = ctx[w][lane];
+
+  bool have = false, draining = false, exhausted = false, dumped = false;
+  long long item = 0, qi = 0;
+  int b1 = 0, b2 = 0, sp = 0;
+  int2 stk[STACK];
+  long long nbv = 0, nleaf = 0;
+  DevMesh A, B;
+  QueryF32 qf;
+  M3<double> R;
+  V3<double> T;
+  int qn = 0;  // queue length (the same in every lane)
+
+  for (;;) {
+    // (a) a free lane takes the next item
+    if (!have && !draining && !exhausted) {
+      const long long k = (long long)atomicAdd(&L.ctr->work, 1ull);
+      if (k >= span) {
+        exhausted = true;
+      } else {
+        item = L.item_lo + k;
+        if (item < L.n) {
+          qi = item;
+          b1 = b2 = 0;
+        } else {
+          const int4 it = L.items[item];
+          qi = it.x;
+          b1 = it.y;
+          b2 = it.z;
+        }
+        const int pi = L.pair_of_query ? L.pair_of_query[qi] : 0;
+        const int2 mp = L.pairs[pi];
+        A = L.meshes[mp.x];
+        B = L.meshes[mp.y];
+        double ta[12];
+        query_transform_collide(L.tf1, L.tf2, qi, R, T, ta);
+        make_query_f32(R, T, A.cmax, B.cmax, A.vmax, B.vmax, qf);
+        me.qf = qf;
+        me.tri_a = reinterpret_cast<const float4*>(A.tri32);
+        me.tri_b = reinterpret_cast<const float4*>(B.tri32);
+        me.qi = qi;
+        me.item = item;
+        me.pair = pi;
+        me.ncont = 0;
+        me.pending = 0;
+        me.nrecheck = 0;
+        sp = 0;
+        nbv = nleaf = 0;
+        dumped = false;
+        have = L.num_max_contacts > 0;
+        draining = !have;
+      }
+    }
+    // (b) up to kWbSteps DFS steps; stop at the first leaf pair to queue
+    bool produced = false;
+    int3 entry = make_int3(lane, 0, 0);
+    for (int step = 0; step < kWbSteps && have && !produced; ++step) {
+      if (me.ncont >= L.num_max_contacts) {  // canStop (known contacts)
+        have = false;
+        draining = true;
+        break;
+      }
+      if (nbv >= L.budget) {
+        sink.dumped = false;
+        sink.dump(item, qi, make_int2(b1, b2), stk, sp);
+        dumped = sink.dumped;
+        have = false;
+        draining = true;
+        break;
+      }
+      const float4* pa = reinterpret_cast<const float4*>(A.nodes32) + 4 * (long long)b1;
+      const float4* pb = reinterpret_cast<const float4*>(B.nodes32) + 4 * (long long)b2;
+      const float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), a2 = __ldg(pa + 2), ea = __ldg(pa + 3);
+      const float4 x0 = __ldg(pb), x1 = __ldg(pb + 1), x2 = __ldg(pb + 2), eb = __ldg(pb + 3);
+      const int c1 = __float_as_int(ea.w), c2 = __float_as_int(eb.w);
+      int r = obb_overlap_f32(qf, a0, a1, a2, ea, x0, x1, x2, eb);
+      if (r == F_UNSURE) {
+        ++me.nrecheck;
+        r = bv_overlap64(A, B, b1, b2, R, T) ? F_TRUE : F_FALSE;
+      }
+      ++nbv;
+      bool next_from_stack = true;
+      if (r == F_TRUE) {
+        const bool l1 = c1 < 0, l2 = c2 < 0;
+        if (l1 && l2) {
+          ++nleaf;
+          produced = true;
+          entry = make_int3(lane, -(c1 + 1), -(c2 + 1));
+        } else {
+          const bool first_over_second = l2 ? true : (l1 ? false : size_key(A, b1) > size_key(B, b2));
+          if (sp >= STACK) {
+            atomicOr(&L.ctr->status, DEV_ERR_STACK);
+            have = false;
+            draining = true;
+            break;
+          }
+          if (first_over_second) {
+            stk[sp++] = make_int2(c1 + 1, b2);
+            b1 = c1;
+          } else {
+            stk[sp++] = make_int2(b1, c2 + 1);
+            b2 = c2;
+          }
+          next_from_stack = false;
+        }
+      }
+      if (next_from_stack) {
+        if (sp == 0) {
+          have = false;
+          draining = true;
+        } else {
+          const int2 e = stk[--sp];
+          b1 = e.x;
+          b2 = e.y;
+        }
+      }
+    }
+    // (c) queue the leaf pairs found in this step, in lane order
+    const unsigned pm = __ballot_sync(full, produced);
+    if (produced) {
+      queue[w][qn + __popc(pm & lt)] = entry;
+      ++me.pending;
+    }
+    qn += __popc(pm);
+    __syncwarp();
+    // (d) test queued leaves: in batches of 32, and whatever is left once no lane can
+    // produce more before its queued leaves are known
+    const unsigned running = __ballot_sync(full, have);
+    while (qn >= 32 || (qn > 0 && running == 0)) {
+      const int cnt = qn < 32 ? qn : 32;
+      const bool mine = lane < cnt;
+      const int3 e = mine ? queue[w][lane] : make_int3(-1 - lane, 0, 0);
+      bool hit = false;
+      if (mine) {
+        const WbCtx& o = ctx[w][e.x];
+        const float4* ta4 = o.tri_a + 3 * (long long)e.y;
+        const float4* tb4 = o.tri_b + 3 * (long long)e.z;
+        int r = tri_intersect_f32(o.qf, __ldg(ta4), __ldg(ta4 + 1), __ldg(ta4 + 2), __ldg(tb4), __ldg(tb4 + 1),
+                                  __ldg(tb4 + 2));
+        if (r == F_UNSURE) {
+          atomicAdd(&ctx[w][e.x].nrecheck, 1);
+          const int2 mp = L.pairs[o.pair];
+          M3<double> Ro;
+          V3<double> To;
+          double ta[12];
+          query_transform_collide(L.tf1, L.tf2, o.qi, Ro, To, ta);
+          r = leaf_collide64(L.meshes[mp.x], L.meshes[mp.y], e.y, e.z, Ro, To) ? F_TRUE : F_FALSE;
+        }
+        hit = (r == F_TRUE);
+      }
+      const unsigned hm = __ballot_sync(full, hit);
+      const unsigned peers = __match_any_sync(full, e.x);
+      if (hit) {
+        const int rank = ctx[w][e.x].ncont + __popc(peers & hm & lt);
+        sink.push((int)ctx[w][e.x].item, rank, e.y, e.z);
+      }
+      __syncwarp();
+      if (mine && (peers & lt) == 0) {  // the first lane of each owner's group
+        ctx[w][e.x].ncont += __popc(peers & hm);
+        ctx[w][e.x].pending -= __popc(peers);
+      }
+      // drop the tested entries
+      int3 rest = make_int3(0, 0, 0);
+      const bool keep = lane < qn - cnt;
+      if (keep) rest = queue[w][cnt + lane];
+      __syncwarp();
+      if (keep) queue[w][lane] = rest;
+      qn -= cnt;
+      __syncwarp();
+    }
+    // (e) a lane whose item ended and whose leaves are all tested records the item
+    if (draining && me.pending == 0) {
+      L.own[item] = me.ncont;
+      if (!dumped) L.child_count[item] = 0;
+      if (L.want_stats) {
+        if (L.nbv) atomicAdd((unsigned long long*)(L.nbv + qi), (unsigned long long)nbv);
+        if (L.nleaf) atomicAdd((unsigned long long*)(L.nleaf + qi), (unsigned long long)nleaf);
+        if (L.nrecheck) atomicAdd((unsigned long long*)(L.nrecheck + qi), (unsigned long long)me.nrecheck);
+      }
+      draining = false;
+    }
+    __syncwarp();
+    if (__all_sync(full, exhausted && !have && !draining) && qn == 0) break;
+  }
+  sink.flush();
+}
+
 // total[i] = own[i] + sum of the totals of its children (children are in a later
 // round, whose totals are already known when rounds are processed last to first).
 __global__ void k_item_totals(const CollideLaunch L, long long lo, long long hi, long long* total) {
@@ -172,7 +407,9 @@ __global__ void k_item_counts(const CollideLaunch L, const long long* total, int
   const long long t = total[q];
   const long long m = L.num_max_contacts;
   L.counts[q] = (int32_t)(t < m ? t : m);
-  if (t >= m && L.child_count[q] > 0 && capped) {
+  // a capped query may have run past FCL's stop point (split across items, or its
+  // leaf tests batched after further BV tests): its statistics need the serial pass
+  if (t >= m && capped) {
     const unsigned long long k = atomicAdd(ncapped, 1ull);
     capped[k] = (int32_t)q;
   }
@@ -382,9 +619,9 @@ cudaError_t launch_collide_round(const CollideLaunch& L, int precision, int stac
       k_collide_round<0, 256><<<grid, block, 0, s>>>(L);
   } else {
     if (stack_entries <= 64)
-      k_collide_round<1, 64><<<grid, block, 0, s>>>(L);
+      k_collide_round_wb<64><<<grid, 32 * kWbWarps, 0, s>>>(L);
     else
-      k_collide_round<1, 256><<<grid, block, 0, s>>>(L);
+      k_collide_round_wb<256><<<grid, 32 * kWbWarps, 0, s>>>(L);
   }
   return cudaGetLastError();
 }
@@ -457,8 +694,8 @@ int collide_round_grid(int precision, int stack_entries, int block) {
   if (precision == 0)
     k = stack_entries <= 64 ? (const void*)k_collide_round<0, 64> : (const void*)k_collide_round<0, 256>;
   else
-    k = stack_entries <= 64 ? (const void*)k_collide_round<1, 64> : (const void*)k_collide_round<1, 256>;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, 0);
+    k = stack_entries <= 64 ? (const void*)k_collide_round_wb<64> : (const void*)k_collide_round_wb<256>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, precision == 0 ? block : 32 * kWbWarps, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }
