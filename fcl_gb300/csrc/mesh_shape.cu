@@ -189,20 +189,35 @@ __global__ void __launch_bounds__(128) k_ms_chunk_tests(MeshShapeLaunch L, const
     double P[9];
     load_tri_local(g.m, leaf_prim[j], P);
     SimplexVert V[kSimplexSlots];
-    EpaState epa;
-    hit[j] = shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa) ? 1 : 0;
+    hit[j] = shape_triangle_gjk_stage(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V);
   }
 }
 
-__global__ void k_ms_chunk_update(MeshShapeLaunch L, const int32_t* act, long long nact, int64_t* cur,
-                                  const int64_t* off, const int32_t* hit, int32_t* next, unsigned long long* nnext) {
+// Walks the chunk in DFS order; a leaf GJK found inside is confirmed by EPA (as
+// shapeTriangleIntersect does) only while the pair still needs contacts.
+__global__ void __launch_bounds__(128) k_ms_chunk_update(MeshShapeLaunch L, const int32_t* act, long long nact,
+                                                         int64_t* cur, const int64_t* off, const int32_t* leaf_prim,
+                                                         const int32_t* hit, int32_t* next,
+                                                         unsigned long long* nnext) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
     const long long i = act[a];
     const long long end = off[i + 1];
     const long long j1 = cur[i] + kChunk < end ? cur[i] + kChunk : end;
     int c = L.counts[i];
-    for (long long j = cur[i]; j < j1 && c < L.max_contacts; ++j) c += hit[j];
+    for (long long j = cur[i]; j < j1 && c < L.max_contacts; ++j) {
+      if (hit[j] == 2) {
+        ++c;
+      } else if (hit[j] == 1) {
+        PairGeom g;
+        pair_geom(L, i, g);
+        double P[9];
+        load_tri_local(g.m, leaf_prim[j], P);
+        SimplexVert V[kSimplexSlots];
+        EpaState epa;
+        if (shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa)) ++c;
+      }
+    }
     L.counts[i] = c;
     cur[i] = j1;
     if (c < L.max_contacts && j1 < end) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
@@ -292,7 +307,7 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
       while (nact > 0) {
         if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
         k_ms_chunk_tests<<<grid128(nact * kChunk), 128, 0, s>>>(L, act, nact, cur, off, leaf_prim, hit);
-        k_ms_chunk_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, cur, off, hit, next, nnext);
+        k_ms_chunk_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, cur, off, leaf_prim, hit, next, nnext);
         g_kernel_launches += 2;
         unsigned long long nn = 0;
         if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||

@@ -560,6 +560,29 @@ FCLG_HD bool shape_triangle_intersect(const ShapeRef& A, const M3<double>& Rs, c
   return o.hit != 0;
 }
 
+// First stage of shapeTriangleIntersect: 0 = no intersection, 1 = GJK reports the
+// origin inside (EPA still decides), 2 = intersection (sphere closed form).
+FCLG_HD int shape_triangle_gjk_stage(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
+                                     const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
+  if (A.s.type == SHAPE_SPHERE) {
+    const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
+    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 2
+                                                                                                          : 0;
+  }
+  ShapeRef B;
+  B.s.type = SHAPE_TRIANGLE;
+  B.s.voff = 0;
+  B.s.vcnt = 3;
+  B.s.pad = 0;
+  B.s.p[0] = B.s.p[1] = B.s.p[2] = 0;
+  B.verts = P;
+  GjkState g;
+  make_minkowski(A, Rs, ts, B, Rm, tm, g.shape);
+  g.V = V;
+  g.tolerance = kGjkTol;
+  return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), 128) == GJK_INSIDE ? 1 : 0;
+}
+
 // shapeTriangleDistance; ps on the shape, pt on the triangle, in FCL's frames
 FCLG_HD bool shape_triangle_distance(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
                                      const M3<double>& Rm, const D3v& tm, SimplexVert* V, double& d, D3v& ps,
