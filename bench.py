@@ -255,6 +255,15 @@ def run_gpu(args):
         return api.collide_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000,
                                  precision=prec, statistics=stats, stream=stream.cuda_stream, budget=args.budget)
 
+    # autotuned knobs of the collide rounds (outside the timed region; results do not
+    # depend on them)
+    tuning = None
+    if not args.no_tune:
+        t_tune = time.time()
+        tuning = api.autotune_collide(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000,
+                                      sample=args.tune_sample)
+        tuning["seconds"] = time.time() - t_tune
+
     # reference run for exact-hit check and algorithmic byte counts (outside timing)
     ref64 = step("fp64", stats=True)
     fp32 = step("fp32", stats=True)
@@ -395,7 +404,8 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "queries": n, "mesh_pairs": int(w.pairs.shape[0]),
                        "triangles_total": int(sum(m[1].shape[0] for m in w.meshes)),
                        "num_max_contacts": 100000, "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "tuning": tuning},
             "clocks": clocks,
             "e2e": {"value": world * n / (t_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e, "exact_hits": e2e_hits},
@@ -436,6 +446,8 @@ def main():
     ap.add_argument("--fp64-scale", type=float, default=0.1,
                     help="fraction of the queries the plain FP64 form is timed on")
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
+    ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
     ap.add_argument("--serve-requests", type=int, default=200, help="requests in the Poisson run")
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.7 x measured capacity)")

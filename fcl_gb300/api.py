@@ -682,3 +682,53 @@ def mesh_shape_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_
                                             shape_idx.ctypes.data, tf_mesh.ctypes.data, tf_shape.ctypes.data,
                                             C.byref(req), C.byref(res), stream), "fclgpu_mesh_shape_batch")
     return out
+
+
+# ------------------------------------------------------------------- autotuner ----
+
+def get_collide_tuning():
+    b, s = C.c_int32(), C.c_int32()
+    N.check(N.lib().fclgpu_get_collide_tuning(C.byref(b), C.byref(s)), "fclgpu_get_collide_tuning")
+    return int(b.value), int(s.value)
+
+
+def set_collide_tuning(budget: int, leaf_batch_steps: int) -> None:
+    N.check(N.lib().fclgpu_set_collide_tuning(int(budget), int(leaf_batch_steps)), "fclgpu_set_collide_tuning")
+
+
+def autotune_collide(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, sample=65536,
+                     budgets=(1024, 4096, 16384), steps=(4, 8, 16, 32), repeats=2, seed=0):
+    """Picks the collide rounds' knobs (BV-test budget per item, DFS steps between warp
+    leaf batches) for a workload: times the FP32 form on a uniform sample of its
+    queries (torch CUDA tensors) for every combination and keeps the fastest.  Results
+    do not depend on the knobs; only the time does.  Returns the timings (ms)."""
+    import torch
+    n = tf2.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    idx = torch.randperm(n, generator=g)[: min(n, sample)].sort().values.to(tf2.device)
+    s_tf2 = tf2[idx].contiguous()
+    s_tf1 = None if tf1 is None else tf1[idx].contiguous()
+    s_pq = None if pair_of_query is None else pair_of_query[idx].contiguous()
+    stream = torch.cuda.current_stream(tf2.device)
+    timings = {}
+    best = None
+    for b in budgets:
+        for st in steps:
+            set_collide_tuning(b, st)
+            collide_batch(meshes, pairs, s_tf1, s_tf2, pair_of_query=s_pq, num_max_contacts=num_max_contacts,
+                          contacts=False)
+            torch.cuda.synchronize()
+            ms = []
+            for _ in range(repeats):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                collide_batch(meshes, pairs, s_tf1, s_tf2, pair_of_query=s_pq, num_max_contacts=num_max_contacts,
+                              contacts=False, stream=stream.cuda_stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            timings[(b, st)] = min(ms)
+            if best is None or timings[(b, st)] < timings[best]:
+                best = (b, st)
+    set_collide_tuning(*best)
+    return {"best": best, "timings_ms": {f"{k[0]}/{k[1]}": v for k, v in timings.items()}}

@@ -142,7 +142,11 @@ struct SplitScratch {
 };
 SplitScratch g_split;
 
+// Tuning knobs of the FP32 collide rounds (set by fclgpu_set_collide_tuning, picked by
+// the autotuner in fcl_gb300/api.py): BV tests per item per round, DFS steps per lane
+// between two warp leaf batches.
 int64_t g_default_budget = 4096;
+int32_t g_wb_steps = 8;
 
 int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
                  const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
@@ -190,6 +194,7 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
     L.items = (int4*)P.items.p;
     L.item_cap = item_cap;
     L.budget = budget;
+    L.wb_steps = g_wb_steps;
     L.own = (int32_t*)P.own.p;
     L.child_start = (int32_t*)P.cstart.p;
     L.child_count = (int32_t*)P.ccount.p;
@@ -318,6 +323,23 @@ int fclgpu_last_kernel_time(double* ms) {
   if (!ms) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   if (g_last_kernel_ms < 0) return fail(FCLGPU_ERR_NOT_INITIALIZED, "no batch has run");
   *ms = g_last_kernel_ms;
+  return FCLGPU_OK;
+}
+
+int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps) {
+  if (budget < 16 || budget > (1 << 24) || leaf_batch_steps < 1 || leaf_batch_steps > 256)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "tuning value out of range");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  g_default_budget = budget;
+  g_wb_steps = leaf_batch_steps;
+  return FCLGPU_OK;
+}
+
+int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps) {
+  if (!budget || !leaf_batch_steps) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  *budget = (int32_t)g_default_budget;
+  *leaf_batch_steps = g_wb_steps;
   return FCLGPU_OK;
 }
 

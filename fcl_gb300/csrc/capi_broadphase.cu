@@ -90,7 +90,7 @@ struct BpScratch {
 };
 BpScratch g_bs;
 
-// Phase times of the most recent collide (row 0) and distance (row 1) call, ms:
+// Phase times of collide (row 0) and distance (row 1) calls, accumulated until read, ms:
 // [0] query prep + candidate passes, [1] shape-shape pairs, [2] mesh-shape pairs,
 // [3] mesh-mesh pairs, [4] reduction; [5] candidates, [6] mesh-shape and [7] mesh-mesh
 // pairs evaluated.
@@ -102,7 +102,7 @@ struct PhaseClock {
   cudaStream_t s;
   std::chrono::steady_clock::time_point t;
   PhaseClock(int r, cudaStream_t st) : row(r), s(st), t(std::chrono::steady_clock::now()) {
-    for (int k = 0; k < 8; ++k) g_phase[r][k] = 0.0;
+    (void)r;
   }
   void tick(int k) {
     cudaStreamSynchronize(s);
@@ -470,7 +470,7 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
   RCB(scan_counts(nq, dctr, &hc, &total, s));
   res->total_candidates = total;
   res->total_node_visits = hc.visits;
-  g_phase[0][5] = (double)total;
+  g_phase[0][5] += (double)total;
   RCB(ensure_pair_buffers(total));
   CKB(g_bs.hit.ensure(4 * (size_t)std::max<int64_t>(total, 1)), "hits");
   const int64_t* off = g_bs.offsets.as<int64_t>();
@@ -495,12 +495,12 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
       CKB(launch_bp_query_done(nq, off, hit, req->num_max_contacts, qdone, s), "query flags");
     }
     RCB(run_mixed(bp, S, Q, total, 0, req->num_max_contacts, dctr, s, qdone));
-    g_phase[0][6] = (double)g_last_mixed;
+    g_phase[0][6] += (double)g_last_mixed;
     pc.tick(2);
     if (qdone) CKB(launch_bp_query_done(nq, off, hit, req->num_max_contacts, qdone, s), "query flags");
     int64_t nl = 0;
     RCB(list_kind(total, 1, dctr, &nl, s, qdone));
-    g_phase[0][7] = (double)nl;
+    g_phase[0][7] += (double)nl;
     if (nl > 0) {
       CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
       CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
@@ -561,7 +561,7 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
   RCB(scan_counts(nq, dctr, &hc, &total, s));
   res->total_candidates = total;
   res->total_node_visits = hc.visits;
-  g_phase[1][5] = (double)total;
+  g_phase[1][5] += (double)total;
   RCB(ensure_pair_buffers(total));
   const size_t t = (size_t)std::max<int64_t>(total, 1);
   CKB(g_bs.dist.ensure(8 * t), "distances");
@@ -582,11 +582,11 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
         "shape narrowphase");
     pc.tick(1);
     RCB(run_mixed(bp, S, Q, total, 1, 0, dctr, s));
-    g_phase[1][6] = (double)g_last_mixed;
+    g_phase[1][6] += (double)g_last_mixed;
     pc.tick(2);
     int64_t nl = 0;
     RCB(list_kind(total, 1, dctr, &nl, s));
-    g_phase[1][7] = (double)nl;
+    g_phase[1][7] += (double)nl;
     if (nl > 0) {
       CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
       CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
@@ -692,7 +692,10 @@ int fclgpu_broadphase_last_phase_ms(double* out16) {
   if (!out16) return FCLGPU_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(g_bp_mu);
   for (int r = 0; r < 2; ++r)
-    for (int k = 0; k < 8; ++k) out16[8 * r + k] = g_phase[r][k];
+    for (int k = 0; k < 8; ++k) {
+      out16[8 * r + k] = g_phase[r][k];
+      g_phase[r][k] = 0.0;
+    }
   return FCLGPU_OK;
 }
 

@@ -46,6 +46,7 @@ struct CollideLaunch {
   int64_t item_cap;
   int64_t item_lo, item_hi;
   int64_t budget;                // BV tests per item per round
+  int32_t wb_steps;              // FP32 form: DFS steps a lane runs between warp leaf batches
   int32_t* own;                  // per item: contacts found by the item itself
   int32_t* child_start;          // per item: id of its first child item
   int32_t* child_count;          // per item: number of child items (0 = finished)

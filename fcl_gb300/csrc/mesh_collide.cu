@@ -165,7 +165,6 @@ __global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
 // ---------------------------------------------------------------------------------
 constexpr int kWbWarps = 4;
 constexpr int kWbQueue = 64;  // >= 31 left over + 32 appended in one step
-constexpr int kWbSteps = 8;   // DFS steps a lane runs between two warp synchronisations
 
 struct WbCtx {
   QueryF32 qf;
@@ -255,7 +254,7 @@ __global__ void __launch_bounds__(128) k_collide_round_wb(const CollideLaunch L)
     // (b) up to kWbSteps DFS steps; stop at the first leaf pair to queue
     bool produced = false;
     int3 entry = make_int3(lane, 0, 0);
-    for (int step = 0; step < kWbSteps && have && !produced; ++step) {
+    for (int step = 0; step < L.wb_steps && have && !produced; ++step) {
       if (me.ncont >= L.num_max_contacts) {  // canStop (known contacts)
         have = false;
         draining = true;

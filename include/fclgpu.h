@@ -187,6 +187,13 @@ FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
 /* Device time (ms, CUDA events on the batch's stream) of the traversal kernel of the
  * most recent collide or distance batch.  No counterpart in FCL (profiling hook). */
 FCLGPU_API int fclgpu_last_kernel_time(double* ms);
+/* Knobs of the collide rounds, chosen by the autotuner (fcl_gb300/api.py
+ * autotune_collide): BV tests an item runs per round before its frontier is re-queued
+ * (the request's budget overrides it when non-zero), and the DFS steps a lane runs
+ * between two warp-wide batches of leaf tests (FP32 form).  Results do not depend on
+ * them.  No counterpart in FCL. */
+FCLGPU_API int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps);
+FCLGPU_API int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps);
 
 /* ---- convex shapes (fcl::Box/Sphere/Capsule/Cylinder/Cone/Convex, geometry/shape/*.h) --
  * GJK/EPA of FCL's own solver (GJKSolver_indep, narrowphase/detail/gjk_solver_indep.h)
@@ -383,8 +390,9 @@ FCLGPU_API int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fcl
 FCLGPU_API int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
                                           const double* tf, const fclgpu_broadphase_distance_request* req,
                                           fclgpu_broadphase_distance_result* res, void* stream);
-/* Wall-clock phases of the most recent broadphase collide (out16[0..7]) and distance
- * (out16[8..15]) call: [0] query setup and candidate passes, [1] shape-shape pairs,
+/* Wall-clock phases of the broadphase collide (out16[0..7]) and distance (out16[8..15])
+ * calls made since the previous read (reading resets them): [0] query setup and
+ * candidate passes, [1] shape-shape pairs,
  * [2] mesh-shape pairs, [3] mesh-mesh pairs, [4] reduction (ms); [5] candidate pairs,
  * [6] mesh-shape and [7] mesh-mesh pairs evaluated.  No counterpart in FCL. */
 FCLGPU_API int fclgpu_broadphase_last_phase_ms(double* out16);
