@@ -687,21 +687,23 @@ def mesh_shape_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_
 # ------------------------------------------------------------------- autotuner ----
 
 def get_collide_tuning():
-    b, s = C.c_int32(), C.c_int32()
-    N.check(N.lib().fclgpu_get_collide_tuning(C.byref(b), C.byref(s)), "fclgpu_get_collide_tuning")
-    return int(b.value), int(s.value)
+    b, s, v = C.c_int32(), C.c_int32(), C.c_int32()
+    N.check(N.lib().fclgpu_get_collide_tuning(C.byref(b), C.byref(s), C.byref(v)), "fclgpu_get_collide_tuning")
+    return int(b.value), int(s.value), int(v.value)
 
 
-def set_collide_tuning(budget: int, leaf_batch_steps: int) -> None:
-    N.check(N.lib().fclgpu_set_collide_tuning(int(budget), int(leaf_batch_steps)), "fclgpu_set_collide_tuning")
+def set_collide_tuning(budget: int, leaf_batch_steps: int, variant: int = 0) -> None:
+    N.check(N.lib().fclgpu_set_collide_tuning(int(budget), int(leaf_batch_steps), int(variant)),
+            "fclgpu_set_collide_tuning")
 
 
 def autotune_collide(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, sample=65536,
-                     budgets=(1024, 4096, 16384), steps=(4, 8, 16, 32), repeats=2, seed=0):
+                     budgets=(1024, 4096, 16384), steps=(4, 8, 16, 32), variants=(0, 1), repeats=2, seed=0):
     """Picks the collide rounds' knobs (BV-test budget per item, DFS steps between warp
-    leaf batches) for a workload: times the FP32 form on a uniform sample of its
-    queries (torch CUDA tensors) for every combination and keeps the fastest.  Results
-    do not depend on the knobs; only the time does.  Returns the timings (ms)."""
+    leaf batches, register variant) for a workload: times the FP32 form on a uniform
+    sample of its queries (torch CUDA tensors) for every combination and keeps the
+    fastest.  Results do not depend on the knobs; only the time does.  Returns the
+    timings (ms)."""
     import torch
     n = tf2.shape[0]
     g = torch.Generator(device="cpu").manual_seed(seed)
@@ -712,23 +714,25 @@ def autotune_collide(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contac
     stream = torch.cuda.current_stream(tf2.device)
     timings = {}
     best = None
-    for b in budgets:
-        for st in steps:
-            set_collide_tuning(b, st)
-            collide_batch(meshes, pairs, s_tf1, s_tf2, pair_of_query=s_pq, num_max_contacts=num_max_contacts,
-                          contacts=False)
-            torch.cuda.synchronize()
-            ms = []
-            for _ in range(repeats):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
+    for var in variants:
+        for b in budgets:
+            for st in steps:
+                set_collide_tuning(b, st, var)
                 collide_batch(meshes, pairs, s_tf1, s_tf2, pair_of_query=s_pq, num_max_contacts=num_max_contacts,
-                              contacts=False, stream=stream.cuda_stream)
-                e1.record(stream)
+                              contacts=False)
                 torch.cuda.synchronize()
-                ms.append(e0.elapsed_time(e1))
-            timings[(b, st)] = min(ms)
-            if best is None or timings[(b, st)] < timings[best]:
-                best = (b, st)
+                ms = []
+                for _ in range(repeats):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    collide_batch(meshes, pairs, s_tf1, s_tf2, pair_of_query=s_pq,
+                                  num_max_contacts=num_max_contacts, contacts=False, stream=stream.cuda_stream)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    ms.append(e0.elapsed_time(e1))
+                key = (b, st, var)
+                timings[key] = min(ms)
+                if best is None or timings[key] < timings[best]:
+                    best = key
     set_collide_tuning(*best)
-    return {"best": best, "timings_ms": {f"{k[0]}/{k[1]}": v for k, v in timings.items()}}
+    return {"best": list(best), "timings_ms": {f"{k[0]}/{k[1]}/{k[2]}": v for k, v in timings.items()}}

@@ -147,6 +147,7 @@ SplitScratch g_split;
 // between two warp leaf batches.
 int64_t g_default_budget = 4096;
 int32_t g_wb_steps = 8;
+int32_t g_wb_variant = 0;
 
 int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
                  const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
@@ -195,11 +196,12 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
     L.item_cap = item_cap;
     L.budget = budget;
     L.wb_steps = g_wb_steps;
+    L.wb_variant = g_wb_variant;
     L.own = (int32_t*)P.own.p;
     L.child_start = (int32_t*)P.cstart.p;
     L.child_count = (int32_t*)P.ccount.p;
     const int block = 128;
-    const int grid = collide_round_grid(req->precision, stack, block);
+    const int grid = collide_round_grid(req->precision, stack, block, g_wb_variant);
     P.rounds.clear();
     int64_t lo = 0, hi = n;
     bool retry = false;
@@ -326,20 +328,23 @@ int fclgpu_last_kernel_time(double* ms) {
   return FCLGPU_OK;
 }
 
-int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps) {
-  if (budget < 16 || budget > (1 << 24) || leaf_batch_steps < 1 || leaf_batch_steps > 256)
+int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps, int32_t variant) {
+  if (budget < 16 || budget > (1 << 24) || leaf_batch_steps < 1 || leaf_batch_steps > 256 || variant < 0 ||
+      variant > 1)
     return fail(FCLGPU_ERR_INVALID_ARGUMENT, "tuning value out of range");
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   g_default_budget = budget;
   g_wb_steps = leaf_batch_steps;
+  g_wb_variant = variant;
   return FCLGPU_OK;
 }
 
-int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps) {
-  if (!budget || !leaf_batch_steps) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
+int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps, int32_t* variant) {
+  if (!budget || !leaf_batch_steps || !variant) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   std::lock_guard<std::recursive_mutex> lk(g_mu);
   *budget = (int32_t)g_default_budget;
   *leaf_batch_steps = g_wb_steps;
+  *variant = g_wb_variant;
   return FCLGPU_OK;
 }
 

@@ -47,6 +47,7 @@ struct CollideLaunch {
   int64_t item_lo, item_hi;
   int64_t budget;                // BV tests per item per round
   int32_t wb_steps;              // FP32 form: DFS steps a lane runs between warp leaf batches
+  int32_t wb_variant;            // FP32 form: 0 = unbounded registers, 1 = 128 registers
   int32_t* own;                  // per item: contacts found by the item itself
   int32_t* child_start;          // per item: id of its first child item
   int32_t* child_count;          // per item: number of child items (0 = finished)
@@ -65,7 +66,7 @@ cudaError_t launch_scatter_items(const CollideLaunch& L, int64_t nrec, const int
 // Serial exact traversal of the listed queries, statistics only (counts untouched).
 cudaError_t launch_collide_stats(const CollideLaunch& L, const int32_t* list, int64_t nlist, int precision,
                                  int stack_entries, cudaStream_t s);
-int collide_round_grid(int precision, int stack_entries, int block);
+int collide_round_grid(int precision, int stack_entries, int block, int variant);
 
 struct DistanceLaunch {
   const DevMesh* meshes;

@@ -178,8 +178,10 @@ struct WbCtx {
   int nrecheck;
 };
 
-template <int STACK>
-__global__ void __launch_bounds__(128) k_collide_round_wb(const CollideLaunch L) {
+// MINB: blocks per SM the register allocation targets (1 = no limit, 158 registers;
+// 4 = 128 registers with a few spills); the autotuner picks the faster.
+template <int STACK, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLaunch L) {
   __shared__ WbCtx ctx[kWbWarps][32];
   __shared__ int3 queue[kWbWarps][kWbQueue];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -616,11 +618,16 @@ cudaError_t launch_collide_round(const CollideLaunch& L, int precision, int stac
       k_collide_round<0, 64><<<grid, block, 0, s>>>(L);
     else
       k_collide_round<0, 256><<<grid, block, 0, s>>>(L);
+  } else if (L.wb_variant == 1) {
+    if (stack_entries <= 64)
+      k_collide_round_wb<64, 4><<<grid, 32 * kWbWarps, 0, s>>>(L);
+    else
+      k_collide_round_wb<256, 4><<<grid, 32 * kWbWarps, 0, s>>>(L);
   } else {
     if (stack_entries <= 64)
-      k_collide_round_wb<64><<<grid, 32 * kWbWarps, 0, s>>>(L);
+      k_collide_round_wb<64, 1><<<grid, 32 * kWbWarps, 0, s>>>(L);
     else
-      k_collide_round_wb<256><<<grid, 32 * kWbWarps, 0, s>>>(L);
+      k_collide_round_wb<256, 1><<<grid, 32 * kWbWarps, 0, s>>>(L);
   }
   return cudaGetLastError();
 }
@@ -685,15 +692,17 @@ cudaError_t launch_collide_stats(const CollideLaunch& L, const int32_t* list, in
   return cudaGetLastError();
 }
 
-int collide_round_grid(int precision, int stack_entries, int block) {
+int collide_round_grid(int precision, int stack_entries, int block, int variant) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const void* k;
   if (precision == 0)
     k = stack_entries <= 64 ? (const void*)k_collide_round<0, 64> : (const void*)k_collide_round<0, 256>;
+  else if (variant == 1)
+    k = stack_entries <= 64 ? (const void*)k_collide_round_wb<64, 4> : (const void*)k_collide_round_wb<256, 4>;
   else
-    k = stack_entries <= 64 ? (const void*)k_collide_round_wb<64> : (const void*)k_collide_round_wb<256>;
+    k = stack_entries <= 64 ? (const void*)k_collide_round_wb<64, 1> : (const void*)k_collide_round_wb<256, 1>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, precision == 0 ? block : 32 * kWbWarps, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;

@@ -132,8 +132,8 @@ _SIGS = {
                                                 C.POINTER(DistanceRequest), C.POINTER(DistanceResult), _VP]),
     "fclgpu_kernel_launch_count": (C.c_int64, []),
     "fclgpu_last_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
-    "fclgpu_set_collide_tuning": (C.c_int, [C.c_int32, C.c_int32]),
-    "fclgpu_get_collide_tuning": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "fclgpu_set_collide_tuning": (C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
+    "fclgpu_get_collide_tuning": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "fclgpu_shapeset_create": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, C.POINTER(C.c_void_p)]),
     "fclgpu_shapeset_destroy": (C.c_int, [_VP]),
     "fclgpu_shape_batch_device": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),

@@ -189,11 +189,12 @@ FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
 FCLGPU_API int fclgpu_last_kernel_time(double* ms);
 /* Knobs of the collide rounds, chosen by the autotuner (fcl_gb300/api.py
  * autotune_collide): BV tests an item runs per round before its frontier is re-queued
- * (the request's budget overrides it when non-zero), and the DFS steps a lane runs
- * between two warp-wide batches of leaf tests (FP32 form).  Results do not depend on
- * them.  No counterpart in FCL. */
-FCLGPU_API int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps);
-FCLGPU_API int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps);
+ * (the request's budget overrides it when non-zero), the DFS steps a lane runs between
+ * two warp-wide batches of leaf tests, and the register variant of that kernel (0 =
+ * unbounded, 1 = 128 registers for a fourth resident block) (FP32 form).  Results do
+ * not depend on them.  No counterpart in FCL. */
+FCLGPU_API int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps, int32_t variant);
+FCLGPU_API int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps, int32_t* variant);
 
 /* ---- convex shapes (fcl::Box/Sphere/Capsule/Cylinder/Cone/Convex, geometry/shape/*.h) --
  * GJK/EPA of FCL's own solver (GJKSolver_indep, narrowphase/detail/gjk_solver_indep.h)
