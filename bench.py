@@ -180,6 +180,78 @@ def run_serving(args):
 
 
 # ------------------------------------------------------------------------------------
+# secondary workloads: the distance batch and the convex-pair batch
+# ------------------------------------------------------------------------------------
+def _time_device(fn, steps, warmup, stream, flush):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for i in range(steps):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return float(np.mean(ms))
+
+
+def run_secondary(args, meshes, stream, flush):
+    """Distance batch (1M poses over the same 64 mesh pairs, translations U[1.5,4]^3,
+    margins U[0.01,0.2]) in both forms, and the 4M convex-pair batch (GJK/EPA)."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    out = {}
+    dev = flush.device
+    w2 = W.config2(total_poses=int(1_000_000 * args.scale), n_pairs=args.pairs, tri_hi=args.tri_hi)
+    tf2 = torch.from_numpy(w2.tf2).to(dev)
+    pq = torch.from_numpy(w2.pair).to(dev)
+    mg = torch.from_numpy(w2.margin).to(dev)
+
+    def dist(prec, t=tf2, p=pq, m=mg):
+        return api.distance_batch(meshes, w2.pairs, None, t, pair_of_query=p, nearest_points=True, precision=prec,
+                                  margins=m, stream=stream.cuda_stream)
+
+    ms32 = _time_device(lambda: dist("fp32"), 2, 1, stream, flush)
+    sub = torch.from_numpy(np.sort(np.random.default_rng(7).choice(w2.n, size=max(1, w2.n // 10),
+                                                                     replace=False))).to(dev)
+    t_s, p_s, m_s = tf2[sub].contiguous(), pq[sub].contiguous(), mg[sub].contiguous()
+    ms64 = _time_device(lambda: dist("fp64", t_s, p_s, m_s), 1, 1, stream, flush)
+    a = dist("fp32", t_s, p_s, m_s)
+    b = dist("fp64", t_s, p_s, m_s)
+    torch.cuda.synchronize()
+    d32, d64 = a["min_distance"].cpu().numpy(), b["min_distance"].cpu().numpy()
+    rel = np.abs(d32 - d64) / np.maximum(np.abs(d64), 1e-300)
+    out["distance"] = {
+        "workload": "c2_distance_1M_poses_64pairs", "queries": w2.n,
+        "fp32_value": w2.n / (ms32 / 1000.0), "fp64_value": sub.numel() / (ms64 / 1000.0), "unit": "queries/s",
+        "fp32_ms_per_step": ms32, "fp64_ms_per_step_on_subset": ms64, "subset": int(sub.numel()),
+        "max_rel_err_vs_fp64": float(rel.max()), "p99_rel_err_vs_fp64": float(np.percentile(rel, 99)),
+        "within_margin_equal": bool(torch.equal(a["within_margin"], b["within_margin"])),
+    }
+    w3 = W.config3(n_pairs=int(4_000_000 * args.scale))
+    ss = api.ShapeSet.from_workload(w3.shapes)
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    ia, ib, t1, t2 = d(w3.ia), d(w3.ib), d(w3.tf1), d(w3.tf2)
+    ms3 = _time_device(lambda: api.shape_batch(ss, ia, ib, t1, t2, stream=stream.cuda_stream), 2, 1, stream, flush)
+    out["shapes"] = {"workload": "c3_convex_4M_pairs_gst_indep", "pairs": w3.n, "value": w3.n / (ms3 / 1000.0),
+                     "unit": "pairs/s", "ms_per_step": ms3, "form": "fp64"}
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        threads = O.hardware_threads()
+        k = 20000
+        t0 = time.perf_counter()
+        O.shape_batch(w3.shapes, w3.ia[:k], w3.ib[:k], w3.tf1[:k], w3.tf2[:k], nthreads=threads)
+        out["shapes"]["cpu_baseline"] = {"value": k / (time.perf_counter() - t0), "unit": "pairs/s",
+                                         "cores": threads, "kind": "port", "sample": f"first {k} pairs"}
+    return out
+
+
+# ------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------
 class ClockSampler:
@@ -422,6 +494,8 @@ def run_gpu(args):
                       "colliding_fraction": float((fp32["counts"] > 0).float().mean().item()),
                       "mesh_build_s": build_s},
         }
+        if world == 1 and not args.no_secondary:
+            line["secondary"] = run_secondary(args, meshes, stream, flush)
         if world == 1 and not args.no_serving:
             line["serving"] = run_serving(args)
         print(json.dumps(line))
@@ -447,6 +521,7 @@ def main():
                     help="fraction of the queries the plain FP64 form is timed on")
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
     ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
     ap.add_argument("--serve-requests", type=int, default=200, help="requests in the Poisson run")

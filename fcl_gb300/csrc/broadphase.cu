@@ -620,7 +620,8 @@ __global__ void __launch_bounds__(128) k_bp_shape_narrow(BpSceneView S, BpQueryV
     const DevShape sa = S.shapes[S.geoms[S.gid[p.y]].index];
     const DevShape sb = S.shapes[S.geoms[Q.gid[p.x]].index];
     PairOut o;
-    shape_pair_query(sa, sb, S.sverts, S.tf + 12 * (long long)p.y, Q.tf + 12 * (long long)p.x, o, mode);
+    shape_pair_query(sa, sb, S.sverts, S.tf + 12 * (long long)p.y, Q.tf + 12 * (long long)p.x, o,
+                     mode == PAIR_INTERSECT ? (PAIR_INTERSECT | PAIR_NO_CONTACT) : mode);
     if (mode == PAIR_INTERSECT) {
       hit[i] = o.hit;
     } else {

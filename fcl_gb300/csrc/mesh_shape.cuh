@@ -576,6 +576,7 @@ FCLG_HD int shape_triangle_gjk_stage(const ShapeRef& A, const M3<double>& Rs, co
   B.s.pad = 0;
   B.s.p[0] = B.s.p[1] = B.s.p[2] = 0;
   B.verts = P;
+  if (certified_disjoint(A, Rs, ts, B, Rm, tm)) return 0;
   GjkState g;
   make_minkowski(A, Rs, ts, B, Rm, tm, g.shape);
   g.V = V;

@@ -3,8 +3,8 @@
 // Per pair: fcl::collide with contact (closed form where GJKSolver_indep has one,
 // gjk_solver_indep-inl.h:242-262, else GJK + EPA, :111-166); if the pair does not
 // collide, fcl::distance (closed form where registered, :710-860, else GJK,
-// :593-645).  Box-box intersection uses GJK/EPA here (FCL has a closed form,
-// boxBoxIntersect, that is not restated).  One thread per pair, FP64, reference
+// :593-645).  Box-box intersection is the closed form boxBoxIntersect with the
+// deepest contact point (num_max_contacts = 1).  One thread per pair, FP64, reference
 // operation order; EPA state lives in thread-local memory and is only touched by
 // colliding pairs.
 #include "shape_pair.cuh"

@@ -3,6 +3,8 @@
 #pragma once
 #include <math.h>
 
+#include "box_box.cuh"
+#include "gjk32.cuh"
 #include "gjk_epa.cuh"
 
 #if !defined(FCLG_LDG)
@@ -331,14 +333,18 @@ FCLG_HD void load_tf(const double* p, M3<double>& R, D3v& t) {
 FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
                               const M3<double>& R2, const D3v& t2, SimplexVert* V, EpaState* epa, PairOut& o) {
   const D3v guess = v3(1.0, 0.0, 0.0);
+  o.estat = -1;
+  o.hit = 0;
+  if (certified_disjoint(A, R1, t1, B, R2, t2)) {  // FCL's GJK ends Valid: no intersection
+    o.gstat = GJK_VALID;
+    return;
+  }
   GjkState g;
   make_minkowski(A, R1, t1, B, R2, t2, g.shape);
   g.V = V;
   g.tolerance = kGjkTol;
   const int gs = g.evaluate(d3neg(guess), 128);
   o.gstat = gs;
-  o.estat = -1;
-  o.hit = 0;
   if (gs != GJK_INSIDE) return;
   epa->tolerance = kGjkTol;
   epa->init();
@@ -379,11 +385,15 @@ FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1
 }
 
 // One pair: shapes a, b (with the vertex pool) at tf1, tf2 (3x4 row-major).
-enum { PAIR_INTERSECT = 1, PAIR_DISTANCE = 2, PAIR_BOTH = 3 };
+enum { PAIR_INTERSECT = 1, PAIR_DISTANCE = 2, PAIR_BOTH = 3, PAIR_NO_CONTACT = 4 };
 
 // mode PAIR_INTERSECT: fcl::collide only; PAIR_DISTANCE: fcl::distance only (dist = -1
 // when the distance dispatch finds the pair intersecting); PAIR_BOTH: collide, then
-// distance when the pair does not collide.
+// distance when the pair does not collide.  PAIR_NO_CONTACT: collide without contact
+// information (CollisionRequest::enable_contact = false); it changes only the box-box
+// case in which the reference's face clipping keeps no point, which then collides
+// (box_box-inl.h:747, 775) while collide() with contacts adds no contact and reports
+// no collision.
 FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const double* verts, const double* tf1p,
                               const double* tf2p, PairOut& o, int mode = PAIR_BOTH) {
   ShapeRef A, B;
@@ -403,6 +413,15 @@ FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const doub
   const int a = A.s.type, b = B.s.type;
   bool hit = false;
   if (!(mode & PAIR_INTERSECT)) {
+  } else if (a == SHAPE_BOX && b == SHAPE_BOX) {
+    BoxBoxOut bb;
+    box_box_contact(A.s.p, R1, t1, B.s.p, R2, t2, bb);
+    hit = (mode & PAIR_NO_CONTACT) ? bb.code != 0 : bb.num_points > 0;
+    if (bb.num_points > 0) {
+      o.normal = bb.normal;
+      o.point = bb.point;
+      o.depth = bb.depth;
+    }
   } else if (a == SHAPE_SPHERE && b == SHAPE_SPHERE) {
     hit = sphere_sphere_intersect(A.s.p[0], t1, B.s.p[0], t2, o);
   } else if (a == SHAPE_SPHERE && b == SHAPE_CAPSULE) {

@@ -227,7 +227,7 @@ int64_t narrow_collide(const BpObject& o1, const BpObject& o2, int64_t max_conta
   if (g1.kind == 0 && g2.kind == 0) {
     // ShapeCollisionTraversalNode::leafTesting (shape_collision_traversal_node-inl.h:70-136)
     ShapeResult r;
-    const bool hit = shape_intersect(g1.shape, o1.tf, g2.shape, o2.tf, r);
+    const bool hit = shape_intersect(g1.shape, o1.tf, g2.shape, o2.tf, r, false);
     return (hit && max_contacts > cur) ? 1 : 0;
   }
   if (g1.kind == 1 && g2.kind == 1) {

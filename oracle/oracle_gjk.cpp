@@ -657,6 +657,327 @@ inline V3 inv_apply(const Tf& X, const V3& p) {
 // translation of X_FA.inverse() * X_FB
 inline V3 rel_translation(const Tf& XA, const Tf& XB) { return inv_apply(XA, XB.t); }
 
+// ---- box-box (box_box-inl.h) -------------------------------------------------------
+// box_box-inl.h:60-80
+void bb_line_closest(const V3& pa, const V3& ua, const V3& pb, const V3& ub, double* alpha, double* beta) {
+  const V3 p = sub(pb, pa);
+  const double uaub = dot(ua, ub);
+  const double q1 = dot(ua, p);
+  const double q2 = -dot(ub, p);
+  double d = 1 - uaub * uaub;
+  if (d <= (double)(0.0001f)) {
+    *alpha = 0;
+    *beta = 0;
+  } else {
+    d = 1 / d;
+    *alpha = (q1 + uaub * q2) * d;
+    *beta = (uaub * q1 + q2) * d;
+  }
+}
+
+// box_box-inl.h:84-164: Sutherland-Hodgman clip of the quad p[8] by |x| < h0 then
+// |y| < h1, stopping once 8 points exist
+int bb_clip(const double h[2], const double p[8], double ret[16]) {
+  std::vector<double> cur(p, p + 8), nxt;
+  int nq = 4;
+  for (int dir = 0; dir <= 1; ++dir) {
+    for (int sign = -1; sign <= 1; sign += 2) {
+      nxt.clear();
+      int nr = 0;
+      for (int i = 0; i < nq; ++i) {
+        const double* a = &cur[2 * i];
+        const double* b = &cur[2 * ((i + 1) % nq)];
+        const bool ina = sign * a[dir] < h[dir], inb = sign * b[dir] < h[dir];
+        if (ina) {
+          nxt.push_back(a[0]);
+          nxt.push_back(a[1]);
+          if (++nr == 8) {
+            std::copy(nxt.begin(), nxt.end(), ret);
+            return 8;
+          }
+        }
+        if (ina != inb) {
+          double pt[2];
+          pt[1 - dir] = a[1 - dir] + (b[1 - dir] - a[1 - dir]) / (b[dir] - a[dir]) * (sign * h[dir] - a[dir]);
+          pt[dir] = sign * h[dir];
+          nxt.push_back(pt[0]);
+          nxt.push_back(pt[1]);
+          if (++nr == 8) {
+            std::copy(nxt.begin(), nxt.end(), ret);
+            return 8;
+          }
+        }
+      }
+      cur = nxt;
+      nq = nr;
+    }
+  }
+  std::copy(cur.begin(), cur.end(), ret);
+  return nq;
+}
+
+// box_box-inl.h:168-240: keep m of the n polygon points, i0 first, then the free point
+// whose angle about the centroid is nearest A[i0] + j 2 pi / m
+void bb_cull(int n, const double p[], int m, int i0, int iret[]) {
+  double a, cx, cy, q;
+  if (n == 1) {
+    cx = p[0];
+    cy = p[1];
+  } else if (n == 2) {
+    cx = 0.5 * (p[0] + p[2]);
+    cy = 0.5 * (p[1] + p[3]);
+  } else {
+    a = cx = cy = 0;
+    for (int i = 0; i < n - 1; ++i) {
+      q = p[i * 2] * p[i * 2 + 3] - p[i * 2 + 2] * p[i * 2 + 1];
+      a += q;
+      cx += q * (p[i * 2] + p[i * 2 + 2]);
+      cy += q * (p[i * 2 + 1] + p[i * 2 + 3]);
+    }
+    q = p[n * 2 - 2] * p[1] - p[0] * p[n * 2 - 1];
+    if (std::abs(a + q) > std::numeric_limits<double>::epsilon())
+      a = 1 / (3 * (a + q));
+    else
+      a = 1e18f;
+    cx = a * (cx + q * (p[n * 2 - 2] + p[0]));
+    cy = a * (cy + q * (p[n * 2 - 1] + p[1]));
+  }
+  double A[8];
+  for (int i = 0; i < n; ++i) A[i] = std::atan2(p[i * 2 + 1] - cy, p[i * 2] - cx);
+  int avail[8];
+  for (int i = 0; i < n; ++i) avail[i] = 1;
+  avail[i0] = 0;
+  iret[0] = i0;
+  const double pi = 3.141592653589793238462643383279502884197169399;
+  for (int j = 1; j < m; ++j) {
+    a = j * (2 * pi / m) + A[i0];
+    if (a > pi) a -= 2 * pi;
+    double maxdiff = 1e9;
+    iret[j] = i0;
+    for (int i = 0; i < n; ++i) {
+      if (!avail[i]) continue;
+      double diff = std::abs(A[i] - a);
+      if (diff > pi) diff = 2 * pi - diff;
+      if (diff < maxdiff) {
+        maxdiff = diff;
+        iret[j] = i;
+      }
+    }
+    avail[iret[j]] = 0;
+  }
+}
+
+struct BbContact {
+  V3 normal, pos;
+  double depth;
+};
+
+// box_box-inl.h:244-834 (boxBox2) with maxc contacts; returns return_code
+int box_box2(const double* side1, const Tf& tf1, const double* side2, const Tf& tf2, int maxc,
+             std::vector<BbContact>& out) {
+  const M3 &R1 = tf1.R, &R2 = tf2.R;
+  const V3 &T1 = tf1.t, &T2 = tf2.t;
+  const V3 p = sub(T2, T1);
+  const V3 pp = mulTv(R1, p);
+  const V3 A = scale(mk(side1[0], side1[1], side1[2]), 0.5);
+  const V3 B = scale(mk(side2[0], side2[1], side2[2]), 0.5);
+  const M3 R = mulT(R1, R2);
+  M3 Q;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) Q(r, c) = std::abs(R(r, c));
+
+  double s = -std::numeric_limits<double>::max();
+  int invert_normal = 0, code = 0;
+  const M3* normalR = nullptr;
+  int best_col = -1;
+  V3 normalC = mk(0, 0, 0);
+  auto face = [&](double tmp, double s2, const M3* Rn, int colid, int c) {
+    if (s2 > 0) return false;
+    if (s2 > s) {
+      s = s2;
+      best_col = colid;
+      normalR = Rn;
+      invert_normal = tmp < 0;
+      code = c;
+    }
+    return true;
+  };
+  for (int i = 0; i < 3; ++i)
+    if (!face(pp[i], std::abs(pp[i]) - (dot(row(Q, i), B) + A[i]), &R1, i, 1 + i)) return 0;
+  for (int j = 0; j < 3; ++j) {
+    const double tmp = dot(col(R2, j), p);
+    if (!face(tmp, std::abs(tmp) - (dot(col(Q, j), A) + B[j]), &R2, j, 4 + j)) return 0;
+  }
+  const double eps = std::numeric_limits<double>::epsilon();
+  {
+    const double mA = std::max(std::max(A[0], A[1]), A[2]), mB = std::max(std::max(B[0], B[1]), B[2]);
+    const double sf = std::max(std::max(mA, mB), 1.0) * 10.0 * eps;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) Q(r, c) += sf;
+  }
+  // the nine edge axes in the reference's order (u1 x v1 .. u3 x v3), each as the
+  // projection tmp, the radius sum and the unnormalised axis n (box-1 frame)
+  struct Edge {
+    double tmp, rad;
+    V3 n;
+  };
+  const Edge edges[9] = {
+      {pp[2] * R(1, 0) - pp[1] * R(2, 0), A[1] * Q(2, 0) + A[2] * Q(1, 0) + B[1] * Q(0, 2) + B[2] * Q(0, 1),
+       mk(0, -R(2, 0), R(1, 0))},
+      {pp[2] * R(1, 1) - pp[1] * R(2, 1), A[1] * Q(2, 1) + A[2] * Q(1, 1) + B[0] * Q(0, 2) + B[2] * Q(0, 0),
+       mk(0, -R(2, 1), R(1, 1))},
+      {pp[2] * R(1, 2) - pp[1] * R(2, 2), A[1] * Q(2, 2) + A[2] * Q(1, 2) + B[0] * Q(0, 1) + B[1] * Q(0, 0),
+       mk(0, -R(2, 2), R(1, 2))},
+      {pp[0] * R(2, 0) - pp[2] * R(0, 0), A[0] * Q(2, 0) + A[2] * Q(0, 0) + B[1] * Q(1, 2) + B[2] * Q(1, 1),
+       mk(R(2, 0), 0, -R(0, 0))},
+      {pp[0] * R(2, 1) - pp[2] * R(0, 1), A[0] * Q(2, 1) + A[2] * Q(0, 1) + B[0] * Q(1, 2) + B[2] * Q(1, 0),
+       mk(R(2, 1), 0, -R(0, 1))},
+      {pp[0] * R(2, 2) - pp[2] * R(0, 2), A[0] * Q(2, 2) + A[2] * Q(0, 2) + B[0] * Q(1, 1) + B[1] * Q(1, 0),
+       mk(R(2, 2), 0, -R(0, 2))},
+      {pp[1] * R(0, 0) - pp[0] * R(1, 0), A[0] * Q(1, 0) + A[1] * Q(0, 0) + B[1] * Q(2, 2) + B[2] * Q(2, 1),
+       mk(-R(1, 0), R(0, 0), 0)},
+      {pp[1] * R(0, 1) - pp[0] * R(1, 1), A[0] * Q(1, 1) + A[1] * Q(0, 1) + B[0] * Q(2, 2) + B[2] * Q(2, 0),
+       mk(-R(1, 1), R(0, 1), 0)},
+      {pp[1] * R(0, 2) - pp[0] * R(1, 2), A[0] * Q(1, 2) + A[1] * Q(0, 2) + B[0] * Q(2, 1) + B[1] * Q(2, 0),
+       mk(-R(1, 2), R(0, 2), 0)},
+  };
+  // the reference evaluates each edge axis only after the previous ones passed; the
+  // table above computes all nine first, which changes no value
+  for (int e = 0; e < 9; ++e) {
+    double s2 = std::abs(edges[e].tmp) - edges[e].rad;
+    if (s2 > 0) return 0;
+    const double l = norm(edges[e].n);
+    if (l > eps) {
+      s2 /= l;
+      if (s2 * 1.05 > s) {
+        s = s2;
+        best_col = -1;
+        normalC = mk(edges[e].n[0] / l, edges[e].n[1] / l, edges[e].n[2] / l);
+        invert_normal = edges[e].tmp < 0;
+        code = 7 + e;
+      }
+    }
+  }
+  if (!code) return 0;
+  V3 normal = best_col != -1 ? col(*normalR, best_col) : mulv(R1, normalC);
+  if (invert_normal) normal = neg(normal);
+  const double depth = -s;
+
+  if (code > 6) {
+    V3 pa = T1;
+    for (int j = 0; j < 3; ++j) pa = add(pa, scale(col(R1, j), A[j] * (dot(col(R1, j), normal) > 0 ? 1 : -1)));
+    V3 pb = T2;
+    for (int j = 0; j < 3; ++j) pb = add(pb, scale(col(R2, j), B[j] * (dot(col(R2, j), normal) > 0 ? -1 : 1)));
+    double alpha, beta;
+    const V3 ua = col(R1, (code - 7) / 3), ub = col(R2, (code - 7) % 3);
+    bb_line_closest(pa, ua, pb, ub, &alpha, &beta);
+    pa = add(pa, scale(ua, alpha));
+    pb = add(pb, scale(ub, beta));
+    out.push_back({normal, scale(add(pa, pb), 0.5), depth});
+    return code;
+  }
+
+  const bool r1 = code <= 3;
+  const M3& Ra = r1 ? R1 : R2;
+  const M3& Rb = r1 ? R2 : R1;
+  const V3& pa = r1 ? T1 : T2;
+  const V3& pb = r1 ? T2 : T1;
+  const V3& Sa = r1 ? A : B;
+  const V3& Sb = r1 ? B : A;
+  const V3 normal2 = r1 ? normal : neg(normal);
+  const V3 nr = mulTv(Rb, normal2);
+  const V3 anr = mk(std::abs(nr[0]), std::abs(nr[1]), std::abs(nr[2]));
+  int lanr, a1, a2;
+  if (anr[1] > anr[0]) {
+    if (anr[1] > anr[2]) {
+      a1 = 0, lanr = 1, a2 = 2;
+    } else {
+      a1 = 0, a2 = 1, lanr = 2;
+    }
+  } else {
+    if (anr[0] > anr[2]) {
+      lanr = 0, a1 = 1, a2 = 2;
+    } else {
+      a1 = 0, a2 = 1, lanr = 2;
+    }
+  }
+  const V3 center = nr[lanr] < 0 ? add(sub(pb, pa), scale(col(Rb, lanr), Sb[lanr]))
+                                 : sub(sub(pb, pa), scale(col(Rb, lanr), Sb[lanr]));
+  const int codeN = r1 ? code - 1 : code - 4;
+  const int code1 = codeN == 0 ? 1 : 0;
+  const int code2 = codeN == 2 ? 1 : 2;
+  const double c1 = dot(col(Ra, code1), center), c2 = dot(col(Ra, code2), center);
+  double m11 = dot(col(Rb, a1), col(Ra, code1)), m12 = dot(col(Rb, a2), col(Ra, code1));
+  double m21 = dot(col(Rb, a1), col(Ra, code2)), m22 = dot(col(Rb, a2), col(Ra, code2));
+  const double k1 = m11 * Sb[a1], k2 = m21 * Sb[a1], k3 = m12 * Sb[a2], k4 = m22 * Sb[a2];
+  const double quad[8] = {c1 - k1 - k3, c2 - k2 - k4, c1 - k1 + k3, c2 - k2 + k4,
+                          c1 + k1 + k3, c2 + k2 + k4, c1 + k1 - k3, c2 + k2 - k4};
+  const double rect[2] = {Sa[code1], Sa[code2]};
+  double ret[16];
+  const int n_int = bb_clip(rect, quad, ret);
+  if (n_int < 1) return code;
+  V3 points[8];
+  double dep[8];
+  const double det1 = 1.f / (m11 * m22 - m12 * m21);
+  m11 *= det1;
+  m12 *= det1;
+  m21 *= det1;
+  m22 *= det1;
+  int cnum = 0;
+  for (int j = 0; j < n_int; ++j) {
+    const double e1 = m22 * (ret[j * 2] - c1) - m12 * (ret[j * 2 + 1] - c2);
+    const double e2 = -m21 * (ret[j * 2] - c1) + m11 * (ret[j * 2 + 1] - c2);
+    points[cnum] = add(add(center, scale(col(Rb, a1), e1)), scale(col(Rb, a2), e2));
+    dep[cnum] = Sa[codeN] - dot(normal2, points[cnum]);
+    if (dep[cnum] >= 0) {
+      ret[cnum * 2] = ret[j * 2];
+      ret[cnum * 2 + 1] = ret[j * 2 + 1];
+      cnum++;
+    }
+  }
+  if (cnum < 1) return code;
+  if (maxc > cnum) maxc = cnum;
+  if (maxc < 1) maxc = 1;
+  int iret[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+  if (cnum > maxc) {
+    int i1 = 0;
+    double maxdepth = dep[0];
+    for (int i = 1; i < cnum; ++i)
+      if (dep[i] > maxdepth) {
+        maxdepth = dep[i];
+        i1 = i;
+      }
+    bb_cull(cnum, ret, maxc, i1, iret);
+    cnum = maxc;
+  }
+  for (int j = 0; j < cnum; ++j) {
+    const int i = iret[j];
+    const V3 half = scale(normal, dep[i] / 2);
+    out.push_back({normal, r1 ? add(add(points[i], pa), half) : sub(add(points[i], pa), half), dep[i]});
+  }
+  return code;
+}
+
+// boxBoxIntersect (box_box-inl.h:858-876) as collide() sees it: with contacts, the
+// traversal node keeps num_max_contacts = 1 of them, the deepest, by a size-1
+// std::partial_sort (shape_collision_traversal_node-inl.h:78-100), which keeps the
+// first maximum in order; the pair counts as colliding only if a contact was added.
+// Without contacts the answer is return_code != 0.
+bool box_box_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, bool enable_contact,
+                       ShapeResult& r) {
+  std::vector<BbContact> cs;
+  const int rc = box_box2(s1.p, tf1, s2.p, tf2, 4, cs);
+  if (!enable_contact) return rc != 0;
+  if (cs.empty()) return false;
+  size_t best = 0;
+  for (size_t i = 1; i < cs.size(); ++i)
+    if (cs[best].depth < cs[i].depth) best = i;
+  r.normal = cs[best].normal;
+  r.point = cs[best].pos;
+  r.depth = cs[best].depth;
+  return true;
+}
+
 // sphere_sphere-inl.h:67-87
 bool sphere_sphere_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
   V3 diff = sub(tf2.t, tf1.t);
@@ -1041,13 +1362,14 @@ bool gjk_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2
 }
 
 // Dispatch of GJKSolver_indep (gjk_solver_indep-inl.h:242-262 intersect, 710-860
-// distance) restricted to Box/Sphere/Capsule/Cylinder/Cone/Convex.  Box-box
-// intersection has a closed form in FCL (boxBoxIntersect); it is not restated here
-// and box pairs go through GJK/EPA (documented gap).
-bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r) {
+// distance) restricted to Box/Sphere/Capsule/Cylinder/Cone/Convex.
+bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r,
+                     bool enable_contact) {
   const int a = s1.type, b = s2.type;
   bool hit;
-  if (a == SH_SPHERE && b == SH_SPHERE) {
+  if (a == SH_BOX && b == SH_BOX) {
+    hit = box_box_intersect(s1, tf1, s2, tf2, enable_contact, r);
+  } else if (a == SH_SPHERE && b == SH_SPHERE) {
     hit = sphere_sphere_intersect(s1, tf1, s2, tf2, r);
   } else if (a == SH_SPHERE && b == SH_CAPSULE) {
     hit = sphere_capsule_intersect(s1, tf1, s2, tf2, r);

@@ -33,7 +33,12 @@ void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, 
 // The two halves of shape_pair: the intersect dispatch (gjk_solver_indep-inl.h:182-200;
 // fills normal/point/depth/statuses when it returns true) and the distance dispatch
 // (gjk_solver_indep-inl.h:686-708; distance -1 when the pair intersects).
-bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
+// enable_contact = false is collide() without contact information: it only changes
+// the box-box answer in the case the reference's clipping keeps no point
+// (box_box-inl.h:747, 775), which collides without contacts and so collide() with
+// contacts reports no contact.
+bool shape_intersect(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r,
+                     bool enable_contact = true);
 void shape_distance(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, ShapeResult& r);
 
 // Pure GJK/EPA without closed-form dispatch (used to check the device solver).

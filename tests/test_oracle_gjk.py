@@ -95,3 +95,70 @@ def test_gjk_tolerance_constant():
     # the oracle and the device code use this literal
     import math
     assert math.pow(np.finfo(np.float64).eps, 7.0 / 8.0) == 2.0097183471152322e-14
+
+
+def _angle_axis(angle, axis):
+    # Eigen::AngleAxis::toRotationMatrix
+    a = np.asarray(axis, float)
+    s = np.sin(angle) * a
+    c = np.cos(angle)
+    c1 = (1 - c) * a
+    R = np.empty((3, 3))
+    t = c1[0] * a[1]; R[0, 1] = t - s[2]; R[1, 0] = t + s[2]
+    t = c1[0] * a[2]; R[0, 2] = t + s[1]; R[2, 0] = t - s[1]
+    t = c1[1] * a[2]; R[1, 2] = t - s[0]; R[2, 1] = t + s[0]
+    for i in range(3):
+        R[i, i] = c1[i] * a[i] + c
+    return R
+
+
+_ISO = [np.eye(3), _angle_axis(np.pi, (1, 0, 0)),
+        _angle_axis(np.pi / 2, (1, 0, 0)), _angle_axis(3 * np.pi / 2, (1, 0, 0)),
+        _angle_axis(np.pi / 2, (0, 1, 0)), _angle_axis(3 * np.pi / 2, (0, 1, 0))]
+
+
+def _box_box_cases(size1, R1, size2, t2, R2):
+    """The twelve collide calls of test_fcl_box_box.cpp:126-150: box 2 (a cube) in its
+    six face-up orientations, in (1, 2) and (2, 1) order."""
+    for P in _ISO:
+        X1 = _tf(R=R1)
+        X2 = _tf(t2, R2 @ P)
+        yield 1.0, _one(W.BOX, [size1] * 3, X1, X2, t2=W.BOX, params2=[size2] * 3)
+        yield -1.0, _one(W.BOX, [size2] * 3, X2, X1, t2=W.BOX, params2=[size1] * 3)
+
+
+def _is_approx(a, b, tol):
+    return np.linalg.norm(a - b) <= tol * min(np.linalg.norm(a), np.linalg.norm(b))
+
+
+def test_box_box_all_contacts_known_answer():
+    # test_fcl_box_box.cpp:227-263 (GST_INDEP, tolerance 1e-12): unit cube turned 45
+    # degrees about y resting in a size-3 cube below it
+    tol = 1e-12
+    for sgn, r in _box_box_cases(1.0, _angle_axis(np.pi / 4, (0, 1, 0)), 3.0, (0, 0, -1.5), np.eye(3)):
+        assert r["hit"][0]
+        assert abs(r["depth"][0] - np.sqrt(2) / 2) <= tol
+        assert _is_approx(r["normal"][0], sgn * np.array([0, 0, -1.0]), tol)
+        pos = r["point"][0]
+        assert abs(pos[2] + np.sqrt(2) / 4) <= tol and abs(pos[0]) <= tol
+        assert -0.5 <= pos[1] <= 0.5
+
+
+def test_box_box_cull_contacts_known_answer():
+    # test_fcl_box_box.cpp:277-318 (GST_INDEP, tolerance 1e-14): two unit cubes, one
+    # tilted pi/8 about x, the other turned pi/4 about z at z = -0.75; eight clipped
+    # points are culled to four and the deepest is reported
+    tol = 1e-14
+    tilt = np.pi / 8
+    depth = np.sqrt(2) / 2 * np.cos(np.pi / 4 - tilt) - 0.25
+    ez = -0.25 - depth / 2
+    ey = -np.sqrt(2) / 2 * np.sin(np.pi / 4 - tilt)
+    ex = np.sqrt(2) / 2 + ey + np.finfo(float).eps
+    for sgn, r in _box_box_cases(1.0, _angle_axis(tilt, (1, 0, 0)), 1.0, (0, 0, -0.75),
+                                 _angle_axis(np.pi / 4, (0, 0, 1))):
+        assert r["hit"][0]
+        assert abs(r["depth"][0] - depth) <= tol
+        assert _is_approx(r["normal"][0], sgn * np.array([0, 0, -1.0]), tol)
+        pos = r["point"][0]
+        assert abs(pos[2] - ez) <= tol and abs(pos[1] - ey) <= tol
+        assert -ex <= pos[0] <= ex
