@@ -76,7 +76,8 @@ __device__ __forceinline__ void pair_geom(const MeshShapeLaunch& L, long long i,
   load_tf(L.tfs + 12 * i, g.Rs, g.ts);
 }
 
-// leaves of each pair: count pass (offsets == null) or write pass
+// distance: leaves of each pair that may hold the minimum, count pass (offsets == null)
+// or write pass
 template <int STACK>
 __global__ void __launch_bounds__(128) k_ms_collect(MeshShapeLaunch L, int32_t* counts, const int64_t* offsets,
                                                     int32_t* leaf_pair, int32_t* leaf_prim, double* leaf_lb,
@@ -97,14 +98,9 @@ __global__ void __launch_bounds__(128) k_ms_collect(MeshShapeLaunch L, int32_t* 
       }
       ++cnt;
     };
-    int st;
-    if (L.mode == 0) {
-      st = mesh_shape_collect_collide<STACK>(g.m, g.Rm, g.tm, bv, emit);
-    } else {
-      double u = DBL_MAX;
-      st = mesh_shape_collect_distance<STACK>(g.m, g.Rm, g.tm, g.A, g.Rs, g.ts, bv, &u, emit);
-      if (ub) ub[i] = u;
-    }
+    double u = DBL_MAX;
+    const int st = mesh_shape_collect_distance<STACK>(g.m, g.Rm, g.tm, g.A, g.Rs, g.ts, bv, &u, emit);
+    if (ub) ub[i] = u;
     if (st) atomicOr(L.status, 1u);
     if (counts) counts[i] = cnt;
   }
@@ -112,11 +108,11 @@ __global__ void __launch_bounds__(128) k_ms_collect(MeshShapeLaunch L, int32_t* 
 
 __global__ void __launch_bounds__(128) k_ms_leaf_tests(MeshShapeLaunch L, long long nl, const int32_t* leaf_pair,
                                                        const int32_t* leaf_prim, const double* leaf_lb,
-                                                       const double* ub, int32_t* hit, double* dist, double* pts) {
+                                                       const double* ub, double* dist, double* pts) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
     const long long i = leaf_pair[j];
-    if (L.mode == 1 && leaf_lb[j] > ub[i]) {  // cannot hold the minimum
+    if (leaf_lb[j] > ub[i]) {  // cannot hold the minimum
       dist[j] = DBL_MAX;
       continue;
     }
@@ -125,111 +121,121 @@ __global__ void __launch_bounds__(128) k_ms_leaf_tests(MeshShapeLaunch L, long l
     double P[9];
     load_tri_local(g.m, leaf_prim[j], P);
     SimplexVert V[kSimplexSlots];
-    if (L.mode == 0) {
-      EpaState epa;
-      hit[j] = shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa) ? 1 : 0;
-    } else {
-      double d;
-      D3v ps, pt;
-      shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
-      dist[j] = d;
-      double* p = pts + 6 * j;
-      p[0] = pt.x;
-      p[1] = pt.y;
-      p[2] = pt.z;
-      p[3] = ps.x;
-      p[4] = ps.y;
-      p[5] = ps.z;
-    }
+    double d;
+    D3v ps, pt;
+    shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+    dist[j] = d;
+    double* p = pts + 6 * j;
+    p[0] = pt.x;
+    p[1] = pt.y;
+    p[2] = pt.z;
+    p[3] = ps.x;
+    p[4] = ps.y;
+    p[5] = ps.z;
   }
 }
 
-// per pair: contacts = min(max_contacts, intersecting leaves); distance = the first
-// minimum in collection order (the seed triangle first, as FCL's strict update)
-__global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t* leaf_prim, const int32_t* hit,
-                            const double* dist, const double* pts) {
+// per pair: distance = the first minimum in collection order (the seed triangle first,
+// as FCL's strict update)
+__global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t* leaf_prim, const double* dist,
+                            const double* pts) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += stride) {
-    if (L.mode == 0) {
-      long long c = 0;
-      for (long long j = off[i]; j < off[i + 1]; ++j) c += hit[j];
-      L.counts[i] = (int32_t)(c < L.max_contacts ? c : L.max_contacts);
-    } else {
-      double best = DBL_MAX;
-      long long bj = -1;
-      for (long long j = off[i]; j < off[i + 1]; ++j)
-        if (best > dist[j]) {
-          best = dist[j];
-          bj = j;
-        }
-      L.dist[i] = best;
-      if (L.tri) L.tri[i] = bj >= 0 ? leaf_prim[bj] : -1;
-      if (L.pts)
-        for (int k = 0; k < 6; ++k) L.pts[6 * i + k] = bj >= 0 ? pts[6 * bj + k] : 0.0;
-    }
+    double best = DBL_MAX;
+    long long bj = -1;
+    for (long long j = off[i]; j < off[i + 1]; ++j)
+      if (best > dist[j]) {
+        best = dist[j];
+        bj = j;
+      }
+    L.dist[i] = best;
+    if (L.tri) L.tri[i] = bj >= 0 ? leaf_prim[bj] : -1;
+    if (L.pts)
+      for (int k = 0; k < 6; ++k) L.pts[6 * i + k] = bj >= 0 ? pts[6 * bj + k] : 0.0;
   }
 }
 
-// Collide in rounds: each unfinished pair tests its next kChunk leaves (in DFS order),
-// then stops once it has max_contacts contacts -- the serial DFS's early stop, kept
-// to a chunk's granularity so that colliding pairs do not test (and run EPA on) every
-// overlapping triangle.
-constexpr int kChunk = 16;
+// Collide in rounds.  Each unfinished pair resumes its DFS (stack kept in global
+// memory) until it has K_r more overlapping leaves; the leaves are then tested one per
+// thread (shape_triangle_gjk_stage: the FP32-certified GJK, no EPA), and a pair stops
+// once it has max_contacts intersecting leaves or its DFS is done -- FCL's early stop,
+// at the granularity of a round.  K_r = 16 * 2^r (at most 1024): colliding pairs usually
+// stop in the first round, long contact-free traversals need few rounds.
+struct MsPairState {
+  ShapeBV bv;
+  ShapeBV32 b32;
+};
 
-__global__ void __launch_bounds__(128) k_ms_chunk_tests(MeshShapeLaunch L, const int32_t* act, long long nact,
-                                                        const int64_t* cur, const int64_t* off,
-                                                        const int32_t* leaf_prim, int32_t* hit) {
+__global__ void __launch_bounds__(128) k_msr_init(MeshShapeLaunch L, MsPairState* ps, int32_t* stack, int cap,
+                                                  int32_t* sp, int32_t* act) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nact * kChunk; t += stride) {
-    const long long i = act[t / kChunk];
-    const long long j = cur[i] + t % kChunk;
-    if (j >= off[i + 1]) continue;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += stride) {
     PairGeom g;
     pair_geom(L, i, g);
-    double P[9];
-    load_tri_local(g.m, leaf_prim[j], P);
-    SimplexVert V[kSimplexSlots];
-    hit[j] = shape_triangle_gjk_stage(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V);
+    MsPairState st;
+    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, st.bv);
+    make_shape_bv32(g.Rm, g.tm, st.bv, g.m, st.b32);
+    ps[i] = st;
+    stack[i * (long long)cap] = 0;
+    sp[i] = 1;
+    L.counts[i] = 0;
+    act[i] = (int32_t)i;
   }
 }
 
-// Walks the chunk in DFS order; a leaf GJK found inside is confirmed by EPA (as
-// shapeTriangleIntersect does) only while the pair still needs contacts.
-__global__ void __launch_bounds__(128) k_ms_chunk_update(MeshShapeLaunch L, const int32_t* act, long long nact,
-                                                         int64_t* cur, const int64_t* off, const int32_t* leaf_prim,
-                                                         const int32_t* hit, int32_t* next,
-                                                         unsigned long long* nnext) {
+__global__ void __launch_bounds__(128) k_msr_dfs(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
+                                                 const MsPairState* ps, int32_t* stack, int cap, int32_t* sp,
+                                                 int32_t* leaf, int32_t* nleaf) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
     const long long i = act[a];
-    const long long end = off[i + 1];
-    const long long j1 = cur[i] + kChunk < end ? cur[i] + kChunk : end;
-    int c = L.counts[i];
-    for (long long j = cur[i]; j < j1 && c < L.max_contacts; ++j) {
-      if (hit[j] == 2) {
-        ++c;
-      } else if (hit[j] == 1) {
-        PairGeom g;
-        pair_geom(L, i, g);
-        double P[9];
-        load_tri_local(g.m, leaf_prim[j], P);
-        SimplexVert V[kSimplexSlots];
-        EpaState epa;
-        if (shape_triangle_intersect(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa)) ++c;
-      }
+    const DevMesh m = L.meshes[L.mesh_idx[i]];
+    M3<double> Rm;
+    D3v tm;
+    load_tf(L.tfm + 12 * i, Rm, tm);
+    const ShapeBV bv = ps[i].bv;
+    const ShapeBV32 b32 = ps[i].b32;
+    int s = sp[i];
+    int32_t* out = leaf + a * (long long)K;
+    const int ne = mesh_shape_dfs_resume(m, Rm, tm, bv, b32, stack + i * (long long)cap, s, cap, K,
+                                         [&](int k, int prim) { out[k] = prim; });
+    if (ne < 0) {
+      atomicOr(L.status, 1u);
+      sp[i] = 0;
+      nleaf[a] = 0;
+    } else {
+      sp[i] = s;
+      nleaf[a] = ne;
     }
-    L.counts[i] = c;
-    cur[i] = j1;
-    if (c < L.max_contacts && j1 < end) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
   }
 }
 
-__global__ void k_ms_iota(int32_t* a, long long n, int64_t* cur, const int64_t* off, int32_t* counts) {
+__global__ void __launch_bounds__(128) k_msr_tests(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
+                                                   const int32_t* leaf, const int32_t* nleaf, int32_t* hit) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    a[i] = (int32_t)i;
-    cur[i] = off[i];
-    counts[i] = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nact * K; t += stride) {
+    const long long a = t / K;
+    if (t % K >= nleaf[a]) continue;
+    PairGeom g;
+    pair_geom(L, act[a], g);
+    double P[9];
+    load_tri_local(g.m, leaf[t], P);
+    SimplexVert V[kSimplexSlots];
+    hit[t] = shape_triangle_gjk_stage(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_msr_update(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
+                                                    const int32_t* nleaf, const int32_t* hit, const int32_t* sp,
+                                                    int32_t* next, unsigned long long* nnext) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
+    const long long i = act[a];
+    int c = L.counts[i];
+    const int nl = nleaf[a];
+    for (int k = 0; k < nl && c < L.max_contacts; ++k) c += hit[a * (long long)K + k];
+    L.counts[i] = c;
+    if (c < L.max_contacts && sp[i] > 0) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
   }
 }
 
@@ -258,10 +264,47 @@ SplitScratch g_split_ms;
 std::mutex g_split_mu;
 }  // namespace
 
-cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
-  if (L.n <= 0) return cudaSuccess;
-  std::lock_guard<std::mutex> lk(g_split_mu);
-  SplitScratch& S = g_split_ms;
+namespace {
+
+cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s, SplitScratch& S) {
+  const long long n = L.n;
+  const int cap = stack_entries;
+  cudaError_t e;
+  if ((e = S.ensure(0, sizeof(MsPairState) * n)) || (e = S.ensure(1, 4ull * cap * n)) || (e = S.ensure(2, 4 * n)) ||
+      (e = S.ensure(3, 4 * n)) || (e = S.ensure(4, 4 * n)) || (e = S.ensure(5, 8)))
+    return e;
+  MsPairState* ps = (MsPairState*)S.p[0];
+  int32_t* stack = (int32_t*)S.p[1];
+  int32_t* sp = (int32_t*)S.p[2];
+  int32_t* act = (int32_t*)S.p[3];
+  int32_t* next = (int32_t*)S.p[4];
+  unsigned long long* nnext = (unsigned long long*)S.p[5];
+  k_msr_init<<<grid128(n), 128, 0, s>>>(L, ps, stack, cap, sp, act);
+  ++g_kernel_launches;
+  long long nact = n;
+  for (int r = 0; nact > 0; ++r) {
+    const int K = 16 << std::min(r, 6);
+    const long long nl = nact * K;
+    if ((e = S.ensure(6, 4 * nl)) || (e = S.ensure(7, 4 * nact)) || (e = S.ensure(8, 4 * nl))) return e;
+    int32_t* leaf = (int32_t*)S.p[6];
+    int32_t* nleaf = (int32_t*)S.p[7];
+    int32_t* hit = (int32_t*)S.p[8];
+    if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
+    k_msr_dfs<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, ps, stack, cap, sp, leaf, nleaf);
+    k_msr_tests<<<grid128(nl), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit);
+    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, nleaf, hit, sp, next, nnext);
+    g_kernel_launches += 3;
+    unsigned long long nn = 0;
+    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return e;
+    nact = (long long)nn;
+    std::swap(act, next);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t run_distance_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s, SplitScratch& S) {
   const long long n = L.n;
   cudaError_t e;
   if ((e = S.ensure(0, 4 * n)) || (e = S.ensure(1, 8 * (n + 1))) || (e = S.ensure(2, 8 * ((n + 4095) / 4096 + 2))) ||
@@ -282,52 +325,34 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
   if ((e = cudaMemcpyAsync(&nl, off + n, 8, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) return e;
   if (nl > 0) {
     if ((e = S.ensure(4, 4 * nl)) || (e = S.ensure(5, 4 * nl)) || (e = S.ensure(6, 8 * nl)) ||
-        (e = S.ensure(7, (L.mode == 0 ? 4 : 56) * nl)))
+        (e = S.ensure(7, 56 * nl)))
       return e;
     int32_t* leaf_pair = (int32_t*)S.p[4];
     int32_t* leaf_prim = (int32_t*)S.p[5];
     double* leaf_lb = (double*)S.p[6];
-    int32_t* hit = (int32_t*)S.p[7];
     double* dist = (double*)S.p[7];
     double* pts = dist + nl;
     if (big)
       k_ms_collect<256><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
     else
       k_ms_collect<64><<<grid128(n), 128, 0, s>>>(L, nullptr, off, leaf_pair, leaf_prim, leaf_lb, nullptr);
-    ++g_kernel_launches;
-    if (L.mode == 0) {
-      if ((e = S.ensure(8, 4 * n)) || (e = S.ensure(9, 4 * n)) || (e = S.ensure(10, 8))) return e;
-      int32_t* act = (int32_t*)S.p[8];
-      int32_t* next = (int32_t*)S.p[9];
-      unsigned long long* nnext = (unsigned long long*)S.p[10];
-      int64_t* cur = (int64_t*)S.p[3];
-      k_ms_iota<<<grid128(n), 128, 0, s>>>(act, n, cur, off, L.counts);
-      ++g_kernel_launches;
-      long long nact = n;
-      while (nact > 0) {
-        if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
-        k_ms_chunk_tests<<<grid128(nact * kChunk), 128, 0, s>>>(L, act, nact, cur, off, leaf_prim, hit);
-        k_ms_chunk_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, cur, off, leaf_prim, hit, next, nnext);
-        g_kernel_launches += 2;
-        unsigned long long nn = 0;
-        if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||
-            (e = cudaStreamSynchronize(s)))
-          return e;
-        nact = (long long)nn;
-        int32_t* t = act;
-        act = next;
-        next = t;
-      }
-    } else {
-      k_ms_leaf_tests<<<grid128(nl), 128, 0, s>>>(L, nl, leaf_pair, leaf_prim, leaf_lb, ub, hit, dist, pts);
-      k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, leaf_prim, hit, dist, pts);
-      g_kernel_launches += 2;
-    }
+    k_ms_leaf_tests<<<grid128(nl), 128, 0, s>>>(L, nl, leaf_pair, leaf_prim, leaf_lb, ub, dist, pts);
+    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, leaf_prim, dist, pts);
+    g_kernel_launches += 3;
   } else {
-    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, nullptr, nullptr, nullptr, nullptr);
+    k_ms_reduce<<<grid128(n), 128, 0, s>>>(L, off, nullptr, nullptr, nullptr);
     ++g_kernel_launches;
   }
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
+  if (L.n <= 0) return cudaSuccess;
+  std::lock_guard<std::mutex> lk(g_split_mu);
+  return L.mode == 0 ? run_collide_rounds(L, stack_entries, s, g_split_ms)
+                     : run_distance_split(L, stack_entries, s, g_split_ms);
 }
 
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {

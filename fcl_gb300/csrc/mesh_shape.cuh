@@ -18,6 +18,7 @@
 #pragma once
 #include <cfloat>
 
+#include "filter32.cuh"
 #include "geom.cuh"
 #include "shape_pair.cuh"
 
@@ -560,13 +561,16 @@ FCLG_HD bool shape_triangle_intersect(const ShapeRef& A, const M3<double>& Rs, c
   return o.hit != 0;
 }
 
-// First stage of shapeTriangleIntersect: 0 = no intersection, 1 = GJK reports the
-// origin inside (EPA still decides), 2 = intersection (sphere closed form).
+// shapeTriangleIntersect without contact information (gjk_solver_indep-inl.h:
+// shapeTriangleIntersect): the sphere closed form, else GJK on the shape and TriangleP;
+// GJK Inside is an intersection, because the EPA that follows only fills the contact:
+// EPA::evaluate never returns Failed (epa-inl.h sets Failed only in initialize, :118,
+// and evaluate ends Valid/.../FallBack).  Returns 1 (intersecting) or 0.
 FCLG_HD int shape_triangle_gjk_stage(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
                                      const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
   if (A.s.type == SHAPE_SPHERE) {
     const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
-    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 2
+    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 1
                                                                                                           : 0;
   }
   ShapeRef B;
@@ -665,25 +669,68 @@ FCLG_HD double shape_point_ub(const ShapeRef& A, const M3<double>& Rs, const D3v
   return d3norm(p - c);
 }
 
-template <int STACK, class Emit>
-FCLG_HD int mesh_shape_collect_collide(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeBV& bv,
-                                       Emit emit) {
-  int stack[STACK];
-  int sp = 0;
-  stack[sp++] = 0;
-  while (sp > 0) {
+FCLG_HD int float_bits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_int(x);
+#else
+  int i;
+  memcpy(&i, &x, 4);
+  return i;
+#endif
+}
+
+// The shape's BV as an FP32 node (axis column k with To[k], then the extents) for the
+// filtered OBB test of filter32.cuh, with its per-pair error-bound state.
+struct ShapeBV32 {
+  QueryF32 q;
+  float4 a0, a1, a2, ea;
+};
+FCLG_HD void make_shape_bv32(const M3<double>& Rm, const D3v& tm, const ShapeBV& bv, const DevMesh& m,
+                             ShapeBV32& o) {
+  const double* ax = bv.obb.axis;
+  const double* to = bv.obb.To;
+  make_query_f32(Rm, tm, sqrt((to[0] * to[0] + to[1] * to[1]) + to[2] * to[2]), m.cmax, 0.0, 0.0, o.q);
+  o.a0 = make_float4((float)ax[0], (float)ax[3], (float)ax[6], (float)to[0]);
+  o.a1 = make_float4((float)ax[1], (float)ax[4], (float)ax[7], (float)to[1]);
+  o.a2 = make_float4((float)ax[2], (float)ax[5], (float)ax[8], (float)to[2]);
+  o.ea = make_float4((float)bv.obb.ext[0], (float)bv.obb.ext[1], (float)bv.obb.ext[2], 0.f);
+}
+
+// BV test of MeshShapeCollisionTraversalNodeOBBRSS (mesh_shape_collision_traversal_node-inl.h):
+// overlap(tf_mesh, shape BV, node) -- FP32 with a rigorous error bound, the FP64 test
+// (same decision as FCL's) only where the bound cannot settle it.  Returns the node's
+// first_child in *child when it overlaps.
+FCLG_HD bool shape_node_overlap(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeBV& bv,
+                                const ShapeBV32& b32, int b, int* child) {
+  const float4* pn = reinterpret_cast<const float4*>(m.nodes32) + 4 * (long long)b;
+  const float4 x0 = FCLG_LDG(pn), x1 = FCLG_LDG(pn + 1), x2 = FCLG_LDG(pn + 2), eb = FCLG_LDG(pn + 3);
+  int r = obb_overlap_f32(b32.q, b32.a0, b32.a1, b32.a2, b32.ea, x0, x1, x2, eb);
+  if (r == F_UNSURE) r = obb_overlap64(Rm, tm, bv.obb, m.nodes64[b]) ? F_TRUE : F_FALSE;
+  *child = float_bits(eb.w);
+  return r == F_TRUE;
+}
+
+// Resumable collide DFS of one pair over an explicit stack (stack[0..sp), capacity cap):
+// visits nodes in FCL's order and emits overlapping leaves until max_emit leaves have
+// been emitted or the stack is empty.  Returns the number emitted, or -1 when the stack
+// would overflow.
+template <class Emit>
+FCLG_HD int mesh_shape_dfs_resume(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeBV& bv,
+                                  const ShapeBV32& b32, int* stack, int& sp, int cap, int max_emit, Emit emit) {
+  int ne = 0;
+  while (sp > 0 && ne < max_emit) {
     const int b = stack[--sp];
-    const NodeD nd = m.nodes64[b];
-    if (!obb_overlap64(Rm, tm, bv.obb, nd)) continue;
-    if (nd.child < 0) {
-      emit(-(nd.child + 1), 0.0);
+    int child;
+    if (!shape_node_overlap(m, Rm, tm, bv, b32, b, &child)) continue;
+    if (child < 0) {
+      emit(ne++, -(child + 1));
       continue;
     }
-    if (sp + 2 > STACK) return 1;
-    stack[sp++] = nd.child + 1;
-    stack[sp++] = nd.child;
+    if (sp + 2 > cap) return -1;
+    stack[sp++] = child + 1;
+    stack[sp++] = child;
   }
-  return 0;
+  return ne;
 }
 
 template <int STACK, class Emit>

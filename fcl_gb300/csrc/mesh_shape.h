@@ -30,8 +30,10 @@ struct MeshShapeLaunch {
 
 // One thread per pair runs the whole FCL traversal (exact statistics).
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s);
-// Split form: BVH traversal per pair, then one thread per leaf test, then a per-pair
-// reduction; same results, no statistics (nbv / nleaf ignored).  Synchronises s once.
+// Split form, same results, no statistics (nbv / nleaf ignored).  Collide: rounds of a
+// resumable per-pair DFS and one thread per leaf test, with the early stop at
+// max_contacts (synchronises s once per round).  Distance: BVH traversal per pair, one
+// thread per leaf test, per-pair reduction (synchronises s once).
 cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s);
 
 }  // namespace fclgpu

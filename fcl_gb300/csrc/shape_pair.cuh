@@ -330,6 +330,10 @@ FCLG_HD void load_tf(const double* p, M3<double>& R, D3v& t) {
   t = v3(FCLG_LDG(p + 3), FCLG_LDG(p + 7), FCLG_LDG(p + 11));
 }
 
+// GJKSolver_indep::shapeIntersect through GJK (+ EPA for the contact).  epa == nullptr
+// asks for the answer only: GJK Inside decides it, since EPA::evaluate never returns
+// Failed (epa-inl.h sets Failed only in initialize, :118), so FCL's EPA never turns
+// an Inside into "no intersection".
 FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
                               const M3<double>& R2, const D3v& t2, SimplexVert* V, EpaState* epa, PairOut& o) {
   const D3v guess = v3(1.0, 0.0, 0.0);
@@ -346,6 +350,10 @@ FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t
   const int gs = g.evaluate(d3neg(guess), 128);
   o.gstat = gs;
   if (gs != GJK_INSIDE) return;
+  if (!epa) {
+    o.hit = 1;
+    return;
+  }
   epa->tolerance = kGjkTol;
   epa->init();
   const int es = epa->evaluate(g, d3neg(guess), 255);
@@ -439,6 +447,9 @@ FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const doub
   } else if (a == SHAPE_CYLINDER && b == SHAPE_SPHERE) {
     hit = sphere_cylinder_intersect(B.s.p[0], t2, A.s.p[0], A.s.p[1], R1, t1, o);
     if (hit) o.normal = d3neg(o.normal);
+  } else if (mode & PAIR_NO_CONTACT) {
+    gjk_intersect(A, R1, t1, B, R2, t2, V, nullptr, o);
+    hit = o.hit != 0;
   } else {
     EpaState epa;
     gjk_intersect(A, R1, t1, B, R2, t2, V, &epa, o);
