@@ -44,6 +44,28 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+def _max_over_ranks(x: float, device, world: int) -> float:
+    """The slowest rank's time (the job's time): all-reduce MAX over the process group."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(x: float, device, world: int) -> float:
+    """Units processed by all ranks: all-reduce SUM over the process group."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def _workload(args, rank):
     from fcl_gb300 import workloads as W
     return W.config1(scale=args.scale, seed=1 + 1000 * rank, n_pairs=args.pairs, tri_hi=args.tri_hi)
@@ -145,13 +167,13 @@ def run_serving(args):
     mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
     mgr.registerObjects(w.refs, w.tf)
     setup_s = time.perf_counter() - t0
-    reqs = W.motion_requests(w, args.serve_requests + 80, seed=5)
+    reqs = W.motion_requests(w, args.serve_requests + 272, seed=5)
     srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=args.serve_step)
     SV.run_burst(srv, reqs[:16])  # warm-up
-    burst = SV.run_burst(srv, reqs[16:80])
+    burst = SV.run_burst(srv, reqs[16:272])
     rate = args.serve_rate if args.serve_rate > 0 else 0.7 * burst["requests_per_s"]
     with ClockSampler(0) as cs:
-        load = SV.run_poisson(srv, reqs[80:], rate, seed=6)
+        load = SV.run_poisson(srv, reqs[272:], rate, seed=6)
     st = srv.stats()
     srv.close()
     out = {
@@ -162,7 +184,7 @@ def run_serving(args):
         "arrival_rate_per_s": rate, "requests": load["requests"],
         "throughput_requests_per_s": load["throughput_requests_per_s"],
         "p50_ms": load["p50_ms"], "p99_ms": load["p99_ms"], "mean_ms": load["mean_ms"], "max_ms": load["max_ms"],
-        "waypoints": int(sum(r.q.shape[0] for r in reqs[80:])),
+        "waypoints": int(sum(r.q.shape[0] for r in reqs[272:])),
         "engine": {k: st[k] for k in ("steps", "waypoints", "queries", "candidates", "busy_ms",
                                       "max_step_waypoints")},
         "scene_setup_s": setup_s, "clocks": cs.summary(),
@@ -171,7 +193,7 @@ def run_serving(args):
         from oracle import pyoracle as O
         O.build()
         threads = O.hardware_threads()
-        sample = reqs[80:80 + args.serve_cpu_sample]
+        sample = reqs[272:272 + args.serve_cpu_sample]
         out["cpu_baseline"] = {"value": _serving_expected_cpu(w, sample, threads), "unit": "requests/s",
                                "cores": threads, "kind": "port",
                                "sample": f"{len(sample)} of the requests, dynamic AABB tree manager "
@@ -377,12 +399,9 @@ def run_gpu(args):
     with ClockSampler(local) as clk:
         total_ms, kms, launches = timed("fp32", args.steps, args.warmup)
     clocks = clk.summary()
-    t_step = total_ms / args.steps
-    if world > 1:
-        t = torch.tensor([t_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = world * n / (t_step / 1000.0)
+    t_step = _max_over_ranks(total_ms / args.steps, dev, world)
+    n_all = _sum_over_ranks(float(n), dev, world)  # ranks hold their own seeded workloads
+    value = n_all / (t_step / 1000.0)
 
     # plain FP64 GPU form (the drop-in denominator), timed on a uniform subset of the
     # queries because it is ~20x slower
@@ -408,7 +427,8 @@ def run_gpu(args):
         native.check(L.fclgpu_last_kernel_time(C.byref(km)), "fclgpu_last_kernel_time")
         kms64 = [km.value]
         t64 = ev0.elapsed_time(ev1)
-        value64 = world * sub.size / (t64 / 1000.0)
+        t64 = _max_over_ranks(t64, dev, world)
+        value64 = _sum_over_ranks(float(sub.size), dev, world) / (t64 / 1000.0)
 
     # end to end through the host C ABI: pinned host inputs, H2D + kernels + D2H per step
     tf2_h = torch.from_numpy(w.tf2).pin_memory()
@@ -440,7 +460,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
     e2e_hits = bool(np.array_equal(counts_h.numpy(), fp32["counts"].cpu().numpy())) if e2e_ms else None
-    t_e2e = float(np.mean(e2e_ms)) if e2e_ms else float("nan")
+    t_e2e = _max_over_ranks(float(np.mean(e2e_ms)) if e2e_ms else float("nan"), dev, world)
     h2d = n * (96 + 4)
     d2h = n * 4 + (n + 1) * 8 + total_contacts * 8
 
@@ -479,7 +499,7 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "tuning": tuning},
             "clocks": clocks,
-            "e2e": {"value": world * n / (t_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": n_all / (t_e2e / 1000.0), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e, "exact_hits": e2e_hits},
             "gpu_launches": int(launches),
             "roofline": roof,
@@ -524,10 +544,10 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
     ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
-    ap.add_argument("--serve-requests", type=int, default=200, help="requests in the Poisson run")
+    ap.add_argument("--serve-requests", type=int, default=1000, help="requests in the Poisson run")
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.7 x measured capacity)")
     ap.add_argument("--serve-step", type=int, default=4096, help="waypoints per loop step")
-    ap.add_argument("--serve-cpu-sample", type=int, default=4, help="requests timed on the CPU baseline")
+    ap.add_argument("--serve-cpu-sample", type=int, default=64, help="requests timed on the CPU baseline")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -64,11 +66,28 @@ int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* 
     h[i].pad = 0;
     for (int k = 0; k < 3; ++k) h[i].p[k] = s.params[k];
   }
+  // vertex pool: the FP64 vertices, then (16-byte aligned) an FP32 float4 copy that the
+  // convex support functions filter with; no copy if a coordinate is outside FP32 range
+  // or the offset does not fit the shape record
+  const int64_t off32 = (3 * nv + 1) & ~int64_t(1);
+  bool use32 = nv > 0 && off32 < INT32_MAX;
+  for (int64_t k = 0; use32 && k < 3 * nv; ++k) use32 = std::fabs(verts[k]) < 1e30;
+  std::vector<float> v32(use32 ? 4 * nv : 0);
+  for (int64_t k = 0; use32 && k < nv; ++k) {
+    for (int c = 0; c < 3; ++c) v32[4 * k + c] = (float)verts[3 * k + c];
+    v32[4 * k + 3] = 0.f;
+  }
+  if (use32)
+    for (auto& d : h)
+      if (d.type == FCLGPU_SHAPE_CONVEX) d.pad = (int32_t)off32;
+  const size_t pool_bytes = sizeof(double) * (use32 ? off32 : 3 * std::max<int64_t>(nv, 1)) + v32.size() * 4;
   fclgpu_shapeset_s* ss = new fclgpu_shapeset_s();
   cudaError_t e = cudaMalloc(&ss->shapes, sizeof(DevShape) * n);
   if (e == cudaSuccess) e = cudaMemcpy(ss->shapes, h.data(), sizeof(DevShape) * n, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMalloc(&ss->verts, sizeof(double) * 3 * std::max<int64_t>(nv, 1));
+  if (e == cudaSuccess) e = cudaMalloc(&ss->verts, pool_bytes);
   if (e == cudaSuccess && nv > 0) e = cudaMemcpy(ss->verts, verts, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && use32)
+    e = cudaMemcpy(ss->verts + off32, v32.data(), v32.size() * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     if (ss->shapes) cudaFree(ss->shapes);
     if (ss->verts) cudaFree(ss->verts);

@@ -67,8 +67,22 @@ FCLG_HD G3f support32(const ShapeRef& sh, const G3f& d) {
       const G3f rim = zd > 0 ? g3f(d.x * (r / zd), d.y * (r / zd), -hh) : g3f(0.f, 0.f, -hh);
       return (d.z * hh > gdot(d, rim)) ? g3f(0.f, 0.f, hh) : rim;
     }
-    case SHAPE_TRIANGLE:
-    case SHAPE_CONVEX: {
+    case SHAPE_CONVEX:
+      if (const float4* V32 = convex_v32(sh)) {
+        G3f best = g3f(V32[0].x, V32[0].y, V32[0].z);
+        float bd = gdot(d, best);
+        for (int i = 1; i < s.vcnt; ++i) {
+          const G3f p = g3f(V32[i].x, V32[i].y, V32[i].z);
+          const float t = gdot(d, p);
+          if (t > bd) {
+            bd = t;
+            best = p;
+          }
+        }
+        return best;
+      }
+      // fall through: FP64 pool only
+    case SHAPE_TRIANGLE: {
       const double* V = sh.verts + 3 * (long long)s.voff;
       const int n = s.type == SHAPE_TRIANGLE ? 3 : s.vcnt;
       G3f best = g3f((float)V[0], (float)V[1], (float)V[2]);

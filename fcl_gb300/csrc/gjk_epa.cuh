@@ -30,6 +30,13 @@ struct ShapeRef {
 
 typedef V3<double> D3v;
 
+// FP32 copy of the convex vertex pool: for a Convex, DevShape.pad is the offset (in
+// doubles) from the pool base to an array of float4 (x, y, z, 0), one per pool vertex;
+// 0 means no copy.
+FCLG_HD const float4* convex_v32(const ShapeRef& sh) {
+  return sh.s.pad > 0 ? reinterpret_cast<const float4*>(sh.verts + sh.s.pad) + sh.s.voff : nullptr;
+}
+
 FCLG_HD D3v d3neg(const D3v& a) { return v3(-a.x, -a.y, -a.z); }
 FCLG_HD D3v d3scale(const D3v& a, double s) { return v3(a.x * s, a.y * s, a.z * s); }
 FCLG_HD double d3norm(const D3v& a) { return sqrt(sqnorm(a)); }
@@ -79,9 +86,39 @@ FCLG_HD D3v shape_support(const ShapeRef& sh, const D3v& dir) {
       return v3(d * dir.x, d * dir.y, (dir.z > 0) ? half_h : -half_h);
     }
     case SHAPE_CONVEX: {
+      // the first vertex of maximal dir.v (strict >), as FCL's linear scan.  With the
+      // FP32 copy, FP32 dot products with a rigorous bound E_i = 8u sum_k |dir_k v_k|
+      // (u = 2^-24; covers the FP32 and the FP64 rounding) select the candidates,
+      // df_i + E_i >= max_j (df_j - E_j); every vertex left out has an FP64 dot below
+      // the maximum, so the FP64 scan over the candidates returns the same vertex.
       double maxdot = -1.7976931348623157e308;
       D3v bestv = v3(0.0, 0.0, 0.0);
       const double* V = sh.verts + 3 * (long long)s.voff;
+      const float4* V32 = convex_v32(sh);
+      if (V32) {
+        const float dx = (float)dir.x, dy = (float)dir.y, dz = (float)dir.z;
+        const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+        float mlo = -3.4e38f;
+        for (int i = 0; i < s.vcnt; ++i) {
+          const float4 p = V32[i];
+          const float df = fmaf(dx, p.x, fmaf(dy, p.y, dz * p.z));
+          const float E = fmaf(4.76837158e-07f, fmaf(ax, fabsf(p.x), fmaf(ay, fabsf(p.y), az * fabsf(p.z))), 1e-30f);
+          mlo = fmaxf(mlo, df - E);
+        }
+        for (int i = 0; i < s.vcnt; ++i) {
+          const float4 p = V32[i];
+          const float df = fmaf(dx, p.x, fmaf(dy, p.y, dz * p.z));
+          const float E = fmaf(4.76837158e-07f, fmaf(ax, fabsf(p.x), fmaf(ay, fabsf(p.y), az * fabsf(p.z))), 1e-30f);
+          if (!(df + E >= mlo)) continue;
+          const D3v vi = v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]);
+          const double d = dot(dir, vi);
+          if (d > maxdot) {
+            bestv = vi;
+            maxdot = d;
+          }
+        }
+        return bestv;
+      }
       for (int i = 0; i < s.vcnt; ++i) {
         const D3v vi = v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]);
         const double d = dot(dir, vi);

@@ -63,3 +63,47 @@ def run_poisson(server, requests, rate: float, seed: int = 0) -> dict:
         "queue_p50_ms": float(np.percentile(queue, 50)),
         "results": results,
     }
+
+
+def main(argv=None) -> None:
+    """Command line: build the motion-checking scene (seeded), then run a burst and,
+    optionally, Poisson arrivals; prints one JSON line with the engine statistics and
+    the broadphase phase times of the last call."""
+    import argparse
+    import ctypes as C
+    import json
+
+    from . import api, native
+    from . import workloads as W
+    ap = argparse.ArgumentParser(prog="python -m fcl_gb300.serving")
+    ap.add_argument("--objects", type=int, default=0, help="scene objects (0 = the seeded draw)")
+    ap.add_argument("--burst", type=int, default=16, help="requests submitted at once")
+    ap.add_argument("--poisson", type=int, default=0, help="requests at Poisson arrivals after the burst")
+    ap.add_argument("--rate", type=float, default=0.0, help="arrivals/s (0 = 0.7 x the burst's rate)")
+    ap.add_argument("--step", type=int, default=4096, help="waypoints per loop step")
+    ap.add_argument("--seed", type=int, default=4)
+    a = ap.parse_args(argv)
+    native.check(native.lib().fclgpu_init(0), "fclgpu_init")
+    w = W.scene4(n_objects=a.objects or None, seed=a.seed)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in w.meshes]
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(w.refs, w.tf)
+    reqs = W.motion_requests(w, a.burst + a.poisson, seed=a.seed + 1)
+    srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=a.step)
+    out = {"objects": w.n}
+    b = run_burst(srv, reqs[:a.burst])
+    out["burst"] = {k: b[k] for k in ("requests", "seconds", "requests_per_s")}
+    if a.poisson:
+        p = run_poisson(srv, reqs[a.burst:], a.rate or 0.7 * b["requests_per_s"], seed=a.seed + 2)
+        out["poisson"] = {k: v for k, v in p.items() if k != "results"}
+    out["engine"] = srv.stats()
+    ph = (C.c_double * 16)()
+    native.check(native.lib().fclgpu_broadphase_last_phase_ms(C.cast(ph, C.c_void_p)), "fclgpu_broadphase_last_phase_ms")
+    out["phases"] = list(ph)
+    srv.close()
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,3 +1,4 @@
+#include <algorithm>
 // Test-only host build of the product's traversal code (collide_traverse.cuh) and
 // BVH construction (bvh_build.cpp), so the kernel logic -- FP32 filters, FP64
 // rechecks, visit order -- can be compared with the oracle without a GPU.  This
@@ -227,17 +228,28 @@ void emu_shape_batch(int ns, const int* type, const double* params, const int* v
                      const double* verts, int64_t n, const int* ia, const int* ib, const double* tf1,
                      const double* tf2, int* hit, double* normal, double* point, double* depth, double* dist,
                      double* p1, double* p2, int* status) {
+  // the pool as fclgpu_shapeset_create lays it out: FP64 vertices, then the FP32
+  // float4 copy the convex supports filter with
+  int64_t nv = 0;
+  for (int i = 0; i < ns; ++i)
+    if (type[i] == SHAPE_CONVEX) nv = std::max<int64_t>(nv, (int64_t)voff[i] + vcnt[i]);
+  const int64_t off32 = (3 * nv + 1) & ~int64_t(1);
+  std::vector<double> pool(off32 + 2 * nv + 2, 0.0);
+  std::copy(verts, verts + 3 * nv, pool.begin());
+  float* v32 = reinterpret_cast<float*>(pool.data() + off32);
+  for (int64_t k = 0; k < nv; ++k)
+    for (int c = 0; c < 3; ++c) v32[4 * k + c] = (float)verts[3 * k + c];
   std::vector<DevShape> sh(ns);
   for (int i = 0; i < ns; ++i) {
     sh[i].type = type[i];
     sh[i].voff = voff[i];
     sh[i].vcnt = vcnt[i];
-    sh[i].pad = 0;
+    sh[i].pad = (type[i] == SHAPE_CONVEX && nv > 0) ? (int)off32 : 0;
     for (int k = 0; k < 3; ++k) sh[i].p[k] = params[3 * i + k];
   }
   for (int64_t q = 0; q < n; ++q) {
     PairOut o;
-    shape_pair_query(sh[ia[q]], sh[ib[q]], verts, tf1 + 12 * q, tf2 + 12 * q, o);
+    shape_pair_query(sh[ia[q]], sh[ib[q]], pool.data(), tf1 + 12 * q, tf2 + 12 * q, o);
     hit[q] = o.hit;
     const D3v* v[4] = {&o.normal, &o.point, &o.p1, &o.p2};
     double* d[4] = {normal, point, p1, p2};
