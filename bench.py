@@ -229,6 +229,8 @@ def run_secondary(args, meshes, stream, flush):
     from fcl_gb300 import workloads as W
     out = {}
     dev = flush.device
+    if args.only == "shapes":
+        return {"shapes": _run_shapes(args, stream, flush)}
     w2 = W.config2(total_poses=int(1_000_000 * args.scale), n_pairs=args.pairs, tri_hi=args.tri_hi)
     tf2 = torch.from_numpy(w2.tf2).to(dev)
     pq = torch.from_numpy(w2.pair).to(dev)
@@ -255,21 +257,31 @@ def run_secondary(args, meshes, stream, flush):
         "max_rel_err_vs_fp64": float(rel.max()), "p99_rel_err_vs_fp64": float(np.percentile(rel, 99)),
         "within_margin_equal": bool(torch.equal(a["within_margin"], b["within_margin"])),
     }
+    out["shapes"] = _run_shapes(args, stream, flush)
+    return out
+
+
+def _run_shapes(args, stream, flush):
+    """The 4M convex-pair batch (GJK/EPA, closed forms), FP64 reference arithmetic."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    dev = flush.device
     w3 = W.config3(n_pairs=int(4_000_000 * args.scale))
     ss = api.ShapeSet.from_workload(w3.shapes)
     d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(dev)
     ia, ib, t1, t2 = d(w3.ia), d(w3.ib), d(w3.tf1), d(w3.tf2)
     ms3 = _time_device(lambda: api.shape_batch(ss, ia, ib, t1, t2, stream=stream.cuda_stream), 2, 1, stream, flush)
-    out["shapes"] = {"workload": "c3_convex_4M_pairs_gst_indep", "pairs": w3.n, "value": w3.n / (ms3 / 1000.0),
-                     "unit": "pairs/s", "ms_per_step": ms3, "form": "fp64"}
+    out = {"workload": "c3_convex_4M_pairs_gst_indep", "pairs": w3.n, "value": w3.n / (ms3 / 1000.0),
+           "unit": "pairs/s", "ms_per_step": ms3, "form": "fp64"}
     if not args.no_cpu:
         from oracle import pyoracle as O
         threads = O.hardware_threads()
-        k = 20000
+        k = w3.n  # about 1 s on 16 cores
         t0 = time.perf_counter()
         O.shape_batch(w3.shapes, w3.ia[:k], w3.ib[:k], w3.tf1[:k], w3.tf2[:k], nthreads=threads)
-        out["shapes"]["cpu_baseline"] = {"value": k / (time.perf_counter() - t0), "unit": "pairs/s",
-                                         "cores": threads, "kind": "port", "sample": f"first {k} pairs"}
+        out["cpu_baseline"] = {"value": k / (time.perf_counter() - t0), "unit": "pairs/s",
+                               "cores": threads, "kind": "port", "sample": f"all {k} pairs"}
     return out
 
 
@@ -331,6 +343,16 @@ def run_gpu(args):
     from fcl_gb300 import api, native
     native.check(native.lib().fclgpu_init(local), "fclgpu_init")
     L = native.lib()
+
+    if args.only != "all":
+        # one secondary section on its own (profiling runs); prints that section only
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=torch.device("cuda", local))
+        stream = torch.cuda.Stream(device=local)
+        if args.only == "serving":
+            print(json.dumps({"serving": run_serving(args)}))
+        else:
+            print(json.dumps(run_secondary(args, None, stream, flush)))
+        return
 
     w = _workload(args, rank)
     t0 = time.time()
@@ -542,6 +564,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
+    ap.add_argument("--only", default="all", choices=["all", "shapes", "serving"],
+                    help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests in the Poisson run")

@@ -15,6 +15,7 @@
 
 #include "broadphase.h"
 #include "kernels.h"
+#include "mesh_shape.cuh"
 #include "shape_pair.cuh"
 
 namespace fclgpu {
@@ -670,7 +671,8 @@ __global__ void k_bp_gather_mesh(BpSceneView S, BpQueryView Q, const int2* pairs
 }
 
 __global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pairs, const int64_t* list, long long nl,
-                                  int32_t* mesh_idx, int32_t* shape_idx, double* tfm, double* tfs) {
+                                  int32_t* mesh_idx, int32_t* shape_idx, double* tfm, double* tfs, int32_t* bv_src,
+                                  int32_t* need) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
     const int2 p = pairs[list[j]];
@@ -679,6 +681,11 @@ __global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pair
     const bool obj_is_mesh = go.kind == GEOM_MESH;
     mesh_idx[j] = obj_is_mesh ? go.index : gq.index;
     shape_idx[j] = obj_is_mesh ? gq.index : go.index;
+    if (bv_src) {
+      const long long src = obj_is_mesh ? (long long)p.x : Q.nq + p.y;
+      bv_src[j] = (int32_t)src;
+      need[src] = 1;
+    }
     const double* a = obj_is_mesh ? S.tf + 12 * (long long)p.y : Q.tf + 12 * (long long)p.x;
     const double* b = obj_is_mesh ? Q.tf + 12 * (long long)p.x : S.tf + 12 * (long long)p.y;
 #pragma unroll
@@ -686,6 +693,22 @@ __global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pair
       tfm[12 * j + k] = a[k];
       tfs[12 * j + k] = b[k];
     }
+  }
+}
+
+// world-frame shape BV per needed source: queries first, then scene objects
+__global__ void __launch_bounds__(128) k_bp_shape_bvs(BpSceneView S, BpQueryView Q, const int32_t* need,
+                                                      ShapeBV* table) {
+  const long long n = Q.nq + S.n;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long src = (long long)blockIdx.x * blockDim.x + threadIdx.x; src < n; src += stride) {
+    if (!need[src]) continue;
+    const bool is_q = src < Q.nq;
+    const GeomRec& g = S.geoms[is_q ? Q.gid[src] : S.gid[src - Q.nq]];
+    M3<double> R;
+    D3v t;
+    load_tf(is_q ? Q.tf + 12 * src : S.tf + 12 * (src - Q.nq), R, t);
+    shape_obbrss(S.shapes[g.index], S.sverts, R, t, table[src]);
   }
 }
 
@@ -900,9 +923,18 @@ cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32
 
 cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
                                    const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
-                                   double* tfm, double* tfs, cudaStream_t s) {
+                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, cudaStream_t s) {
   if (nlist <= 0) return cudaSuccess;
-  k_bp_gather_mixed<<<grid_for(nlist, 256), 256, 0, s>>>(S, Q, pairs, list, nlist, mesh_idx, shape_idx, tfm, tfs);
+  k_bp_gather_mixed<<<grid_for(nlist, 256), 256, 0, s>>>(S, Q, pairs, list, nlist, mesh_idx, shape_idx, tfm, tfs,
+                                                          bv_src, need);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_shape_bvs(const BpSceneView& S, const BpQueryView& Q, const int32_t* need, void* table,
+                                cudaStream_t s) {
+  const long long n = Q.nq + S.n;
+  k_bp_shape_bvs<<<grid_for(n, 128), 128, 0, s>>>(S, Q, need, static_cast<ShapeBV*>(table));
   ++g_kernel_launches;
   return cudaGetLastError();
 }

@@ -118,9 +118,16 @@ cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32
 // Mixed pairs (kind 2): FCL calls BVH-shape with the mesh first whichever object is
 // the mesh (collision-inl.h:100-111, distance-inl.h:117-126); gather (mesh, shape)
 // indices and poses in that order.
+// bv_src (optional): per pair, the shape's BV source (query q -> q, scene object o ->
+// nq + o), with need[src] = 1 set for every source used.
 cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
                                    const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
-                                   double* tfm, double* tfs, cudaStream_t s);
+                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, cudaStream_t s);
+// The shape BV (computeBV<OBBRSS> in the world frame) of every needed source into
+// table (ShapeBV records of mesh_shape.cuh): a shape at one pose is fitted once however
+// many mesh-shape pairs it is in.
+cudaError_t launch_bp_shape_bvs(const BpSceneView& S, const BpQueryView& Q, const int32_t* need, void* table,
+                                cudaStream_t s);
 cudaError_t launch_bp_scatter_mixed_dist(const int64_t* list, int64_t nlist, const double* d, const int32_t* tri,
                                          const double* pts, double* dist, int32_t* b12, double* outpts,
                                          cudaStream_t s);

@@ -16,6 +16,7 @@
 #include "broadphase.h"
 #include "kernels.h"
 #include "mesh_handle.h"
+#include "mesh_shape.cuh"
 #include "mesh_shape.h"
 #include "shape_pair.cuh"
 #include "shapeset_handle.h"
@@ -85,7 +86,7 @@ struct BpScratch {
   Buf ctr, qgid, q64, q32, counts, offsets, scan_tmp, ub;
   Buf pairs, kind, hit, dist, b12, pts, list;
   Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
-  Buf x_midx, x_sidx, x_counts, x_tri, qdone;
+  Buf x_midx, x_sidx, x_counts, x_tri, qdone, x_bvsrc, x_need, x_bvtab;
   Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
 };
 BpScratch g_bs;
@@ -288,9 +289,22 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
   CKB(g_bs.m_dist.ensure(8 * nl), "mixed scratch");
   CKB(g_bs.x_tri.ensure(4 * nl), "mixed scratch");
   CKB(g_bs.m_pts.ensure(48 * nl), "mixed scratch");
+  // one shape BV per (shape, pose) source, shared by all its mesh-shape pairs (sources
+  // are int32 indices; beyond that every pair fits its own)
+  const int64_t nsrc = Q.nq + S.n;
+  const bool table = nsrc < INT32_MAX;
+  if (table) {
+    CKB(g_bs.x_bvsrc.ensure(4 * nl), "mixed scratch");
+    CKB(g_bs.x_need.ensure(4 * nsrc), "mixed scratch");
+    CKB(g_bs.x_bvtab.ensure(sizeof(ShapeBV) * nsrc), "mixed scratch");
+    CKB(cudaMemsetAsync(g_bs.x_need.p, 0, 4 * nsrc, s), "mixed scratch");
+  }
   CKB(launch_bp_gather_mixed(S, Q, g_bs.pairs.as<int2>(), g_bs.list.as<int64_t>(), nl, g_bs.x_midx.as<int32_t>(),
-                             g_bs.x_sidx.as<int32_t>(), g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
+                             g_bs.x_sidx.as<int32_t>(), g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(),
+                             table ? g_bs.x_bvsrc.as<int32_t>() : nullptr,
+                             table ? g_bs.x_need.as<int32_t>() : nullptr, s),
       "mixed gather");
+  if (table) CKB(launch_bp_shape_bvs(S, Q, g_bs.x_need.as<int32_t>(), g_bs.x_bvtab.p, s), "shape BVs");
   MeshShapeLaunch L;
   L.meshes = bp->dmeshes;
   L.shapes = bp->shapes->shapes;
@@ -309,6 +323,8 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
   L.nbv = nullptr;
   L.nleaf = nullptr;
   L.status = &dctr->status;
+  L.bv_table = table ? g_bs.x_bvtab.p : nullptr;
+  L.bv_src = table ? g_bs.x_bvsrc.as<int32_t>() : nullptr;
   CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
   if (mode == 0) {
     CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.x_counts.as<int32_t>(), g_bs.hit.as<int32_t>(), s),

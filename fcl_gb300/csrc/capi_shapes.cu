@@ -32,7 +32,7 @@ struct Buf {
     return e;
   }
 };
-Buf g_ctr, g_ia, g_ib, g_tf1, g_tf2, g_hit, g_nrm, g_pt, g_dep, g_dist, g_p1, g_p2, g_st;
+Buf g_ctr, g_ia, g_ib, g_tf1, g_tf2, g_hit, g_nrm, g_pt, g_dep, g_dist, g_p1, g_p2, g_st, g_order, g_epa, g_bins;
 cudaEvent_t g_ev[2] = {nullptr, nullptr};
 
 int cfail(cudaError_t e, const char* where) {
@@ -143,13 +143,18 @@ int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const int32_t* ia,
   L.p1 = res->p1 ? res->p1 : (double*)g_p1.p;
   L.p2 = res->p2 ? res->p2 : (double*)g_p2.p;
   L.status = res->status;
+  CKS(g_order.ensure(4 * nn), "scratch");
+  CKS(g_epa.ensure(4 * nn), "scratch");
+  CKS(g_bins.ensure(64 * 4 + 8), "scratch");
+  L.order = (int32_t*)g_order.p;
+  L.epa_list = (int32_t*)g_epa.p;
+  L.epa_count = (unsigned long long*)((char*)g_bins.p + 64 * 4);
   if (!g_ev[0]) {
     CKS(cudaEventCreate(&g_ev[0]), "event");
     CKS(cudaEventCreate(&g_ev[1]), "event");
   }
-  const int block = 128;
   CKS(cudaEventRecord(g_ev[0], s), "event");
-  CKS(launch_shape_batch(L, shape_grid(block), block, s), "shape kernel");
+  CKS(launch_shape_batch(L, (unsigned*)g_bins.p, s), "shape kernel");
   CKS(cudaEventRecord(g_ev[1], s), "event");
   CKS(cudaStreamSynchronize(s), "shape kernel");
   float ms = 0.f;

@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(128) k_ms_collect(MeshShapeLaunch L, int32_t* 
     PairGeom g;
     pair_geom(L, i, g);
     ShapeBV bv;
-    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
+    if (L.bv_src)
+      bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
+    else
+      shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
     const long long base = offsets ? offsets[i] : 0;
     int cnt = 0;
     auto emit = [&](int prim, double lb) {
@@ -156,10 +159,11 @@ __global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t
 }
 
 // Collide in rounds.  Each unfinished pair resumes its DFS (stack kept in global
-// memory) until it has K_r more overlapping leaves; the leaves are then tested one per
-// thread (shape_triangle_gjk_stage: the FP32-certified GJK, no EPA), and a pair stops
-// once it has max_contacts intersecting leaves or its DFS is done -- FCL's early stop,
-// at the granularity of a round.  K_r = 16 * 2^r (at most 1024): colliding pairs usually
+// memory) until it has K_r more overlapping leaves; stage 1 of the leaf test runs one
+// leaf per thread (sphere closed form, FP32 GJK with the FP64 disjointness
+// certificate), then one thread per pair walks its leaves in DFS order, running the
+// FP64 GJK on undecided leaves, and stops once it has max_contacts intersecting leaves
+// -- FCL's early stop (the rest of the DFS is not visited either).  K_r = 16 * 2^r (at most 1024): colliding pairs usually
 // stop in the first round, long contact-free traversals need few rounds.
 struct MsPairState {
   ShapeBV bv;
@@ -173,7 +177,10 @@ __global__ void __launch_bounds__(128) k_msr_init(MeshShapeLaunch L, MsPairState
     PairGeom g;
     pair_geom(L, i, g);
     MsPairState st;
-    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, st.bv);
+    if (L.bv_src)
+      st.bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
+    else
+      shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, st.bv);
     make_shape_bv32(g.Rm, g.tm, st.bv, g.m, st.b32);
     ps[i] = st;
     stack[i * (long long)cap] = 0;
@@ -220,20 +227,33 @@ __global__ void __launch_bounds__(128) k_msr_tests(MeshShapeLaunch L, const int3
     pair_geom(L, act[a], g);
     double P[9];
     load_tri_local(g.m, leaf[t], P);
-    SimplexVert V[kSimplexSlots];
-    hit[t] = shape_triangle_gjk_stage(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V);
+    hit[t] = shape_triangle_stage1(g.A, g.Rs, g.ts, P, g.Rm, g.tm);
   }
 }
 
 __global__ void __launch_bounds__(128) k_msr_update(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
-                                                    const int32_t* nleaf, const int32_t* hit, const int32_t* sp,
-                                                    int32_t* next, unsigned long long* nnext) {
+                                                    const int32_t* leaf, const int32_t* nleaf, const int32_t* hit,
+                                                    const int32_t* sp, int32_t* next, unsigned long long* nnext) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
     const long long i = act[a];
     int c = L.counts[i];
     const int nl = nleaf[a];
-    for (int k = 0; k < nl && c < L.max_contacts; ++k) c += hit[a * (long long)K + k];
+    // leaves in DFS order; the FP64 GJK runs only for undecided leaves and only while
+    // the pair still needs contacts
+    for (int k = 0; k < nl && c < L.max_contacts; ++k) {
+      const int h = hit[a * (long long)K + k];
+      if (h == 2) {
+        ++c;
+      } else if (h == 1) {
+        PairGeom g;
+        pair_geom(L, i, g);
+        double P[9];
+        load_tri_local(g.m, leaf[a * (long long)K + k], P);
+        SimplexVert V[kSimplexSlots];
+        if (shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V)) ++c;
+      }
+    }
     L.counts[i] = c;
     if (c < L.max_contacts && sp[i] > 0) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
   }
@@ -292,7 +312,7 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
     if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
     k_msr_dfs<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, ps, stack, cap, sp, leaf, nleaf);
     k_msr_tests<<<grid128(nl), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit);
-    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, nleaf, hit, sp, next, nnext);
+    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit, sp, next, nnext);
     g_kernel_launches += 3;
     unsigned long long nn = 0;
     if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||

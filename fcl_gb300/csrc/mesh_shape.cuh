@@ -565,14 +565,10 @@ FCLG_HD bool shape_triangle_intersect(const ShapeRef& A, const M3<double>& Rs, c
 // shapeTriangleIntersect): the sphere closed form, else GJK on the shape and TriangleP;
 // GJK Inside is an intersection, because the EPA that follows only fills the contact:
 // EPA::evaluate never returns Failed (epa-inl.h sets Failed only in initialize, :118,
-// and evaluate ends Valid/.../FallBack).  Returns 1 (intersecting) or 0.
-FCLG_HD int shape_triangle_gjk_stage(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
-                                     const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
-  if (A.s.type == SHAPE_SPHERE) {
-    const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
-    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 1
-                                                                                                          : 0;
-  }
+// and evaluate ends Valid/.../FallBack).  In two stages: stage 1 settles the sphere
+// closed form (0 / 2) and the pairs the FP32 GJK certifies disjoint (0); the rest (1)
+// need stage 2, the FP64 GJK.
+FCLG_HD ShapeRef triangle_ref(const double* P) {
   ShapeRef B;
   B.s.type = SHAPE_TRIANGLE;
   B.s.voff = 0;
@@ -580,12 +576,24 @@ FCLG_HD int shape_triangle_gjk_stage(const ShapeRef& A, const M3<double>& Rs, co
   B.s.pad = 0;
   B.s.p[0] = B.s.p[1] = B.s.p[2] = 0;
   B.verts = P;
-  if (certified_disjoint(A, Rs, ts, B, Rm, tm)) return 0;
+  return B;
+}
+FCLG_HD int shape_triangle_stage1(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
+                                  const M3<double>& Rm, const D3v& tm) {
+  if (A.s.type == SHAPE_SPHERE) {
+    const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
+    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 2
+                                                                                                          : 0;
+  }
+  return certified_disjoint(A, Rs, ts, triangle_ref(P), Rm, tm) ? 0 : 1;
+}
+FCLG_HD bool shape_triangle_gjk64(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
+                                  const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
   GjkState g;
-  make_minkowski(A, Rs, ts, B, Rm, tm, g.shape);
+  make_minkowski(A, Rs, ts, triangle_ref(P), Rm, tm, g.shape);
   g.V = V;
   g.tolerance = kGjkTol;
-  return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), 128) == GJK_INSIDE ? 1 : 0;
+  return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), 128) == GJK_INSIDE;
 }
 
 // shapeTriangleDistance; ps on the shape, pt on the triangle, in FCL's frames

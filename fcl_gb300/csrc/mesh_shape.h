@@ -26,6 +26,10 @@ struct MeshShapeLaunch {
   int64_t* nbv;
   int64_t* nleaf;
   unsigned* status;
+  // optional precomputed shape BVs: pair i uses ShapeBV bv_table[bv_src[i]] (records of
+  // mesh_shape.cuh) instead of fitting its own; null = fit per pair
+  const void* bv_table = nullptr;
+  const int32_t* bv_src = nullptr;
 };
 
 // One thread per pair runs the whole FCL traversal (exact statistics).

@@ -393,11 +393,16 @@ FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1
 }
 
 // One pair: shapes a, b (with the vertex pool) at tf1, tf2 (3x4 row-major).
-enum { PAIR_INTERSECT = 1, PAIR_DISTANCE = 2, PAIR_BOTH = 3, PAIR_NO_CONTACT = 4 };
+enum { PAIR_INTERSECT = 1, PAIR_DISTANCE = 2, PAIR_BOTH = 3, PAIR_NO_CONTACT = 4, PAIR_DEFER_EPA = 8 };
+// estat of a pair whose GJK ended Inside under PAIR_DEFER_EPA: the contact (EPA) is
+// still to be computed by a full PAIR_INTERSECT query
+constexpr int kEpaPending = -2;
 
 // mode PAIR_INTERSECT: fcl::collide only; PAIR_DISTANCE: fcl::distance only (dist = -1
 // when the distance dispatch finds the pair intersecting); PAIR_BOTH: collide, then
-// distance when the pair does not collide.  PAIR_NO_CONTACT: collide without contact
+// distance when the pair does not collide.  PAIR_DEFER_EPA: a GJK pair that ends
+// Inside is reported hit with estat = kEpaPending and no contact (EPA is run later,
+// apart from the GJK pairs).  PAIR_NO_CONTACT: collide without contact
 // information (CollisionRequest::enable_contact = false); it changes only the box-box
 // case in which the reference's face clipping keeps no point, which then collides
 // (box_box-inl.h:747, 775) while collide() with contacts adds no contact and reports
@@ -447,9 +452,10 @@ FCLG_HD void shape_pair_query(const DevShape& sa, const DevShape& sb, const doub
   } else if (a == SHAPE_CYLINDER && b == SHAPE_SPHERE) {
     hit = sphere_cylinder_intersect(B.s.p[0], t2, A.s.p[0], A.s.p[1], R1, t1, o);
     if (hit) o.normal = d3neg(o.normal);
-  } else if (mode & PAIR_NO_CONTACT) {
+  } else if (mode & (PAIR_NO_CONTACT | PAIR_DEFER_EPA)) {
     gjk_intersect(A, R1, t1, B, R2, t2, V, nullptr, o);
     hit = o.hit != 0;
+    if (hit && (mode & PAIR_DEFER_EPA)) o.estat = kEpaPending;
   } else {
     EpaState epa;
     gjk_intersect(A, R1, t1, B, R2, t2, V, &epa, o);

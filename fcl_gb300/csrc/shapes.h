@@ -22,9 +22,12 @@ struct ShapeLaunch {
   double* p1;
   double* p2;
   int32_t* status;
+  int32_t* order;                   // n: pair indices bucketed by (type, type)
+  int32_t* epa_list;                // n: pairs whose GJK ended Inside
+  unsigned long long* epa_count;
 };
 
-cudaError_t launch_shape_batch(const ShapeLaunch& L, int grid, int block, cudaStream_t s);
-int shape_grid(int block);
+// Whole batch in stages (bucket, intersect, EPA, distance); bins: 64 unsigned scratch.
+cudaError_t launch_shape_batch(const ShapeLaunch& L, unsigned* bins, cudaStream_t s);
 
 }  // namespace fclgpu
