@@ -97,6 +97,21 @@ def _time_cpu(w_sample, nthreads):
     return time.perf_counter() - t0, total
 
 
+def _time_cpu_distance(w_sample, nthreads):
+    from oracle import pyoracle as O
+    om = {}
+    for p in np.unique(w_sample.pair):
+        for m in w_sample.pairs[p]:
+            if m not in om:
+                om[m] = O.Mesh(*w_sample.meshes[m])
+    t0 = time.perf_counter()
+    for p in np.unique(w_sample.pair):
+        idx = np.nonzero(w_sample.pair == p)[0]
+        O.distance_batch(om[w_sample.pairs[p, 0]], om[w_sample.pairs[p, 1]], w_sample.tf2[idx], nearest=True,
+                         nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -257,6 +272,13 @@ def run_secondary(args, meshes, stream, flush):
         "max_rel_err_vs_fp64": float(rel.max()), "p99_rel_err_vs_fp64": float(np.percentile(rel, 99)),
         "within_margin_equal": bool(torch.equal(a["within_margin"], b["within_margin"])),
     }
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        threads = O.hardware_threads()
+        k = min(w2.n, 4000)
+        dt = _time_cpu_distance(W.subsample(w2, k, seed=3), threads)
+        out["distance"]["cpu_baseline"] = {"value": k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+                                           "sample": f"{k} queries drawn uniformly from the {w2.n}-query workload"}
     out["shapes"] = _run_shapes(args, stream, flush)
     return out
 
