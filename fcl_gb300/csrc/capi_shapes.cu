@@ -145,7 +145,7 @@ int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const int32_t* ia,
   L.status = res->status;
   CKS(g_order.ensure(4 * nn), "scratch");
   CKS(g_epa.ensure(4 * nn), "scratch");
-  CKS(g_bins.ensure(64 * 4 + 8), "scratch");
+  CKS(g_bins.ensure(64 * 4 + 16), "scratch");  // bins, EPA count, distance work counter
   L.order = (int32_t*)g_order.p;
   L.epa_list = (int32_t*)g_epa.p;
   L.epa_count = (unsigned long long*)((char*)g_bins.p + 64 * 4);

@@ -30,6 +30,16 @@ struct ShapeRef {
 
 typedef V3<double> D3v;
 
+FCLG_HD unsigned long long dbits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+
 // FP32 copy of the convex vertex pool: for a Convex, DevShape.pad is the offset (in
 // doubles) from the pool base to an array of float4 (x, y, z, 0), one per pool vertex;
 // 0 means no copy.
@@ -317,11 +327,20 @@ struct GjkState {
     get_support(v, V[s.c[s.rank++]]);
   }
 
-  FCLG_HD int evaluate(const D3v& guess, int max_iterations) {
-    int iterations = 0;
-    double alpha = 0;
-    D3v lastw[4];
-    int clastw = 0;
+  // GJK::evaluate (gjk-inl.h:81-231) as begin / step / finish, so that a lane can run
+  // one iteration at a time (the batch kernels refill a lane with the next pair as soon
+  // as its GJK ends); evaluate() is the three in sequence.
+  int iterations;
+  double alpha;
+  D3v lastw[4];
+  int clastw;
+  int max_iter;
+
+  FCLG_HD void begin(const D3v& guess, int max_iterations) {
+    iterations = 0;
+    alpha = 0;
+    clastw = 0;
+    max_iter = max_iterations;
     free_v[0] = 0;
     free_v[1] = 1;
     free_v[2] = 2;
@@ -336,69 +355,79 @@ struct GjkState {
     simplices[0].p[0] = 1;
     ray = V[simplices[0].c[0]].w;
     lastw[0] = lastw[1] = lastw[2] = lastw[3] = ray;
-    do {
-      const int next = 1 - current;
-      Simplex& curr = simplices[current];
-      Simplex& nxt = simplices[next];
-      const double rl = d3norm(ray);
-      if (rl < tolerance) {
-        status = GJK_INSIDE;
+  }
+  // one pass of the do-while body; true when the loop ends
+  FCLG_HD bool step() {
+    const int next = 1 - current;
+    Simplex& curr = simplices[current];
+    Simplex& nxt = simplices[next];
+    const double rl = d3norm(ray);
+    if (rl < tolerance) {
+      status = GJK_INSIDE;
+      return true;
+    }
+    append_vertex(curr, d3neg(ray));
+    const D3v w = V[curr.c[curr.rank - 1]].w;
+    bool found = false;
+    for (int i = 0; i < 4; ++i) {
+      if (sqnorm(w - lastw[i]) < tolerance) {
+        found = true;
         break;
       }
-      append_vertex(curr, d3neg(ray));
-      const D3v w = V[curr.c[curr.rank - 1]].w;
-      bool found = false;
-      for (int i = 0; i < 4; ++i) {
-        if (sqnorm(w - lastw[i]) < tolerance) {
-          found = true;
-          break;
+    }
+    if (found) {
+      remove_vertex(simplices[current]);
+      return true;
+    } else {
+      lastw[clastw = (clastw + 1) & 3] = w;
+    }
+    const double omega = dot(ray, w) / rl;
+    alpha = fmax(alpha, omega);
+    if ((rl - alpha) - tolerance * rl <= 0) {
+      remove_vertex(simplices[current]);
+      return true;
+    }
+    ProjRes pr;
+    proj_init(pr);
+    switch (curr.rank) {
+      case 2: pr = project_line_origin(V[curr.c[0]].w, V[curr.c[1]].w); break;
+      case 3: pr = project_triangle_origin(V[curr.c[0]].w, V[curr.c[1]].w, V[curr.c[2]].w); break;
+      case 4: pr = project_tetra_origin(V[curr.c[0]].w, V[curr.c[1]].w, V[curr.c[2]].w, V[curr.c[3]].w); break;
+    }
+    if (pr.sqd >= 0) {
+      nxt.rank = 0;
+      ray = v3(0.0, 0.0, 0.0);
+      current = next;
+      for (int i = 0; i < curr.rank; ++i) {
+        if (pr.enc & (1u << i)) {
+          nxt.c[nxt.rank] = curr.c[i];
+          nxt.p[nxt.rank++] = pr.par[i];
+          ray = ray + d3scale(V[curr.c[i]].w, pr.par[i]);
+        } else {
+          free_v[nfree++] = curr.c[i];
         }
       }
-      if (found) {
-        remove_vertex(simplices[current]);
-        break;
-      } else {
-        lastw[clastw = (clastw + 1) & 3] = w;
-      }
-      const double omega = dot(ray, w) / rl;
-      alpha = fmax(alpha, omega);
-      if ((rl - alpha) - tolerance * rl <= 0) {
-        remove_vertex(simplices[current]);
-        break;
-      }
-      ProjRes pr;
-      proj_init(pr);
-      switch (curr.rank) {
-        case 2: pr = project_line_origin(V[curr.c[0]].w, V[curr.c[1]].w); break;
-        case 3: pr = project_triangle_origin(V[curr.c[0]].w, V[curr.c[1]].w, V[curr.c[2]].w); break;
-        case 4: pr = project_tetra_origin(V[curr.c[0]].w, V[curr.c[1]].w, V[curr.c[2]].w, V[curr.c[3]].w); break;
-      }
-      if (pr.sqd >= 0) {
-        nxt.rank = 0;
-        ray = v3(0.0, 0.0, 0.0);
-        current = next;
-        for (int i = 0; i < curr.rank; ++i) {
-          if (pr.enc & (1u << i)) {
-            nxt.c[nxt.rank] = curr.c[i];
-            nxt.p[nxt.rank++] = pr.par[i];
-            ray = ray + d3scale(V[curr.c[i]].w, pr.par[i]);
-          } else {
-            free_v[nfree++] = curr.c[i];
-          }
-        }
-        if (pr.enc == 15) status = GJK_INSIDE;
-      } else {
-        remove_vertex(simplices[current]);
-        break;
-      }
-      status = ((++iterations) < max_iterations) ? status : GJK_FAILED;
-    } while (status == GJK_VALID);
+      if (pr.enc == 15) status = GJK_INSIDE;
+    } else {
+      remove_vertex(simplices[current]);
+      return true;
+    }
+    status = ((++iterations) < max_iter) ? status : GJK_FAILED;
+    return status != GJK_VALID;
+  }
+  FCLG_HD int finish() {
     switch (status) {
       case GJK_VALID: distance = d3norm(ray); break;
       case GJK_INSIDE: distance = 0; break;
       default: break;
     }
     return status;
+  }
+  FCLG_HD int evaluate(const D3v& guess, int max_iterations) {
+    begin(guess, max_iterations);
+    while (!step()) {
+    }
+    return finish();
   }
 
   // encloseOrigin (gjk-inl.h:235-298), unrolled by rank
@@ -472,6 +501,7 @@ enum : int {
 struct EpaFace {
   D3v n;
   double d;
+  unsigned long long sqd;  // bits of d * d (>= 0): findBest compares them as integers
   int pass;
   short c[3];   // vertex slots
   short f[3];   // adjacent faces
@@ -561,6 +591,7 @@ struct EpaState {
           fc.d = dot(V[a].w, fc.n) / l;
         }
         fc.n = v3(fc.n.x / l, fc.n.y / l, fc.n.z / l);
+        fc.sqd = dbits(fc.d * fc.d);
         if (forced || fc.d >= -tolerance)
           return face;
         else
@@ -575,11 +606,17 @@ struct EpaState {
     status = (stock.root >= 0) ? EPA_OUTOFVERTICES : EPA_OUTOFFACES;
     return -1;
   }
+  // findBest (epa-inl.h): the first face in hull order with the smallest d * d.  The
+  // squares are non-negative doubles, whose order is the order of their bit patterns,
+  // so the scan compares integers; a NaN square at the root wins as in FCL (no later
+  // face compares less than NaN), and later NaN squares never win (their bits exceed
+  // every finite square's).
   FCLG_HD int find_best() const {
     int minf = hull.root;
-    double mind = F[minf].d * F[minf].d;
+    unsigned long long mind = F[minf].sqd;
+    if (mind > 0x7FF0000000000000ull) return minf;
     for (int f = F[minf].l[1]; f >= 0; f = F[f].l[1]) {
-      const double sqd = F[f].d * F[f].d;
+      const unsigned long long sqd = F[f].sqd;
       if (sqd < mind) {
         minf = f;
         mind = sqd;

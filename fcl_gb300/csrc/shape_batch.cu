@@ -113,20 +113,60 @@ __global__ void __launch_bounds__(128) k_shape_epa(ShapeLaunch L) {
   }
 }
 
-__global__ void __launch_bounds__(128) k_shape_distance(ShapeLaunch L) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < L.n; t += stride) {
-    const long long q = L.order[t];
-    if (L.hit[q]) continue;
-    PairOut o;
-    shape_pair_query(L.shapes[__ldg(L.ia + q)], L.shapes[__ldg(L.ib + q)], L.verts, L.tf1 + 12 * q, L.tf2 + 12 * q, o,
-                     PAIR_DISTANCE);
-    L.dist[q] = o.dist;
-    store3(L.p1 + 3 * q, o.p1);
-    store3(L.p2 + 3 * q, o.p2);
-    // the distance GJK's status replaces the intersect's, as in fcl::collide then
-    // fcl::distance on one solver; closed-form distances leave it
-    if (L.status && o.gstat != -1) L.status[2 * q] = o.gstat;
+// Distance for the separated pairs, in bucket order, with lane refill: a lane whose GJK
+// ends writes its result and takes the next pair at once (a closed-form pair is done
+// in the same pass), so the lanes of a warp stay in the GJK iteration together instead
+// of idling until the warp's slowest pair ends.  The distance GJK's status replaces the
+// intersect's, as fcl::collide then fcl::distance on one solver; closed-form distances
+// leave it.
+__global__ void __launch_bounds__(128) k_shape_distance(ShapeLaunch L, unsigned long long* next) {
+  SimplexVert V[4];
+  GjkState g;
+  M3<double> R1;
+  D3v t1;
+  long long q = -1;
+  bool has = false, exhausted = false;
+  for (;;) {
+    if (!has && !exhausted) {
+      const long long t = (long long)atomicAdd(next, 1ull);
+      if (t >= L.n) {
+        exhausted = true;
+      } else {
+        q = L.order[t];
+        if (!L.hit[q]) {
+          const DevShape sa = L.shapes[__ldg(L.ia + q)], sb = L.shapes[__ldg(L.ib + q)];
+          if (distance_uses_gjk(sa.type, sb.type)) {
+            ShapeRef A, B;
+            A.s = sa;
+            B.s = sb;
+            A.verts = B.verts = L.verts;
+            M3<double> R2;
+            D3v t2;
+            load_tf(L.tf1 + 12 * q, R1, t1);
+            load_tf(L.tf2 + 12 * q, R2, t2);
+            gjk_distance_begin(A, R1, t1, B, R2, t2, V, g);
+            has = true;
+          } else {
+            PairOut o;
+            shape_pair_query(sa, sb, L.verts, L.tf1 + 12 * q, L.tf2 + 12 * q, o, PAIR_DISTANCE);
+            L.dist[q] = o.dist;
+            store3(L.p1 + 3 * q, o.p1);
+            store3(L.p2 + 3 * q, o.p2);
+          }
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, exhausted && !has)) break;
+    if (has && g.step()) {
+      PairOut o;
+      o.p1 = o.p2 = v3(0.0, 0.0, 0.0);
+      gjk_distance_end(g, R1, t1, o);
+      L.dist[q] = o.dist;
+      store3(L.p1 + 3 * q, o.p1);
+      store3(L.p2 + 3 * q, o.p2);
+      if (L.status) L.status[2 * q] = o.gstat;
+      has = false;
+    }
   }
 }
 
@@ -152,7 +192,9 @@ cudaError_t launch_shape_batch(const ShapeLaunch& L, unsigned* bins, cudaStream_
   k_shape_scatter<<<grid_of((const void*)k_shape_scatter, 256, L.n), 256, 0, s>>>(L, bins);
   k_shape_intersect<<<grid_of((const void*)k_shape_intersect, block, L.n), block, 0, s>>>(L);
   k_shape_epa<<<grid_of((const void*)k_shape_epa, block, L.n), block, 0, s>>>(L);
-  k_shape_distance<<<grid_of((const void*)k_shape_distance, block, L.n), block, 0, s>>>(L);
+  unsigned long long* next = L.epa_count + 1;
+  if ((e = cudaMemsetAsync(next, 0, sizeof(unsigned long long), s))) return e;
+  k_shape_distance<<<grid_of((const void*)k_shape_distance, block, L.n), block, 0, s>>>(L, next);
   g_kernel_launches += 6;
   return cudaGetLastError();
 }

@@ -367,14 +367,19 @@ FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t
   o.hit = 1;
 }
 
-FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
-                             const M3<double>& R2, const D3v& t2, SimplexVert* V, PairOut& o) {
+// GJKSolver_indep::shapeDistance through GJK (gjk_solver_indep-inl.h:593-645): the
+// solver's setup, then (after the GJK loop) the witness points and the distance
+FCLG_HD void gjk_distance_begin(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
+                                const M3<double>& R2, const D3v& t2, SimplexVert* V, GjkState& g) {
   const D3v guess = v3(1.0, 0.0, 0.0);
-  GjkState g;
   make_minkowski(A, R1, t1, B, R2, t2, g.shape);
   g.V = V;
   g.tolerance = kGjkTol;
-  const int gs = g.evaluate(d3neg(guess), 128);
+  g.begin(d3neg(guess), 128);
+}
+FCLG_HD void gjk_distance_end(GjkState& g, const M3<double>& R1, const D3v& t1, PairOut& o) {
+  const SimplexVert* V = g.V;
+  const int gs = g.finish();
   o.gstat = gs;
   if (gs == GJK_VALID) {
     D3v w0 = v3(0.0, 0.0, 0.0), w1 = v3(0.0, 0.0, 0.0);
@@ -390,6 +395,23 @@ FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1
   } else {
     o.dist = -1;
   }
+}
+FCLG_HD void gjk_distance(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
+                             const M3<double>& R2, const D3v& t2, SimplexVert* V, PairOut& o) {
+  GjkState g;
+  gjk_distance_begin(A, R1, t1, B, R2, t2, V, g);
+  while (!g.step()) {
+  }
+  gjk_distance_end(g, R1, t1, o);
+}
+
+// true when fcl::distance on this ordered type pair runs GJK (no closed form is
+// registered for it in GJKSolver_indep, gjk_solver_indep-inl.h:686-708)
+FCLG_HD bool distance_uses_gjk(int a, int b) {
+  if (a == SHAPE_SPHERE && (b == SHAPE_SPHERE || b == SHAPE_CAPSULE || b == SHAPE_BOX || b == SHAPE_CYLINDER))
+    return false;
+  if (b == SHAPE_SPHERE && (a == SHAPE_CAPSULE || a == SHAPE_BOX || a == SHAPE_CYLINDER)) return false;
+  return !(a == SHAPE_CAPSULE && b == SHAPE_CAPSULE);
 }
 
 // One pair: shapes a, b (with the vertex pool) at tf1, tf2 (3x4 row-major).

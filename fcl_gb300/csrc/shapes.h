@@ -24,7 +24,7 @@ struct ShapeLaunch {
   int32_t* status;
   int32_t* order;                   // n: pair indices bucketed by (type, type)
   int32_t* epa_list;                // n: pairs whose GJK ended Inside
-  unsigned long long* epa_count;
+  unsigned long long* epa_count;     // followed by one more counter (distance work)
 };
 
 // Whole batch in stages (bucket, intersect, EPA, distance); bins: 64 unsigned scratch.
