@@ -190,7 +190,7 @@ def run_serving(args):
     srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=args.serve_step)
     SV.run_burst(srv, reqs[:16])  # warm-up
     burst = SV.run_burst(srv, reqs[16:272])
-    rate = args.serve_rate if args.serve_rate > 0 else 0.7 * burst["requests_per_s"]
+    rate = args.serve_rate if args.serve_rate > 0 else 0.5 * burst["requests_per_s"]
     with ClockSampler(0) as cs:
         load = SV.run_poisson(srv, reqs[272:], rate, seed=6)
     st = srv.stats()
@@ -250,6 +250,9 @@ def run_secondary(args, meshes, stream, flush):
     dev = flush.device
     if args.only == "shapes":
         return {"shapes": _run_shapes(args, stream, flush)}
+    if meshes is None:  # the distance section alone: the mesh set of the C1/C2 workloads
+        w1 = _workload(args, 0)
+        meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
     w2 = W.config2(total_poses=int(1_000_000 * args.scale), n_pairs=args.pairs, tri_hi=args.tri_hi)
     tf2 = torch.from_numpy(w2.tf2).to(dev)
     pq = torch.from_numpy(w2.pair).to(dev)
@@ -283,6 +286,8 @@ def run_secondary(args, meshes, stream, flush):
         dt = _time_cpu_distance(W.subsample(w2, k, seed=3), threads)
         out["distance"]["cpu_baseline"] = {"value": k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
                                            "sample": f"{k} queries drawn uniformly from the {w2.n}-query workload"}
+    if args.only == "distance":
+        return out
     out["shapes"] = _run_shapes(args, stream, flush)
     return out
 
@@ -595,12 +600,12 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "shapes", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests in the Poisson run")
-    ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.7 x measured capacity)")
+    ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.5 x measured capacity)")
     ap.add_argument("--serve-step", type=int, default=4096, help="waypoints per loop step")
     ap.add_argument("--serve-cpu-sample", type=int, default=64, help="requests timed on the CPU baseline")
     args = ap.parse_args()

@@ -698,7 +698,7 @@ def set_collide_tuning(budget: int, leaf_batch_steps: int, variant: int = 0) -> 
 
 
 def autotune_collide(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, sample=65536,
-                     budgets=(1024, 4096, 16384), steps=(4, 8, 16, 32), variants=(0, 1), repeats=2, seed=0):
+                     budgets=(256, 512, 1024, 2048), steps=(2, 4, 8), variants=(0, 1), repeats=2, seed=0):
     """Picks the collide rounds' knobs (BV-test budget per item, DFS steps between warp
     leaf batches, register variant) for a workload: times the FP32 form on a uniform
     sample of its queries (torch CUDA tensors) for every combination and keeps the

@@ -145,9 +145,10 @@ SplitScratch g_split;
 // Tuning knobs of the FP32 collide rounds (set by fclgpu_set_collide_tuning, picked by
 // the autotuner in fcl_gb300/api.py): BV tests per item per round, DFS steps per lane
 // between two warp leaf batches.
-int64_t g_default_budget = 4096;
-int32_t g_wb_steps = 8;
-int32_t g_wb_variant = 0;
+// defaults: the autotuner's pick on the 64-pair exhaustive-contact workload
+int64_t g_default_budget = 1024;
+int32_t g_wb_steps = 4;
+int32_t g_wb_variant = 1;
 
 int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
                  const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
