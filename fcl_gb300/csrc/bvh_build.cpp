@@ -66,6 +66,7 @@ class Builder {
       RssD& rs = out.rss[tk.id];
       uint32_t* span = prim_.data() + tk.first;
       fit(span, tk.count, nd, rs);
+      for (int k = 0; k < 9; ++k) rs.axis[k] = nd.axis[k];  // BVFitter<OBBRSS>: rss.axis = obb.axis
       if (tk.count == 1) {
         nd.child = -((int)span[0] + 1);
         continue;
@@ -375,7 +376,7 @@ void pack_fp32(const double* verts, const int32_t* tris, int64_t nt, const HostB
   const size_t nn = bvh.nodes.size();
   pk.nodes32.resize(16 * nn);
   pk.size64.resize(nn);
-  pk.rss32.resize(8 * nn);
+  pk.rss32.resize(20 * nn);
   pk.cmax = 0.0;
   pk.rmax = 0.0;
   for (size_t i = 0; i < nn; ++i) {
@@ -393,7 +394,7 @@ void pack_fp32(const double* verts, const int32_t* tris, int64_t nt, const HostB
     o[14] = f32(n.ext[2]);
     std::memcpy(&o[15], &n.child, 4);
     pk.size64[i] = (n.ext[0] * n.ext[0] + n.ext[1] * n.ext[1]) + n.ext[2] * n.ext[2];
-    float* q = &pk.rss32[8 * i];
+    float* q = &pk.rss32[20 * i];
     q[0] = f32(r.To[0]);
     q[1] = f32(r.To[1]);
     q[2] = f32(r.To[2]);
@@ -402,6 +403,12 @@ void pack_fp32(const double* verts, const int32_t* tris, int64_t nt, const HostB
     q[5] = f32(r.l[1]);
     q[6] = 0.f;
     q[7] = 0.f;
+    for (int k = 0; k < 3; ++k) {
+      q[8 + 4 * k + 0] = f32(r.axis[0 + k]);
+      q[8 + 4 * k + 1] = f32(r.axis[3 + k]);
+      q[8 + 4 * k + 2] = f32(r.axis[6 + k]);
+      q[8 + 4 * k + 3] = 0.f;
+    }
     pk.cmax = std::max(pk.cmax, std::sqrt((n.To[0] * n.To[0] + n.To[1] * n.To[1]) + n.To[2] * n.To[2]));
     pk.rmax = std::max(pk.rmax, std::sqrt((r.To[0] * r.To[0] + r.To[1] * r.To[1]) + r.To[2] * r.To[2]));
   }

@@ -17,7 +17,7 @@ struct HostBVH {
 struct PackedF32 {
   std::vector<float> nodes32;  // 16 floats per node
   std::vector<double> size64;  // per node
-  std::vector<float> rss32;    // 8 floats per node
+  std::vector<float> rss32;    // 20 floats per node
   std::vector<float> tri32;    // 12 floats per triangle
   double cmax = 0.0;
   double rmax = 0.0;

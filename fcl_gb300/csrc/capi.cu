@@ -303,6 +303,7 @@ const char* fclgpu_status_string(int status) {
     case FCLGPU_ERR_NOT_INITIALIZED: return "not initialized";
     case FCLGPU_ERR_UNSUPPORTED: return "unsupported";
     case FCLGPU_ERR_PENDING: return "request not finished";
+    case FCLGPU_ERR_INCORRECT_DATA: return "incorrect data";
     default: return "unknown status";
   }
 }
@@ -433,13 +434,42 @@ int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int
     }
     m->aabb_radius = std::sqrt(r);
   }
+  {
+    // internal nodes by depth, for the level-by-level refit
+    std::vector<int32_t> depth(nn, 0);
+    int maxd = 0;
+    for (size_t b = 0; b < nn; ++b) {  // children always follow their parent
+      const int c = bvh.nodes[b].child;
+      if (c >= 0) {
+        depth[c] = depth[c + 1] = depth[b] + 1;
+        maxd = std::max(maxd, depth[b]);
+      }
+    }
+    std::vector<int64_t> off(maxd + 2, 0);
+    for (size_t b = 0; b < nn; ++b)
+      if (bvh.nodes[b].child >= 0) ++off[depth[b] + 1];
+    for (int l = 0; l <= maxd; ++l) off[l + 1] += off[l];
+    std::vector<int32_t> ids(std::max<int64_t>(off[maxd + 1], 1));
+    std::vector<int64_t> fill(off.begin(), off.end() - 1);
+    for (size_t b = 0; b < nn; ++b)
+      if (bvh.nodes[b].child >= 0) ids[fill[depth[b]]++] = (int32_t)b;
+    void* p_lv = nullptr;
+    e = alloc(&p_lv, sizeof(int32_t) * ids.size(), ids.data());
+    if (e != cudaSuccess) {
+      for (void* p : m->allocations) cudaFree(p);
+      delete m;
+      return cuda_fail(e, "mesh upload");
+    }
+    m->levels = (int32_t*)p_lv;
+    m->level_off = off;
+  }
   m->info.num_vertices = nv;
   m->info.num_tris = nt;
   m->info.num_nodes = (int64_t)nn;
   m->info.max_depth = bvh.max_depth;
   m->info.reserved = 0;
   m->info.max_abs_coord = vmax;
-  m->info.device_bytes = (int64_t)(nn * (sizeof(NodeD) + sizeof(RssD) + 64 + 8 + 32) + nv * 24 + nt * (12 + 48));
+  m->info.device_bytes = (int64_t)(nn * (sizeof(NodeD) + sizeof(RssD) + 64 + 8 + 80) + nv * 24 + nt * (12 + 48));
   *out = m;
   return FCLGPU_OK;
 }
@@ -470,7 +500,7 @@ int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t* first_chil
     for (int k = 0; k < 9; ++k) o[k] = nd[i].axis[k];
     for (int k = 0; k < 3; ++k) o[9 + k] = nd[i].To[k];
     for (int k = 0; k < 3; ++k) o[12 + k] = nd[i].ext[k];
-    for (int k = 0; k < 9; ++k) o[15 + k] = nd[i].axis[k];
+    for (int k = 0; k < 9; ++k) o[15 + k] = rs[i].axis[k];
     for (int k = 0; k < 3; ++k) o[24 + k] = rs[i].To[k];
     o[27] = rs[i].l[0];
     o[28] = rs[i].l[1];

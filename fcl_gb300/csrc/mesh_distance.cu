@@ -76,8 +76,8 @@ __device__ __noinline__ double leaf_distance64(const DevMesh& A, const DevMesh& 
 __device__ __forceinline__ double rss_distance64(const DevMesh& A, const DevMesh& B, int b1, int b2,
                                                  const M3<double>& R, const V3<double>& T) {
   M3<double> A1, A2;
-  const double* x1 = A.nodes64[b1].axis;
-  const double* x2 = B.nodes64[b2].axis;
+  const double* x1 = A.rss64[b1].axis;
+  const double* x2 = B.rss64[b2].axis;
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
     A1.m[i] = __ldg(x1 + i);
@@ -229,14 +229,12 @@ __device__ __forceinline__ float tri_distance_f32(const QueryF32& q, const float
 
 __device__ __forceinline__ float rss_distance_f32(const QueryF32& q, const DevMesh& A, const DevMesh& B, int b1,
                                                   int b2) {
-  const float4* na = reinterpret_cast<const float4*>(A.nodes32) + 4 * (long long)b1;
-  const float4* nb = reinterpret_cast<const float4*>(B.nodes32) + 4 * (long long)b2;
-  const float4* ra = reinterpret_cast<const float4*>(A.rss32) + 2 * (long long)b1;
-  const float4* rb = reinterpret_cast<const float4*>(B.rss32) + 2 * (long long)b2;
+  const float4* ra = reinterpret_cast<const float4*>(A.rss32) + 5 * (long long)b1;
+  const float4* rb = reinterpret_cast<const float4*>(B.rss32) + 5 * (long long)b2;
   M3<float> A1, A2, R0;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float4 ca = __ldg(na + k), cb = __ldg(nb + k);
+    const float4 ca = __ldg(ra + 2 + k), cb = __ldg(rb + 2 + k);
     A1(0, k) = ca.x; A1(1, k) = ca.y; A1(2, k) = ca.z;
     A2(0, k) = cb.x; A2(1, k) = cb.y; A2(2, k) = cb.z;
   }

@@ -15,4 +15,11 @@ struct fclgpu_mesh_s {
   double aabb_center[3];
   double aabb_radius;
   double first_vertex[3];
+  // bottom-up refit (fclgpu_mesh_update): internal node ids grouped by depth (level l
+  // = levels[level_off[l] .. level_off[l+1]) on the device), the previous frame's
+  // vertices and the magnitude-bound scratch (allocated at the first update)
+  int32_t* levels = nullptr;
+  std::vector<int64_t> level_off;
+  void* prev_verts = nullptr;
+  void* bounds = nullptr;
 };

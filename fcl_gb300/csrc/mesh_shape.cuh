@@ -185,13 +185,15 @@ FCLG_HD void jacobi3(const double C[3][3], double evals[3], double evecs[3][3]) 
   }
 }
 
-// computeBV<OBBRSS>(shape, tf): OBB and RSS fitted to the world bound vertices
-FCLG_HD void shape_obbrss(const DevShape& s, const double* pool, const M3<double>& R, const D3v& t, ShapeBV& bv) {
-  const int n = bound_vertex_count(s);
-  auto world = [&](int i) { return mulv(R, bound_vertex_local(s, pool, i)) + t; };
+// ---- point-set fits (math/geometry-inl.h, math/bv/utility-inl.h) ----------------------
+// pts(i) returns point i (FP64); every function reads the points in index order.
+
+// getCovariance, point branch (math/geometry-inl.h:1383-1421)
+template <class Pts>
+FCLG_HD void covariance_of(Pts pts, int n, double C[3][3]) {
   double s1x = 0, s1y = 0, s1z = 0, sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
   for (int i = 0; i < n; ++i) {
-    const D3v p = world(i);
+    const D3v p = pts(i);
     s1x += p.x;
     s1y += p.y;
     s1z += p.z;
@@ -202,7 +204,6 @@ FCLG_HD void shape_obbrss(const DevShape& s, const double* pool, const M3<double
     sxz += (p.x * p.z);
     syz += (p.y * p.z);
   }
-  double C[3][3];
   C[0][0] = sxx - s1x * s1x / n;
   C[1][1] = syy - s1y * s1y / n;
   C[2][2] = szz - s1z * s1z / n;
@@ -212,54 +213,60 @@ FCLG_HD void shape_obbrss(const DevShape& s, const double* pool, const M3<double
   C[1][0] = C[0][1];
   C[2][0] = C[0][2];
   C[2][1] = C[1][2];
-  double evals[3], evecs[3][3];
-  jacobi3(C, evals, evecs);
-  // axisFromEigen (math/geometry-inl.h:294-318)
-  int lo, mid, hi;
-  if (evals[0] > evals[1]) {
+}
+
+// the (min, mid, max) order of three eigenvalues used by axisFromEigen and the merges
+FCLG_HD void order3(const double e[3], int& lo, int& mid, int& hi) {
+  if (e[0] > e[1]) {
     hi = 0;
     lo = 1;
   } else {
     lo = 0;
     hi = 1;
   }
-  if (evals[2] < evals[lo]) {
+  if (e[2] < e[lo]) {
     mid = lo;
     lo = 2;
-  } else if (evals[2] > evals[hi]) {
+  } else if (e[2] > e[hi]) {
     mid = hi;
     hi = 2;
   } else {
     mid = 2;
   }
-  const D3v a0 = v3(evecs[hi][0], evecs[hi][1], evecs[hi][2]);
-  const D3v a1 = v3(evecs[mid][0], evecs[mid][1], evecs[mid][2]);
-  const D3v a2 = cross(a0, a1);
-  const D3v ax[3] = {a0, a1, a2};
-  bv.obb.axis[0] = a0.x; bv.obb.axis[1] = a1.x; bv.obb.axis[2] = a2.x;
-  bv.obb.axis[3] = a0.y; bv.obb.axis[4] = a1.y; bv.obb.axis[5] = a2.y;
-  bv.obb.axis[6] = a0.z; bv.obb.axis[7] = a1.z; bv.obb.axis[8] = a2.z;
-  auto proj = [&](int i) {
-    const D3v p = world(i);
-    return v3(dot(ax[0], p), dot(ax[1], p), dot(ax[2], p));
-  };
-  // getExtentAndCenter_pointcloud
+}
+
+FCLG_HD void set_axis9(double a9[9], const D3v ax[3]) {
+  a9[0] = ax[0].x; a9[1] = ax[1].x; a9[2] = ax[2].x;
+  a9[3] = ax[0].y; a9[4] = ax[1].y; a9[5] = ax[2].y;
+  a9[6] = ax[0].z; a9[7] = ax[1].z; a9[8] = ax[2].z;
+}
+
+// getExtentAndCenter_pointcloud (math/geometry-inl.h:229-287)
+template <class Pts>
+FCLG_HD void extent_center_of(Pts pts, int n, const D3v ax[3], double To[3], double ext[3]) {
   double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
   for (int i = 0; i < n; ++i) {
-    const D3v q = proj(i);
-    const double c3[3] = {q.x, q.y, q.z};
+    const D3v p = pts(i);
+    const double c3[3] = {dot(ax[0], p), dot(ax[1], p), dot(ax[2], p)};
     for (int j = 0; j < 3; ++j) {
       if (c3[j] > mx[j]) mx[j] = c3[j];
       if (c3[j] < mn[j]) mn[j] = c3[j];
     }
   }
   const double o0 = (mx[0] + mn[0]) / 2, o1 = (mx[1] + mn[1]) / 2, o2 = (mx[2] + mn[2]) / 2;
-  for (int r = 0; r < 3; ++r)
-    bv.obb.To[r] = (bv.obb.axis[3 * r] * o0 + bv.obb.axis[3 * r + 1] * o1) + bv.obb.axis[3 * r + 2] * o2;
-  for (int k = 0; k < 3; ++k) bv.obb.ext[k] = (mx[k] - mn[k]) * 0.5;
-  bv.obb.child = 0;
-  bv.obb.pad = 0;
-  // getRadiusAndOriginAndRectangleSize over the projected points
+  const double a9[9] = {ax[0].x, ax[1].x, ax[2].x, ax[0].y, ax[1].y, ax[2].y, ax[0].z, ax[1].z, ax[2].z};
+  for (int r = 0; r < 3; ++r) To[r] = (a9[3 * r] * o0 + a9[3 * r + 1] * o1) + a9[3 * r + 2] * o2;
+  for (int k = 0; k < 3; ++k) ext[k] = (mx[k] - mn[k]) * 0.5;
+}
+
+// getRadiusAndOriginAndRectangleSize over the points projected onto ax
+// (math/geometry-inl.h:709-990, point branch)
+template <class Pts>
+FCLG_HD void rss_fit_of(Pts pts, int n, const D3v ax[3], double rTo[3], double rl[2], double& rr) {
+  auto proj = [&](int i) {
+    const D3v p = pts(i);
+    return v3(dot(ax[0], p), dot(ax[1], p), dot(ax[2], p));
+  };
   const D3v p0 = proj(0);
   double minz = p0.z, maxz = p0.z;
   for (int i = 1; i < n; ++i) {
@@ -382,12 +389,41 @@ FCLG_HD void shape_obbrss(const DevShape& s, const double* pool, const M3<double
   const double ox[3] = {ax[0].x * minx, ax[0].y * minx, ax[0].z * minx};
   const double oy[3] = {ax[1].x * miny, ax[1].y * miny, ax[1].z * miny};
   const double oz[3] = {ax[2].x * cz, ax[2].y * cz, ax[2].z * cz};
-  for (int k = 0; k < 3; ++k) bv.rTo[k] = (ox[k] + oy[k]) + oz[k];
-  bv.rl[0] = maxx - minx;
-  if (bv.rl[0] < 0) bv.rl[0] = 0;
-  bv.rl[1] = maxy - miny;
-  if (bv.rl[1] < 0) bv.rl[1] = 0;
-  bv.rr = r;
+  for (int k = 0; k < 3; ++k) rTo[k] = (ox[k] + oy[k]) + oz[k];
+  rl[0] = maxx - minx;
+  if (rl[0] < 0) rl[0] = 0;
+  rl[1] = maxy - miny;
+  if (rl[1] < 0) rl[1] = 0;
+  rr = r;
+}
+
+
+// fit<OBBRSS> of n >= 4 points: OBB fitn and RSS fitn share the covariance, the eigen
+// decomposition and the axes (math/bv/utility-inl.h:133-145, 247-259)
+template <class Pts>
+FCLG_HD void fit_points_bv(Pts pts, int n, NodeD& obb, double rTo[3], double rl[2], double& rr) {
+  double C[3][3];
+  covariance_of(pts, n, C);
+  double evals[3], evecs[3][3];
+  jacobi3(C, evals, evecs);
+  // axisFromEigen (math/geometry-inl.h:294-318)
+  int lo, mid, hi;
+  order3(evals, lo, mid, hi);
+  const D3v a0 = v3(evecs[hi][0], evecs[hi][1], evecs[hi][2]);
+  const D3v a1 = v3(evecs[mid][0], evecs[mid][1], evecs[mid][2]);
+  const D3v ax[3] = {a0, a1, cross(a0, a1)};
+  set_axis9(obb.axis, ax);
+  extent_center_of(pts, n, ax, obb.To, obb.ext);
+  obb.child = 0;
+  obb.pad = 0;
+  rss_fit_of(pts, n, ax, rTo, rl, rr);
+}
+
+// computeBV<OBBRSS>(shape, tf): OBB and RSS fitted to the world bound vertices
+FCLG_HD void shape_obbrss(const DevShape& s, const double* pool, const M3<double>& R, const D3v& t, ShapeBV& bv) {
+  const int n = bound_vertex_count(s);
+  auto world = [&](int i) { return mulv(R, bound_vertex_local(s, pool, i)) + t; };
+  fit_points_bv(world, n, bv.obb, bv.rTo, bv.rl, bv.rr);
 }
 
 // ------------------------------------------------------------- sphere-triangle ----
@@ -755,10 +791,9 @@ FCLG_HD int mesh_shape_collect_distance(const DevMesh& m, const M3<double>& Rm, 
     return shape_point_ub(A, Rs, ts, c);
   };
   auto bvd = [&](int b) {
-    const NodeD nd = m.nodes64[b];
     const RssD& rs = m.rss64[b];
     M3<double> A2;
-    for (int i = 0; i < 9; ++i) A2.m[i] = nd.axis[i];
+    for (int i = 0; i < 9; ++i) A2.m[i] = rs.axis[i];
     return rss_distance<double>(Rm, tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
   };
   double ub = tri_ub(0);
@@ -865,10 +900,9 @@ FCLG_HD void mesh_shape_distance(const DevMesh& m, const M3<double>& Rm, const D
   };
   auto bvd = [&](int b) {
     ++o.nbv;
-    const NodeD nd = m.nodes64[b];
     const RssD& rs = m.rss64[b];
     M3<double> A2;
-    for (int i = 0; i < 9; ++i) A2.m[i] = nd.axis[i];
+    for (int i = 0; i < 9; ++i) A2.m[i] = rs.axis[i];
     return rss_distance<double>(Rm, tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
   };
   leaf(0);  // preprocess seeds with the first triangle

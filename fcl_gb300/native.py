@@ -107,6 +107,8 @@ class MeshShapeResult(C.Structure):
 GEOM_SHAPE = 0
 GEOM_MESH = 1
 FCLGPU_ERR_PENDING = -10
+FCLGPU_ERR_INCORRECT_DATA = -11
+FCLGPU_ERR_UNSUPPORTED = -9
 
 _lib = None
 
@@ -120,6 +122,8 @@ _SIGS = {
     "fclgpu_mesh_destroy": (C.c_int, [_VP]),
     "fclgpu_mesh_get_info": (C.c_int, [_VP, C.POINTER(MeshInfo)]),
     "fclgpu_mesh_get_nodes": (C.c_int, [_VP, _VP, _VP]),
+    "fclgpu_mesh_update": (C.c_int, [_VP, _VP, C.c_int64, _VP]),
+    "fclgpu_mesh_update_device": (C.c_int, [_VP, _VP, C.c_int64, _VP]),
     "fclgpu_collide_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                               C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
     "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,

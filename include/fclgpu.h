@@ -48,7 +48,8 @@ enum {
   FCLGPU_ERR_DEVICE_STATUS = -7,   /* a kernel reported an internal error word */
   FCLGPU_ERR_NOT_INITIALIZED = -8,
   FCLGPU_ERR_UNSUPPORTED = -9,
-  FCLGPU_ERR_PENDING = -10          /* a served request has not finished yet */
+  FCLGPU_ERR_PENDING = -10,         /* a served request has not finished yet */
+  FCLGPU_ERR_INCORRECT_DATA = -11   /* BVH_ERR_INCORRECT_DATA (BVH_internal.h:61-72) */
 };
 
 FCLGPU_API const char* fclgpu_status_string(int status);
@@ -89,6 +90,18 @@ FCLGPU_API int fclgpu_mesh_get_info(fclgpu_mesh mesh, fclgpu_mesh_info* info);
  * obb.To 3, obb.extent 3, rss.axis 9, rss.To 3, rss.l 2, rss.r 1) and first_child
  * (<0: leaf, primitive = -(first_child+1)), in FCL's node order. */
 FCLGPU_API int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t* first_child);
+
+/* Moves the mesh's vertices and refits its BVH on the device: replaces
+ * BVHModel::beginUpdateModel + updateVertex (all vertices, in order) +
+ * endUpdateModel(refit = true, bottomup = true) (geometry/bvh/BVH_model-inl.h:624-727,
+ * 961-1027).  The tree keeps its shape; each leaf is refitted to its triangle in the
+ * previous and the new frame, each internal node is the OBBRSS sum of its children.
+ * nv must equal the mesh's vertex count (else FCLGPU_ERR_INCORRECT_DATA, as FCL's
+ * endUpdateModel).  The local AABB is not recomputed (FCL does not either).  verts: host
+ * (fclgpu_mesh_update) or device (fclgpu_mesh_update_device) pointer, 3 doubles per
+ * vertex.  Synchronises the stream. */
+FCLGPU_API int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
+FCLGPU_API int fclgpu_mesh_update_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
 
 /* ---- batched queries ----------------------------------------------------------------
  * A batch is n queries over a table of mesh pairs.  Query i tests meshes

@@ -46,6 +46,15 @@ struct Mesh {
 // --- BVH build (geometry/bvh/BVH_model-inl.h:450-517, 833-938) -------------------
 void build_bvh(Mesh& m);
 
+// --- point-set fits and bottom-up refit (oracle_refit.cpp) ---------------------------
+void covariance_points(const V3* ps, int n, M3& M);
+void extent_center_points(const V3* ps, int n, const M3& axis, V3& center, V3& extent, std::vector<V3>* P);
+void fit_points_obbrss(const V3* ps, int n, OBB& obb, RSS& rss);  // fit<OBBRSS>, n >= 4
+OBB obb_merge(const OBB& a, const OBB& b);                           // OBB::operator+
+RSS rss_merge(const RSS& self, const RSS& other);                    // RSS::operator+
+// beginUpdateModel, updateVertex x nv, endUpdateModel(refit = true, bottomup = true)
+void update_refit_bottomup(Mesh& m, const std::vector<V3>& new_verts);
+
 // --- point-set RSS fit for three points (math/bv/utility-inl.h:208-230) ----------
 void rss_fit3(const V3 ps[3], RSS& bv);
 

@@ -127,53 +127,7 @@ std::vector<V3> bound_vertices(const Shape& s, const Tf& tf) {
 
 void shape_obbrss(const Shape& s, const Tf& tf, OBB& obb, RSS& rss) {
   const std::vector<V3> ps = bound_vertices(s, tf);
-  const int n = (int)ps.size();
-  // getCovariance, point branch (math/geometry-inl.h:1383-1421)
-  V3 S1 = mk(0, 0, 0);
-  double S2[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-  for (int i = 0; i < n; ++i) {
-    const V3& p = ps[i];
-    S1 = add(S1, p);
-    S2[0][0] += (p[0] * p[0]);
-    S2[1][1] += (p[1] * p[1]);
-    S2[2][2] += (p[2] * p[2]);
-    S2[0][1] += (p[0] * p[1]);
-    S2[0][2] += (p[0] * p[2]);
-    S2[1][2] += (p[1] * p[2]);
-  }
-  M3 M;
-  M(0, 0) = S2[0][0] - S1[0] * S1[0] / n;
-  M(1, 1) = S2[1][1] - S1[1] * S1[1] / n;
-  M(2, 2) = S2[2][2] - S1[2] * S1[2] / n;
-  M(0, 1) = S2[0][1] - S1[0] * S1[1] / n;
-  M(1, 2) = S2[1][2] - S1[1] * S1[2] / n;
-  M(0, 2) = S2[0][2] - S1[0] * S1[2] / n;
-  M(1, 0) = M(0, 1);
-  M(2, 0) = M(0, 2);
-  M(2, 1) = M(1, 2);
-  // OBB fitn and RSS fitn each compute the same covariance and eigen decomposition
-  M3 E = ident();
-  V3 sv = mk(0, 0, 0);
-  eigen_old(M, sv, E);
-  axis_from_eigen(E, sv, obb.axis);
-  rss.axis = obb.axis;
-  // getExtentAndCenter_pointcloud (math/geometry-inl.h:229-287)
-  const double real_max = std::numeric_limits<double>::max();
-  V3 mn = mk(real_max, real_max, real_max), mx = mk(-real_max, -real_max, -real_max);
-  std::vector<V3> P(n);
-  for (int i = 0; i < n; ++i) {
-    const V3 proj = mk(dot(col(obb.axis, 0), ps[i]), dot(col(obb.axis, 1), ps[i]), dot(col(obb.axis, 2), ps[i]));
-    P[i] = proj;
-    for (int j = 0; j < 3; ++j) {
-      if (proj[j] > mx[j]) mx[j] = proj[j];
-      if (proj[j] < mn[j]) mn[j] = proj[j];
-    }
-  }
-  const V3 o = mk((mx[0] + mn[0]) / 2, (mx[1] + mn[1]) / 2, (mx[2] + mn[2]) / 2);
-  obb.To = mulv(obb.axis, o);
-  obb.extent = mk((mx[0] - mn[0]) * 0.5, (mx[1] - mn[1]) * 0.5, (mx[2] - mn[2]) * 0.5);
-  // getRadiusAndOriginAndRectangleSize, point branch (math/geometry-inl.h:709-990)
-  rss_from_projected(P, rss.axis, rss.To, rss.l, rss.r);
+  fit_points_obbrss(ps.data(), (int)ps.size(), obb, rss);
 }
 
 bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3) {

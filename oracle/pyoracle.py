@@ -38,6 +38,7 @@ def lib():
         L.orc_mesh_free.argtypes = [C.c_void_p]
         L.orc_mesh_num_nodes.argtypes = [C.c_void_p]
         L.orc_mesh_get_nodes.argtypes = [C.c_void_p, _dp, _ip]
+        L.orc_mesh_update.argtypes = [C.c_void_p, _dp]
         L.orc_collide_batch.restype = C.c_int64
         L.orc_collide_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64, C.c_int,
                                         _i64p, _i64p, _i64p, _ip, C.c_int64]
@@ -88,6 +89,14 @@ class Mesh:
         if getattr(self, "h", None) and _lib is not None:
             _lib.orc_mesh_free(self.h)
             self.h = None
+
+    def update(self, verts: np.ndarray) -> None:
+        """beginUpdateModel / updateVertex / endUpdateModel() with the default
+        bottom-up refit: the previous frame is the current vertices."""
+        v = np.ascontiguousarray(verts, dtype=np.float64)
+        assert v.shape == self.verts.shape
+        lib().orc_mesh_update(self.h, _d(v))
+        self.verts = v
 
     def nodes(self):
         n = lib().orc_mesh_num_nodes(self.h)

@@ -29,6 +29,17 @@ def build(v, t):
     return out, fc, md.value
 
 
+def refit(v0, t, frames):
+    """Device refit math run on the host: build from v0, then refit to each frame."""
+    v0 = np.ascontiguousarray(v0, np.float64); t = np.ascontiguousarray(t, np.int32)
+    vs = np.ascontiguousarray(np.stack(frames), np.float64)
+    nn = 2 * t.shape[0] - 1
+    out = np.empty((nn, 30)); fc = np.empty(nn, np.int32)
+    lib().emu_refit(_p(v0), C.c_int64(v0.shape[0]), _p(t), C.c_int64(t.shape[0]), _p(vs), C.c_int(len(frames)),
+                    _p(out), _p(fc))
+    return out, fc
+
+
 def collide(prec, a, b, tf2, maxc, tf1=None):
     n = tf2.shape[0]
     tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)

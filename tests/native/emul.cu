@@ -7,6 +7,7 @@
 
 #include "bvh_build.h"
 #include "collide_traverse.cuh"
+#include "refit.cuh"
 #include "shape_pair.cuh"
 
 using namespace fclgpu;
@@ -159,6 +160,59 @@ int64_t emu_collide_split(int prec, const double* v1, int64_t nv1, const int32_t
   return tot;
 }
 
+// Host run of the device refit math (refit.cuh): build from v0, then the bottom-up
+// refit to each of the k frames in vs (k * nv * 3 doubles) in turn; nodes30 as emu_build.
+void emu_refit(const double* v0, int64_t nv, const int32_t* t, int64_t nt, const double* vs, int k, double* nodes30,
+               int32_t* fc) {
+  HostMesh m;
+  make_mesh(v0, nv, t, nt, m);
+  std::vector<double> prev;
+  const int nn = (int)m.bvh.nodes.size();
+  for (int f = 0; f < k; ++f) {
+    prev = m.verts;
+    m.verts.assign(vs + 3 * nv * f, vs + 3 * nv * (f + 1));
+    for (int b = nn - 1; b >= 0; --b) {  // children follow their parent: reverse order is bottom up
+      NodeD& nd = m.bvh.nodes[b];
+      RssD& rs = m.bvh.rss[b];
+      const int c = nd.child;
+      if (c < 0) {
+        const int tt = -(c + 1);
+        D3v v[6];
+        for (int i = 0; i < 3; ++i) {
+          const double* p = prev.data() + 3 * m.tris[3 * tt + i];
+          const double* q = m.verts.data() + 3 * m.tris[3 * tt + i];
+          v[i] = v3(p[0], p[1], p[2]);
+          v[i + 3] = v3(q[0], q[1], q[2]);
+        }
+        auto pts = [&](int i) { return v[i]; };
+        fit_points_bv(pts, 6, nd, rs.To, rs.l, rs.r);
+        for (int j = 0; j < 9; ++j) rs.axis[j] = nd.axis[j];
+        nd.child = c;
+      } else {
+        NodeD mg = obb_merge(m.bvh.nodes[c], m.bvh.nodes[c + 1]);
+        mg.child = c;
+        const RssD rm = rss_merge(m.bvh.rss[c], m.bvh.rss[c + 1]);
+        nd = mg;
+        rs = rm;
+      }
+    }
+  }
+  for (int i = 0; i < nn; ++i) {
+    const NodeD& n = m.bvh.nodes[i];
+    const RssD& r = m.bvh.rss[i];
+    double* o = nodes30 + 30 * i;
+    for (int j = 0; j < 9; ++j) o[j] = n.axis[j];
+    for (int j = 0; j < 3; ++j) o[9 + j] = n.To[j];
+    for (int j = 0; j < 3; ++j) o[12 + j] = n.ext[j];
+    for (int j = 0; j < 9; ++j) o[15 + j] = r.axis[j];
+    for (int j = 0; j < 3; ++j) o[24 + j] = r.To[j];
+    o[27] = r.l[0];
+    o[28] = r.l[1];
+    o[29] = r.r;
+    fc[i] = n.child;
+  }
+}
+
 int emu_build(const double* v, int64_t nv, const int32_t* t, int64_t nt, double* nodes30, int32_t* fc,
               int32_t* max_depth) {
   HostMesh m;
@@ -170,7 +224,7 @@ int emu_build(const double* v, int64_t nv, const int32_t* t, int64_t nt, double*
     for (int k = 0; k < 9; ++k) o[k] = n.axis[k];
     for (int k = 0; k < 3; ++k) o[9 + k] = n.To[k];
     for (int k = 0; k < 3; ++k) o[12 + k] = n.ext[k];
-    for (int k = 0; k < 9; ++k) o[15 + k] = n.axis[k];
+    for (int k = 0; k < 9; ++k) o[15 + k] = r.axis[k];
     for (int k = 0; k < 3; ++k) o[24 + k] = r.To[k];
     o[27] = r.l[0];
     o[28] = r.l[1];

@@ -95,3 +95,21 @@ def test_shape_pairs_bit_exact_vs_oracle():
     assert np.array_equal(e["hit"], o["hit"]) and np.array_equal(e["status"], o["status"])
     for k in ("normal", "point", "depth", "dist", "p1", "p2"):
         assert np.array_equal(e[k], o[k]), k
+
+
+@pytest.mark.parametrize("freq,seed", [(2, 0), (6, 1), (12, 2)])
+def test_refit_bit_exact_vs_oracle(freq, seed):
+    """BVHModel update + endUpdateModel() bottom-up refit: the device refit math (leaf
+    fit over both frames, OBB/RSS sums) built for the host equals the oracle bit for bit,
+    over two successive updates."""
+    v, t = W.perturbed_ellipsoid(freq, (1.0, 0.7, 0.5), 0.01, seed)
+    rng = np.random.default_rng(seed + 100)
+    v1 = v + rng.normal(0, 0.03, v.shape)
+    v2 = v1 @ W.random_poses(1, -0.5, 0.5, seed)[0][:, :3].T + 0.2
+    o = O.Mesh(v, t)
+    o.update(v1)
+    o.update(v2)
+    on, ofc = o.nodes()
+    en, efc = emul.refit(v, t, [v1, v2])
+    assert np.array_equal(ofc, efc)
+    assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
