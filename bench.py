@@ -250,6 +250,8 @@ def run_secondary(args, meshes, stream, flush):
     dev = flush.device
     if args.only == "shapes":
         return {"shapes": _run_shapes(args, stream, flush)}
+    if args.only == "refit":
+        return {"refit": _run_refit(args, stream, flush)}
     if meshes is None:  # the distance section alone: the mesh set of the C1/C2 workloads
         w1 = _workload(args, 0)
         meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
@@ -289,6 +291,45 @@ def run_secondary(args, meshes, stream, flush):
     if args.only == "distance":
         return out
     out["shapes"] = _run_shapes(args, stream, flush)
+    out["refit"] = _run_refit(args, stream, flush)
+    return out
+
+
+def _run_refit(args, stream, flush):
+    """BVHModel update + bottom-up refit (endUpdateModel()) of the largest mesh of the
+    C1 set, on a fresh copy of it: the vertices are perturbed (N(0, 0.01^2)) and refitted
+    on the device; CPU baseline = the oracle's sequential refit of the same update."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    w1 = _workload(args, 0)
+    k = int(np.argmax([t.shape[0] for _, t in w1.meshes]))
+    v, t = w1.meshes[k]
+    g = api.BVHModel.from_arrays(v, t)
+    rng = np.random.default_rng(11)
+    frames = [torch.from_numpy(v + rng.normal(0, 0.01, v.shape)).to(flush.device) for _ in range(4)]
+    g.update_vertices(frames[0], stream=stream.cuda_stream)  # warm-up
+    torch.cuda.synchronize()
+    ms = []
+    for f in frames[1:]:
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.update_vertices(f, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    out = {"workload": f"bottom-up refit of a {t.shape[0]}-triangle mesh after a vertex update",
+           "triangles": int(t.shape[0]), "ms_per_refit": float(np.mean(ms)),
+           "value": t.shape[0] / (float(np.mean(ms)) / 1000.0), "unit": "triangles/s"}
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        o = O.Mesh(v, t)
+        t0 = time.perf_counter()
+        o.update(frames[1].cpu().numpy())
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": t.shape[0] / dt, "unit": "triangles/s", "cores": 1, "kind": "port",
+                               "sample": "one refit of the same mesh (FCL's refit is sequential)"}
     return out
 
 
@@ -600,7 +641,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
