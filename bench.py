@@ -643,7 +643,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
     ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
-    ap.add_argument("--tune-sample", type=int, default=65536, help="queries the autotuner times each setting on")
+    ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
     ap.add_argument("--serve-requests", type=int, default=1000, help="requests in the Poisson run")
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.5 x measured capacity)")

@@ -672,7 +672,7 @@ __global__ void k_bp_gather_mesh(BpSceneView S, BpQueryView Q, const int2* pairs
 
 __global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pairs, const int64_t* list, long long nl,
                                   int32_t* mesh_idx, int32_t* shape_idx, double* tfm, double* tfs, int32_t* bv_src,
-                                  int32_t* need) {
+                                  int32_t* need, int32_t* query_of) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nl; j += stride) {
     const int2 p = pairs[list[j]];
@@ -681,6 +681,7 @@ __global__ void k_bp_gather_mixed(BpSceneView S, BpQueryView Q, const int2* pair
     const bool obj_is_mesh = go.kind == GEOM_MESH;
     mesh_idx[j] = obj_is_mesh ? go.index : gq.index;
     shape_idx[j] = obj_is_mesh ? gq.index : go.index;
+    if (query_of) query_of[j] = p.x;
     if (bv_src) {
       const long long src = obj_is_mesh ? (long long)p.x : Q.nq + p.y;
       bv_src[j] = (int32_t)src;
@@ -923,10 +924,11 @@ cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32
 
 cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
                                    const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
-                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, cudaStream_t s) {
+                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, int32_t* query_of,
+                                   cudaStream_t s) {
   if (nlist <= 0) return cudaSuccess;
   k_bp_gather_mixed<<<grid_for(nlist, 256), 256, 0, s>>>(S, Q, pairs, list, nlist, mesh_idx, shape_idx, tfm, tfs,
-                                                          bv_src, need);
+                                                          bv_src, need, query_of);
   ++g_kernel_launches;
   return cudaGetLastError();
 }

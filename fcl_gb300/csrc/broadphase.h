@@ -122,7 +122,8 @@ cudaError_t launch_bp_query_done(int64_t nq, const int64_t* offsets, const int32
 // nq + o), with need[src] = 1 set for every source used.
 cudaError_t launch_bp_gather_mixed(const BpSceneView& S, const BpQueryView& Q, const int2* pairs,
                                    const int64_t* list, int64_t nlist, int32_t* mesh_idx, int32_t* shape_idx,
-                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, cudaStream_t s);
+                                   double* tfm, double* tfs, int32_t* bv_src, int32_t* need, int32_t* query_of,
+                                   cudaStream_t s);
 // The shape BV (computeBV<OBBRSS> in the world frame) of every needed source into
 // table (ShapeBV records of mesh_shape.cuh): a shape at one pose is fitted once however
 // many mesh-shape pairs it is in.

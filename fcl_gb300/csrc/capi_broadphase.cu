@@ -86,7 +86,7 @@ struct BpScratch {
   Buf ctr, qgid, q64, q32, counts, offsets, scan_tmp, ub;
   Buf pairs, kind, hit, dist, b12, pts, list;
   Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
-  Buf x_midx, x_sidx, x_counts, x_tri, qdone, x_bvsrc, x_need, x_bvtab;
+  Buf x_midx, x_sidx, x_counts, x_tri, qdone, x_bvsrc, x_need, x_bvtab, x_group, x_gcount;
   Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
 };
 BpScratch g_bs;
@@ -299,10 +299,19 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
     CKB(g_bs.x_bvtab.ensure(sizeof(ShapeBV) * nsrc), "mixed scratch");
     CKB(cudaMemsetAsync(g_bs.x_need.p, 0, 4 * nsrc, s), "mixed scratch");
   }
+  // collide without exhaustive search: a query's mesh-shape pairs stop together once
+  // the query has num_max_contacts contacts (FCL's manager stops visiting objects then)
+  const bool grouped = mode == 0 && qdone != nullptr;
+  if (grouped) {
+    CKB(g_bs.x_group.ensure(4 * nl), "mixed scratch");
+    CKB(g_bs.x_gcount.ensure(8 * Q.nq), "mixed scratch");
+    CKB(cudaMemsetAsync(g_bs.x_gcount.p, 0, 8 * Q.nq, s), "mixed scratch");
+  }
   CKB(launch_bp_gather_mixed(S, Q, g_bs.pairs.as<int2>(), g_bs.list.as<int64_t>(), nl, g_bs.x_midx.as<int32_t>(),
                              g_bs.x_sidx.as<int32_t>(), g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(),
                              table ? g_bs.x_bvsrc.as<int32_t>() : nullptr,
-                             table ? g_bs.x_need.as<int32_t>() : nullptr, s),
+                             table ? g_bs.x_need.as<int32_t>() : nullptr, grouped ? g_bs.x_group.as<int32_t>() : nullptr,
+                             s),
       "mixed gather");
   if (table) CKB(launch_bp_shape_bvs(S, Q, g_bs.x_need.as<int32_t>(), g_bs.x_bvtab.p, s), "shape BVs");
   MeshShapeLaunch L;
@@ -325,6 +334,11 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
   L.status = &dctr->status;
   L.bv_table = table ? g_bs.x_bvtab.p : nullptr;
   L.bv_src = table ? g_bs.x_bvsrc.as<int32_t>() : nullptr;
+  if (grouped) {
+    L.group = g_bs.x_group.as<int32_t>();
+    L.group_count = (unsigned long long*)g_bs.x_gcount.p;
+    L.group_max = max_contacts;
+  }
   CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
   if (mode == 0) {
     CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.x_counts.as<int32_t>(), g_bs.hit.as<int32_t>(), s),

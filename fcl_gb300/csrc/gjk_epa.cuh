@@ -703,9 +703,18 @@ struct EpaState {
     return ret;
   }
 
-  // EPA::evaluate (epa-inl.h:224-344).  V holds the GJK simplex slots 0-3 and EPA's
-  // support vertices at 4..4+kEpaVerts-1.
-  FCLG_HD int evaluate(GjkState& gjk, const D3v& guess, int max_iterations) {
+  // EPA::evaluate (epa-inl.h:224-344) as begin / step / finish, so that a lane can run
+  // one expansion at a time; evaluate() is the three in sequence.  V holds the GJK
+  // simplex slots 0-3 and EPA's support vertices at 4..4+kEpaVerts-1.
+  GjkState* gk;
+  int best, pass, iterations, max_iter;
+  EpaFace outer;
+
+  // true when the expansion loop has to run; false when the result is already final
+  // (the FallBack case)
+  FCLG_HD bool begin(GjkState& gjk, const D3v& guess, int max_iterations) {
+    gk = &gjk;
+    max_iter = max_iterations;
     SimplexVert* V = gjk.V;
     Simplex& simplex = gjk.simplices[gjk.current];
     if ((simplex.rank > 1) && gjk.enclose_origin()) {
@@ -730,9 +739,9 @@ struct EpaState {
       const int t2 = new_face(V, simplex.c[2], simplex.c[1], simplex.c[3], true);
       const int t3 = new_face(V, simplex.c[0], simplex.c[2], simplex.c[3], true);
       if (hull.count == 4) {
-        int best = find_best();
-        EpaFace outer = F[best];
-        int pass = 0;
+        best = find_best();
+        outer = F[best];
+        pass = 0;
         bind(t0, 0, t1, 0);
         bind(t0, 1, t2, 0);
         bind(t0, 2, t3, 0);
@@ -740,52 +749,10 @@ struct EpaState {
         bind(t1, 2, t2, 1);
         bind(t2, 2, t3, 1);
         status = EPA_VALID;
-        for (int iterations = 0; iterations < max_iterations; ++iterations) {
-          if (nextsv < kEpaVerts) {
-            Horizon hz{-1, -1, 0};
-            const int w = 4 + nextsv++;
-            bool valid = true;
-            F[best].pass = ++pass;
-            gjk.get_support(F[best].n, V[w]);
-            const double wdist = dot(F[best].n, V[w].w) - F[best].d;
-            if (wdist > tolerance) {
-              bool overflow = false;
-              for (int j = 0; (j < 3) && valid; ++j) valid &= expand(V, pass, w, F[best].f[j], F[best].e[j], hz, overflow);
-              if (overflow) valid = false;
-              if (valid && hz.nf >= 3) {
-                bind(hz.ff, 2, hz.cf, 1);
-                list_remove(hull, best);
-                list_append(stock, best);
-                best = find_best();
-                outer = F[best];
-              } else {
-                status = EPA_INVALIDHULL;
-                break;
-              }
-            } else {
-              status = EPA_ACCURACYREACHED;
-              break;
-            }
-          } else {
-            status = EPA_OUTOFVERTICES;
-            break;
-          }
-        }
-        const D3v projection = d3scale(outer.n, outer.d);
-        normal = outer.n;
-        depth = outer.d;
-        res_rank = 3;
-        res_c[0] = outer.c[0];
-        res_c[1] = outer.c[1];
-        res_c[2] = outer.c[2];
-        res_p[0] = d3norm(cross(V[outer.c[1]].w - projection, V[outer.c[2]].w - projection));
-        res_p[1] = d3norm(cross(V[outer.c[2]].w - projection, V[outer.c[0]].w - projection));
-        res_p[2] = d3norm(cross(V[outer.c[0]].w - projection, V[outer.c[1]].w - projection));
-        const double sum = res_p[0] + res_p[1] + res_p[2];
-        res_p[0] /= sum;
-        res_p[1] /= sum;
-        res_p[2] /= sum;
-        return status;
+        iterations = 0;
+        if (max_iter > 0) return true;
+        finish();
+        return false;
       }
     }
     status = EPA_FALLBACK;
@@ -799,6 +766,66 @@ struct EpaState {
     res_rank = 1;
     res_c[0] = simplex.c[0];
     res_p[0] = 1;
+    return false;
+  }
+  // one pass of the expansion loop; true when the loop ends (then finish() has run)
+  FCLG_HD bool step() {
+    SimplexVert* V = gk->V;
+    bool done = false;
+    if (nextsv < kEpaVerts) {
+      Horizon hz{-1, -1, 0};
+      const int w = 4 + nextsv++;
+      bool valid = true;
+      F[best].pass = ++pass;
+      gk->get_support(F[best].n, V[w]);
+      const double wdist = dot(F[best].n, V[w].w) - F[best].d;
+      if (wdist > tolerance) {
+        bool overflow = false;
+        for (int j = 0; (j < 3) && valid; ++j) valid &= expand(V, pass, w, F[best].f[j], F[best].e[j], hz, overflow);
+        if (overflow) valid = false;
+        if (valid && hz.nf >= 3) {
+          bind(hz.ff, 2, hz.cf, 1);
+          list_remove(hull, best);
+          list_append(stock, best);
+          best = find_best();
+          outer = F[best];
+        } else {
+          status = EPA_INVALIDHULL;
+          done = true;
+        }
+      } else {
+        status = EPA_ACCURACYREACHED;
+        done = true;
+      }
+    } else {
+      status = EPA_OUTOFVERTICES;
+      done = true;
+    }
+    if (!done && ++iterations >= max_iter) done = true;
+    if (done) finish();
+    return done;
+  }
+  FCLG_HD void finish() {
+    const SimplexVert* V = gk->V;
+    const D3v projection = d3scale(outer.n, outer.d);
+    normal = outer.n;
+    depth = outer.d;
+    res_rank = 3;
+    res_c[0] = outer.c[0];
+    res_c[1] = outer.c[1];
+    res_c[2] = outer.c[2];
+    res_p[0] = d3norm(cross(V[outer.c[1]].w - projection, V[outer.c[2]].w - projection));
+    res_p[1] = d3norm(cross(V[outer.c[2]].w - projection, V[outer.c[0]].w - projection));
+    res_p[2] = d3norm(cross(V[outer.c[0]].w - projection, V[outer.c[1]].w - projection));
+    const double sum = res_p[0] + res_p[1] + res_p[2];
+    res_p[0] /= sum;
+    res_p[1] /= sum;
+    res_p[2] /= sum;
+  }
+  FCLG_HD int evaluate(GjkState& gjk, const D3v& guess, int max_iterations) {
+    if (begin(gjk, guess, max_iterations))
+      while (!step()) {
+      }
     return status;
   }
 };

@@ -159,7 +159,8 @@ __global__ void k_ms_reduce(MeshShapeLaunch L, const int64_t* off, const int32_t
 }
 
 // Collide in rounds.  Each unfinished pair resumes its DFS (stack kept in global
-// memory) until it has K_r more overlapping leaves; stage 1 of the leaf test runs one
+// memory) until it has K_r more overlapping leaves or has tested 128 * 2^min(r, 3)
+// nodes this round; stage 1 of the leaf test runs one
 // leaf per thread (sphere closed form, FP32 GJK with the FP64 disjointness
 // certificate), then one thread per pair walks its leaves in DFS order, running the
 // FP64 GJK on undecided leaves, and stops once it has max_contacts intersecting leaves
@@ -191,11 +192,16 @@ __global__ void __launch_bounds__(128) k_msr_init(MeshShapeLaunch L, MsPairState
 }
 
 __global__ void __launch_bounds__(128) k_msr_dfs(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
-                                                 const MsPairState* ps, int32_t* stack, int cap, int32_t* sp,
-                                                 int32_t* leaf, int32_t* nleaf) {
+                                                 int max_visits, const MsPairState* ps, int32_t* stack, int cap,
+                                                 int32_t* sp, int32_t* leaf, int32_t* nleaf) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
     const long long i = act[a];
+    if (L.group && L.group_count[L.group[i]] >= (unsigned long long)L.group_max) {  // the query has its contacts
+      sp[i] = 0;
+      nleaf[a] = 0;
+      continue;
+    }
     const DevMesh m = L.meshes[L.mesh_idx[i]];
     M3<double> Rm;
     D3v tm;
@@ -204,7 +210,7 @@ __global__ void __launch_bounds__(128) k_msr_dfs(MeshShapeLaunch L, const int32_
     const ShapeBV32 b32 = ps[i].b32;
     int s = sp[i];
     int32_t* out = leaf + a * (long long)K;
-    const int ne = mesh_shape_dfs_resume(m, Rm, tm, bv, b32, stack + i * (long long)cap, s, cap, K,
+    const int ne = mesh_shape_dfs_resume(m, Rm, tm, bv, b32, stack + i * (long long)cap, s, cap, K, max_visits,
                                          [&](int k, int prim) { out[k] = prim; });
     if (ne < 0) {
       atomicOr(L.status, 1u);
@@ -231,31 +237,100 @@ __global__ void __launch_bounds__(128) k_msr_tests(MeshShapeLaunch L, const int3
   }
 }
 
+// Walks a pair's leaves in DFS order and counts intersections until it has max_contacts:
+// stage-1 hits count at once, undecided leaves run the FP64 GJK in this thread -- at
+// most kSerialGjk of them; the pair's further undecided leaves are deferred to one
+// thread each (k_msr_deferred) and the pair is recounted after them (k_msr_recount).
+// The count is min(max_contacts, intersecting leaves) either way; the serial part keeps
+// the early stop for the usual pair whose first undecided leaf intersects, the deferral
+// bounds the tail of a pair with many near misses.
+constexpr int kSerialGjk = 4;
+
+// adds a pair's new contacts to its group; false once the group has group_max (the
+// pair's query needs no more contacts, so its traversal can stop)
+__device__ __forceinline__ bool group_open(const MeshShapeLaunch& L, long long i, int delta) {
+  if (!L.group) return true;
+  const unsigned long long t = (delta > 0 ? atomicAdd(&L.group_count[L.group[i]], (unsigned long long)delta)
+                                          : L.group_count[L.group[i]]) +
+                               (unsigned long long)delta;
+  return t < (unsigned long long)L.group_max;
+}
+
 __global__ void __launch_bounds__(128) k_msr_update(MeshShapeLaunch L, const int32_t* act, long long nact, int K,
-                                                    const int32_t* leaf, const int32_t* nleaf, const int32_t* hit,
-                                                    const int32_t* sp, int32_t* next, unsigned long long* nnext) {
+                                                    const int32_t* leaf, const int32_t* nleaf, int32_t* hit,
+                                                    const int32_t* sp, int32_t* next, unsigned long long* nnext,
+                                                    int32_t* defer_leaf, unsigned long long* ndefer,
+                                                    int32_t* defer_pair, unsigned long long* ndefer_pair) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nact; a += stride) {
     const long long i = act[a];
     int c = L.counts[i];
     const int nl = nleaf[a];
-    // leaves in DFS order; the FP64 GJK runs only for undecided leaves and only while
-    // the pair still needs contacts
+    int budget = kSerialGjk;
+    bool deferred = false;
     for (int k = 0; k < nl && c < L.max_contacts; ++k) {
-      const int h = hit[a * (long long)K + k];
+      const long long slot = a * (long long)K + k;
+      const int h = hit[slot];
       if (h == 2) {
         ++c;
       } else if (h == 1) {
-        PairGeom g;
-        pair_geom(L, i, g);
-        double P[9];
-        load_tri_local(g.m, leaf[a * (long long)K + k], P);
-        SimplexVert V[kSimplexSlots];
-        if (shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V)) ++c;
+        if (budget > 0) {
+          --budget;
+          PairGeom g;
+          pair_geom(L, i, g);
+          double P[9];
+          load_tri_local(g.m, leaf[slot], P);
+          SimplexVert V[kSimplexSlots];
+          const bool in = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V);
+          hit[slot] = in ? 2 : 0;
+          if (in) ++c;
+        } else {
+          defer_leaf[atomicAdd(ndefer, 1ull)] = (int32_t)slot;
+          deferred = true;
+        }
       }
     }
+    if (deferred) {
+      defer_pair[atomicAdd(ndefer_pair, 1ull)] = (int32_t)a;
+      continue;
+    }
+    const int c0 = L.counts[i];
     L.counts[i] = c;
-    if (c < L.max_contacts && sp[i] > 0) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
+    if (c < L.max_contacts && sp[i] > 0 && group_open(L, i, c - c0)) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_msr_deferred(MeshShapeLaunch L, const int32_t* act, int K,
+                                                      const int32_t* leaf, int32_t* hit, const int32_t* defer_leaf,
+                                                      const unsigned long long* ndefer) {
+  const long long n = (long long)*ndefer;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const long long slot = defer_leaf[t];
+    PairGeom g;
+    pair_geom(L, act[slot / K], g);
+    double P[9];
+    load_tri_local(g.m, leaf[slot], P);
+    SimplexVert V[kSimplexSlots];
+    hit[slot] = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V) ? 2 : 0;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const int32_t* act, int K,
+                                                     const int32_t* nleaf, const int32_t* hit, const int32_t* sp,
+                                                     const int32_t* defer_pair, const unsigned long long* ndefer_pair,
+                                                     int32_t* next, unsigned long long* nnext) {
+  const long long n = (long long)*ndefer_pair;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const long long a = defer_pair[t];
+    const long long i = act[a];
+    int c = L.counts[i];
+    const int nl = nleaf[a];
+    for (int k = 0; k < nl && c < L.max_contacts; ++k) c += hit[a * (long long)K + k] == 2 ? 1 : 0;
+    const int c0 = L.counts[i];
+    L.counts[i] = c;
+    if (c < L.max_contacts && sp[i] > 0 && group_open(L, i, c - c0)) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
   }
 }
 
@@ -291,7 +366,7 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
   const int cap = stack_entries;
   cudaError_t e;
   if ((e = S.ensure(0, sizeof(MsPairState) * n)) || (e = S.ensure(1, 4ull * cap * n)) || (e = S.ensure(2, 4 * n)) ||
-      (e = S.ensure(3, 4 * n)) || (e = S.ensure(4, 4 * n)) || (e = S.ensure(5, 8)))
+      (e = S.ensure(3, 4 * n)) || (e = S.ensure(4, 4 * n)) || (e = S.ensure(5, 24)))
     return e;
   MsPairState* ps = (MsPairState*)S.p[0];
   int32_t* stack = (int32_t*)S.p[1];
@@ -309,11 +384,21 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
     int32_t* leaf = (int32_t*)S.p[6];
     int32_t* nleaf = (int32_t*)S.p[7];
     int32_t* hit = (int32_t*)S.p[8];
-    if ((e = cudaMemsetAsync(nnext, 0, 8, s))) return e;
-    k_msr_dfs<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, ps, stack, cap, sp, leaf, nleaf);
+    if ((e = S.ensure(9, 4 * nl)) || (e = S.ensure(10, 4 * nact))) return e;
+    int32_t* defer_leaf = (int32_t*)S.p[9];
+    int32_t* defer_pair = (int32_t*)S.p[10];
+    // nnext, then the deferred-leaf and deferred-pair counters
+    if ((e = cudaMemsetAsync(nnext, 0, 24, s))) return e;
+    // node tests per pair per round are capped too, so that one pair with a long
+    // traversal does not hold every round up
+    const int max_visits = 128 << std::min(r, 3);
+    k_msr_dfs<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, max_visits, ps, stack, cap, sp, leaf, nleaf);
     k_msr_tests<<<grid128(nl), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit);
-    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit, sp, next, nnext);
-    g_kernel_launches += 3;
+    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit, sp, next, nnext, defer_leaf,
+                                               nnext + 1, defer_pair, nnext + 2);
+    k_msr_deferred<<<grid128(nl), 128, 0, s>>>(L, act, K, leaf, hit, defer_leaf, nnext + 1);
+    k_msr_recount<<<grid128(nact), 128, 0, s>>>(L, act, K, nleaf, hit, sp, defer_pair, nnext + 2, next, nnext);
+    g_kernel_launches += 5;
     unsigned long long nn = 0;
     if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))

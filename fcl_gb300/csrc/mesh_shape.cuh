@@ -756,13 +756,14 @@ FCLG_HD bool shape_node_overlap(const DevMesh& m, const M3<double>& Rm, const D3
 
 // Resumable collide DFS of one pair over an explicit stack (stack[0..sp), capacity cap):
 // visits nodes in FCL's order and emits overlapping leaves until max_emit leaves have
-// been emitted or the stack is empty.  Returns the number emitted, or -1 when the stack
-// would overflow.
+// been emitted, max_visits nodes have been tested or the stack is empty.  Returns the
+// number emitted, or -1 when the stack would overflow.
 template <class Emit>
 FCLG_HD int mesh_shape_dfs_resume(const DevMesh& m, const M3<double>& Rm, const D3v& tm, const ShapeBV& bv,
-                                  const ShapeBV32& b32, int* stack, int& sp, int cap, int max_emit, Emit emit) {
+                                  const ShapeBV32& b32, int* stack, int& sp, int cap, int max_emit, int max_visits,
+                                  Emit emit) {
   int ne = 0;
-  while (sp > 0 && ne < max_emit) {
+  for (int visits = 0; sp > 0 && ne < max_emit && visits < max_visits; ++visits) {
     const int b = stack[--sp];
     int child;
     if (!shape_node_overlap(m, Rm, tm, bv, b32, b, &child)) continue;

@@ -30,6 +30,11 @@ struct MeshShapeLaunch {
   // mesh_shape.cuh) instead of fitting its own; null = fit per pair
   const void* bv_table = nullptr;
   const int32_t* bv_src = nullptr;
+  // optional early stop across pairs (collide): pairs of one group (a broadphase query)
+  // add their contacts to group_count[group[i]] and stop once it reaches group_max
+  const int32_t* group = nullptr;
+  unsigned long long* group_count = nullptr;
+  int64_t group_max = 0;
 };
 
 // One thread per pair runs the whole FCL traversal (exact statistics).

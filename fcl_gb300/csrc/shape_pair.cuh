@@ -330,6 +330,20 @@ FCLG_HD void load_tf(const double* p, M3<double>& R, D3v& t) {
   t = v3(FCLG_LDG(p + 3), FCLG_LDG(p + 7), FCLG_LDG(p + 11));
 }
 
+// the contact of an EPA that ended with status es (gjk_solver_indep-inl.h:130-154)
+FCLG_HD void epa_contact(const GjkState& g, const EpaState& epa, const M3<double>& R1, const D3v& t1, int es,
+                         PairOut& o) {
+  o.estat = es;
+  if (es == EPA_FAILED) return;
+  const SimplexVert* V = g.V;
+  D3v w0 = v3(0.0, 0.0, 0.0);
+  for (int i = 0; i < epa.res_rank; ++i) w0 = w0 + d3scale(g.shape.support(V[epa.res_c[i]].d, 0), epa.res_p[i]);
+  o.normal = epa.normal;
+  o.point = tf_apply(R1, t1, w0 - d3scale(epa.normal, epa.depth * 0.5));
+  o.depth = -epa.depth;  // ContactPoint depth of GST_INDEP
+  o.hit = 1;
+}
+
 // GJKSolver_indep::shapeIntersect through GJK (+ EPA for the contact).  epa == nullptr
 // asks for the answer only: GJK Inside decides it, since EPA::evaluate never returns
 // Failed (epa-inl.h sets Failed only in initialize, :118), so FCL's EPA never turns
@@ -357,14 +371,7 @@ FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t
   epa->tolerance = kGjkTol;
   epa->init();
   const int es = epa->evaluate(g, d3neg(guess), 255);
-  o.estat = es;
-  if (es == EPA_FAILED) return;
-  D3v w0 = v3(0.0, 0.0, 0.0);
-  for (int i = 0; i < epa->res_rank; ++i) w0 = w0 + d3scale(g.shape.support(V[epa->res_c[i]].d, 0), epa->res_p[i]);
-  o.normal = epa->normal;
-  o.point = tf_apply(R1, t1, w0 - d3scale(epa->normal, epa->depth * 0.5));
-  o.depth = -epa->depth;  // ContactPoint depth of GST_INDEP
-  o.hit = 1;
+  epa_contact(g, *epa, R1, t1, es, o);
 }
 
 // GJKSolver_indep::shapeDistance through GJK (gjk_solver_indep-inl.h:593-645): the
