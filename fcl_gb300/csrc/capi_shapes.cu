@@ -80,6 +80,17 @@ int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* 
   if (use32)
     for (auto& d : h)
       if (d.type == FCLGPU_SHAPE_CONVEX) d.pad = (int32_t)off32;
+  // a Convex's params are unused by FCL; params[0] holds the largest vertex norm (its
+  // radius about the frame origin), rounded up, for the FP32 separation certificates
+  for (auto& d : h)
+    if (d.type == FCLGPU_SHAPE_CONVEX) {
+      double r = 0.0;
+      for (int i = 0; i < d.vcnt; ++i) {
+        const double* v = verts + 3 * ((int64_t)d.voff + i);
+        r = std::max(r, std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]));
+      }
+      d.p[0] = r * (1.0 + 1e-6);
+    }
   const size_t pool_bytes = sizeof(double) * (use32 ? off32 : 3 * std::max<int64_t>(nv, 1)) + v32.size() * 4;
   fclgpu_shapeset_s* ss = new fclgpu_shapeset_s();
   cudaError_t e = cudaMalloc(&ss->shapes, sizeof(DevShape) * n);

@@ -1,23 +1,24 @@
-// FP32 GJK pre-pass for convex pairs, certified in FP64.
+// FP32 GJK pre-pass for convex pairs, with an FP32 separation certificate that carries
+// a rigorous error bound.
 //
 // FP64 arithmetic runs at 1/64 of the FP32 rate on GB300, and FCL's GJK/EPA
 // (GJKSolver_indep, narrowphase/detail/convexity_based_algorithm/gjk-inl.h) is FP64 from
 // the first iteration.  This pass runs GJK in FP32 -- Gilbert, Johnson and Keerthi's
 // iteration with the closest-point-on-simplex case analysis of Ericson, "Real-Time
-// Collision Detection" (2005), 5.1.2-5.1.6 -- to find a separating direction d.  The
-// pair is then certified separated in FP64: with pA the support point of shape A
-// toward -d and pB that of B toward d (FP64 support functions of
-// minkowski_diff-inl.h:65-265), d.pA - d.pB > 0 means every point of A lies beyond every
-// point of B along d, so the shapes are disjoint and FCL's GJK/EPA, whose simplices
-// stay inside the Minkowski difference, cannot report an intersection.  Only pairs
-// without a certificate run the FP64 solver.  The certificate asks for a gap of 2^-24
-// of the coordinate scale: far above the FP64 rounding of the support points and dot
-// products (2^-52 of the scale) and of FCL's absolute GJK tolerance (2^-45.5), so
-// that the FP64 solver's own rounding cannot place the origin inside its simplex, and
-// below what the FP32 pass can resolve anyway (coordinates rounded to 2^-24).
-//
-// The pass also returns its last closest point v, a good start for FCL's GJK distance
-// iteration (its guess argument) when the caller wants the distance.
+// Collision Detection" (2005), 5.1.2-5.1.6 -- to find a separating direction, then
+// certifies it: for the world direction D (an FP32 vector, taken as exact),
+//   gap = min over A of D.a - max over B of D.b
+//       = D.ta - h_A(-Ra^T D) - D.tb - h_B(Rb^T D),   h_S(u) = max over S of u.s,
+// is evaluated in FP32 from the FP64 poses rounded to FP32.  Every step's error is
+// bounded by u ||D||_1 times the shapes' radii and the translations (u = 2^-24): the
+// rotated directions (4u per component, each moving a support value by at most that
+// times the shape's radius), the support values (under 10u relative), the translation
+// terms and the final sums -- under 40u ||D||_1 S in all, S = 1 + rho_A + rho_B + |ta|
+// + |tb|.  The pair is certified disjoint when the computed gap exceeds 64u ||D||_1 S:
+// the true gap along the unit direction then exceeds 24u S, every point of A lies beyond
+// every point of B, and FCL's GJK cannot end Inside (its simplex stays inside the
+// Minkowski difference; the gap is far above its rounding and its absolute tolerance
+// 2^-45.5).  Only pairs without a certificate run the FP64 solver.
 #pragma once
 #include "gjk_epa.cuh"
 
@@ -119,19 +120,6 @@ struct Mink32 {
   }
 };
 
-FCLG_HD void make_mink32(const ShapeRef& A, const M3<double>& Ra, const D3v& ta, const ShapeRef& B,
-                         const M3<double>& Rb, const D3v& tb, Mink32& m) {
-  m.a = A;
-  m.b = B;
-  const M3<double> R1 = mulT(Rb, Ra);  // Rb^T Ra
-  const M3<double> R0 = mulT(Ra, Rb);  // Ra^T Rb
-  for (int i = 0; i < 9; ++i) {
-    m.R1[i] = (float)R1.m[i];
-    m.R0[i] = (float)R0.m[i];
-  }
-  const D3v dt = mulTv(Ra, tb - ta);
-  m.t0 = g3f((float)dt.x, (float)dt.y, (float)dt.z);
-}
 
 // closest point to the origin on the triangle W[0..3) (Ericson 5.1.5 with p = origin);
 // reduces W to the supporting vertex / edge / face
@@ -246,10 +234,9 @@ FCLG_HD bool closest_on_simplex(G3f* W, int& n, G3f& v) {
 
 enum : int { G32_SEPARATED = 0, G32_UNKNOWN = 1 };
 
-// want_distance = false stops at the first separating direction; true iterates until
-// the distance estimate converges (relative 2^-16) so that v is close to the closest
-// point of the Minkowski difference.
-FCLG_HD int gjk32(const Mink32& m, bool want_distance, G3f& v_out, float scale) {
+// Stops at the first direction v whose support gap v.w exceeds target |v| (or when the
+// distance estimate converges, relative 2^-16); G32_SEPARATED when v.w > 0 at the end.
+FCLG_HD int gjk32(const Mink32& m, float target, G3f& v_out, float scale) {
   G3f W[4];
   int n = 0;
   G3f v = m.sup(g3f(1.f, 0.f, 0.f));
@@ -263,7 +250,7 @@ FCLG_HD int gjk32(const Mink32& m, bool want_distance, G3f& v_out, float scale) 
     const float vw = gdot(v, w);
     if (vw > 0.f) {
       separated = true;
-      if (!want_distance) break;
+      if (vw * vw > target * target * vv) break;
     }
     if (vv - vw <= 1.5e-5f * vv) break;  // converged
     W[n++] = w;
@@ -276,51 +263,89 @@ FCLG_HD int gjk32(const Mink32& m, bool want_distance, G3f& v_out, float scale) 
   return separated ? G32_SEPARATED : G32_UNKNOWN;
 }
 
-// FP64 certificate along d (A-frame direction): world supports of A toward -d and of B
-// toward d, both FCL's FP64 support functions on the unit direction.
-FCLG_HD bool certify_separated(const ShapeRef& A, const M3<double>& Ra, const D3v& ta, const ShapeRef& B,
-                               const M3<double>& Rb, const D3v& tb, const G3f& dA, double scale) {
-  D3v d = mulv(Ra, v3((double)dA.x, (double)dA.y, (double)dA.z));  // world direction
-  const double len = d3norm(d);
-  if (!(len > 0)) return false;
-  d = d3scale(d, 1.0 / len);
-  const D3v pa = mulv(Ra, shape_support(A, mulTv(Ra, d3neg(d)))) + ta;
-  const D3v pb = mulv(Rb, shape_support(B, mulTv(Rb, d))) + tb;
-  return dot(d, pa) - dot(d, pb) > 5.9604644775390625e-08 * scale;  // 2^-24 of the scale
-}
-
-// bound on the coordinates: the translations plus each shape's extent
-FCLG_HD double pair_scale(const ShapeRef& A, const D3v& ta, const ShapeRef& B, const D3v& tb) {
-  auto ext = [](const ShapeRef& s) {
-    switch (s.s.type) {
-      case SHAPE_BOX: return 0.5 * (fabs(s.s.p[0]) + fabs(s.s.p[1]) + fabs(s.s.p[2]));
-      case SHAPE_SPHERE: return fabs(s.s.p[0]);
-      case SHAPE_CAPSULE: return fabs(s.s.p[0]) + 0.5 * fabs(s.s.p[1]);
-      case SHAPE_CYLINDER:
-      case SHAPE_CONE: return fabs(s.s.p[0]) + 0.5 * fabs(s.s.p[1]);
-      default: {
-        double r = 0;
-        const double* V = s.verts + 3 * (long long)s.s.voff;
-        const int n = s.s.type == SHAPE_TRIANGLE ? 3 : s.s.vcnt;
-        for (int i = 0; i < 3 * n; ++i) r = fmax(r, fabs(V[i]));
-        return 1.7320508075688772 * r;
-      }
+// an upper bound of the distance from a shape's frame origin to its points
+FCLG_HD float shape_radius32(const ShapeRef& sh) {
+  const DevShape& s = sh.s;
+  float r;
+  switch (s.type) {
+    case SHAPE_BOX: r = 0.5f * ((fabsf((float)s.p[0]) + fabsf((float)s.p[1])) + fabsf((float)s.p[2])); break;
+    case SHAPE_SPHERE: r = fabsf((float)s.p[0]); break;
+    case SHAPE_CAPSULE:
+    case SHAPE_CYLINDER:
+    case SHAPE_CONE: r = fabsf((float)s.p[0]) + 0.5f * fabsf((float)s.p[1]); break;
+    case SHAPE_CONVEX: r = (float)s.p[0]; break;  // the vertex pool's radius, set at upload
+    default: {  // triangle: the largest L1 norm of its vertices
+      const double* V = sh.verts + 3 * (long long)s.voff;
+      r = 0.f;
+      for (int i = 0; i < 3; ++i)
+        r = fmaxf(r, (fabsf((float)V[3 * i]) + fabsf((float)V[3 * i + 1])) + fabsf((float)V[3 * i + 2]));
     }
-  };
-  return 1.0 + fmax(fabs(ta.x), fmax(fabs(ta.y), fabs(ta.z))) + fmax(fabs(tb.x), fmax(fabs(tb.y), fabs(tb.z))) +
-         ext(A) + ext(B);
+  }
+  return r * 1.0001f;
 }
 
-// FP32 GJK, then the FP64 certificate: true when FCL's GJK on this pair cannot end
+struct Pose32 {
+  float R[9];  // row-major
+  float t[3];
+};
+FCLG_HD void pose32(const M3<double>& R, const D3v& t, Pose32& p) {
+  for (int i = 0; i < 9; ++i) p.R[i] = (float)R.m[i];
+  p.t[0] = (float)t.x;
+  p.t[1] = (float)t.y;
+  p.t[2] = (float)t.z;
+}
+FCLG_HD G3f rot32(const float* R, const G3f& v) {
+  return g3f(R[0] * v.x + R[1] * v.y + R[2] * v.z, R[3] * v.x + R[4] * v.y + R[5] * v.z,
+             R[6] * v.x + R[7] * v.y + R[8] * v.z);
+}
+FCLG_HD G3f rot32T(const float* R, const G3f& v) {
+  return g3f(R[0] * v.x + R[3] * v.y + R[6] * v.z, R[1] * v.x + R[4] * v.y + R[7] * v.z,
+             R[2] * v.x + R[5] * v.y + R[8] * v.z);
+}
+
+// the Minkowski difference of A and B posed by a and b, in A's frame, in FP32
+FCLG_HD void make_mink32(const ShapeRef& A, const Pose32& a, const ShapeRef& B, const Pose32& b, Mink32& m) {
+  m.a = A;
+  m.b = B;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      // R1 = Rb^T Ra, R0 = Ra^T Rb
+      m.R1[3 * i + j] = b.R[i] * a.R[j] + b.R[3 + i] * a.R[3 + j] + b.R[6 + i] * a.R[6 + j];
+      m.R0[3 * i + j] = a.R[i] * b.R[j] + a.R[3 + i] * b.R[3 + j] + a.R[6 + i] * b.R[6 + j];
+    }
+  m.t0 = rot32T(a.R, g3f(b.t[0] - a.t[0], b.t[1] - a.t[1], b.t[2] - a.t[2]));
+}
+
+// the FP32 certificate along the world direction D = Ra dA
+FCLG_HD bool certify_separated32(const ShapeRef& A, const Pose32& a, const ShapeRef& B, const Pose32& b,
+                                 const G3f& dA, float S) {
+  const G3f D = rot32(a.R, dA);
+  const float n1 = (fabsf(D.x) + fabsf(D.y)) + fabsf(D.z);
+  if (!(n1 > 0.f)) return false;
+  const G3f uA = rot32T(a.R, g3f(-D.x, -D.y, -D.z)), uB = rot32T(b.R, D);
+  const float hA = gdot(uA, support32(A, uA)), hB = gdot(uB, support32(B, uB));
+  const G3f ta = g3f(a.t[0], a.t[1], a.t[2]), tb = g3f(b.t[0], b.t[1], b.t[2]);
+  const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
+  return gap > 3.81469727e-06f * n1 * S;  // 64u ||D||_1 S
+}
+
+// FP32 GJK, then the FP32 certificate: true when FCL's GJK on this pair cannot end
 // Inside, i.e. when GJKSolver_indep::shapeIntersect is certainly false
 FCLG_HD bool certified_disjoint(const ShapeRef& A, const M3<double>& Ra, const D3v& ta, const ShapeRef& B,
                                 const M3<double>& Rb, const D3v& tb) {
+  Pose32 a, b;
+  pose32(Ra, ta, a);
+  pose32(Rb, tb, b);
+  const float S = 1.f + shape_radius32(A) + shape_radius32(B) +
+                  fmaxf(fabsf(a.t[0]), fmaxf(fabsf(a.t[1]), fabsf(a.t[2]))) +
+                  fmaxf(fabsf(b.t[0]), fmaxf(fabsf(b.t[1]), fabsf(b.t[2])));
+  if (!(S < 1e30f)) return false;
   Mink32 m;
-  make_mink32(A, Ra, ta, B, Rb, tb, m);
-  const double scale = pair_scale(A, ta, B, tb);
+  make_mink32(A, a, B, b, m);
   G3f v;
-  if (gjk32(m, false, v, (float)scale) != G32_SEPARATED) return false;
-  return certify_separated(A, Ra, ta, B, Rb, tb, v, scale);
+  // a direction whose gap clears the certificate's threshold with room to spare
+  if (gjk32(m, 1.32e-5f * S, v, S) != G32_SEPARATED) return false;
+  return certify_separated32(A, a, B, b, v, S);
 }
 
 }  // namespace fclgpu

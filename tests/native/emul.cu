@@ -300,6 +300,14 @@ void emu_shape_batch(int ns, const int* type, const double* params, const int* v
     sh[i].vcnt = vcnt[i];
     sh[i].pad = (type[i] == SHAPE_CONVEX && nv > 0) ? (int)off32 : 0;
     for (int k = 0; k < 3; ++k) sh[i].p[k] = params[3 * i + k];
+    if (type[i] == SHAPE_CONVEX) {  // the radius fclgpu_shapeset_create stores
+      double r = 0.0;
+      for (int j = 0; j < vcnt[i]; ++j) {
+        const double* v = verts + 3 * ((int64_t)voff[i] + j);
+        r = std::max(r, std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]));
+      }
+      sh[i].p[0] = r * (1.0 + 1e-6);
+    }
   }
   for (int64_t q = 0; q < n; ++q) {
     PairOut o;
