@@ -13,6 +13,8 @@
  * Reference interfaces replaced (paths inside the FCL repository):
  *   fclgpu_mesh_create      BVHModel<OBBRSS<double>>::beginModel/addSubModel/endModel
  *                           (geometry/bvh/BVH_model-inl.h:207-517), MEAN split
+ *   fclgpu_mesh_update*     BVHModel<OBBRSS<double>>::beginUpdateModel/updateVertex/
+ *                           endUpdateModel() (BVH_model-inl.h:624-727, 961-1027)
  *   fclgpu_collide_batch*   fcl::collide(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
  *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
