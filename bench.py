@@ -252,6 +252,8 @@ def run_secondary(args, meshes, stream, flush):
         return {"shapes": _run_shapes(args, stream, flush)}
     if args.only == "refit":
         return {"refit": _run_refit(args, stream, flush)}
+    if args.only == "contacts":
+        return {"contacts": _run_contacts(args, meshes, stream, flush)}
     if meshes is None:  # the distance section alone: the mesh set of the C1/C2 workloads
         w1 = _workload(args, 0)
         meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
@@ -292,6 +294,78 @@ def run_secondary(args, meshes, stream, flush):
         return out
     out["shapes"] = _run_shapes(args, stream, flush)
     out["refit"] = _run_refit(args, stream, flush)
+    out["contacts"] = _run_contacts(args, meshes, stream, flush)
+    return out
+
+
+def _run_contacts(args, meshes, stream, flush):
+    """collide() with enable_contact (contact position, normal, depth per contact) on a
+    5% sample of the C1 queries, num_max_contacts = 100,000: the pair traversal (FP32 +
+    FP64 recheck) plus the FP64 contact pass, against the same sample without contact
+    geometry; 300 queries checked bit for bit against the oracle; CPU baseline = the
+    oracle on all host cores."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    w1 = _workload(args, 0)
+    if meshes is None:
+        meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
+    w = W.subsample(w1, max(1, w1.n // 20), seed=5)
+    dev = flush.device
+    tf2 = torch.from_numpy(w.tf2).to(dev)
+    pq = torch.from_numpy(w.pair).to(dev)
+    res = {}
+
+    def run():
+        res["g"] = api.collide_contacts_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000,
+                                              precision="fp32", stream=stream.cuda_stream)
+
+    def pairs_only():
+        api.collide_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, num_max_contacts=100000, precision="fp32",
+                          stream=stream.cuda_stream)
+
+    ms = _time_device(run, 2, 1, stream, flush)
+    ms_pairs = _time_device(pairs_only, 2, 1, stream, flush)
+    g = res["g"]
+    total = int(g["total_contacts"])
+    out = {"workload": f"c1 sample of {w.n} queries, enable_contact, num_max_contacts=100000", "queries": w.n,
+           "contacts": total, "ms_per_step": ms, "value": w.n / (ms / 1000.0), "unit": "queries/s",
+           "contacts_per_s": total / (ms / 1000.0), "pairs_only_ms_per_step": ms_pairs}
+    # bit-exact check of a sample against the oracle
+    from oracle import pyoracle as O
+    rng = np.random.default_rng(2)
+    chk = np.sort(rng.choice(w.n, size=min(300, w.n), replace=False))
+    off = g["offsets"].cpu().numpy()
+    ids, pos = g["contacts"].cpu().numpy(), g["pos"].cpu().numpy()
+    nrm, dep = g["normal"].cpu().numpy(), g["depth"].cpu().numpy()
+    om = {}
+    ok = True
+    for q in chk:
+        a, b = w.pairs[w.pair[q]]
+        for m in (a, b):
+            if m not in om:
+                om[m] = O.Mesh(*w.meshes[m])
+        c, i2, p2, n2, d2 = O.collide_contacts_batch(om[a], om[b], w.tf2[q:q + 1], num_max_contacts=100000)
+        r = slice(off[q], off[q + 1])
+        ok &= bool(np.array_equal(ids[r], i2) and np.array_equal(pos[r], p2) and np.array_equal(nrm[r], n2)
+                   and np.array_equal(dep[r], d2))
+    out["oracle_checked_queries"] = int(chk.size)
+    out["bit_exact_vs_oracle"] = ok
+    if not args.no_cpu:
+        threads = O.hardware_threads()
+        k = min(w.n, 2000)
+        ws = W.subsample(w, k, seed=3)
+        t0 = time.perf_counter()
+        for p in np.unique(ws.pair):
+            idx = np.nonzero(ws.pair == p)[0]
+            a, b = ws.pairs[p]
+            for m in (a, b):
+                if m not in om:
+                    om[m] = O.Mesh(*ws.meshes[m])
+            O.collide_contacts_batch(om[a], om[b], ws.tf2[idx], num_max_contacts=100000, nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+                               "sample": f"{k} queries drawn uniformly from the {w.n}-query sample"}
     return out
 
 
@@ -641,7 +715,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "contacts", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")

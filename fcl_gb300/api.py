@@ -198,6 +198,10 @@ class Contact:
     o2: object
     b1: int
     b2: int
+    # set when CollisionRequest.enable_contact (contact.h: pos, normal, penetration_depth)
+    pos: np.ndarray | None = None
+    normal: np.ndarray | None = None
+    penetration_depth: float = 0.0
 
     def __lt__(self, other):  # contact-inl.h:98-104
         if self.b1 == other.b1:
@@ -251,10 +255,9 @@ class DistanceResult:
 
 
 def _unsupported(req):
-    if getattr(req, "enable_contact", False):
-        raise N.FclGpuError(-9, "collide", "enable_contact (contact points/normals) is not on the GPU path")
-    if getattr(req, "enable_signed_distance", False):
-        raise N.FclGpuError(-9, "distance", "enable_signed_distance is not on the GPU path")
+    # enable_signed_distance needs no check: FCL's signed-distance step
+    # (narrowphase/distance-inl.h:147-187) runs only when min_distance < 0, which the
+    # BVHModel distance traversal never reports (triangle and RSS distances are >= 0).
     if getattr(req, "rel_err", 0.0) or getattr(req, "abs_err", 0.0):
         raise N.FclGpuError(-9, "distance", "rel_err/abs_err must be 0 on the GPU path")
 
@@ -264,6 +267,18 @@ def collide(o1: CollisionObject, o2: CollisionObject, request: CollisionRequest,
     _unsupported(request)
     if request.num_max_contacts == 0:
         return 0
+    if request.enable_contact:
+        if request.enable_statistics:
+            raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "collide", "statistics are not produced with contacts")
+        out = collide_contacts_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None],
+                                     o2.tf[None], num_max_contacts=request.num_max_contacts,
+                                     precision=request.precision)
+        room = max(0, request.num_max_contacts - len(result.contacts))
+        for i in range(min(room, out["total_contacts"])):
+            b1, b2 = out["contacts"][i]
+            result.contacts.append(Contact(o1.geometry, o2.geometry, int(b1), int(b2), out["pos"][i].copy(),
+                                           out["normal"][i].copy(), float(out["depth"][i])))
+        return result.numContacts()
     out = collide_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None], o2.tf[None],
                         pair_of_query=None, num_max_contacts=request.num_max_contacts, precision=request.precision,
                         statistics=request.enable_statistics)
@@ -342,6 +357,72 @@ def collide_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=
 
 
 _contacts_hint = {"cap": 1 << 16}
+
+
+def collide_contacts_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=1, precision="fp32",
+                           stream=None):
+    """Batched fcl::collide with CollisionRequest::enable_contact = true.  Returns a dict
+    with counts, offsets, total_contacts and per contact (query after query, in the
+    reference's DFS order): contacts (b1, b2), pos (world), normal (world) and depth.
+    numpy inputs use the host entry point; torch CUDA tensors the device one."""
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    req = N.CollideRequest(int(num_max_contacts), _prec(precision), 0, 0)
+    hs = _handles(meshes)
+    if _is_torch(tf2):
+        import torch
+        dev = tf2.device
+        n = tf2.shape[0]
+        counts = torch.zeros(n, dtype=torch.int32, device=dev)
+        offsets = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        args = (hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+                None if pair_of_query is None else pair_of_query.data_ptr(),
+                None if tf1 is None else tf1.data_ptr(), tf2.data_ptr(), C.byref(req))
+        # buffers sized from the previous batch; a batch that outgrows them runs again
+        cap = _contacts_hint["cap"]
+        while True:
+            ids = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=dev)
+            pos = torch.empty((max(cap, 1), 3), dtype=torch.float64, device=dev)
+            nrm = torch.empty((max(cap, 1), 3), dtype=torch.float64, device=dev)
+            dep = torch.empty(max(cap, 1), dtype=torch.float64, device=dev)
+            res = N.ContactResult(counts.data_ptr(), offsets.data_ptr(), ids.data_ptr(), pos.data_ptr(),
+                                  nrm.data_ptr(), dep.data_ptr(), cap, 0)
+            rc = N.lib().fclgpu_collide_contacts_device(*args, C.byref(res), s)
+            if rc == N.FCLGPU_ERR_CAPACITY:
+                cap = int(res.total_contacts * 1.25) + 1024
+                _contacts_hint["cap"] = cap
+                continue
+            N.check(rc, "fclgpu_collide_contacts_device")
+            break
+        total = int(res.total_contacts)
+        return {"counts": counts, "offsets": offsets, "total_contacts": total, "contacts": ids[:total],
+                "pos": pos[:total], "normal": nrm[:total], "depth": dep[:total]}
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(-1, 12)
+    pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
+    counts = np.zeros(n, np.int32)
+    offsets = np.zeros(n + 1, np.int64)
+    cap = _contacts_hint["cap"]
+    while True:
+        ids = np.empty((max(cap, 1), 2), np.int32)
+        pos = np.empty((max(cap, 1), 3))
+        nrm = np.empty((max(cap, 1), 3))
+        dep = np.empty(max(cap, 1))
+        res = N.ContactResult(counts.ctypes.data, offsets.ctypes.data, ids.ctypes.data, pos.ctypes.data,
+                              nrm.ctypes.data, dep.ctypes.data, cap, 0)
+        rc = N.lib().fclgpu_collide_contacts(hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+                                             None if pq is None else pq.ctypes.data,
+                                             None if tf1a is None else tf1a.ctypes.data, tf2.ctypes.data,
+                                             C.byref(req), C.byref(res), stream)
+        if rc == N.FCLGPU_ERR_CAPACITY:
+            cap = int(res.total_contacts)
+            continue
+        N.check(rc, "fclgpu_collide_contacts")
+        break
+    t = int(res.total_contacts)
+    return {"counts": counts, "offsets": offsets, "total_contacts": t, "contacts": ids[:t], "pos": pos[:t],
+            "normal": nrm[:t], "depth": dep[:t]}
 
 
 def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statistics, contacts, stream):

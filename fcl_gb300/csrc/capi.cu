@@ -284,6 +284,88 @@ int collide_scatter(const int64_t* offsets, int32_t* contacts, cudaStream_t s) {
   return FCLGPU_OK;
 }
 
+// ---------------------------------------------------------------------------------
+// Collide with contact geometry (enable_contact): the pair traversal lists the
+// intersecting triangle pairs; mesh_contact.cu turns them into contacts.
+// ---------------------------------------------------------------------------------
+struct ContactScratch {
+  DevBuf pcounts, poff, plist, qid, nc, info, G, flag, scan_tmp;
+  ContactLaunch last{};
+};
+ContactScratch g_contact;
+
+// Per-query contact counts and offsets (n + 1) of the batch; the pairs and their contact
+// geometry stay in g_contact for contacts_emit.
+int contacts_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
+                  const fclgpu_collide_request* req, int stack, int32_t* counts, int64_t* offsets, cudaStream_t s,
+                  int64_t* total_out) {
+  ContactScratch& C = g_contact;
+  const int64_t maxc = std::max<int64_t>(req->num_max_contacts, 0);
+  int64_t pair_cap = maxc;
+  CK(C.pcounts.ensure(4 * (size_t)n), "contact scratch");
+  CK(C.poff.ensure(8 * (size_t)(n + 1)), "contact scratch");
+  CK(C.flag.ensure(sizeof(unsigned int)), "contact scratch");
+  for (int attempt = 0; attempt < 40; ++attempt) {
+    fclgpu_collide_request r = *req;
+    r.num_max_contacts = (int32_t)pair_cap;
+    r.enable_statistics = 0;
+    int64_t npairs = 0;
+    int rc = collide_core(n, pair_of_query, tf1, tf2, &r, (int32_t*)C.pcounts.p, (int64_t*)C.poff.p, nullptr,
+                          nullptr, nullptr, stack, s, &npairs);
+    if (rc) return rc;
+    const size_t np = (size_t)std::max<int64_t>(npairs, 1);
+    CK(C.plist.ensure(8 * np), "contact scratch");
+    CK(C.qid.ensure(4 * np), "contact scratch");
+    CK(C.nc.ensure(4 * np), "contact scratch");
+    CK(C.info.ensure(80 * np), "contact scratch");
+    CK(C.G.ensure(8 * (np + 1)), "contact scratch");
+    const int64_t scan_n = std::max<int64_t>(npairs, n);
+    CK(C.scan_tmp.ensure(sizeof(int64_t) * (size_t)(2 * ((scan_n + 4095) / 4096) + 4)), "scan scratch");
+    rc = collide_scatter((const int64_t*)C.poff.p, (int32_t*)C.plist.p, s);
+    if (rc) return rc;
+    ContactLaunch L{};
+    L.meshes = (const DevMesh*)g_scratch.meshes.p;
+    L.pairs = (const int2*)g_scratch.pairs.p;
+    L.pair_of_query = pair_of_query;
+    L.tf1 = tf1;
+    L.tf2 = tf2;
+    L.n = n;
+    L.poff = (const int64_t*)C.poff.p;
+    L.plist = (const int2*)C.plist.p;
+    L.npairs = npairs;
+    L.max_contacts = (int32_t)std::min<int64_t>(maxc, INT32_MAX);
+    L.pair_cap = (int32_t)pair_cap;
+    L.qid = (int32_t*)C.qid.p;
+    L.nc = (int32_t*)C.nc.p;
+    L.info = (double*)C.info.p;
+    L.G = (const int64_t*)C.G.p;
+    CK(launch_contact_info(L, s), "contact info");
+    CK(launch_exclusive_scan(L.nc, npairs, (int64_t*)C.G.p, (int64_t*)C.scan_tmp.p, s), "contact scan");
+    CK(cudaMemsetAsync(C.flag.p, 0, sizeof(unsigned int), s), "contact flag");
+    CK(launch_contact_counts(L, (const int32_t*)C.pcounts.p, counts, (unsigned int*)C.flag.p, s), "contact counts");
+    unsigned int incomplete = 0;
+    CK(cudaMemcpyAsync(&incomplete, C.flag.p, sizeof(incomplete), cudaMemcpyDeviceToHost, s), "contact flag");
+    CK(cudaStreamSynchronize(s), "contact counts");
+    C.last = L;
+    if (incomplete == 0 || pair_cap >= INT32_MAX) break;
+    // some query's pair list ended at the cap with fewer contacts than it may hold (pairs
+    // without a contact point): list more pairs
+    pair_cap = std::min<int64_t>(2 * std::max<int64_t>(pair_cap, 1), INT32_MAX);
+  }
+  CK(launch_exclusive_scan(counts, n, offsets, (int64_t*)C.scan_tmp.p, s), "contact offsets");
+  int64_t total = 0;
+  CK(cudaMemcpyAsync(&total, offsets + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read total");
+  CK(cudaStreamSynchronize(s), "contact offsets");
+  *total_out = total;
+  return FCLGPU_OK;
+}
+
+int contacts_emit(const int64_t* offsets, int32_t* ids, double* pos, double* normal, double* depth,
+                  cudaStream_t s) {
+  CK(launch_contact_emit(g_contact.last, offsets, ids, pos, normal, depth, s), "contact emit");
+  return FCLGPU_OK;
+}
+
 }  // namespace
 
 void fclgpu::set_error_detail(const std::string& what) { g_detail = what; }
@@ -602,6 +684,103 @@ int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const in
     CK(cudaMemcpyAsync(res->num_leaf_tests, S.out_nleaf.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
   if (res->num_rechecks) CK(cudaMemcpyAsync(res->num_rechecks, S.out_nrc.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
   CK(cudaStreamSynchronize(s), "collide batch");
+  return FCLGPU_OK;
+}
+
+int fclgpu_collide_contacts_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                   int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                                   const double* tf2, const fclgpu_collide_request* req, fclgpu_contact_result* res,
+                                   void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts || !res->offsets)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2, counts or offsets");
+  if (n >= (int64_t)1 << 31) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "batch too large");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (req->enable_statistics) return fail(FCLGPU_ERR_UNSUPPORTED, "statistics are not produced with contacts");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int stack = 64;
+  rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+  if (rc) return rc;
+  res->total_contacts = 0;
+  if (n == 0) {
+    CK(cudaMemsetAsync(res->offsets, 0, sizeof(int64_t), s), "offsets");
+    CK(cudaStreamSynchronize(s), "contacts");
+    return FCLGPU_OK;
+  }
+  int64_t total = 0;
+  rc = contacts_core(n, pair_of_query, tf1, tf2, req, stack, res->counts, res->offsets, s, &total);
+  if (rc) return rc;
+  res->total_contacts = total;
+  if (!res->ids && !res->pos && !res->normal && !res->depth) return FCLGPU_OK;
+  if (total > res->capacity) return fail(FCLGPU_ERR_CAPACITY, "contact buffers too small");
+  rc = contacts_emit(res->offsets, res->ids, res->pos, res->normal, res->depth, s);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s), "contacts");
+  return FCLGPU_OK;
+}
+
+int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                            int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                            const double* tf2, const fclgpu_collide_request* req, fclgpu_contact_result* res,
+                            void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or counts");
+  cudaStream_t s = (cudaStream_t)stream;
+  Scratch& S = g_scratch;
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (pair_of_query) CK(S.in_pair.ensure(4 * nn), "inputs");
+    if (tf1) CK(S.in_tf1.ensure(96 * nn), "inputs");
+    CK(S.in_tf2.ensure(96 * nn), "inputs");
+    CK(S.counts.ensure(4 * nn), "outputs");
+    CK(S.offsets.ensure(8 * (nn + 1)), "outputs");
+    if (n > 0) {
+      if (pair_of_query) CK(cudaMemcpyAsync(S.in_pair.p, pair_of_query, 4 * n, cudaMemcpyHostToDevice, s), "h2d");
+      if (tf1) CK(cudaMemcpyAsync(S.in_tf1.p, tf1, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+      CK(cudaMemcpyAsync(S.in_tf2.p, tf2, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    }
+  }
+  fclgpu_contact_result dr{};
+  dr.counts = (int32_t*)S.counts.p;
+  dr.offsets = (int64_t*)S.offsets.p;
+  int rc = fclgpu_collide_contacts_device(meshes, num_meshes, pairs_host, num_pairs, n,
+                                          pair_of_query ? (const int32_t*)S.in_pair.p : nullptr,
+                                          tf1 ? (const double*)S.in_tf1.p : nullptr, (const double*)S.in_tf2.p, req,
+                                          &dr, stream);
+  if (rc) return rc;
+  const int64_t total = dr.total_contacts;
+  res->total_contacts = total;
+  const bool want = res->ids || res->pos || res->normal || res->depth;
+  if (want && total > res->capacity) return fail(FCLGPU_ERR_CAPACITY, "contact buffers too small");
+  if (want && total > 0) {
+    // output scratch: ids 8 B, pos 24 B, normal 24 B, depth 8 B per contact
+    const size_t nt = (size_t)total;
+    CK(S.out_contacts.ensure(64 * nt), "contacts scratch");
+    char* base = (char*)S.out_contacts.p;
+    int32_t* ids = (int32_t*)base;
+    double* pos = (double*)(base + 8 * nt);
+    double* nrm = (double*)(base + 32 * nt);
+    double* dep = (double*)(base + 56 * nt);
+    rc = contacts_emit((const int64_t*)S.offsets.p, ids, pos, nrm, dep, s);
+    if (rc) return rc;
+    if (res->ids) CK(cudaMemcpyAsync(res->ids, ids, 8 * nt, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->pos) CK(cudaMemcpyAsync(res->pos, pos, 24 * nt, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->normal) CK(cudaMemcpyAsync(res->normal, nrm, 24 * nt, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->depth) CK(cudaMemcpyAsync(res->depth, dep, 8 * nt, cudaMemcpyDeviceToHost, s), "d2h");
+  }
+  if (n > 0) {
+    CK(cudaMemcpyAsync(res->counts, S.counts.p, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->offsets) CK(cudaMemcpyAsync(res->offsets, S.offsets.p, 8 * (n + 1), cudaMemcpyDeviceToHost, s), "d2h");
+  } else if (res->offsets) {
+    res->offsets[0] = 0;
+  }
+  CK(cudaStreamSynchronize(s), "collide contacts");
   return FCLGPU_OK;
 }
 

@@ -88,6 +88,32 @@ struct DistanceLaunch {
   int64_t* nrecheck;
 };
 
+// Contact information of a collide batch (enable_contact): the intersecting triangle
+// pairs listed by the pair traversal, query after query (plist at poff[q]), get their
+// contacts; see mesh_contact.cu.
+struct ContactLaunch {
+  const DevMesh* meshes;
+  const int2* pairs;
+  const int32_t* pair_of_query;
+  const double* tf1;
+  const double* tf2;
+  int64_t n;                 // queries
+  const int64_t* poff;       // n + 1 offsets into plist
+  const int2* plist;         // (b1, b2) per intersecting triangle pair
+  int64_t npairs;
+  int32_t max_contacts;      // CollisionRequest::num_max_contacts
+  int32_t pair_cap;          // the cap the pair traversal ran with
+  int32_t* qid;              // per pair: its query
+  int32_t* nc;               // per pair: contacts (0, 1 or 2)
+  double* info;              // per pair: pos[2][3], normal[3], depth (world frame)
+  const int64_t* G;          // npairs + 1: exclusive scan of nc
+};
+cudaError_t launch_contact_info(const ContactLaunch& L, cudaStream_t s);
+cudaError_t launch_contact_counts(const ContactLaunch& L, const int32_t* pair_counts, int32_t* counts,
+                                  unsigned int* incomplete, cudaStream_t s);
+cudaError_t launch_contact_emit(const ContactLaunch& L, const int64_t* out_off, int32_t* ids, double* pos,
+                                double* normal, double* depth, cudaStream_t s);
+
 // precision: 0 = plain FP64, 1 = FP32 with FP64 recheck.  stack_entries: 64 or 256.
 cudaError_t launch_mesh_collide(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
                                 cudaStream_t s);

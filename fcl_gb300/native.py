@@ -40,6 +40,12 @@ class CollideResult(C.Structure):
                 ("num_rechecks", C.c_void_p), ("total_contacts", C.c_int64)]
 
 
+class ContactResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("ids", C.c_void_p), ("pos", C.c_void_p),
+                ("normal", C.c_void_p), ("depth", C.c_void_p), ("capacity", C.c_int64),
+                ("total_contacts", C.c_int64)]
+
+
 class DistanceRequest(C.Structure):
     _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32), ("enable_statistics", C.c_int32),
                 ("reserved", C.c_int32)]
@@ -128,6 +134,10 @@ _SIGS = {
                                               C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
     "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                        C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
+    "fclgpu_collide_contacts_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                                 C.POINTER(CollideRequest), C.POINTER(ContactResult), _VP]),
+    "fclgpu_collide_contacts": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                          C.POINTER(CollideRequest), C.POINTER(ContactResult), _VP]),
     "fclgpu_distance_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                                C.POINTER(DistanceRequest), C.POINTER(DistanceResult), _VP]),
     "fclgpu_distance_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,

@@ -118,6 +118,40 @@ def identity_poses(n: int) -> np.ndarray:
     return tf
 
 
+def grid_box(n: int, half=(0.5, 0.5, 0.5)) -> tuple[np.ndarray, np.ndarray]:
+    """Surface of an axis-aligned box with half-extents `half`, each face split into
+    n x n squares of two triangles (12 n^2 triangles, outward winding).  Faces meet at
+    shared vertices; flat faces and parallel edges give ties in contact depths."""
+    g = np.linspace(-1.0, 1.0, n + 1)
+    verts, tris, index = [], [], {}
+
+    def vid(p):
+        key = tuple(np.round(p, 12))
+        if key not in index:
+            index[key] = len(verts)
+            verts.append(p)
+        return index[key]
+
+    for axis in range(3):
+        for sign in (-1.0, 1.0):
+            u, v = (axis + 1) % 3, (axis + 2) % 3
+            for i in range(n):
+                for j in range(n):
+                    quad = []
+                    for di, dj in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        p = np.zeros(3)
+                        p[axis] = sign
+                        p[u] = g[i + di]
+                        p[v] = g[j + dj]
+                        quad.append(vid(p * np.asarray(half, float)))
+                    a, b, c, d = quad
+                    if sign > 0:
+                        tris += [(a, b, c), (a, c, d)]
+                    else:
+                        tris += [(a, c, b), (a, d, c)]
+    return np.asarray(verts, np.float64), np.asarray(tris, np.int32)
+
+
 # ---------------------------------------------------------------------------------
 # Mesh-pair workloads
 # ---------------------------------------------------------------------------------

@@ -17,6 +17,8 @@
  *                           endUpdateModel() (BVH_model-inl.h:624-727, 961-1027)
  *   fclgpu_collide_batch*   fcl::collide(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
+ *   fclgpu_collide_contacts*  fcl::collide(...) with enable_contact (contact position,
+ *                           normal, depth; mesh_collision_traversal_node-inl.h:579-600)
  *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/distance.h:51-62, distance-inl.h:71-246)
  *   fclgpu_shape_batch*     fcl::collide / fcl::distance on convex shapes (GJKSolver_indep)
@@ -148,6 +150,43 @@ FCLGPU_API int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshe
                                     const int32_t* pair_of_query, const double* tf1,
                                     const double* tf2, const fclgpu_collide_request* req,
                                     fclgpu_collide_result* res, void* stream);
+
+/* Contacts with their geometry: fcl::collide with CollisionRequest::enable_contact = true
+ * on BVHModel<OBBRSS> pairs (mesh_collision_traversal_node-inl.h:579-600;
+ * Intersect::intersect_Triangle with contact output, intersect-inl.h:597-617, 800-886).
+ * Each intersecting triangle pair, in the reference's DFS order, adds 0, 1 or 2
+ * contacts: the deepest points of one triangle below the other's plane (world frame),
+ * the world normal (that plane's normal, negated when it is the second triangle's) and
+ * the penetration depth, as many as fit under num_max_contacts; the query stops once it
+ * holds num_max_contacts contacts.  counts[n] and offsets[n+1] (per query, contacts) are
+ * always written; ids (b1, b2: 2 per contact), pos (3 per contact), normal (3 per
+ * contact) and depth (1 per contact) when non-NULL, if total_contacts <= capacity
+ * (else FCLGPU_ERR_CAPACITY with total_contacts set).  req->precision selects the pair
+ * traversal's form; the contact geometry is FP64.  Statistics are not produced here
+ * (req->enable_statistics must be 0).  "_device": device pointers, stream-ordered;
+ * plain: host pointers.  Synchronises the stream. */
+typedef struct {
+  int32_t* counts;
+  int64_t* offsets;
+  int32_t* ids;
+  double* pos;
+  double* normal;
+  double* depth;
+  int64_t capacity;
+  int64_t total_contacts;     /* written by the call */
+} fclgpu_contact_result;
+
+FCLGPU_API int fclgpu_collide_contacts_device(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                              const int32_t* pairs_host, int32_t num_pairs,
+                                              int64_t n, const int32_t* pair_of_query,
+                                              const double* tf1, const double* tf2,
+                                              const fclgpu_collide_request* req,
+                                              fclgpu_contact_result* res, void* stream);
+FCLGPU_API int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                       const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+                                       const int32_t* pair_of_query, const double* tf1,
+                                       const double* tf2, const fclgpu_collide_request* req,
+                                       fclgpu_contact_result* res, void* stream);
 
 typedef struct {
   int32_t enable_nearest_points;  /* DistanceRequest::enable_nearest_points */

@@ -127,6 +127,59 @@ int64_t orc_collide_batch(void* h1, void* h2, int64_t n, const double* tf1, cons
   return total;
 }
 
+// Batched fcl::collide with enable_contact = true over n poses of one mesh pair.
+// counts[i] = contacts of pose i; per contact (pose after pose, DFS order): ids (b1,b2),
+// pos (3), normal (3), depth (1), up to cap contacts.  Returns the total.
+int64_t orc_collide_contacts_batch(void* h1, void* h2, int64_t n, const double* tf1, const double* tf2,
+                                   int64_t num_max_contacts, int nthreads, int64_t* counts, int* ids,
+                                   double* pos, double* normal, double* depth, int64_t cap) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  std::vector<std::vector<ContactOut>> per(n);
+  parallel_for(n, nthreads, [&](int64_t i, int) {
+    Tf a = tf1 ? load_tf(tf1 + 12 * i) : identity_tf();
+    Tf b = load_tf(tf2 + 12 * i);
+    counts[i] = (int64_t)collide_mesh_contacts(*m1, a, *m2, b, (size_t)num_max_contacts, per[i], nullptr);
+  });
+  int64_t total = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    for (const ContactOut& c : per[i]) {
+      if (total < cap) {
+        ids[2 * total] = c.b1;
+        ids[2 * total + 1] = c.b2;
+        for (int k = 0; k < 3; ++k) {
+          pos[3 * total + k] = c.pos[k];
+          normal[3 * total + k] = c.normal[k];
+        }
+        depth[total] = c.depth;
+      }
+      ++total;
+    }
+  }
+  return total;
+}
+
+// The contact part of intersect_Triangle for n triangle pairs (P: 9 doubles, Qm: 9
+// doubles, Q already in P's frame): counts[i], pts (6), normal (3), depth (1).
+void orc_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* counts, double* pts,
+                           double* normal, double* depth) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3 a[3], b[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = mk(P[9 * i + 3 * k], P[9 * i + 3 * k + 1], P[9 * i + 3 * k + 2]);
+      b[k] = mk(Qm[9 * i + 3 * k], Qm[9 * i + 3 * k + 1], Qm[9 * i + 3 * k + 2]);
+    }
+    V3 cp[2], nrm;
+    double d;
+    int k = tri_contact_info(a, b, cp, nrm, d);
+    counts[i] = k;
+    for (int j = 0; j < 2; ++j)
+      for (int c = 0; c < 3; ++c) pts[6 * i + 3 * j + c] = j < k ? cp[j][c] : 0.0;
+    for (int c = 0; c < 3; ++c) normal[3 * i + c] = nrm[c];
+    depth[i] = d;
+  }
+}
+
 // Batched fcl::distance over n poses of one mesh pair.  Outputs per pose: dist,
 // (b1,b2), and when nearest != 0 the two world-frame nearest points (6 doubles).
 void orc_distance_batch(void* h1, void* h2, int64_t n, const double* tf1, const double* tf2,

@@ -913,6 +913,77 @@ bool tri_intersect(const V3& P1, const V3& P2, const V3& P3, const V3& Q1, const
   return true;
 }
 
+// intersect-inl.h:1040-1053 (buildTrianglePlane).  FCL leaves the plane unset for a
+// triangle without a normal; this restatement gives it the zero plane.
+static void build_triangle_plane(const V3& a, const V3& b, const V3& c, V3& n, double& t) {
+  V3 m = cross(sub(b, a), sub(c, a));
+  double sq = sqnorm(m);
+  if (sq > 0) {
+    double l = std::sqrt(sq);
+    n = mk(m[0] / l, m[1] / l, m[2] / l);
+    t = dot(n, a);
+  } else {
+    n = mk(0, 0, 0);
+    t = 0;
+  }
+}
+
+// intersect-inl.h:848-886 (computeDeepestPoints), getEpsilon() = 1e-5 (:1117-1120)
+static void compute_deepest_points(const V3* pts, int np, const V3& n, double t, double& depth, V3* out,
+                                   int& nout) {
+  const double eps = 1e-5;
+  double max_depth = -std::numeric_limits<double>::max();
+  int k = 0, num_neg = 0, num_pos = 0, num_zero = 0;
+  for (int i = 0; i < np; ++i) {
+    double dist = -(dot(n, pts[i]) - t);  // -distanceToPlane (:1033-1037)
+    if (dist > eps)
+      num_pos++;
+    else if (dist < -eps)
+      num_neg++;
+    else
+      num_zero++;
+    if (dist > max_depth) {
+      max_depth = dist;
+      k = 1;
+      out[k - 1] = pts[i];
+    } else if (dist + 1e-6 >= max_depth) {
+      k++;
+      out[k - 1] = pts[i];
+    }
+  }
+  if (max_depth < -eps) k = 0;
+  if (num_zero == 0 && ((num_neg == 0) || (num_pos == 0))) k = 0;
+  depth = max_depth;
+  nout = k;
+}
+
+// intersect-inl.h:800-844: the contact part of intersect_Triangle, on P and on Q
+// already moved into P's frame (R Q + T)
+int tri_contact_info(const V3 P[3], const V3 Qm[3], V3 cp[2], V3& normal, double& depth) {
+  V3 n1, n2;
+  double t1, t2;
+  build_triangle_plane(P[0], P[1], P[2], n1, t1);
+  build_triangle_plane(Qm[0], Qm[1], Qm[2], n2, t2);
+  V3 deep1[3], deep2[3];
+  int nd1 = 0, nd2 = 0;
+  double pd1, pd2;
+  compute_deepest_points(Qm, 3, n1, t1, pd2, deep2, nd2);
+  compute_deepest_points(P, 3, n2, t2, pd1, deep1, nd1);
+  int k;
+  if (pd1 > pd2) {
+    k = std::min(nd2, 2);
+    for (int i = 0; i < k; ++i) cp[i] = deep2[i];
+    normal = n1;
+    depth = pd2;
+  } else {
+    k = std::min(nd1, 2);
+    for (int i = 0; i < k; ++i) cp[i] = deep1[i];
+    normal = neg(n2);
+    depth = pd1;
+  }
+  return k;
+}
+
 // narrowphase/detail/primitive_shape_algorithm/triangle_distance-inl.h:54-167
 static void seg_points(const V3& P, const V3& A, const V3& Q, const V3& B, V3& VEC, V3& X, V3& Y) {
   V3 T, TMP;
@@ -1112,6 +1183,8 @@ struct CollideCtx {
   size_t num_max_contacts;
   std::vector<int>* contacts;  // pairs (b1,b2)
   size_t n_contacts;
+  std::vector<ContactOut>* full;  // enable_contact: contacts with their geometry
+  Tf tf1;
   CollideStats st;
   bool can_stop() const { return n_contacts > 0 && num_max_contacts <= n_contacts; }
 };
@@ -1133,6 +1206,28 @@ inline void leaf_testing(CollideCtx& c, int b1, int b2) {
   const auto& v2 = c.m2->verts;
   if (tri_intersect(v1[t1.v[0]], v1[t1.v[1]], v1[t1.v[2]], v2[t2.v[0]], v2[t2.v[1]], v2[t2.v[2]],
                     c.R, c.T)) {
+    if (c.full) {
+      // enable_contact branch (mesh_collision_traversal_node-inl.h:579-600)
+      V3 P[3] = {v1[t1.v[0]], v1[t1.v[1]], v1[t1.v[2]]};
+      V3 Qm[3];
+      for (int k = 0; k < 3; ++k) Qm[k] = add(mulv(c.R, v2[t2.v[k]]), c.T);
+      V3 cp[2], nrm;
+      double depth;
+      size_t k = (size_t)tri_contact_info(P, Qm, cp, nrm, depth);
+      if (c.num_max_contacts < c.n_contacts + k)
+        k = (c.num_max_contacts > c.n_contacts) ? (c.num_max_contacts - c.n_contacts) : 0;
+      for (size_t i = 0; i < k; ++i) {
+        ContactOut o;
+        o.b1 = p1;
+        o.b2 = p2;
+        o.pos = apply(c.tf1, cp[i]);
+        o.normal = mulv(c.tf1.R, nrm);
+        o.depth = depth;
+        c.full->push_back(o);
+        c.n_contacts++;
+      }
+      return;
+    }
     if (c.n_contacts < c.num_max_contacts) {
       c.contacts->push_back(p1);
       c.contacts->push_back(p2);
@@ -1262,6 +1357,26 @@ size_t collide_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2
   c.num_max_contacts = num_max_contacts;
   c.contacts = &contacts;
   c.n_contacts = 0;
+  c.full = nullptr;
+  c.tf1 = tf1;
+  collision_recurse(c, 0, 0);
+  if (st) *st = c.st;
+  return c.n_contacts;
+}
+
+size_t collide_mesh_contacts(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
+                             size_t num_max_contacts, std::vector<ContactOut>& out, CollideStats* st) {
+  if (num_max_contacts == 0) return 0;
+  CollideCtx c;
+  c.m1 = &m1;
+  c.m2 = &m2;
+  c.R = mulT(tf1.R, tf2.R);
+  c.T = mulTv(tf1.R, sub(tf2.t, tf1.t));
+  c.num_max_contacts = num_max_contacts;
+  c.contacts = nullptr;
+  c.n_contacts = 0;
+  c.full = &out;
+  c.tf1 = tf1;
   collision_recurse(c, 0, 0);
   if (st) *st = c.st;
   return c.n_contacts;

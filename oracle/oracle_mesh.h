@@ -84,6 +84,19 @@ struct CollideStats {
 size_t collide_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
                     size_t num_max_contacts, std::vector<int>& contacts, CollideStats* st);
 
+// fcl::collide with enable_contact = true: each intersecting triangle pair adds 0..2
+// contacts with position and normal in the world frame and the penetration depth
+// (mesh_collision_traversal_node-inl.h:579-600, intersect-inl.h:800-886).
+struct ContactOut {
+  int b1, b2;
+  V3 pos, normal;
+  double depth;
+};
+size_t collide_mesh_contacts(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
+                             size_t num_max_contacts, std::vector<ContactOut>& out, CollideStats* st);
+// the contact part of intersect_Triangle on P and Qm (Q moved into P's frame)
+int tri_contact_info(const V3 P[3], const V3 Qm[3], V3 cp[2], V3& normal, double& depth);
+
 struct DistanceOut {
   double min_distance;
   int b1, b2;

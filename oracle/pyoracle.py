@@ -42,6 +42,10 @@ def lib():
         L.orc_collide_batch.restype = C.c_int64
         L.orc_collide_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64, C.c_int,
                                         _i64p, _i64p, _i64p, _ip, C.c_int64]
+        L.orc_collide_contacts_batch.restype = C.c_int64
+        L.orc_collide_contacts_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64,
+                                                 C.c_int, _i64p, _ip, _dp, _dp, _dp, C.c_int64]
+        L.orc_tri_contact_batch.argtypes = [C.c_int64, _dp, _dp, _ip, _dp, _dp, _dp]
         L.orc_distance_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int, C.c_int,
                                          _dp, _ip, _dp, _i64p, _i64p]
         L.orc_rss_fit3.argtypes = [_dp, _dp]
@@ -123,6 +127,41 @@ def collide_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = 
         if total <= cap:
             return counts, out[:total].copy(), nbv, nleaf
         cap = int(total)
+
+
+def collide_contacts_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None,
+                           num_max_contacts: int = 1, nthreads: int = 1):
+    """fcl::collide with enable_contact = true.  Returns (counts, ids (total,2) int32,
+    pos (total,3), normal (total,3), depth (total,)) in per-pose DFS order."""
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1p = None if tf1 is None else _d(np.ascontiguousarray(tf1, np.float64).reshape(-1, 12))
+    counts = np.zeros(n, np.int64)
+    cap = 1 << 16
+    while True:
+        ids = np.empty((cap, 2), np.int32)
+        pos = np.empty((cap, 3), np.float64)
+        nrm = np.empty((cap, 3), np.float64)
+        dep = np.empty(cap, np.float64)
+        total = lib().orc_collide_contacts_batch(m1.h, m2.h, n, tf1p, _d(tf2), num_max_contacts, nthreads,
+                                                 _q(counts), _i(ids), _d(pos), _d(nrm), _d(dep), cap)
+        if total <= cap:
+            return counts, ids[:total].copy(), pos[:total].copy(), nrm[:total].copy(), dep[:total].copy()
+        cap = int(total)
+
+
+def tri_contact_batch(P: np.ndarray, Qm: np.ndarray):
+    """Contact part of intersect_Triangle per pair: (counts, points (n,2,3), normal (n,3),
+    depth (n,)); Qm is the second triangle already in the first one's frame."""
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 9)
+    Qm = np.ascontiguousarray(Qm, np.float64).reshape(-1, 9)
+    n = P.shape[0]
+    cnt = np.empty(n, np.int32)
+    pts = np.empty((n, 2, 3), np.float64)
+    nrm = np.empty((n, 3), np.float64)
+    dep = np.empty(n, np.float64)
+    lib().orc_tri_contact_batch(n, _d(P), _d(Qm), _i(cnt), _d(pts), _d(nrm), _d(dep))
+    return cnt, pts, nrm, dep
 
 
 def distance_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None,

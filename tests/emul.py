@@ -96,3 +96,13 @@ def shape_batch(shapes, ia, ib, tf1, tf2):
                                                                     "p2", "status")))
     out["hit"] = out["hit"].astype(bool)
     return out
+
+
+def tri_contact_batch(P, Qm):
+    """tri_contact.cuh on the host: (counts, points (n,2,3), normal (n,3), depth (n,))."""
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 9)
+    Qm = np.ascontiguousarray(Qm, np.float64).reshape(-1, 9)
+    n = P.shape[0]
+    cnt = np.empty(n, np.int32); pts = np.empty((n, 2, 3)); nrm = np.empty((n, 3)); dep = np.empty(n)
+    lib().emu_tri_contact_batch(C.c_int64(n), _p(P), _p(Qm), _p(cnt), _p(pts), _p(nrm), _p(dep))
+    return cnt, pts, nrm, dep

@@ -9,6 +9,7 @@
 #include "collide_traverse.cuh"
 #include "refit.cuh"
 #include "shape_pair.cuh"
+#include "tri_contact.cuh"
 
 using namespace fclgpu;
 
@@ -324,6 +325,32 @@ void emu_shape_batch(int ns, const int* type, const double* params, const int* v
     dist[q] = o.dist;
     status[2 * q] = o.gstat;
     status[2 * q + 1] = o.estat;
+  }
+}
+
+// The product's contact computation of an intersecting triangle pair (tri_contact.cuh),
+// run on the host: P (9 doubles) and Qm (9 doubles, already in P's frame) per pair.
+void emu_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* counts, double* pts, double* normal,
+                           double* depth) {
+  for (int64_t i = 0; i < n; ++i) {
+    V3<double> a[3], b[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = v3<double>(P[9 * i + 3 * k], P[9 * i + 3 * k + 1], P[9 * i + 3 * k + 2]);
+      b[k] = v3<double>(Qm[9 * i + 3 * k], Qm[9 * i + 3 * k + 1], Qm[9 * i + 3 * k + 2]);
+    }
+    V3<double> cp[2], nrm;
+    double d;
+    const int k = tri_contact(a, b, cp, nrm, d);
+    counts[i] = k;
+    for (int j = 0; j < 2; ++j) {
+      pts[6 * i + 3 * j] = j < k ? cp[j].x : 0.0;
+      pts[6 * i + 3 * j + 1] = j < k ? cp[j].y : 0.0;
+      pts[6 * i + 3 * j + 2] = j < k ? cp[j].z : 0.0;
+    }
+    normal[3 * i] = nrm.x;
+    normal[3 * i + 1] = nrm.y;
+    normal[3 * i + 2] = nrm.z;
+    depth[i] = d;
   }
 }
 
