@@ -254,6 +254,8 @@ def run_secondary(args, meshes, stream, flush):
         return {"refit": _run_refit(args, stream, flush)}
     if args.only == "contacts":
         return {"contacts": _run_contacts(args, meshes, stream, flush)}
+    if args.only == "ccd":
+        return {"ccd": _run_ccd(args, meshes, stream, flush)}
     if meshes is None:  # the distance section alone: the mesh set of the C1/C2 workloads
         w1 = _workload(args, 0)
         meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
@@ -295,6 +297,73 @@ def run_secondary(args, meshes, stream, flush):
     out["shapes"] = _run_shapes(args, stream, flush)
     out["refit"] = _run_refit(args, stream, flush)
     out["contacts"] = _run_contacts(args, meshes, stream, flush)
+    out["ccd"] = _run_ccd(args, meshes, stream, flush)
+    return out
+
+
+def _run_ccd(args, meshes, stream, flush):
+    """fcl::continuousCollide (default request: naive solver, 10 samples, translation
+    motion) on the C1 mesh pairs: 100,000 motions drawn like the C1 queries' pairs, each
+    starting separated (translation U[1.5,4]^3, Haar rotation) and moving by a random
+    vector of length U[0.5,3]; CPU baseline = the oracle on all host cores."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    w1 = _workload(args, 0)
+    if meshes is None:
+        meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
+    n = max(1, int(100_000 * args.scale))
+    rng = np.random.default_rng(17)
+    pq = w1.pair[rng.integers(0, w1.n, n)].astype(np.int32)
+    b0 = W.random_poses(n, 1.5, 4.0, 18)
+    d = rng.normal(size=(n, 3))
+    d *= (rng.uniform(0.5, 3.0, n) / np.linalg.norm(d, axis=1))[:, None]
+    b1 = b0.copy()
+    b1[:, :, 3] -= np.abs(d) * np.sign(b0[:, :, 3])   # towards the other object
+    dev = flush.device
+    t0, t1, tq = (torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (b0, b1, pq))
+    res = {}
+
+    def run():
+        res["g"] = api.continuous_collide_batch(meshes, w1.pairs, None, None, t0, t1, pair_of_query=tq,
+                                                stream=stream.cuda_stream)
+
+    ms = _time_device(run, 2, 1, stream, flush)
+    g = res["g"]
+    hit = g["is_collide"].cpu().numpy()
+    toc = g["time_of_contact"].cpu().numpy()
+    out = {"workload": f"{n} translation motions over the 64 C1 mesh pairs, 10 samples each", "motions": n,
+           "ms_per_step": ms, "value": n / (ms / 1000.0), "unit": "motions/s",
+           "colliding_fraction": float(hit.mean()), "mean_time_of_contact_colliding":
+               float(toc[hit > 0].mean()) if hit.any() else None}
+    from oracle import pyoracle as O
+    om = {}
+    chk = np.sort(rng.choice(n, size=min(200, n), replace=False))
+    ok = True
+    for q in chk:
+        a, b = w1.pairs[pq[q]]
+        for m in (a, b):
+            if m not in om:
+                om[m] = O.Mesh(*w1.meshes[m])
+        h2, t2, _, _ = O.continuous_collide_batch(om[a], om[b], b0[q:q + 1], b1[q:q + 1])
+        ok &= bool(h2[0] == hit[q] and t2[0] == toc[q])
+    out["oracle_checked_motions"] = int(chk.size)
+    out["exact_vs_oracle"] = ok
+    if not args.no_cpu:
+        threads = O.hardware_threads()
+        k = min(n, 1000)
+        sel = np.sort(rng.choice(n, size=k, replace=False))
+        t_start = time.perf_counter()
+        for p in np.unique(pq[sel]):
+            idx = sel[pq[sel] == p]
+            a, b = w1.pairs[p]
+            for m in (a, b):
+                if m not in om:
+                    om[m] = O.Mesh(*w1.meshes[m])
+            O.continuous_collide_batch(om[a], om[b], b0[idx], b1[idx], nthreads=threads)
+        dt = time.perf_counter() - t_start
+        out["cpu_baseline"] = {"value": k / dt, "unit": "motions/s", "cores": threads, "kind": "port",
+                               "sample": f"{k} of the motions"}
     return out
 
 
@@ -715,7 +784,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "contacts", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "contacts", "ccd", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")

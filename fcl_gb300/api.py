@@ -306,6 +306,91 @@ def distance(o1: CollisionObject, o2: CollisionObject, request: DistanceRequest,
     return result.min_distance
 
 
+CCDM = {"trans": 0, "linear": 1, "screw": 2, "spline": 3}   # CCDMotionType (continuous_collision_request.h:48)
+CCDC = {"naive": 0, "conservative_advancement": 1, "ray_shooting": 2, "polynomial_solver": 3}   # CCDSolverType
+
+
+@dataclass
+class ContinuousCollisionRequest:
+    num_max_iterations: int = 10
+    toc_err: float = 1e-4
+    ccd_motion_type: str = "trans"
+    ccd_solver_type: str = "naive"
+    precision: str = "fp32"
+
+
+@dataclass
+class ContinuousCollisionResult:
+    is_collide: bool = False
+    time_of_contact: float = 1.0
+    contact_tf1: np.ndarray = field(default_factory=lambda: transform())
+    contact_tf2: np.ndarray = field(default_factory=lambda: transform())
+
+
+def continuous_collide_batch(meshes, pairs, tf1_beg, tf1_end, tf2_beg, tf2_end, pair_of_query=None,
+                             num_max_iterations=10, toc_err=1e-4, motion="trans", solver="naive", precision="fp32",
+                             stream=None):
+    """Batched fcl::continuousCollide on mesh pairs (naive solver, translation motion).
+    Returns is_collide (n,), time_of_contact (n,), contact_tf1/contact_tf2 (n,3,4; zero
+    where no collision).  numpy inputs use the host entry point, torch CUDA tensors the
+    device one."""
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    req = N.CcdRequest(int(num_max_iterations), float(toc_err), CCDM[motion], CCDC[solver], _prec(precision), 0)
+    hs = _handles(meshes)
+    if _is_torch(tf2_beg):
+        import torch
+        dev = tf2_beg.device
+        n = tf2_beg.shape[0]
+        hit = torch.zeros(n, dtype=torch.int32, device=dev)
+        toc = torch.zeros(n, dtype=torch.float64, device=dev)
+        c1 = torch.zeros((n, 3, 4), dtype=torch.float64, device=dev)
+        c2 = torch.zeros((n, 3, 4), dtype=torch.float64, device=dev)
+        s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+        res = N.CcdResult(hit.data_ptr(), toc.data_ptr(), c1.data_ptr(), c2.data_ptr())
+        N.check(N.lib().fclgpu_continuous_collide_batch_device(
+            hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+            None if pair_of_query is None else pair_of_query.data_ptr(),
+            None if tf1_beg is None else tf1_beg.data_ptr(), None if tf1_end is None else tf1_end.data_ptr(),
+            tf2_beg.data_ptr(), tf2_end.data_ptr(), C.byref(req), C.byref(res), s),
+            "fclgpu_continuous_collide_batch_device")
+        return {"is_collide": hit, "time_of_contact": toc, "contact_tf1": c1, "contact_tf2": c2}
+    b0 = np.ascontiguousarray(tf2_beg, np.float64).reshape(-1, 12)
+    b1 = np.ascontiguousarray(tf2_end, np.float64).reshape(-1, 12)
+    n = b0.shape[0]
+    a0 = None if tf1_beg is None else np.ascontiguousarray(tf1_beg, np.float64).reshape(-1, 12)
+    a1 = None if tf1_end is None else np.ascontiguousarray(tf1_end, np.float64).reshape(-1, 12)
+    pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
+    hit = np.zeros(n, np.int32)
+    toc = np.zeros(n)
+    c1 = np.zeros((n, 3, 4))
+    c2 = np.zeros((n, 3, 4))
+    res = N.CcdResult(hit.ctypes.data, toc.ctypes.data, c1.ctypes.data, c2.ctypes.data)
+    N.check(N.lib().fclgpu_continuous_collide_batch(
+        hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n, None if pq is None else pq.ctypes.data,
+        None if a0 is None else a0.ctypes.data, None if a1 is None else a1.ctypes.data, b0.ctypes.data,
+        b1.ctypes.data, C.byref(req), C.byref(res), stream), "fclgpu_continuous_collide_batch")
+    return {"is_collide": hit, "time_of_contact": toc, "contact_tf1": c1, "contact_tf2": c2}
+
+
+def continuousCollide(o1: CollisionObject, tf1_end, o2: CollisionObject, tf2_end,
+                      request: ContinuousCollisionRequest, result: ContinuousCollisionResult) -> float:
+    """fcl::continuousCollide(o1, tf1_end, o2, tf2_end, request, result) for two
+    BVHModel<OBBRSS> objects (continuous_collision-inl.h:455-469): the motions run from the
+    objects' transforms to tf1_end / tf2_end."""
+    out = continuous_collide_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None],
+                                   np.asarray(tf1_end, np.float64)[None], o2.tf[None],
+                                   np.asarray(tf2_end, np.float64)[None],
+                                   num_max_iterations=request.num_max_iterations, toc_err=request.toc_err,
+                                   motion=request.ccd_motion_type, solver=request.ccd_solver_type,
+                                   precision=request.precision)
+    result.is_collide = bool(out["is_collide"][0])
+    result.time_of_contact = float(out["time_of_contact"][0])
+    if result.is_collide:
+        result.contact_tf1 = out["contact_tf1"][0].copy()
+        result.contact_tf2 = out["contact_tf2"][0].copy()
+    return result.time_of_contact
+
+
 def _handles(meshes):
     arr = (C.c_void_p * len(meshes))()
     for i, m in enumerate(meshes):

@@ -784,6 +784,147 @@ int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, const
   return FCLGPU_OK;
 }
 
+// ---- continuous collide (naive solver, translation motion) -------------------------
+namespace {
+struct CcdScratch {
+  DevBuf tfa, tfb, pq, counts, offsets, in_pq, in_a0, in_a1, in_b0, in_b1, out_hit, out_toc, out_tf1, out_tf2;
+};
+CcdScratch g_ccd;
+
+int ccd_samples(const fclgpu_ccd_request* req, int64_t* n_iter) {
+  if (req->solver_type != FCLGPU_CCDC_NAIVE)
+    return fail(FCLGPU_ERR_UNSUPPORTED, "only the naive continuous-collision solver is on the GPU path");
+  if (req->motion_type != FCLGPU_CCDM_TRANS)
+    return fail(FCLGPU_ERR_UNSUPPORTED, "only the translation motion is on the GPU path");
+  if (req->num_max_iterations < 0 || !(req->toc_err > 0))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_iterations must be >= 0 and toc_err > 0");
+  // continuous_collision-inl.h:144: min(num_max_iterations, (size_t)ceil(1 / toc_err))
+  const double c = std::ceil(1.0 / req->toc_err);
+  const int64_t k = c >= 9.0e18 ? INT64_MAX : (int64_t)c;
+  *n_iter = std::min<int64_t>(req->num_max_iterations, k);
+  if (*n_iter == 1) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "one sample: FCL computes t = 0/0");
+  return FCLGPU_OK;
+}
+}  // namespace
+
+int fclgpu_continuous_collide_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                           int32_t num_pairs, int64_t n, const int32_t* pair_of_query,
+                                           const double* tf1_beg, const double* tf1_end, const double* tf2_beg,
+                                           const double* tf2_end, const fclgpu_ccd_request* req,
+                                           fclgpu_ccd_result* res, void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2_beg || !tf2_end || !res->is_collide || !res->time_of_contact)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or outputs");
+  if ((tf1_beg == nullptr) != (tf1_end == nullptr))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "tf1_beg and tf1_end must both be given or both be NULL");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  int64_t n_iter = 0;
+  int rc = ccd_samples(req, &n_iter);
+  if (rc) return rc;
+  if (n * std::max<int64_t>(n_iter, 1) >= (int64_t)1 << 31)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "queries x samples must stay below 2^31");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int stack = 64;
+  rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+  if (rc) return rc;
+  if (n == 0) return FCLGPU_OK;
+  CcdLaunch L{};
+  L.pair_of_query = pair_of_query;
+  L.tf1_beg = tf1_beg;
+  L.tf1_end = tf1_end;
+  L.tf2_beg = tf2_beg;
+  L.tf2_end = tf2_end;
+  L.n = n;
+  L.n_iter = n_iter;
+  L.is_collide = res->is_collide;
+  L.toc = res->time_of_contact;
+  L.contact_tf1 = res->contact_tf1;
+  L.contact_tf2 = res->contact_tf2;
+  if (n_iter == 0) {  // no sample: is_collide = false, time_of_contact = 1
+    CK(g_ccd.counts.ensure(4), "ccd scratch");
+    CK(launch_ccd_reduce(L, (const int32_t*)g_ccd.counts.p, s), "ccd reduce");
+    CK(cudaStreamSynchronize(s), "ccd");
+    return FCLGPU_OK;
+  }
+  const size_t N = (size_t)(n * n_iter);
+  CK(g_ccd.tfa.ensure(96 * N), "ccd scratch");
+  CK(g_ccd.tfb.ensure(96 * N), "ccd scratch");
+  CK(g_ccd.pq.ensure(4 * N), "ccd scratch");
+  CK(g_ccd.counts.ensure(4 * N), "ccd scratch");
+  CK(g_ccd.offsets.ensure(8 * (N + 1)), "ccd scratch");
+  L.tfa = (double*)g_ccd.tfa.p;
+  L.tfb = (double*)g_ccd.tfb.p;
+  L.pq_expanded = (int32_t*)g_ccd.pq.p;
+  CK(launch_ccd_poses(L, s), "ccd poses");
+  // the discrete collides: default CollisionRequest (one contact, no contact geometry)
+  fclgpu_collide_request cr{};
+  cr.num_max_contacts = 1;
+  cr.precision = req->precision;
+  int64_t total = 0;
+  rc = collide_core((int64_t)N, L.pq_expanded, L.tfa, L.tfb, &cr, (int32_t*)g_ccd.counts.p,
+                    (int64_t*)g_ccd.offsets.p, nullptr, nullptr, nullptr, stack, s, &total);
+  if (rc) return rc;
+  CK(launch_ccd_reduce(L, (const int32_t*)g_ccd.counts.p, s), "ccd reduce");
+  CK(cudaStreamSynchronize(s), "ccd");
+  return FCLGPU_OK;
+}
+
+int fclgpu_continuous_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                    int32_t num_pairs, int64_t n, const int32_t* pair_of_query,
+                                    const double* tf1_beg, const double* tf1_end, const double* tf2_beg,
+                                    const double* tf2_end, const fclgpu_ccd_request* req, fclgpu_ccd_result* res,
+                                    void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2_beg || !tf2_end || !res->is_collide || !res->time_of_contact)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or outputs");
+  cudaStream_t s = (cudaStream_t)stream;
+  CcdScratch& G = g_ccd;
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (pair_of_query) CK(G.in_pq.ensure(4 * nn), "inputs");
+  if (tf1_beg) CK(G.in_a0.ensure(96 * nn), "inputs");
+  if (tf1_end) CK(G.in_a1.ensure(96 * nn), "inputs");
+  CK(G.in_b0.ensure(96 * nn), "inputs");
+  CK(G.in_b1.ensure(96 * nn), "inputs");
+  CK(G.out_hit.ensure(4 * nn), "outputs");
+  CK(G.out_toc.ensure(8 * nn), "outputs");
+  CK(G.out_tf1.ensure(96 * nn), "outputs");
+  CK(G.out_tf2.ensure(96 * nn), "outputs");
+  if (n > 0) {
+    if (pair_of_query) CK(cudaMemcpyAsync(G.in_pq.p, pair_of_query, 4 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (tf1_beg) CK(cudaMemcpyAsync(G.in_a0.p, tf1_beg, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (tf1_end) CK(cudaMemcpyAsync(G.in_a1.p, tf1_end, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    CK(cudaMemcpyAsync(G.in_b0.p, tf2_beg, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    CK(cudaMemcpyAsync(G.in_b1.p, tf2_end, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    // entries of non-colliding queries are left unchanged: start from the caller's values
+    if (res->contact_tf1) CK(cudaMemcpyAsync(G.out_tf1.p, res->contact_tf1, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (res->contact_tf2) CK(cudaMemcpyAsync(G.out_tf2.p, res->contact_tf2, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+  }
+  fclgpu_ccd_result dr{};
+  dr.is_collide = (int32_t*)G.out_hit.p;
+  dr.time_of_contact = (double*)G.out_toc.p;
+  dr.contact_tf1 = res->contact_tf1 ? (double*)G.out_tf1.p : nullptr;
+  dr.contact_tf2 = res->contact_tf2 ? (double*)G.out_tf2.p : nullptr;
+  rc = fclgpu_continuous_collide_batch_device(meshes, num_meshes, pairs_host, num_pairs, n,
+                                              pair_of_query ? (const int32_t*)G.in_pq.p : nullptr,
+                                              tf1_beg ? (const double*)G.in_a0.p : nullptr,
+                                              tf1_end ? (const double*)G.in_a1.p : nullptr,
+                                              (const double*)G.in_b0.p, (const double*)G.in_b1.p, req, &dr, stream);
+  if (rc) return rc;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(res->is_collide, G.out_hit.p, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    CK(cudaMemcpyAsync(res->time_of_contact, G.out_toc.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->contact_tf1) CK(cudaMemcpyAsync(res->contact_tf1, G.out_tf1.p, 96 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->contact_tf2) CK(cudaMemcpyAsync(res->contact_tf2, G.out_tf2.p, 96 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  }
+  CK(cudaStreamSynchronize(s), "continuous collide");
+  return FCLGPU_OK;
+}
+
 int fclgpu_distance_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
                                  int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
                                  const double* tf2, const fclgpu_distance_request* req, fclgpu_distance_result* res,

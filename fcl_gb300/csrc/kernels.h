@@ -114,6 +114,27 @@ cudaError_t launch_contact_counts(const ContactLaunch& L, const int32_t* pair_co
 cudaError_t launch_contact_emit(const ContactLaunch& L, const int64_t* out_off, int32_t* ids, double* pos,
                                 double* normal, double* depth, cudaStream_t s);
 
+// Continuous collide (naive solver, translation motion): sampled poses of every query,
+// then the first colliding sample; see ccd.cu.
+struct CcdLaunch {
+  const int32_t* pair_of_query;
+  const double* tf1_beg;     // may be null (identity at both ends)
+  const double* tf1_end;
+  const double* tf2_beg;
+  const double* tf2_end;
+  int64_t n;                 // queries
+  int64_t n_iter;            // samples per query (>= 2)
+  double* tfa;               // n * n_iter sampled transforms of object 1 (12 doubles)
+  double* tfb;               // ... of object 2
+  int32_t* pq_expanded;      // n * n_iter pair indices
+  int32_t* is_collide;
+  double* toc;
+  double* contact_tf1;       // may be null
+  double* contact_tf2;       // may be null
+};
+cudaError_t launch_ccd_poses(const CcdLaunch& L, cudaStream_t s);
+cudaError_t launch_ccd_reduce(const CcdLaunch& L, const int32_t* counts, cudaStream_t s);
+
 // precision: 0 = plain FP64, 1 = FP32 with FP64 recheck.  stack_entries: 64 or 256.
 cudaError_t launch_mesh_collide(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
                                 cudaStream_t s);

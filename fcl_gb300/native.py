@@ -46,6 +46,16 @@ class ContactResult(C.Structure):
                 ("total_contacts", C.c_int64)]
 
 
+class CcdRequest(C.Structure):
+    _fields_ = [("num_max_iterations", C.c_int64), ("toc_err", C.c_double), ("motion_type", C.c_int32),
+                ("solver_type", C.c_int32), ("precision", C.c_int32), ("reserved", C.c_int32)]
+
+
+class CcdResult(C.Structure):
+    _fields_ = [("is_collide", C.c_void_p), ("time_of_contact", C.c_void_p), ("contact_tf1", C.c_void_p),
+                ("contact_tf2", C.c_void_p)]
+
+
 class DistanceRequest(C.Structure):
     _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32), ("enable_statistics", C.c_int32),
                 ("reserved", C.c_int32)]
@@ -134,6 +144,10 @@ _SIGS = {
                                               C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
     "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                        C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
+    "fclgpu_continuous_collide_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
+                                                         _VP, _VP, C.POINTER(CcdRequest), C.POINTER(CcdResult), _VP]),
+    "fclgpu_continuous_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP, _VP,
+                                                  _VP, C.POINTER(CcdRequest), C.POINTER(CcdResult), _VP]),
     "fclgpu_collide_contacts_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                                  C.POINTER(CollideRequest), C.POINTER(ContactResult), _VP]),
     "fclgpu_collide_contacts": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,

@@ -19,6 +19,9 @@
  *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
  *   fclgpu_collide_contacts*  fcl::collide(...) with enable_contact (contact position,
  *                           normal, depth; mesh_collision_traversal_node-inl.h:579-600)
+ *   fclgpu_continuous_collide_batch*  fcl::continuousCollide(...) on BVHModel<OBBRSS>
+ *                           pairs, naive solver, translation motion
+ *                           (narrowphase/continuous_collision-inl.h:134-171, 436-451)
  *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/distance.h:51-62, distance-inl.h:71-246)
  *   fclgpu_shape_batch*     fcl::collide / fcl::distance on convex shapes (GJKSolver_indep)
@@ -187,6 +190,47 @@ FCLGPU_API int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_me
                                        const int32_t* pair_of_query, const double* tf1,
                                        const double* tf2, const fclgpu_collide_request* req,
                                        fclgpu_contact_result* res, void* stream);
+
+/* Continuous collision of mesh pairs: fcl::continuousCollide(o1, tf1_beg, tf1_end, o2,
+ * tf2_beg, tf2_end, request, result) (narrowphase/continuous_collision-inl.h:436-451) with
+ * the request's default solver CCDC_NAIVE (:134-171) and default motion CCDM_TRANS
+ * (math/motion/translation_motion-inl.h): the motion is sampled at
+ * n_iter = min(num_max_iterations, ceil(1/toc_err)) times t_i = i/(n_iter-1), each sample is
+ * a discrete collide with the default CollisionRequest, and the first colliding t_i is the
+ * time of contact (1 and no collision otherwise).  n_iter must be 0 (no sample: no
+ * collision) or >= 2 (FCL divides 0 by 0 at n_iter = 1).  Other solvers and motions return
+ * FCLGPU_ERR_UNSUPPORTED.  tf1_beg/tf1_end may both be NULL (identity).  Outputs per query:
+ * is_collide, time_of_contact, and for colliding queries contact_tf1/contact_tf2 (the
+ * sampled transforms at the time of contact, 12 doubles each; other entries are left
+ * unchanged).  "_device": device pointers, plain: host pointers; both synchronise. */
+enum { FCLGPU_CCDM_TRANS = 0, FCLGPU_CCDM_LINEAR = 1, FCLGPU_CCDM_SCREW = 2, FCLGPU_CCDM_SPLINE = 3 };
+enum { FCLGPU_CCDC_NAIVE = 0, FCLGPU_CCDC_CONSERVATIVE_ADVANCEMENT = 1, FCLGPU_CCDC_RAY_SHOOTING = 2,
+       FCLGPU_CCDC_POLYNOMIAL_SOLVER = 3 };
+
+typedef struct {
+  int64_t num_max_iterations; /* ContinuousCollisionRequest::num_max_iterations (10) */
+  double toc_err;             /* ::toc_err (1e-4) */
+  int32_t motion_type;        /* ::ccd_motion_type (FCLGPU_CCDM_TRANS) */
+  int32_t solver_type;        /* ::ccd_solver_type (FCLGPU_CCDC_NAIVE) */
+  int32_t precision;          /* form of the discrete collides */
+  int32_t reserved;
+} fclgpu_ccd_request;
+
+typedef struct {
+  int32_t* is_collide;        /* ContinuousCollisionResult::is_collide */
+  double* time_of_contact;    /* ::time_of_contact */
+  double* contact_tf1;        /* ::contact_tf1 (3x4 row-major), may be NULL */
+  double* contact_tf2;        /* ::contact_tf2, may be NULL */
+} fclgpu_ccd_result;
+
+FCLGPU_API int fclgpu_continuous_collide_batch_device(
+    const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+    const int32_t* pair_of_query, const double* tf1_beg, const double* tf1_end, const double* tf2_beg,
+    const double* tf2_end, const fclgpu_ccd_request* req, fclgpu_ccd_result* res, void* stream);
+FCLGPU_API int fclgpu_continuous_collide_batch(
+    const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+    const int32_t* pair_of_query, const double* tf1_beg, const double* tf1_end, const double* tf2_beg,
+    const double* tf2_end, const fclgpu_ccd_request* req, fclgpu_ccd_result* res, void* stream);
 
 typedef struct {
   int32_t enable_nearest_points;  /* DistanceRequest::enable_nearest_points */

@@ -149,6 +149,8 @@ OBB merge_largedist(const OBB& b1, const OBB& b2) {
   return b;
 }
 
+}  // namespace
+
 // Eigen's rotation matrix -> quaternion (x, y, z, w)
 void quat_from_matrix(const M3& m, double q[4]) {
   const double t = (m(0, 0) + m(1, 1)) + m(2, 2);
@@ -192,6 +194,8 @@ M3 matrix_from_quat(const double q[4]) {
   r(2, 2) = 1 - (txx + tyy);
   return r;
 }
+
+namespace {
 
 OBB merge_smalldist(const OBB& b1, const OBB& b2) {
   OBB b;

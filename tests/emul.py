@@ -106,3 +106,13 @@ def tri_contact_batch(P, Qm):
     cnt = np.empty(n, np.int32); pts = np.empty((n, 2, 3)); nrm = np.empty((n, 3)); dep = np.empty(n)
     lib().emu_tri_contact_batch(C.c_int64(n), _p(P), _p(Qm), _p(cnt), _p(pts), _p(nrm), _p(dep))
     return cnt, pts, nrm, dep
+
+
+def translation_motion(beg, end, t):
+    """motion.cuh's TranslationMotion on the host: (n,3,4) transforms at times t."""
+    beg = np.ascontiguousarray(beg, np.float64).reshape(-1, 12)
+    end = np.ascontiguousarray(end, np.float64).reshape(-1, 12)
+    t = np.ascontiguousarray(t, np.float64)
+    out = np.empty((beg.shape[0], 3, 4))
+    lib().emu_translation_motion(C.c_int64(beg.shape[0]), _p(beg), _p(end), _p(t), _p(out))
+    return out

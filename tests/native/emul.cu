@@ -10,6 +10,7 @@
 #include "refit.cuh"
 #include "shape_pair.cuh"
 #include "tri_contact.cuh"
+#include "motion.cuh"
 
 using namespace fclgpu;
 
@@ -352,6 +353,11 @@ void emu_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* co
     normal[3 * i + 2] = nrm.z;
     depth[i] = d;
   }
+}
+
+// The product's translation motion (motion.cuh) on the host: n (beg, end, t) triples.
+void emu_translation_motion(int64_t n, const double* beg, const double* end, const double* t, double* out) {
+  for (int64_t i = 0; i < n; ++i) translation_motion_at(beg + 12 * i, end + 12 * i, t[i], out + 12 * i);
 }
 
 }  // extern "C"

@@ -1,0 +1,103 @@
+"""Continuous collision of mesh pairs on the GPU (fcl::continuousCollide, naive solver,
+translation motion) against the FP64 oracle: collision flags, times of contact and the
+transforms at the time of contact, bit for bit, through the host and device entry points
+and the fcl mirror."""
+import numpy as np
+import pytest
+
+from fcl_gb300 import api
+from fcl_gb300 import native as N
+from fcl_gb300 import workloads as W
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _meshes():
+    va, ta = W.perturbed_ellipsoid(10, (1, 0.7, 0.5), 0.01, 0)
+    vb, tb = W.perturbed_ellipsoid(8, (0.8, 0.56, 0.4), 0.01, 1)
+    return (va, ta), (vb, tb)
+
+
+def _motions(n, seed, both):
+    b0 = W.random_poses(n, -2.5, 2.5, seed)
+    b1 = b0.copy()
+    rng = np.random.default_rng(seed + 1)
+    b1[:, :, 3] += rng.normal(0, 1.0, (n, 3))
+    if not both:
+        return None, None, b0, b1
+    a0 = W.random_poses(n, -0.5, 0.5, seed + 3)
+    a1 = a0.copy()
+    a1[:, :, 3] += rng.normal(0, 1.0, (n, 3))
+    return a0, a1, b0, b1
+
+
+def _same(g, ref):
+    hit, toc, c1, c2 = ref
+    assert np.array_equal(np.asarray(g["is_collide"]), hit)
+    assert np.array_equal(np.asarray(g["time_of_contact"]), toc)
+    assert np.array_equal(np.asarray(g["contact_tf1"]).view(np.uint64), c1.view(np.uint64))
+    assert np.array_equal(np.asarray(g["contact_tf2"]).view(np.uint64), c2.view(np.uint64))
+
+
+@pytest.mark.parametrize("both", [False, True])
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("iters,toc_err", [(10, 1e-4), (10, 0.25), (0, 1e-4)])
+def test_ccd_matches_oracle(gpu_lib, both, prec, iters, toc_err):
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(700, 5, both)
+    ref = O.continuous_collide_batch(O.Mesh(va, ta), O.Mesh(vb, tb), b0, b1, a0, a1, num_max_iterations=iters,
+                                     toc_err=toc_err, nthreads=8)
+    g = api.continuous_collide_batch([A, B], [[0, 1]], a0, a1, b0, b1, num_max_iterations=iters, toc_err=toc_err,
+                                     precision=prec)
+    _same(g, ref)
+    if iters:
+        assert 0 < ref[0].sum() < len(b0)
+
+
+def test_ccd_device_entry_and_mixed_pairs(gpu_lib):
+    import torch
+    (va, ta), (vb, tb) = _meshes()
+    vc, tc = W.grid_box(4)
+    geo = [(va, ta), (vb, tb), (vc, tc)]
+    ms = [api.BVHModel.from_arrays(v, t) for v, t in geo]
+    os_ = [O.Mesh(v, t) for v, t in geo]
+    pairs = np.array([[0, 1], [2, 1], [0, 2]], np.int32)
+    a0, a1, b0, b1 = _motions(600, 9, True)
+    pq = np.random.default_rng(2).integers(0, 3, 600).astype(np.int32)
+    d = lambda x: torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    g = api.continuous_collide_batch(ms, pairs, d(a0), d(a1), d(b0), d(b1), pair_of_query=d(pq))
+    torch.cuda.synchronize()
+    g = {k: v.cpu().numpy() for k, v in g.items()}
+    for p in range(3):
+        sel = np.nonzero(pq == p)[0]
+        ref = O.continuous_collide_batch(os_[pairs[p, 0]], os_[pairs[p, 1]], b0[sel], b1[sel], a0[sel], a1[sel],
+                                         nthreads=8)
+        _same({k: v[sel] for k, v in g.items()}, ref)
+
+
+def test_ccd_rejects_what_fcl_cannot_run_here(gpu_lib):
+    (va, ta), (vb, tb) = _meshes()
+    ms = [api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)]
+    _, _, b0, b1 = _motions(4, 1, False)
+    for kw in ({"motion": "linear"}, {"solver": "conservative_advancement"}):
+        with pytest.raises(N.FclGpuError) as e:
+            api.continuous_collide_batch(ms, [[0, 1]], None, None, b0, b1, **kw)
+        assert e.value.code == N.FCLGPU_ERR_UNSUPPORTED
+    with pytest.raises(N.FclGpuError):   # one sample: FCL divides 0 by 0
+        api.continuous_collide_batch(ms, [[0, 1]], None, None, b0, b1, num_max_iterations=1)
+
+
+def test_continuous_collide_mirror(gpu_lib):
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(60, 21, True)
+    ref = O.continuous_collide_batch(O.Mesh(va, ta), O.Mesh(vb, tb), b0, b1, a0, a1)
+    for q in range(60):
+        res = api.ContinuousCollisionResult()
+        t = api.continuousCollide(api.CollisionObject(A, a0[q]), a1[q], api.CollisionObject(B, b0[q]), b1[q],
+                                  api.ContinuousCollisionRequest(), res)
+        assert t == ref[1][q] and res.is_collide == bool(ref[0][q])
+        if res.is_collide:
+            assert np.array_equal(res.contact_tf1, ref[2][q]) and np.array_equal(res.contact_tf2, ref[3][q])
