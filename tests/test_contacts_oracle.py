@@ -32,6 +32,15 @@ def test_tri_contact_known_answers():
     assert np.allclose(dep, 0.1, atol=1e-15)
 
 
+def _move(Q, tf):
+    """R Q + T with the oracle's summation order ((r0 x + r1 y) + r2 z) + t."""
+    R, T = tf[:, :3], tf[:, 3]
+    out = np.empty_like(Q)
+    for r in range(3):
+        out[..., r] = ((R[r, 0] * Q[..., 0] + R[r, 1] * Q[..., 1]) + R[r, 2] * Q[..., 2]) + T[r]
+    return out
+
+
 def _pairs(c, ct):
     off = np.concatenate([[0], np.cumsum(c)])
     return [ct[off[i]:off[i + 1]] for i in range(len(c))]
@@ -62,7 +71,7 @@ def test_contact_traversal_visits_the_same_pairs(kind):
     for q, (pairs, got) in enumerate(zip(_pairs(c, ct), _pairs(cc, ids))):
         # every intersecting pair, in DFS order, contributes its tri_contact count
         P = va[ta[pairs[:, 0]]]
-        Qm = vb[tb[pairs[:, 1]]] @ tf[q, :, :3].T + tf[q, :, 3]
+        Qm = _move(vb[tb[pairs[:, 1]]], tf[q])
         k, _, _, _ = O.tri_contact_batch(P, Qm)
         assert np.array_equal(np.repeat(pairs, k, axis=0), got)
         two += int((k == 2).sum())
@@ -107,3 +116,23 @@ def test_product_tri_contact_bit_exact(seed):
     for a, b in zip(ref[1:], got[1:]):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
     assert set(np.unique(ref[0])) >= {1, 2}
+
+
+@pytest.mark.parametrize("i", [0, 3, 7])
+def test_reference_fixture_contact_mode(golden, i):
+    """FCL's collision test runs with enable_contact = true and num_max_contacts = INT_MAX
+    (test_fcl_collision.cpp:74-75) and compares sorted contact lists across BV types; the
+    OBBRSS list here holds every intersecting triangle pair (the brute-force set) once per
+    contact point of the pair."""
+    env = O.Mesh(golden["env_v"], golden["env_t"])
+    rob = O.Mesh(golden["rob_v"], golden["rob_t"])
+    tf = golden["tf"][i]
+    cnt, ids, pos, nrm, dep = O.collide_contacts_batch(env, rob, tf[None], num_max_contacts=2 ** 31 - 1)
+    brute = O.brute_collide(env, rob, tf)
+    assert sorted(set(map(tuple, ids))) == sorted(map(tuple, brute))
+    P = golden["env_v"][golden["env_t"][ids[:, 0]]]
+    Qm = _move(golden["rob_v"][golden["rob_t"][ids[:, 1]]], tf)
+    k, _, _, d = O.tri_contact_batch(P, Qm)
+    uniq, first, mult = np.unique(ids, axis=0, return_index=True, return_counts=True)
+    assert np.array_equal(mult, k[first])
+    assert np.array_equal(dep, d) and np.all(dep >= -1e-5)
