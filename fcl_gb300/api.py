@@ -806,6 +806,33 @@ class DynamicAABBTreeCollisionManager:
 
 # ------------------------------------------------------------- request loop ----
 
+class NaiveCollisionManager(DynamicAABBTreeCollisionManager):
+    """FCL's brute-force manager (broadphase/broadphase_bruteforce.h).  The queries run on
+    the device tree; what they report (contact totals capped at num_max_contacts, the
+    colliding objects, the distance of queries in no contact) does not depend on the order
+    a manager meets the objects, so it equals the brute-force manager's answer."""
+
+
+class SaPCollisionManager(DynamicAABBTreeCollisionManager):
+    """FCL's sweep-and-prune manager (broadphase/broadphase_SaP.h), answered by the device
+    tree: same order-independent results (see NaiveCollisionManager)."""
+
+
+class SSaPCollisionManager(DynamicAABBTreeCollisionManager):
+    """FCL's simple sweep-and-prune manager (broadphase/broadphase_SSaP.h), answered by the
+    device tree: same order-independent results (see NaiveCollisionManager)."""
+
+
+class IntervalTreeCollisionManager(DynamicAABBTreeCollisionManager):
+    """FCL's interval-tree manager (broadphase/broadphase_interval_tree.h), answered by the
+    device tree: same order-independent results (see NaiveCollisionManager)."""
+
+
+class DynamicAABBTreeCollisionManager_Array(DynamicAABBTreeCollisionManager):
+    """FCL's array-backed dynamic AABB tree (broadphase/broadphase_dynamic_AABB_tree_array.h),
+    answered by the device tree: same order-independent results (see NaiveCollisionManager)."""
+
+
 class MotionServer:
     """Continuous-batching loop of motion-checking requests over a resident
     broadphase scene (fclgpu_server_*).  robot: workloads.Robot-like (axis, offset,

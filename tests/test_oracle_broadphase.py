@@ -136,3 +136,17 @@ def test_tree_manager_matches_naive_manager_mixed():
     sep = db["dist"] > 0
     np.testing.assert_array_equal(da["dist"] <= 0, db["dist"] <= 0)
     np.testing.assert_array_equal(da["dist"][sep], db["dist"][sep])
+
+
+def test_other_manager_names_answer_like_the_tree():
+    """FCL's other BroadPhaseCollisionManager implementations are offered under their names
+    and answered by the device tree: the results the device manager reports are
+    order-independent, so the tree and the brute-force manager agree (checked above on
+    the oracle); the classes keep the manager interface."""
+    from fcl_gb300 import api
+    for name in ("NaiveCollisionManager", "SaPCollisionManager", "SSaPCollisionManager",
+                 "IntervalTreeCollisionManager", "DynamicAABBTreeCollisionManager_Array"):
+        cls = getattr(api, name)
+        assert issubclass(cls, api.DynamicAABBTreeCollisionManager)
+        for m in ("registerObjects", "setup", "update", "collide_batch", "distance_batch", "size"):
+            assert callable(getattr(cls, m))
