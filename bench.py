@@ -70,9 +70,16 @@ def _sum_over_ranks(x: float, device, world: int) -> float:
     return float(t.item())
 
 
+_WORKLOADS = {}
+
+
 def _workload(args, rank):
+    """The C1 workload of this rank (generated once per process)."""
     from fcl_gb300 import workloads as W
-    return W.config1(scale=args.scale, seed=1 + 1000 * rank, n_pairs=args.pairs, tri_hi=args.tri_hi)
+    key = (args.scale, rank, args.pairs, args.tri_hi)
+    if key not in _WORKLOADS:
+        _WORKLOADS[key] = W.config1(scale=args.scale, seed=1 + 1000 * rank, n_pairs=args.pairs, tri_hi=args.tri_hi)
+    return _WORKLOADS[key]
 
 
 # ------------------------------------------------------------------------------------
