@@ -294,7 +294,7 @@ FCLGPU_API int fclgpu_last_kernel_time(double* ms);
 FCLGPU_API int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps, int32_t variant);
 FCLGPU_API int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps, int32_t* variant);
 
-/* ---- convex shapes (fcl::Box/Sphere/Capsule/Cylinder/Cone/Convex, geometry/shape/*.h) --
+/* ---- convex shapes (fcl::Box/Sphere/Capsule/Cylinder/Cone/Convex, geometry/shape/ headers) --
  * GJK/EPA of FCL's own solver (GJKSolver_indep, narrowphase/detail/gjk_solver_indep.h)
  * with its closed-form pairs; replaces fcl::collide / fcl::distance on shape pairs
  * (collision_func_matrix-inl.h:278-311, distance_func_matrix-inl.h:207-226). */

@@ -32,3 +32,18 @@ def test_status_strings_without_gpu():
     L = N.lib()
     assert L.fclgpu_status_string(0) == b"ok"
     assert L.fclgpu_status_string(-4) == b"output capacity too small"
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/fclgpu.h is a C header: it compiles as C99 with warnings as errors."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    src = tmp_path / "t.c"
+    src.write_text('#include "fclgpu.h"\nint main(void) { return FCLGPU_OK; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
