@@ -330,7 +330,8 @@ class ContinuousCollisionResult:
 def continuous_collide_batch(meshes, pairs, tf1_beg, tf1_end, tf2_beg, tf2_end, pair_of_query=None,
                              num_max_iterations=10, toc_err=1e-4, motion="trans", solver="naive", precision="fp32",
                              stream=None):
-    """Batched fcl::continuousCollide on mesh pairs (naive solver, translation motion).
+    """Batched fcl::continuousCollide on mesh pairs (naive solver; motion "trans" (FCL's
+    default), "linear" or "screw").
     Returns is_collide (n,), time_of_contact (n,), contact_tf1/contact_tf2 (n,3,4; zero
     where no collision).  numpy inputs use the host entry point, torch CUDA tensors the
     device one."""

@@ -784,7 +784,7 @@ int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, const
   return FCLGPU_OK;
 }
 
-// ---- continuous collide (naive solver, translation motion) -------------------------
+// ---- continuous collide (naive solver; translation, linear or screw motion) --------
 namespace {
 struct CcdScratch {
   DevBuf tfa, tfb, pq, counts, offsets, in_pq, in_a0, in_a1, in_b0, in_b1, out_hit, out_toc, out_tf1, out_tf2;
@@ -794,8 +794,9 @@ CcdScratch g_ccd;
 int ccd_samples(const fclgpu_ccd_request* req, int64_t* n_iter) {
   if (req->solver_type != FCLGPU_CCDC_NAIVE)
     return fail(FCLGPU_ERR_UNSUPPORTED, "only the naive continuous-collision solver is on the GPU path");
-  if (req->motion_type != FCLGPU_CCDM_TRANS)
-    return fail(FCLGPU_ERR_UNSUPPORTED, "only the translation motion is on the GPU path");
+  if (req->motion_type != FCLGPU_CCDM_TRANS && req->motion_type != FCLGPU_CCDM_LINEAR &&
+      req->motion_type != FCLGPU_CCDM_SCREW)
+    return fail(FCLGPU_ERR_UNSUPPORTED, "the spline motion is not on the GPU path");
   if (req->num_max_iterations < 0 || !(req->toc_err > 0))
     return fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_iterations must be >= 0 and toc_err > 0");
   // continuous_collision-inl.h:144: min(num_max_iterations, (size_t)ceil(1 / toc_err))
@@ -839,6 +840,7 @@ int fclgpu_continuous_collide_batch_device(const fclgpu_mesh* meshes, int32_t nu
   L.tf2_end = tf2_end;
   L.n = n;
   L.n_iter = n_iter;
+  L.motion = req->motion_type;
   L.is_collide = res->is_collide;
   L.toc = res->time_of_contact;
   L.contact_tf1 = res->contact_tf1;

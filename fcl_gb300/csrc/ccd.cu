@@ -1,11 +1,9 @@
 // Continuous collision of mesh pairs, FCL's default solver: continuousCollideNaive
-// (narrowphase/continuous_collision-inl.h:134-171) with the default motion,
-// TranslationMotion (math/motion/translation_motion-inl.h).  FCL samples the motion at
+// (narrowphase/continuous_collision-inl.h:134-171) with the translation (default), linear
+// or screw motion (math/motion/, motion.cuh).  FCL samples the motion at
 // n_iter = min(num_max_iterations, ceil(1 / toc_err)) times t_i = i / (n_iter - 1) and
 // returns the first t_i at which the discrete collide() (default request: one contact)
-// reports a collision.  The translation motion keeps the start rotation as a quaternion
-// and turns it back into a matrix at every step (Quaternion(R) and toRotationMatrix(),
-// Eigen's formulas); the translation is start + (end - start) * t.
+// reports a collision.
 //
 // On the device every (query, sample) pair becomes one query of the collide batch:
 // k_ccd_poses writes the sampled transforms, the batch runs with num_max_contacts = 1,
@@ -38,8 +36,8 @@ __global__ void k_ccd_poses(CcdLaunch L) {
       b0[j] = __ldg(L.tf2_beg + 12 * q + j);
       b1[j] = __ldg(L.tf2_end + 12 * q + j);
     }
-    translation_motion_at(a0, a1, t, L.tfa + 12 * k);
-    translation_motion_at(b0, b1, t, L.tfb + 12 * k);
+    motion_at(L.motion, a0, a1, t, L.tfa + 12 * k);
+    motion_at(L.motion, b0, b1, t, L.tfb + 12 * k);
     L.pq_expanded[k] = L.pair_of_query ? __ldg(L.pair_of_query + q) : 0;
   }
 }

@@ -114,7 +114,7 @@ cudaError_t launch_contact_counts(const ContactLaunch& L, const int32_t* pair_co
 cudaError_t launch_contact_emit(const ContactLaunch& L, const int64_t* out_off, int32_t* ids, double* pos,
                                 double* normal, double* depth, cudaStream_t s);
 
-// Continuous collide (naive solver, translation motion): sampled poses of every query,
+// Continuous collide (naive solver): sampled poses of every query,
 // then the first colliding sample; see ccd.cu.
 struct CcdLaunch {
   const int32_t* pair_of_query;
@@ -124,6 +124,7 @@ struct CcdLaunch {
   const double* tf2_end;
   int64_t n;                 // queries
   int64_t n_iter;            // samples per query (>= 2)
+  int32_t motion;            // MOTION_TRANS / MOTION_LINEAR / MOTION_SCREW (motion.cuh)
   double* tfa;               // n * n_iter sampled transforms of object 1 (12 doubles)
   double* tfb;               // ... of object 2
   int32_t* pq_expanded;      // n * n_iter pair indices

@@ -20,7 +20,7 @@
  *   fclgpu_collide_contacts*  fcl::collide(...) with enable_contact (contact position,
  *                           normal, depth; mesh_collision_traversal_node-inl.h:579-600)
  *   fclgpu_continuous_collide_batch*  fcl::continuousCollide(...) on BVHModel<OBBRSS>
- *                           pairs, naive solver, translation motion
+ *                           pairs, naive solver, translation / linear / screw motion
  *                           (narrowphase/continuous_collision-inl.h:134-171, 436-451)
  *   fclgpu_distance_batch*  fcl::distance(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/distance.h:51-62, distance-inl.h:71-246)
@@ -193,13 +193,16 @@ FCLGPU_API int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_me
 
 /* Continuous collision of mesh pairs: fcl::continuousCollide(o1, tf1_beg, tf1_end, o2,
  * tf2_beg, tf2_end, request, result) (narrowphase/continuous_collision-inl.h:436-451) with
- * the request's default solver CCDC_NAIVE (:134-171) and default motion CCDM_TRANS
- * (math/motion/translation_motion-inl.h): the motion is sampled at
+ * the request's default solver CCDC_NAIVE (:134-171) and the motion CCDM_TRANS (default,
+ * math/motion/translation_motion-inl.h), CCDM_LINEAR (interp_motion-inl.h, reference point
+ * at the origin: FCL's two-transform constructor leaves it unset) or CCDM_SCREW
+ * (screw_motion-inl.h): the motion is sampled at
  * n_iter = min(num_max_iterations, ceil(1/toc_err)) times t_i = i/(n_iter-1), each sample is
  * a discrete collide with the default CollisionRequest, and the first colliding t_i is the
  * time of contact (1 and no collision otherwise).  n_iter must be 0 (no sample: no
- * collision) or >= 2 (FCL divides 0 by 0 at n_iter = 1).  Other solvers and motions return
- * FCLGPU_ERR_UNSUPPORTED.  tf1_beg/tf1_end may both be NULL (identity).  Outputs per query:
+ * collision) or >= 2 (FCL divides 0 by 0 at n_iter = 1).  The linear and screw motions use
+ * sin/cos/tan/atan2, whose device results differ from a host's in the last bits.  Other
+ * solvers and the spline motion return FCLGPU_ERR_UNSUPPORTED.  tf1_beg/tf1_end may both be NULL (identity).  Outputs per query:
  * is_collide, time_of_contact, and for colliding queries contact_tf1/contact_tf2 (the
  * sampled transforms at the time of contact, 12 doubles each; other entries are left
  * unchanged).  "_device": device pointers, plain: host pointers; both synchronise. */
@@ -210,7 +213,7 @@ enum { FCLGPU_CCDC_NAIVE = 0, FCLGPU_CCDC_CONSERVATIVE_ADVANCEMENT = 1, FCLGPU_C
 typedef struct {
   int64_t num_max_iterations; /* ContinuousCollisionRequest::num_max_iterations (10) */
   double toc_err;             /* ::toc_err (1e-4) */
-  int32_t motion_type;        /* ::ccd_motion_type (FCLGPU_CCDM_TRANS) */
+  int32_t motion_type;        /* ::ccd_motion_type (FCLGPU_CCDM_TRANS, _LINEAR or _SCREW) */
   int32_t solver_type;        /* ::ccd_solver_type (FCLGPU_CCDC_NAIVE) */
   int32_t precision;          /* form of the discrete collides */
   int32_t reserved;

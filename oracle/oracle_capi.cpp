@@ -180,13 +180,13 @@ void orc_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* co
   }
 }
 
-// Batched fcl::continuousCollide (naive solver, translation motion) over n motions of
+// Batched fcl::continuousCollide (naive solver; motion 0 translation, 1 linear, 2 screw) over n motions of
 // one mesh pair: tf1_beg/tf1_end may be NULL (identity).  Outputs per motion: hit,
 // time of contact, the transforms at the time of contact (12 doubles each; untouched
 // when there is no collision).
 void orc_ccd_batch(void* h1, void* h2, int64_t n, const double* a0, const double* a1, const double* b0,
-                   const double* b1, int64_t num_max_iterations, double toc_err, int nthreads, int* hit, double* toc,
-                   double* ctf1, double* ctf2) {
+                   const double* b1, int64_t num_max_iterations, double toc_err, int motion, int nthreads, int* hit,
+                   double* toc, double* ctf1, double* ctf2) {
   const Mesh* m1 = static_cast<Mesh*>(h1);
   const Mesh* m2 = static_cast<Mesh*>(h2);
   parallel_for(n, nthreads, [&](int64_t i, int) {
@@ -195,7 +195,8 @@ void orc_ccd_batch(void* h1, void* h2, int64_t n, const double* a0, const double
     Tf tb0 = load_tf(b0 + 12 * i), tb1 = load_tf(b1 + 12 * i);
     Tf ca, cb;
     double t;
-    bool h = continuous_collide_naive(*m1, ta0, ta1, *m2, tb0, tb1, (size_t)num_max_iterations, toc_err, t, ca, cb);
+    bool h = continuous_collide_naive(*m1, ta0, ta1, *m2, tb0, tb1, (size_t)num_max_iterations, toc_err, motion, t,
+                                      ca, cb);
     hit[i] = h ? 1 : 0;
     toc[i] = t;
     if (h) {

@@ -97,11 +97,12 @@ size_t collide_mesh_contacts(const Mesh& m1, const Tf& tf1, const Mesh& m2, cons
 // the contact part of intersect_Triangle on P and Qm (Q moved into P's frame)
 int tri_contact_info(const V3 P[3], const V3 Qm[3], V3 cp[2], V3& normal, double& depth);
 
-// fcl::continuousCollide with the naive solver and the translation motion; toc = time of
+// fcl::continuousCollide with the naive solver and the translation (0), linear (1) or
+// screw (2) motion; toc = time of
 // contact (1 without collision), ca / cb = the sampled transforms at that time.
 bool continuous_collide_naive(const Mesh& m1, const Tf& a0, const Tf& a1, const Mesh& m2, const Tf& b0,
-                              const Tf& b1, size_t num_max_iterations, double toc_err, double& toc, Tf& ca,
-                              Tf& cb);
+                              const Tf& b1, size_t num_max_iterations, double toc_err, int motion, double& toc,
+                              Tf& ca, Tf& cb);
 
 struct DistanceOut {
   double min_distance;

@@ -46,8 +46,8 @@ def lib():
         L.orc_collide_contacts_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64,
                                                  C.c_int, _i64p, _ip, _dp, _dp, _dp, C.c_int64]
         L.orc_ccd_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, C.c_int64, C.c_double,
-                                    C.c_int, _ip, _dp, _dp, _dp]
-        L.orc_translation_motion.argtypes = [C.c_int64, _dp, _dp, _dp, _dp]
+                                    C.c_int, C.c_int, _ip, _dp, _dp, _dp]
+        L.orc_motion.argtypes = [C.c_int, C.c_int64, _dp, _dp, _dp, _dp]
         L.orc_tri_contact_batch.argtypes = [C.c_int64, _dp, _dp, _ip, _dp, _dp, _dp]
         L.orc_distance_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int, C.c_int,
                                          _dp, _ip, _dp, _i64p, _i64p]
@@ -153,9 +153,13 @@ def collide_contacts_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray 
         cap = int(total)
 
 
+_MOTIONS = {"trans": 0, "linear": 1, "screw": 2}
+
+
 def continuous_collide_batch(m1: Mesh, m2: Mesh, tf2_beg, tf2_end, tf1_beg=None, tf1_end=None,
-                             num_max_iterations: int = 10, toc_err: float = 1e-4, nthreads: int = 1):
-    """fcl::continuousCollide, naive solver, translation motion.  Returns (hit, toc,
+                             num_max_iterations: int = 10, toc_err: float = 1e-4, nthreads: int = 1,
+                             motion: str = "trans"):
+    """fcl::continuousCollide, naive solver, translation / linear / screw motion.  Returns (hit, toc,
     contact_tf1 (n,3,4), contact_tf2 (n,3,4)); the transforms are zero where no hit."""
     b0 = np.ascontiguousarray(tf2_beg, np.float64).reshape(-1, 12)
     b1 = np.ascontiguousarray(tf2_end, np.float64).reshape(-1, 12)
@@ -167,18 +171,24 @@ def continuous_collide_batch(m1: Mesh, m2: Mesh, tf2_beg, tf2_end, tf1_beg=None,
     c1 = np.zeros((n, 3, 4))
     c2 = np.zeros((n, 3, 4))
     lib().orc_ccd_batch(m1.h, m2.h, n, None if a0 is None else _d(a0), None if a1 is None else _d(a1), _d(b0),
-                        _d(b1), num_max_iterations, toc_err, nthreads, _i(hit), _d(toc), _d(c1), _d(c2))
+                        _d(b1), num_max_iterations, toc_err, _MOTIONS[motion], nthreads, _i(hit), _d(toc), _d(c1),
+                        _d(c2))
     return hit, toc, c1, c2
 
 
-def translation_motion(beg, end, t):
-    """TranslationMotion(beg, end) at times t: (n,3,4) transforms."""
+def motion(beg, end, t, kind: str = "trans"):
+    """TranslationMotion / InterpMotion / ScrewMotion(beg, end) at times t: (n,3,4)."""
     beg = np.ascontiguousarray(beg, np.float64).reshape(-1, 12)
     end = np.ascontiguousarray(end, np.float64).reshape(-1, 12)
     t = np.ascontiguousarray(t, np.float64)
     out = np.empty((beg.shape[0], 3, 4))
-    lib().orc_translation_motion(beg.shape[0], _d(beg), _d(end), _d(t), _d(out))
+    lib().orc_motion(_MOTIONS[kind], beg.shape[0], _d(beg), _d(end), _d(t), _d(out))
     return out
+
+
+def translation_motion(beg, end, t):
+    """TranslationMotion(beg, end) at times t: (n,3,4) transforms."""
+    return motion(beg, end, t, "trans")
 
 
 def tri_contact_batch(P: np.ndarray, Qm: np.ndarray):

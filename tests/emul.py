@@ -108,11 +108,16 @@ def tri_contact_batch(P, Qm):
     return cnt, pts, nrm, dep
 
 
-def translation_motion(beg, end, t):
-    """motion.cuh's TranslationMotion on the host: (n,3,4) transforms at times t."""
+def motion(beg, end, t, kind="trans"):
+    """motion.cuh's motions on the host: (n,3,4) transforms at times t."""
     beg = np.ascontiguousarray(beg, np.float64).reshape(-1, 12)
     end = np.ascontiguousarray(end, np.float64).reshape(-1, 12)
     t = np.ascontiguousarray(t, np.float64)
     out = np.empty((beg.shape[0], 3, 4))
-    lib().emu_translation_motion(C.c_int64(beg.shape[0]), _p(beg), _p(end), _p(t), _p(out))
+    lib().emu_motion(C.c_int({"trans": 0, "linear": 1, "screw": 2}[kind]), C.c_int64(beg.shape[0]), _p(beg),
+                     _p(end), _p(t), _p(out))
     return out
+
+
+def translation_motion(beg, end, t):
+    return motion(beg, end, t, "trans")

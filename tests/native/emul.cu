@@ -355,9 +355,10 @@ void emu_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* co
   }
 }
 
-// The product's translation motion (motion.cuh) on the host: n (beg, end, t) triples.
-void emu_translation_motion(int64_t n, const double* beg, const double* end, const double* t, double* out) {
-  for (int64_t i = 0; i < n; ++i) translation_motion_at(beg + 12 * i, end + 12 * i, t[i], out + 12 * i);
+// The product's motions (motion.cuh) on the host: n (beg, end, t) triples; type 0
+// translation, 1 linear, 2 screw.
+void emu_motion(int type, int64_t n, const double* beg, const double* end, const double* t, double* out) {
+  for (int64_t i = 0; i < n; ++i) motion_at(type, beg + 12 * i, end + 12 * i, t[i], out + 12 * i);
 }
 
 }  // extern "C"

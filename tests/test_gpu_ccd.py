@@ -1,7 +1,8 @@
-"""Continuous collision of mesh pairs on the GPU (fcl::continuousCollide, naive solver,
-translation motion) against the FP64 oracle: collision flags, times of contact and the
-transforms at the time of contact, bit for bit, through the host and device entry points
-and the fcl mirror."""
+"""Continuous collision of mesh pairs on the GPU (fcl::continuousCollide, naive solver)
+against the FP64 oracle: with the translation motion the collision flags, times of contact
+and the transforms at the time of contact bit for bit, through the host and device entry
+points and the fcl mirror; with the linear and screw motions the flags and times exactly and
+the transforms to 1e-12."""
 import numpy as np
 import pytest
 
@@ -56,6 +57,24 @@ def test_ccd_matches_oracle(gpu_lib, both, prec, iters, toc_err):
         assert 0 < ref[0].sum() < len(b0)
 
 
+@pytest.mark.parametrize("kind", ["linear", "screw"])
+def test_ccd_rotating_motions(gpu_lib, kind):
+    """The linear and screw motions call sin/cos/tan/atan2, whose device results differ
+    from the host's in the last bits: the sampled transforms agree with the oracle's to
+    1e-12, the collision flags and times of contact exactly (no sampled pose of this
+    workload lies within rounding of touching)."""
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(700, 31, True)
+    b1[:, :, :3] = W.random_poses(700, 0, 0, 32)[:, :, :3]
+    ref = O.continuous_collide_batch(O.Mesh(va, ta), O.Mesh(vb, tb), b0, b1, a0, a1, nthreads=8, motion=kind)
+    g = api.continuous_collide_batch([A, B], [[0, 1]], a0, a1, b0, b1, motion=kind)
+    assert np.array_equal(g["is_collide"], ref[0]) and np.array_equal(g["time_of_contact"], ref[1])
+    assert np.allclose(g["contact_tf1"], ref[2], rtol=0, atol=1e-12)
+    assert np.allclose(g["contact_tf2"], ref[3], rtol=0, atol=1e-12)
+    assert 0 < ref[0].sum() < 700
+
+
 def test_ccd_device_entry_and_mixed_pairs(gpu_lib):
     import torch
     (va, ta), (vb, tb) = _meshes()
@@ -81,7 +100,7 @@ def test_ccd_rejects_what_fcl_cannot_run_here(gpu_lib):
     (va, ta), (vb, tb) = _meshes()
     ms = [api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)]
     _, _, b0, b1 = _motions(4, 1, False)
-    for kw in ({"motion": "linear"}, {"solver": "conservative_advancement"}):
+    for kw in ({"motion": "spline"}, {"solver": "conservative_advancement"}):
         with pytest.raises(N.FclGpuError) as e:
             api.continuous_collide_batch(ms, [[0, 1]], None, None, b0, b1, **kw)
         assert e.value.code == N.FCLGPU_ERR_UNSUPPORTED
