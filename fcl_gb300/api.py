@@ -127,6 +127,55 @@ class BVHModel:
             self.vertices = V
         self.build_state = "updated"
 
+    # geometry/bvh/BVH_model-inl.h:521-620
+    def beginReplaceModel(self) -> int:
+        if self.build_state not in ("processed", "updated"):
+            return -10  # BVH_ERR_BUILD_EMPTY_PREVIOUS_FRAME
+        self._upd = []
+        self._nupd = 0
+        self.build_state = "replace_begun"
+        return 0
+
+    def replaceVertex(self, p) -> int:
+        return self.replaceSubModel(np.asarray(p, np.float64).reshape(1, 3))
+
+    def replaceTriangle(self, p1, p2, p3) -> int:
+        return self.replaceSubModel(np.array([p1, p2, p3], np.float64))
+
+    def replaceSubModel(self, ps) -> int:
+        if self.build_state != "replace_begun":
+            return -8  # BVH_ERR_BUILD_OUT_OF_SEQUENCE
+        v = np.ascontiguousarray(ps, dtype=np.float64).reshape(-1, 3)
+        self._upd.append(v)
+        self._nupd += v.shape[0]
+        return 0
+
+    def endReplaceModel(self, refit: bool = True, bottomup: bool = True) -> int:
+        """The default (refit = True, bottomup = True) is the GPU bottom-up refit without a
+        previous frame; a rebuild or a top-down refit is not on the GPU path."""
+        if self.build_state != "replace_begun":
+            return -8
+        if not (refit and bottomup):
+            raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "endReplaceModel", "only the bottom-up refit")
+        V = np.concatenate(self._upd) if self._upd else np.zeros((0, 3))
+        if V.shape[0] != self.num_vertices:
+            return -7  # BVH_ERR_INCORRECT_DATA
+        self.replace_vertices(V)
+        return 0
+
+    def replace_vertices(self, vertices, stream=None) -> None:
+        """beginReplaceModel + replaceVertex for all vertices + endReplaceModel() at once:
+        numpy (host) or a CUDA torch tensor (device), (nv, 3) float64."""
+        if hasattr(vertices, "data_ptr"):
+            N.check(N.lib().fclgpu_mesh_replace_device(self.handle, vertices.data_ptr(), vertices.shape[0], 1,
+                                                       stream), "fclgpu_mesh_replace_device")
+        else:
+            V = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
+            N.check(N.lib().fclgpu_mesh_replace(self.handle, V.ctypes.data, V.shape[0], 1, stream),
+                    "fclgpu_mesh_replace")
+            self.vertices = V
+        self.build_state = "processed"
+
     @classmethod
     def from_arrays(cls, vertices, triangles) -> "BVHModel":
         m = cls()

@@ -39,13 +39,18 @@ __global__ void k_refit_leaves(DevMesh m, const double* prev, NodeD* nodes, RssD
     if (child >= 0) continue;
     const int t = -(child + 1);
     const int i0 = m.tris[3 * t], i1 = m.tris[3 * t + 1], i2 = m.tris[3 * t + 2];
-    const D3v v[6] = {vtx(prev, i0), vtx(prev, i1), vtx(prev, i2),
-                      vtx(m.verts64, i0), vtx(m.verts64, i1), vtx(m.verts64, i2)};
-    auto pts = [&](int i) { return v[i]; };
     NodeD nd;
     RssD rs;
-    fit_points_bv(pts, 6, nd, rs.To, rs.l, rs.r);
-    for (int k = 0; k < 9; ++k) rs.axis[k] = nd.axis[k];
+    if (prev) {  // both frames: fit over six points (fitn)
+      const D3v v[6] = {vtx(prev, i0), vtx(prev, i1), vtx(prev, i2),
+                        vtx(m.verts64, i0), vtx(m.verts64, i1), vtx(m.verts64, i2)};
+      auto pts = [&](int i) { return v[i]; };
+      fit_points_bv(pts, 6, nd, rs.To, rs.l, rs.r);
+      for (int k = 0; k < 9; ++k) rs.axis[k] = nd.axis[k];
+    } else {     // no previous frame (replaced model): fit3
+      const D3v v[3] = {vtx(m.verts64, i0), vtx(m.verts64, i1), vtx(m.verts64, i2)};
+      fit3_obbrss(v, nd, rs);
+    }
     nd.child = child;
     nodes[b] = nd;
     rss[b] = rs;
@@ -126,8 +131,10 @@ int refit_cuda(cudaError_t e, const char* where) {
   return e == cudaErrorMemoryAllocation ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
 }
 
-// verts: device pointer with the new positions (3 doubles per vertex)
-int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s) {
+// verts: device pointer with the new positions (3 doubles per vertex).  replace = false:
+// update (the current frame becomes the previous one, leaves fit both frames); true:
+// replace (FCL drops the previous frame, leaves fit the new triangle alone).
+int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool replace) {
   DevMesh& d = m->dev;
   const size_t vbytes = sizeof(double) * 3 * (size_t)d.n_verts;
   cudaError_t e = cudaSuccess;
@@ -144,12 +151,14 @@ int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s) {
   double* cur = const_cast<double*>(d.verts64);
   // beginUpdateModel: the current frame becomes the previous one; updateVertex: the new
   // positions become the current frame
-  if ((e = cudaMemcpyAsync(m->prev_verts, cur, vbytes, cudaMemcpyDeviceToDevice, s))) return refit_cuda(e, "frames");
+  if (!replace && (e = cudaMemcpyAsync(m->prev_verts, cur, vbytes, cudaMemcpyDeviceToDevice, s)))
+    return refit_cuda(e, "frames");
   if ((e = cudaMemcpyAsync(cur, verts, vbytes, cudaMemcpyDeviceToDevice, s))) return refit_cuda(e, "frames");
   if ((e = cudaMemsetAsync(m->bounds, 0, 4 * sizeof(unsigned long long), s))) return refit_cuda(e, "bounds");
   NodeD* nodes = const_cast<NodeD*>(d.nodes64);
   RssD* rss = const_cast<RssD*>(d.rss64);
-  k_refit_leaves<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, (const double*)m->prev_verts, nodes, rss);
+  k_refit_leaves<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, replace ? nullptr : (const double*)m->prev_verts,
+                                                           nodes, rss);
   ++g_kernel_launches;
   for (size_t l = m->level_off.size() - 1; l-- > 0;) {  // deepest level first
     const int64_t a = m->level_off[l], b = m->level_off[l + 1];
@@ -185,15 +194,16 @@ int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s) {
 
 extern "C" {
 
-int fclgpu_mesh_update_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream) {
+namespace {
+int move_vertices_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace) {
   if (!mesh || !verts) return refit_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   if (nv != mesh->dev.n_verts)
     return refit_fail(FCLGPU_ERR_INCORRECT_DATA, "the updated model must have the same number of vertices");
   std::lock_guard<std::mutex> lk(g_refit_mu);
-  return refit_from_device(mesh, verts, (cudaStream_t)stream);
+  return refit_from_device(mesh, verts, (cudaStream_t)stream, replace);
 }
 
-int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream) {
+int move_vertices_host(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace) {
   if (!mesh || !verts) return refit_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   if (nv != mesh->dev.n_verts)
     return refit_fail(FCLGPU_ERR_INCORRECT_DATA, "the updated model must have the same number of vertices");
@@ -204,10 +214,29 @@ int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* 
   cudaError_t e = cudaMalloc(&staging, vbytes);
   if (e != cudaSuccess) return refit_cuda(e, "staging");
   e = cudaMemcpyAsync(staging, verts, vbytes, cudaMemcpyHostToDevice, s);
-  int rc = e == cudaSuccess ? refit_from_device(mesh, staging, s) : refit_cuda(e, "h2d");
+  int rc = e == cudaSuccess ? refit_from_device(mesh, staging, s, replace) : refit_cuda(e, "h2d");
   cudaStreamSynchronize(s);
   cudaFree(staging);
   return rc;
+}
+}  // namespace
+
+int fclgpu_mesh_update_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream) {
+  return move_vertices_device(mesh, verts, nv, stream, false);
+}
+
+int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream) {
+  return move_vertices_host(mesh, verts, nv, stream, false);
+}
+
+int fclgpu_mesh_replace_device(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
+  if (!refit) return refit_fail(FCLGPU_ERR_UNSUPPORTED, "endReplaceModel(refit = false) rebuilds on the host");
+  return move_vertices_device(mesh, verts, nv, stream, true);
+}
+
+int fclgpu_mesh_replace(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
+  if (!refit) return refit_fail(FCLGPU_ERR_UNSUPPORTED, "endReplaceModel(refit = false) rebuilds on the host");
+  return move_vertices_host(mesh, verts, nv, stream, true);
 }
 
 }  // extern "C"

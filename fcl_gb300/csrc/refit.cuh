@@ -148,6 +148,36 @@ FCLG_HD NodeD obb_merge_smalldist(const NodeD& b1, const NodeD& b2) {
   return b;
 }
 
+// Eigen's normalized(): v / |v| when |v|^2 > 0, else v
+FCLG_HD D3v eigen_normalized(const D3v& v) {
+  const double z = sqnorm(v);
+  if (z > 0) {
+    const double n = sqrt(z);
+    return v3(v.x / n, v.y / n, v.z / n);
+  }
+  return v;
+}
+
+// fit<OBBRSS>(ps, 3) of a leaf refitted without a previous frame (after
+// beginReplaceModel): OBB fit3 and RSS fit3 (math/bv/utility-inl.h:92-119, 208-233) share
+// the axes (third = normalised e0 x e1, first = the longest edge normalised, second =
+// third x first); then the extent / centre and the RSS rectangle of the three points.
+FCLG_HD void fit3_obbrss(const D3v p[3], NodeD& obb, RssD& rss) {
+  const D3v e[3] = {p[0] - p[1], p[1] - p[2], p[2] - p[0]};
+  const double len[3] = {sqnorm(e[0]), sqnorm(e[1]), sqnorm(e[2])};
+  int imax = 0;
+  if (len[1] > len[0]) imax = 1;
+  if (len[2] > len[imax]) imax = 2;
+  const D3v a2 = eigen_normalized(cross(e[0], e[1]));
+  const D3v a0 = eigen_normalized(e[imax]);
+  const D3v ax[3] = {a0, cross(a2, a0), a2};
+  set_axis9(obb.axis, ax);
+  auto pts = [&](int i) { return p[i]; };
+  extent_center_of(pts, 3, ax, obb.To, obb.ext);
+  for (int k = 0; k < 9; ++k) rss.axis[k] = obb.axis[k];
+  rss_fit_of(pts, 3, ax, rss.To, rss.l, rss.r);
+}
+
 // OBB::operator+
 FCLG_HD NodeD obb_merge(const NodeD& a, const NodeD& b) {
   const D3v cd = v3(a.To[0] - b.To[0], a.To[1] - b.To[1], a.To[2] - b.To[2]);

@@ -140,6 +140,8 @@ _SIGS = {
     "fclgpu_mesh_get_nodes": (C.c_int, [_VP, _VP, _VP]),
     "fclgpu_mesh_update": (C.c_int, [_VP, _VP, C.c_int64, _VP]),
     "fclgpu_mesh_update_device": (C.c_int, [_VP, _VP, C.c_int64, _VP]),
+    "fclgpu_mesh_replace": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP]),
+    "fclgpu_mesh_replace_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP]),
     "fclgpu_collide_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                               C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
     "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,

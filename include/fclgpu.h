@@ -15,6 +15,8 @@
  *                           (geometry/bvh/BVH_model-inl.h:207-517), MEAN split
  *   fclgpu_mesh_update*     BVHModel<OBBRSS<double>>::beginUpdateModel/updateVertex/
  *                           endUpdateModel() (BVH_model-inl.h:624-727, 961-1027)
+ *   fclgpu_mesh_replace*    BVHModel<OBBRSS<double>>::beginReplaceModel/replaceVertex/
+ *                           endReplaceModel(true, true) (BVH_model-inl.h:521-620)
  *   fclgpu_collide_batch*   fcl::collide(...) on BVHModel<OBBRSS> pairs
  *                           (narrowphase/collision.h:55-66, collision-inl.h:79-207)
  *   fclgpu_collide_contacts*  fcl::collide(...) with enable_contact (contact position,
@@ -109,6 +111,17 @@ FCLGPU_API int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t*
  * vertex.  Synchronises the stream. */
 FCLGPU_API int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
 FCLGPU_API int fclgpu_mesh_update_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
+
+/* Replaces the mesh's vertices: BVHModel::beginReplaceModel + replaceVertex (all
+ * vertices, in order) + endReplaceModel(refit, bottomup = true) (BVH_model-inl.h:521-620,
+ * 961-1027).  FCL drops the previous frame here, so each leaf is refitted to its new
+ * triangle alone (fit3 of OBB and RSS), the internal nodes as in fclgpu_mesh_update; a
+ * later update uses these vertices as its previous frame.  refit = 0 (rebuild the tree)
+ * returns FCLGPU_ERR_UNSUPPORTED: create a new mesh instead.  Synchronises the stream. */
+FCLGPU_API int fclgpu_mesh_replace(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit,
+                                   void* stream);
+FCLGPU_API int fclgpu_mesh_replace_device(fclgpu_mesh mesh, const double* verts, int64_t nv,
+                                          int32_t refit, void* stream);
 
 /* ---- batched queries ----------------------------------------------------------------
  * A batch is n queries over a table of mesh pairs.  Query i tests meshes

@@ -76,6 +76,13 @@ void orc_mesh_update(void* h, const double* verts) {
   update_refit_bottomup(*m, nv);
 }
 
+void orc_mesh_replace(void* h, const double* verts) {
+  Mesh* m = static_cast<Mesh*>(h);
+  std::vector<V3> nv(m->verts.size());
+  for (size_t i = 0; i < nv.size(); ++i) nv[i] = mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+  replace_refit_bottomup(*m, nv);
+}
+
 int orc_mesh_num_nodes(void* h) { return (int)static_cast<Mesh*>(h)->nodes.size(); }
 
 // Per node: obb.axis (9, row-major), obb.To (3), obb.extent (3), rss.axis (9),

@@ -54,6 +54,9 @@ OBB obb_merge(const OBB& a, const OBB& b);                           // OBB::ope
 RSS rss_merge(const RSS& self, const RSS& other);                    // RSS::operator+
 // beginUpdateModel, updateVertex x nv, endUpdateModel(refit = true, bottomup = true)
 void update_refit_bottomup(Mesh& m, const std::vector<V3>& new_verts);
+// beginReplaceModel, replaceVertex x nv, endReplaceModel(refit = true, bottomup = true)
+void replace_refit_bottomup(Mesh& m, const std::vector<V3>& new_verts);
+void fit3_obbrss(const V3 ps[3], OBB& obb, RSS& rss);                // fit<OBBRSS>, n = 3
 
 // --- point-set RSS fit for three points (math/bv/utility-inl.h:208-230) ----------
 void rss_fit3(const V3 ps[3], RSS& bv);

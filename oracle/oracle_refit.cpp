@@ -306,6 +306,56 @@ static void refit_node(Mesh& m, const std::vector<V3>& prev, int id) {
 
 // beginUpdateModel + updateVertex (all vertices) + endUpdateModel(true, true): the
 // previous frame becomes the vertices before this update
+// Eigen's normalized(): v / |v| when |v|^2 > 0, else v
+static V3 eigen_normalized(const V3& v) {
+  double z = sqnorm(v);
+  if (z > 0) {
+    double n = std::sqrt(z);
+    return mk(v[0] / n, v[1] / n, v[2] / n);
+  }
+  return v;
+}
+
+// fit<OBBRSS>(ps, 3): OBB fit3 + RSS fit3 (math/bv/utility-inl.h:92-119, 208-233, 507-511)
+void fit3_obbrss(const V3 ps[3], OBB& obb, RSS& rss) {
+  V3 e[3] = {sub(ps[0], ps[1]), sub(ps[1], ps[2]), sub(ps[2], ps[0])};
+  double len[3] = {sqnorm(e[0]), sqnorm(e[1]), sqnorm(e[2])};
+  int imax = 0;
+  if (len[1] > len[0]) imax = 1;
+  if (len[2] > len[imax]) imax = 2;
+  setcol(obb.axis, 2, eigen_normalized(cross(e[0], e[1])));
+  setcol(obb.axis, 0, eigen_normalized(e[imax]));
+  setcol(obb.axis, 1, cross(col(obb.axis, 2), col(obb.axis, 0)));
+  rss.axis = obb.axis;
+  std::vector<V3> P;
+  extent_center_points(ps, 3, obb.axis, obb.To, obb.extent, &P);
+  rss_from_projected(P, rss.axis, rss.To, rss.l, rss.r);
+}
+
+// recursiveRefitTree_bottomup without a previous frame (BVH_model-inl.h:961-1027 after
+// beginReplaceModel dropped prev_vertices): leaves fit3, internal nodes as the update's
+static void refit_node_replace(Mesh& m, int id) {
+  Node& nd = m.nodes[id];
+  if (nd.first_child < 0) {
+    const Tri& t = m.tris[-(nd.first_child + 1)];
+    V3 v[3] = {m.verts[t.v[0]], m.verts[t.v[1]], m.verts[t.v[2]]};
+    fit3_obbrss(v, nd.obb, nd.rss);
+    return;
+  }
+  refit_node_replace(m, nd.first_child);
+  refit_node_replace(m, nd.first_child + 1);
+  const Node& l = m.nodes[nd.first_child];
+  const Node& r = m.nodes[nd.first_child + 1];
+  Node& me = m.nodes[id];
+  me.obb = obb_merge(l.obb, r.obb);
+  me.rss = rss_merge(l.rss, r.rss);
+}
+
+void replace_refit_bottomup(Mesh& m, const std::vector<V3>& new_verts) {
+  m.verts = new_verts;
+  refit_node_replace(m, 0);
+}
+
 void update_refit_bottomup(Mesh& m, const std::vector<V3>& new_verts) {
   const std::vector<V3> prev = m.verts;
   m.verts = new_verts;

@@ -39,6 +39,7 @@ def lib():
         L.orc_mesh_num_nodes.argtypes = [C.c_void_p]
         L.orc_mesh_get_nodes.argtypes = [C.c_void_p, _dp, _ip]
         L.orc_mesh_update.argtypes = [C.c_void_p, _dp]
+        L.orc_mesh_replace.argtypes = [C.c_void_p, _dp]
         L.orc_collide_batch.restype = C.c_int64
         L.orc_collide_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64, C.c_int,
                                         _i64p, _i64p, _i64p, _ip, C.c_int64]
@@ -103,6 +104,14 @@ class Mesh:
         v = np.ascontiguousarray(verts, dtype=np.float64)
         assert v.shape == self.verts.shape
         lib().orc_mesh_update(self.h, _d(v))
+        self.verts = v
+
+    def replace(self, verts: np.ndarray) -> None:
+        """beginReplaceModel / replaceVertex / endReplaceModel(refit = true, bottomup =
+        true): no previous frame, each leaf refitted to its new triangle (fit3)."""
+        v = np.ascontiguousarray(verts, dtype=np.float64)
+        assert v.shape == self.verts.shape
+        lib().orc_mesh_replace(self.h, _d(v))
         self.verts = v
 
     def nodes(self):

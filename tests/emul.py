@@ -29,14 +29,16 @@ def build(v, t):
     return out, fc, md.value
 
 
-def refit(v0, t, frames):
-    """Device refit math run on the host: build from v0, then refit to each frame."""
+def refit(v0, t, frames, replace=None):
+    """Device refit math run on the host: build from v0, then refit to each frame
+    (replace[f] true: the frame replaces the vertices, no previous frame)."""
     v0 = np.ascontiguousarray(v0, np.float64); t = np.ascontiguousarray(t, np.int32)
     vs = np.ascontiguousarray(np.stack(frames), np.float64)
+    rp = np.ascontiguousarray(np.zeros(len(frames)) if replace is None else replace, np.int32)
     nn = 2 * t.shape[0] - 1
     out = np.empty((nn, 30)); fc = np.empty(nn, np.int32)
     lib().emu_refit(_p(v0), C.c_int64(v0.shape[0]), _p(t), C.c_int64(t.shape[0]), _p(vs), C.c_int(len(frames)),
-                    _p(out), _p(fc))
+                    _p(out), _p(fc), _p(rp))
     return out, fc
 
 

@@ -165,7 +165,7 @@ int64_t emu_collide_split(int prec, const double* v1, int64_t nv1, const int32_t
 // Host run of the device refit math (refit.cuh): build from v0, then the bottom-up
 // refit to each of the k frames in vs (k * nv * 3 doubles) in turn; nodes30 as emu_build.
 void emu_refit(const double* v0, int64_t nv, const int32_t* t, int64_t nt, const double* vs, int k, double* nodes30,
-               int32_t* fc) {
+               int32_t* fc, const int32_t* replace) {
   HostMesh m;
   make_mesh(v0, nv, t, nt, m);
   std::vector<double> prev;
@@ -177,7 +177,16 @@ void emu_refit(const double* v0, int64_t nv, const int32_t* t, int64_t nt, const
       NodeD& nd = m.bvh.nodes[b];
       RssD& rs = m.bvh.rss[b];
       const int c = nd.child;
-      if (c < 0) {
+      if (c < 0 && replace && replace[f]) {  // replaced frame: fit3 of the new triangle
+        const int tt = -(c + 1);
+        D3v v[3];
+        for (int i = 0; i < 3; ++i) {
+          const double* q = m.verts.data() + 3 * m.tris[3 * tt + i];
+          v[i] = v3(q[0], q[1], q[2]);
+        }
+        fit3_obbrss(v, nd, rs);
+        nd.child = c;
+      } else if (c < 0) {
         const int tt = -(c + 1);
         D3v v[6];
         for (int i = 0; i < 3; ++i) {

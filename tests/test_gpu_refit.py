@@ -86,3 +86,25 @@ def test_update_with_wrong_vertex_count(gpu_lib):
     assert g.beginUpdateModel() == 0
     g.updateSubModel(v1[:-1])
     assert g.endUpdateModel() == -7  # BVH_ERR_INCORRECT_DATA, as FCL's endUpdateModel
+
+
+def test_replace_model_bit_exact(gpu_lib):
+    """beginReplaceModel / replaceVertex / endReplaceModel(): leaves refitted to the new
+    triangle alone (fit3), then an update on top, against the oracle bit for bit."""
+    v, t, v1, v2 = _frames(8)
+    g = api.BVHModel.from_arrays(v, t)
+    o = O.Mesh(v, t)
+    assert g.beginReplaceModel() == 0
+    for p in v1:
+        g.replaceVertex(p)
+    assert g.endReplaceModel() == 0
+    o.replace(v1)
+    assert np.array_equal(g.get_nodes()[0].view(np.uint64), o.nodes()[0].view(np.uint64))
+    g.update_vertices(v2)
+    o.update(v2)
+    assert np.array_equal(g.get_nodes()[0].view(np.uint64), o.nodes()[0].view(np.uint64))
+    with pytest.raises(N.FclGpuError) as e:
+        assert g.beginReplaceModel() == 0
+        g.replaceSubModel(v1)
+        g.endReplaceModel(refit=False)
+    assert e.value.code == N.FCLGPU_ERR_UNSUPPORTED

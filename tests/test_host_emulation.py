@@ -113,3 +113,21 @@ def test_refit_bit_exact_vs_oracle(freq, seed):
     en, efc = emul.refit(v, t, [v1, v2])
     assert np.array_equal(ofc, efc)
     assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
+
+
+def test_replace_then_update_bit_exact_vs_oracle():
+    """endReplaceModel() refits each leaf to its new triangle alone (fit3: FCL drops the
+    previous frame); a later update uses the replaced vertices as its previous frame."""
+    v, t = W.perturbed_ellipsoid(8, (1, 0.7, 0.5), 0.01, 0)
+    rng = np.random.default_rng(1)
+    f1 = v + rng.normal(0, 0.02, v.shape)
+    f2 = f1 + rng.normal(0, 0.02, v.shape)
+    f3 = f2 + rng.normal(0, 0.02, v.shape)
+    o = O.Mesh(v, t)
+    o.replace(f1)
+    o.update(f2)
+    o.replace(f3)
+    on, ofc = o.nodes()
+    en, efc = emul.refit(v, t, [f1, f2, f3], [1, 0, 1])
+    assert np.array_equal(ofc, efc)
+    assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
