@@ -162,3 +162,49 @@ def test_box_box_cull_contacts_known_answer():
         pos = r["point"][0]
         assert abs(pos[2] - ez) <= tol and abs(pos[1] - ey) <= tol
         assert -ex <= pos[0] <= ex
+
+
+_RX90 = np.array([[1, 0, 0], [0, 0, -1], [0, 1, 0]], float)   # AngleAxis(pi/2, UnitX)
+
+
+def test_sphere_capsule_known_answers():
+    # test_fcl_sphere_capsule.cpp:48-260: Sphere(50) vs Capsule(50, 200); the closed forms
+    # sphereCapsuleIntersect / sphereCapsuleDistance are the GST_INDEP dispatch too
+    def run(ts, tc, R=None):
+        return _one(W.SPHERE, [50, 0, 0], _tf(ts), _tf(tc, R), t2=W.CAPSULE, params2=[50, 200, 0])
+    for ts, tc, R in [((0, 0, -50), (0, 0, 200), None), ((0, 0, 50), (0, 0, -200), None),
+                      ((0, 0, -50), (150, 0, 0), None), ((0, 0, -50), (150, 0, 0), _RX90)]:
+        assert not run(ts, tc, R)["hit"][0]                      # separated_z / _negative / _x / rotated
+    r = run((0, 0, -50), (0, 0, 125))                            # penetration_z
+    assert r["hit"][0] and r["depth"][0] == 25.0
+    assert np.allclose(r["normal"][0], (0, 0, 1)) and np.allclose(r["point"][0], (0, 0, 0))
+    r = run((0, 0, 0), (0, 50, 75), _RX90)                       # penetration_z_rotated
+    assert r["hit"][0] and abs(r["depth"][0] - 25) < 1e-6
+    assert np.allclose(r["normal"][0], (0, 0, 1)) and np.allclose(r["point"][0], (0, 0, 50), atol=1e-6)
+    assert run((0, 0, -50), (0, 0, 100))["hit"][0]               # Distance_test_collision
+    r = run((0, 0, -50), (0, 0, 175))                            # Distance_test_separated
+    assert not r["hit"][0] and r["dist"][0] == 25.0
+
+
+def _angle_axis_matrix(angle, axis):
+    k = np.asarray(axis, float) / np.linalg.norm(axis)
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.cos(angle) * np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * np.outer(k, k)
+
+
+def test_capsule_capsule_separated_known_answer():
+    # test_fcl_capsule_capsule.cpp:535-740 (CapsuleCapsuleSegmentTest, NominalSeparatedCase):
+    # Capsule(1.5, 2.5) and Capsule(2, 3) (the second turned by pi/2 about y) 0.25 apart
+    # along z in a frame T, evaluated in F = X_FT (angle pi/7 about (1,2,3), translation
+    # (10.5, 12.75, -2.5)); distance 0.25 and witnesses X_FT (0,0,2.75), X_FT (0,0,3) within
+    # eps^(3/4)
+    R_FT = _angle_axis_matrix(np.pi / 7, (1, 2, 3))
+    t_FT = np.array([10.5, 12.75, -2.5])
+    R_TC2 = _angle_axis_matrix(np.pi / 2, (0, 1, 0))
+    X1 = _tf(t_FT, R_FT)
+    X2 = _tf(R_FT @ np.array([0, 0, 1.25 + 1.5 + 2 + 0.25]) + t_FT, R_FT @ R_TC2)
+    r = _one(W.CAPSULE, [1.5, 2.5, 0], X1, X2, t2=W.CAPSULE, params2=[2, 3, 0])
+    eps = np.finfo(float).eps ** 0.75
+    assert not r["hit"][0] and abs(r["dist"][0] - 0.25) < eps
+    assert np.allclose(r["p1"][0], R_FT @ np.array([0, 0, 2.75]) + t_FT, atol=eps, rtol=0)
+    assert np.allclose(r["p2"][0], R_FT @ np.array([0, 0, 3.0]) + t_FT, atol=eps, rtol=0)
