@@ -208,3 +208,77 @@ def test_capsule_capsule_separated_known_answer():
     assert not r["hit"][0] and abs(r["dist"][0] - 0.25) < eps
     assert np.allclose(r["p1"][0], R_FT @ np.array([0, 0, 2.75]) + t_FT, atol=eps, rtol=0)
     assert np.allclose(r["p2"][0], R_FT @ np.array([0, 0, 3.0]) + t_FT, atol=eps, rtol=0)
+
+
+@pytest.mark.parametrize("r", [0.0, np.finfo(float).eps, 4.5, 9 - 0.0015])
+def test_sphere_cylinder_known_answers(r):
+    # test_fcl_sphere_cylinder.cpp:100-224 (LargeCylinderSmallSphereTest, GST_INDEP): a
+    # sphere of radius 0.0015 sinks half its radius into the top face of Cylinder(9,
+    # 0.0025) at radial offsets r and angles theta + pi/7; depth 0.00075, normal -z (+z in
+    # the reversed order), contact at (sx, sy, h/2 - depth/2), all within machine epsilon
+    eps = np.finfo(float).eps
+    r_c, h_c, r_s = 9.0, 0.0025, 0.0015
+    depth = r_s * 0.5
+    sz = h_c / 2 + r_s - depth
+    pz = h_c / 2 - depth / 2
+    for theta in (0, np.pi / 2, np.pi, 3 * np.pi / 4):
+        a = theta + np.pi / 7
+        sx, sy = np.cos(a) * r, np.sin(a) * r
+        for order in (0, 1):
+            if order == 0:
+                res = _one(W.SPHERE, [r_s, 0, 0], _tf((sx, sy, sz)), _tf(), t2=W.CYLINDER, params2=[r_c, h_c, 0])
+                nrm = (0, 0, -1)
+            else:
+                res = _one(W.CYLINDER, [r_c, h_c, 0], _tf(), _tf((sx, sy, sz)), t2=W.SPHERE, params2=[r_s, 0, 0])
+                nrm = (0, 0, 1)
+            assert res["hit"][0]
+            assert abs(res["depth"][0] - depth) <= eps
+            assert np.allclose(res["normal"][0], nrm, atol=eps, rtol=0)
+            assert np.allclose(res["point"][0], (sx, sy, pz), atol=eps, rtol=0)
+
+
+def test_sphere_box_known_answers():
+    # test_fcl_sphere_box.cpp:91-210 (LargeBoxSmallSphereTest, GST_INDEP): a sphere of
+    # radius 0.0015 sinks half its radius into the top face of Box(0.115, 0.01, 0.0025) at
+    # a grid of offsets; depth 0.00075, normal -z (+z reversed), contact at (sx, sy,
+    # h/2 - depth/2), within machine epsilon
+    eps = np.finfo(float).eps
+    w, d, h, r = 0.115, 0.01, 0.0025, 0.0015
+    depth = r * 0.5
+    sz = h / 2 + r - depth
+    pz = h / 2 - depth / 2
+    hx, hy = w / 2, d / 2
+    xs = (-hx + r, -hx * 0.5, -eps, 0.0, eps, hx * 0.5, hx - r)
+    ys = (-hy + r, -hy * 0.5, -eps, 0.0, eps, hy * 0.5, hy - r)
+    for sx in xs:
+        for sy in ys:
+            for order in (0, 1):
+                if order == 0:
+                    res = _one(W.SPHERE, [r, 0, 0], _tf((sx, sy, sz)), _tf(), t2=W.BOX, params2=[w, d, h])
+                    nrm = (0, 0, -1)
+                else:
+                    res = _one(W.BOX, [w, d, h], _tf(), _tf((sx, sy, sz)), t2=W.SPHERE, params2=[r, 0, 0])
+                    nrm = (0, 0, 1)
+                assert res["hit"][0]
+                assert abs(res["depth"][0] - depth) <= eps
+                assert np.allclose(res["normal"][0], nrm, atol=eps, rtol=0)
+                assert np.allclose(res["point"][0], (sx, sy, pz), atol=eps, rtol=0)
+
+
+def test_separating_spheres_known_answers():
+    # test_fcl_sphere_sphere.cpp:55-178 (TestSeparatingSpheres, GST_INDEP, tolerance 1e-14):
+    # every pair of four separated spheres, both orders: distance |cA - cB| - rA - rB and
+    # the witnesses on the centre line
+    spheres = [(0.5, (0, 0, -1)), (0.6, (1.2, 0, 0)), (0.4, (-0.3, 0, 0)), (0.3, (0, 0, 1))]
+    for i in range(4):
+        for j in range(4):
+            if i == j:
+                continue
+            (ra, ca), (rb, cb) = spheres[i], spheres[j]
+            ca, cb = np.array(ca, float), np.array(cb, float)
+            ab = (ca - cb) / np.linalg.norm(ca - cb)
+            res = _one(W.SPHERE, [ra, 0, 0], _tf(ca), _tf(cb), t2=W.SPHERE, params2=[rb, 0, 0])
+            assert not res["hit"][0]
+            assert abs(res["dist"][0] - (np.linalg.norm(ca - cb) - ra - rb)) < 1e-14
+            assert np.allclose(res["p1"][0], ca - ab * ra, atol=1e-14, rtol=0)
+            assert np.allclose(res["p2"][0], cb + ab * rb, atol=1e-14, rtol=0)
