@@ -99,3 +99,18 @@ def test_fcl_collide_mirror_with_contacts(gpu_lib):
     with pytest.raises(N.FclGpuError):
         api.collide(o1, o2, api.CollisionRequest(num_max_contacts=4, enable_contact=True, enable_statistics=True),
                     api.CollisionResult())
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_contacts_on_reference_fixture(gpu_lib, golden, prec):
+    """FCL's collision test setting (enable_contact = true, num_max_contacts = INT_MAX,
+    test_fcl_collision.cpp:74-75) on its env.obj / rob.obj fixture and poses: contact lists
+    and geometry equal the oracle's bit for bit."""
+    ms = [api.BVHModel.from_arrays(golden["env_v"], golden["env_t"]),
+          api.BVHModel.from_arrays(golden["rob_v"], golden["rob_t"])]
+    tf = golden["tf"]
+    g = api.collide_contacts_batch(ms, [[0, 1]], None, tf, num_max_contacts=2 ** 31 - 1, precision=prec)
+    ref = O.collide_contacts_batch(O.Mesh(golden["env_v"], golden["env_t"]),
+                                   O.Mesh(golden["rob_v"], golden["rob_t"]), tf, num_max_contacts=2 ** 31 - 1)
+    _same(g, ref)
+    assert ref[0].sum() > 0
