@@ -282,3 +282,28 @@ def test_separating_spheres_known_answers():
             assert abs(res["dist"][0] - (np.linalg.norm(ca - cb) - ra - rb)) < 1e-14
             assert np.allclose(res["p1"][0], ca - ab * ra, atol=1e-14, rtol=0)
             assert np.allclose(res["p2"][0], cb + ab * rb, atol=1e-14, rtol=0)
+
+
+@pytest.mark.parametrize("kind", ["boxbox", "cylindercylinder", "conecone"])
+def test_gjk_distance_known_answers(kind):
+    # test_fcl_geometric_shapes.cpp:4939-5133 (shapeDistanceGJK_boxbox / _cylindercylinder /
+    # _conecone, GJKSolver_indep): overlapping at identity; 0.1 and 5 / 30 apart along an axis;
+    # the same under a common rigid transform; tolerance 0.001
+    if kind == "boxbox":
+        a, b = (W.BOX, [20, 40, 50]), (W.BOX, [10, 10, 10])
+        cases = [((15.1, 0, 0), 0.1), ((20, 0, 0), 5.0)]
+    elif kind == "cylindercylinder":
+        a = b = (W.CYLINDER, [5, 10, 0])
+        cases = [((10.1, 0, 0), 0.1), ((40, 0, 0), 30.0)]
+    else:
+        a = b = (W.CONE, [5, 10, 0])
+        cases = [((10.1, 0, 0), 0.1), ((0, 0, 40), 30.0)]
+    for X in (_tf(), W.random_poses(1, -10, 10, 321)[0]):
+        def comp(t):
+            out = X.copy()
+            out[:, 3] = X[:, :3] @ np.array(t, float) + X[:, 3]
+            return out
+        assert _one(a[0], a[1], X, X, t2=b[0], params2=b[1])["hit"][0]
+        for t, expect in cases:
+            r = _one(a[0], a[1], X, comp(t), t2=b[0], params2=b[1])
+            assert not r["hit"][0] and abs(r["dist"][0] - expect) < 0.001
