@@ -307,3 +307,28 @@ def test_gjk_distance_known_answers(kind):
         for t, expect in cases:
             r = _one(a[0], a[1], X, comp(t), t2=b[0], params2=b[1])
             assert not r["hit"][0] and abs(r["dist"][0] - expect) < 0.001
+
+
+def test_sphere_sphere_intersection_known_answers():
+    # test_fcl_geometric_shapes.cpp:544-610 (shapeIntersection_spheresphere; the closed form
+    # sphereSphereIntersect serves both solvers): Sphere(20) and Sphere(10) apart by 40 and
+    # 30.01 (no contact), touching at 30 (depth 0 at x = 20), overlapping at 29.9 (depth 0.1
+    # at x = 20 - 0.1 * 20/30, normal +x, also under a rigid transform) and concentric
+    # (normal 0, position 0, depth 30)
+    X = W.random_poses(1, -10, 10, 77)[0]
+
+    def at(base, t):
+        out = base.copy()
+        out[:, 3] = base[:, :3] @ np.array(t, float) + base[:, 3]
+        return out
+    for base in (_tf(), X):
+        for d in (40.0, 30.01):
+            assert not _one(W.SPHERE, [20, 0, 0], base, at(base, (d, 0, 0)), t2=W.SPHERE, params2=[10, 0, 0])["hit"][0]
+        for d, depth in ((30.0, 0.0), (29.9, 0.1)):
+            r = _one(W.SPHERE, [20, 0, 0], base, at(base, (d, 0, 0)), t2=W.SPHERE, params2=[10, 0, 0])
+            assert r["hit"][0] and abs(r["depth"][0] - depth) < 1e-12
+            assert np.allclose(r["normal"][0], base[:, :3] @ np.array([1.0, 0, 0]), atol=1e-12)
+            assert np.allclose(r["point"][0], at(base, (20.0 - depth * 20.0 / 30.0, 0, 0))[:, 3], atol=1e-12)
+    r = _one(W.SPHERE, [20, 0, 0], _tf(), _tf(), t2=W.SPHERE, params2=[10, 0, 0])
+    assert r["hit"][0] and r["depth"][0] == 30.0
+    assert np.array_equal(r["normal"][0], [0, 0, 0]) and np.array_equal(r["point"][0], [0, 0, 0])
