@@ -949,6 +949,7 @@ int fclgpu_distance_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, 
   DistanceLaunch L;
   L.meshes = (const DevMesh*)S.meshes.p;
   L.pairs = (const int2*)S.pairs.p;
+  L.num_pairs = num_pairs;
   L.pair_of_query = pair_of_query;
   L.tf1 = tf1;
   L.tf2 = tf2;

@@ -12,6 +12,7 @@ enum : uint32_t {
   DEV_ERR_STACK = 1u,     // traversal stack overflow
   DEV_ERR_RECORDS = 2u,   // contact record scratch overflow
   DEV_ERR_ITEMS = 4u,     // work-item scratch overflow
+  DEV_ERR_PAIR = 8u,      // a query's pair index lies outside the pair table
 };
 
 // Counters shared by one batch launch (device scratch).
@@ -71,6 +72,7 @@ int collide_round_grid(int precision, int stack_entries, int block, int variant)
 struct DistanceLaunch {
   const DevMesh* meshes;
   const int2* pairs;
+  int32_t num_pairs;              // entries of pairs[]; a query naming another index is skipped
   const int32_t* pair_of_query;
   const double* tf1;
   const double* tf2;

@@ -252,6 +252,11 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
     const long long qi = (long long)atomicAdd(&L.ctr->work, 1ull);
     if (qi >= L.n) break;
     const int pi = L.pair_of_query ? __ldg(L.pair_of_query + qi) : 0;
+    if (pi < 0 || pi >= L.num_pairs) {  // reported through the status word, query left NaN
+      atomicOr(&L.ctr->status, DEV_ERR_PAIR);
+      L.dist[qi] = __longlong_as_double(0x7ff8000000000000ll);
+      continue;
+    }
     const int2 mp = L.pairs[pi];
     const DevMesh A = L.meshes[mp.x];
     const DevMesh B = L.meshes[mp.y];

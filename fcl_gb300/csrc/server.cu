@@ -173,6 +173,7 @@ struct fclgpu_server_s {
   std::vector<Request*> active;
   std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
   int64_t next_id = 1;
+  int waiters = 0;  // threads inside fclgpu_server_wait (destroy waits for them to leave)
   fclgpu_server_stats stats;
   double cand_per_query = 8.0;  // running estimate for the memory admission
   std::thread worker;
@@ -505,10 +506,22 @@ int fclgpu_server_wait(fclgpu_server s, int64_t id, double timeout_ms, fclgpu_mo
   }
   Request* r = it->second.get();
   auto ready = [&] { return r->done; };
+  struct WaiterCount {  // lets destroy wait until no thread is left inside this call
+    fclgpu_server_s* s;
+    explicit WaiterCount(fclgpu_server_s* s_) : s(s_) { ++s->waiters; }
+    ~WaiterCount() {
+      --s->waiters;
+      s->cv_done.notify_all();
+    }
+  } counted(s);
   if (timeout_ms < 0)
     s->cv_done.wait(lk, ready);
   else if (!s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready))
     return FCLGPU_ERR_PENDING;
+  if (s->stop && r->res.reserved == FCLGPU_ERR_NOT_INITIALIZED) {
+    set_error_detail("the server was destroyed before this request finished");
+    return FCLGPU_ERR_NOT_INITIALIZED;
+  }
   *out = r->res;
   const int rc = r->res.reserved;
   out->reserved = 0;
@@ -560,6 +573,22 @@ int fclgpu_server_destroy(fclgpu_server s) {
   s->cv_work.notify_all();
   if (s->worker.joinable()) s->worker.join();
   cudaStreamSynchronize(s->stream);
+  {
+    // unfinished requests end with an error, and every thread blocked in
+    // fclgpu_server_wait returns before the server's memory is released
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (auto& kv : s->reqs) {
+      Request* r = kv.second.get();
+      if (!r->done) {
+        r->res.reserved = FCLGPU_ERR_NOT_INITIALIZED;
+        r->done = true;
+      }
+    }
+    s->pending.clear();
+    s->active.clear();
+    s->cv_done.notify_all();
+    s->cv_done.wait(lk, [&] { return s->waiters == 0; });
+  }
   free_server(s);
   return FCLGPU_OK;
 }

@@ -12,7 +12,11 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libfclgpu.so")
 
 FCLGPU_OK = 0
+FCLGPU_ERR_INVALID_ARGUMENT = -1
 FCLGPU_ERR_CAPACITY = -4
+FCLGPU_ERR_STACK_DEPTH = -6
+FCLGPU_ERR_DEVICE_STATUS = -7
+FCLGPU_ERR_NOT_INITIALIZED = -8
 PLAIN_FP64 = 0
 FP32_RECHECK = 1
 

@@ -283,11 +283,11 @@ FCLGPU_API int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_mesh
 
 /* Same query and outputs as fclgpu_distance_batch_device (device pointers), but the
  * call allocates no memory: for callers that cannot allocate GPU memory at query time
- * (deadline-bound control loops, processes whose HBM is owned by another allocator,
- * work issued during stream capture).  Its scratch is a fixed array inside the
- * library, shared by all calls: at most 64 meshes and 256 pairs per call (larger
- * requests return FCLGPU_ERR_INVALID_ARGUMENT), and calls that overlap on the GPU
- * race, so serialise them.  The first call on a device looks the array up and should
+ * (deadline-bound control loops, processes whose HBM is owned by another allocator).
+ * Its scratch is a fixed array inside the library, shared by all calls: at most 64
+ * meshes and 256 pairs per call (larger requests return FCLGPU_ERR_INVALID_ARGUMENT),
+ * and calls that overlap on the GPU race, so serialise them.  The call waits for its
+ * stream before it returns.  The first call on a device looks the array up and should
  * come before any stream capture.  No counterpart in FCL. */
 FCLGPU_API int fclgpu_distance_batch_noalloc(const fclgpu_mesh* meshes, int32_t num_meshes,
                                              const int32_t* pairs_host, int32_t num_pairs,
@@ -580,7 +580,10 @@ FCLGPU_API int fclgpu_server_get_stats(fclgpu_server srv, fclgpu_server_stats* o
  * num_links x 12 doubles, host), for checking results against another engine. */
 FCLGPU_API int fclgpu_server_link_poses(fclgpu_server srv, const double* base_tf, const double* q,
                                         int32_t num_waypoints, double* out_tf);
-/* Stops the loop after its current step; unfinished requests are dropped. */
+/* Stops the loop after its current step.  Unfinished requests are dropped: threads
+ * blocked in fclgpu_server_wait on them return FCLGPU_ERR_NOT_INITIALIZED, and this
+ * call returns only after every such thread has left fclgpu_server_wait.  No call on
+ * the handle may start after destroy has begun. */
 FCLGPU_API int fclgpu_server_destroy(fclgpu_server srv);
 
 #ifdef __cplusplus

@@ -7,15 +7,17 @@ transforms from generateRandomTransforms (test_fcl_utility.h:348-372) with exten
 (-3000,-3000,0)..(3000,3000,3000), Euler angles in [0, 2pi) mapped by eulerToMatrix
 (:313-325), driven by glibc rand() from its default seed.
 
-Run here (where the reference is mounted):  python tests/golden/make_fixtures.py
+Usage:  python tests/golden/make_fixtures.py FCL_CHECKOUT
+where FCL_CHECKOUT is the root of an FCL source tree (the directory holding
+test/fcl_resources).
 """
+import argparse
 import ctypes
 import math
 import os
 
 import numpy as np
 
-REF = "/root/reference/test/fcl_resources"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "env_rob.npz")
 
 
@@ -65,8 +67,11 @@ def reference_transforms(n, extents):
 
 
 def main():
-    ev, et = load_obj(os.path.join(REF, "env.obj"))
-    rv, rt = load_obj(os.path.join(REF, "rob.obj"))
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("fcl_checkout", help="root of an FCL source tree (holds test/fcl_resources)")
+    res = os.path.join(ap.parse_args().fcl_checkout, "test", "fcl_resources")
+    ev, et = load_obj(os.path.join(res, "env.obj"))
+    rv, rt = load_obj(os.path.join(res, "rob.obj"))
     tfs = reference_transforms(10, (-3000, -3000, 0, 3000, 3000, 3000))
     np.savez_compressed(OUT, env_v=ev, env_t=et, rob_v=rv, rob_t=rt, tf=tfs)
     print("wrote", OUT, ev.shape, et.shape, rv.shape, rt.shape)

@@ -206,3 +206,21 @@ def test_distance_fp32_tf1_and_fixture(gpu_lib, golden):
     env = O.Mesh(golden["env_v"], golden["env_t"]); rob = O.Mesh(golden["rob_v"], golden["rob_t"])
     d, ids, pts, _, _ = O.distance_batch(env, rob, tf, tf1=tf1, nearest=True)
     _dist_check(out, d, pts)
+
+
+def test_distance_rejects_out_of_range_pair_index(gpu_lib):
+    """A pair index outside the pair table is not read: the device entry point skips
+    that query, sets the status word and returns FCLGPU_ERR_DEVICE_STATUS; the other
+    queries keep their results."""
+    import torch
+    from fcl_gb300 import native as N
+    w = W.config0(n_poses=8, freq=2)
+    ms = _meshes(w)
+    tf2 = torch.from_numpy(w.tf2).cuda()
+    pq = torch.zeros(8, dtype=torch.int32, device="cuda")
+    pq[3] = 7
+    with pytest.raises(N.FclGpuError) as e:
+        api.distance_batch(ms, w.pairs, None, tf2, pair_of_query=pq, precision="fp32")
+    assert e.value.code == N.FCLGPU_ERR_DEVICE_STATUS
+    good = api.distance_batch(ms, w.pairs, None, tf2, pair_of_query=torch.zeros_like(pq), precision="fp32")
+    assert torch.isfinite(good["min_distance"]).all()

@@ -92,3 +92,37 @@ def test_serving_with_mesh_links_and_mesh_objects(gpu_lib):
         else:
             assert g["min_clearance"] <= 0
     srv.close()
+
+
+def test_destroy_releases_blocked_waiters(gpu_lib):
+    """Threads blocked in wait() on unfinished requests return when the server is
+    destroyed (FCLGPU_ERR_NOT_INITIALIZED, or the result if the request finished
+    first); destroy returns only after they have left the call."""
+    import threading
+    from fcl_gb300 import native as N
+    w = W.scene4(n_objects=2000, seed=5, box=12.0, n_shape_geoms=128, mesh_fraction=0.0, mesh_links=False)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    mgr = api.DynamicAABBTreeCollisionManager(ss)
+    mgr.registerObjects(w.refs, w.tf)
+    reqs = W.motion_requests(w, 6, seed=7, k_lo=200, k_hi=400)
+    srv = api.MotionServer(mgr, w.robot, max_waypoints_per_step=8)
+    ids = [srv.submit(r.base, r.q) for r in reqs]
+    outcome = {}
+
+    def waiter(i):
+        try:
+            outcome[i] = srv.wait(i)
+        except N.FclGpuError as e:
+            outcome[i] = e.code
+
+    th = [threading.Thread(target=waiter, args=(i,), daemon=True) for i in ids]
+    for t in th:
+        t.start()
+    import time
+    time.sleep(0.5)  # every waiter is inside wait() before destroy begins (the documented contract)
+    srv.close()
+    for t in th:
+        t.join(timeout=60)
+    assert not any(t.is_alive() for t in th)
+    assert set(outcome) == set(ids)
+    assert all(isinstance(v, dict) or v == N.FCLGPU_ERR_NOT_INITIALIZED for v in outcome.values())

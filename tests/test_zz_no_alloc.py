@@ -1,11 +1,12 @@
 """The allocation-free distance entry point (fclgpu_distance_batch_noalloc).
 
 Callers that cannot allocate GPU memory at query time -- deadline-bound control
-loops, processes whose device memory belongs to another allocator, work recorded
-during stream capture -- use this entry point; its scratch is a fixed array inside
-the library.  It must return what the allocating entry point
-(fclgpu_distance_batch_device) returns, on consecutive calls that reuse the shared
-scratch.  This file is collected last so a failure here does not hide the others.
+loops, processes whose device memory belongs to another allocator -- use this entry
+point; its scratch is a fixed array inside the library.  It must return what the
+allocating entry point (fclgpu_distance_batch_device) returns, on consecutive calls
+that reuse the shared scratch, including after a larger call with another mesh and
+pair table has left its contents there.  This file is collected last so a failure
+here does not hide the others.
 """
 import ctypes as C
 
@@ -40,6 +41,16 @@ def _noalloc(meshes, pairs, tf2, pq, precision):
     return {k: v.cpu().numpy() for k, v in out.items()}
 
 
+def _check(got, ref):
+    rd = ref["min_distance"].cpu().numpy()
+    rp = ref["nearest_points"].cpu().numpy()
+    ri = ref["ids"].cpu().numpy()
+    assert np.all(np.abs(got["d"] - rd) <= np.maximum(REL * np.abs(rd), ABS))
+    assert np.all(np.abs(got["pts"] - rp) <= REL * np.maximum(np.abs(rp), 1.0) + ABS)
+    sep = rd > 0  # at distance 0 the reported triangles depend on the visit order
+    assert np.array_equal(got["ids"][sep], ri[sep])
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_noalloc_distance_matches_allocating_entry_point(gpu_lib, precision):
     import torch
@@ -48,13 +59,18 @@ def test_noalloc_distance_matches_allocating_entry_point(gpu_lib, precision):
     tf2 = torch.from_numpy(w.tf2).cuda()
     pq = torch.from_numpy(w.pair).cuda()
     ref = api.distance_batch(meshes, w.pairs, None, tf2, pair_of_query=pq, nearest_points=True, precision=precision)
+    # a larger call in between: more meshes, more pairs, and another pair mapping
+    wb = W.config2(total_poses=3000, n_pairs=9, tri_hi=8000, seed=31)
+    mb = [api.BVHModel.from_arrays(v, t) for v, t in wb.meshes]
+    pairs_b = np.ascontiguousarray(wb.pairs[::-1], np.int32)
+    pq_b = torch.from_numpy((len(pairs_b) - 1 - wb.pair).astype(np.int32)).cuda()
+    tf2_b = torch.from_numpy(wb.tf2).cuda()
+    ref_b = api.distance_batch(mb, pairs_b, None, tf2_b, pair_of_query=pq_b, nearest_points=True,
+                               precision=precision)
     torch.cuda.synchronize()
-    rd = ref["min_distance"].cpu().numpy()
-    rp = ref["nearest_points"].cpu().numpy()
-    for _ in range(2):  # two calls in a row share (and reuse) the fixed scratch
-        got = _noalloc(meshes, w.pairs, tf2, pq, precision)
-        assert np.all(np.abs(got["d"] - rd) <= np.maximum(REL * np.abs(rd), ABS))
-        assert np.all(np.abs(got["pts"] - rp) <= REL * np.maximum(np.abs(rp), 1.0) + ABS)
+    _check(_noalloc(meshes, w.pairs, tf2, pq, precision), ref)
+    _check(_noalloc(mb, pairs_b, tf2_b, pq_b, precision), ref_b)
+    _check(_noalloc(meshes, w.pairs, tf2, pq, precision), ref)
 
 
 def test_noalloc_rejects_requests_beyond_its_limits(gpu_lib):
