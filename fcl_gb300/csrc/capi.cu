@@ -490,6 +490,8 @@ int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int
   d.vmax = vmax * (1.0 + 1e-12);
   d.cmax = pk.cmax * (1.0 + 1e-12);
   d.rmax = pk.rmax * (1.0 + 1e-12);
+  d.refitted = 0;
+  d.pad2 = 0;
   {
     double lo[3], hi[3];
     for (int k = 0; k < 3; ++k) {

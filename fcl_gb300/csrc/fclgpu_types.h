@@ -54,6 +54,10 @@ struct DevMesh {
   double vmax;  // max |vertex coordinate|
   double cmax;  // max ||obb.To||_2
   double rmax;  // max ||rss.To||_2
+  // 1 after a bottom-up refit: FCL's OBB and RSS merges need not contain the
+  // children's geometry, so bounds of this mesh are not valid lower bounds
+  int32_t refitted;
+  int32_t pad2;
 };
 
 }  // namespace fclgpu

@@ -9,15 +9,13 @@
 // "<" update (distance_result-inl.h:84-105); nearest points mapped to world by tf1
 // (postprocess, :589-603).
 //
-// The FP32 form (PREC 1) traverses with FP32 RSS distances widened by a slack
-// (2^-12 relative + 64u times the coordinate scale) as pruning lower bounds, and FP32
-// triangle distances (points taken relative to the first vertex, offset in
-// float-float) with a slack E = 2^-18 d + 128u times the pair's coordinate scale.  A
-// leaf whose FP32 interval can still reach the best distance so far -- and every
-// leaf near contact, where triDistance switches branches -- is re-evaluated at once
-// with the exact FP64 triangle distance and the strict "<" update, in visit order,
-// so the reported distance, triangle ids and witness points are FP64 values of the
-// winning pair, and the pruning bound is the exact best.
+// The FP32 form (PREC 1) is the certified traversal of distance_traverse.cuh: BV
+// pairs are pruned with FP32 support-function gaps whose forward error is bounded,
+// triangle pairs are skipped only when a certified FP32 lower bound exceeds the best
+// FP64 distance so far, and every other triangle pair is evaluated with FCL's FP64
+// triDistance and the strict "<" update.  The reported distance, triangle ids and
+// witness points are FP64 values of the winning pair.
+#include "distance_traverse.cuh"
 #include "filter32.cuh"
 #include "geom.cuh"
 #include "kernels.h"
@@ -29,18 +27,6 @@ namespace {
 struct DStack {
   int b1, b2;
   double d;
-};
-struct FStack {
-  int b1, b2;
-  float d;
-};
-
-struct DistOut {
-  double d;
-  int id1, id2;
-  V3<double> P, Q;  // first mesh's frame
-  long long nbv, nleaf, nrc;
-  unsigned status;
 };
 
 __device__ __forceinline__ void load_tfs(const DistanceLaunch& L, long long qi, double* a, double* b) {
@@ -179,84 +165,59 @@ __device__ __noinline__ void distance_query_fp64(const DevMesh& A, const DevMesh
   }
 }
 
-// ---------------------------------------------------------------------------------
-// FP32 form helpers
-// ---------------------------------------------------------------------------------
-
-// Triangle pair in FP32, both relative to triangle 1's first vertex (Q moved by R,T).
-__device__ __forceinline__ float tri_distance_f32(const QueryF32& q, const float4* ta, const float4* tb,
-                                                  float& scale) {
-  const float4 x0 = __ldg(ta), x1 = __ldg(ta + 1), x2 = __ldg(ta + 2);
-  const float4 y0 = __ldg(tb), y1 = __ldg(tb + 1), y2 = __ldg(tb + 2);
-  const float Ph[3] = {x0.x, x0.y, x0.z}, Pl[3] = {x0.w, x1.x, x1.y};
-  const float Qh[3] = {y0.x, y0.y, y0.z}, Ql[3] = {y0.w, y1.x, y1.y};
-  float D[3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    float hi, lo;
-    two_sum(q.T[r], -Ph[r], hi, lo);
-    lo += q.Tl[r] - Pl[r];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float Rh = q.R[3 * r + k], Rlo = q.Rl[3 * r + k];
-      const float p = Rh * Qh[k];
-      const float pe = fmaf(Rh, Qh[k], -p) + fmaf(Rh, Ql[k], Rlo * Qh[k]);
-      float s, e;
-      two_sum(hi, p, s, e);
-      hi = s;
-      lo += e + pe;
+// Writes one query's result (witness points to world by tf1, the postprocess of
+// mesh_distance_traversal_node-inl.h:589-603).
+__device__ __forceinline__ void write_result(const DistanceLaunch& L, long long qi, const DistOut& o) {
+  L.dist[qi] = o.d;
+  if (L.ids) {
+    L.ids[2 * qi] = o.id1;
+    L.ids[2 * qi + 1] = o.id2;
+  }
+  if (L.nearest && L.points) {
+    M3<double> R1;
+    V3<double> t1;
+    if (L.tf1) {
+      const double* ta = L.tf1 + 12 * qi;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) R1(r, c) = __ldg(ta + 4 * r + c);
+      t1 = v3(__ldg(ta + 3), __ldg(ta + 7), __ldg(ta + 11));
+    } else {
+      for (int i = 0; i < 9; ++i) R1.m[i] = (i == 0 || i == 4 || i == 8) ? 1.0 : 0.0;
+      t1 = v3(0.0, 0.0, 0.0);
     }
-    D[r] = hi + lo;
+    const V3<double> w1 = mulv(R1, o.P) + t1;
+    const V3<double> w2 = mulv(R1, o.Q) + t1;
+    double* out = L.points + 6 * qi;
+    out[0] = w1.x; out[1] = w1.y; out[2] = w1.z;
+    out[3] = w2.x; out[4] = w2.y; out[5] = w2.z;
   }
-  const F3 dq2 = rot3(q.R, f3(y1.z, y1.w, y2.x));
-  const F3 dq3 = rot3(q.R, f3(y2.y, y2.z, y2.w));
-  V3<float> T1[3], T2[3];
-  T1[0] = v3(0.f, 0.f, 0.f);
-  T1[1] = v3(x1.z, x1.w, x2.x);
-  T1[2] = v3(x2.y, x2.z, x2.w);
-  T2[0] = v3(D[0], D[1], D[2]);
-  T2[1] = v3(D[0] + dq2.x, D[1] + dq2.y, D[2] + dq2.z);
-  T2[2] = v3(D[0] + dq3.x, D[1] + dq3.y, D[2] + dq3.z);
-  float l = 0.f;
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    l = fmaxf(l, fmaxf(fmaxf(fabsf(T1[k].x), fabsf(T1[k].y)), fmaxf(fmaxf(fabsf(T1[k].z), fabsf(T2[k].x)),
-                                                                      fmaxf(fabsf(T2[k].y), fabsf(T2[k].z)))));
-  scale = l;
-  V3<float> P, Q;
-  return tri_distance<float>(T1, T2, P, Q);
+  if (L.margins && L.within) L.within[qi] = (o.d <= __ldg(L.margins + qi)) ? 1 : 0;
+  if (L.want_stats) {
+    if (L.nbv) L.nbv[qi] = o.nbv;
+    if (L.nleaf) L.nleaf[qi] = o.nleaf;
+    if (L.nrecheck) L.nrecheck[qi] = o.nrc;
+  }
 }
 
-__device__ __forceinline__ float rss_distance_f32(const QueryF32& q, const DevMesh& A, const DevMesh& B, int b1,
-                                                  int b2) {
-  const float4* ra = reinterpret_cast<const float4*>(A.rss32) + 5 * (long long)b1;
-  const float4* rb = reinterpret_cast<const float4*>(B.rss32) + 5 * (long long)b2;
-  M3<float> A1, A2, R0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float4 ca = __ldg(ra + 2 + k), cb = __ldg(rb + 2 + k);
-    A1(0, k) = ca.x; A1(1, k) = ca.y; A1(2, k) = ca.z;
-    A2(0, k) = cb.x; A2(1, k) = cb.y; A2(2, k) = cb.z;
+// Pair index of query qi, or -1 (status set, result NaN) when it is out of range.
+__device__ __forceinline__ int query_pair(const DistanceLaunch& L, long long qi) {
+  const int pi = L.pair_of_query ? __ldg(L.pair_of_query + qi) : 0;
+  if (pi < 0 || pi >= L.num_pairs) {
+    atomicOr(&L.ctr->status, DEV_ERR_PAIR);
+    L.dist[qi] = __longlong_as_double(0x7ff8000000000000ll);
+    return -1;
   }
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R0.m[i] = q.R[i];
-  const float4 r1a = __ldg(ra), r1b = __ldg(ra + 1), r2a = __ldg(rb), r2b = __ldg(rb + 1);
-  const float l1[2] = {r1b.x, r1b.y}, l2[2] = {r2b.x, r2b.y};
-  return rss_distance<float>(R0, v3(q.T[0], q.T[1], q.T[2]), A1, v3(r1a.x, r1a.y, r1a.z), l1, r1a.w, A2,
-                             v3(r2a.x, r2a.y, r2a.z), l2, r2a.w);
+  return pi;
 }
 
+// The plain FP64 form: one query per thread, FCL's traversal.
 template <int STACK>
-__global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, int prec) {
+__global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L) {
   for (;;) {
     const long long qi = (long long)atomicAdd(&L.ctr->work, 1ull);
     if (qi >= L.n) break;
-    const int pi = L.pair_of_query ? __ldg(L.pair_of_query + qi) : 0;
-    if (pi < 0 || pi >= L.num_pairs) {  // reported through the status word, query left NaN
-      atomicOr(&L.ctr->status, DEV_ERR_PAIR);
-      L.dist[qi] = __longlong_as_double(0x7ff8000000000000ll);
-      continue;
-    }
+    const int pi = query_pair(L, qi);
+    if (pi < 0) continue;
     const int2 mp = L.pairs[pi];
     const DevMesh A = L.meshes[mp.x];
     const DevMesh B = L.meshes[mp.y];
@@ -266,131 +227,69 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
     V3<double> T;
     rel_distance(ta, tb, R, T);
     DistOut o;
-    bool exact = (prec == 0);
-    if (!exact) {
-      QueryF32 qf;
-      make_query_f32(R, T, A.rmax, B.rmax, A.vmax, B.vmax, qf);
-      const float u = FCLG_U32;
-      const float tau = fmaxf(fabsf(qf.T[0]), fmaxf(fabsf(qf.T[1]), fabsf(qf.T[2])));
-      const float rss_abs = 64.f * u * (float)(A.rmax + B.rmax) + 64.f * u * 1.7321f * tau;
-      const float rel = 3.814697265625e-6f;  // 2^-18 of the distance
-      long long nbv = 0, nleaf = 0, nrc64 = 0;
-      // exact FP64 best so far (strict "<" in visit order, as DistanceResult::update);
-      // best_up is a float upper bound of it used for pruning
-      o.d = 1.7976931348623157e308;
-      o.id1 = o.id2 = 0;
-      o.P = o.Q = v3(0.0, 0.0, 0.0);
-      float best_up = 3.0e38f;
-      auto exact_leaf = [&](int p1, int p2) {
-        V3<double> P, Q;
-        const double d64 = leaf_distance64(A, B, p1, p2, R, T, P, Q);
-        ++nrc64;
-        if (o.d > d64) {
-          o.d = d64;
-          o.id1 = p1;
-          o.id2 = p2;
-          o.P = P;
-          o.Q = Q;
-          best_up = (float)d64 * (1.f + 2.f * u) + 1e-37f;
-        }
-      };
-      // preprocess pair (triangle 0, triangle 0)
-      exact_leaf(0, 0);
-      FStack stk[STACK];
-      int sp = 0;
-      int b1 = 0, b2 = 0;
-      for (;;) {
-        const int c1 = __float_as_int(__ldg(reinterpret_cast<const float4*>(A.nodes32) + 4 * (long long)b1 + 3).w);
-        const int c2 = __float_as_int(__ldg(reinterpret_cast<const float4*>(B.nodes32) + 4 * (long long)b2 + 3).w);
-        const bool l1 = c1 < 0, l2 = c2 < 0;
-        bool descend = false;
-        if (l1 && l2) {
-          ++nleaf;
-          const int p1 = -(c1 + 1), p2 = -(c2 + 1);
-          float sc;
-          const float d = tri_distance_f32(qf, reinterpret_cast<const float4*>(A.tri32) + 3 * (long long)p1,
-                                           reinterpret_cast<const float4*>(B.tri32) + 3 * (long long)p2, sc);
-          const float E = rel * d + 128.f * u * sc + qf.dabs * 2.f;
-          // near contact triDistance switches between its edge/face and overlap
-          // branches, so such pairs always take the exact value; otherwise only a
-          // pair whose FP32 interval can still reach the best is re-evaluated
-          if (d <= 3.90625e-3f * sc || d - E <= best_up) exact_leaf(p1, p2);
-        } else {
-          int a1, a2, e1, e2;
-          if (first_over_second(A, B, b1, b2, l1, l2)) {
-            a1 = c1; a2 = b2; e1 = c1 + 1; e2 = b2;
-          } else {
-            a1 = b1; a2 = c2; e1 = b1; e2 = c2 + 1;
-          }
-          float d1 = rss_distance_f32(qf, A, B, a1, a2);
-          float d2 = rss_distance_f32(qf, A, B, e1, e2);
-          d1 = d1 - (2.44140625e-4f * d1 + rss_abs);
-          d2 = d2 - (2.44140625e-4f * d2 + rss_abs);
-          nbv += 2;
-          if (sp >= STACK) {
-            atomicOr(&L.ctr->status, DEV_ERR_STACK);
-            break;
-          }
-          int f1, f2;
-          float fd;
-          if (d2 < d1) {
-            stk[sp++] = FStack{a1, a2, d1};
-            f1 = e1; f2 = e2; fd = d2;
-          } else {
-            stk[sp++] = FStack{e1, e2, d2};
-            f1 = a1; f2 = a2; fd = d1;
-          }
-          if (!(fd > best_up)) {
-            b1 = f1;
-            b2 = f2;
-            descend = true;
-          }
-        }
-        if (descend) continue;
-        bool found = false;
-        while (sp > 0) {
-          const FStack e = stk[--sp];
-          if (!(e.d > best_up)) {
-            b1 = e.b1;
-            b2 = e.b2;
-            found = true;
-            break;
-          }
-        }
-        if (!found) break;
-      }
-      o.nbv = nbv;
-      o.nleaf = nleaf;
-      o.nrc = nrc64;
-      o.status = 0;
-    }
-    if (exact) {
-      distance_query_fp64<STACK>(A, B, R, T, o);
+    distance_query_fp64<STACK>(A, B, R, T, o);
+    if (o.status) atomicOr(&L.ctr->status, o.status);
+    write_result(L, qi, o);
+  }
+}
+
+// The certified FP32 form (distance_traverse.cuh).  Each lane owns one query at a
+// time.  In every iteration of the warp loop the warp picks one phase and the lanes
+// whose query is in that phase advance it by one step; __syncwarp() then brings the
+// lanes back together.  Traversal steps run whenever lanes are traversing, except
+// that once at least kBatch lanes wait for an FP64 triangle distance (or for the
+// FP32 witness stage) those run first, so these long, FP64-heavy steps execute with
+// many lanes at once.  A lane whose query ends fetches the next one.  Queries that
+// the certified form does not take (DistCert::init) run the FP64 form in place.
+// Capped at 128 registers: the FP64 leaf and fallback functions spill a little.
+template <int STACK>
+__global__ void __launch_bounds__(128, 4) k_mesh_distance_cert(const DistanceLaunch L) {
+  constexpr int kBatch = 8;
+  DistCert<STACK> c;
+  long long qi = 0;
+  auto start = [&]() -> bool {
+    for (;;) {
+      qi = (long long)atomicAdd(&L.ctr->work, 1ull);
+      if (qi >= L.n) return false;
+      const int pi = query_pair(L, qi);
+      if (pi < 0) continue;
+      const int2 mp = L.pairs[pi];
+      double ta[12], tb[12];
+      load_tfs(L, qi, ta, tb);
+      M3<double> R;
+      V3<double> T;
+      rel_distance(ta, tb, R, T);
+      if (c.init(L.meshes + mp.x, L.meshes + mp.y, R, T)) return true;
+      DistOut o;
+      distance_query_fp64<STACK>(L.meshes[mp.x], L.meshes[mp.y], R, T, o);
       if (o.status) atomicOr(&L.ctr->status, o.status);
-      if (prec != 0) o.nrc = -1;  // marks an FP64 re-run
+      o.nrc = -1;  // marks an FP64 run
+      write_result(L, qi, o);
     }
-    L.dist[qi] = o.d;
-    if (L.ids) {
-      L.ids[2 * qi] = o.id1;
-      L.ids[2 * qi + 1] = o.id2;
+  };
+  bool have = start();
+  for (;;) {
+    const int ph = have ? c.phase : DC_DONE;
+    const unsigned mT = __ballot_sync(0xffffffffu, ph == DC_TRAVERSE);
+    const unsigned mW = __ballot_sync(0xffffffffu, ph == DC_WITNESS);
+    const unsigned mE = __ballot_sync(0xffffffffu, ph == DC_EXACT);
+    if (!(mT | mW | mE)) break;
+    int run;
+    if (__popc(mE) >= kBatch || (mE && !mT && !mW))
+      run = DC_EXACT;
+    else if (__popc(mW) >= kBatch || (mW && !mT))
+      run = DC_WITNESS;
+    else
+      run = DC_TRAVERSE;
+    if (ph == run) {
+      c.run_phase(run);
+      if (c.phase == DC_DONE) {
+        if (c.o.status) atomicOr(&L.ctr->status, c.o.status);
+        write_result(L, qi, c.o);
+        have = start();
+      }
     }
-    if (L.nearest && L.points) {
-      M3<double> R1;
-      for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) R1(r, c) = ta[4 * r + c];
-      const V3<double> t1 = v3(ta[3], ta[7], ta[11]);
-      const V3<double> w1 = mulv(R1, o.P) + t1;
-      const V3<double> w2 = mulv(R1, o.Q) + t1;
-      double* out = L.points + 6 * qi;
-      out[0] = w1.x; out[1] = w1.y; out[2] = w1.z;
-      out[3] = w2.x; out[4] = w2.y; out[5] = w2.z;
-    }
-    if (L.margins && L.within) L.within[qi] = (o.d <= __ldg(L.margins + qi)) ? 1 : 0;
-    if (L.want_stats) {
-      if (L.nbv) L.nbv[qi] = o.nbv;
-      if (L.nleaf) L.nleaf[qi] = o.nleaf;
-      if (L.nrecheck) L.nrecheck[qi] = o.nrc;
-    }
+    __syncwarp();
   }
 }
 
@@ -399,20 +298,29 @@ __global__ void __launch_bounds__(128) k_mesh_distance(const DistanceLaunch L, i
 cudaError_t launch_mesh_distance(const DistanceLaunch& L, int precision, int stack_entries, int grid, int block,
                                  cudaStream_t s) {
   ++g_kernel_launches;
-  if (stack_entries <= 64)
-    k_mesh_distance<64><<<grid, block, 0, s>>>(L, precision);
-  else
-    k_mesh_distance<256><<<grid, block, 0, s>>>(L, precision);
+  if (precision == 0) {
+    if (stack_entries <= 64)
+      k_mesh_distance<64><<<grid, block, 0, s>>>(L);
+    else
+      k_mesh_distance<256><<<grid, block, 0, s>>>(L);
+  } else {
+    if (stack_entries <= 64)
+      k_mesh_distance_cert<64><<<grid, block, 0, s>>>(L);
+    else
+      k_mesh_distance_cert<256><<<grid, block, 0, s>>>(L);
+  }
   return cudaGetLastError();
 }
 
 int distance_grid(int precision, int stack_entries, int block) {
-  (void)precision;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, stack_entries <= 64 ? (const void*)k_mesh_distance<64> : (const void*)k_mesh_distance<256>, block, 0);
+  const void* k = precision == 0
+                      ? (stack_entries <= 64 ? (const void*)k_mesh_distance<64> : (const void*)k_mesh_distance<256>)
+                      : (stack_entries <= 64 ? (const void*)k_mesh_distance_cert<64>
+                                             : (const void*)k_mesh_distance_cert<256>);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }

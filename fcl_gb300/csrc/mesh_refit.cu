@@ -183,6 +183,7 @@ int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool r
   d.vmax = bd[0] * (1.0 + 1e-12);
   d.cmax = bd[1] * (1.0 + 1e-12);
   d.rmax = bd[2] * (1.0 + 1e-12);
+  d.refitted = 1;
   m->info.max_abs_coord = bd[0];
   if ((e = cudaMemcpyAsync(m->first_vertex, cur, 3 * sizeof(double), cudaMemcpyDeviceToHost, s)) ||
       (e = cudaStreamSynchronize(s)))

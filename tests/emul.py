@@ -123,3 +123,18 @@ def motion(beg, end, t, kind="trans"):
 
 def translation_motion(beg, end, t):
     return motion(beg, end, t, "trans")
+
+
+def distance_cert(a, b, tf2):
+    """The certified FP32 distance traversal run on the host (tf1 = I)."""
+    n = tf2.shape[0]
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(n, 12)
+    d = np.zeros(n); ids = np.zeros((n, 2), np.int32); pts = np.zeros((n, 2, 3))
+    nbv = np.zeros(n, np.int64); nl = np.zeros(n, np.int64); nrc = np.zeros(n, np.int64)
+    av, at = [np.ascontiguousarray(x) for x in a]
+    bv, bt = [np.ascontiguousarray(x) for x in b]
+    rc = lib().emu_distance_cert(_p(av), C.c_int64(av.shape[0]), _p(at), C.c_int64(at.shape[0]), _p(bv),
+                                 C.c_int64(bv.shape[0]), _p(bt), C.c_int64(bt.shape[0]), C.c_int64(n), _p(tf2),
+                                 _p(d), _p(ids), _p(pts), _p(nbv), _p(nl), _p(nrc))
+    assert rc == 0
+    return d, ids, pts, nbv, nl, nrc

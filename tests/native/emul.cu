@@ -7,6 +7,7 @@
 
 #include "bvh_build.h"
 #include "collide_traverse.cuh"
+#include "distance_traverse.cuh"
 #include "refit.cuh"
 #include "shape_pair.cuh"
 #include "tri_contact.cuh"
@@ -47,6 +48,8 @@ void make_mesh(const double* v, int64_t nv, const int32_t* t, int64_t nt, HostMe
   d.vmax = vmax * (1.0 + 1e-12);
   d.cmax = m.pk.cmax * (1.0 + 1e-12);
   d.rmax = m.pk.rmax * (1.0 + 1e-12);
+  d.refitted = 0;
+  d.pad2 = 0;
 }
 
 struct VecSink {
@@ -78,6 +81,34 @@ struct SplitHostSink {
 }  // namespace
 
 extern "C" {
+
+// Certified FP32 distance traversal on the host (the device code of the FP32 form):
+// per query distance, triangle ids, witness points (first mesh's frame: tf1 = I),
+// statistics; returns -1 when a query fell back to FP64 or overflowed its stack.
+int emu_distance_cert(const double* v1, int64_t nv1, const int32_t* t1, int64_t nt1, const double* v2, int64_t nv2,
+                      const int32_t* t2, int64_t nt2, int64_t n, const double* tf2, double* dist, int32_t* ids,
+                      double* pts, int64_t* nbv, int64_t* nleaf, int64_t* nrc) {
+  HostMesh A, B;
+  make_mesh(v1, nv1, t1, nt1, A);
+  make_mesh(v2, nv2, t2, nt2, B);
+  const double I[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  for (int64_t q = 0; q < n; ++q) {
+    M3<double> R;
+    V3<double> T;
+    rel_distance(I, tf2 + 12 * q, R, T);
+    DistOut o;
+    if (!distance_query_cert<256>(A.view, B.view, R, T, o) || o.status) return -1;
+    dist[q] = o.d;
+    ids[2 * q] = o.id1;
+    ids[2 * q + 1] = o.id2;
+    const double p[6] = {o.P.x, o.P.y, o.P.z, o.Q.x, o.Q.y, o.Q.z};
+    for (int k = 0; k < 6; ++k) pts[6 * q + k] = p[k];
+    nbv[q] = o.nbv;
+    nleaf[q] = o.nleaf;
+    nrc[q] = o.nrc;
+  }
+  return 0;
+}
 
 // Work-splitting batch on the host: same rounds, frontier dumps and item-tree
 // assembly as the GPU path (budget = BV tests per item per round).

@@ -131,3 +131,43 @@ def test_replace_then_update_bit_exact_vs_oracle():
     en, efc = emul.refit(v, t, [f1, f2, f3], [1, 0, 1])
     assert np.array_equal(ofc, efc)
     assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
+
+
+def _cert_vs_oracle(a, b, tf2):
+    oa, ob = O.Mesh(*a), O.Mesh(*b)
+    od, oids, opts, _, _ = O.distance_batch(oa, ob, tf2, nearest=True, nthreads=4)
+    ed, eids, epts, _, _, nrc = emul.distance_cert(a, b, tf2)
+    return od, opts, ed, epts, nrc
+
+
+@pytest.mark.parametrize("seed", [2, 5])
+def test_certified_fp32_distance_equals_oracle_c0(seed):
+    """The FP32 distance form (distance_traverse.cuh) run on the host: its distance is
+    the smallest FP64 triDistance over all triangle pairs, so it equals FCL's, and the
+    witness points are those of a pair at that distance (identical at shared vertices)."""
+    w = W.config0(n_poses=200, seed=seed)
+    od, opts, ed, epts, nrc = _cert_vs_oracle(w.meshes[0], w.meshes[1], w.tf2)
+    assert np.array_equal(ed, od)
+    sep = od > 0
+    assert np.abs(epts[sep] - opts[sep]).max() <= 1e-12
+    assert nrc.mean() < 40  # far fewer FP64 triangle distances than FCL's ~230 per query
+
+
+def test_certified_fp32_distance_reference_fixture(golden):
+    """FCL's env/rob fixture (coordinates up to 3,000) at its own poses and at random ones."""
+    a = (golden["env_v"], golden["env_t"]); b = (golden["rob_v"], golden["rob_t"])
+    tf = np.concatenate([golden["tf"], W.random_poses(60, -3000, 3000, 7)])
+    od, opts, ed, epts, _ = _cert_vs_oracle(a, b, tf)
+    assert np.array_equal(ed, od)
+    sep = od > 0
+    assert np.abs(epts[sep] - opts[sep]).max() <= 1e-12 * np.abs(opts).max()
+
+
+def test_certified_fp32_distance_separated_pairs():
+    w = W.config2(total_poses=900, n_pairs=3, tri_hi=30000, seed=4)
+    for p in range(3):
+        idx = np.nonzero(w.pair == p)[0][:100]
+        a, b = w.meshes[w.pairs[p, 0]], w.meshes[w.pairs[p, 1]]
+        od, opts, ed, epts, _ = _cert_vs_oracle(a, b, w.tf2[idx])
+        assert np.array_equal(ed, od)
+        assert np.abs(epts - opts).max() <= 1e-12
