@@ -91,7 +91,9 @@ def _cpu_sample(w, n_sample, seed=0):
     return W.subsample(w, n_sample, seed)
 
 
-def _time_cpu(w_sample, nthreads):
+def _time_cpu(w_sample, nthreads, results=None):
+    """Times the oracle's collide over the sample; fills results[p] = (sample indices,
+    counts, contacts) when a dict is given."""
     from oracle import pyoracle as O
     om = {}
     for p in np.unique(w_sample.pair):
@@ -102,10 +104,32 @@ def _time_cpu(w_sample, nthreads):
     total = 0
     for p in np.unique(w_sample.pair):
         idx = np.nonzero(w_sample.pair == p)[0]
-        c, _, _, _ = O.collide_batch(om[w_sample.pairs[p, 0]], om[w_sample.pairs[p, 1]], w_sample.tf2[idx],
-                                     num_max_contacts=100000, nthreads=nthreads)
+        c, ct, _, _ = O.collide_batch(om[w_sample.pairs[p, 0]], om[w_sample.pairs[p, 1]], w_sample.tf2[idx],
+                                      num_max_contacts=100000, nthreads=nthreads)
         total += int(c.sum())
+        if results is not None:
+            results[int(p)] = (idx, c, ct)
     return time.perf_counter() - t0, total
+
+
+def _oracle_check(w, sample_idx, results, gpu):
+    """Compares the GPU's counts and contact lists of the sampled queries with the
+    oracle's (same triangle pairs in the same order)."""
+    counts = gpu["counts"].cpu().numpy()
+    offs = gpu["offsets"].cpu().numpy()
+    cont = gpu["contacts"].cpu().numpy()
+    ok = True
+    for p, (idx, c, ct) in results.items():
+        q = sample_idx[idx]
+        ok &= bool(np.array_equal(counts[q], c))
+        if not ok:
+            break
+        off = np.concatenate([[0], np.cumsum(c)])
+        for j, qq in enumerate(q):
+            if not np.array_equal(cont[offs[qq]:offs[qq + 1]], ct[off[j]:off[j + 1]]):
+                ok = False
+                break
+    return ok
 
 
 def _time_cpu_distance(w_sample, nthreads):
@@ -730,14 +754,18 @@ def run_gpu(args):
             pass
 
     cpu = None
+    oracle_checked = (0, None)
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import pyoracle as O
         O.build()
         threads = O.hardware_threads()
         ws = _cpu_sample(w, args.cpu_sample, seed=123)
-        dt, _ = _time_cpu(ws, threads)
+        results = {}
+        dt, _ = _time_cpu(ws, threads, results)
         cpu = {"value": args.cpu_sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{args.cpu_sample} queries drawn uniformly from the {n}-query workload"}
+        from fcl_gb300 import workloads as W
+        oracle_checked = (ws.n, _oracle_check(w, W.subsample_indices(n, args.cpu_sample, 123), results, fp32))
 
     if rank == 0:
         line = {
@@ -760,6 +788,9 @@ def run_gpu(args):
                            max(1, int(n * args.fp64_scale))},
             "fp32_vs_fp64_speedup": None if value64 is None else value / value64,
             "exact_hits": exact,
+            # the CPU-baseline sample (uniform over the headline queries) checked against
+            # the oracle: counts and contact lists in DFS order
+            "oracle_checked_queries": oracle_checked[0], "oracle_exact": oracle_checked[1],
             "stats": {"bv_tests": n_bv, "leaf_tests": n_leaf, "fp64_rechecks": n_rc,
                       "recheck_rate": n_rc / max(1, n_bv + n_leaf), "contacts": total_contacts,
                       "colliding_fraction": float((fp32["counts"] > 0).float().mean().item()),

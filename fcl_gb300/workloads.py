@@ -200,6 +200,21 @@ def mesh_pair_set(n_pairs: int = 64, seed: int = 1, tri_lo: int = 500, tri_hi: i
     return meshes, pairs
 
 
+def mesh_pair_set_subset(pair_ids, n_pairs: int = 64, seed: int = 1, tri_lo: int = 500, tri_hi: int = 200000):
+    """Only the meshes of the listed pairs of mesh_pair_set (same draws, same meshes),
+    as {mesh index: (verts, tris)}; the rest of the set is not generated."""
+    rng = np.random.default_rng(seed)
+    want = {2 * int(p) + j for p in pair_ids for j in (0, 1)}
+    out = {}
+    for k in range(2 * n_pairs):
+        T = _loguniform_int(rng, tri_lo, tri_hi)
+        freq = max(1, int(round(math.sqrt(T / 20.0))))
+        radii = rng.uniform(0.5, 1.5, size=3)
+        if k in want:
+            out[k] = perturbed_ellipsoid(freq, radii, 0.01, seed * 100003 + k)
+    return out
+
+
 def config1(scale: float = 1.0, seed: int = 1, n_pairs: int = 64, tri_hi: int = 200000,
             pose_lo: int = 2000, pose_hi: int = 50000) -> MeshPairWorkload:
     """Exhaustive contacts: per pair log-uniform [2,000, 50,000] poses (times `scale`),
@@ -227,10 +242,15 @@ def config2(total_poses: int = 1_000_000, seed: int = 1, n_pairs: int = 64, tri_
     return MeshPairWorkload(meshes=meshes, pairs=pairs, pair=pair, tf2=tf2, margin=margin, name="c2")
 
 
+def subsample_indices(total: int, n: int, seed: int = 0) -> np.ndarray:
+    """The query indices subsample() keeps: n drawn uniformly without replacement, sorted."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(total, size=min(n, total), replace=False))
+
+
 def subsample(w: MeshPairWorkload, n: int, seed: int = 0) -> MeshPairWorkload:
     """A uniform random subset of n queries (sorted by original order)."""
-    rng = np.random.default_rng(seed)
-    idx = np.sort(rng.choice(w.n, size=min(n, w.n), replace=False))
+    idx = subsample_indices(w.n, n, seed)
     return MeshPairWorkload(meshes=w.meshes, pairs=w.pairs, pair=w.pair[idx], tf2=w.tf2[idx],
                             tf1=None if w.tf1 is None else w.tf1[idx],
                             margin=None if w.margin is None else w.margin[idx], name=w.name + "_sub")

@@ -224,3 +224,49 @@ def test_distance_rejects_out_of_range_pair_index(gpu_lib):
     assert e.value.code == N.FCLGPU_ERR_DEVICE_STATUS
     good = api.distance_batch(ms, w.pairs, None, tf2, pair_of_query=torch.zeros_like(pq), precision="fp32")
     assert torch.isfinite(good["min_distance"]).all()
+
+
+def _largest_c1_workload(n_per=100):
+    """The C1 pairs that hold the meshes of 150k-200k triangles (tree depth about 38),
+    n_per poses each with C1's translations U[-1.5,1.5]^3."""
+    big = [3, 13, 16, 52]
+    ms = W.mesh_pair_set_subset(big)
+    ids = sorted(ms)
+    local = {k: i for i, k in enumerate(ids)}
+    pairs = np.array([[local[2 * p], local[2 * p + 1]] for p in big], np.int32)
+    pair = np.repeat(np.arange(len(big), dtype=np.int32), n_per)
+    tf2 = W.random_poses(pair.shape[0], -1.5, 1.5, 21)
+    return W.MeshPairWorkload(meshes=[ms[k] for k in ids], pairs=pairs, pair=pair, tf2=tf2, name="c1_largest")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_collide_largest_c1_meshes_match_oracle(gpu_lib, precision):
+    """Exhaustive contacts (num_max_contacts = 100,000) on the largest C1 meshes: counts,
+    contact lists in DFS order and traversal statistics equal the oracle's."""
+    w = _largest_c1_workload()
+    assert max(t.shape[0] for _, t in w.meshes) >= 150000
+    ms = _meshes(w)
+    out = api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                            precision=precision, statistics=True)
+    C, ct, BV, LF = _oracle_collide(w, 100000)
+    assert (C > 0).sum() >= 50 and C.max() > 1000
+    assert np.array_equal(out["counts"], C)
+    assert np.array_equal(out["contacts"], ct)
+    assert np.array_equal(out["num_bv_tests"], BV) and np.array_equal(out["num_leaf_tests"], LF)
+
+
+def test_distance_fp32_largest_c1_meshes(gpu_lib):
+    """Distance on the largest C1 meshes at C2's separations: the FP32 form against the oracle."""
+    w = _largest_c1_workload(60)
+    w.tf2 = W.random_poses(w.n, 1.5, 4.0, 22)
+    ms = _meshes(w)
+    out = api.distance_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, nearest_points=True,
+                             precision="fp32")
+    om = [O.Mesh(v, t) for v, t in w.meshes]
+    d = np.empty(w.n); pts = np.empty((w.n, 2, 3))
+    for p in range(w.pairs.shape[0]):
+        idx = np.nonzero(w.pair == p)[0]
+        dd, _, pp, _, _ = O.distance_batch(om[w.pairs[p, 0]], om[w.pairs[p, 1]], w.tf2[idx], nearest=True,
+                                           nthreads=8)
+        d[idx] = dd; pts[idx] = pp
+    _dist_check(out, d, pts)
