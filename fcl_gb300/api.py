@@ -844,6 +844,106 @@ class DynamicAABBTreeCollisionManager:
         out["node_visits"] = res.total_node_visits
         return out
 
+    def collide_contacts(self, refs=None, tf=None, num_max_contacts: int = 1, precision: str = "fp32",
+                         stream=None):
+        """Contact lists of manager.collide(obj, cdata, DefaultCollisionFunction) for every
+        query object (refs, tf: host numpy), or of manager.collide(cdata,
+        DefaultCollisionFunction) -- the scene against itself -- when refs is None.
+        Returns counts (per query; per scene object o2 in the self case), offsets and
+        contacts (rows (object, b1, b2); in the self case (o1, b1, b2) with o1 < o2).  Each
+        (query, object) pair is evaluated with its own cap of num_max_contacts; per query
+        the objects come in ascending index order, each object's contacts in the order
+        FCL's narrowphase adds them."""
+        req = N.BpContactsRequest(int(num_max_contacts), _prec(precision), 0)
+        if refs is not None:
+            refs = np.ascontiguousarray(refs, np.int32).reshape(-1, 2)
+            tf = np.ascontiguousarray(tf, np.float64).reshape(-1, 12)
+            n = refs.shape[0]
+        else:
+            n = self.size()
+        counts = np.zeros(n, np.int64)
+        offsets = np.zeros(n + 1, np.int64)
+        cap = max(64, 2 * n)
+        for _ in range(2):
+            contacts = np.zeros((cap, 3), np.int32)
+            res = N.BpContactsResult(counts.ctypes.data, offsets.ctypes.data, contacts.ctypes.data, cap, 0, 0, 0)
+            if refs is not None:
+                rc = N.lib().fclgpu_broadphase_collide_contacts(self.handle, refs.ctypes.data, n, tf.ctypes.data,
+                                                                C.byref(req), C.byref(res), stream)
+            else:
+                rc = N.lib().fclgpu_broadphase_self_collide_contacts(self.handle, C.byref(req), C.byref(res), stream)
+            if rc == N.FCLGPU_ERR_CAPACITY:
+                cap = int(res.total_contacts)
+                continue
+            N.check(rc, "fclgpu_broadphase_collide_contacts")
+            return {"counts": counts, "offsets": offsets, "contacts": contacts[: int(res.total_contacts)],
+                    "total_candidates": int(res.total_candidates)}
+        raise N.FclGpuError(N.FCLGPU_ERR_CAPACITY, "fclgpu_broadphase_collide_contacts", "contact total changed")
+
+    def self_distance(self, nearest_points: bool = True, precision: str = "fp32", stream=None):
+        """manager.distance(cdata, DefaultDistanceFunction): the smallest distance between
+        two scene objects, with o1 < o2, their triangle ids and world witness points."""
+        req = N.BpDistanceRequest(int(nearest_points), _prec(precision))
+        r = N.BpSelfDistanceResult()
+        N.check(N.lib().fclgpu_broadphase_self_distance(self.handle, C.byref(req), C.byref(r), stream),
+                "fclgpu_broadphase_self_distance")
+        return {"min_distance": r.min_distance, "o1": r.o1, "o2": r.o2, "b1": r.b1, "b2": r.b2,
+                "nearest_points": np.array(r.nearest_points[:]).reshape(2, 3), "total_candidates": r.total_candidates}
+
+    def collide(self, other=None, request: "CollisionRequest | None" = None, result: "CollisionResult | None" = None):
+        """FCL's three collide forms with DefaultCollisionFunction: other = None -> the
+        scene against itself (collide(cdata, callback)); other = (ref, tf) of one query
+        object (collide(obj, cdata, callback)); other = another manager -> every object of
+        the other manager against this scene (collide(other_manager, cdata, callback)).
+        Appends Contact(o1, o2, b1, b2) rows (object indices; in the other-manager form o2
+        is the other manager's object) up to request.num_max_contacts in all, in the order
+        collide_contacts states, and returns result.numContacts()."""
+        request = request or CollisionRequest()
+        result = result if result is not None else CollisionResult()
+        if other is None:
+            out = self.collide_contacts(None, None, request.num_max_contacts, request.precision)
+            q_of = np.repeat(np.arange(self.size()), out["counts"])
+        elif isinstance(other, DynamicAABBTreeCollisionManager):
+            out = self.collide_contacts(other._refs, other._tf, request.num_max_contacts, request.precision)
+            q_of = np.repeat(np.arange(other.size()), out["counts"])
+        else:
+            ref, tf = other
+            out = self.collide_contacts(np.asarray(ref, np.int32).reshape(1, 2), np.asarray(tf).reshape(1, 12),
+                                        request.num_max_contacts, request.precision)
+            q_of = np.zeros(int(out["counts"][0]), np.int64)
+        room = max(0, request.num_max_contacts - len(result.contacts))
+        for (o, b1, b2), q in list(zip(out["contacts"], q_of))[:room]:
+            result.contacts.append(Contact(int(o), int(q), int(b1), int(b2)))
+        return result.numContacts()
+
+    def distance(self, other=None, request: "DistanceRequest | None" = None,
+                 result: "DistanceResult | None" = None) -> float:
+        """FCL's distance forms with DefaultDistanceFunction: other = None -> the scene
+        against itself; other = (ref, tf) of one query object; other = another manager.
+        Updates result with DistanceResult's strict "<" (o1, o2 = object indices)."""
+        request = request or DistanceRequest()
+        result = result if result is not None else DistanceResult()
+        if other is None:
+            r = self.self_distance(request.enable_nearest_points, request.precision)
+            cand = [(r["min_distance"], r["o1"], r["o2"], r["b1"], r["b2"], r["nearest_points"])]
+        else:
+            if isinstance(other, DynamicAABBTreeCollisionManager):
+                refs, tf = other._refs, other._tf
+            else:
+                refs, tf = np.asarray(other[0], np.int32).reshape(1, 2), np.asarray(other[1]).reshape(1, 12)
+            out = self.distance_batch(refs, tf, nearest_points=request.enable_nearest_points,
+                                      precision=request.precision)
+            q = int(np.argmin(out["min_distance"])) if len(out["min_distance"]) else 0
+            cand = [(float(out["min_distance"][q]), int(out["object"][q]), q, int(out["ids"][q, 0]),
+                     int(out["ids"][q, 1]), out["nearest_points"][q])] if len(out["min_distance"]) else []
+        for d, o1, o2, b1, b2, pts in cand:
+            if result.min_distance > d:
+                result.min_distance = float(d)
+                result.o1, result.o2, result.b1, result.b2 = o1, o2, b1, b2
+                if request.enable_nearest_points:
+                    result.nearest_points = np.asarray(pts).copy()
+        return result.min_distance
+
     def _release(self):
         h = getattr(self, "handle", None)
         if h is not None and N._lib is not None:
@@ -974,6 +1074,35 @@ def mesh_shape_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_
                                             shape_idx.ctypes.data, tf_mesh.ctypes.data, tf_shape.ctypes.data,
                                             C.byref(req), C.byref(res), stream), "fclgpu_mesh_shape_batch")
     return out
+
+
+def mesh_shape_contacts_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_shape,
+                              num_max_contacts: int = 1, stream=None):
+    """fcl::collide of BVHModel<OBBRSS> meshes against convex shapes with the contact
+    list: per pair the triangles FCL records as Contact(mesh, shape, triangle, NONE), in
+    the order its traversal adds them (at most num_max_contacts).  Returns counts,
+    offsets (n + 1) and tris.  Host numpy inputs."""
+    hs = _handles(meshes)
+    mesh_idx = np.ascontiguousarray(mesh_idx, np.int32)
+    shape_idx = np.ascontiguousarray(shape_idx, np.int32)
+    n = mesh_idx.shape[0]
+    tf_mesh = np.ascontiguousarray(tf_mesh, np.float64).reshape(n, 12)
+    tf_shape = np.ascontiguousarray(tf_shape, np.float64).reshape(n, 12)
+    counts = np.zeros(n, np.int32)
+    offsets = np.zeros(n + 1, np.int64)
+    cap = max(16, 4 * n)
+    for _ in range(2):
+        tris = np.zeros(cap, np.int32)
+        res = N.MeshShapeContactsResult(counts.ctypes.data, offsets.ctypes.data, tris.ctypes.data, cap, 0)
+        rc = N.lib().fclgpu_mesh_shape_contacts(hs, len(meshes), shapes.handle, n, mesh_idx.ctypes.data,
+                                                shape_idx.ctypes.data, tf_mesh.ctypes.data, tf_shape.ctypes.data,
+                                                int(num_max_contacts), C.byref(res), stream)
+        if rc == N.FCLGPU_ERR_CAPACITY:
+            cap = int(res.total_contacts)
+            continue
+        N.check(rc, "fclgpu_mesh_shape_contacts")
+        return {"counts": counts, "offsets": offsets, "tris": tris[: int(res.total_contacts)]}
+    raise N.FclGpuError(N.FCLGPU_ERR_CAPACITY, "fclgpu_mesh_shape_contacts", "contact total changed between calls")
 
 
 # ------------------------------------------------------------------- autotuner ----

@@ -422,6 +422,7 @@ __global__ void __launch_bounds__(128) k_bp_candidates(BpSceneView S, BpQueryVie
   int cnt = 0;
   long long visits = 0;
   auto leaf = [&](int obj) {
+    if (Q.self && obj >= q) return;
     const double* a = S.aabb64 + 6 * (long long)obj;
     const bool take = WITHIN ? (dist64(qb, a) <= bound) : ov64(a, qb);
     if (take) {
@@ -522,6 +523,7 @@ __global__ void __launch_bounds__(128) k_bp_dist_bound(BpSceneView S, BpQueryVie
   load_qbox(Q, q, qb);
   double best = DBL_MAX;
   auto leaf = [&](int obj) {
+    if (Q.self && obj >= q) return;
     if (dist64(qb, S.aabb64 + 6 * (long long)obj) > best) return;
     best = fmin(best, pair_upper_bound(S, Q, obj, q));
   };
@@ -795,6 +797,81 @@ __global__ void k_bp_reduce_distance(long long nq, const int64_t* off, const int
   }
 }
 
+// ------------------------------------------------------------- contact lists ----
+
+// One thread per query: its candidate slots sorted by object index (insertion sort;
+// a query overlaps few objects).
+__global__ void k_bp_sort_segments(long long nq, const int64_t* off, const int2* pairs, int64_t* perm) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const long long lo = off[q], hi = off[q + 1];
+    for (long long i = lo; i < hi; ++i) {
+      const int oi = pairs[i].y;
+      long long j = i;
+      while (j > lo && pairs[perm[j - 1]].y > oi) {
+        perm[j] = perm[j - 1];
+        --j;
+      }
+      perm[j] = i;
+    }
+  }
+}
+
+__global__ void k_bp_inverse_index(const int64_t* list, long long nl, int32_t* index) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nl; k += stride)
+    index[list[k]] = (int32_t)k;
+}
+
+__global__ void k_bp_gather_counts(const int64_t* perm, long long n, const int32_t* hit, int32_t* ccount) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) ccount[j] = hit[perm[j]];
+}
+
+__global__ void k_bp_query_contacts(long long nq, const int64_t* off, const int64_t* coff, int64_t* counts,
+                                    int64_t* out_off) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q <= nq; q += stride) {
+    const int64_t a = coff[off[q]];
+    if (out_off) out_off[q] = a;
+    if (q < nq && counts) counts[q] = coff[off[q + 1]] - a;
+  }
+}
+
+__global__ void k_bp_fill_contacts(const int64_t* perm, long long n, const int2* pairs, const int32_t* kind,
+                                   const int32_t* hit, const int64_t* coff, const int32_t* mm_index,
+                                   const int64_t* mm_off, const int32_t* mm_contacts, const int32_t* ms_index,
+                                   const int64_t* ms_off, const int32_t* ms_tris, int32_t* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const long long slot = perm[j];
+    const int c = hit[slot];
+    if (c <= 0) continue;
+    const int obj = pairs[slot].y;
+    int32_t* o = out + 3 * coff[j];
+    const int k = kind[slot];
+    if (k == 0) {
+      o[0] = obj;
+      o[1] = -1;
+      o[2] = -1;
+    } else if (k == 1) {
+      const int32_t* src = mm_contacts + 2 * mm_off[mm_index[slot]];
+      for (int t = 0; t < c; ++t) {
+        o[3 * t] = obj;
+        o[3 * t + 1] = src[2 * t];
+        o[3 * t + 2] = src[2 * t + 1];
+      }
+    } else {
+      const int32_t* src = ms_tris + ms_off[ms_index[slot]];
+      for (int t = 0; t < c; ++t) {
+        o[3 * t] = obj;
+        o[3 * t + 1] = src[t];
+        o[3 * t + 2] = -1;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launches ----
@@ -982,6 +1059,46 @@ cudaError_t launch_bp_reduce_distance(int64_t nq, const int64_t* offsets, const 
   if (nq <= 0) return cudaSuccess;
   k_bp_reduce_distance<<<grid_for(nq, 256), 256, 0, s>>>(nq, offsets, pairs, dist, b12, pts, min_distance, object,
                                                          ids, nearest);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_sort_segments(int64_t nq, const int64_t* offsets, const int2* pairs, int64_t* perm,
+                                    cudaStream_t s) {
+  k_bp_sort_segments<<<grid_for(nq, 128), 128, 0, s>>>(nq, offsets, pairs, perm);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_inverse_index(const int64_t* list, int64_t nlist, int32_t* index, cudaStream_t s) {
+  if (nlist <= 0) return cudaSuccess;
+  k_bp_inverse_index<<<grid_for(nlist, 256), 256, 0, s>>>(list, nlist, index);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_gather_counts(const int64_t* perm, int64_t total, const int32_t* hit, int32_t* ccount,
+                                    cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  k_bp_gather_counts<<<grid_for(total, 256), 256, 0, s>>>(perm, total, hit, ccount);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_query_contacts(int64_t nq, const int64_t* offsets, const int64_t* coff, int64_t* counts,
+                                     int64_t* out_offsets, cudaStream_t s) {
+  k_bp_query_contacts<<<grid_for(nq + 1, 256), 256, 0, s>>>(nq, offsets, coff, counts, out_offsets);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_fill_contacts(const int64_t* perm, int64_t total, const int2* pairs, const int32_t* kind,
+                                    const int32_t* hit, const int64_t* coff, const int32_t* mm_index,
+                                    const int64_t* mm_off, const int32_t* mm_contacts, const int32_t* ms_index,
+                                    const int64_t* ms_off, const int32_t* ms_tris, int32_t* out, cudaStream_t s) {
+  if (total <= 0) return cudaSuccess;
+  k_bp_fill_contacts<<<grid_for(total, 128), 128, 0, s>>>(perm, total, pairs, kind, hit, coff, mm_index, mm_off,
+                                                          mm_contacts, ms_index, ms_off, ms_tris, out);
   ++g_kernel_launches;
   return cudaGetLastError();
 }

@@ -74,6 +74,9 @@ struct BpQueryView {
   const double* tf;     // 12 per query
   const double* aabb64; // 6 per query
   const float* aabb32;  // 6 per query
+  // 1: the queries are the scene objects themselves (query q is object q) and only
+  // objects of a smaller index are candidates, so each unordered pair is met once
+  int32_t self = 0;
 };
 
 enum : uint32_t { BP_ERR_STACK = 1u, BP_ERR_REF = 2u };
@@ -137,6 +140,25 @@ cudaError_t launch_bp_scatter_hits(const int64_t* list, int64_t nlist, const int
                                    cudaStream_t s);
 cudaError_t launch_bp_scatter_dist(const int64_t* list, int64_t nlist, const double* d, const int32_t* ids,
                                    const double* pts, double* dist, int32_t* b12, double* outpts, cudaStream_t s);
+
+// Contact lists.  perm: each query's candidate slots sorted by scene-object index.
+cudaError_t launch_bp_sort_segments(int64_t nq, const int64_t* offsets, const int2* pairs, int64_t* perm,
+                                    cudaStream_t s);
+// index[list[k]] = k for the nlist slots of one pair kind
+cudaError_t launch_bp_inverse_index(const int64_t* list, int64_t nlist, int32_t* index, cudaStream_t s);
+// ccount[j] = contacts of slot perm[j] (hit)
+cudaError_t launch_bp_gather_counts(const int64_t* perm, int64_t total, const int32_t* hit, int32_t* ccount,
+                                    cudaStream_t s);
+// per query: counts[q] and offsets[q] of its contacts from the scanned per-slot counts
+cudaError_t launch_bp_query_contacts(int64_t nq, const int64_t* offsets, const int64_t* coff, int64_t* counts,
+                                     int64_t* out_offsets, cudaStream_t s);
+// (object, b1, b2) triples of every slot in perm order at coff[j]: shape pairs
+// (object, -1, -1); mesh-mesh pairs the (b1, b2) list of their collide; mesh-shape
+// pairs (object, triangle, -1)
+cudaError_t launch_bp_fill_contacts(const int64_t* perm, int64_t total, const int2* pairs, const int32_t* kind,
+                                    const int32_t* hit, const int64_t* coff, const int32_t* mm_index,
+                                    const int64_t* mm_off, const int32_t* mm_contacts, const int32_t* ms_index,
+                                    const int64_t* ms_off, const int32_t* ms_tris, int32_t* out, cudaStream_t s);
 
 // Per-query reductions over the candidate segments [offsets[q], offsets[q+1]).
 cudaError_t launch_bp_reduce_collide(int64_t nq, const int64_t* offsets, const int2* pairs, const int32_t* hit,

@@ -87,6 +87,9 @@ struct BpScratch {
   Buf pairs, kind, hit, dist, b12, pts, list;
   Buf m_pair, m_tf1, m_tf2, m_counts, m_dist, m_ids, m_pts;
   Buf x_midx, x_sidx, x_counts, x_tri, qdone, x_bvsrc, x_need, x_bvtab, x_group, x_gcount;
+  // contact lists: mesh-shape lists and slot index, mesh-mesh lists and slot index,
+  // the per-query order of the slots and the scanned contact counts
+  Buf x_loff, x_ltris, x_index, mm_off, mm_cont, mm_index, perm, ccount, coff, c_out;
   Buf h_refs, h_tf, h_out1, h_out2, h_out3, h_out4;
 };
 BpScratch g_bs;
@@ -274,8 +277,11 @@ int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cud
 
 // Mesh-shape candidates (kind 2): BVH-shape collide (mode 0, contacts into hit) or
 // distance (mode 1, into the distance slots), mesh first as FCL calls it.
+// With lists (collide only): every listed pair's triangle list (g_bs.x_loff,
+// g_bs.x_ltris) and index[slot] = its list position (g_bs.x_index).
 int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQueryView& Q, int64_t total, int mode,
-              int64_t max_contacts, BpCounters* dctr, cudaStream_t s, const int32_t* qdone = nullptr) {
+              int64_t max_contacts, BpCounters* dctr, cudaStream_t s, const int32_t* qdone = nullptr,
+              bool lists = false) {
   int64_t nl = 0;
   RCB(list_kind(total, 2, dctr, &nl, s, qdone));
   g_last_mixed = nl;
@@ -339,7 +345,26 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
     L.group_count = (unsigned long long*)g_bs.x_gcount.p;
     L.group_max = max_contacts;
   }
-  CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+  if (lists) {
+    CKB(g_bs.x_loff.ensure(8 * (nl + 1)), "mixed lists");
+    CKB(g_bs.x_ltris.ensure(4 * std::max<int64_t>(nl, 1024)), "mixed lists");
+    CKB(g_bs.x_index.ensure(4 * std::max<int64_t>(total, 1)), "mixed lists");
+    L.list_offsets = g_bs.x_loff.as<int64_t>();
+    L.list_tris = g_bs.x_ltris.as<int32_t>();
+    L.list_cap = (int64_t)(g_bs.x_ltris.cap / 4);
+    int64_t ltotal = 0;
+    L.list_total = &ltotal;
+    CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+    if (ltotal > L.list_cap) {  // the lists did not fit: once more with room for all of them
+      CKB(g_bs.x_ltris.ensure(4 * (size_t)ltotal), "mixed lists");
+      L.list_tris = g_bs.x_ltris.as<int32_t>();
+      L.list_cap = (int64_t)(g_bs.x_ltris.cap / 4);
+      CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+    }
+    CKB(launch_bp_inverse_index(g_bs.list.as<int64_t>(), nl, g_bs.x_index.as<int32_t>(), s), "mixed index");
+  } else {
+    CKB(run_mesh_shape_split(L, bp->max_depth + 2, s), "mesh-shape narrowphase");
+  }
   if (mode == 0) {
     CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.x_counts.as<int32_t>(), g_bs.hit.as<int32_t>(), s),
         "mixed scatter");
@@ -559,26 +584,15 @@ int fclgpu_broadphase_collide_device(fclgpu_broadphase bp, const fclgpu_geometry
   return check_status(hc);
 }
 
-int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
-                                      const double* tf, const fclgpu_broadphase_distance_request* req,
-                                      fclgpu_broadphase_distance_result* res, void* stream) {
-  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->min_distance)))
-    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase distance argument");
-  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
-    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
-  if (nq >= ((int64_t)1 << 31)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many queries");
-  std::lock_guard<std::mutex> lk(g_bp_mu);
-  cudaStream_t s = (cudaStream_t)stream;
-  res->total_candidates = 0;
-  res->total_node_visits = 0;
-  if (nq == 0) return FCLGPU_OK;
-  PhaseClock pc(1, s);
-  g_last_mixed = 0;
-  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
-  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
-  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
-  BpQueryView Q;
-  RCB(prepare_queries(bp, queries, nq, tf, Q, dctr, s));
+}  // extern "C"
+
+namespace {
+
+// The broadphase distance of the queries Q (per query: the nearest scene object among
+// the candidates, its triangle ids and world witness points).
+int distance_core(fclgpu_broadphase_s* bp, const BpQueryView& Q, const fclgpu_broadphase_distance_request* req,
+                  fclgpu_broadphase_distance_result* res, BpCounters* dctr, cudaStream_t s, PhaseClock& pc) {
+  const int64_t nq = Q.nq;
   const BpSceneView S = scene_view(bp);
   CKB(g_bs.ub.ensure(8 * nq), "bounds");
   CKB(g_bs.counts.ensure(4 * nq), "counts");
@@ -633,7 +647,7 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
       const int rc = fclgpu_distance_batch_device(bp->meshes.data(), bp->nm, bp->mesh_pairs.data(),
                                                   bp->nm * bp->nm, nl, g_bs.m_pair.as<int32_t>(),
                                                   g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), &mr, &mres,
-                                                  stream);
+                                                  (void*)s);
       if (rc) return rc;
       CKB(launch_bp_scatter_dist(g_bs.list.as<int64_t>(), nl, g_bs.m_dist.as<double>(), g_bs.m_ids.as<int32_t>(),
                                  g_bs.m_pts.as<double>(), dist, b12, pts, s),
@@ -648,6 +662,33 @@ int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometr
   CKB(cudaStreamSynchronize(s), "broadphase distance");
   pc.tick(4);
   return check_status(hc);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                      const double* tf, const fclgpu_broadphase_distance_request* req,
+                                      fclgpu_broadphase_distance_result* res, void* stream) {
+  if (!bp || !req || !res || nq < 0 || (nq > 0 && (!queries || !tf || !res->min_distance)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase distance argument");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (nq >= ((int64_t)1 << 31)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many queries");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_candidates = 0;
+  res->total_node_visits = 0;
+  if (nq == 0) return FCLGPU_OK;
+  PhaseClock pc(1, s);
+  g_last_mixed = 0;
+  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
+  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
+  BpQueryView Q;
+  RCB(prepare_queries(bp, queries, nq, tf, Q, dctr, s));
+  return distance_core(bp, Q, req, res, dctr, s, pc);
 }
 
 int fclgpu_broadphase_collide(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq, const double* tf,
@@ -715,6 +756,295 @@ int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* 
     if (e != cudaSuccess) rc = bp_cuda(e, "d2h");
   }
   for (Buf* b : {&refs, &tfd, &d, &ob, &ids, &pts}) cudaFree(b->p);
+  return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Contact lists of the candidate pairs of Q (every pair evaluated, each capped at
+// num_max_contacts): per query, its contacts ordered by scene-object index, each
+// object's in the order FCL's traversal of that pair adds them.  Device outputs.
+int contacts_core(fclgpu_broadphase_s* bp, const BpQueryView& Q, const fclgpu_broadphase_contacts_request* req,
+                  fclgpu_broadphase_contacts_result* res, BpCounters* dctr, cudaStream_t s) {
+  const int64_t nq = Q.nq;
+  const BpSceneView S = scene_view(bp);
+  CKB(g_bs.counts.ensure(4 * nq), "counts");
+  CKB(launch_bp_overlap(S, Q, g_bs.counts.as<int32_t>(), nullptr, nullptr, &dctr->visits, &dctr->status, s),
+      "overlap count");
+  BpCounters hc;
+  int64_t total = 0;
+  RCB(scan_counts(nq, dctr, &hc, &total, s));
+  res->total_candidates = total;
+  RCB(ensure_pair_buffers(total));
+  const size_t t1 = (size_t)std::max<int64_t>(total, 1);
+  CKB(g_bs.hit.ensure(4 * t1), "hits");
+  const int64_t* off = g_bs.offsets.as<int64_t>();
+  int2* pairs = g_bs.pairs.as<int2>();
+  int32_t* hit = g_bs.hit.as<int32_t>();
+  CKB(g_bs.mm_index.ensure(4 * t1), "mesh index");
+  CKB(g_bs.x_index.ensure(4 * t1), "mixed index");
+  if (total > 0) {
+    CKB(launch_bp_overlap(S, Q, nullptr, off, pairs, nullptr, &dctr->status, s), "overlap write");
+    CKB(launch_bp_classify(S, Q, pairs, total, g_bs.kind.as<int32_t>(), s), "classify");
+    CKB(cudaMemsetAsync(hit, 0, 4 * (size_t)total, s), "hits");
+    CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_INTERSECT, hit, nullptr, nullptr,
+                               s),
+        "shape narrowphase");
+    RCB(run_mixed(bp, S, Q, total, 0, req->num_max_contacts, dctr, s, nullptr, true));
+    int64_t nl = 0;
+    RCB(list_kind(total, 1, dctr, &nl, s, nullptr));
+    if (nl > 0) {
+      CKB(g_bs.m_pair.ensure(4 * nl), "mesh scratch");
+      CKB(g_bs.m_tf1.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_tf2.ensure(96 * nl), "mesh scratch");
+      CKB(g_bs.m_counts.ensure(4 * nl), "mesh scratch");
+      CKB(g_bs.mm_off.ensure(8 * (nl + 1)), "mesh scratch");
+      CKB(g_bs.mm_cont.ensure(8 * std::max<int64_t>(nl, 1024)), "mesh scratch");
+      CKB(launch_bp_gather_mesh(S, Q, pairs, g_bs.list.as<int64_t>(), nl, bp->nm, g_bs.m_pair.as<int32_t>(),
+                                g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
+          "mesh gather");
+      fclgpu_collide_request mr = {(int32_t)std::min<int64_t>(req->num_max_contacts, INT32_MAX), req->precision, 0,
+                                   0};
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        fclgpu_collide_result mres = {g_bs.m_counts.as<int32_t>(), g_bs.mm_off.as<int64_t>(),
+                                      g_bs.mm_cont.as<int32_t>(), (int64_t)(g_bs.mm_cont.cap / 8), nullptr, nullptr,
+                                      nullptr, 0};
+        const int rc = fclgpu_collide_batch_device(bp->meshes.data(), bp->nm, bp->mesh_pairs.data(),
+                                                   bp->nm * bp->nm, nl, g_bs.m_pair.as<int32_t>(),
+                                                   g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), &mr, &mres,
+                                                   (void*)s);
+        if (rc == FCLGPU_ERR_CAPACITY && attempt == 0) {
+          CKB(g_bs.mm_cont.ensure(8 * (size_t)mres.total_contacts), "mesh scratch");
+          continue;
+        }
+        if (rc) return rc;
+        break;
+      }
+      CKB(launch_bp_scatter_hits(g_bs.list.as<int64_t>(), nl, g_bs.m_counts.as<int32_t>(), hit, s), "mesh scatter");
+      CKB(launch_bp_inverse_index(g_bs.list.as<int64_t>(), nl, g_bs.mm_index.as<int32_t>(), s), "mesh index");
+    }
+  }
+  // order: per query by object index; scan of the per-slot contact counts
+  CKB(g_bs.perm.ensure(8 * t1), "lists");
+  CKB(g_bs.ccount.ensure(4 * t1), "lists");
+  CKB(g_bs.coff.ensure(8 * (t1 + 1)), "lists");
+  CKB(g_bs.scan_tmp.ensure(8 * ((total + 4095) / 4096 + 2)), "scan scratch");
+  CKB(launch_bp_sort_segments(nq, off, pairs, g_bs.perm.as<int64_t>(), s), "sort");
+  CKB(launch_bp_gather_counts(g_bs.perm.as<int64_t>(), total, hit, g_bs.ccount.as<int32_t>(), s), "counts");
+  CKB(launch_exclusive_scan(g_bs.ccount.as<int32_t>(), total, g_bs.coff.as<int64_t>(), g_bs.scan_tmp.as<int64_t>(),
+                            s),
+      "scan");
+  CKB(launch_bp_query_contacts(nq, off, g_bs.coff.as<int64_t>(), res->counts, res->offsets, s), "query counts");
+  int64_t nc = 0;
+  CKB(cudaMemcpyAsync(&nc, g_bs.coff.as<int64_t>() + total, 8, cudaMemcpyDeviceToHost, s), "read total");
+  CKB(cudaMemcpyAsync(&hc, dctr, sizeof(BpCounters), cudaMemcpyDeviceToHost, s), "read counters");
+  CKB(cudaStreamSynchronize(s), "broadphase contacts");
+  res->total_contacts = nc;
+  res->total_node_visits = hc.visits;
+  RCB(check_status(hc));
+  if (nc > res->capacity) return bp_fail(FCLGPU_ERR_CAPACITY, "contacts buffer too small");
+  CKB(launch_bp_fill_contacts(g_bs.perm.as<int64_t>(), total, pairs, g_bs.kind.as<int32_t>(), hit,
+                              g_bs.coff.as<int64_t>(), g_bs.mm_index.as<int32_t>(), g_bs.mm_off.as<int64_t>(),
+                              g_bs.mm_cont.as<int32_t>(), g_bs.x_index.as<int32_t>(), g_bs.x_loff.as<int64_t>(),
+                              g_bs.x_ltris.as<int32_t>(), res->contacts, s),
+      "fill");
+  CKB(cudaStreamSynchronize(s), "broadphase contacts");
+  return FCLGPU_OK;
+}
+
+// The scene's own objects as queries (object q against the objects below it).
+BpQueryView self_queries(const fclgpu_broadphase_s* bp) {
+  BpQueryView Q;
+  Q.nq = bp->n;
+  Q.gid = bp->gid;
+  Q.tf = bp->tf;
+  Q.aabb64 = bp->aabb64;
+  Q.aabb32 = bp->aabb32;
+  Q.self = 1;
+  return Q;
+}
+
+int check_contacts_args(const fclgpu_broadphase_contacts_request* req, const fclgpu_broadphase_contacts_result* res,
+                        int64_t nq) {
+  if (!req || !res || !res->offsets || (nq > 0 && !res->counts) || res->capacity < 0 ||
+      (res->capacity > 0 && !res->contacts))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase contacts argument");
+  if (req->num_max_contacts < 1) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_contacts must be >= 1");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  return FCLGPU_OK;
+}
+
+// Host form of a contacts call: device outputs staged per call, then copied back.
+template <class F>
+int contacts_host(int64_t nq, fclgpu_broadphase_contacts_result* res, cudaStream_t s, F&& run_device) {
+  Buf c, o, l;
+  CKB(c.ensure(8 * (size_t)std::max<int64_t>(nq, 1)), "staging");
+  CKB(o.ensure(8 * (size_t)(nq + 1)), "staging");
+  CKB(l.ensure(12 * (size_t)std::max<int64_t>(res->capacity, 1)), "staging");
+  fclgpu_broadphase_contacts_result dr = {c.as<int64_t>(), o.as<int64_t>(), l.as<int32_t>(), res->capacity, 0, 0, 0};
+  int rc = run_device(&dr);
+  res->total_contacts = dr.total_contacts;
+  res->total_candidates = dr.total_candidates;
+  res->total_node_visits = dr.total_node_visits;
+  if (rc == FCLGPU_OK || rc == FCLGPU_ERR_CAPACITY) {
+    cudaError_t e = cudaSuccess;
+    if (nq > 0) e = cudaMemcpyAsync(res->counts, dr.counts, 8 * (size_t)nq, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res->offsets, dr.offsets, 8 * (size_t)(nq + 1), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && rc == FCLGPU_OK && dr.total_contacts > 0)
+      e = cudaMemcpyAsync(res->contacts, dr.contacts, 12 * (size_t)dr.total_contacts, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = bp_cuda(e, "d2h");
+  }
+  for (Buf* b : {&c, &o, &l}) cudaFree(b->p);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fclgpu_broadphase_collide_contacts_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                              const double* tf, const fclgpu_broadphase_contacts_request* req,
+                                              fclgpu_broadphase_contacts_result* res, void* stream) {
+  if (!bp || nq < 0 || (nq > 0 && (!queries || !tf)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase contacts argument");
+  RCB(check_contacts_args(req, res, nq));
+  if (nq >= ((int64_t)1 << 31)) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many queries");
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_contacts = res->total_candidates = res->total_node_visits = 0;
+  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
+  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
+  if (nq == 0) {
+    CKB(cudaMemsetAsync(res->offsets, 0, 8, s), "offsets");
+    CKB(cudaStreamSynchronize(s), "offsets");
+    return FCLGPU_OK;
+  }
+  BpQueryView Q;
+  RCB(prepare_queries(bp, queries, nq, tf, Q, dctr, s));
+  return contacts_core(bp, Q, req, res, dctr, s);
+}
+
+int fclgpu_broadphase_collide_contacts(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
+                                       const double* tf, const fclgpu_broadphase_contacts_request* req,
+                                       fclgpu_broadphase_contacts_result* res, void* stream) {
+  if (!bp || nq < 0 || (nq > 0 && (!queries || !tf)))
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase contacts argument");
+  RCB(check_contacts_args(req, res, nq));
+  cudaStream_t s = (cudaStream_t)stream;
+  // inputs to the device (the device entry point takes the lock)
+  void* dq = nullptr;
+  void* dt = nullptr;
+  if (nq > 0) {
+    CKB(cudaMalloc(&dq, 8 * (size_t)nq), "staging");
+    cudaError_t e = cudaMalloc(&dt, 96 * (size_t)nq);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dq, queries, 8 * (size_t)nq, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, tf, 96 * (size_t)nq, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      cudaFree(dq);
+      if (dt) cudaFree(dt);
+      return bp_cuda(e, "staging");
+    }
+  }
+  const int rc = contacts_host(nq, res, s, [&](fclgpu_broadphase_contacts_result* dr) {
+    return fclgpu_broadphase_collide_contacts_device(bp, (const fclgpu_geometry_ref*)dq, nq, (const double*)dt, req,
+                                                     dr, stream);
+  });
+  if (dq) cudaFree(dq);
+  if (dt) cudaFree(dt);
+  return rc;
+}
+
+int fclgpu_broadphase_self_collide_contacts_device(fclgpu_broadphase bp,
+                                                   const fclgpu_broadphase_contacts_request* req,
+                                                   fclgpu_broadphase_contacts_result* res, void* stream) {
+  if (!bp) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase");
+  RCB(check_contacts_args(req, res, bp->n));
+  std::lock_guard<std::mutex> lk(g_bp_mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_contacts = res->total_candidates = res->total_node_visits = 0;
+  CKB(g_bs.ctr.ensure(sizeof(BpCounters)), "counters");
+  BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+  CKB(cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s), "counters");
+  if (bp->n == 0) {
+    CKB(cudaMemsetAsync(res->offsets, 0, 8, s), "offsets");
+    CKB(cudaStreamSynchronize(s), "offsets");
+    return FCLGPU_OK;
+  }
+  const BpQueryView Q = self_queries(bp);
+  return contacts_core(bp, Q, req, res, dctr, s);
+}
+
+int fclgpu_broadphase_self_collide_contacts(fclgpu_broadphase bp, const fclgpu_broadphase_contacts_request* req,
+                                            fclgpu_broadphase_contacts_result* res, void* stream) {
+  if (!bp) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase");
+  RCB(check_contacts_args(req, res, bp->n));
+  return contacts_host(bp->n, res, (cudaStream_t)stream, [&](fclgpu_broadphase_contacts_result* dr) {
+    return fclgpu_broadphase_self_collide_contacts_device(bp, req, dr, stream);
+  });
+}
+
+int fclgpu_broadphase_self_distance(fclgpu_broadphase bp, const fclgpu_broadphase_distance_request* req,
+                                    fclgpu_broadphase_self_distance_result* out, void* stream) {
+  if (!bp || !req || !out) return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing broadphase self-distance argument");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return bp_fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  out->min_distance = std::numeric_limits<double>::max();
+  out->o1 = out->o2 = out->b1 = out->b2 = -1;
+  for (double& p : out->nearest_points) p = 0.0;
+  out->total_candidates = 0;
+  const int64_t n = bp->n;
+  if (n < 2) return FCLGPU_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  Buf d, o, ids, pts;  // per-object results (object q against the objects below it)
+  CKB(d.ensure(8 * n), "staging");
+  CKB(o.ensure(4 * n), "staging");
+  CKB(ids.ensure(8 * n), "staging");
+  CKB(pts.ensure(48 * n), "staging");
+  fclgpu_broadphase_distance_result dr = {d.as<double>(), o.as<int32_t>(), ids.as<int32_t>(), pts.as<double>(), 0, 0};
+  int rc;
+  {
+    std::lock_guard<std::mutex> lk(g_bp_mu);
+    PhaseClock pc(1, s);
+    g_last_mixed = 0;
+    rc = g_bs.ctr.ensure(sizeof(BpCounters)) == cudaSuccess ? FCLGPU_OK : FCLGPU_ERR_OUT_OF_MEMORY;
+    if (rc == FCLGPU_OK) {
+      BpCounters* dctr = g_bs.ctr.as<BpCounters>();
+      const cudaError_t e = cudaMemsetAsync(dctr, 0, sizeof(BpCounters), s);
+      rc = e == cudaSuccess ? distance_core(bp, self_queries(bp), req, &dr, dctr, s, pc) : bp_cuda(e, "counters");
+    }
+  }
+  if (rc == FCLGPU_OK) {
+    std::vector<double> hd(n), hp(6 * n);
+    std::vector<int32_t> ho(n), hi(2 * n);
+    cudaError_t e = cudaMemcpyAsync(hd.data(), d.p, 8 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ho.data(), o.p, 4 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hi.data(), ids.p, 8 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), pts.p, 48 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      rc = bp_cuda(e, "d2h");
+    } else {
+      // the smallest distance over all pairs; ties to the smaller o2, then o1
+      int64_t best = -1;
+      for (int64_t q = 1; q < n; ++q)
+        if (ho[q] >= 0 && (best < 0 || hd[q] < hd[best])) best = q;
+      out->total_candidates = dr.total_candidates;
+      if (best >= 0) {
+        out->min_distance = hd[best];
+        out->o1 = ho[best];
+        out->o2 = (int32_t)best;
+        out->b1 = hi[2 * best];
+        out->b2 = hi[2 * best + 1];
+        for (int k = 0; k < 6; ++k) out->nearest_points[k] = req->enable_nearest_points ? hp[6 * best + k] : 0.0;
+      }
+    }
+  }
+  for (Buf* b : {&d, &o, &ids, &pts}) cudaFree(b->p);
   return rc;
 }
 

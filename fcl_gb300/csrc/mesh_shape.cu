@@ -246,6 +246,23 @@ __global__ void __launch_bounds__(128) k_msr_tests(MeshShapeLaunch L, const int3
 // bounds the tail of a pair with many near misses.
 constexpr int kSerialGjk = 4;
 
+// Lists the pair's contacts c0..c-1: its first intersecting leaves of this round in
+// DFS order, as (pair, rank, triangle) records.
+__device__ __forceinline__ void emit_contacts(const MeshShapeLaunch& L, long long i, long long a, int K,
+                                              const int32_t* leaf, const int32_t* nleaf, const int32_t* hit, int c0,
+                                              int c) {
+  if (!L.rec || c <= c0) return;
+  int r = c0;
+  const int nl = nleaf[a];
+  for (int k = 0; k < nl && r < c; ++k) {
+    const long long slot = a * (long long)K + k;
+    if (hit[slot] == 2) {
+      L.rec[atomicAdd(L.nrec, 1ull)] = make_int4((int)i, r, leaf[slot], 0);
+      ++r;
+    }
+  }
+}
+
 // adds a pair's new contacts to its group; false once the group has group_max (the
 // pair's query needs no more contacts, so its traversal can stop)
 __device__ __forceinline__ bool group_open(const MeshShapeLaunch& L, long long i, int delta) {
@@ -296,6 +313,7 @@ __global__ void __launch_bounds__(128) k_msr_update(MeshShapeLaunch L, const int
     }
     const int c0 = L.counts[i];
     L.counts[i] = c;
+    emit_contacts(L, i, a, K, leaf, nleaf, hit, c0, c);
     if (c < L.max_contacts && sp[i] > 0 && group_open(L, i, c - c0)) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
   }
 }
@@ -317,9 +335,10 @@ __global__ void __launch_bounds__(128) k_msr_deferred(MeshShapeLaunch L, const i
 }
 
 __global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const int32_t* act, int K,
-                                                     const int32_t* nleaf, const int32_t* hit, const int32_t* sp,
-                                                     const int32_t* defer_pair, const unsigned long long* ndefer_pair,
-                                                     int32_t* next, unsigned long long* nnext) {
+                                                     const int32_t* leaf, const int32_t* nleaf, const int32_t* hit,
+                                                     const int32_t* sp, const int32_t* defer_pair,
+                                                     const unsigned long long* ndefer_pair, int32_t* next,
+                                                     unsigned long long* nnext) {
   const long long n = (long long)*ndefer_pair;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
@@ -330,7 +349,18 @@ __global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const in
     for (int k = 0; k < nl && c < L.max_contacts; ++k) c += hit[a * (long long)K + k] == 2 ? 1 : 0;
     const int c0 = L.counts[i];
     L.counts[i] = c;
+    emit_contacts(L, i, a, K, leaf, nleaf, hit, c0, c);
     if (c < L.max_contacts && sp[i] > 0 && group_open(L, i, c - c0)) next[atomicAdd(nnext, 1ull)] = (int32_t)i;
+  }
+}
+
+// tris[offsets[pair] + rank] = triangle for every record
+__global__ void k_msr_scatter(const int4* rec, const unsigned long long* nrec, const int64_t* offsets, int32_t* tris) {
+  const long long n = (long long)*nrec;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int4 r = rec[t];
+    tris[offsets[r.x] + r.y] = r.z;
   }
 }
 
@@ -342,8 +372,8 @@ cudaError_t launch_exclusive_scan(const int32_t* counts, int64_t n, int64_t* off
 
 namespace {
 struct SplitScratch {
-  void* p[12] = {nullptr};
-  size_t cap[12] = {0};
+  void* p[16] = {nullptr};
+  size_t cap[16] = {0};
   cudaError_t ensure(int k, size_t bytes) {
     if (bytes <= cap[k]) return cudaSuccess;
     if (p[k]) cudaFree(p[k]);
@@ -366,21 +396,44 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
   const int cap = stack_entries;
   cudaError_t e;
   if ((e = S.ensure(0, sizeof(MsPairState) * n)) || (e = S.ensure(1, 4ull * cap * n)) || (e = S.ensure(2, 4 * n)) ||
-      (e = S.ensure(3, 4 * n)) || (e = S.ensure(4, 4 * n)) || (e = S.ensure(5, 24)))
+      (e = S.ensure(3, 4 * n)) || (e = S.ensure(4, 4 * n)) || (e = S.ensure(5, 32)))
     return e;
+  // contact list: records (pair, rank, triangle) in slot 11, counter nnext[3]
+  MeshShapeLaunch Lr = L;
+  const bool listing = L.list_offsets != nullptr;
+  unsigned long long nrec_host = 0;
+  if (listing) {
+    Lr.nrec = (unsigned long long*)S.p[5] + 3;
+    if ((e = cudaMemsetAsync(Lr.nrec, 0, 8, s))) return e;
+  }
   MsPairState* ps = (MsPairState*)S.p[0];
   int32_t* stack = (int32_t*)S.p[1];
   int32_t* sp = (int32_t*)S.p[2];
   int32_t* act = (int32_t*)S.p[3];
   int32_t* next = (int32_t*)S.p[4];
   unsigned long long* nnext = (unsigned long long*)S.p[5];
-  k_msr_init<<<grid128(n), 128, 0, s>>>(L, ps, stack, cap, sp, act);
+  k_msr_init<<<grid128(n), 128, 0, s>>>(Lr, ps, stack, cap, sp, act);
   ++g_kernel_launches;
   long long nact = n;
   for (int r = 0; nact > 0; ++r) {
     const int K = 16 << std::min(r, 6);
     const long long nl = nact * K;
     if ((e = S.ensure(6, 4 * nl)) || (e = S.ensure(7, 4 * nact)) || (e = S.ensure(8, 4 * nl))) return e;
+    if (listing) {  // a round adds at most one record per leaf it lists; grow keeping the records
+      const size_t need = sizeof(int4) * (size_t)(nrec_host + nl);
+      if (need > S.cap[11]) {
+        void* np = nullptr;
+        const size_t want = std::max<size_t>(need + need / 2, 4096);
+        if ((e = cudaMalloc(&np, want))) return e;
+        if (nrec_host && (e = cudaMemcpyAsync(np, S.p[11], sizeof(int4) * nrec_host, cudaMemcpyDeviceToDevice, s)))
+          return e;
+        if ((e = cudaStreamSynchronize(s))) return e;
+        if (S.p[11]) cudaFree(S.p[11]);
+        S.p[11] = np;
+        S.cap[11] = want;
+      }
+      Lr.rec = (int4*)S.p[11];
+    }
     int32_t* leaf = (int32_t*)S.p[6];
     int32_t* nleaf = (int32_t*)S.p[7];
     int32_t* hit = (int32_t*)S.p[8];
@@ -392,19 +445,34 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
     // node tests per pair per round are capped too, so that one pair with a long
     // traversal does not hold every round up
     const int max_visits = 128 << std::min(r, 3);
-    k_msr_dfs<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, max_visits, ps, stack, cap, sp, leaf, nleaf);
-    k_msr_tests<<<grid128(nl), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit);
-    k_msr_update<<<grid128(nact), 128, 0, s>>>(L, act, nact, K, leaf, nleaf, hit, sp, next, nnext, defer_leaf,
+    k_msr_dfs<<<grid128(nact), 128, 0, s>>>(Lr, act, nact, K, max_visits, ps, stack, cap, sp, leaf, nleaf);
+    k_msr_tests<<<grid128(nl), 128, 0, s>>>(Lr, act, nact, K, leaf, nleaf, hit);
+    k_msr_update<<<grid128(nact), 128, 0, s>>>(Lr, act, nact, K, leaf, nleaf, hit, sp, next, nnext, defer_leaf,
                                                nnext + 1, defer_pair, nnext + 2);
-    k_msr_deferred<<<grid128(nl), 128, 0, s>>>(L, act, K, leaf, hit, defer_leaf, nnext + 1);
-    k_msr_recount<<<grid128(nact), 128, 0, s>>>(L, act, K, nleaf, hit, sp, defer_pair, nnext + 2, next, nnext);
+    k_msr_deferred<<<grid128(nl), 128, 0, s>>>(Lr, act, K, leaf, hit, defer_leaf, nnext + 1);
+    k_msr_recount<<<grid128(nact), 128, 0, s>>>(Lr, act, K, leaf, nleaf, hit, sp, defer_pair, nnext + 2, next,
+                                                nnext);
     g_kernel_launches += 5;
-    unsigned long long nn = 0;
-    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&nn, nnext, 8, cudaMemcpyDeviceToHost, s)) ||
+    unsigned long long nn[4] = {0, 0, 0, 0};
+    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(nn, nnext, 32, cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       return e;
-    nact = (long long)nn;
+    nact = (long long)nn[0];
+    nrec_host = nn[3];
     std::swap(act, next);
+  }
+  if (listing) {
+    if ((e = S.ensure(12, 8 * ((n + 4095) / 4096 + 2)))) return e;
+    if ((e = launch_exclusive_scan(L.counts, n, L.list_offsets, (int64_t*)S.p[12], s))) return e;
+    int64_t total = 0;
+    if ((e = cudaMemcpyAsync(&total, L.list_offsets + n, 8, cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return e;
+    if (L.list_total) *L.list_total = total;
+    if (total <= L.list_cap && nrec_host > 0) {
+      k_msr_scatter<<<grid128((long long)nrec_host), 128, 0, s>>>(Lr.rec, Lr.nrec, L.list_offsets, L.list_tris);
+      ++g_kernel_launches;
+    }
   }
   return cudaGetLastError();
 }
@@ -615,6 +683,121 @@ int fclgpu_mesh_shape_batch(const fclgpu_mesh* meshes, int32_t num_meshes, fclgp
         e = cudaMemcpyAsync(res->num_bv_tests, db, 8 * nn, cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess && res->num_leaf_tests)
         e = cudaMemcpyAsync(res->num_leaf_tests, dl, 8 * nn, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = ms_cuda(e, "d2h");
+    }
+  }
+  cudaFree(d);
+  return rc;
+}
+
+int fclgpu_mesh_shape_contacts_device(const fclgpu_mesh* meshes, int32_t num_meshes, fclgpu_shapeset shapes,
+                                      int64_t n, const int32_t* mesh_idx, const int32_t* shape_idx,
+                                      const double* tf_mesh, const double* tf_shape, int64_t num_max_contacts,
+                                      fclgpu_mesh_shape_contacts_result* res, void* stream) {
+  if (!res || n < 0 || !meshes || num_meshes <= 0 || !shapes)
+    return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing mesh-shape argument");
+  if (num_max_contacts < 1) return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_contacts must be >= 1");
+  if (!res->offsets || (n > 0 && (!mesh_idx || !shape_idx || !tf_mesh || !tf_shape || !res->counts)) ||
+      (res->capacity > 0 && !res->tris) || res->capacity < 0)
+    return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing mesh-shape input or output");
+  std::vector<DevMesh> table(num_meshes);
+  int depth = 0;
+  for (int32_t i = 0; i < num_meshes; ++i) {
+    if (!meshes[i]) return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null mesh handle");
+    table[i] = meshes[i]->dev;
+    depth = std::max(depth, (int)meshes[i]->dev.max_depth);
+  }
+  if (depth + 2 > 256) return ms_fail(FCLGPU_ERR_STACK_DEPTH, "BVH deeper than the traversal stack");
+  cudaStream_t s = (cudaStream_t)stream;
+  res->total_contacts = 0;
+  if (n == 0) {
+    const int64_t zero = 0;
+    cudaError_t e = cudaMemcpyAsync(res->offsets, &zero, 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? FCLGPU_OK : ms_cuda(e, "offsets");
+  }
+  std::lock_guard<std::mutex> lk(g_ms_mu);
+  cudaError_t e = g_ms_meshes.ensure(sizeof(DevMesh) * num_meshes);
+  if (e == cudaSuccess) e = g_ms_status.ensure(sizeof(unsigned));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g_ms_meshes.p, table.data(), sizeof(DevMesh) * num_meshes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g_ms_status.p, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return ms_cuda(e, "mesh-shape setup");
+  MeshShapeLaunch L;
+  L.meshes = static_cast<const DevMesh*>(g_ms_meshes.p);
+  L.shapes = shapes->shapes;
+  L.sverts = shapes->verts;
+  L.n = n;
+  L.mesh_idx = mesh_idx;
+  L.shape_idx = shape_idx;
+  L.tfm = tf_mesh;
+  L.tfs = tf_shape;
+  L.mode = 0;
+  L.max_contacts = (int32_t)std::min<int64_t>(num_max_contacts, INT32_MAX);
+  L.counts = res->counts;
+  L.dist = nullptr;
+  L.tri = nullptr;
+  L.pts = nullptr;
+  L.nbv = nullptr;
+  L.nleaf = nullptr;
+  L.status = static_cast<unsigned*>(g_ms_status.p);
+  L.list_offsets = res->offsets;
+  L.list_tris = res->tris;
+  L.list_cap = res->capacity;
+  int64_t total = 0;
+  L.list_total = &total;
+  e = run_mesh_shape_split(L, depth + 2, s);
+  unsigned st = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&st, g_ms_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return ms_cuda(e, "mesh-shape kernel");
+  if (st) return ms_fail(FCLGPU_ERR_STACK_DEPTH, "mesh-shape traversal stack overflow");
+  res->total_contacts = total;
+  if (total > res->capacity) return ms_fail(FCLGPU_ERR_CAPACITY, "tris buffer too small");
+  return FCLGPU_OK;
+}
+
+int fclgpu_mesh_shape_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, fclgpu_shapeset shapes, int64_t n,
+                               const int32_t* mesh_idx, const int32_t* shape_idx, const double* tf_mesh,
+                               const double* tf_shape, int64_t num_max_contacts,
+                               fclgpu_mesh_shape_contacts_result* res, void* stream) {
+  if (!res || n < 0 || res->capacity < 0 || !res->offsets || (n > 0 && !res->counts) ||
+      (res->capacity > 0 && !res->tris))
+    return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing mesh-shape argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nn = (size_t)n;
+  // inputs, counts, offsets and a device list as large as the caller's
+  const size_t bytes = nn * (4 + 4 + 96 + 96 + 4) + 8 * (nn + 2) + 4 * (size_t)res->capacity + 64;
+  char* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) return ms_cuda(e, "staging");
+  double* dtm = (double*)d;
+  double* dts = dtm + 12 * nn;
+  int64_t* doff = (int64_t*)(dts + 12 * nn);
+  int32_t* dm = (int32_t*)(doff + nn + 2);
+  int32_t* ds = dm + nn;
+  int32_t* dc = ds + nn;
+  int32_t* dt = dc + nn;
+  if (n > 0) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dm, mesh_idx, 4 * nn, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ds, shape_idx, 4 * nn, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtm, tf_mesh, 96 * nn, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dts, tf_shape, 96 * nn, cudaMemcpyHostToDevice, s);
+  }
+  int rc = FCLGPU_OK;
+  if (e != cudaSuccess) {
+    rc = ms_cuda(e, "h2d");
+  } else {
+    fclgpu_mesh_shape_contacts_result dr = {dc, doff, dt, res->capacity, 0};
+    rc = fclgpu_mesh_shape_contacts_device(meshes, num_meshes, shapes, n, dm, ds, dtm, dts, num_max_contacts, &dr,
+                                           stream);
+    res->total_contacts = dr.total_contacts;
+    if (rc == FCLGPU_OK || rc == FCLGPU_ERR_CAPACITY) {
+      if (n > 0) e = cudaMemcpyAsync(res->counts, dc, 4 * nn, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(res->offsets, doff, 8 * (nn + 1), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && rc == FCLGPU_OK && dr.total_contacts > 0)
+        e = cudaMemcpyAsync(res->tris, dt, 4 * (size_t)dr.total_contacts, cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) rc = ms_cuda(e, "d2h");
     }

@@ -35,6 +35,18 @@ struct MeshShapeLaunch {
   const int32_t* group = nullptr;
   unsigned long long* group_count = nullptr;
   int64_t group_max = 0;
+  // optional contact list (collide, split form): the intersecting triangles of every
+  // pair in the order FCL's traversal adds them (Contact b1; b2 is NONE), at most
+  // max_contacts per pair: offsets[n + 1] and tris[] are device arrays, tris holding
+  // list_cap entries; *list_total (host) receives the total, and tris is filled only
+  // when it fits
+  int64_t* list_offsets = nullptr;
+  int32_t* list_tris = nullptr;
+  int64_t list_cap = 0;
+  int64_t* list_total = nullptr;
+  // record scratch of the list (set inside the split form)
+  int4* rec = nullptr;
+  unsigned long long* nrec = nullptr;
 };
 
 // One thread per pair runs the whole FCL traversal (exact statistics).

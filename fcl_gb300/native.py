@@ -84,6 +84,20 @@ class BpCollideResult(C.Structure):
                 ("total_candidates", C.c_int64), ("total_node_visits", C.c_int64)]
 
 
+class BpContactsRequest(C.Structure):
+    _fields_ = [("num_max_contacts", C.c_int64), ("precision", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BpContactsResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("contacts", C.c_void_p), ("capacity", C.c_int64),
+                ("total_contacts", C.c_int64), ("total_candidates", C.c_int64), ("total_node_visits", C.c_int64)]
+
+
+class BpSelfDistanceResult(C.Structure):
+    _fields_ = [("min_distance", C.c_double), ("o1", C.c_int32), ("o2", C.c_int32), ("b1", C.c_int32),
+                ("b2", C.c_int32), ("nearest_points", C.c_double * 6), ("total_candidates", C.c_int64)]
+
+
 class BpDistanceRequest(C.Structure):
     _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32)]
 
@@ -117,6 +131,11 @@ class ServerStats(C.Structure):
 
 class MeshShapeRequest(C.Structure):
     _fields_ = [("mode", C.c_int32), ("reserved", C.c_int32), ("num_max_contacts", C.c_int64)]
+
+
+class MeshShapeContactsResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("tris", C.c_void_p), ("capacity", C.c_int64),
+                ("total_contacts", C.c_int64)]
 
 
 class MeshShapeResult(C.Structure):
@@ -181,6 +200,16 @@ _SIGS = {
                                                    C.POINTER(BpCollideResult), _VP]),
     "fclgpu_broadphase_collide": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpCollideRequest),
                                             C.POINTER(BpCollideResult), _VP]),
+    "fclgpu_broadphase_collide_contacts_device": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpContactsRequest),
+                                                            C.POINTER(BpContactsResult), _VP]),
+    "fclgpu_broadphase_collide_contacts": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpContactsRequest),
+                                                     C.POINTER(BpContactsResult), _VP]),
+    "fclgpu_broadphase_self_collide_contacts_device": (C.c_int, [_VP, C.POINTER(BpContactsRequest),
+                                                                 C.POINTER(BpContactsResult), _VP]),
+    "fclgpu_broadphase_self_collide_contacts": (C.c_int, [_VP, C.POINTER(BpContactsRequest),
+                                                          C.POINTER(BpContactsResult), _VP]),
+    "fclgpu_broadphase_self_distance": (C.c_int, [_VP, C.POINTER(BpDistanceRequest), C.POINTER(BpSelfDistanceResult),
+                                                  _VP]),
     "fclgpu_broadphase_distance_device": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
                                                     C.POINTER(BpDistanceResult), _VP]),
     "fclgpu_broadphase_distance": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.POINTER(BpDistanceRequest),
@@ -196,6 +225,10 @@ _SIGS = {
                                                  C.POINTER(MeshShapeRequest), C.POINTER(MeshShapeResult), _VP]),
     "fclgpu_mesh_shape_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, _VP, _VP, _VP, _VP,
                                           C.POINTER(MeshShapeRequest), C.POINTER(MeshShapeResult), _VP]),
+    "fclgpu_mesh_shape_contacts_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, _VP, _VP, _VP, _VP, C.c_int64,
+                                                    C.POINTER(MeshShapeContactsResult), _VP]),
+    "fclgpu_mesh_shape_contacts": (C.c_int, [_VP, C.c_int32, _VP, C.c_int64, _VP, _VP, _VP, _VP, C.c_int64,
+                                             C.POINTER(MeshShapeContactsResult), _VP]),
 }
 
 

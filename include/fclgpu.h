@@ -406,6 +406,32 @@ FCLGPU_API int fclgpu_mesh_shape_batch(const fclgpu_mesh* meshes, int32_t num_me
                                        const fclgpu_mesh_shape_request* req, fclgpu_mesh_shape_result* res,
                                        void* stream);
 
+/* Mesh x convex shape collide with the contact list: the mesh triangles that
+ * MeshShapeCollisionTraversalNode::leafTesting adds as Contact(mesh, shape, triangle,
+ * NONE) (mesh_shape_collision_traversal_node-inl.h:64-102; FCL records the mesh first
+ * whichever argument order fcl::collide got, collision-inl.h:124-131), in the order the
+ * traversal adds them, at most num_max_contacts per pair.  Pair i's triangles are
+ * tris[offsets[i] .. offsets[i+1]); counts[i] = offsets[i+1] - offsets[i].
+ * total_contacts is set on return; when it exceeds capacity the call returns
+ * FCLGPU_ERR_CAPACITY and tris is left untouched (counts and offsets are filled). */
+typedef struct {
+  int32_t* counts;
+  int64_t* offsets;  /* n + 1 entries */
+  int32_t* tris;
+  int64_t capacity;  /* entries tris can hold */
+  int64_t total_contacts;
+} fclgpu_mesh_shape_contacts_result;
+
+FCLGPU_API int fclgpu_mesh_shape_contacts_device(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                                 fclgpu_shapeset shapes, int64_t n, const int32_t* mesh_idx,
+                                                 const int32_t* shape_idx, const double* tf_mesh,
+                                                 const double* tf_shape, int64_t num_max_contacts,
+                                                 fclgpu_mesh_shape_contacts_result* res, void* stream);
+FCLGPU_API int fclgpu_mesh_shape_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, fclgpu_shapeset shapes,
+                                          int64_t n, const int32_t* mesh_idx, const int32_t* shape_idx,
+                                          const double* tf_mesh, const double* tf_shape, int64_t num_max_contacts,
+                                          fclgpu_mesh_shape_contacts_result* res, void* stream);
+
 /* ---- broadphase -------------------------------------------------------------------
  * Replaces DynamicAABBTreeCollisionManager<double> (broadphase/
  * broadphase_dynamic_AABB_tree.h:56-157, -inl.h:727-1009) behind
@@ -505,6 +531,77 @@ FCLGPU_API int fclgpu_broadphase_distance_device(fclgpu_broadphase bp, const fcl
 FCLGPU_API int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries, int64_t nq,
                                           const double* tf, const fclgpu_broadphase_distance_request* req,
                                           fclgpu_broadphase_distance_result* res, void* stream);
+/* Contact lists of broadphase collide queries: the contacts DefaultCollisionFunction
+ * records (default_broadphase_callbacks.h:88-106) as Contact(o1, o2, b1, b2), with o1
+ * the scene object and o2 the query, as FCL's manager calls the narrowphase
+ * (broadphase_dynamic_AABB_tree-inl.h:526-547).  Every (query, scene object) pair
+ * whose AABBs overlap is evaluated, each capped at num_max_contacts contacts (a fresh
+ * CollisionResult per pair).  Per query the contacts are ordered by scene-object index,
+ * and each object's contacts come in the order FCL's narrowphase adds them: (object,
+ * -1, -1) for a shape pair, (object, b1, b2) for a mesh pair (b1 the object's
+ * triangle, b2 the query's), (object, triangle, -1) for a mesh-shape pair (FCL records
+ * the mesh's triangle as b1 whichever is the mesh).  FCL's manager meets the objects in
+ * its tree's order and stops at num_max_contacts in all: with num_max_contacts at least
+ * the query's total its contact set is this list's; FCL's numContacts() is
+ * min(num_max_contacts, counts[q]). */
+typedef struct {
+  int64_t num_max_contacts;  /* per (query, object) pair, >= 1 */
+  int32_t precision;         /* mesh-mesh narrowphase form */
+  int32_t reserved;
+} fclgpu_broadphase_contacts_request;
+
+/* counts[q] contacts of query q at contacts[3 * offsets[q] ..) as (object, b1, b2)
+ * int32 triples; offsets has nq + 1 entries.  capacity = triples contacts can hold;
+ * total_contacts is set on return and a larger total returns FCLGPU_ERR_CAPACITY with
+ * counts and offsets filled and contacts untouched. */
+typedef struct {
+  int64_t* counts;
+  int64_t* offsets;
+  int32_t* contacts;
+  int64_t capacity;
+  int64_t total_contacts;
+  int64_t total_candidates;
+  int64_t total_node_visits;
+} fclgpu_broadphase_contacts_result;
+
+FCLGPU_API int fclgpu_broadphase_collide_contacts_device(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries,
+                                                         int64_t nq, const double* tf,
+                                                         const fclgpu_broadphase_contacts_request* req,
+                                                         fclgpu_broadphase_contacts_result* res, void* stream);
+FCLGPU_API int fclgpu_broadphase_collide_contacts(fclgpu_broadphase bp, const fclgpu_geometry_ref* queries,
+                                                  int64_t nq, const double* tf,
+                                                  const fclgpu_broadphase_contacts_request* req,
+                                                  fclgpu_broadphase_contacts_result* res, void* stream);
+/* manager.collide(cdata, DefaultCollisionFunction): the scene against itself
+ * (broadphase_dynamic_AABB_tree-inl.h:949-965, selfCollisionRecurse :552-567).  Every
+ * unordered pair of scene objects with overlapping AABBs is evaluated once, as
+ * Contact(o1, o2, ...) with o1 < o2; the lists are grouped by o2 (counts and offsets
+ * have one entry per scene object, segment q holding the pairs (o1 < q, o2 = q) in
+ * ascending o1), each triple (o1, b1, b2) with b1 on o1 and b2 on o2. */
+FCLGPU_API int fclgpu_broadphase_self_collide_contacts_device(fclgpu_broadphase bp,
+                                                              const fclgpu_broadphase_contacts_request* req,
+                                                              fclgpu_broadphase_contacts_result* res, void* stream);
+FCLGPU_API int fclgpu_broadphase_self_collide_contacts(fclgpu_broadphase bp,
+                                                       const fclgpu_broadphase_contacts_request* req,
+                                                       fclgpu_broadphase_contacts_result* res, void* stream);
+/* manager.distance(cdata, DefaultDistanceFunction): the smallest distance between two
+ * scene objects (broadphase_dynamic_AABB_tree-inl.h:968-987 -> selfDistanceRecurse
+ * :706-720), evaluated over every unordered pair whose AABB distance is within an
+ * upper bound of it.  o1 < o2; b1, b2 their triangle ids (-1 for shapes);
+ * nearest_points the world witnesses on o1 then o2 (with enable_nearest_points).  Ties
+ * go to the smaller o2, then the smaller o1; FCL reports the first its traversal
+ * meets.  A value <= 0 means some pair is in contact (FCL stops there).  DBL_MAX with
+ * fewer than two objects.  Host result. */
+typedef struct {
+  double min_distance;
+  int32_t o1, o2;
+  int32_t b1, b2;
+  double nearest_points[6];
+  int64_t total_candidates;
+} fclgpu_broadphase_self_distance_result;
+
+FCLGPU_API int fclgpu_broadphase_self_distance(fclgpu_broadphase bp, const fclgpu_broadphase_distance_request* req,
+                                               fclgpu_broadphase_self_distance_result* out, void* stream);
 /* Wall-clock phases of the broadphase collide (out16[0..7]) and distance (out16[8..15])
  * calls made since the previous read (reading resets them): [0] query setup and
  * candidate passes, [1] shape-shape pairs,

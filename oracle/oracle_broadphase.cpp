@@ -220,7 +220,11 @@ int select_child(const AABB& q, const AABB& b1, const AABB& b2) {
 // fcl::collide(o1, o2, request, result) accumulating into one CollisionResult
 // (collision-inl.h:79-149): ShapeShapeCollide (collision_func_matrix-inl.h:278-311)
 // or orientedMeshCollide (:571-626).  Returns the contacts it added.
-int64_t narrow_collide(const BpObject& o1, const BpObject& o2, int64_t max_contacts, int64_t cur) {
+// With ids, each added contact's (b1, b2) is appended: NONE (-1) for shapes, the mesh
+// triangle as b1 for a mesh-shape pair (FCL records the mesh first whichever argument
+// order it got, collision-inl.h:124-131).
+int64_t narrow_collide(const BpObject& o1, const BpObject& o2, int64_t max_contacts, int64_t cur,
+                       std::vector<int>* ids = nullptr) {
   if (cur > 0 && max_contacts <= cur) return 0;  // CollisionRequest::isSatisfied
   const BpGeom& g1 = *o1.geom;
   const BpGeom& g2 = *o2.geom;
@@ -228,17 +232,32 @@ int64_t narrow_collide(const BpObject& o1, const BpObject& o2, int64_t max_conta
     // ShapeCollisionTraversalNode::leafTesting (shape_collision_traversal_node-inl.h:70-136)
     ShapeResult r;
     const bool hit = shape_intersect(g1.shape, o1.tf, g2.shape, o2.tf, r, false);
-    return (hit && max_contacts > cur) ? 1 : 0;
+    const int64_t added = (hit && max_contacts > cur) ? 1 : 0;
+    if (ids && added) {
+      ids->push_back(-1);
+      ids->push_back(-1);
+    }
+    return added;
   }
   if (g1.kind == 1 && g2.kind == 1) {
     std::vector<int> contacts;
-    return (int64_t)collide_mesh(*g1.mesh, o1.tf, *g2.mesh, o2.tf, (size_t)(max_contacts - cur), contacts, nullptr);
+    const size_t k =
+        collide_mesh(*g1.mesh, o1.tf, *g2.mesh, o2.tf, (size_t)(max_contacts - cur), contacts, nullptr);
+    if (ids) ids->insert(ids->end(), contacts.begin(), contacts.begin() + 2 * k);
+    return (int64_t)k;
   }
   // BVHShapeCollider; a shape first is swapped to mesh first (collision-inl.h:100-111)
   const BpObject& om = g1.kind == 1 ? o1 : o2;
   const BpObject& os = g1.kind == 1 ? o2 : o1;
-  return (int64_t)collide_mesh_shape(*om.geom->mesh, om.tf, os.geom->shape, os.tf, (size_t)(max_contacts - cur),
-                                     nullptr, nullptr);
+  std::vector<int> tris;
+  const size_t k = collide_mesh_shape(*om.geom->mesh, om.tf, os.geom->shape, os.tf, (size_t)(max_contacts - cur),
+                                      ids ? &tris : nullptr, nullptr);
+  if (ids)
+    for (size_t i = 0; i < k; ++i) {
+      ids->push_back(tris[i]);
+      ids->push_back(-1);
+    }
+  return (int64_t)k;
 }
 
 // fcl::distance(o1, o2, request, result) accumulating into one DistanceResult:
@@ -348,6 +367,70 @@ bool distance_recurse(const DynTree& t, int node, DistanceCtx& c, double& min_di
 }
 
 }  // namespace
+
+void bp_collide_lists(const std::vector<BpObject>& scene, const BpObject& query, int64_t max_per_pair,
+                      std::vector<int>& out) {
+  for (int i = 0; i < (int)scene.size(); ++i) {
+    if (!aabb_overlap(scene[i].aabb, query.aabb)) continue;
+    std::vector<int> ids;
+    const int64_t k = narrow_collide(scene[i], query, max_per_pair, 0, &ids);
+    for (int64_t t = 0; t < k; ++t) {
+      out.push_back(i);
+      out.push_back(ids[2 * t]);
+      out.push_back(ids[2 * t + 1]);
+    }
+  }
+}
+
+int64_t bp_self_collide_naive(const std::vector<BpObject>& scene, int64_t max_contacts) {
+  int64_t num = 0;
+  for (int i = 0; i < (int)scene.size(); ++i)
+    for (int j = i + 1; j < (int)scene.size(); ++j) {
+      if (!aabb_overlap(scene[i].aabb, scene[j].aabb)) continue;
+      num += narrow_collide(scene[i], scene[j], max_contacts, num);
+      if (num > 0 && num >= max_contacts) return num;  // DefaultCollisionFunction's done
+    }
+  return num;
+}
+
+void bp_self_collide_lists(const std::vector<BpObject>& scene, int64_t max_per_pair, std::vector<int64_t>& counts,
+                           std::vector<int>& out) {
+  counts.assign(scene.size(), 0);
+  for (int j = 0; j < (int)scene.size(); ++j)
+    for (int i = 0; i < j; ++i) {
+      if (!aabb_overlap(scene[i].aabb, scene[j].aabb)) continue;
+      std::vector<int> ids;
+      const int64_t k = narrow_collide(scene[i], scene[j], max_per_pair, 0, &ids);
+      counts[j] += k;
+      for (int64_t t = 0; t < k; ++t) {
+        out.push_back(i);
+        out.push_back(ids[2 * t]);
+        out.push_back(ids[2 * t + 1]);
+      }
+    }
+}
+
+void bp_self_distance_naive(const std::vector<BpObject>& scene, BpSelfDistanceOut& out) {
+  BpDistanceOut d;
+  d.min_distance = std::numeric_limits<double>::max();
+  out = BpSelfDistanceOut();
+  double min_dist = std::numeric_limits<double>::max();
+  for (int i = 0; i < (int)scene.size(); ++i)
+    for (int j = i + 1; j < (int)scene.size(); ++j) {
+      if (!(aabb_distance(scene[i].aabb, scene[j].aabb) < min_dist)) continue;
+      const double before = d.min_distance;
+      narrow_distance(scene[i], i, scene[j], d);
+      if (d.min_distance < before) out.o2 = j;
+      min_dist = d.min_distance;
+      if (min_dist <= 0) break;
+    }
+  out.min_distance = d.min_distance;
+  out.o1 = d.object;
+  out.b1 = d.b1;
+  out.b2 = d.b2;
+  out.p1 = d.p1;
+  out.p2 = d.p2;
+}
 
 void DynTree::build(const std::vector<AABB>& leaf_bv) {
   nodes.clear();

@@ -86,4 +86,31 @@ void bp_collide(const std::vector<BpObject>& scene, const DynTree* tree, const B
 void bp_distance(const std::vector<BpObject>& scene, const DynTree* tree, const BpObject& query,
                  BpDistanceOut& out);
 
+// The contact lists of the GPU broadphase contacts call: every scene object whose
+// AABB overlaps the query, in index order, collide(object, query) with a fresh
+// CollisionResult capped at max_per_pair; triples (object, b1, b2) appended to out.
+void bp_collide_lists(const std::vector<BpObject>& scene, const BpObject& query, int64_t max_per_pair,
+                      std::vector<int>& out);
+
+// NaiveCollisionManager::collide(cdata, DefaultCollisionFunction)
+// (broadphase_bruteforce-inl.h:140-157): pairs (i < j) with overlapping AABBs in list
+// order, one CollisionResult capped at max_contacts; returns its numContacts().
+int64_t bp_self_collide_naive(const std::vector<BpObject>& scene, int64_t max_contacts);
+
+// The self-collision lists of the GPU call: for each o2, the objects o1 < o2 with
+// overlapping AABBs in ascending order, collide(o1, o2) with a fresh result capped at
+// max_per_pair; counts per o2 and (o1, b1, b2) triples.
+void bp_self_collide_lists(const std::vector<BpObject>& scene, int64_t max_per_pair, std::vector<int64_t>& counts,
+                           std::vector<int>& out);
+
+// NaiveCollisionManager::distance(cdata, DefaultDistanceFunction)
+// (broadphase_bruteforce-inl.h:161-177): the first smallest distance over pairs
+// (i < j) in list order, pruned by AABB distance; stops at a distance <= 0.
+struct BpSelfDistanceOut {
+  double min_distance = 0;
+  int o1 = -1, o2 = -1, b1 = -1, b2 = -1;
+  V3 p1, p2;
+};
+void bp_self_distance_naive(const std::vector<BpObject>& scene, BpSelfDistanceOut& out);
+
 }  // namespace oracle

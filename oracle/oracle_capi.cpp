@@ -589,6 +589,62 @@ int64_t orc_scene_collide(void* h, int64_t nq, const int* qgid, const double* qt
   return total;
 }
 
+// Contact lists of the GPU broadphase contacts call per query (bp_collide_lists):
+// counts[q], and the (object, b1, b2) triples of every query one after the other in
+// trip when the total fits cap.  Returns the total.
+int64_t orc_scene_collide_lists(void* h, int64_t nq, const int* qgid, const double* qtf, int64_t max_per_pair,
+                                int nthreads, int64_t* counts, int* trip, int64_t cap) {
+  const OrcScene* S = static_cast<OrcScene*>(h);
+  std::vector<std::vector<int>> per(nq);
+  parallel_for(nq, nthreads, [&](int64_t q, int) {
+    const BpObject Q = make_object(*S->geoms, qgid[q], qtf + 12 * q);
+    bp_collide_lists(S->objs, Q, max_per_pair, per[q]);
+    counts[q] = (int64_t)(per[q].size() / 3);
+  });
+  int64_t total = 0;
+  for (const auto& v : per) total += (int64_t)(v.size() / 3);
+  if (total <= cap) {
+    int64_t k = 0;
+    for (const auto& v : per)
+      for (int x : v) trip[k++] = x;
+  }
+  return total;
+}
+
+// Self-collision lists (bp_self_collide_lists): counts per o2 and (o1, b1, b2) triples.
+int64_t orc_scene_self_collide_lists(void* h, int64_t max_per_pair, int64_t* counts, int* trip, int64_t cap) {
+  const OrcScene* S = static_cast<OrcScene*>(h);
+  std::vector<int64_t> c;
+  std::vector<int> v;
+  bp_self_collide_lists(S->objs, max_per_pair, c, v);
+  for (size_t i = 0; i < c.size(); ++i) counts[i] = c[i];
+  const int64_t total = (int64_t)(v.size() / 3);
+  if (total <= cap)
+    for (size_t i = 0; i < v.size(); ++i) trip[i] = v[i];
+  return total;
+}
+
+// NaiveCollisionManager::collide(cdata, DefaultCollisionFunction): numContacts().
+int64_t orc_scene_self_collide_naive(void* h, int64_t max_contacts) {
+  return bp_self_collide_naive(static_cast<OrcScene*>(h)->objs, max_contacts);
+}
+
+// NaiveCollisionManager::distance(cdata, DefaultDistanceFunction): d[0] = distance,
+// d[1..6] = witnesses (on o1, on o2); ids = (o1, o2, b1, b2).
+void orc_scene_self_distance(void* h, double* d, int* ids) {
+  BpSelfDistanceOut o;
+  bp_self_distance_naive(static_cast<OrcScene*>(h)->objs, o);
+  d[0] = o.min_distance;
+  for (int k = 0; k < 3; ++k) {
+    d[1 + k] = o.p1[k];
+    d[4 + k] = o.p2[k];
+  }
+  ids[0] = o.o1;
+  ids[1] = o.o2;
+  ids[2] = o.b1;
+  ids[3] = o.b2;
+}
+
 // manager.distance(query, DefaultDistanceFunction) per query.  Outputs: min distance,
 // scene object, (b1, b2) triangle ids (-1 for shapes), world witnesses (6 doubles).
 void orc_scene_distance(void* h, int64_t nq, const int* qgid, const double* qtf, int use_tree, int nthreads,
@@ -645,6 +701,30 @@ void orc_mesh_shape_batch(void* h, void* g, int64_t n, const int* sid, const dou
     if (nbv) nbv[q] = st.num_bv_tests;
     if (nleaf) nleaf[q] = st.num_leaf_tests;
   });
+}
+
+// fcl::collide(mesh, shape) per query with the contact list: the triangle ids of the
+// contacts FCL adds (Contact b1), in order, at most max_contacts per query.  counts[q]
+// per query; tris holds the lists one after the other when the total fits cap.
+// Returns the total.
+int64_t orc_mesh_shape_contacts(void* h, void* g, int64_t n, const int* sid, const double* tfm, const double* tfs,
+                                int64_t max_contacts, int nthreads, int64_t* counts, int* tris, int64_t cap) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  const OrcGeoms* G = static_cast<OrcGeoms*>(g);
+  std::vector<std::vector<int>> lists((size_t)n);
+  parallel_for(n, nthreads, [&](int64_t q, int) {
+    const Shape& s = G->g[sid[q]].shape;
+    const Tf a = load_tf(tfm + 12 * q), b = load_tf(tfs + 12 * q);
+    counts[q] = (int64_t)collide_mesh_shape(*m, a, s, b, (size_t)max_contacts, &lists[(size_t)q], nullptr);
+  });
+  int64_t total = 0;
+  for (const auto& l : lists) total += (int64_t)l.size();
+  if (total <= cap) {
+    int64_t k = 0;
+    for (const auto& l : lists)
+      for (int t : l) tris[k++] = t;
+  }
+  return total;
 }
 
 // Brute force over every triangle of the mesh (for the traversal tests): collide ->

@@ -443,6 +443,59 @@ class Scene:
                                     _q(nc), _i(nh), _i(hits), total, _q(calls))
         return dict(num_contacts=nc, num_hits=nh, hits=hits[:total], narrow_calls=calls)
 
+    def collide_lists(self, qgid, qtf, max_per_pair: int = 1, nthreads: int = 1):
+        """The GPU broadphase contacts call's definition: per query, the overlapping
+        scene objects in index order, each collided with a fresh result capped at
+        max_per_pair -> (counts, (total, 3) rows (object, b1, b2))."""
+        L = lib()
+        L.orc_scene_collide_lists.restype = C.c_int64
+        L.orc_scene_collide_lists.argtypes = [C.c_void_p, C.c_int64, _ip, _dp, C.c_int64, C.c_int, _i64p, _ip,
+                                              C.c_int64]
+        qgid = np.ascontiguousarray(qgid, np.int32)
+        qtf = np.ascontiguousarray(qtf, np.float64).reshape(-1, 12)
+        n = qgid.shape[0]
+        counts = np.zeros(n, np.int64)
+        cap = 64 * n + 64
+        while True:
+            trip = np.zeros((cap, 3), np.int32)
+            total = L.orc_scene_collide_lists(self.h, n, _i(qgid), _d(qtf), max_per_pair, nthreads, _q(counts),
+                                              _i(trip), cap)
+            if total <= cap:
+                return counts, trip[:total]
+            cap = total
+
+    def self_collide_lists(self, max_per_pair: int = 1):
+        """Self-collision lists: per o2 the objects o1 < o2 in ascending order ->
+        (counts per o2, rows (o1, b1, b2))."""
+        L = lib()
+        L.orc_scene_self_collide_lists.restype = C.c_int64
+        L.orc_scene_self_collide_lists.argtypes = [C.c_void_p, C.c_int64, _i64p, _ip, C.c_int64]
+        n = self.gid.shape[0]
+        counts = np.zeros(n, np.int64)
+        cap = 64 * n + 64
+        while True:
+            trip = np.zeros((cap, 3), np.int32)
+            total = L.orc_scene_self_collide_lists(self.h, max_per_pair, _q(counts), _i(trip), cap)
+            if total <= cap:
+                return counts, trip[:total]
+            cap = total
+
+    def self_collide_count(self, max_contacts: int = 1) -> int:
+        """NaiveCollisionManager::collide(cdata, DefaultCollisionFunction): numContacts()."""
+        L = lib()
+        L.orc_scene_self_collide_naive.restype = C.c_int64
+        L.orc_scene_self_collide_naive.argtypes = [C.c_void_p, C.c_int64]
+        return int(L.orc_scene_self_collide_naive(self.h, max_contacts))
+
+    def self_distance(self):
+        """NaiveCollisionManager::distance(cdata, DefaultDistanceFunction)."""
+        L = lib()
+        L.orc_scene_self_distance.argtypes = [C.c_void_p, _dp, _ip]
+        d = np.zeros(7); ids = np.zeros(4, np.int32)
+        L.orc_scene_self_distance(self.h, _d(d), _i(ids))
+        return dict(min_distance=float(d[0]), o1=int(ids[0]), o2=int(ids[1]), b1=int(ids[2]), b2=int(ids[3]),
+                    nearest_points=d[1:].reshape(2, 3))
+
     def distance(self, qgid, qtf, use_tree: bool = True, nthreads: int = 1):
         qgid = np.ascontiguousarray(qgid, np.int32)
         qtf = np.ascontiguousarray(qtf, np.float64).reshape(-1, 12)
@@ -479,6 +532,28 @@ def mesh_shape_collide(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, max_contacts: in
     L.orc_mesh_shape_batch(mesh.h, geoms.h, n, _i(sid), _d(tfm), _d(tfs), max_contacts, 0, nthreads, _q(counts),
                            _d(dummy_d), _i(dummy_i), _d(dummy_d), _q(nbv), _q(nleaf))
     return counts, nbv, nleaf
+
+
+def mesh_shape_contacts(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, max_contacts: int = 1, nthreads: int = 1):
+    """fcl::collide(mesh, shape) per query with the contact list -> (counts, tris): the
+    triangle ids of every query's contacts, in the order FCL adds them, concatenated."""
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    L.orc_mesh_shape_contacts.restype = C.c_int64
+    L.orc_mesh_shape_contacts.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _ip, _dp, _dp, C.c_int64, C.c_int,
+                                          _i64p, _ip, C.c_int64]
+    sid = np.ascontiguousarray(sid, np.int32)
+    n = sid.shape[0]
+    tfm = np.ascontiguousarray(tfm, np.float64).reshape(n, 12)
+    tfs = np.ascontiguousarray(tfs, np.float64).reshape(n, 12)
+    counts = np.zeros(n, np.int64)
+    cap = 16 * n + 16
+    while True:
+        tris = np.zeros(cap, np.int32)
+        total = L.orc_mesh_shape_contacts(mesh.h, geoms.h, n, _i(sid), _d(tfm), _d(tfs), max_contacts, nthreads,
+                                          _q(counts), _i(tris), cap)
+        if total <= cap:
+            return counts, tris[:total]
+        cap = total
 
 
 def mesh_shape_distance(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, nthreads: int = 1):

@@ -147,3 +147,101 @@ def test_broadphase_rejects_bad_refs(gpu_lib):
     bad[3] = (0, 10 ** 6)
     with pytest.raises(FclGpuError):
         mgr.collide_batch(bad, qtf)
+
+
+def _mixed_scene(seed=41, n=500, nq=300, box=7.0):
+    """Shapes and meshes in the scene and among the queries (every pair kind)."""
+    shapes = W.random_shapes(64, seed)
+    vt = [W.perturbed_ellipsoid(f, r, 0.01, seed + 10 + k) for k, (f, r) in
+          enumerate([(5, (0.6, 0.4, 0.3)), (7, (0.5, 0.5, 0.5)), (4, (0.8, 0.3, 0.3))])]
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in vt]
+    om = [P.Mesh(v, t) for v, t in vt]
+    ss = api.ShapeSet.from_workload(shapes)
+    rng = np.random.default_rng(seed + 1)
+
+    def refs_of(k):
+        kind = (rng.uniform(size=k) < 0.35).astype(np.int32)
+        return np.stack([kind, np.where(kind == 1, rng.integers(0, 3, size=k), rng.integers(0, 64, size=k))],
+                        1).astype(np.int32)
+
+    refs, qrefs = refs_of(n), refs_of(nq)
+    tf = W.random_poses(n, 0.0, box, seed + 2)
+    qtf = W.random_poses(nq, 0.0, box, seed + 3)
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(refs, tf)
+    G = P.Geoms(shapes, om)
+    gid = np.where(refs[:, 0] == 1, 64 + refs[:, 1], refs[:, 1]).astype(np.int32)
+    qgid = np.where(qrefs[:, 0] == 1, 64 + qrefs[:, 1], qrefs[:, 1]).astype(np.int32)
+    return mgr, P.Scene(G, gid, tf), refs, tf, qrefs, qtf, qgid
+
+
+@pytest.mark.parametrize("M", [1, 3, 100000])
+def test_broadphase_contact_lists_match_oracle(gpu_lib, M):
+    """Per query every (object, b1, b2) DefaultCollisionFunction records, objects in
+    index order, each pair's contacts in FCL's narrowphase order, capped per pair."""
+    mgr, S, refs, tf, qrefs, qtf, qgid = _mixed_scene()
+    g = mgr.collide_contacts(qrefs, qtf, num_max_contacts=M)
+    c, trip = S.collide_lists(qgid, qtf, max_per_pair=M, nthreads=8)
+    np.testing.assert_array_equal(g["counts"], c)
+    np.testing.assert_array_equal(g["contacts"], trip)
+    kinds = set(map(int, refs[trip[:, 0], 0]))
+    assert kinds == {0, 1} and (trip[:, 1] >= 0).any() and (trip[:, 2] >= 0).any()
+    # FCL's numContacts() is min(num_max_contacts, the query's list length)
+    o = S.collide(qgid, qtf, max_contacts=M, use_tree=True, nthreads=8)
+    np.testing.assert_array_equal(np.minimum(g["counts"], M), o["num_contacts"])
+
+
+def test_broadphase_self_collide_matches_oracle(gpu_lib):
+    """manager.collide(cdata, DefaultCollisionFunction): every overlapping pair (o1 < o2)
+    once; lists equal the oracle's, and the total is FCL's naive manager numContacts()."""
+    mgr, S, refs, tf, qrefs, qtf, qgid = _mixed_scene(seed=43, n=700)
+    for M in (1, 100000):
+        g = mgr.collide_contacts(None, None, num_max_contacts=M)
+        c, trip = S.self_collide_lists(max_per_pair=M)
+        np.testing.assert_array_equal(g["counts"], c)
+        np.testing.assert_array_equal(g["contacts"], trip)
+    assert g["counts"].sum() > 10
+    assert S.self_collide_count(1 << 40) == g["counts"].sum()
+    assert S.self_collide_count(1) == min(1, int(g["counts"].sum()))
+    # the FCL-style entry point appends Contact(o1, o2, b1, b2) up to num_max_contacts
+    res = api.CollisionResult()
+    n = mgr.collide(None, api.CollisionRequest(num_max_contacts=5), res)
+    assert n == min(5, int(g["counts"].sum()))
+    o2 = np.repeat(np.arange(mgr.size()), g["counts"])
+    assert [(ct.o1, ct.o2, ct.b1, ct.b2) for ct in res.contacts] == \
+        [(int(a), int(q), int(b), int(d)) for (a, b, d), q in zip(g["contacts"][:5], o2[:5])]
+
+
+def test_broadphase_self_distance_matches_oracle(gpu_lib):
+    """manager.distance(cdata, DefaultDistanceFunction): the nearest pair of scene objects."""
+    for seed, n, box in ((45, 300, 30.0), (47, 300, 60.0)):  # some pair in contact
+        mgr, S, *_ = _mixed_scene(seed=seed, n=n, box=box)
+        assert S.self_distance()["min_distance"] <= 0 and mgr.self_distance()["min_distance"] <= 0
+    # separated scenes: nearest pair mesh-shape, shape-shape, mesh-shape
+    for seed, n, box in ((45, 200, 60.0), (47, 200, 80.0), (51, 150, 60.0)):
+        mgr, S, *_ = _mixed_scene(seed=seed, n=n, box=box)
+        g = mgr.self_distance()
+        o = S.self_distance()
+        assert o["min_distance"] > 0
+        assert abs(g["min_distance"] - o["min_distance"]) <= max(REL * o["min_distance"], ABS)
+        assert (g["o1"], g["o2"]) == (o["o1"], o["o2"])
+        assert (g["b1"], g["b2"]) == (o["b1"], o["b2"])
+        assert np.all(np.abs(g["nearest_points"] - o["nearest_points"]) <= REL * np.maximum(
+            np.abs(o["nearest_points"]), 1.0) + ABS)
+        r = api.DistanceResult()
+        mgr.distance(None, api.DistanceRequest(enable_nearest_points=True), r)
+        assert r.min_distance == g["min_distance"] and (r.o1, r.o2) == (g["o1"], g["o2"])
+
+
+def test_broadphase_manager_against_manager(gpu_lib):
+    """collide(other_manager, ...): every object of the other manager against this scene."""
+    mgr, S, refs, tf, qrefs, qtf, qgid = _mixed_scene(seed=49)
+    other = api.DynamicAABBTreeCollisionManager(mgr.shapes, mgr.meshes)
+    other.registerObjects(qrefs, qtf)
+    res = api.CollisionResult()
+    total = mgr.collide(other, api.CollisionRequest(num_max_contacts=1 << 30), res)
+    c, trip = S.collide_lists(qgid, qtf, max_per_pair=1 << 30, nthreads=8)
+    assert total == c.sum() > 0
+    q = np.repeat(np.arange(qgid.shape[0]), c)
+    assert [(ct.o1, ct.o2, ct.b1, ct.b2) for ct in res.contacts] == \
+        [(int(a), int(b), int(d), int(e)) for (a, d, e), b in zip(trip, q)]

@@ -111,3 +111,42 @@ def test_mesh_shape_split_form_matches_oracle(gpu_lib, seed):
         np.testing.assert_array_equal(g["min_distance"][sel], o["dist"])
         np.testing.assert_array_equal(g["tri"][sel], o["tri"])
         np.testing.assert_array_equal(g["nearest_points"][sel], o["pts"])
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mesh_shape_contact_lists_match_oracle(gpu_lib, seed):
+    """Mesh-shape collide with the contact list: the triangles FCL records as
+    Contact(mesh, shape, triangle, NONE), in the order its traversal adds them, at caps
+    1, 7 and 100,000 (exhaustive)."""
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(seed, n=2000)
+    for M in (1, 7, 100000):
+        g = api.mesh_shape_contacts_batch(meshes, ss, midx, sidx, tfm, tfs, num_max_contacts=M)
+        assert np.array_equal(np.diff(g["offsets"]), g["counts"])
+        for k in range(2):
+            sel = np.nonzero(midx == k)[0]
+            c, tris = P.mesh_shape_contacts(om[k], G, sidx[sel], tfm[sel], tfs[sel], max_contacts=M, nthreads=8)
+            np.testing.assert_array_equal(g["counts"][sel], c)
+            got = np.concatenate([g["tris"][g["offsets"][q]:g["offsets"][q + 1]] for q in sel])
+            np.testing.assert_array_equal(got, tris)
+        assert g["counts"].max() > (1 if M > 1 else 0)
+
+
+def test_mesh_shape_contact_list_capacity(gpu_lib):
+    """A tris buffer smaller than the total returns FCLGPU_ERR_CAPACITY with the total,
+    counts and offsets set, and leaves the buffer untouched."""
+    import ctypes as C
+    from fcl_gb300 import native as N
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(3, n=500)
+    full = api.mesh_shape_contacts_batch(meshes, ss, midx, sidx, tfm, tfs, num_max_contacts=100000)
+    total = int(full["offsets"][-1])
+    assert total > 4
+    counts = np.zeros(500, np.int32); offsets = np.zeros(501, np.int64); tris = np.full(4, -7, np.int32)
+    res = N.MeshShapeContactsResult(counts.ctypes.data, offsets.ctypes.data, tris.ctypes.data, 4, 0)
+    hs = (C.c_void_p * 2)(*[m.handle.value for m in meshes])
+    m_, s_ = np.ascontiguousarray(midx), np.ascontiguousarray(sidx)
+    rc = N.lib().fclgpu_mesh_shape_contacts(hs, 2, ss.handle, 500, m_.ctypes.data, s_.ctypes.data,
+                                            np.ascontiguousarray(tfm).ctypes.data,
+                                            np.ascontiguousarray(tfs).ctypes.data, 100000, C.byref(res), None)
+    assert rc == N.FCLGPU_ERR_CAPACITY and res.total_contacts == total
+    assert np.array_equal(counts, full["counts"]) and np.array_equal(offsets, full["offsets"])
+    assert (tris == -7).all()

@@ -150,3 +150,33 @@ def test_other_manager_names_answer_like_the_tree():
         assert issubclass(cls, api.DynamicAABBTreeCollisionManager)
         for m in ("registerObjects", "setup", "update", "collide_batch", "distance_batch", "size"):
             assert callable(getattr(cls, m))
+
+
+def test_contact_lists_hold_fcl_callback_contacts():
+    """The list definition (each overlapping object in index order, a fresh result per
+    pair) against FCL's manager with DefaultCollisionFunction: with a cap above every
+    total the per-query totals and the colliding objects are FCL's; with cap M FCL's
+    numContacts() is min(M, the list length)."""
+    shapes = W.random_shapes(64, 3)
+    vt = [W.perturbed_ellipsoid(4, (0.6, 0.4, 0.3), 0.01, 5)]
+    G = P.Geoms(shapes, [P.Mesh(*vt[0])])
+    rng = np.random.default_rng(4)
+    n, nq = 300, 200
+    gid = np.where(rng.uniform(size=n) < 0.3, 64, rng.integers(0, 64, size=n)).astype(np.int32)
+    qgid = np.where(rng.uniform(size=nq) < 0.3, 64, rng.integers(0, 64, size=nq)).astype(np.int32)
+    S = P.Scene(G, gid, W.random_poses(n, 0.0, 6.0, 5))
+    qtf = W.random_poses(nq, 0.0, 6.0, 6)
+    c, trip = S.collide_lists(qgid, qtf, max_per_pair=1 << 30, nthreads=4)
+    o = S.collide(qgid, qtf, max_contacts=1 << 30, use_tree=True, nthreads=4)
+    np.testing.assert_array_equal(c, o["num_contacts"])
+    segs = np.split(trip[:, 0], np.cumsum(c)[:-1])
+    hits = np.split(o["hits"], np.cumsum(o["num_hits"])[:-1])
+    assert all(sorted(set(a)) == sorted(h) for a, h in zip(segs, hits))
+    for M in (1, 3):
+        cm, _ = S.collide_lists(qgid, qtf, max_per_pair=M, nthreads=4)
+        om = S.collide(qgid, qtf, max_contacts=M, use_tree=False, nthreads=4)
+        np.testing.assert_array_equal(np.minimum(cm, M), om["num_contacts"])
+    # the scene against itself: the lists' total is the naive manager's numContacts()
+    sc, strip = S.self_collide_lists(max_per_pair=1 << 30)
+    assert S.self_collide_count(1 << 40) == sc.sum() > 0
+    assert np.all(strip[:, 0] < np.repeat(np.arange(n), sc))
