@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
+from typing import ClassVar
 
 import numpy as np
 
@@ -226,11 +227,27 @@ def transform(R=None, t=None) -> np.ndarray:
 
 @dataclass
 class CollisionObject:
-    geometry: BVHModel
+    geometry: "BVHModel | ShapeRef"
     tf: np.ndarray = field(default_factory=lambda: transform())
 
     def setTransform(self, R, t):
         self.tf = transform(R, t)
+
+
+# GJKSolverType (narrowphase/gjk_solver_type.h): FCL's default is GST_LIBCCD, whose
+# MPR penetration and GJK distance come from libccd; this library provides FCL's own
+# solver, GST_INDEP (GJKSolver_indep).  Shape pairs asked for GST_LIBCCD are rejected
+# with FCLGPU_ERR_UNSUPPORTED; mesh-mesh pairs use no GJK solver and accept either.
+GST_LIBCCD = 0
+GST_INDEP = 1
+
+
+@dataclass
+class ShapeRef:
+    """A convex shape of a ShapeSet used as a CollisionObject's geometry (FCL's Box,
+    Sphere, Capsule, Cylinder, Cone and Convex behind shared_ptr<CollisionGeometry>)."""
+    shapes: "ShapeSet"
+    index: int
 
 
 @dataclass
@@ -239,10 +256,12 @@ class CollisionRequest:
     enable_contact: bool = False
     enable_statistics: bool = False
     precision: str = "fp32"
+    gjk_solver_type: int = GST_LIBCCD
 
 
 @dataclass
 class Contact:
+    NONE: ClassVar[int] = -1  # Contact::NONE, the primitive id of a shape (contact.h)
     o1: object
     o2: object
     b1: int
@@ -285,6 +304,7 @@ class DistanceRequest:
     abs_err: float = 0.0
     enable_statistics: bool = False
     precision: str = "fp32"
+    gjk_solver_type: int = GST_LIBCCD
 
 
 @dataclass
@@ -311,11 +331,93 @@ def _unsupported(req):
         raise N.FclGpuError(-9, "distance", "rel_err/abs_err must be 0 on the GPU path")
 
 
+def _shape_solver(request, where):
+    if request.gjk_solver_type != GST_INDEP:
+        raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED_, where,
+                            "GST_LIBCCD (libccd's MPR and GJK) is not provided: set gjk_solver_type = GST_INDEP "
+                            "for FCL's own GJK/EPA (GJKSolver_indep)")
+
+
+def _mesh_first(o1, o2):
+    """(mesh object, shape object): FCL calls the BVH-shape functions mesh first
+    whichever argument order it got (collision-inl.h:124-131, distance-inl.h:117-126)."""
+    return (o1, o2) if isinstance(o1.geometry, BVHModel) else (o2, o1)
+
+
+def _collide_shapes(o1, o2, request, result):
+    """Shape x shape and mesh x shape pairs of fcl::collide (GST_INDEP)."""
+    _shape_solver(request, "collide")
+    g1, g2 = o1.geometry, o2.geometry
+    room = max(0, request.num_max_contacts - len(result.contacts))
+    if isinstance(g1, ShapeRef) and isinstance(g2, ShapeRef):
+        if g1.shapes is not g2.shapes:
+            raise N.FclGpuError(N.FCLGPU_ERR_INVALID_ARGUMENT, "collide", "both shapes must come from one ShapeSet")
+        ia, ib = np.array([g1.index], np.int32), np.array([g2.index], np.int32)
+        if not request.enable_contact:
+            hit = np.zeros(1, np.int32)
+            N.check(N.lib().fclgpu_shape_collide_batch(g1.shapes.handle, 1, ia.ctypes.data, ib.ctypes.data,
+                                                       np.ascontiguousarray(o1.tf).ctypes.data,
+                                                       np.ascontiguousarray(o2.tf).ctypes.data, hit.ctypes.data, None),
+                    "fclgpu_shape_collide_batch")
+            if hit[0] and room > 0:
+                result.contacts.append(Contact(g1, g2, Contact.NONE, Contact.NONE))
+            return result.numContacts()
+        if request.num_max_contacts > 1:
+            types = [int(g.shapes._types[g.index]) for g in (g1, g2)]
+            if types == [0, 0]:  # boxBoxIntersect can add up to four contacts
+                raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED_, "collide",
+                                    "box-box contacts beyond the deepest one (num_max_contacts > 1)")
+        out = shape_batch(g1.shapes, ia, ib, o1.tf[None], o2.tf[None])
+        if out["hit"][0] and room > 0:
+            result.contacts.append(Contact(g1, g2, Contact.NONE, Contact.NONE, out["point"][0].copy(),
+                                           out["normal"][0].copy(), float(out["depth"][0])))
+        return result.numContacts()
+    if request.enable_contact:
+        raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED_, "collide", "contact geometry of mesh-shape pairs")
+    om, os_ = _mesh_first(o1, o2)
+    gs = os_.geometry
+    out = mesh_shape_contacts_batch([om.geometry], gs.shapes, np.zeros(1, np.int32), np.array([gs.index], np.int32),
+                                    om.tf[None], os_.tf[None], num_max_contacts=max(1, room))
+    for t in out["tris"][:room]:
+        result.contacts.append(Contact(om.geometry, gs, int(t), Contact.NONE))
+    return result.numContacts()
+
+
+def _distance_shapes(o1, o2, request, result):
+    """Shape x shape and mesh x shape pairs of fcl::distance (GST_INDEP)."""
+    _shape_solver(request, "distance")
+    g1, g2 = o1.geometry, o2.geometry
+    if isinstance(g1, ShapeRef) and isinstance(g2, ShapeRef):
+        if g1.shapes is not g2.shapes:
+            raise N.FclGpuError(N.FCLGPU_ERR_INVALID_ARGUMENT, "distance", "both shapes must come from one ShapeSet")
+        out = shape_batch(g1.shapes, np.array([g1.index], np.int32), np.array([g2.index], np.int32), o1.tf[None],
+                          o2.tf[None])
+        d = float(out["dist"][0]) if not out["hit"][0] else -1.0
+        cand = (d, g1, g2, Contact.NONE, Contact.NONE, np.stack([out["p1"][0], out["p2"][0]]))
+    else:
+        om, os_ = _mesh_first(o1, o2)
+        gs = os_.geometry
+        out = mesh_shape_batch([om.geometry], gs.shapes, np.zeros(1, np.int32), np.array([gs.index], np.int32),
+                               om.tf[None], os_.tf[None], mode="distance")
+        cand = (float(out["min_distance"][0]), om.geometry, gs, int(out["tri"][0]), Contact.NONE,
+                out["nearest_points"][0].copy())
+    d, a, b, b1, b2, pts = cand
+    if result.min_distance > d:
+        result.min_distance = d
+        result.o1, result.o2, result.b1, result.b2 = a, b, b1, b2
+        if request.enable_nearest_points:
+            result.nearest_points = pts
+    return result.min_distance
+
+
 def collide(o1: CollisionObject, o2: CollisionObject, request: CollisionRequest, result: CollisionResult) -> int:
-    """fcl::collide for two BVHModel<OBBRSS> objects; appends to result like FCL."""
+    """fcl::collide; appends to result like FCL.  Mesh x mesh (BVHModel<OBBRSS>), shape x
+    shape and mesh x shape pairs (ShapeRef geometries; GJKSolver_indep)."""
     _unsupported(request)
     if request.num_max_contacts == 0:
         return 0
+    if isinstance(o1.geometry, ShapeRef) or isinstance(o2.geometry, ShapeRef):
+        return _collide_shapes(o1, o2, request, result)
     if request.enable_contact:
         if request.enable_statistics:
             raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "collide", "statistics are not produced with contacts")
@@ -341,8 +443,11 @@ def collide(o1: CollisionObject, o2: CollisionObject, request: CollisionRequest,
 
 
 def distance(o1: CollisionObject, o2: CollisionObject, request: DistanceRequest, result: DistanceResult) -> float:
-    """fcl::distance for two BVHModel<OBBRSS> objects; DistanceResult::update semantics."""
+    """fcl::distance; DistanceResult::update semantics.  Mesh x mesh, shape x shape and
+    mesh x shape pairs (ShapeRef geometries; GJKSolver_indep)."""
     _unsupported(request)
+    if isinstance(o1.geometry, ShapeRef) or isinstance(o2.geometry, ShapeRef):
+        return _distance_shapes(o1, o2, request, result)
     out = distance_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None], o2.tf[None],
                          nearest_points=request.enable_nearest_points, precision=request.precision)
     d = float(out["min_distance"][0])
@@ -673,6 +778,7 @@ class ShapeSet:
             for k in range(3):
                 arr[i].params[k] = float(params[i, k])
         self._verts = verts if verts.shape[0] else np.zeros((1, 3))
+        self._types = types
         h = C.c_void_p()
         N.check(N.lib().fclgpu_shapeset_create(arr, n, self._verts.ctypes.data, verts.shape[0], C.byref(h)),
                 "fclgpu_shapeset_create")

@@ -222,4 +222,35 @@ int fclgpu_last_shape_kernel_time(double* ms) {
   return FCLGPU_OK;
 }
 
+int fclgpu_shape_collide_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
+                               const double* tf1, const double* tf2, int32_t* hit, void* stream) {
+  if (!set || n < 0 || (n > 0 && (!ia || !ib || !tf1 || !tf2 || !hit))) return FCLGPU_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FCLGPU_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nn = (size_t)n;
+  std::lock_guard<std::mutex> lk(g_mu);
+  CKS(g_ia.ensure(4 * nn), "inputs");
+  CKS(g_ib.ensure(4 * nn), "inputs");
+  CKS(g_tf1.ensure(96 * nn), "inputs");
+  CKS(g_tf2.ensure(96 * nn), "inputs");
+  CKS(g_hit.ensure(4 * nn), "outputs");
+  CKS(cudaMemcpyAsync(g_ia.p, ia, 4 * nn, cudaMemcpyHostToDevice, s), "h2d");
+  CKS(cudaMemcpyAsync(g_ib.p, ib, 4 * nn, cudaMemcpyHostToDevice, s), "h2d");
+  CKS(cudaMemcpyAsync(g_tf1.p, tf1, 96 * nn, cudaMemcpyHostToDevice, s), "h2d");
+  CKS(cudaMemcpyAsync(g_tf2.p, tf2, 96 * nn, cudaMemcpyHostToDevice, s), "h2d");
+  ShapeLaunch L{};
+  L.shapes = set->shapes;
+  L.verts = set->verts;
+  L.ia = (const int32_t*)g_ia.p;
+  L.ib = (const int32_t*)g_ib.p;
+  L.tf1 = (const double*)g_tf1.p;
+  L.tf2 = (const double*)g_tf2.p;
+  L.n = n;
+  L.hit = (int32_t*)g_hit.p;
+  CKS(launch_shape_collide_only(L, s), "shape collide");
+  CKS(cudaMemcpyAsync(hit, g_hit.p, 4 * nn, cudaMemcpyDeviceToHost, s), "d2h");
+  CKS(cudaStreamSynchronize(s), "shape collide");
+  return FCLGPU_OK;
+}
+
 }  // extern "C"

@@ -180,7 +180,23 @@ int grid_of(const void* kernel, int block, long long n) {
   return (int)std::max<long long>(1, std::min<long long>(want, (long long)sms * per_sm));
 }
 
+__global__ void __launch_bounds__(128) k_shape_collide_only(ShapeLaunch L) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < L.n; q += stride) {
+    PairOut o;
+    shape_pair_query(L.shapes[__ldg(L.ia + q)], L.shapes[__ldg(L.ib + q)], L.verts, L.tf1 + 12 * q, L.tf2 + 12 * q, o,
+                     PAIR_INTERSECT | PAIR_NO_CONTACT);
+    L.hit[q] = o.hit;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_shape_collide_only(const ShapeLaunch& L, cudaStream_t s) {
+  k_shape_collide_only<<<grid_of((const void*)k_shape_collide_only, 128, L.n), 128, 0, s>>>(L);
+  ++g_kernel_launches;
+  return cudaGetLastError();
+}
 
 cudaError_t launch_shape_batch(const ShapeLaunch& L, unsigned* bins, cudaStream_t s) {
   const int block = 128;

@@ -29,5 +29,8 @@ struct ShapeLaunch {
 
 // Whole batch in stages (bucket, intersect, EPA, distance); bins: 64 unsigned scratch.
 cudaError_t launch_shape_batch(const ShapeLaunch& L, unsigned* bins, cudaStream_t s);
+// fcl::collide with enable_contact = false: the boolean of every pair into L.hit (no
+// contact, no EPA, no distance).
+cudaError_t launch_shape_collide_only(const ShapeLaunch& L, cudaStream_t s);
 
 }  // namespace fclgpu

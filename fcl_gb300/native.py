@@ -17,6 +17,7 @@ FCLGPU_ERR_CAPACITY = -4
 FCLGPU_ERR_STACK_DEPTH = -6
 FCLGPU_ERR_DEVICE_STATUS = -7
 FCLGPU_ERR_NOT_INITIALIZED = -8
+FCLGPU_ERR_UNSUPPORTED_ = -9
 PLAIN_FP64 = 0
 FP32_RECHECK = 1
 
@@ -191,6 +192,7 @@ _SIGS = {
     "fclgpu_shapeset_destroy": (C.c_int, [_VP]),
     "fclgpu_shape_batch_device": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_shape_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "fclgpu_shape_collide_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_last_shape_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
     "fclgpu_broadphase_create": (C.c_int, [_VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.POINTER(C.c_void_p)]),
     "fclgpu_broadphase_update": (C.c_int, [_VP, _VP, C.c_int32, _VP]),

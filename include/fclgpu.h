@@ -360,6 +360,12 @@ FCLGPU_API int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const i
                                          void* stream);
 FCLGPU_API int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
                                   const double* tf1, const double* tf2, fclgpu_shape_result* res, void* stream);
+/* fcl::collide on convex shape pairs with enable_contact = false (GJKSolver_indep):
+ * hit[i] = 1 when FCL's ShapeCollisionTraversalNode::leafTesting adds
+ * Contact(o1, o2, NONE, NONE) (shape_collision_traversal_node-inl.h:70-136); no contact
+ * geometry, no EPA.  Host arrays. */
+FCLGPU_API int fclgpu_shape_collide_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
+                                          const double* tf1, const double* tf2, int32_t* hit, void* stream);
 /* Device time (ms) of the most recent shape-pair kernel.  No counterpart in FCL. */
 FCLGPU_API int fclgpu_last_shape_kernel_time(double* ms);
 
