@@ -257,6 +257,7 @@ class CollisionRequest:
     enable_statistics: bool = False
     precision: str = "fp32"
     gjk_solver_type: int = GST_LIBCCD
+    gjk_tolerance: float = 1e-6  # CollisionRequest::gjk_tolerance (collision_request.h:94)
 
 
 @dataclass
@@ -305,6 +306,7 @@ class DistanceRequest:
     enable_statistics: bool = False
     precision: str = "fp32"
     gjk_solver_type: int = GST_LIBCCD
+    distance_tolerance: float = 1e-6  # DistanceRequest::distance_tolerance (distance_request.h:99)
 
 
 @dataclass
@@ -329,6 +331,39 @@ def _unsupported(req):
     # BVHModel distance traversal never reports (triangle and RSS distances are >= 0).
     if getattr(req, "rel_err", 0.0) or getattr(req, "abs_err", 0.0):
         raise N.FclGpuError(-9, "distance", "rel_err/abs_err must be 0 on the GPU path")
+
+
+SOLVER_DEFAULTS = (2.0097183471152322e-14, 2.0097183471152322e-14, 128, 255)
+
+
+def set_gjk_solver_params(gjk_tolerance=SOLVER_DEFAULTS[0], epa_tolerance=SOLVER_DEFAULTS[1],
+                          gjk_max_iterations=SOLVER_DEFAULTS[2], epa_max_iterations=SOLVER_DEFAULTS[3]):
+    """GJKSolver_indep's parameters for every later shape, mesh-shape and broadphase
+    call (process-wide; fclgpu_set_gjk_solver_params).  Defaults: the solver's own."""
+    p = N.GjkSolverParams(gjk_tolerance, epa_tolerance, gjk_max_iterations, epa_max_iterations)
+    N.check(N.lib().fclgpu_set_gjk_solver_params(C.byref(p)), "fclgpu_set_gjk_solver_params")
+
+
+def get_gjk_solver_params():
+    p = N.GjkSolverParams()
+    N.check(N.lib().fclgpu_get_gjk_solver_params(C.byref(p)), "fclgpu_get_gjk_solver_params")
+    return (p.gjk_tolerance, p.epa_tolerance, p.gjk_max_iterations, p.epa_max_iterations)
+
+
+class _RequestSolver:
+    """The solver fcl::collide / fcl::distance build for one call: the request's
+    tolerance (collision-inl.h:164-170, distance-inl.h:211-215), default iteration caps;
+    the previous process-wide parameters come back afterwards."""
+
+    def __init__(self, gjk_tol, epa_tol):
+        self.want = (gjk_tol, epa_tol, SOLVER_DEFAULTS[2], SOLVER_DEFAULTS[3])
+
+    def __enter__(self):
+        self.prev = get_gjk_solver_params()
+        set_gjk_solver_params(*self.want)
+
+    def __exit__(self, *exc):
+        set_gjk_solver_params(*self.prev)
 
 
 def _shape_solver(request, where):
@@ -417,7 +452,9 @@ def collide(o1: CollisionObject, o2: CollisionObject, request: CollisionRequest,
     if request.num_max_contacts == 0:
         return 0
     if isinstance(o1.geometry, ShapeRef) or isinstance(o2.geometry, ShapeRef):
-        return _collide_shapes(o1, o2, request, result)
+        _shape_solver(request, "collide")
+        with _RequestSolver(request.gjk_tolerance, request.gjk_tolerance):
+            return _collide_shapes(o1, o2, request, result)
     if request.enable_contact:
         if request.enable_statistics:
             raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "collide", "statistics are not produced with contacts")
@@ -447,7 +484,9 @@ def distance(o1: CollisionObject, o2: CollisionObject, request: DistanceRequest,
     mesh x shape pairs (ShapeRef geometries; GJKSolver_indep)."""
     _unsupported(request)
     if isinstance(o1.geometry, ShapeRef) or isinstance(o2.geometry, ShapeRef):
-        return _distance_shapes(o1, o2, request, result)
+        _shape_solver(request, "distance")
+        with _RequestSolver(request.distance_tolerance, SOLVER_DEFAULTS[1]):
+            return _distance_shapes(o1, o2, request, result)
     out = distance_batch([o1.geometry, o2.geometry], np.array([[0, 1]], np.int32), o1.tf[None], o2.tf[None],
                          nearest_points=request.enable_nearest_points, precision=request.precision)
     d = float(out["min_distance"][0])

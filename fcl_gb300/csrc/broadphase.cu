@@ -968,6 +968,8 @@ cudaError_t launch_bp_classify(const BpSceneView& S, const BpQueryView& Q, const
 cudaError_t launch_bp_shape_narrow(const BpSceneView& S, const BpQueryView& Q, const int2* pairs, int64_t n,
                                    const int32_t* kind, int mode, int32_t* hit, double* dist, double* pts,
                                    cudaStream_t s) {
+  const cudaError_t ep = upload_solver_params(s);
+  if (ep != cudaSuccess) return ep;
   if (n <= 0) return cudaSuccess;
   k_bp_shape_narrow<<<grid_for(n, 128), 128, 0, s>>>(S, Q, pairs, n, kind, mode, hit, dist, pts);
   ++g_kernel_launches;

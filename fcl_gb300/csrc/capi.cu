@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -149,6 +150,9 @@ SplitScratch g_split;
 int64_t g_default_budget = 1024;
 int32_t g_wb_steps = 4;
 int32_t g_wb_variant = 1;
+// testing aids (fclgpu_set_collide_test_limits): initial scratch capacities, stack limit
+int64_t g_test_records = 0, g_test_items = 0;
+int32_t g_test_stack = 0;
 
 int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
                  const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
@@ -160,11 +164,15 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
   const int64_t budget = req->budget > 0 ? req->budget : g_default_budget;
   int64_t rec_cap = std::max<int64_t>(S.record_hint, std::min<int64_t>(n * std::max<int64_t>(maxc, 1), 4 * n) + 65536);
   int64_t item_cap = std::max<int64_t>(P.item_hint, 4 * n + (1 << 20));
+  if (g_test_records > 0) rec_cap = g_test_records;
+  if (g_test_items > 0) item_cap = std::max<int64_t>(g_test_items, n);
   for (int attempt = 0; attempt < 8; ++attempt) {
     CK(S.records.ensure(sizeof(int4) * (size_t)rec_cap), "record scratch");
-    rec_cap = (int64_t)(S.records.cap / sizeof(int4));
+    // the buffers only grow; a test limit still caps the part a batch may use
+    rec_cap = std::min<int64_t>((int64_t)(S.records.cap / sizeof(int4)),
+                                g_test_records > 0 ? rec_cap : INT64_MAX);
     CK(P.items.ensure(sizeof(int4) * (size_t)item_cap), "item scratch");
-    item_cap = (int64_t)(P.items.cap / sizeof(int4));
+    item_cap = std::min<int64_t>((int64_t)(P.items.cap / sizeof(int4)), g_test_items > 0 ? item_cap : INT64_MAX);
     CK(P.own.ensure(4 * (size_t)item_cap), "item scratch");
     CK(P.cstart.ensure(4 * (size_t)item_cap), "item scratch");
     CK(P.ccount.ensure(4 * (size_t)item_cap), "item scratch");
@@ -198,6 +206,7 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
     L.budget = budget;
     L.wb_steps = g_wb_steps;
     L.wb_variant = g_wb_variant;
+    L.stack_limit = g_test_stack;
     L.own = (int32_t*)P.own.p;
     L.child_start = (int32_t*)P.cstart.p;
     L.child_count = (int32_t*)P.ccount.p;
@@ -420,6 +429,18 @@ int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps, int32_t 
   g_default_budget = budget;
   g_wb_steps = leaf_batch_steps;
   g_wb_variant = variant;
+  return FCLGPU_OK;
+}
+
+int fclgpu_set_collide_test_limits(int64_t initial_records, int64_t initial_items, int32_t stack_limit) {
+  if (initial_records < 0 || initial_items < 0 || stack_limit < 0)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "test limits must be >= 0");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  g_test_records = initial_records;
+  g_test_items = initial_items;
+  g_test_stack = stack_limit;
+  if (initial_records > 0) g_scratch.record_hint = 0;
+  if (initial_items > 0) g_split.item_hint = 0;
   return FCLGPU_OK;
 }
 

@@ -47,6 +47,16 @@ int cfail(cudaError_t e, const char* where) {
 
 }  // namespace
 
+namespace {
+std::mutex g_solver_mu;
+SolverParams g_solver = FCLG_SOLVER_DEFAULTS;
+}  // namespace
+
+SolverParams fclgpu::current_solver_params() {
+  std::lock_guard<std::mutex> lk(g_solver_mu);
+  return g_solver;
+}
+
 extern "C" {
 
 int fclgpu_shapeset_create(const fclgpu_shape* shapes, int32_t n, const double* verts, int64_t nv,
@@ -250,6 +260,26 @@ int fclgpu_shape_collide_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia
   CKS(launch_shape_collide_only(L, s), "shape collide");
   CKS(cudaMemcpyAsync(hit, g_hit.p, 4 * nn, cudaMemcpyDeviceToHost, s), "d2h");
   CKS(cudaStreamSynchronize(s), "shape collide");
+  return FCLGPU_OK;
+}
+
+int fclgpu_set_gjk_solver_params(const fclgpu_gjk_solver_params* p) {
+  SolverParams v = FCLG_SOLVER_DEFAULTS;
+  if (p) {
+    if (!(p->gjk_tolerance > 0.0) || !(p->epa_tolerance > 0.0) || !(p->gjk_tolerance < 1e300) ||
+        !(p->epa_tolerance < 1e300) || p->gjk_max_iterations < 1 || p->epa_max_iterations < 1)
+      return FCLGPU_ERR_INVALID_ARGUMENT;
+    v = SolverParams{p->gjk_tolerance, p->epa_tolerance, p->gjk_max_iterations, p->epa_max_iterations};
+  }
+  std::lock_guard<std::mutex> lk(g_solver_mu);
+  g_solver = v;
+  return FCLGPU_OK;
+}
+
+int fclgpu_get_gjk_solver_params(fclgpu_gjk_solver_params* p) {
+  if (!p) return FCLGPU_ERR_INVALID_ARGUMENT;
+  const SolverParams v = current_solver_params();
+  *p = fclgpu_gjk_solver_params{v.gjk_tolerance, v.epa_tolerance, v.gjk_max_iterations, v.epa_max_iterations};
   return FCLGPU_OK;
 }
 

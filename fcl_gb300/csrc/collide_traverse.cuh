@@ -180,7 +180,7 @@ FCLG_HD int collide_item(const CollideLaunch& L, long long qi, int sb1, int sb2,
           first_over_second = false;
         else
           first_over_second = size_key(A, b1) > size_key(B, b2);
-        if (sp >= STACK) {
+        if (sp >= STACK || (L.stack_limit > 0 && sp >= L.stack_limit)) {
           st.status |= DEV_ERR_STACK;
           break;
         }
@@ -282,7 +282,7 @@ FCLG_HD int collide_query(const CollideLaunch& L, long long qi, Sink& sink, Quer
           first_over_second = false;
         else
           first_over_second = size_key(A, b1) > size_key(B, b2);
-        if (sp >= STACK) {
+        if (sp >= STACK || (L.stack_limit > 0 && sp >= L.stack_limit)) {
           st.status |= DEV_ERR_STACK;
           break;
         }

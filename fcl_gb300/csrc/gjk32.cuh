@@ -17,8 +17,10 @@
 // + |tb|.  The pair is certified disjoint when the computed gap exceeds 64u ||D||_1 S:
 // the true gap along the unit direction then exceeds 24u S, every point of A lies beyond
 // every point of B, and FCL's GJK cannot end Inside (its simplex stays inside the
-// Minkowski difference; the gap is far above its rounding and its absolute tolerance
-// 2^-45.5).  Only pairs without a certificate run the FP64 solver.
+// Minkowski difference; the gap is far above its rounding).  GJK also ends Inside once
+// its ray is shorter than its absolute tolerance (2^-45.5 by default, 1e-6 through
+// fcl::collide), so the threshold adds 1.01 times that tolerance times ||D||_1.  Only
+// pairs without a certificate run the FP64 solver.
 #pragma once
 #include "gjk_epa.cuh"
 
@@ -326,7 +328,10 @@ FCLG_HD bool certify_separated32(const ShapeRef& A, const Pose32& a, const Shape
   const float hA = gdot(uA, support32(A, uA)), hB = gdot(uB, support32(B, uB));
   const G3f ta = g3f(a.t[0], a.t[1], a.t[2]), tb = g3f(b.t[0], b.t[1], b.t[2]);
   const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
-  return gap > 3.81469727e-06f * n1 * S;  // 64u ||D||_1 S
+  // 64u ||D||_1 S, plus the GJK tolerance: FCL's GJK ends Inside once its ray is
+  // shorter than gjk_tolerance, so a certified pair is also farther apart than that
+  const float tol = (float)solver_params().gjk_tolerance * 1.01f;
+  return gap > (3.81469727e-06f * S + tol) * n1;
 }
 
 // FP32 GJK, then the FP32 certificate: true when FCL's GJK on this pair cannot end

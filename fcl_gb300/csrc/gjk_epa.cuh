@@ -12,6 +12,40 @@
 
 namespace fclgpu {
 
+// GJKSolver_indep's parameters (narrowphase/detail/gjk_solver_indep.h; defaults
+// gjk_solver_indep-inl.h:1039-1049): GJK and EPA tolerances and iteration caps.  The
+// defaults are the solver's own; fcl::collide sets both tolerances to
+// CollisionRequest::gjk_tolerance and fcl::distance the GJK tolerance to
+// DistanceRequest::distance_tolerance (collision-inl.h:164-170, distance-inl.h:211-215).
+struct SolverParams {
+  double gjk_tolerance;
+  double epa_tolerance;
+  int32_t gjk_max_iterations;
+  int32_t epa_max_iterations;
+};
+constexpr double kSolverDefaultTol = 2.0097183471152322e-14;  // std::pow(eps, 7/8) (math/constants.h:164-167)
+#define FCLG_SOLVER_DEFAULTS {kSolverDefaultTol, kSolverDefaultTol, 128, 255}
+
+#if defined(__CUDACC__)
+// One copy per translation unit that launches solver kernels; each launch refreshes it
+// from the process-wide values (upload_solver_params).
+static __device__ SolverParams g_dev_solver_params = FCLG_SOLVER_DEFAULTS;
+// Host: the values set by fclgpu_set_gjk_solver_params.
+SolverParams current_solver_params();
+static inline cudaError_t upload_solver_params(cudaStream_t s) {
+  const SolverParams p = current_solver_params();
+  return cudaMemcpyToSymbolAsync(g_dev_solver_params, &p, sizeof(p), 0, cudaMemcpyHostToDevice, s);
+}
+#endif
+
+FCLG_HD SolverParams solver_params() {
+#if defined(__CUDA_ARCH__)
+  return g_dev_solver_params;
+#else
+  return SolverParams FCLG_SOLVER_DEFAULTS;  // host builds of the device code use the defaults
+#endif
+}
+
 enum : int { SHAPE_BOX = 0, SHAPE_SPHERE = 1, SHAPE_CAPSULE = 2, SHAPE_CYLINDER = 3, SHAPE_CONE = 4, SHAPE_CONVEX = 5,
              SHAPE_TRIANGLE = 6 /* TriangleP: 9 doubles at verts + 3 * voff (mesh-shape leaves) */ };
 

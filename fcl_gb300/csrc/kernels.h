@@ -49,6 +49,7 @@ struct CollideLaunch {
   int64_t budget;                // BV tests per item per round
   int32_t wb_steps;              // FP32 form: DFS steps a lane runs between warp leaf batches
   int32_t wb_variant;            // FP32 form: 0 = unbounded registers, 1 = 128 registers
+  int32_t stack_limit;           // > 0: traversal stack entries allowed, below STACK (testing)
   int32_t* own;                  // per item: contacts found by the item itself
   int32_t* child_start;          // per item: id of its first child item
   int32_t* child_count;          // per item: number of child items (0 = finished)

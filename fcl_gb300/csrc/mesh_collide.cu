@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLau
           entry = make_int3(lane, -(c1 + 1), -(c2 + 1));
         } else {
           const bool first_over_second = l2 ? true : (l1 ? false : size_key(A, b1) > size_key(B, b2));
-          if (sp >= STACK) {
+          if (sp >= STACK || (L.stack_limit > 0 && sp >= L.stack_limit)) {
             atomicOr(&L.ctr->status, DEV_ERR_STACK);
             have = false;
             draining = true;

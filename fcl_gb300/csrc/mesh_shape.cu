@@ -523,6 +523,8 @@ cudaError_t run_distance_split(const MeshShapeLaunch& L, int stack_entries, cuda
 
 cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
   if (L.n <= 0) return cudaSuccess;
+  const cudaError_t ep = upload_solver_params(s);
+  if (ep != cudaSuccess) return ep;
   std::lock_guard<std::mutex> lk(g_split_mu);
   return L.mode == 0 ? run_collide_rounds(L, stack_entries, s, g_split_ms)
                      : run_distance_split(L, stack_entries, s, g_split_ms);
@@ -530,6 +532,8 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
 
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {
   if (L.n <= 0) return cudaSuccess;
+  const cudaError_t ep = upload_solver_params(s);
+  if (ep != cudaSuccess) return ep;
   const long long want = (L.n + 127) / 128;
   const int grid = (int)std::min<long long>(std::max<long long>(want, 1), 152 * 32);
   if (stack_entries <= 64)

@@ -627,9 +627,10 @@ FCLG_HD bool shape_triangle_gjk64(const ShapeRef& A, const M3<double>& Rs, const
                                   const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
   GjkState g;
   make_minkowski(A, Rs, ts, triangle_ref(P), Rm, tm, g.shape);
+  const SolverParams sp = solver_params();
   g.V = V;
-  g.tolerance = kGjkTol;
-  return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), 128) == GJK_INSIDE;
+  g.tolerance = sp.gjk_tolerance;
+  return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), sp.gjk_max_iterations) == GJK_INSIDE;
 }
 
 // shapeTriangleDistance; ps on the shape, pt on the triangle, in FCL's frames

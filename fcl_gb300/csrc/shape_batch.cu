@@ -193,6 +193,8 @@ __global__ void __launch_bounds__(128) k_shape_collide_only(ShapeLaunch L) {
 }  // namespace
 
 cudaError_t launch_shape_collide_only(const ShapeLaunch& L, cudaStream_t s) {
+  const cudaError_t ep = upload_solver_params(s);
+  if (ep != cudaSuccess) return ep;
   k_shape_collide_only<<<grid_of((const void*)k_shape_collide_only, 128, L.n), 128, 0, s>>>(L);
   ++g_kernel_launches;
   return cudaGetLastError();
@@ -201,6 +203,7 @@ cudaError_t launch_shape_collide_only(const ShapeLaunch& L, cudaStream_t s) {
 cudaError_t launch_shape_batch(const ShapeLaunch& L, unsigned* bins, cudaStream_t s) {
   const int block = 128;
   cudaError_t e;
+  if ((e = upload_solver_params(s))) return e;
   if ((e = cudaMemsetAsync(bins, 0, sizeof(unsigned) * kKeys, s))) return e;
   if ((e = cudaMemsetAsync(L.epa_count, 0, sizeof(unsigned long long), s))) return e;
   k_shape_hist<<<grid_of((const void*)k_shape_hist, 256, L.n), 256, 0, s>>>(L, bins);

@@ -17,7 +17,7 @@
 
 namespace fclgpu {
 
-constexpr double kGjkTol = 2.0097183471152322e-14;  // std::pow(eps, 7/8) = 2^-45.5 (math/constants.h:164-167)
+constexpr double kGjkTol = kSolverDefaultTol;  // std::pow(eps, 7/8) = 2^-45.5 (math/constants.h:164-167)
 
 struct PairOut {
   int hit;
@@ -351,26 +351,29 @@ FCLG_HD void epa_contact(const GjkState& g, const EpaState& epa, const M3<double
 FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
                               const M3<double>& R2, const D3v& t2, SimplexVert* V, EpaState* epa, PairOut& o) {
   const D3v guess = v3(1.0, 0.0, 0.0);
+  const SolverParams sp = solver_params();
   o.estat = -1;
   o.hit = 0;
-  if (certified_disjoint(A, R1, t1, B, R2, t2)) {  // FCL's GJK ends Valid: no intersection
+  // FCL's GJK ends Valid on a certified pair: no intersection (with fewer iterations
+  // than the default it may end Failed instead, so the status needs the FP64 run)
+  if (sp.gjk_max_iterations >= 128 && certified_disjoint(A, R1, t1, B, R2, t2)) {
     o.gstat = GJK_VALID;
     return;
   }
   GjkState g;
   make_minkowski(A, R1, t1, B, R2, t2, g.shape);
   g.V = V;
-  g.tolerance = kGjkTol;
-  const int gs = g.evaluate(d3neg(guess), 128);
+  g.tolerance = sp.gjk_tolerance;
+  const int gs = g.evaluate(d3neg(guess), sp.gjk_max_iterations);
   o.gstat = gs;
   if (gs != GJK_INSIDE) return;
   if (!epa) {
     o.hit = 1;
     return;
   }
-  epa->tolerance = kGjkTol;
+  epa->tolerance = sp.epa_tolerance;
   epa->init();
-  const int es = epa->evaluate(g, d3neg(guess), 255);
+  const int es = epa->evaluate(g, d3neg(guess), sp.epa_max_iterations);
   epa_contact(g, *epa, R1, t1, es, o);
 }
 
@@ -379,10 +382,11 @@ FCLG_HD void gjk_intersect(const ShapeRef& A, const M3<double>& R1, const D3v& t
 FCLG_HD void gjk_distance_begin(const ShapeRef& A, const M3<double>& R1, const D3v& t1, const ShapeRef& B,
                                 const M3<double>& R2, const D3v& t2, SimplexVert* V, GjkState& g) {
   const D3v guess = v3(1.0, 0.0, 0.0);
+  const SolverParams sp = solver_params();
   make_minkowski(A, R1, t1, B, R2, t2, g.shape);
   g.V = V;
-  g.tolerance = kGjkTol;
-  g.begin(d3neg(guess), 128);
+  g.tolerance = sp.gjk_tolerance;
+  g.begin(d3neg(guess), sp.gjk_max_iterations);
 }
 FCLG_HD void gjk_distance_end(GjkState& g, const M3<double>& R1, const D3v& t1, PairOut& o) {
   const SimplexVert* V = g.V;

@@ -99,6 +99,11 @@ class BpSelfDistanceResult(C.Structure):
                 ("b2", C.c_int32), ("nearest_points", C.c_double * 6), ("total_candidates", C.c_int64)]
 
 
+class GjkSolverParams(C.Structure):
+    _fields_ = [("gjk_tolerance", C.c_double), ("epa_tolerance", C.c_double), ("gjk_max_iterations", C.c_int32),
+                ("epa_max_iterations", C.c_int32)]
+
+
 class BpDistanceRequest(C.Structure):
     _fields_ = [("enable_nearest_points", C.c_int32), ("precision", C.c_int32)]
 
@@ -193,6 +198,9 @@ _SIGS = {
     "fclgpu_shape_batch_device": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_shape_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_shape_collide_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "fclgpu_set_gjk_solver_params": (C.c_int, [C.POINTER(GjkSolverParams)]),
+    "fclgpu_set_collide_test_limits": (C.c_int, [C.c_int64, C.c_int64, C.c_int32]),
+    "fclgpu_get_gjk_solver_params": (C.c_int, [C.POINTER(GjkSolverParams)]),
     "fclgpu_last_shape_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
     "fclgpu_broadphase_create": (C.c_int, [_VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.POINTER(C.c_void_p)]),
     "fclgpu_broadphase_update": (C.c_int, [_VP, _VP, C.c_int32, _VP]),

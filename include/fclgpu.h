@@ -296,6 +296,13 @@ FCLGPU_API int fclgpu_distance_batch_noalloc(const fclgpu_mesh* meshes, int32_t 
                                              const fclgpu_distance_request* req,
                                              fclgpu_distance_result* res, void* stream);
 
+/* Testing aid: the record and work-item capacities the next mesh collide batches start
+ * from (0 = automatic; a batch that outgrows them doubles them and runs again), and a
+ * traversal stack limit below the compiled one (0 = none; a traversal that needs more
+ * reports FCLGPU_ERR_DEVICE_STATUS).  For exercising those two paths.  No counterpart
+ * in FCL. */
+FCLGPU_API int fclgpu_set_collide_test_limits(int64_t initial_records, int64_t initial_items, int32_t stack_limit);
+
 /* Number of this library's kernel launches issued since load (for launch accounting). */
 FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
 /* Device time (ms, CUDA events on the batch's stream) of the traversal kernel of the
@@ -360,6 +367,23 @@ FCLGPU_API int fclgpu_shape_batch_device(fclgpu_shapeset set, int64_t n, const i
                                          void* stream);
 FCLGPU_API int fclgpu_shape_batch(fclgpu_shapeset set, int64_t n, const int32_t* ia, const int32_t* ib,
                                   const double* tf1, const double* tf2, fclgpu_shape_result* res, void* stream);
+/* GJKSolver_indep's parameters (narrowphase/detail/gjk_solver_indep.h: gjk_tolerance,
+ * epa_tolerance, gjk_max_iterations, epa_max_iterations).  Process-wide: every later
+ * shape-pair, mesh-shape and broadphase call that runs GJK or EPA uses them.  The
+ * defaults are the solver's own (2^-45.5, 2^-45.5, 128, 255; gjk_solver_indep-inl.h:
+ * 1039-1049); FCL's fcl::collide sets both tolerances to CollisionRequest::gjk_tolerance
+ * and fcl::distance the GJK tolerance to DistanceRequest::distance_tolerance (both
+ * 1e-6 by default; collision-inl.h:164-170, distance-inl.h:211-215).  NULL restores the
+ * defaults.  Tolerances must be positive and finite, iteration caps at least 1. */
+typedef struct {
+  double gjk_tolerance;
+  double epa_tolerance;
+  int32_t gjk_max_iterations;
+  int32_t epa_max_iterations;
+} fclgpu_gjk_solver_params;
+FCLGPU_API int fclgpu_set_gjk_solver_params(const fclgpu_gjk_solver_params* params);
+FCLGPU_API int fclgpu_get_gjk_solver_params(fclgpu_gjk_solver_params* params);
+
 /* fcl::collide on convex shape pairs with enable_contact = false (GJKSolver_indep):
  * hit[i] = 1 when FCL's ShapeCollisionTraversalNode::leafTesting adds
  * Contact(o1, o2, NONE, NONE) (shape_collision_traversal_node-inl.h:70-136); no contact

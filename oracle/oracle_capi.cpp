@@ -611,6 +611,11 @@ int64_t orc_scene_collide_lists(void* h, int64_t nq, const int* qgid, const doub
   return total;
 }
 
+// GJKSolver_indep parameters for every later GJK / EPA of the oracle.
+void orc_set_gjk_solver_params(double gjk_tol, double epa_tol, int64_t gjk_iter, int64_t epa_iter) {
+  set_solver_params(gjk_tol, epa_tol, (size_t)gjk_iter, (size_t)epa_iter);
+}
+
 // Self-collision lists (bp_self_collide_lists): counts per o2 and (o1, b1, b2) triples.
 int64_t orc_scene_self_collide_lists(void* h, int64_t max_per_pair, int64_t* counts, int* trip, int64_t cap) {
   const OrcScene* S = static_cast<OrcScene*>(h);

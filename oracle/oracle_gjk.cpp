@@ -18,6 +18,15 @@ inline V3 normalized(const V3& v) {
 }
 const double kTol = 2.0097183471152322e-14;  // std::pow(eps, 7/8) = 2^-45.5 (math/constants.h:164-167)
 
+// GJKSolver_indep's parameters as the solver used by fcl::collide / fcl::distance holds
+// them (gjk_solver_indep-inl.h:1039-1049 defaults; collision-inl.h:164-170 and
+// distance-inl.h:211-215 set the tolerances from the request).
+struct SolverParamsO {
+  double gjk_tolerance = kTol, epa_tolerance = kTol;
+  size_t gjk_max_iterations = 128, epa_max_iterations = 255;
+};
+SolverParamsO g_solver_params;
+
 // narrowphase/detail/convexity_based_algorithm/minkowski_diff-inl.h:65-206
 V3 get_support(const Shape& s, const V3& dir) {
   switch (s.type) {
@@ -236,8 +245,8 @@ struct GJK {
   size_t current;
   Simplex* simplex;
   int status;
-  size_t max_iterations = 128;
-  double tolerance = kTol;
+  size_t max_iterations = g_solver_params.gjk_max_iterations;
+  double tolerance = g_solver_params.gjk_tolerance;
 
   void get_support(const V3& d, SimplexV& sv) const {
     sv.d = normalized(d);
@@ -427,8 +436,8 @@ struct SimplexHorizon {
 };
 
 struct EPA {
-  size_t max_face_num = 128, max_vertex_num = 64, max_iterations = 255;
-  double tolerance = kTol;
+  size_t max_face_num = 128, max_vertex_num = 64, max_iterations = g_solver_params.epa_max_iterations;
+  double tolerance = g_solver_params.epa_tolerance;
   int status;
   Simplex result;
   V3 normal;
@@ -1425,6 +1434,14 @@ void shape_pair(const Shape& s1, const Tf& tf1, const Shape& s2, const Tf& tf2, 
   r.gjk_status = r.epa_status = -1;
   r.collide = shape_intersect(s1, tf1, s2, tf2, r);
   if (!r.collide) shape_distance(s1, tf1, s2, tf2, r);
+}
+
+void set_solver_params(double gjk_tolerance, double epa_tolerance, size_t gjk_max_iterations,
+                       size_t epa_max_iterations) {
+  g_solver_params.gjk_tolerance = gjk_tolerance;
+  g_solver_params.epa_tolerance = epa_tolerance;
+  g_solver_params.gjk_max_iterations = gjk_max_iterations;
+  g_solver_params.epa_max_iterations = epa_max_iterations;
 }
 
 }  // namespace oracle

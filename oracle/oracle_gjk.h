@@ -58,4 +58,9 @@ ProjectResult project_line(const V3& a, const V3& b);
 ProjectResult project_triangle(const V3& a, const V3& b, const V3& c);
 ProjectResult project_tetra(const V3& a, const V3& b, const V3& c, const V3& d);
 
+// The GJKSolver_indep parameters every later GJK / EPA uses (process-wide; defaults
+// 2^-45.5, 2^-45.5, 128, 255 as gjk_solver_indep-inl.h:1039-1049).
+void set_solver_params(double gjk_tolerance, double epa_tolerance, size_t gjk_max_iterations,
+                       size_t epa_max_iterations);
+
 }  // namespace oracle

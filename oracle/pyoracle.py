@@ -294,6 +294,17 @@ def brute_distance(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None =
     return float(lib().orc_brute_distance(m1.h, m2.h, None if tf1a is None else _d(tf1a), _d(tf2)))
 
 
+SOLVER_DEFAULTS = (2.0097183471152322e-14, 2.0097183471152322e-14, 128, 255)
+
+
+def set_gjk_solver_params(gjk_tolerance=SOLVER_DEFAULTS[0], epa_tolerance=SOLVER_DEFAULTS[1],
+                          gjk_max_iterations=SOLVER_DEFAULTS[2], epa_max_iterations=SOLVER_DEFAULTS[3]):
+    """GJKSolver_indep parameters of every later oracle GJK / EPA (process-wide)."""
+    L = lib()
+    L.orc_set_gjk_solver_params.argtypes = [C.c_double, C.c_double, C.c_int64, C.c_int64]
+    L.orc_set_gjk_solver_params(gjk_tolerance, epa_tolerance, gjk_max_iterations, epa_max_iterations)
+
+
 def shape_batch(shapes, ia, ib, tf1, tf2, nthreads: int = 1):
     """GJKSolver_indep collide (+ EPA contact) and, for separated pairs, distance.
     Returns dict: hit, normal, point, depth, dist, p1, p2, status (n,2)."""

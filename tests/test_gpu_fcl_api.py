@@ -30,6 +30,8 @@ def test_shape_pairs_collide_and_distance(gpu_lib):
     req = api.CollisionRequest(gjk_solver_type=api.GST_INDEP)
     reqc = api.CollisionRequest(gjk_solver_type=api.GST_INDEP, enable_contact=True)
     dreq = api.DistanceRequest(enable_nearest_points=True, gjk_solver_type=api.GST_INDEP)
+    # fcl::collide / fcl::distance run the solver at the request's tolerance (1e-6)
+    P.set_gjk_solver_params(1e-6, 1e-6)
     ref = P.shape_batch(shapes, ia, ib, tfa, tfb, nthreads=8)
     hits = 0
     for k in range(300):
@@ -56,7 +58,9 @@ def test_shape_pairs_collide_and_distance(gpu_lib):
         else:
             assert d == ref["dist"][k]
             assert np.array_equal(dr.nearest_points, np.stack([ref["p1"][k], ref["p2"][k]]))
+    P.set_gjk_solver_params()
     assert 20 < hits < 280
+    assert api.get_gjk_solver_params() == api.SOLVER_DEFAULTS  # the mirror restores the parameters
 
 
 def test_mesh_shape_pairs_both_orders(gpu_lib):
@@ -71,9 +75,11 @@ def test_mesh_shape_pairs_both_orders(gpu_lib):
     sid = rng.integers(0, 32, size=n).astype(np.int32)
     tfm = W.random_poses(n, -0.3, 0.3, 66)
     tfs = W.random_poses(n, -1.3, 1.3, 67)
+    P.set_gjk_solver_params(1e-6, 1e-6)
     c, tris = P.mesh_shape_contacts(om, G, sid, tfm, tfs, max_contacts=4, nthreads=8)
     off = np.concatenate([[0], np.cumsum(c)])
     dist = P.mesh_shape_distance(om, G, sid, tfm, tfs, nthreads=8)
+    P.set_gjk_solver_params()
     req = api.CollisionRequest(num_max_contacts=4, gjk_solver_type=api.GST_INDEP)
     dreq = api.DistanceRequest(enable_nearest_points=True, gjk_solver_type=api.GST_INDEP)
     for k in range(n):
@@ -109,3 +115,34 @@ def test_gst_libccd_is_rejected_for_shape_pairs(gpu_lib):
     r = api.CollisionResult()
     api.collide(api.CollisionObject(m), api.CollisionObject(m), api.CollisionRequest(), r)
     assert r.numContacts() == 1
+
+
+@pytest.mark.parametrize("params", [(1e-6, 1e-6, 128, 255), (2.0097183471152322e-14, 2.0097183471152322e-14, 1, 255),
+                                    (2.0097183471152322e-14, 2.0097183471152322e-14, 128, 1),
+                                    (1e-3, 1e-3, 3, 2)])
+def test_solver_parameters_match_oracle(gpu_lib, params):
+    """GJKSolver_indep's tolerances and iteration caps: the request tolerance of
+    fcl::collide (1e-6), a GJK cap of 1 (status Failed, gjk-inl.h:188), an EPA cap of 1
+    (epa-inl.h:309-343) and coarse settings give the oracle's booleans, statuses, depths
+    and distances bit for bit."""
+    w3 = W.config3(n_pairs=6000, n_shapes=96, seed=71)
+    ss = api.ShapeSet.from_workload(w3.shapes)
+    try:
+        api.set_gjk_solver_params(*params)
+        P.set_gjk_solver_params(*params)
+        g = api.shape_batch(ss, w3.ia, w3.ib, w3.tf1, w3.tf2)
+        o = P.shape_batch(w3.shapes, w3.ia, w3.ib, w3.tf1, w3.tf2, nthreads=8)
+    finally:
+        api.set_gjk_solver_params()
+        P.set_gjk_solver_params()
+    for k in ("hit", "status", "depth", "normal", "point", "dist", "p1", "p2"):
+        assert np.array_equal(g[k], o[k]), k
+    if params[2] == 1:
+        assert (g["status"][:, 0] == 2).any()  # GJK Failed (gjk-inl.h:188)
+
+
+def test_solver_parameters_are_validated(gpu_lib):
+    for bad in ((0.0, 1e-6, 128, 255), (1e-6, -1.0, 128, 255), (1e-6, 1e-6, 0, 255), (1e-6, 1e-6, 128, 0)):
+        with pytest.raises(N.FclGpuError):
+            api.set_gjk_solver_params(*bad)
+    assert api.get_gjk_solver_params() == api.SOLVER_DEFAULTS

@@ -270,3 +270,33 @@ def test_distance_fp32_largest_c1_meshes(gpu_lib):
                                            nthreads=8)
         d[idx] = dd; pts[idx] = pp
     _dist_check(out, d, pts)
+
+
+def test_collide_capacity_retry_and_stack_limit(gpu_lib):
+    """Error paths of the collide batch, forced through the test limits: record and
+    work-item scratch far too small (the batch doubles them and runs again, with the
+    same result), and a traversal stack limit below the trees' depth (the device
+    reports it and the call returns FCLGPU_ERR_DEVICE_STATUS)."""
+    from fcl_gb300 import native as N
+    w = W.config1(scale=0.004, n_pairs=6, tri_hi=30000, seed=3)
+    ms = _meshes(w)
+
+    def run():
+        return api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                                 precision="fp32", statistics=True, budget=64)
+
+    ref = run()
+    assert ref["contacts"].shape[0] > 1000
+    try:
+        N.check(N.lib().fclgpu_set_collide_test_limits(16, w.n + 8, 0), "limits")
+        got = run()
+        for k in ("counts", "contacts", "num_bv_tests", "num_leaf_tests"):
+            assert np.array_equal(got[k], ref[k]), k
+        N.check(N.lib().fclgpu_set_collide_test_limits(0, 0, 6), "limits")
+        with pytest.raises(N.FclGpuError) as e:
+            run()
+        assert e.value.code == N.FCLGPU_ERR_DEVICE_STATUS and "stack" in str(e.value)
+    finally:
+        N.check(N.lib().fclgpu_set_collide_test_limits(0, 0, 0), "limits")
+    again = run()
+    assert np.array_equal(again["contacts"], ref["contacts"])

@@ -126,3 +126,26 @@ def test_destroy_releases_blocked_waiters(gpu_lib):
     assert not any(t.is_alive() for t in th)
     assert set(outcome) == set(ids)
     assert all(isinstance(v, dict) or v == N.FCLGPU_ERR_NOT_INITIALIZED for v in outcome.values())
+
+
+def test_memory_budget_limits_step_size_not_results(gpu_lib):
+    """Admission under a small free-memory budget: every step takes only the few
+    waypoints the budget allows, and each request still returns what it returns
+    without the budget."""
+    w = W.scene4(n_objects=1500, seed=12, box=10.0, n_shape_geoms=128, mesh_fraction=0.0, mesh_links=False)
+    ss = api.ShapeSet.from_workload(w.shapes)
+    mgr = api.DynamicAABBTreeCollisionManager(ss)
+    mgr.registerObjects(w.refs, w.tf)
+    reqs = W.motion_requests(w, 4, seed=13, k_lo=10, k_hi=30)
+    free = api.MotionServer(mgr, w.robot, max_waypoints_per_step=256)
+    want = [free.wait(free.submit(r.base, r.q)) for r in reqs]
+    free.close()
+    tight = api.MotionServer(mgr, w.robot, max_waypoints_per_step=256, memory_budget_bytes=100_000)
+    got = [tight.wait(tight.submit(r.base, r.q)) for r in reqs]
+    st = tight.stats()
+    tight.close()
+    assert 1 <= st["max_step_waypoints"] <= 4
+    for a, b in zip(want, got):
+        for k in ("first_colliding_waypoint", "min_clearance", "clearance_waypoint", "clearance_link",
+                  "clearance_object"):
+            assert a[k] == b[k], k
