@@ -32,10 +32,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "queries/s batched FP32+FP64-recheck vs plain GPU (exact hits); p50/p99 request ms"
-# ncu (dram__bytes_read.sum + dram__bytes_write.sum, gpu__time_duration.sum) over the 15
-# round launches of one timed step of the default workload
-C1_STEP_DRAM_BYTES = 80.19e9
-C1_STEP_DRAM_MS = 2493.9
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the collide round kernel
+# per C1 step, from ncu on two small cases of the same workload (5 % and 20 % of the
+# poses, the 128-register variant the autotuner picks): 83.36 GB at 55,143 queries and
+# 211.44 GB at 220,586.  Traffic grows less than in proportion to the queries (the poses
+# of one mesh pair share its tree in L2), so a full step is priced by the straight line
+# through the two points, a + b * queries.
+C1_TRAFFIC_A = 40.663e9
+C1_TRAFFIC_B = 774190.0  # bytes per query
+C1_TRAFFIC_VARIANT = 1
 UNIT = "queries/s"
 WORKLOAD = "c1_exhaustive_contacts_64pairs_500-200k_tris"
 
@@ -281,6 +286,8 @@ def run_secondary(args, meshes, stream, flush):
     dev = flush.device
     if args.only == "shapes":
         return {"shapes": _run_shapes(args, stream, flush)}
+    if args.only == "c0":
+        return {"c0": _run_c0(args, stream, flush)}
     if args.only == "refit":
         return {"refit": _run_refit(args, stream, flush)}
     if args.only == "contacts":
@@ -325,6 +332,7 @@ def run_secondary(args, meshes, stream, flush):
                                            "sample": f"{k} queries drawn uniformly from the {w2.n}-query workload"}
     if args.only == "distance":
         return out
+    out["c0"] = _run_c0(args, stream, flush)
     out["shapes"] = _run_shapes(args, stream, flush)
     out["refit"] = _run_refit(args, stream, flush)
     out["contacts"] = _run_contacts(args, meshes, stream, flush)
@@ -396,6 +404,57 @@ def _run_ccd(args, meshes, stream, flush):
         dt = time.perf_counter() - t_start
         out["cpu_baseline"] = {"value": k / dt, "unit": "motions/s", "cores": threads, "kind": "port",
                                "sample": f"{k} of the motions"}
+    return out
+
+
+def _run_c0(args, stream, flush):
+    """The reference's CPU-runnable configuration: the 5,120-triangle perturbed
+    ellipsoid pair (radii (1, 0.7, 0.5), B scaled 0.8), 10,000 Haar poses with
+    translations U[-2,2]^3; per pose collide (num_max_contacts = 1) and distance with
+    nearest points.  Both forms timed on the GPU; every query checked against the
+    oracle (collide bit for bit, distance within 1e-6 relative); CPU baseline = the
+    oracle on all host cores."""
+    import torch
+    from fcl_gb300 import api
+    from fcl_gb300 import workloads as W
+    w = W.config0(n_poses=10_000, seed=1)
+    ms = [api.BVHModel.from_arrays(*m) for m in w.meshes]
+    dev = flush.device
+    tf2 = torch.from_numpy(w.tf2).to(dev)
+
+    def col(prec):
+        return api.collide_batch(ms, w.pairs, None, tf2, num_max_contacts=1, precision=prec,
+                                 stream=stream.cuda_stream)
+
+    def dist(prec):
+        return api.distance_batch(ms, w.pairs, None, tf2, nearest_points=True, precision=prec,
+                                  stream=stream.cuda_stream)
+
+    out = {"workload": "c0_5120tri_pair_10k_poses", "queries": w.n, "unit": "queries/s"}
+    for name, fn in (("collide", col), ("distance", dist)):
+        for prec in ("fp32", "fp64"):
+            ms_ = _time_device(lambda: fn(prec), 5, 3, stream, flush)
+            out[f"{name}_{prec}_value"] = w.n / (ms_ / 1000.0)
+    c = col("fp32")
+    d = dist("fp32")
+    torch.cuda.synchronize()
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        threads = O.hardware_threads()
+        a, b = O.Mesh(*w.meshes[0]), O.Mesh(*w.meshes[1])
+        t0 = time.perf_counter()
+        oc, ocont, _, _ = O.collide_batch(a, b, w.tf2, num_max_contacts=1, nthreads=threads)
+        t1 = time.perf_counter()
+        od, _, opts, _, _ = O.distance_batch(a, b, w.tf2, nearest=True, nthreads=threads)
+        t2 = time.perf_counter()
+        gd = d["min_distance"].cpu().numpy()
+        rel = np.abs(gd - od) / np.maximum(np.abs(od), 1e-9)
+        out["oracle_collide_exact"] = bool(np.array_equal(c["counts"].cpu().numpy(), oc) and
+                                           np.array_equal(c["contacts"].cpu().numpy(), ocont))
+        out["oracle_distance_max_rel_err"] = float(rel.max())
+        out["cpu_baseline"] = {"collide_value": w.n / (t1 - t0), "distance_value": w.n / (t2 - t1),
+                               "unit": "queries/s", "cores": threads, "kind": "port",
+                               "sample": "all 10,000 queries"}
     return out
 
 
@@ -740,18 +799,15 @@ def run_gpu(args):
     achieved = alg_bytes / (k_ms / 1000.0) / 1e9
     # DRAM bytes (read + write) of the round kernels of one timed step of the default
     # workload, from one ncu capture of that step; other workloads have no capture
-    default_workload = args.scale == 1.0 and args.pairs == 64 and args.tri_hi == 200000
+    default_workload = args.pairs == 64 and args.tri_hi == 200000
+    variant = api.get_collide_tuning()[2]
+    traffic = C1_TRAFFIC_A + C1_TRAFFIC_B * n if (default_workload and variant == C1_TRAFFIC_VARIANT) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": C1_STEP_DRAM_BYTES if default_workload else None, "peak_kind": peak_kind,
+            "traffic": traffic, "peak_kind": peak_kind,
             "kernel": "k_collide_round_wb (FP32 + FP64 recheck), all rounds of one step",
             "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg_bytes,
-            "dram_gbs_measured": C1_STEP_DRAM_BYTES / (C1_STEP_DRAM_MS / 1000.0) / 1e9 if default_workload else None}
-    prof = os.path.join(ROOT, "profiles", "mesh_collide_c1_traffic.json")
-    if os.path.exists(prof):
-        try:
-            roof["traffic"] = float(json.load(open(prof))["dram_bytes_per_launch"])
-        except Exception:
-            pass
+            "traffic_source": "small-case ncu captures (5 % and 20 % of the poses), linear in the queries",
+            "dram_gbs_estimated": None if traffic is None else traffic / (k_ms / 1000.0) / 1e9}
 
     cpu = None
     oracle_checked = (0, None)
@@ -824,7 +880,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "distance", "shapes", "refit", "contacts", "ccd", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "c0", "distance", "shapes", "refit", "contacts", "ccd", "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
