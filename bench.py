@@ -227,8 +227,11 @@ def run_serving(args):
     SV.run_burst(srv, reqs[:16])  # warm-up
     burst = SV.run_burst(srv, reqs[16:272])
     rate = args.serve_rate if args.serve_rate > 0 else 0.5 * burst["requests_per_s"]
+    ph = (C.c_double * 16)()
+    api.N.lib().fclgpu_broadphase_last_phase_ms(ph)  # reset the phase clocks
     with ClockSampler(0) as cs:
         load = SV.run_poisson(srv, reqs[272:], rate, seed=6)
+    api.N.lib().fclgpu_broadphase_last_phase_ms(ph)
     st = srv.stats()
     srv.close()
     out = {
@@ -238,10 +241,16 @@ def run_serving(args):
         "capacity_requests_per_s": burst["requests_per_s"],
         "arrival_rate_per_s": rate, "requests": load["requests"],
         "throughput_requests_per_s": load["throughput_requests_per_s"],
+        "sustained_requests_per_s": load["sustained_requests_per_s"],
+        "latency_p50_first_half_ms": load["latency_first_half_p50_ms"],
+        "latency_p50_second_half_ms": load["latency_second_half_p50_ms"],
         "p50_ms": load["p50_ms"], "p99_ms": load["p99_ms"], "mean_ms": load["mean_ms"], "max_ms": load["max_ms"],
         "waypoints": int(sum(r.q.shape[0] for r in reqs[272:])),
         "engine": {k: st[k] for k in ("steps", "waypoints", "queries", "candidates", "busy_ms",
                                       "max_step_waypoints")},
+        # broadphase wall-clock phases over the Poisson run (fclgpu_broadphase_last_phase_ms):
+        # setup + candidates, shape pairs, mesh-shape pairs, mesh-mesh pairs, reduction
+        "phases_ms": {"collide": [round(x, 1) for x in ph[0:5]], "distance": [round(x, 1) for x in ph[8:13]]},
         "scene_setup_s": setup_s, "clocks": cs.summary(),
     }
     if not args.no_cpu:
@@ -884,7 +893,7 @@ def main():
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")
-    ap.add_argument("--serve-requests", type=int, default=1000, help="requests in the Poisson run")
+    ap.add_argument("--serve-requests", type=int, default=3000, help="requests in the Poisson run")
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrivals/s (0 = 0.5 x measured capacity)")
     ap.add_argument("--serve-step", type=int, default=4096, help="waypoints per loop step")
     ap.add_argument("--serve-cpu-sample", type=int, default=64, help="requests timed on the CPU baseline")

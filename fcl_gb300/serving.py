@@ -43,19 +43,32 @@ def run_poisson(server, requests, rate: float, seed: int = 0) -> dict:
 
     th = threading.Thread(target=submitter)
     th.start()
+    done_at = np.zeros(len(requests))
     for i in range(len(requests)):
         ready[i].wait()
         results[i] = server.wait(ids[i])
+        done_at[i] = time.perf_counter() - t0
     th.join()
     t_end = time.perf_counter()
     lat = np.array([r["latency_ms"] for r in results])
     queue = np.array([r["queue_ms"] for r in results])
+    # steady state: completions per second over the middle 60 % of the arrival window
+    # (the first 20 % fill the pipeline, the drain after the last arrival is excluded); a
+    # server that keeps up completes requests at the arrival rate there, and its latency
+    # does not grow with the arrival index
+    T = float(arrivals[-1])
+    lo_t, hi_t = 0.2 * T, 0.8 * T
+    done_in = int(np.count_nonzero((done_at >= lo_t) & (done_at < hi_t)))
+    half = len(requests) // 2
     return {
         "requests": len(requests),
         "arrival_rate_per_s": rate,
-        "offered_seconds": float(arrivals[-1]),
+        "offered_seconds": T,
         "seconds": t_end - t0,
         "throughput_requests_per_s": len(requests) / (t_end - t0),
+        "sustained_requests_per_s": done_in / (hi_t - lo_t) if hi_t > lo_t else float("nan"),
+        "latency_first_half_p50_ms": float(np.percentile(lat[:half], 50)) if half else float("nan"),
+        "latency_second_half_p50_ms": float(np.percentile(lat[half:], 50)) if half else float("nan"),
         "p50_ms": float(np.percentile(lat, 50)),
         "p99_ms": float(np.percentile(lat, 99)),
         "mean_ms": float(lat.mean()),
