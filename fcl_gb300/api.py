@@ -407,14 +407,17 @@ def _collide_shapes(o1, o2, request, result):
             result.contacts.append(Contact(g1, g2, Contact.NONE, Contact.NONE, out["point"][0].copy(),
                                            out["normal"][0].copy(), float(out["depth"][0])))
         return result.numContacts()
-    if request.enable_contact:
-        raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED_, "collide", "contact geometry of mesh-shape pairs")
     om, os_ = _mesh_first(o1, o2)
     gs = os_.geometry
     out = mesh_shape_contacts_batch([om.geometry], gs.shapes, np.zeros(1, np.int32), np.array([gs.index], np.int32),
-                                    om.tf[None], os_.tf[None], num_max_contacts=max(1, room))
-    for t in out["tris"][:room]:
-        result.contacts.append(Contact(om.geometry, gs, int(t), Contact.NONE))
+                                    om.tf[None], os_.tf[None], num_max_contacts=max(1, room),
+                                    enable_contact=request.enable_contact)
+    for k, t in enumerate(out["tris"][:room]):
+        if request.enable_contact:  # Contact(mesh, shape, tri, NONE, contactp, -normal, penetration)
+            result.contacts.append(Contact(om.geometry, gs, int(t), Contact.NONE, out["pos"][k].copy(),
+                                           out["normal"][k].copy(), float(out["penetration_depth"][k])))
+        else:
+            result.contacts.append(Contact(om.geometry, gs, int(t), Contact.NONE))
     return result.numContacts()
 
 
@@ -1222,11 +1225,12 @@ def mesh_shape_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_
 
 
 def mesh_shape_contacts_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_mesh, tf_shape,
-                              num_max_contacts: int = 1, stream=None):
+                              num_max_contacts: int = 1, enable_contact: bool = False, stream=None):
     """fcl::collide of BVHModel<OBBRSS> meshes against convex shapes with the contact
     list: per pair the triangles FCL records as Contact(mesh, shape, triangle, NONE), in
     the order its traversal adds them (at most num_max_contacts).  Returns counts,
-    offsets (n + 1) and tris.  Host numpy inputs."""
+    offsets (n + 1) and tris; with enable_contact also pos (total, 3), normal (total, 3)
+    and penetration_depth (total,), the geometry FCL's leaf records.  Host numpy inputs."""
     hs = _handles(meshes)
     mesh_idx = np.ascontiguousarray(mesh_idx, np.int32)
     shape_idx = np.ascontiguousarray(shape_idx, np.int32)
@@ -1239,6 +1243,9 @@ def mesh_shape_contacts_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_
     for _ in range(2):
         tris = np.zeros(cap, np.int32)
         res = N.MeshShapeContactsResult(counts.ctypes.data, offsets.ctypes.data, tris.ctypes.data, cap, 0)
+        if enable_contact:
+            pos, nrm, dep = np.zeros((cap, 3)), np.zeros((cap, 3)), np.zeros(cap)
+            res.pos, res.normal, res.penetration_depth = pos.ctypes.data, nrm.ctypes.data, dep.ctypes.data
         rc = N.lib().fclgpu_mesh_shape_contacts(hs, len(meshes), shapes.handle, n, mesh_idx.ctypes.data,
                                                 shape_idx.ctypes.data, tf_mesh.ctypes.data, tf_shape.ctypes.data,
                                                 int(num_max_contacts), C.byref(res), stream)
@@ -1246,7 +1253,11 @@ def mesh_shape_contacts_batch(meshes, shapes: ShapeSet, mesh_idx, shape_idx, tf_
             cap = int(res.total_contacts)
             continue
         N.check(rc, "fclgpu_mesh_shape_contacts")
-        return {"counts": counts, "offsets": offsets, "tris": tris[: int(res.total_contacts)]}
+        t = int(res.total_contacts)
+        out = {"counts": counts, "offsets": offsets, "tris": tris[:t]}
+        if enable_contact:
+            out.update(pos=pos[:t], normal=nrm[:t], penetration_depth=dep[:t])
+        return out
     raise N.FclGpuError(N.FCLGPU_ERR_CAPACITY, "fclgpu_mesh_shape_contacts", "contact total changed between calls")
 
 

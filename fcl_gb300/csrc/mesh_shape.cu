@@ -364,6 +364,39 @@ __global__ void k_msr_scatter(const int4* rec, const unsigned long long* nrec, c
   }
 }
 
+// contact geometry of every record (enable_contact), written beside its triangle; one
+// thread per contact, each running the shape-triangle intersection with EPA in FP64
+__global__ void __launch_bounds__(128) k_msr_geometry(MeshShapeLaunch L, const int4* rec,
+                                                      const unsigned long long* nrec) {
+  const long long n = (long long)*nrec;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int4 r = rec[t];
+    PairGeom g;
+    pair_geom(L, r.x, g);
+    double P[9];
+    load_tri_local(g.m, r.z, P);
+    SimplexVert V[kSimplexSlots];
+    EpaState epa;
+    D3v pos, nrm;
+    double depth = 0;
+    if (!shape_triangle_contact(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, &epa, pos, nrm, depth)) {
+      // the record came from the same tests, so this does not happen; keep it visible
+      const double q = __longlong_as_double(0x7ff8000000000000ll);
+      pos = nrm = v3(q, q, q);
+      depth = q;
+    }
+    const long long o = L.list_offsets[r.x] + r.y;
+    L.list_pos[3 * o] = pos.x;
+    L.list_pos[3 * o + 1] = pos.y;
+    L.list_pos[3 * o + 2] = pos.z;
+    L.list_normal[3 * o] = nrm.x;
+    L.list_normal[3 * o + 1] = nrm.y;
+    L.list_normal[3 * o + 2] = nrm.z;
+    L.list_depth[o] = depth;
+  }
+}
+
 int grid128(long long n) { return (int)std::min<long long>(std::max<long long>((n + 127) / 128, 1), 152 * 32); }
 
 }  // namespace
@@ -472,6 +505,10 @@ cudaError_t run_collide_rounds(const MeshShapeLaunch& L, int stack_entries, cuda
     if (total <= L.list_cap && nrec_host > 0) {
       k_msr_scatter<<<grid128((long long)nrec_host), 128, 0, s>>>(Lr.rec, Lr.nrec, L.list_offsets, L.list_tris);
       ++g_kernel_launches;
+      if (L.list_pos) {
+        k_msr_geometry<<<grid128((long long)nrec_host), 128, 0, s>>>(Lr, Lr.rec, Lr.nrec);
+        ++g_kernel_launches;
+      }
     }
   }
   return cudaGetLastError();
@@ -705,6 +742,9 @@ int fclgpu_mesh_shape_contacts_device(const fclgpu_mesh* meshes, int32_t num_mes
   if (!res->offsets || (n > 0 && (!mesh_idx || !shape_idx || !tf_mesh || !tf_shape || !res->counts)) ||
       (res->capacity > 0 && !res->tris) || res->capacity < 0)
     return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing mesh-shape input or output");
+  const int ngeo = (res->pos ? 1 : 0) + (res->normal ? 1 : 0) + (res->penetration_depth ? 1 : 0);
+  if (ngeo != 0 && ngeo != 3)
+    return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "pos, normal and penetration_depth go together");
   std::vector<DevMesh> table(num_meshes);
   int depth = 0;
   for (int32_t i = 0; i < num_meshes; ++i) {
@@ -749,6 +789,11 @@ int fclgpu_mesh_shape_contacts_device(const fclgpu_mesh* meshes, int32_t num_mes
   L.list_offsets = res->offsets;
   L.list_tris = res->tris;
   L.list_cap = res->capacity;
+  if (ngeo == 3 && res->capacity > 0) {
+    L.list_pos = res->pos;
+    L.list_normal = res->normal;
+    L.list_depth = res->penetration_depth;
+  }
   int64_t total = 0;
   L.list_total = &total;
   e = run_mesh_shape_split(L, depth + 2, s);
@@ -769,17 +814,24 @@ int fclgpu_mesh_shape_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, fc
   if (!res || n < 0 || res->capacity < 0 || !res->offsets || (n > 0 && !res->counts) ||
       (res->capacity > 0 && !res->tris))
     return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing mesh-shape argument");
+  const int ngeo = (res->pos ? 1 : 0) + (res->normal ? 1 : 0) + (res->penetration_depth ? 1 : 0);
+  if (ngeo != 0 && ngeo != 3)
+    return ms_fail(FCLGPU_ERR_INVALID_ARGUMENT, "pos, normal and penetration_depth go together");
+  const bool geo = ngeo == 3;
   cudaStream_t s = (cudaStream_t)stream;
-  const size_t nn = (size_t)n;
-  // inputs, counts, offsets and a device list as large as the caller's
-  const size_t bytes = nn * (4 + 4 + 96 + 96 + 4) + 8 * (nn + 2) + 4 * (size_t)res->capacity + 64;
+  const size_t nn = (size_t)n, cap = (size_t)res->capacity;
+  // inputs, counts, offsets, the contact geometry and a device list as large as the caller's
+  const size_t bytes = nn * (4 + 4 + 96 + 96 + 4) + 8 * (nn + 2) + (geo ? 56 * cap : 0) + 4 * cap + 64;
   char* d = nullptr;
   cudaError_t e = cudaMalloc(&d, bytes);
   if (e != cudaSuccess) return ms_cuda(e, "staging");
   double* dtm = (double*)d;
   double* dts = dtm + 12 * nn;
   int64_t* doff = (int64_t*)(dts + 12 * nn);
-  int32_t* dm = (int32_t*)(doff + nn + 2);
+  double* dpos = (double*)(doff + nn + 2);
+  double* dnrm = dpos + (geo ? 3 * cap : 0);
+  double* ddep = dnrm + (geo ? 3 * cap : 0);
+  int32_t* dm = (int32_t*)(ddep + (geo ? cap : 0));
   int32_t* ds = dm + nn;
   int32_t* dc = ds + nn;
   int32_t* dt = dc + nn;
@@ -793,7 +845,8 @@ int fclgpu_mesh_shape_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, fc
   if (e != cudaSuccess) {
     rc = ms_cuda(e, "h2d");
   } else {
-    fclgpu_mesh_shape_contacts_result dr = {dc, doff, dt, res->capacity, 0};
+    fclgpu_mesh_shape_contacts_result dr = {dc,  doff, dt, res->capacity, 0, geo ? dpos : nullptr,
+                                             geo ? dnrm : nullptr, geo ? ddep : nullptr};
     rc = fclgpu_mesh_shape_contacts_device(meshes, num_meshes, shapes, n, dm, ds, dtm, dts, num_max_contacts, &dr,
                                            stream);
     res->total_contacts = dr.total_contacts;
@@ -802,6 +855,12 @@ int fclgpu_mesh_shape_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, fc
       if (e == cudaSuccess) e = cudaMemcpyAsync(res->offsets, doff, 8 * (nn + 1), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess && rc == FCLGPU_OK && dr.total_contacts > 0)
         e = cudaMemcpyAsync(res->tris, dt, 4 * (size_t)dr.total_contacts, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && geo && rc == FCLGPU_OK && dr.total_contacts > 0) {
+        const size_t tc = (size_t)dr.total_contacts;
+        e = cudaMemcpyAsync(res->pos, dpos, 24 * tc, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res->normal, dnrm, 24 * tc, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res->penetration_depth, ddep, 8 * tc, cudaMemcpyDeviceToHost, s);
+      }
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) rc = ms_cuda(e, "d2h");
     }

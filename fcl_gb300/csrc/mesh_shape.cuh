@@ -465,8 +465,11 @@ FCLG_HD bool project_in_triangle(const D3v& p1, const D3v& p2, const D3v& p3, co
   return (r1 > 0 && r2 > 0 && r3 > 0) || (r1 <= 0 && r2 <= 0 && r3 <= 0);
 }
 
+// sphereTriangleIntersect (sphere_triangle-inl.h:139-220); with the optional outputs the
+// contact point, normal_ and penetration_depth it reports
 FCLG_HD bool sphere_triangle_intersect(double radius, const D3v& center, const D3v& P1, const D3v& P2,
-                                       const D3v& P3) {
+                                       const D3v& P3, D3v* contact_point = nullptr, D3v* normal_out = nullptr,
+                                       double* depth = nullptr) {
   D3v normal = normalized3(cross(P2 - P1, P3 - P1));
   const double rwt = radius + DBL_EPSILON;
   double dfp = dot(center - P1, normal);
@@ -497,8 +500,19 @@ FCLG_HD bool sphere_triangle_intersect(double radius, const D3v& center, const D
       }
     }
   }
-  if (has_contact) return sqnorm(contact - center) < rwt * rwt;
-  return false;
+  if (!has_contact) return false;
+  const D3v c2c = contact - center;
+  const double dsq = sqnorm(c2c);
+  if (!(dsq < rwt * rwt)) return false;
+  if (contact_point) *contact_point = contact;
+  if (dsq > 0) {
+    if (normal_out) *normal_out = normalized3(c2c);
+    if (depth) *depth = -(radius - sqrt(dsq));
+  } else {
+    if (normal_out) *normal_out = d3scale(normal, -1.0);
+    if (depth) *depth = -radius;
+  }
+  return true;
 }
 
 struct ProjResult {
@@ -623,6 +637,32 @@ FCLG_HD int shape_triangle_stage1(const ShapeRef& A, const M3<double>& Rs, const
   }
   return certified_disjoint(A, Rs, ts, triangle_ref(P), Rm, tm) ? 0 : 1;
 }
+// The contact MeshShapeCollisionTraversalNodeOBBRSS::leafTesting records with
+// enable_contact (mesh_shape_collision_traversal_node-inl.h:233-244): shapeTriangleIntersect
+// with its outputs, stored as Contact(..., contactp, -normal, penetration).  Sphere: the
+// closed form's point and depth, its normal negated; the other shapes: the shape-pair
+// EPA contact (ShapeTransformedTriangleIntersectIndepImpl, gjk_solver_indep-inl.h:449-505,
+// reports -epa.normal, so the recorded normal is epa.normal).  pos/normal in the world frame.
+FCLG_HD bool shape_triangle_contact(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
+                                    const M3<double>& Rm, const D3v& tm, SimplexVert* V, EpaState* epa, D3v& pos,
+                                    D3v& normal, double& depth) {
+  if (A.s.type == SHAPE_SPHERE) {
+    const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
+    D3v n;
+    if (!sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm, &pos, &n,
+                                   &depth))
+      return false;
+    normal = d3scale(n, -1.0);
+    return true;
+  }
+  PairOut o;
+  gjk_intersect(A, Rs, ts, triangle_ref(P), Rm, tm, V, epa, o);
+  pos = o.point;
+  normal = o.normal;
+  depth = o.depth;
+  return o.hit != 0;
+}
+
 FCLG_HD bool shape_triangle_gjk64(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
                                   const M3<double>& Rm, const D3v& tm, SimplexVert* V) {
   GjkState g;

@@ -44,6 +44,10 @@ struct MeshShapeLaunch {
   int32_t* list_tris = nullptr;
   int64_t list_cap = 0;
   int64_t* list_total = nullptr;
+  // optional contact geometry of the listed contacts (device, 3 / 3 / 1 doubles each)
+  double* list_pos = nullptr;
+  double* list_normal = nullptr;
+  double* list_depth = nullptr;
   // record scratch of the list (set inside the split form)
   int4* rec = nullptr;
   unsigned long long* nrec = nullptr;

@@ -141,7 +141,8 @@ class MeshShapeRequest(C.Structure):
 
 class MeshShapeContactsResult(C.Structure):
     _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("tris", C.c_void_p), ("capacity", C.c_int64),
-                ("total_contacts", C.c_int64)]
+                ("total_contacts", C.c_int64), ("pos", C.c_void_p), ("normal", C.c_void_p),
+                ("penetration_depth", C.c_void_p)]
 
 
 class MeshShapeResult(C.Structure):

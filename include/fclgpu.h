@@ -443,13 +443,23 @@ FCLGPU_API int fclgpu_mesh_shape_batch(const fclgpu_mesh* meshes, int32_t num_me
  * traversal adds them, at most num_max_contacts per pair.  Pair i's triangles are
  * tris[offsets[i] .. offsets[i+1]); counts[i] = offsets[i+1] - offsets[i].
  * total_contacts is set on return; when it exceeds capacity the call returns
- * FCLGPU_ERR_CAPACITY and tris is left untouched (counts and offsets are filled). */
+ * FCLGPU_ERR_CAPACITY and tris is left untouched (counts and offsets are filled).
+ * With pos, normal and penetration_depth set (all three or none: CollisionRequest::
+ * enable_contact) contact k also gets the geometry the leaf records,
+ * Contact(mesh, shape, tri, NONE, contactp, -normal, penetration)
+ * (mesh_shape_collision_traversal_node-inl.h:233-244): pos[3k..3k+2], normal[3k..3k+2]
+ * (world frame) and penetration_depth[k], as shapeTriangleIntersect computes them
+ * (sphere: sphereTriangleIntersect, sphere_triangle-inl.h:139-220; other shapes: GJK then
+ * EPA, gjk_solver_indep-inl.h:449-505).  The triangle list is the same either way. */
 typedef struct {
   int32_t* counts;
   int64_t* offsets;  /* n + 1 entries */
   int32_t* tris;
   int64_t capacity;  /* entries tris can hold */
   int64_t total_contacts;
+  double* pos;               /* optional: 3 x capacity */
+  double* normal;            /* optional: 3 x capacity */
+  double* penetration_depth; /* optional: capacity */
 } fclgpu_mesh_shape_contacts_result;
 
 FCLGPU_API int fclgpu_mesh_shape_contacts_device(const fclgpu_mesh* meshes, int32_t num_meshes,

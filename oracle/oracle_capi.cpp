@@ -732,6 +732,30 @@ int64_t orc_mesh_shape_contacts(void* h, void* g, int64_t n, const int* sid, con
   return total;
 }
 
+// Contact geometry of listed mesh-shape contacts: for contact k (pair sid[k], poses
+// tfm/tfs of that contact, mesh triangle tri[k]) the position, normal and depth FCL's
+// leaf records with enable_contact; ok[k] = 0 when the pair does not intersect.
+void orc_mesh_shape_contact_geometry(void* h, void* g, int64_t n, const int* sid, const double* tfm,
+                                     const double* tfs, const int* tri, double* pos, double* nrm, double* depth,
+                                     int* ok) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  const OrcGeoms* G = static_cast<OrcGeoms*>(g);
+  for (int64_t k = 0; k < n; ++k) {
+    const Tri& t = m->tris[tri[k]];
+    V3 p, nv;
+    double d = 0;
+    ok[k] = shape_triangle_contact(G->g[sid[k]].shape, load_tf(tfs + 12 * k), m->verts[t.v[0]], m->verts[t.v[1]],
+                                   m->verts[t.v[2]], load_tf(tfm + 12 * k), p, nv, d)
+                ? 1
+                : 0;
+    for (int c = 0; c < 3; ++c) {
+      pos[3 * k + c] = p[c];
+      nrm[3 * k + c] = nv[c];
+    }
+    depth[k] = d;
+  }
+}
+
 // Brute force over every triangle of the mesh (for the traversal tests): collide ->
 // number of intersecting triangles; distance -> min over triangles.
 void orc_mesh_shape_brute(void* h, void* g, int sid, const double* tfm, const double* tfs, int64_t* count,

@@ -130,7 +130,8 @@ void shape_obbrss(const Shape& s, const Tf& tf, OBB& obb, RSS& rss) {
   fit_points_obbrss(ps.data(), (int)ps.size(), obb, rss);
 }
 
-bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3) {
+bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3,
+                               V3* contact_point, V3* normal_out, double* depth) {
   V3 normal = normalized(cross(sub(P2, P1), sub(P3, P1)));
   const double rwt = radius + std::numeric_limits<double>::epsilon();
   const V3 p1_to_center = sub(center, P1);
@@ -166,9 +167,42 @@ bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, co
   }
   if (has_contact) {
     const V3 c2c = sub(contact, center);
-    if (sqnorm(c2c) < rwt * rwt) return true;
+    const double dsq = sqnorm(c2c);
+    if (dsq < rwt * rwt) {
+      if (dsq > 0) {
+        const double d = std::sqrt(dsq);
+        if (normal_out) *normal_out = normalized(c2c);
+        if (contact_point) *contact_point = contact;
+        if (depth) *depth = -(radius - d);
+      } else {
+        if (normal_out) *normal_out = scale(normal, -1);
+        if (contact_point) *contact_point = contact;
+        if (depth) *depth = -radius;
+      }
+      return true;
+    }
   }
   return false;
+}
+
+bool shape_triangle_contact(const Shape& s, const Tf& tfs, const V3& P1, const V3& P2, const V3& P3, const Tf& tfm,
+                            V3& pos, V3& normal, double& depth) {
+  if (s.type == SH_SPHERE) {
+    V3 n;
+    if (!sphere_triangle_intersect(s.p[0], tfs.t, apply(tfm, P1), apply(tfm, P2), apply(tfm, P3), &pos, &n, &depth))
+      return false;
+    normal = scale(n, -1);  // the leaf records -normal (mesh_shape_collision_traversal_node-inl.h:97-102)
+    return true;
+  }
+  const V3 tv[3] = {P1, P2, P3};
+  Shape tri;
+  tri.type = SH_TRIANGLE;
+  tri.verts = tv;
+  tri.nverts = 3;
+  int gs, es;
+  // EPA's contact: normal epa.normal (the leaf's -(-epa.normal)), point
+  // tf1 (w0 - epa.normal epa.depth / 2), depth -epa.depth (gjk_solver_indep-inl.h:488-497)
+  return gjk_intersect(s, tfs, tri, tfm, &normal, &pos, &depth, &gs, &es);
 }
 
 ProjectResult project_line_p(const V3& a, const V3& b, const V3& p) {
@@ -233,7 +267,8 @@ ProjectResult project_triangle_p(const V3& a, const V3& b, const V3& c, const V3
 bool shape_triangle_intersect(const Shape& s, const Tf& tfs, const V3& P1, const V3& P2, const V3& P3,
                               const Tf& tfm) {
   if (s.type == SH_SPHERE)  // ShapeTransformedTriangleIntersectIndepImpl<Sphere> (:527-547)
-    return sphere_triangle_intersect(s.p[0], tfs.t, apply(tfm, P1), apply(tfm, P2), apply(tfm, P3));
+    return sphere_triangle_intersect(s.p[0], tfs.t, apply(tfm, P1), apply(tfm, P2), apply(tfm, P3), nullptr, nullptr,
+                                     nullptr);
   const V3 tv[3] = {P1, P2, P3};
   Shape tri;
   tri.type = SH_TRIANGLE;

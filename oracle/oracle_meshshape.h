@@ -21,7 +21,18 @@ void shape_obbrss(const Shape& s, const Tf& tf, OBB& obb, RSS& rss);
 
 // detail::sphereTriangleIntersect (primitive_shape_algorithm/sphere_triangle-inl.h),
 // triangle already in the world frame.
-bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3);
+// With the optional outputs: contact point, normal and depth as the function reports
+// them (contact_points, normal_, penetration_depth).
+bool sphere_triangle_intersect(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3,
+                               V3* contact_point = nullptr, V3* normal_out = nullptr, double* depth = nullptr);
+
+// The contact MeshShapeCollisionTraversalNode::leafTesting adds with enable_contact
+// (mesh_shape_collision_traversal_node-inl.h:91-103): shapeTriangleIntersect with its
+// contact outputs (gjk_solver_indep-inl.h:449-548; sphere: sphereTriangleIntersect),
+// recorded as Contact(..., contactp, -normal, penetration).  pos, normal, depth are those
+// recorded values; false when the pair does not intersect.
+bool shape_triangle_contact(const Shape& s, const Tf& tfs, const V3& P1, const V3& P2, const V3& P3, const Tf& tfm,
+                            V3& pos, V3& normal, double& depth);
 
 // Project<S>::projectLine / projectTriangle with an explicit point
 // (math/detail/project-inl.h:54-136).

@@ -567,6 +567,25 @@ def mesh_shape_contacts(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, max_contacts: i
         cap = total
 
 
+def mesh_shape_contact_geometry(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, tris):
+    """The geometry FCL's mesh-shape leaf records with enable_contact for contact k
+    (shape sid[k] at tfs[k], the mesh at tfm[k], triangle tris[k]) -> dict(pos (k, 3),
+    normal (k, 3), depth (k,), ok (k,))."""
+    L = lib(); _bp_sigs(L); _ms_sigs(L)
+    L.orc_mesh_shape_contact_geometry.restype = None
+    L.orc_mesh_shape_contact_geometry.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _ip, _dp, _dp, _ip, _dp, _dp,
+                                                  _dp, _ip]
+    sid = np.ascontiguousarray(sid, np.int32)
+    n = sid.shape[0]
+    tfm = np.ascontiguousarray(tfm, np.float64).reshape(n, 12)
+    tfs = np.ascontiguousarray(tfs, np.float64).reshape(n, 12)
+    tris = np.ascontiguousarray(tris, np.int32)
+    out = dict(pos=np.zeros((n, 3)), normal=np.zeros((n, 3)), depth=np.zeros(n), ok=np.zeros(n, np.int32))
+    L.orc_mesh_shape_contact_geometry(mesh.h, geoms.h, n, _i(sid), _d(tfm), _d(tfs), _i(tris), _d(out["pos"]),
+                                      _d(out["normal"]), _d(out["depth"]), _i(out["ok"]))
+    return out
+
+
 def mesh_shape_distance(mesh: Mesh, geoms: Geoms, sid, tfm, tfs, nthreads: int = 1):
     """fcl::distance(mesh, shape) per query -> dict(dist, tri, pts (n,2,3), nbv, nleaf)."""
     L = lib(); _bp_sigs(L); _ms_sigs(L)

@@ -96,6 +96,23 @@ def test_mesh_shape_pairs_both_orders(gpu_lib):
             if d > 0:
                 assert dr.b1 == dist["tri"][k] and np.array_equal(dr.nearest_points, dist["pts"][k])
     assert (c > 0).any() and (c == 0).any()
+    # enable_contact: Contact(mesh, shape, tri, NONE, contactp, -normal, penetration)
+    reqc = api.CollisionRequest(num_max_contacts=4, enable_contact=True, gjk_solver_type=api.GST_INDEP)
+    pair = np.repeat(np.arange(n), c)
+    P.set_gjk_solver_params(1e-6, 1e-6)
+    geo = P.mesh_shape_contact_geometry(om, G, sid[pair], tfm[pair], tfs[pair], tris)
+    P.set_gjk_solver_params()
+    assert geo["ok"].all()
+    for k in np.nonzero(c)[0][:60]:
+        om_, os_ = api.CollisionObject(mesh, tfm[k]), api.CollisionObject(api.ShapeRef(ss, int(sid[k])), tfs[k])
+        for x, y in ((om_, os_), (os_, om_)):
+            r = api.CollisionResult()
+            assert api.collide(x, y, reqc, r) == c[k]
+            for j, ct in enumerate(r.contacts):
+                q = off[k] + j
+                assert ct.b1 == tris[q]
+                assert np.array_equal(ct.pos, geo["pos"][q]) and np.array_equal(ct.normal, geo["normal"][q])
+                assert ct.penetration_depth == geo["depth"][q]
 
 
 def test_gst_libccd_is_rejected_for_shape_pairs(gpu_lib):

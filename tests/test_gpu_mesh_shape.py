@@ -150,3 +150,28 @@ def test_mesh_shape_contact_list_capacity(gpu_lib):
     assert rc == N.FCLGPU_ERR_CAPACITY and res.total_contacts == total
     assert np.array_equal(counts, full["counts"]) and np.array_equal(offsets, full["offsets"])
     assert (tris == -7).all()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mesh_shape_contact_geometry_matches_oracle(gpu_lib, seed):
+    """enable_contact: the same triangle list, and per contact the point, normal and depth
+    FCL's leaf records (sphereTriangleIntersect for spheres, GJK + EPA otherwise),
+    bit-identical to the oracle's FP64 restatement."""
+    meshes, om, ss, G, midx, sidx, tfm, tfs = _setup(seed, n=1500)
+    for M in (1, 100000):
+        plain = api.mesh_shape_contacts_batch(meshes, ss, midx, sidx, tfm, tfs, num_max_contacts=M)
+        g = api.mesh_shape_contacts_batch(meshes, ss, midx, sidx, tfm, tfs, num_max_contacts=M, enable_contact=True)
+        np.testing.assert_array_equal(g["tris"], plain["tris"])
+        np.testing.assert_array_equal(g["offsets"], plain["offsets"])
+        pair = np.repeat(np.arange(len(midx)), g["counts"])
+        assert len(pair) > 50
+        for k in range(2):
+            sel = midx[pair] == k
+            o = P.mesh_shape_contact_geometry(om[k], G, sidx[pair[sel]], tfm[pair[sel]], tfs[pair[sel]],
+                                              g["tris"][sel])
+            assert o["ok"].all()
+            np.testing.assert_array_equal(g["pos"][sel], o["pos"])
+            np.testing.assert_array_equal(g["normal"][sel], o["normal"])
+            np.testing.assert_array_equal(g["penetration_depth"][sel], o["depth"])
+        assert np.all(g["penetration_depth"] <= 0)
+        assert np.allclose(np.linalg.norm(g["normal"], axis=1), 1.0)

@@ -33,6 +33,36 @@ def test_sphere_triangle_known_answers():
     assert abs(d["dist"][0] - 0.1) < 1e-12
 
 
+def test_sphere_triangle_contact_known_answers():
+    # test_fcl_geometric_shapes.cpp:4697-4705: sphere r = 10, triangle (30,0,0), (9.9,-20,0),
+    # (9.9,20,0): shapeTriangleIntersect's normal is (1,0,0), and R (1,0,0) under a shared
+    # transform; the mesh-shape leaf records -normal, the nearest edge point, depth -0.1
+    S = W.ShapeSet(np.array([W.SPHERE], np.int32), np.array([[10.0, 0, 0]]), np.zeros(1, np.int32),
+                   np.zeros(1, np.int32), np.zeros((0, 3)))
+    G = P.Geoms(S)
+    m = _tri_mesh([[30, 0, 0], [9.9, -20, 0], [9.9, 20, 0]])
+    tf = W.random_poses(1, -1.0, 1.0, 3)[0]
+    eye = W.identity_poses(1)[0]
+    for t in (eye, tf):
+        R = t.reshape(3, 4)[:, :3]
+        o = P.mesh_shape_contact_geometry(m, G, [0], t, t, [0])
+        assert o["ok"][0] == 1
+        np.testing.assert_allclose(o["normal"][0], -R @ np.array([1.0, 0, 0]), atol=1e-9)
+        np.testing.assert_allclose(o["depth"][0], -0.1, atol=1e-9)
+        np.testing.assert_allclose(o["pos"][0], R @ np.array([9.9, 0, 0]) + t.reshape(3, 4)[:, 3], atol=1e-9)
+    # a GJK shape: a box of side 2 resting 0.05 deep in a large triangle; EPA's contact
+    B = W.ShapeSet(np.array([W.BOX], np.int32), np.array([[2.0, 2.0, 2.0]]), np.zeros(1, np.int32),
+                   np.zeros(1, np.int32), np.zeros((0, 3)))
+    Gb = P.Geoms(B)
+    mb = _tri_mesh([[-20, -20, 0], [20, -20, 0], [0, 20, 0]])
+    tb = eye.copy().reshape(3, 4)
+    tb[2, 3] = 0.95
+    o = P.mesh_shape_contact_geometry(mb, Gb, [0], eye, tb.reshape(12), [0])
+    assert o["ok"][0] == 1
+    np.testing.assert_allclose(o["depth"][0], -0.05, atol=1e-9)
+    np.testing.assert_allclose(np.abs(o["normal"][0]), [0, 0, 1], atol=1e-9)
+
+
 @pytest.mark.parametrize("seed", [0, 1])
 def test_mesh_shape_traversals_match_brute_force(seed):
     v, t = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, seed)
