@@ -135,6 +135,7 @@ int prepare_tables(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t*
 // ---------------------------------------------------------------------------------
 struct SplitScratch {
   DevBuf items, own, cstart, ccount, total, rel_start, capped;
+  DevBuf persist;  // PersistCtl, then the round table (persistent launch)
   int64_t item_hint = 0;
   CollideLaunch last;       // launch description of the last batch (for the scatter)
   int64_t last_nrec = 0;
@@ -153,6 +154,15 @@ int32_t g_wb_variant = 1;
 // testing aids (fclgpu_set_collide_test_limits): initial scratch capacities, stack limit
 int64_t g_test_records = 0, g_test_items = 0;
 int32_t g_test_stack = 0;
+// all rounds in one cooperative launch (fclgpu_set_collide_persistent): on/off, the
+// grid barrier's wait limit, and (testing) blocks the barrier waits for beyond the grid
+int32_t g_persist = 1;
+int64_t g_persist_fallbacks = 0;
+int64_t g_barrier_timeout_ns = 60000000000ll;
+int32_t g_test_missing_blocks = 0;
+constexpr int kPersistRounds = 1024;
+constexpr size_t kPersistCtlBytes = 64;
+static_assert(sizeof(PersistCtl) <= kPersistCtlBytes, "control block");
 
 int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, const double* tf2,
                  const fclgpu_collide_request* req, int32_t* counts, int64_t* offsets, int64_t* nbv, int64_t* nleaf,
@@ -166,7 +176,8 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
   int64_t item_cap = std::max<int64_t>(P.item_hint, 4 * n + (1 << 20));
   if (g_test_records > 0) rec_cap = g_test_records;
   if (g_test_items > 0) item_cap = std::max<int64_t>(g_test_items, n);
-  for (int attempt = 0; attempt < 8; ++attempt) {
+  bool persist_ok = true;
+  for (int attempt = 0; attempt < 9; ++attempt) {
     CK(S.records.ensure(sizeof(int4) * (size_t)rec_cap), "record scratch");
     // the buffers only grow; a test limit still caps the part a batch may use
     rec_cap = std::min<int64_t>((int64_t)(S.records.cap / sizeof(int4)),
@@ -217,17 +228,66 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
     bool retry = false;
     double kernel_ms = 0.0;
     BatchCounters hc;
+    // a capacity overflow: grow the scratch and run the batch again
+    auto overflow = [&]() {
+      if (hc.status & DEV_ERR_RECORDS) rec_cap = std::max<int64_t>(rec_cap * 2, (int64_t)hc.records + 65536);
+      if (hc.status & DEV_ERR_ITEMS) item_cap = std::max<int64_t>(item_cap * 2, (int64_t)hc.items + 65536);
+      S.record_hint = rec_cap;
+      P.item_hint = item_cap;
+    };
+    if (P.ev.size() < 2) {
+      for (int k = 0; k < 2; ++k) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e), "event");
+        P.ev.push_back(e);
+      }
+    }
+    // all rounds in one cooperative launch; the rounds' ranges come back in one read
+    const int pgrid = (g_persist && persist_ok) ? collide_persistent_grid(req->precision, stack, g_wb_variant) : 0;
+    if (pgrid > 0 && hi > lo) {
+      CK(P.persist.ensure(kPersistCtlBytes + 16 * (size_t)kPersistRounds), "persistent control");
+      std::vector<unsigned char> hb(kPersistCtlBytes + 16 * (size_t)kPersistRounds);
+      PersistCtl c;
+      std::memset(&c, 0, sizeof(c));
+      c.lo = 0;
+      c.hi = (unsigned long long)n;
+      c.nblocks = (unsigned)(pgrid + g_test_missing_blocks);
+      c.max_rounds = kPersistRounds;
+      c.timeout_ns = (unsigned long long)g_barrier_timeout_ns;
+      PersistCtl* dctl = (PersistCtl*)P.persist.p;
+      int64_t* dtab = (int64_t*)((char*)P.persist.p + kPersistCtlBytes);
+      CK(cudaMemcpyAsync(dctl, &c, sizeof(c), cudaMemcpyHostToDevice, s), "persistent control");
+      CK(cudaEventRecord(P.ev[0], s), "event");
+      CK(launch_collide_persistent(L, req->precision, stack, pgrid, dctl, dtab, s), "persistent collide");
+      CK(cudaEventRecord(P.ev[1], s), "event");
+      CK(cudaMemcpyAsync(hb.data(), P.persist.p, hb.size(), cudaMemcpyDeviceToHost, s), "persistent control");
+      CK(cudaMemcpyAsync(&hc, S.ctr.p, sizeof(hc), cudaMemcpyDeviceToHost, s), "read counters");
+      CK(cudaStreamSynchronize(s), "persistent collide");
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, P.ev[0], P.ev[1]), "event");
+      kernel_ms += ms;
+      std::memcpy(&c, hb.data(), sizeof(c));
+      if (c.err & DEV_ERR_BARRIER) {  // run the batch again, one launch per round
+        persist_ok = false;
+        g_persist_fallbacks++;
+        continue;
+      }
+      if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
+      if (hc.status & (DEV_ERR_RECORDS | DEV_ERR_ITEMS)) {
+        overflow();
+        if (item_cap > 0x7fffffffll) return fail(FCLGPU_ERR_OUT_OF_MEMORY, "work items exceed 2^31");
+        continue;
+      }
+      const int64_t* tab = (const int64_t*)(hb.data() + kPersistCtlBytes);
+      for (unsigned r = 0; r < c.nrounds; ++r) P.rounds.emplace_back(tab[2 * r], tab[2 * r + 1]);
+      lo = (int64_t)c.lo;
+      hi = (int64_t)c.hi;
+      CK(cudaMemsetAsync(&L.ctr->work, 0, sizeof(unsigned long long), s), "counters");
+    }
     for (int round = 0; round < 100000 && hi > lo; ++round) {
       L.item_lo = lo;
       L.item_hi = hi;
       P.rounds.emplace_back(lo, hi);
-      if (P.ev.size() < 2) {
-        for (int k = 0; k < 2; ++k) {
-          cudaEvent_t e;
-          CK(cudaEventCreate(&e), "event");
-          P.ev.push_back(e);
-        }
-      }
       CK(cudaMemsetAsync(&L.ctr->work, 0, sizeof(unsigned long long), s), "counters");
       CK(cudaEventRecord(P.ev[0], s), "event");
       CK(launch_collide_round(L, req->precision, stack, grid, block, s), "collide round");
@@ -239,11 +299,8 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
       kernel_ms += ms;
       if (hc.status & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
       if (hc.status & (DEV_ERR_RECORDS | DEV_ERR_ITEMS)) {
-        if (hc.status & DEV_ERR_RECORDS) rec_cap = std::max<int64_t>(rec_cap * 2, (int64_t)hc.records + 65536);
-        if (hc.status & DEV_ERR_ITEMS) item_cap = std::max<int64_t>(item_cap * 2, (int64_t)hc.items + 65536);
+        overflow();
         if (item_cap > 0x7fffffffll) return fail(FCLGPU_ERR_OUT_OF_MEMORY, "work items exceed 2^31");
-        S.record_hint = rec_cap;
-        P.item_hint = item_cap;
         retry = true;
         break;
       }
@@ -431,6 +488,18 @@ int fclgpu_set_collide_tuning(int32_t budget, int32_t leaf_batch_steps, int32_t 
   g_wb_variant = variant;
   return FCLGPU_OK;
 }
+
+int fclgpu_set_collide_persistent(int32_t enable, int64_t barrier_timeout_ns, int32_t test_missing_blocks) {
+  if (enable < 0 || enable > 1 || barrier_timeout_ns < 1000 || test_missing_blocks < 0 || test_missing_blocks > 1)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "persistent-launch setting out of range");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  g_persist = enable;
+  g_barrier_timeout_ns = barrier_timeout_ns;
+  g_test_missing_blocks = test_missing_blocks;
+  return FCLGPU_OK;
+}
+
+int64_t fclgpu_collide_persistent_fallbacks(void) { return g_persist_fallbacks; }
 
 int fclgpu_set_collide_test_limits(int64_t initial_records, int64_t initial_items, int32_t stack_limit) {
   if (initial_records < 0 || initial_items < 0 || stack_limit < 0)

@@ -13,6 +13,7 @@ enum : uint32_t {
   DEV_ERR_RECORDS = 2u,   // contact record scratch overflow
   DEV_ERR_ITEMS = 4u,     // work-item scratch overflow
   DEV_ERR_PAIR = 8u,      // a query's pair index lies outside the pair table
+  DEV_ERR_BARRIER = 16u,  // a persistent launch's grid barrier timed out
 };
 
 // Counters shared by one batch launch (device scratch).
@@ -57,6 +58,28 @@ struct CollideLaunch {
 
 cudaError_t launch_collide_round(const CollideLaunch& L, int precision, int stack_entries, int grid, int block,
                                  cudaStream_t s);
+
+// Control block of the persistent (one-launch) collide rounds, in device memory.  The
+// host sets lo = 0, hi = n, nblocks = the grid, max_rounds, timeout_ns and zeroes the
+// rest; afterwards [lo, hi) is the range still to run (empty when all rounds ran), the
+// round table holds the ranges of the nrounds rounds that ran, and err has
+// DEV_ERR_BARRIER if a barrier wait gave up.
+struct PersistCtl {
+  unsigned long long lo, hi;
+  unsigned int arrive, gen;
+  unsigned int nblocks, stop;
+  unsigned int nrounds, max_rounds;
+  unsigned long long timeout_ns;
+  unsigned int err, pad;
+};
+constexpr unsigned long long kBarrierMaxSpins = 1ull << 32;
+// One cooperative launch of all rounds of L's batch (the FP32 forms and the plain FP64
+// form alike); table receives 2 x max_rounds range entries.
+cudaError_t launch_collide_persistent(const CollideLaunch& L, int precision, int stack_entries, int grid,
+                                      PersistCtl* ctl, int64_t* table, cudaStream_t s);
+// Grid of the persistent launch (all blocks resident); 0 when cooperative launches are
+// not available.
+int collide_persistent_grid(int precision, int stack_entries, int variant);
 cudaError_t launch_item_totals(const CollideLaunch& L, int64_t lo, int64_t hi, int64_t* total, cudaStream_t s);
 // counts[q] = min(total[q], num_max_contacts); queries that were split and reached the
 // cap are listed in capped[] (their statistics need the exact serial pass).

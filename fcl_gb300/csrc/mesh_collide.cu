@@ -106,8 +106,11 @@ struct SplitSink : ContactSink {
   }
 };
 
+// One round over items [lo, hi): threads fetch items from the work counter until it
+// passes hi.  Items of this round were written by other blocks in the previous round of
+// a persistent launch, so they are read past L1 (__ldcg).
 template <int PREC, int STACK>
-__global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
+__device__ __forceinline__ void collide_round_body(const CollideLaunch& L, long long lo, long long hi) {
   SplitSink sink;
   sink.rec = L.records;
   sink.cap = L.record_cap;
@@ -120,18 +123,18 @@ __global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
   sink.item_ctr = &L.ctr->items;
   sink.child_start = L.child_start;
   sink.child_count = L.child_count;
-  const long long span = L.item_hi - L.item_lo;
+  const long long span = hi - lo;
   for (;;) {
     const long long k = (long long)atomicAdd(&L.ctr->work, 1ull);
     if (k >= span) break;
-    const long long item = L.item_lo + k;
+    const long long item = lo + k;
     long long qi;
     int b1, b2;
     if (item < L.n) {
       qi = item;
       b1 = b2 = 0;
     } else {
-      const int4 it = L.items[item];
+      const int4 it = __ldcg(L.items + item);
       qi = it.x;
       b1 = it.y;
       b2 = it.z;
@@ -149,6 +152,11 @@ __global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
     }
   }
   sink.flush();
+}
+
+template <int PREC, int STACK>
+__global__ void __launch_bounds__(128) k_collide_round(const CollideLaunch L) {
+  collide_round_body<PREC, STACK>(L, L.item_lo, L.item_hi);
 }
 
 // ---------------------------------------------------------------------------------
@@ -178,12 +186,16 @@ struct WbCtx {
   int nrecheck;
 };
 
-// MINB: blocks per SM the register allocation targets (1 = no limit, 158 registers;
-// 4 = 128 registers with a few spills); the autotuner picks the faster.
-template <int STACK, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLaunch L) {
-  __shared__ WbCtx ctx[kWbWarps][32];
-  __shared__ int3 queue[kWbWarps][kWbQueue];
+struct WbShared {
+  WbCtx ctx[kWbWarps][32];
+  int3 queue[kWbWarps][kWbQueue];
+};
+
+template <int STACK>
+__device__ __forceinline__ void collide_round_wb_body(const CollideLaunch& L, long long lo, long long hi,
+                                                      WbShared& sh) {
+  WbCtx (&ctx)[kWbWarps][32] = sh.ctx;
+  int3 (&queue)[kWbWarps][kWbQueue] = sh.queue;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
   const unsigned lt = (1u << lane) - 1u;
@@ -199,7 +211,7 @@ __global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLau
   sink.item_ctr = &L.ctr->items;
   sink.child_start = L.child_start;
   sink.child_count = L.child_count;
-  const long long span = L.item_hi - L.item_lo;
+  const long long span = hi - lo;
   WbCtx& me = ctx[w][lane];
 
   bool have = false, draining = false, exhausted = false, dumped = false;
@@ -220,12 +232,12 @@ __global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLau
       if (k >= span) {
         exhausted = true;
       } else {
-        item = L.item_lo + k;
+        item = lo + k;
         if (item < L.n) {
           qi = item;
           b1 = b2 = 0;
         } else {
-          const int4 it = L.items[item];
+          const int4 it = __ldcg(L.items + item);
           qi = it.x;
           b1 = it.y;
           b2 = it.z;
@@ -386,6 +398,97 @@ __global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLau
   }
   sink.flush();
 }
+
+// MINB: blocks per SM the register allocation targets (1 = no limit, 158 registers;
+// 4 = 128 registers with a few spills); the autotuner picks the faster.
+template <int STACK, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_collide_round_wb(const CollideLaunch L) {
+  __shared__ WbShared sh;
+  collide_round_wb_body<STACK>(L, L.item_lo, L.item_hi, sh);
+}
+
+// ---------------------------------------------------------------------------------
+// Persistent form: all rounds in one cooperative launch.  Between rounds the grid meets
+// at a barrier; block 0 then records the round's item range, moves the range on to the
+// items the round appended and clears the work counter, and the grid meets again.  The
+// barrier's wait is bounded (PersistCtl::timeout_ns): a block that gives up sets
+// DEV_ERR_BARRIER and returns, the others give up at their next barrier, and the host
+// runs the batch again one launch per round.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool grid_barrier(PersistCtl* c) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = &c->gen;
+    const unsigned g = *vgen;
+    __threadfence();
+    const unsigned a = atomicAdd(&c->arrive, 1u);
+    int ok = 1;
+    if (a + 1 == c->nblocks) {
+      atomicExch(&c->arrive, 0u);
+      __threadfence();
+      atomicAdd(&c->gen, 1u);
+    } else {
+      ok = 0;
+      const unsigned long long t0 = global_ns();
+      for (unsigned long long it = 0; it < kBarrierMaxSpins; ++it) {
+        if (*vgen != g) {
+          ok = 1;
+          break;
+        }
+        __nanosleep(256);
+        if ((it & 63) == 63 && global_ns() - t0 > c->timeout_ns) break;
+      }
+      if (!ok) atomicOr(&c->err, DEV_ERR_BARRIER);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <int PREC, int STACK, bool WB>
+__device__ __forceinline__ void run_round(const CollideLaunch& L, long long lo, long long hi) {
+  if constexpr (WB) {
+    __shared__ WbShared sh;
+    collide_round_wb_body<STACK>(L, lo, hi, sh);
+  } else {
+    collide_round_body<PREC, STACK>(L, lo, hi);
+  }
+}
+
+template <int PREC, int STACK, int MINB, bool WB>
+__global__ void __launch_bounds__(128, MINB) k_collide_persist(const CollideLaunch L, PersistCtl* ctl,
+                                                                long long* table) {
+  volatile PersistCtl* vc = ctl;
+  for (unsigned r = 0;; ++r) {
+    const long long lo = (long long)vc->lo, hi = (long long)vc->hi;
+    if (vc->stop || lo >= hi) break;
+    run_round<PREC, STACK, WB>(L, lo, hi);
+    if (!grid_barrier(ctl)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      table[2 * r] = lo;
+      table[2 * r + 1] = hi;
+      const unsigned st = atomicOr(&L.ctr->status, 0u);
+      const unsigned long long items = atomicAdd(&L.ctr->items, 0ull);
+      atomicExch(&L.ctr->work, 0ull);
+      vc->nrounds = r + 1;
+      vc->lo = (unsigned long long)hi;
+      vc->hi = items;
+      if ((st & (DEV_ERR_STACK | DEV_ERR_RECORDS | DEV_ERR_ITEMS)) || r + 1 >= vc->max_rounds) vc->stop = 1;
+      __threadfence();
+    }
+    if (!grid_barrier(ctl)) return;
+  }
+}
+
 
 // total[i] = own[i] + sum of the totals of its children (children are in a later
 // round, whose totals are already known when rounds are processed last to first).
@@ -690,6 +793,40 @@ cudaError_t launch_collide_stats(const CollideLaunch& L, const int32_t* list, in
       k_collide_stats<1, 256><<<grid, 128, 0, s>>>(L, list, nlist);
   }
   return cudaGetLastError();
+}
+
+namespace {
+// the persistent kernel of a configuration: FP64 form, or the FP32 warp-batched form
+// in its register variant
+const void* persist_kernel(int precision, int stack_entries, int variant) {
+  const bool small = stack_entries <= 64;
+  if (precision == 0)
+    return small ? (const void*)k_collide_persist<0, 64, 1, false> : (const void*)k_collide_persist<0, 256, 1, false>;
+  if (variant == 1)
+    return small ? (const void*)k_collide_persist<1, 64, 4, true> : (const void*)k_collide_persist<1, 256, 4, true>;
+  return small ? (const void*)k_collide_persist<1, 64, 1, true> : (const void*)k_collide_persist<1, 256, 1, true>;
+}
+}  // namespace
+
+int collide_persistent_grid(int precision, int stack_entries, int variant) {
+  int dev = 0, sms = 0, coop = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persist_kernel(precision, stack_entries, variant),
+                                                    32 * kWbWarps, 0) != cudaSuccess)
+    return 0;
+  return per_sm < 1 ? 0 : sms * per_sm;
+}
+
+cudaError_t launch_collide_persistent(const CollideLaunch& L, int precision, int stack_entries, int grid,
+                                      PersistCtl* ctl, int64_t* table, cudaStream_t s) {
+  CollideLaunch Lc = L;
+  long long* tab = reinterpret_cast<long long*>(table);
+  void* args[] = {&Lc, &ctl, &tab};
+  ++g_kernel_launches;
+  return cudaLaunchCooperativeKernel(persist_kernel(precision, stack_entries, L.wb_variant), dim3(grid),
+                                     dim3(32 * kWbWarps), args, 0, s);
 }
 
 int collide_round_grid(int precision, int stack_entries, int block, int variant) {

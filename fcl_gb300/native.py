@@ -201,6 +201,8 @@ _SIGS = {
     "fclgpu_shape_collide_batch": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP]),
     "fclgpu_set_gjk_solver_params": (C.c_int, [C.POINTER(GjkSolverParams)]),
     "fclgpu_set_collide_test_limits": (C.c_int, [C.c_int64, C.c_int64, C.c_int32]),
+    "fclgpu_set_collide_persistent": (C.c_int, [C.c_int32, C.c_int64, C.c_int32]),
+    "fclgpu_collide_persistent_fallbacks": (C.c_int64, []),
     "fclgpu_get_gjk_solver_params": (C.c_int, [C.POINTER(GjkSolverParams)]),
     "fclgpu_last_shape_kernel_time": (C.c_int, [C.POINTER(C.c_double)]),
     "fclgpu_broadphase_create": (C.c_int, [_VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.POINTER(C.c_void_p)]),

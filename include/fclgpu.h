@@ -303,6 +303,17 @@ FCLGPU_API int fclgpu_distance_batch_noalloc(const fclgpu_mesh* meshes, int32_t 
  * in FCL. */
 FCLGPU_API int fclgpu_set_collide_test_limits(int64_t initial_records, int64_t initial_items, int32_t stack_limit);
 
+/* The mesh collide rounds run as one cooperative launch (enable = 1, the default): the
+ * grid meets at a device-wide barrier between rounds and the next round's work items
+ * come from the device queue, with no host read-back between rounds.  A barrier wait
+ * longer than barrier_timeout_ns (default 60 s) makes the launch give up, and the batch
+ * runs again one launch per round (enable = 0 always does; results are the same).
+ * test_missing_blocks = 1 makes every barrier wait for one block more than the grid
+ * has (testing the give-up path).  No counterpart in FCL. */
+FCLGPU_API int fclgpu_set_collide_persistent(int32_t enable, int64_t barrier_timeout_ns, int32_t test_missing_blocks);
+/* Batches that fell back from the persistent launch since load. */
+FCLGPU_API int64_t fclgpu_collide_persistent_fallbacks(void);
+
 /* Number of this library's kernel launches issued since load (for launch accounting). */
 FCLGPU_API int64_t fclgpu_kernel_launch_count(void);
 /* Device time (ms, CUDA events on the batch's stream) of the traversal kernel of the

@@ -300,3 +300,66 @@ def test_collide_capacity_retry_and_stack_limit(gpu_lib):
         N.check(N.lib().fclgpu_set_collide_test_limits(0, 0, 0), "limits")
     again = run()
     assert np.array_equal(again["contacts"], ref["contacts"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_collide_persistent_launch_matches_round_launches(gpu_lib, precision):
+    """All collide rounds in one cooperative launch (the default) against one launch per
+    round: the same counts, contact lists and statistics, many rounds deep (budget 64),
+    and the oracle's on the C0 pair."""
+    from fcl_gb300 import native as N
+    w = W.config1(scale=0.004, n_pairs=6, tri_hi=30000, seed=4)
+    ms = _meshes(w)
+
+    def run():
+        return api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                                 precision=precision, statistics=True, budget=64)
+
+    launches0 = N.lib().fclgpu_kernel_launch_count()
+    one = run()
+    launches_one = N.lib().fclgpu_kernel_launch_count() - launches0
+    try:
+        N.check(N.lib().fclgpu_set_collide_persistent(0, 60 * 10**9, 0), "persistent")
+        launches0 = N.lib().fclgpu_kernel_launch_count()
+        per_round = run()
+        launches_rounds = N.lib().fclgpu_kernel_launch_count() - launches0
+    finally:
+        N.check(N.lib().fclgpu_set_collide_persistent(1, 60 * 10**9, 0), "persistent")
+    for k in ("counts", "contacts", "num_bv_tests", "num_leaf_tests"):
+        assert np.array_equal(one[k], per_round[k]), k
+    assert one["contacts"].shape[0] > 1000
+    assert launches_rounds > launches_one + 5  # the per-round form launched every round
+    w0 = W.config0(n_poses=500)
+    out = api.collide_batch(_meshes(w0), w0.pairs, None, w0.tf2, num_max_contacts=100000, precision=precision,
+                            statistics=True, budget=64)
+    C, ct, BV, LF = _oracle_collide(w0, 100000)
+    assert np.array_equal(out["counts"], C) and np.array_equal(out["contacts"], ct)
+    assert np.array_equal(out["num_bv_tests"], BV)
+
+
+def test_collide_persistent_barrier_timeout_falls_back(gpu_lib):
+    """A grid barrier that waits for a block the grid does not have gives up after its
+    limit (20 ms here): the launch reports it, the batch runs again one launch per round,
+    and the result is unchanged."""
+    from fcl_gb300 import native as N
+    w = W.config1(scale=0.004, n_pairs=6, tri_hi=30000, seed=5)
+    ms = _meshes(w)
+
+    def run():
+        return api.collide_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, num_max_contacts=100000,
+                                 precision="fp32", statistics=True, budget=64)
+
+    ref = run()
+    before = N.lib().fclgpu_collide_persistent_fallbacks()
+    try:
+        N.check(N.lib().fclgpu_set_collide_persistent(1, 20 * 10**6, 1), "persistent")
+        got = run()
+    finally:
+        N.check(N.lib().fclgpu_set_collide_persistent(1, 60 * 10**9, 0), "persistent")
+    after = N.lib().fclgpu_collide_persistent_fallbacks()
+    assert after > before  # every batch of the call fell back
+    for k in ("counts", "contacts", "num_bv_tests", "num_leaf_tests"):
+        assert np.array_equal(got[k], ref[k]), k
+    again = run()
+    assert np.array_equal(again["contacts"], ref["contacts"])
+    assert N.lib().fclgpu_collide_persistent_fallbacks() == after
