@@ -638,6 +638,90 @@ def collide_batch(meshes, pairs, tf1, tf2, pair_of_query=None, num_max_contacts=
     return out
 
 
+class BVHFrontList:
+    """detail::BVHFrontList (geometry/bvh/detail/BVH_front.h): the (b1, b2) BV node pairs
+    where the last traversal of a mesh pair stopped, to restart from at the next pose."""
+
+    def __init__(self, nodes=None):
+        self.nodes = np.zeros((0, 2), np.int32) if nodes is None else np.asarray(nodes, np.int32).reshape(-1, 2)
+
+    def size(self) -> int:
+        return int(self.nodes.shape[0])
+
+    def clear(self):
+        self.nodes = np.zeros((0, 2), np.int32)
+
+
+def collide_front_batch(meshes, pairs, tf1, tf2, fronts=None, pair_of_query=None, num_max_contacts=1,
+                        precision="fp32", statistics=False, stream=None):
+    """Front-list collide (collide(node, front_list), collision_node-inl.h:72-82) of n
+    queries: fronts is a list of n (m_i, 2) node-pair arrays from a previous call (or
+    None: start from the roots).  Returns counts, contact_offsets, contacts (FCL's order
+    for a front traversal), fronts (the new list per query) and optional statistics."""
+    pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    hs = _handles(meshes)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(-1, 12)
+    n = tf2.shape[0]
+    tf1a = None if tf1 is None else np.ascontiguousarray(tf1, np.float64).reshape(-1, 12)
+    pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
+    fin_off = fin = None
+    if fronts is not None:
+        if len(fronts) != n:
+            raise N.FclGpuError(N.FCLGPU_ERR_INVALID_ARGUMENT, "collide_front_batch", "one front per query")
+        arrs = [np.asarray(f.nodes if isinstance(f, BVHFrontList) else f, np.int32).reshape(-1, 2) for f in fronts]
+        fin_off = np.concatenate([[0], np.cumsum([a.shape[0] for a in arrs])]).astype(np.int64)
+        fin = np.ascontiguousarray(np.concatenate(arrs) if arrs else np.zeros((0, 2), np.int32), np.int32)
+        if fin.shape[0] == 0:
+            fin = np.zeros((1, 2), np.int32)
+    req = N.FrontRequest(int(num_max_contacts), _prec(precision))
+    counts = np.zeros(n, np.int32)
+    coff = np.zeros(n + 1, np.int64)
+    foff = np.zeros(n + 1, np.int64)
+    st = [np.zeros(n, np.int64) for _ in range(2)] if statistics else [None] * 2
+    ccap, fcap = max(16, n), max(64, 4 * n + (0 if fin is None else 2 * fin.shape[0]))
+    for _ in range(3):
+        cont = np.zeros((ccap, 2), np.int32)
+        fr = np.zeros((fcap, 2), np.int32)
+        res = N.FrontResult(counts.ctypes.data, coff.ctypes.data, cont.ctypes.data, ccap, foff.ctypes.data,
+                            fr.ctypes.data, fcap, *(None if a is None else a.ctypes.data for a in st), 0, 0)
+        rc = N.lib().fclgpu_collide_front_batch(hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n,
+                                                None if pq is None else pq.ctypes.data,
+                                                None if tf1a is None else tf1a.ctypes.data, tf2.ctypes.data,
+                                                None if fin_off is None else fin_off.ctypes.data,
+                                                None if fin is None else fin.ctypes.data, C.byref(req),
+                                                C.byref(res), stream)
+        if rc == N.FCLGPU_ERR_CAPACITY:
+            ccap, fcap = max(ccap, int(res.total_contacts)), max(fcap, int(res.total_front))
+            continue
+        N.check(rc, "fclgpu_collide_front_batch")
+        tf = int(res.total_front)
+        out = {"counts": counts, "contact_offsets": coff, "contacts": cont[: int(res.total_contacts)],
+               "front_offsets": foff, "front": fr[:tf],
+               "fronts": [fr[foff[i]:foff[i + 1]].copy() for i in range(n)]}
+        if statistics:
+            out["num_bv_tests"], out["num_leaf_tests"] = st
+        return out
+    raise N.FclGpuError(N.FCLGPU_ERR_CAPACITY, "fclgpu_collide_front_batch", "totals changed between calls")
+
+
+def collide_front(o1: "CollisionObject", o2: "CollisionObject", request: "CollisionRequest",
+                  result: "CollisionResult", front_list: BVHFrontList) -> int:
+    """collide(node, front_list) on a mesh pair (BVHModel<OBBRSS>): an empty front_list
+    runs the full traversal and records the front, a non-empty one restarts from it
+    (propagateBVHFrontListCollisionRecurse); front_list is updated in place."""
+    if not (isinstance(o1.geometry, BVHModel) and isinstance(o2.geometry, BVHModel)):
+        raise N.FclGpuError(N.FCLGPU_ERR_INVALID_ARGUMENT, "collide_front", "front lists are for mesh pairs")
+    room = max(0, request.num_max_contacts - len(result.contacts))
+    if room == 0:
+        return result.numContacts()
+    out = collide_front_batch([o1.geometry, o2.geometry], [[0, 1]], o1.tf[None], o2.tf[None],
+                              fronts=[front_list.nodes], num_max_contacts=room, precision=request.precision)
+    for b1, b2 in out["contacts"]:
+        result.contacts.append(Contact(o1.geometry, o2.geometry, int(b1), int(b2)))
+    front_list.nodes = out["fronts"][0]
+    return result.numContacts()
+
+
 _contacts_hint = {"cap": 1 << 16}
 
 

@@ -227,7 +227,7 @@ int collide_core(int64_t n, const int32_t* pair_of_query, const double* tf1, con
     int64_t lo = 0, hi = n;
     bool retry = false;
     double kernel_ms = 0.0;
-    BatchCounters hc;
+    BatchCounters hc{};
     // a capacity overflow: grow the scratch and run the batch again
     auto overflow = [&]() {
       if (hc.status & DEV_ERR_RECORDS) rec_cap = std::max<int64_t>(rec_cap * 2, (int64_t)hc.records + 65536);
@@ -1131,6 +1131,181 @@ int fclgpu_distance_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const i
   if (res->num_rechecks) CK(cudaMemcpyAsync(res->num_rechecks, dr.num_rechecks, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
   CK(cudaStreamSynchronize(s), "distance batch");
   return FCLGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Front-list collide (mesh_front.cu): a count launch, scans, a fill launch.
+// ---------------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+struct FrontScratch {
+  DevBuf ncont, nseg, flen, status, scan_tmp, coff, foff;
+  DevBuf in_pq, in_tf1, in_tf2, in_foff, in_front, out_counts, out_coff, out_cont, out_foff, out_front, out_nbv,
+      out_nleaf;
+};
+FrontScratch g_front;
+}  // namespace
+
+extern "C" {
+
+int fclgpu_collide_front_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                                      int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                                      const double* tf2, const int64_t* front_in_offsets, const int32_t* front_in,
+                                      const fclgpu_front_request* req, fclgpu_front_result* res, void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts || !res->contact_offsets || !res->front_offsets)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or outputs");
+  if (n >= (int64_t)1 << 31) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "batch too large");
+  if (req->num_max_contacts < 1) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "num_max_contacts must be >= 1");
+  if (req->precision != FCLGPU_PLAIN_FP64 && req->precision != FCLGPU_FP32_RECHECK)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "unknown precision");
+  if ((front_in_offsets == nullptr) != (front_in == nullptr))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "front_in_offsets and front_in go together");
+  if ((res->contacts_capacity > 0 && !res->contacts) || (res->front_capacity > 0 && !res->front) ||
+      res->contacts_capacity < 0 || res->front_capacity < 0)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing contact or front buffer");
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  int stack = 64;
+  rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+  if (rc) return rc;
+  res->total_contacts = 0;
+  res->total_front = 0;
+  if (n == 0) {
+    CK(cudaMemsetAsync(res->contact_offsets, 0, 8, s), "offsets");
+    CK(cudaMemsetAsync(res->front_offsets, 0, 8, s), "offsets");
+    CK(cudaStreamSynchronize(s), "front collide");
+    return FCLGPU_OK;
+  }
+  FrontScratch& F = g_front;
+  const size_t nn = (size_t)n;
+  CK(F.nseg.ensure(12 * nn), "front scratch");
+  CK(F.flen.ensure(4 * nn), "front scratch");
+  CK(F.status.ensure(4), "front scratch");
+  CK(F.scan_tmp.ensure(sizeof(int64_t) * (size_t)(2 * ((n + 4095) / 4096) + 4)), "scan scratch");
+  CK(cudaMemsetAsync(F.status.p, 0, 4, s), "front scratch");
+  FrontLaunch L{};
+  L.meshes = (const DevMesh*)g_scratch.meshes.p;
+  L.pairs = (const int2*)g_scratch.pairs.p;
+  L.num_pairs = num_pairs;
+  L.pair_of_query = pair_of_query;
+  L.tf1 = tf1;
+  L.tf2 = tf2;
+  L.n = n;
+  L.num_max_contacts = req->num_max_contacts;
+  L.front_in_off = front_in_offsets;
+  L.front_in = front_in;
+  L.ncont = res->counts;
+  L.nseg = (int32_t*)F.nseg.p;
+  L.status = (unsigned*)F.status.p;
+  CK(launch_collide_front(L, req->precision, stack, false, s), "front count");
+  CK(launch_exclusive_scan(res->counts, n, res->contact_offsets, (int64_t*)F.scan_tmp.p, s), "scan");
+  CK(launch_front_lengths(L.nseg, n, (int32_t*)F.flen.p, s), "front lengths");
+  CK(launch_exclusive_scan((const int32_t*)F.flen.p, n, res->front_offsets, (int64_t*)F.scan_tmp.p, s), "scan");
+  int64_t tot[2] = {0, 0};
+  unsigned st = 0;
+  CK(cudaMemcpyAsync(&tot[0], res->contact_offsets + n, 8, cudaMemcpyDeviceToHost, s), "totals");
+  CK(cudaMemcpyAsync(&tot[1], res->front_offsets + n, 8, cudaMemcpyDeviceToHost, s), "totals");
+  CK(cudaMemcpyAsync(&st, F.status.p, 4, cudaMemcpyDeviceToHost, s), "status");
+  CK(cudaStreamSynchronize(s), "front count");
+  if (st & DEV_ERR_PAIR) return fail(FCLGPU_ERR_DEVICE_STATUS, "a query's pair index lies outside the pair table");
+  if (st & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
+  res->total_contacts = tot[0];
+  res->total_front = tot[1];
+  if (tot[0] > res->contacts_capacity || tot[1] > res->front_capacity)
+    return fail(FCLGPU_ERR_CAPACITY, "contact or front buffer too small");
+  L.cont_off = res->contact_offsets;
+  L.contacts = res->contacts;
+  L.front_out_off = res->front_offsets;
+  L.front_out = res->front;
+  L.nbv = res->num_bv_tests;
+  L.nleaf = res->num_leaf_tests;
+  CK(launch_collide_front(L, req->precision, stack, true, s), "front fill");
+  CK(cudaStreamSynchronize(s), "front fill");
+  return FCLGPU_OK;
+}
+
+int fclgpu_collide_front_batch(const fclgpu_mesh* meshes, int32_t num_meshes, const int32_t* pairs_host,
+                               int32_t num_pairs, int64_t n, const int32_t* pair_of_query, const double* tf1,
+                               const double* tf2, const int64_t* front_in_offsets, const int32_t* front_in,
+                               const fclgpu_front_request* req, fclgpu_front_result* res, void* stream) {
+  if (!req || !res || n < 0 || (n > 0 && (!tf2 || !res->counts || !res->contact_offsets || !res->front_offsets)))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing request, result, tf2 or outputs");
+  if ((front_in_offsets == nullptr) != (front_in == nullptr))
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "front_in_offsets and front_in go together");
+  if ((res->contacts_capacity > 0 && !res->contacts) || (res->front_capacity > 0 && !res->front) ||
+      res->contacts_capacity < 0 || res->front_capacity < 0)
+    return fail(FCLGPU_ERR_INVALID_ARGUMENT, "missing contact or front buffer");
+  cudaStream_t s = (cudaStream_t)stream;
+  FrontScratch& F = g_front;
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  int rc = ensure_init();
+  if (rc) return rc;
+  const int64_t nfin = front_in_offsets && n > 0 ? front_in_offsets[n] : 0;
+  if (nfin < 0) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "negative front length");
+  if (pair_of_query) CK(F.in_pq.ensure(4 * nn), "inputs");
+  if (tf1) CK(F.in_tf1.ensure(96 * nn), "inputs");
+  CK(F.in_tf2.ensure(96 * nn), "inputs");
+  if (front_in) {
+    CK(F.in_foff.ensure(8 * (nn + 1)), "inputs");
+    CK(F.in_front.ensure(8 * (size_t)std::max<int64_t>(nfin, 1)), "inputs");
+  }
+  CK(F.out_counts.ensure(4 * nn), "outputs");
+  CK(F.out_coff.ensure(8 * (nn + 1)), "outputs");
+  CK(F.out_foff.ensure(8 * (nn + 1)), "outputs");
+  CK(F.out_cont.ensure(8 * (size_t)std::max<int64_t>(res->contacts_capacity, 1)), "outputs");
+  CK(F.out_front.ensure(8 * (size_t)std::max<int64_t>(res->front_capacity, 1)), "outputs");
+  if (res->num_bv_tests) CK(F.out_nbv.ensure(8 * nn), "outputs");
+  if (res->num_leaf_tests) CK(F.out_nleaf.ensure(8 * nn), "outputs");
+  if (n > 0) {
+    if (pair_of_query) CK(cudaMemcpyAsync(F.in_pq.p, pair_of_query, 4 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (tf1) CK(cudaMemcpyAsync(F.in_tf1.p, tf1, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    CK(cudaMemcpyAsync(F.in_tf2.p, tf2, 96 * n, cudaMemcpyHostToDevice, s), "h2d");
+    if (front_in) {
+      CK(cudaMemcpyAsync(F.in_foff.p, front_in_offsets, 8 * (n + 1), cudaMemcpyHostToDevice, s), "h2d");
+      if (nfin > 0) CK(cudaMemcpyAsync(F.in_front.p, front_in, 8 * nfin, cudaMemcpyHostToDevice, s), "h2d");
+    }
+  }
+  fclgpu_front_result dr{};
+  dr.counts = (int32_t*)F.out_counts.p;
+  dr.contact_offsets = (int64_t*)F.out_coff.p;
+  dr.contacts = (int32_t*)F.out_cont.p;
+  dr.contacts_capacity = res->contacts_capacity;
+  dr.front_offsets = (int64_t*)F.out_foff.p;
+  dr.front = (int32_t*)F.out_front.p;
+  dr.front_capacity = res->front_capacity;
+  dr.num_bv_tests = res->num_bv_tests ? (int64_t*)F.out_nbv.p : nullptr;
+  dr.num_leaf_tests = res->num_leaf_tests ? (int64_t*)F.out_nleaf.p : nullptr;
+  rc = fclgpu_collide_front_batch_device(meshes, num_meshes, pairs_host, num_pairs, n,
+                                         pair_of_query ? (const int32_t*)F.in_pq.p : nullptr,
+                                         tf1 ? (const double*)F.in_tf1.p : nullptr, (const double*)F.in_tf2.p,
+                                         front_in ? (const int64_t*)F.in_foff.p : nullptr,
+                                         front_in ? (const int32_t*)F.in_front.p : nullptr, req, &dr, stream);
+  res->total_contacts = dr.total_contacts;
+  res->total_front = dr.total_front;
+  if (rc != FCLGPU_OK && rc != FCLGPU_ERR_CAPACITY) return rc;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(res->counts, dr.counts, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    CK(cudaMemcpyAsync(res->contact_offsets, dr.contact_offsets, 8 * (n + 1), cudaMemcpyDeviceToHost, s), "d2h");
+    CK(cudaMemcpyAsync(res->front_offsets, dr.front_offsets, 8 * (n + 1), cudaMemcpyDeviceToHost, s), "d2h");
+  } else {
+    res->contact_offsets[0] = 0;
+    res->front_offsets[0] = 0;
+  }
+  if (rc == FCLGPU_OK && n > 0) {
+    if (dr.total_contacts > 0)
+      CK(cudaMemcpyAsync(res->contacts, dr.contacts, 8 * dr.total_contacts, cudaMemcpyDeviceToHost, s), "d2h");
+    if (dr.total_front > 0)
+      CK(cudaMemcpyAsync(res->front, dr.front, 8 * dr.total_front, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->num_bv_tests) CK(cudaMemcpyAsync(res->num_bv_tests, dr.num_bv_tests, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->num_leaf_tests)
+      CK(cudaMemcpyAsync(res->num_leaf_tests, dr.num_leaf_tests, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
+  }
+  CK(cudaStreamSynchronize(s), "front collide");
+  return rc;
 }
 
 }  // extern "C"

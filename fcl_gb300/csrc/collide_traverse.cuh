@@ -59,7 +59,7 @@ FCLG_HD void query_transform_collide(const double* tf1, const double* tf2, long 
 
 // Exact FP64 leaf test (intersect-inl.h:597-617) on triangle ids p1, p2.
 #if defined(__CUDACC__)
-__device__ __host__ __noinline__
+static __device__ __host__ __noinline__
 #else
 inline
 #endif
@@ -77,7 +77,7 @@ bool leaf_collide64(const DevMesh& A, const DevMesh& B, int p1, int p2, const M3
 }
 
 #if defined(__CUDACC__)
-__device__ __host__ __noinline__
+static __device__ __host__ __noinline__
 #else
 inline
 #endif

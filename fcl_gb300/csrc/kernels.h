@@ -175,6 +175,33 @@ cudaError_t launch_scatter_contacts(const int4* records, int64_t nrec, const int
 int collide_grid(int precision, int stack_entries, int block);
 int distance_grid(int precision, int stack_entries, int block);
 
+// Front-list collide (mesh_front.cu): one thread per query; the COUNT launch fills
+// ncont and nseg (kept originals, kept appended entries, append list), the FILL launch
+// writes contacts at cont_off, the new front at front_out_off and the statistics.
+struct FrontLaunch {
+  const DevMesh* meshes;
+  const int2* pairs;
+  int32_t num_pairs;
+  const int32_t* pair_of_query;
+  const double* tf1;
+  const double* tf2;
+  int64_t n;
+  int32_t num_max_contacts;
+  const int64_t* front_in_off;  // n + 1, or null (no fronts)
+  const int32_t* front_in;      // (b1, b2) pairs
+  int32_t* ncont;
+  int32_t* nseg;                // 3 per query
+  const int64_t* cont_off;
+  int32_t* contacts;
+  const int64_t* front_out_off;
+  int32_t* front_out;
+  int64_t* nbv;
+  int64_t* nleaf;
+  unsigned* status;
+};
+cudaError_t launch_collide_front(const FrontLaunch& L, int precision, int stack_entries, bool fill, cudaStream_t s);
+cudaError_t launch_front_lengths(const int32_t* nseg, int64_t n, int32_t* len, cudaStream_t s);
+
 extern int64_t g_kernel_launches;
 extern double g_last_shape_ms;
 

@@ -39,6 +39,17 @@ class CollideRequest(C.Structure):
                 ("budget", C.c_int32)]
 
 
+class FrontRequest(C.Structure):
+    _fields_ = [("num_max_contacts", C.c_int32), ("precision", C.c_int32)]
+
+
+class FrontResult(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("contact_offsets", C.c_void_p), ("contacts", C.c_void_p),
+                ("contacts_capacity", C.c_int64), ("front_offsets", C.c_void_p), ("front", C.c_void_p),
+                ("front_capacity", C.c_int64), ("num_bv_tests", C.c_void_p), ("num_leaf_tests", C.c_void_p),
+                ("total_contacts", C.c_int64), ("total_front", C.c_int64)]
+
+
 class CollideResult(C.Structure):
     _fields_ = [("counts", C.c_void_p), ("offsets", C.c_void_p), ("contacts", C.c_void_p),
                 ("contacts_capacity", C.c_int64), ("num_bv_tests", C.c_void_p), ("num_leaf_tests", C.c_void_p),
@@ -176,6 +187,10 @@ _SIGS = {
                                               C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
     "fclgpu_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                        C.POINTER(CollideRequest), C.POINTER(CollideResult), _VP]),
+    "fclgpu_collide_front_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP, _VP,
+                                                    _VP, C.POINTER(FrontRequest), C.POINTER(FrontResult), _VP]),
+    "fclgpu_collide_front_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP, _VP, _VP,
+                                             C.POINTER(FrontRequest), C.POINTER(FrontResult), _VP]),
     "fclgpu_continuous_collide_batch_device": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP,
                                                          _VP, _VP, C.POINTER(CcdRequest), C.POINTER(CcdResult), _VP]),
     "fclgpu_continuous_collide_batch": (C.c_int, [_VP, C.c_int32, _VP, C.c_int32, C.c_int64, _VP, _VP, _VP, _VP,

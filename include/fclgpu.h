@@ -167,6 +167,51 @@ FCLGPU_API int fclgpu_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshe
                                     const double* tf2, const fclgpu_collide_request* req,
                                     fclgpu_collide_result* res, void* stream);
 
+/* Front-list (temporal coherence) collide of BVHModel<OBBRSS> pairs: FCL's
+ * collide(node, front_list) with a BVHFrontList (geometry/bvh/detail/BVH_front.h;
+ * collision_node-inl.h:72-82; traversal_recurse-inl.h:82-129, 463-521).  Query i's front
+ * is front_in[2 * front_in_offsets[i] ..] up to front_in_offsets[i + 1] ((b1, b2) BV node
+ * pairs, FCL's node ids), as a previous call returned it; an empty front (or
+ * front_in == NULL) starts from the roots.  The call returns the contacts (b1, b2)
+ * triangle ids in FCL's order for a front traversal (contacts are kept while fewer than
+ * num_max_contacts exist; the traversal does not stop early, and a leaf reached from a
+ * front node that overlaps is tested twice, as in FCL) and the query's new front, both
+ * per query at int64 offsets (n + 1 entries).  total_contacts and total_front are set;
+ * when either exceeds its capacity the call returns FCLGPU_ERR_CAPACITY with counts and
+ * both offset arrays filled.  Optional statistics count FCL's BVTesting / leafTesting
+ * calls.  front_in and front must not overlap.  "_device": device pointers; plain: host
+ * pointers.  Synchronises the stream. */
+typedef struct {
+  int32_t num_max_contacts;  /* >= 1 */
+  int32_t precision;         /* FCLGPU_PLAIN_FP64 or FCLGPU_FP32_RECHECK (same results) */
+} fclgpu_front_request;
+
+typedef struct {
+  int32_t* counts;           /* n */
+  int64_t* contact_offsets;  /* n + 1 */
+  int32_t* contacts;         /* 2 x contacts_capacity */
+  int64_t contacts_capacity;
+  int64_t* front_offsets;    /* n + 1 */
+  int32_t* front;            /* 2 x front_capacity */
+  int64_t front_capacity;
+  int64_t* num_bv_tests;     /* optional, n */
+  int64_t* num_leaf_tests;   /* optional, n */
+  int64_t total_contacts;    /* written by the call */
+  int64_t total_front;       /* written by the call */
+} fclgpu_front_result;
+
+FCLGPU_API int fclgpu_collide_front_batch_device(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                                 const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+                                                 const int32_t* pair_of_query, const double* tf1,
+                                                 const double* tf2, const int64_t* front_in_offsets,
+                                                 const int32_t* front_in, const fclgpu_front_request* req,
+                                                 fclgpu_front_result* res, void* stream);
+FCLGPU_API int fclgpu_collide_front_batch(const fclgpu_mesh* meshes, int32_t num_meshes,
+                                          const int32_t* pairs_host, int32_t num_pairs, int64_t n,
+                                          const int32_t* pair_of_query, const double* tf1, const double* tf2,
+                                          const int64_t* front_in_offsets, const int32_t* front_in,
+                                          const fclgpu_front_request* req, fclgpu_front_result* res, void* stream);
+
 /* Contacts with their geometry: fcl::collide with CollisionRequest::enable_contact = true
  * on BVHModel<OBBRSS> pairs (mesh_collision_traversal_node-inl.h:579-600;
  * Intersect::intersect_Triangle with contact output, intersect-inl.h:597-617, 800-886).

@@ -134,6 +134,32 @@ int64_t orc_collide_batch(void* h1, void* h2, int64_t n, const double* tf1, cons
   return total;
 }
 
+// collide(node, front_list) for one pose of a mesh pair: the front (b1, b2 pairs) in and
+// out.  Returns the number of contacts; *nfront_out and the contacts / front written up
+// to their capacities (pairs).
+int64_t orc_collide_front(void* h1, void* h2, const double* tf1, const double* tf2, int64_t num_max_contacts,
+                          const int* front_in, int64_t nfront_in, int* front_out, int64_t front_cap,
+                          int64_t* nfront_out, int* contacts, int64_t cont_cap, int64_t* nbv, int64_t* nleaf) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  std::vector<int> front(front_in, front_in + 2 * nfront_in), cont;
+  CollideStats st;
+  const size_t k = collide_mesh_front(*m1, tf1 ? load_tf(tf1) : identity_tf(), *m2, load_tf(tf2),
+                                      (size_t)num_max_contacts, front, cont, &st);
+  *nfront_out = (int64_t)front.size() / 2;
+  for (int64_t j = 0; j < std::min<int64_t>(*nfront_out, front_cap); ++j) {
+    front_out[2 * j] = front[2 * j];
+    front_out[2 * j + 1] = front[2 * j + 1];
+  }
+  for (int64_t j = 0; j < std::min<int64_t>((int64_t)k, cont_cap); ++j) {
+    contacts[2 * j] = cont[2 * j];
+    contacts[2 * j + 1] = cont[2 * j + 1];
+  }
+  if (nbv) *nbv = st.num_bv_tests;
+  if (nleaf) *nleaf = st.num_leaf_tests;
+  return (int64_t)k;
+}
+
 // Batched fcl::collide with enable_contact = true over n poses of one mesh pair.
 // counts[i] = contacts of pose i; per contact (pose after pose, DFS order): ids (b1,b2),
 // pos (3), normal (3), depth (1), up to cap contacts.  Returns the total.

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <limits>
+#include <list>
 #include <utility>
 
 namespace oracle {
@@ -1268,6 +1269,74 @@ void collision_recurse(CollideCtx& c, int b1, int b2) {
   }
 }
 
+// BVHFrontList (geometry/bvh/detail/BVH_front.h): a std::list of (left, right, valid)
+struct FrontNode {
+  int left, right;
+  bool valid;
+};
+using FrontList = std::list<FrontNode>;
+
+// traversal_recurse-inl.h:82-129 (collisionRecurse with a front list): leaf pairs join the
+// list before their BV test, disjoint pairs after it; no early stop while a list is given
+void collision_recurse_front(CollideCtx& c, int b1, int b2, FrontList* fl) {
+  bool l1 = c.m1->nodes[b1].first_child < 0;
+  bool l2 = c.m2->nodes[b2].first_child < 0;
+  if (l1 && l2) {
+    if (fl) fl->push_back({b1, b2, true});
+    if (bv_testing(c, b1, b2)) return;
+    leaf_testing(c, b1, b2);
+    return;
+  }
+  if (bv_testing(c, b1, b2)) {
+    if (fl) fl->push_back({b1, b2, true});
+    return;
+  }
+  if (first_over_second(*c.m1, *c.m2, b1, b2)) {
+    int c1 = c.m1->nodes[b1].first_child, c2 = c1 + 1;
+    collision_recurse_front(c, c1, b2, fl);
+    if (c.can_stop() && !fl) return;
+    collision_recurse_front(c, c2, b2, fl);
+  } else {
+    int c1 = c.m2->nodes[b2].first_child, c2 = c1 + 1;
+    collision_recurse_front(c, b1, c1, fl);
+    if (c.can_stop() && !fl) return;
+    collision_recurse_front(c, b1, c2, fl);
+  }
+}
+
+// traversal_recurse-inl.h:463-521 (propagateBVHFrontListCollisionRecurse): the loop walks
+// the std::list while the recursions append to it, so appended entries are visited too
+void propagate_front(CollideCtx& c, FrontList& fl) {
+  FrontList append;
+  for (auto it = fl.begin(); it != fl.end(); ++it) {
+    const int b1 = it->left, b2 = it->right;
+    const bool l1 = c.m1->nodes[b1].first_child < 0;
+    const bool l2 = c.m2->nodes[b2].first_child < 0;
+    if (l1 & l2) {
+      it->valid = false;
+      collision_recurse_front(c, b1, b2, &append);
+    } else if (!bv_testing(c, b1, b2)) {
+      it->valid = false;
+      if (first_over_second(*c.m1, *c.m2, b1, b2)) {
+        int c1 = c.m1->nodes[b1].first_child, c2 = c1 + 1;
+        collision_recurse_front(c, c1, b2, &fl);
+        collision_recurse_front(c, c2, b2, &fl);
+      } else {
+        int c1 = c.m2->nodes[b2].first_child, c2 = c1 + 1;
+        collision_recurse_front(c, b1, c1, &fl);
+        collision_recurse_front(c, b1, c2, &fl);
+      }
+    }
+  }
+  for (auto it = fl.begin(); it != fl.end();) {
+    if (!it->valid)
+      it = fl.erase(it);
+    else
+      ++it;
+  }
+  for (const auto& e : append) fl.push_back(e);
+}
+
 struct DistCtx {
   const Mesh* m1;
   const Mesh* m2;
@@ -1360,6 +1429,35 @@ size_t collide_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2
   c.full = nullptr;
   c.tf1 = tf1;
   collision_recurse(c, 0, 0);
+  if (st) *st = c.st;
+  return c.n_contacts;
+}
+
+// collide(node, front_list) (collision_node-inl.h:72-82) on the oriented OBBRSS node
+// initialised as collide_mesh does; front is the list in and out as (b1, b2) pairs
+size_t collide_mesh_front(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2, size_t num_max_contacts,
+                          std::vector<int>& front, std::vector<int>& contacts, CollideStats* st) {
+  CollideCtx c;
+  c.m1 = &m1;
+  c.m2 = &m2;
+  c.R = mulT(tf1.R, tf2.R);
+  c.T = mulTv(tf1.R, sub(tf2.t, tf1.t));
+  c.num_max_contacts = num_max_contacts;
+  c.contacts = &contacts;
+  c.n_contacts = 0;
+  c.full = nullptr;
+  c.tf1 = tf1;
+  FrontList fl;
+  for (size_t k = 0; k + 1 < front.size(); k += 2) fl.push_back({front[k], front[k + 1], true});
+  if (!fl.empty())
+    propagate_front(c, fl);
+  else
+    collision_recurse_front(c, 0, 0, &fl);
+  front.clear();
+  for (const auto& e : fl) {
+    front.push_back(e.left);
+    front.push_back(e.right);
+  }
   if (st) *st = c.st;
   return c.n_contacts;
 }

@@ -87,6 +87,13 @@ struct CollideStats {
 size_t collide_mesh(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2,
                     size_t num_max_contacts, std::vector<int>& contacts, CollideStats* st);
 
+// collide(node, front_list) with a BVHFrontList (collision_node-inl.h:72-82,
+// traversal_recurse-inl.h:82-129, 463-521): front holds the (b1, b2) list in and out;
+// an empty list starts from the roots.  Contacts are kept while fewer than
+// num_max_contacts exist; the traversal does not stop early.
+size_t collide_mesh_front(const Mesh& m1, const Tf& tf1, const Mesh& m2, const Tf& tf2, size_t num_max_contacts,
+                          std::vector<int>& front, std::vector<int>& contacts, CollideStats* st);
+
 // fcl::collide with enable_contact = true: each intersecting triangle pair adds 0..2
 // contacts with position and normal in the world frame and the penetration depth
 // (mesh_collision_traversal_node-inl.h:579-600, intersect-inl.h:800-886).

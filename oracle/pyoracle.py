@@ -141,6 +141,28 @@ def collide_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = 
         cap = int(total)
 
 
+def collide_front(m1: Mesh, m2: Mesh, tf2, tf1=None, front=None, num_max_contacts: int = 1):
+    """collide(node, front_list) for one pose: returns (contacts (k,2), new front (m,2),
+    nbv, nleaf).  front: (m,2) int32 node pairs from a previous call, or None / empty."""
+    L = lib()
+    L.orc_collide_front.restype = C.c_int64
+    L.orc_collide_front.argtypes = [C.c_void_p, C.c_void_p, _dp, _dp, C.c_int64, _ip, C.c_int64, _ip, C.c_int64,
+                                    _i64p, _ip, C.c_int64, _i64p, _i64p]
+    fin = np.ascontiguousarray(np.zeros((0, 2), np.int32) if front is None else front, np.int32).reshape(-1, 2)
+    tf2 = np.ascontiguousarray(tf2, np.float64).reshape(12)
+    t1 = None if tf1 is None else _d(np.ascontiguousarray(tf1, np.float64).reshape(12))
+    fcap, ccap = max(1024, 4 * fin.shape[0]), 1024
+    while True:
+        fout = np.zeros((fcap, 2), np.int32)
+        cont = np.zeros((ccap, 2), np.int32)
+        nf, nbv, nleaf = (np.zeros(1, np.int64) for _ in range(3))
+        k = L.orc_collide_front(m1.h, m2.h, t1, _d(tf2), num_max_contacts, _i(fin), fin.shape[0], _i(fout), fcap,
+                                _q(nf), _i(cont), ccap, _q(nbv), _q(nleaf))
+        if nf[0] <= fcap and k <= ccap:
+            return cont[:k].copy(), fout[:nf[0]].copy(), int(nbv[0]), int(nleaf[0])
+        fcap, ccap = max(fcap, int(nf[0])), max(ccap, int(k))
+
+
 def collide_contacts_batch(m1: Mesh, m2: Mesh, tf2: np.ndarray, tf1: np.ndarray | None = None,
                            num_max_contacts: int = 1, nthreads: int = 1):
     """fcl::collide with enable_contact = true.  Returns (counts, ids (total,2) int32,
