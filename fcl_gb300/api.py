@@ -526,11 +526,11 @@ class ContinuousCollisionResult:
 def continuous_collide_batch(meshes, pairs, tf1_beg, tf1_end, tf2_beg, tf2_end, pair_of_query=None,
                              num_max_iterations=10, toc_err=1e-4, motion="trans", solver="naive", precision="fp32",
                              stream=None):
-    """Batched fcl::continuousCollide on mesh pairs (naive solver; motion "trans" (FCL's
-    default), "linear" or "screw").
+    """Batched fcl::continuousCollide on mesh pairs (solver "naive" (FCL's default) or
+    "conservative_advancement"; motion "trans" (FCL's default), "linear" or "screw").
     Returns is_collide (n,), time_of_contact (n,), contact_tf1/contact_tf2 (n,3,4; zero
-    where no collision).  numpy inputs use the host entry point, torch CUDA tensors the
-    device one."""
+    where no collision) and, with conservative advancement on numpy inputs, iterations
+    (n,).  numpy inputs use the host entry point, torch CUDA tensors the device one."""
     pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
     req = N.CcdRequest(int(num_max_iterations), float(toc_err), CCDM[motion], CCDC[solver], _prec(precision), 0)
     hs = _handles(meshes)
@@ -561,12 +561,17 @@ def continuous_collide_batch(meshes, pairs, tf1_beg, tf1_end, tf2_beg, tf2_end, 
     toc = np.zeros(n)
     c1 = np.zeros((n, 3, 4))
     c2 = np.zeros((n, 3, 4))
-    res = N.CcdResult(hit.ctypes.data, toc.ctypes.data, c1.ctypes.data, c2.ctypes.data)
+    its = np.zeros(n, np.int32) if solver == "conservative_advancement" else None
+    res = N.CcdResult(hit.ctypes.data, toc.ctypes.data, c1.ctypes.data, c2.ctypes.data,
+                      None if its is None else its.ctypes.data)
     N.check(N.lib().fclgpu_continuous_collide_batch(
         hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n, None if pq is None else pq.ctypes.data,
         None if a0 is None else a0.ctypes.data, None if a1 is None else a1.ctypes.data, b0.ctypes.data,
         b1.ctypes.data, C.byref(req), C.byref(res), stream), "fclgpu_continuous_collide_batch")
-    return {"is_collide": hit, "time_of_contact": toc, "contact_tf1": c1, "contact_tf2": c2}
+    out = {"is_collide": hit, "time_of_contact": toc, "contact_tf1": c1, "contact_tf2": c2}
+    if its is not None:
+        out["iterations"] = its
+    return out
 
 
 def continuousCollide(o1: CollisionObject, tf1_end, o2: CollisionObject, tf2_end,

@@ -880,12 +880,21 @@ int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_meshes, const
 namespace {
 struct CcdScratch {
   DevBuf tfa, tfb, pq, counts, offsets, in_pq, in_a0, in_a1, in_b0, in_b1, out_hit, out_toc, out_tf1, out_tf2;
+  DevBuf status, out_iter;
 };
 CcdScratch g_ccd;
 
 int ccd_samples(const fclgpu_ccd_request* req, int64_t* n_iter) {
-  if (req->solver_type != FCLGPU_CCDC_NAIVE)
-    return fail(FCLGPU_ERR_UNSUPPORTED, "only the naive continuous-collision solver is on the GPU path");
+  if (req->solver_type != FCLGPU_CCDC_NAIVE && req->solver_type != FCLGPU_CCDC_CONSERVATIVE_ADVANCEMENT)
+    return fail(FCLGPU_ERR_UNSUPPORTED,
+                "only the naive and conservative-advancement continuous-collision solvers are on the GPU path");
+  if (req->solver_type == FCLGPU_CCDC_CONSERVATIVE_ADVANCEMENT) {  // samples nothing; t_err is FCL's 1e-5
+    if (req->motion_type != FCLGPU_CCDM_TRANS && req->motion_type != FCLGPU_CCDM_LINEAR &&
+        req->motion_type != FCLGPU_CCDM_SCREW)
+      return fail(FCLGPU_ERR_UNSUPPORTED, "the spline motion is not on the GPU path");
+    *n_iter = 0;
+    return FCLGPU_OK;
+  }
   if (req->motion_type != FCLGPU_CCDM_TRANS && req->motion_type != FCLGPU_CCDM_LINEAR &&
       req->motion_type != FCLGPU_CCDM_SCREW)
     return fail(FCLGPU_ERR_UNSUPPORTED, "the spline motion is not on the GPU path");
@@ -914,6 +923,57 @@ int fclgpu_continuous_collide_batch_device(const fclgpu_mesh* meshes, int32_t nu
   int64_t n_iter = 0;
   int rc = ccd_samples(req, &n_iter);
   if (rc) return rc;
+  if (req->solver_type == FCLGPU_CCDC_CONSERVATIVE_ADVANCEMENT) {
+    if (n >= (int64_t)1 << 31) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "batch too large");
+    std::lock_guard<std::recursive_mutex> lk(g_mu);
+    rc = ensure_init();
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int stack = 64;
+    rc = prepare_tables(meshes, num_meshes, pairs_host, num_pairs, s, &stack);
+    if (rc) return rc;
+    if (n == 0) return FCLGPU_OK;
+    CK(g_ccd.counts.ensure(4 * (size_t)n), "ccd scratch");
+    CK(g_ccd.offsets.ensure(8 * (size_t)(n + 1)), "ccd scratch");
+    CK(g_ccd.status.ensure(4), "ccd scratch");
+    CK(cudaMemsetAsync(g_ccd.status.p, 0, 4, s), "ccd scratch");
+    // the discrete collide at the start poses (the motions' transforms before integrate)
+    fclgpu_collide_request cr{};
+    cr.num_max_contacts = 1;
+    cr.precision = req->precision;
+    int64_t total = 0;
+    rc = collide_core(n, pair_of_query, tf1_beg, tf2_beg, &cr, (int32_t*)g_ccd.counts.p, (int64_t*)g_ccd.offsets.p,
+                      nullptr, nullptr, nullptr, stack, s, &total);
+    if (rc) return rc;
+    CcdLaunch L{};
+    L.pair_of_query = pair_of_query;
+    L.tf1_beg = tf1_beg;
+    L.tf1_end = tf1_end;
+    L.tf2_beg = tf2_beg;
+    L.tf2_end = tf2_end;
+    L.n = n;
+    L.motion = req->motion_type;
+    L.is_collide = res->is_collide;
+    L.toc = res->time_of_contact;
+    L.contact_tf1 = res->contact_tf1;
+    L.contact_tf2 = res->contact_tf2;
+    L.meshes = (const DevMesh*)g_scratch.meshes.p;
+    L.pairs = (const int2*)g_scratch.pairs.p;
+    L.num_pairs = num_pairs;
+    L.hit0 = (const int32_t*)g_ccd.counts.p;
+    // each iteration that does not end the loop advances t by more than 1e-5
+    L.max_iterations = 200000;
+    L.iterations = res->iterations;
+    L.status = (unsigned*)g_ccd.status.p;
+    CK(launch_ccd_ca(L, stack, s), "conservative advancement");
+    unsigned st = 0;
+    CK(cudaMemcpyAsync(&st, g_ccd.status.p, 4, cudaMemcpyDeviceToHost, s), "status");
+    CK(cudaStreamSynchronize(s), "conservative advancement");
+    if (st & DEV_ERR_PAIR) return fail(FCLGPU_ERR_DEVICE_STATUS, "a query's pair index lies outside the pair table");
+    if (st & DEV_ERR_STACK) return fail(FCLGPU_ERR_DEVICE_STATUS, "traversal stack overflow");
+    if (st & DEV_ERR_ITERATIONS) return fail(FCLGPU_ERR_DEVICE_STATUS, "conservative advancement iteration cap");
+    return FCLGPU_OK;
+  }
   if (n * std::max<int64_t>(n_iter, 1) >= (int64_t)1 << 31)
     return fail(FCLGPU_ERR_INVALID_ARGUMENT, "queries x samples must stay below 2^31");
   std::lock_guard<std::recursive_mutex> lk(g_mu);
@@ -1003,6 +1063,10 @@ int fclgpu_continuous_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshe
   dr.time_of_contact = (double*)G.out_toc.p;
   dr.contact_tf1 = res->contact_tf1 ? (double*)G.out_tf1.p : nullptr;
   dr.contact_tf2 = res->contact_tf2 ? (double*)G.out_tf2.p : nullptr;
+  if (res->iterations) {
+    CK(G.out_iter.ensure(4 * nn), "outputs");
+    dr.iterations = (int32_t*)G.out_iter.p;
+  }
   rc = fclgpu_continuous_collide_batch_device(meshes, num_meshes, pairs_host, num_pairs, n,
                                               pair_of_query ? (const int32_t*)G.in_pq.p : nullptr,
                                               tf1_beg ? (const double*)G.in_a0.p : nullptr,
@@ -1014,6 +1078,7 @@ int fclgpu_continuous_collide_batch(const fclgpu_mesh* meshes, int32_t num_meshe
     CK(cudaMemcpyAsync(res->time_of_contact, G.out_toc.p, 8 * n, cudaMemcpyDeviceToHost, s), "d2h");
     if (res->contact_tf1) CK(cudaMemcpyAsync(res->contact_tf1, G.out_tf1.p, 96 * n, cudaMemcpyDeviceToHost, s), "d2h");
     if (res->contact_tf2) CK(cudaMemcpyAsync(res->contact_tf2, G.out_tf2.p, 96 * n, cudaMemcpyDeviceToHost, s), "d2h");
+    if (res->iterations) CK(cudaMemcpyAsync(res->iterations, dr.iterations, 4 * n, cudaMemcpyDeviceToHost, s), "d2h");
   }
   CK(cudaStreamSynchronize(s), "continuous collide");
   return FCLGPU_OK;

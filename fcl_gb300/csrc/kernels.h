@@ -14,6 +14,7 @@ enum : uint32_t {
   DEV_ERR_ITEMS = 4u,     // work-item scratch overflow
   DEV_ERR_PAIR = 8u,      // a query's pair index lies outside the pair table
   DEV_ERR_BARRIER = 16u,  // a persistent launch's grid barrier timed out
+  DEV_ERR_ITERATIONS = 32u,  // a conservative-advancement query reached its iteration cap
 };
 
 // Counters shared by one batch launch (device scratch).
@@ -158,8 +159,19 @@ struct CcdLaunch {
   double* toc;
   double* contact_tf1;       // may be null
   double* contact_tf2;       // may be null
+  // conservative advancement (launch_ccd_ca): mesh and pair tables, the collide counts at
+  // the start poses, the iteration cap and count, the status word
+  const DevMesh* meshes;
+  const int2* pairs;
+  int32_t num_pairs;
+  const int32_t* hit0;
+  int64_t max_iterations;
+  int32_t* iterations;       // may be null
+  unsigned* status;
 };
 cudaError_t launch_ccd_poses(const CcdLaunch& L, cudaStream_t s);
+// One thread per motion: FCL's conservative advancement with the oriented OBBRSS node.
+cudaError_t launch_ccd_ca(const CcdLaunch& L, int stack_entries, cudaStream_t s);
 cudaError_t launch_ccd_reduce(const CcdLaunch& L, const int32_t* counts, cudaStream_t s);
 
 // precision: 0 = plain FP64, 1 = FP32 with FP64 recheck.  stack_entries: 64 or 256.

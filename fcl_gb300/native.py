@@ -69,7 +69,7 @@ class CcdRequest(C.Structure):
 
 class CcdResult(C.Structure):
     _fields_ = [("is_collide", C.c_void_p), ("time_of_contact", C.c_void_p), ("contact_tf1", C.c_void_p),
-                ("contact_tf2", C.c_void_p)]
+                ("contact_tf2", C.c_void_p), ("iterations", C.c_void_p)]
 
 
 class DistanceRequest(C.Structure):

@@ -260,6 +260,17 @@ FCLGPU_API int fclgpu_collide_contacts(const fclgpu_mesh* meshes, int32_t num_me
  * time of contact (1 and no collision otherwise).  n_iter must be 0 (no sample: no
  * collision) or >= 2 (FCL divides 0 by 0 at n_iter = 1).  The linear and screw motions use
  * sin/cos/tan/atan2, whose device results differ from a host's in the last bits.  Other
+ * CCDC_CONSERVATIVE_ADVANCEMENT runs FCL's conservative advancement as its oriented
+ * OBBRSS node computes it (conservativeAdvancementMeshOriented with
+ * MeshConservativeAdvancementTraversalNodeOBBRSS, conservative_advancement_func_matrix-inl.h
+ * :149-218, mesh_conservative_advancement_traversal_node-inl.h:417-747): a discrete collide
+ * at the start poses, then distance traversals at the motions' current transforms, each
+ * advancing t by the smallest d / (motion bound) over the tested triangle pairs until the
+ * step is <= 1e-5 (contact) or t passes 1; num_max_iterations and toc_err are not used, and
+ * `iterations` (optional) receives the traversal count per query.  (fcl::continuousCollide's
+ * dispatch table reaches the generic node for BVHModel<OBBRSS>, which re-transforms and
+ * rebuilds copies of both meshes in the world frame every iteration; the oriented node is
+ * FCL's OBBRSS specialisation of the same algorithm.)  The remaining
  * solvers and the spline motion return FCLGPU_ERR_UNSUPPORTED.  tf1_beg/tf1_end may both be NULL (identity).  Outputs per query:
  * is_collide, time_of_contact, and for colliding queries contact_tf1/contact_tf2 (the
  * sampled transforms at the time of contact, 12 doubles each; other entries are left
@@ -282,6 +293,7 @@ typedef struct {
   double* time_of_contact;    /* ::time_of_contact */
   double* contact_tf1;        /* ::contact_tf1 (3x4 row-major), may be NULL */
   double* contact_tf2;        /* ::contact_tf2, may be NULL */
+  int32_t* iterations;        /* conservative advancement: traversals per query, may be NULL */
 } fclgpu_ccd_result;
 
 FCLGPU_API int fclgpu_continuous_collide_batch_device(

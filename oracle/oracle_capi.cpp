@@ -245,6 +245,35 @@ void orc_ccd_batch(void* h1, void* h2, int64_t n, const double* a0, const double
   });
 }
 
+// Batched continuous collide with conservative advancement over n motions of one mesh
+// pair (the oriented OBBRSS node); outputs as orc_ccd_batch plus the iteration count.
+void orc_ca_batch(void* h1, void* h2, int64_t n, const double* a0, const double* a1, const double* b0,
+                  const double* b1, int motion, int nthreads, int* hit, double* toc, double* ctf1, double* ctf2,
+                  int64_t* iters) {
+  const Mesh* m1 = static_cast<Mesh*>(h1);
+  const Mesh* m2 = static_cast<Mesh*>(h2);
+  parallel_for(n, nthreads, [&](int64_t i, int) {
+    Tf ta0 = a0 ? load_tf(a0 + 12 * i) : identity_tf();
+    Tf ta1 = a1 ? load_tf(a1 + 12 * i) : identity_tf();
+    Tf tb0 = load_tf(b0 + 12 * i), tb1 = load_tf(b1 + 12 * i);
+    Tf ca, cb;
+    double t;
+    bool h = continuous_collide_ca(*m1, ta0, ta1, *m2, tb0, tb1, motion, t, ca, cb, iters ? iters + i : nullptr);
+    hit[i] = h ? 1 : 0;
+    toc[i] = t;
+    if (h) {
+      for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) {
+          ctf1[12 * i + 4 * r + c] = ca.R(r, c);
+          ctf2[12 * i + 4 * r + c] = cb.R(r, c);
+        }
+        ctf1[12 * i + 4 * r + 3] = ca.t[r];
+        ctf2[12 * i + 4 * r + 3] = cb.t[r];
+      }
+    }
+  });
+}
+
 // Batched fcl::distance over n poses of one mesh pair.  Outputs per pose: dist,
 // (b1,b2), and when nearest != 0 the two world-frame nearest points (6 doubles).
 void orc_distance_batch(void* h1, void* h2, int64_t n, const double* tf1, const double* tf2,

@@ -110,6 +110,16 @@ int tri_contact_info(const V3 P[3], const V3 Qm[3], V3 cp[2], V3& normal, double
 // fcl::continuousCollide with the naive solver and the translation (0), linear (1) or
 // screw (2) motion; toc = time of
 // contact (1 without collision), ca / cb = the sampled transforms at that time.
+// continuousCollide with CCDC_CONSERVATIVE_ADVANCEMENT on BVHModel<OBBRSS> pairs, as
+// FCL's oriented OBBRSS node computes it (conservativeAdvancementMeshOriented with
+// MeshConservativeAdvancementTraversalNodeOBBRSS, conservative_advancement_func_matrix-inl.h
+// :149-218, mesh_conservative_advancement_traversal_node-inl.h:417-747): a discrete collide
+// at the start; then repeated distance traversals under the current relative transform,
+// each giving delta_t = min over tested triangle pairs of d / (motion bound along the
+// pair's direction), advancing t by delta_t until delta_t <= 1e-5 (contact) or t > 1.
+bool continuous_collide_ca(const Mesh& m1, const Tf& a0, const Tf& a1, const Mesh& m2, const Tf& b0, const Tf& b1,
+                           int motion, double& toc, Tf& ca, Tf& cb, int64_t* iterations);
+
 bool continuous_collide_naive(const Mesh& m1, const Tf& a0, const Tf& a1, const Mesh& m2, const Tf& b0,
                               const Tf& b1, size_t num_max_iterations, double toc_err, int motion, double& toc,
                               Tf& ca, Tf& cb);

@@ -49,6 +49,8 @@ def lib():
         L.orc_ccd_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, C.c_int64, C.c_double,
                                     C.c_int, C.c_int, _ip, _dp, _dp, _dp]
         L.orc_motion.argtypes = [C.c_int, C.c_int64, _dp, _dp, _dp, _dp]
+        L.orc_ca_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _dp,
+                                   _dp, _dp, _i64p]
         L.orc_tri_contact_batch.argtypes = [C.c_int64, _dp, _dp, _ip, _dp, _dp, _dp]
         L.orc_distance_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int, C.c_int,
                                          _dp, _ip, _dp, _i64p, _i64p]
@@ -205,6 +207,24 @@ def continuous_collide_batch(m1: Mesh, m2: Mesh, tf2_beg, tf2_end, tf1_beg=None,
                         _d(b1), num_max_iterations, toc_err, _MOTIONS[motion], nthreads, _i(hit), _d(toc), _d(c1),
                         _d(c2))
     return hit, toc, c1, c2
+
+
+def ca_batch(m1: Mesh, m2: Mesh, b0, b1, a0=None, a1=None, motion: str = "trans", nthreads: int = 1):
+    """continuousCollide with conservative advancement (the oriented OBBRSS node) for n
+    motions -> (hit, toc, contact_tf1 (n,3,4), contact_tf2, iterations)."""
+    b0 = np.ascontiguousarray(b0, np.float64).reshape(-1, 12)
+    b1 = np.ascontiguousarray(b1, np.float64).reshape(-1, 12)
+    n = b0.shape[0]
+    a0 = None if a0 is None else np.ascontiguousarray(a0, np.float64).reshape(-1, 12)
+    a1 = None if a1 is None else np.ascontiguousarray(a1, np.float64).reshape(-1, 12)
+    hit = np.zeros(n, np.int32)
+    toc = np.zeros(n)
+    c1 = np.zeros((n, 3, 4))
+    c2 = np.zeros((n, 3, 4))
+    it = np.zeros(n, np.int64)
+    lib().orc_ca_batch(m1.h, m2.h, n, None if a0 is None else _d(a0), None if a1 is None else _d(a1), _d(b0),
+                       _d(b1), _MOTIONS[motion], nthreads, _i(hit), _d(toc), _d(c1), _d(c2), _q(it))
+    return hit, toc, c1, c2, it
 
 
 def motion(beg, end, t, kind: str = "trans"):

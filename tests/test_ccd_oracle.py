@@ -118,3 +118,33 @@ def test_screw_without_rotation_keeps_fcl_scaling():
     f = O.motion(b0, b1, np.full(50, 0.5), "screw")
     d = b1[:, :, 3] - b0[:, :, 3]
     assert np.allclose(f[:, :, 3], b0[:, :, 3] + d * (0.5 * np.linalg.norm(d, axis=1))[:, None], atol=1e-12)
+
+
+def test_conservative_advancement_oracle_properties():
+    """The oracle's conservative advancement (FCL's oriented OBBRSS node): a contact it
+    reports lies within the last step's reach of touching, its time is within one
+    fine-sampling step of the first colliding sample for these smooth translations, and a
+    motion that never collides runs to t = 1."""
+    va, ta = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, 1)
+    vb, tb = W.perturbed_ellipsoid(5, (0.5, 0.4, 0.6), 0.01, 2)
+    A, B = O.Mesh(va, ta), O.Mesh(vb, tb)
+    n = 12
+    b0 = W.random_poses(n, -3, 3, 5)
+    b1 = b0.copy()
+    b1[:, :, 3] = -b1[:, :, 3]  # through the other mesh
+    hit, toc, _, c2, it = O.ca_batch(A, B, b0, b1, nthreads=4)
+    assert hit.all() and (it >= 2).all()
+    d, _, _, _, _ = O.distance_batch(A, B, c2)
+    assert (d < 1e-4).all()
+    ts = np.linspace(0, 1, 801)
+    for q in range(n):
+        poses = O.motion(np.repeat(b0[q].reshape(1, 12), ts.size, 0), np.repeat(b1[q].reshape(1, 12), ts.size, 0), ts)
+        c, _, _, _ = O.collide_batch(A, B, poses.reshape(-1, 12), num_max_contacts=1)
+        first = ts[np.argmax(c > 0)]
+        assert abs(toc[q] - first) <= 2.5e-3
+    far = b0.copy()
+    far[:, :, 3] += 20.0
+    far1 = far.copy()
+    far1[:, 0, 3] += 1.0
+    hit, toc, _, _, _ = O.ca_batch(A, B, far, far1)
+    assert not hit.any() and (toc == 1.0).all()

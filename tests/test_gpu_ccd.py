@@ -100,7 +100,8 @@ def test_ccd_rejects_what_fcl_cannot_run_here(gpu_lib):
     (va, ta), (vb, tb) = _meshes()
     ms = [api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)]
     _, _, b0, b1 = _motions(4, 1, False)
-    for kw in ({"motion": "spline"}, {"solver": "conservative_advancement"}):
+    for kw in ({"motion": "spline"}, {"solver": "ray_shooting"}, {"solver": "polynomial_solver"},
+               {"motion": "spline", "solver": "conservative_advancement"}):
         with pytest.raises(N.FclGpuError) as e:
             api.continuous_collide_batch(ms, [[0, 1]], None, None, b0, b1, **kw)
         assert e.value.code == N.FCLGPU_ERR_UNSUPPORTED
@@ -120,3 +121,58 @@ def test_continuous_collide_mirror(gpu_lib):
         assert t == ref[1][q] and res.is_collide == bool(ref[0][q])
         if res.is_collide:
             assert np.array_equal(res.contact_tf1, ref[2][q]) and np.array_equal(res.contact_tf2, ref[3][q])
+
+
+@pytest.mark.parametrize("both", [False, True])
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_conservative_advancement_matches_oracle(gpu_lib, both, prec):
+    """Conservative advancement with the translation motion: flags, times of contact,
+    transforms at contact and the number of traversals bit for bit against the oracle's
+    restatement of FCL's oriented OBBRSS node (the start collide runs in either form)."""
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(400, 41, both)
+    ref = O.ca_batch(O.Mesh(va, ta), O.Mesh(vb, tb), b0, b1, a0, a1, nthreads=8)
+    g = api.continuous_collide_batch([A, B], [[0, 1]], a0, a1, b0, b1, solver="conservative_advancement",
+                                     precision=prec)
+    _same(g, ref[:4])
+    assert np.array_equal(g["iterations"], ref[4])
+    assert 0 < ref[0].sum() < 400 and ref[4].max() >= 3
+
+
+@pytest.mark.parametrize("kind", ["linear", "screw"])
+def test_conservative_advancement_rotating_motions(gpu_lib, kind):
+    """With the linear and screw motions (sin/cos/tan/atan2 differ from the host's in the
+    last bits) the times of contact agree with the oracle's to 1e-9 and the flags exactly."""
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(300, 43, True)
+    b1[:, :, :3] = W.random_poses(300, 0, 0, 44)[:, :, :3]
+    ref = O.ca_batch(O.Mesh(va, ta), O.Mesh(vb, tb), b0, b1, a0, a1, motion=kind, nthreads=8)
+    g = api.continuous_collide_batch([A, B], [[0, 1]], a0, a1, b0, b1, solver="conservative_advancement",
+                                     motion=kind)
+    assert np.array_equal(g["is_collide"], ref[0])
+    assert np.allclose(g["time_of_contact"], ref[1], rtol=0, atol=1e-9)
+    assert np.allclose(g["contact_tf2"], ref[3], rtol=0, atol=1e-9)
+    assert 0 < ref[0].sum() < 300
+
+
+def test_conservative_advancement_mirror_and_contact_distance(gpu_lib):
+    """api.continuousCollide with CCDC_CONSERVATIVE_ADVANCEMENT equals the batch; at a
+    reported time of contact the meshes are within the last step's reach of touching (the
+    oracle's distance at the contact transforms is below 1e-4)."""
+    (va, ta), (vb, tb) = _meshes()
+    A, B = api.BVHModel.from_arrays(va, ta), api.BVHModel.from_arrays(vb, tb)
+    a0, a1, b0, b1 = _motions(60, 45, True)
+    batch = api.continuous_collide_batch([A, B], [[0, 1]], a0, a1, b0, b1, solver="conservative_advancement")
+    req = api.ContinuousCollisionRequest(ccd_solver_type="conservative_advancement")
+    MA, MB = O.Mesh(va, ta), O.Mesh(vb, tb)
+    for q in range(60):
+        res = api.ContinuousCollisionResult()
+        t = api.continuousCollide(api.CollisionObject(A, a0[q]), a1[q], api.CollisionObject(B, b0[q]), b1[q], req,
+                                  res)
+        assert t == batch["time_of_contact"][q] and res.is_collide == bool(batch["is_collide"][q])
+        if res.is_collide:
+            d, _, _, _, _ = O.distance_batch(MA, MB, res.contact_tf2[None], res.contact_tf1[None])
+            assert d[0] < 1e-4
+    assert batch["is_collide"].sum() > 0
