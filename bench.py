@@ -303,6 +303,8 @@ def run_secondary(args, meshes, stream, flush):
         return {"contacts": _run_contacts(args, meshes, stream, flush)}
     if args.only == "ccd":
         return {"ccd": _run_ccd(args, meshes, stream, flush)}
+    if args.only == "front":
+        return {"front": _run_front(args, meshes, stream, flush)}
     if meshes is None:  # the distance section alone: the mesh set of the C1/C2 workloads
         w1 = _workload(args, 0)
         meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
@@ -346,6 +348,7 @@ def run_secondary(args, meshes, stream, flush):
     out["refit"] = _run_refit(args, stream, flush)
     out["contacts"] = _run_contacts(args, meshes, stream, flush)
     out["ccd"] = _run_ccd(args, meshes, stream, flush)
+    out["front"] = _run_front(args, meshes, stream, flush)
     return out
 
 
@@ -413,6 +416,135 @@ def _run_ccd(args, meshes, stream, flush):
         dt = time.perf_counter() - t_start
         out["cpu_baseline"] = {"value": k / dt, "unit": "motions/s", "cores": threads, "kind": "port",
                                "sample": f"{k} of the motions"}
+    out["conservative_advancement"] = _run_ca(args, w1, meshes, pq, b0, b1, stream, flush)
+    return out
+
+
+def _run_ca(args, w1, meshes, pq, b0, b1, stream, flush):
+    """The same motions with CCDC_CONSERVATIVE_ADVANCEMENT (FCL's oriented OBBRSS node, FP64
+    distance traversals until the step is <= 1e-5): a 20 % subset, host inputs through the
+    C ABI (the start collide batch and the CA kernel); oracle check on 100 motions."""
+    from fcl_gb300 import api
+    from oracle import pyoracle as O
+    rng = np.random.default_rng(23)
+    n = max(1, b0.shape[0] // 5)
+    sel = np.sort(rng.choice(b0.shape[0], size=n, replace=False))
+    q, a, b = pq[sel], b0[sel], b1[sel]
+    res = {}
+
+    def run():
+        res["g"] = api.continuous_collide_batch(meshes, w1.pairs, None, None, a, b, pair_of_query=q,
+                                                solver="conservative_advancement")
+
+    for _ in range(1):
+        run()
+    t_start = time.perf_counter()
+    run()
+    dt = time.perf_counter() - t_start
+    g = res["g"]
+    out = {"workload": f"{n} of those translation motions, conservative advancement", "motions": n,
+           "ms_per_step": dt * 1e3, "value": n / dt, "unit": "motions/s", "timing": "host wall clock, host inputs",
+           "colliding_fraction": float(g["is_collide"].mean()), "mean_iterations": float(g["iterations"].mean()),
+           "max_iterations": int(g["iterations"].max())}
+    chk = np.sort(rng.choice(n, size=min(100, n), replace=False))
+    om = {}
+    ok = True
+    for k in chk:
+        p0, p1 = w1.pairs[q[k]]
+        for m in (p0, p1):
+            if m not in om:
+                om[m] = O.Mesh(*w1.meshes[m])
+        h, t, _, _, it = O.ca_batch(om[p0], om[p1], a[k:k + 1], b[k:k + 1])
+        ok &= bool(h[0] == g["is_collide"][k] and t[0] == g["time_of_contact"][k] and it[0] == g["iterations"][k])
+    out["oracle_checked_motions"] = int(chk.size)
+    out["exact_vs_oracle"] = ok
+    if not args.no_cpu:
+        threads = O.hardware_threads()
+        k = min(n, 400)
+        s2 = np.sort(rng.choice(n, size=k, replace=False))
+        for p in np.unique(q[s2]):
+            for m in w1.pairs[p]:
+                if m not in om:
+                    om[m] = O.Mesh(*w1.meshes[m])
+        t_start = time.perf_counter()
+        for p in np.unique(q[s2]):
+            idx = s2[q[s2] == p]
+            p0, p1 = w1.pairs[p]
+            O.ca_batch(om[p0], om[p1], a[idx], b[idx], nthreads=threads)
+        dt = time.perf_counter() - t_start
+        out["cpu_baseline"] = {"value": k / dt, "unit": "motions/s", "cores": threads, "kind": "port",
+                               "sample": f"{k} of the motions"}
+    return out
+
+
+def _run_front(args, meshes, stream, flush):
+    """Front-list coherence (collide(node, front_list)) on the C1 mesh pairs: 10,000 C1
+    poses; fronts built by a full traversal, then propagated to nearby poses (translation
+    +-0.01, rotation +-0.005 rad per Euler angle) with num_max_contacts = 1, against a plain
+    collide at the new poses; host inputs through the C ABI, host wall clock.  Oracle check
+    of 50 propagated queries (contacts, fronts, statistics)."""
+    from fcl_gb300 import api
+    from oracle import pyoracle as O
+    w1 = _workload(args, 0)
+    if meshes is None:
+        meshes = [api.BVHModel.from_arrays(*m) for m in w1.meshes]
+    rng = np.random.default_rng(29)
+    n = max(1, int(10_000 * args.scale))
+    sel = np.sort(rng.choice(w1.n, size=n, replace=False))
+    pq, tf0 = w1.pair[sel], w1.tf2[sel].reshape(-1, 3, 4)
+    ang = rng.uniform(-0.005, 0.005, (n, 3))
+    tf1 = tf0.copy()
+    for k in range(n):
+        cx, cy, cz = np.cos(ang[k])
+        sx, sy, sz = np.sin(ang[k])
+        Rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+        Ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+        Rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+        tf1[k, :, :3] = tf0[k, :, :3] @ (Rx @ Ry @ Rz)
+    tf1[:, :, 3] += rng.uniform(-0.01, 0.01, (n, 3))
+    t_start = time.perf_counter()
+    base = api.collide_front_batch(meshes, w1.pairs, None, tf0, pair_of_query=pq, num_max_contacts=1 << 30)
+    build_s = time.perf_counter() - t_start
+    fronts = base["fronts"]
+    res = {}
+
+    def prop():
+        res["f"] = api.collide_front_batch(meshes, w1.pairs, None, tf1, fronts=fronts, pair_of_query=pq,
+                                           num_max_contacts=1, statistics=True)
+
+    def plain():
+        res["p"] = api.collide_batch(meshes, w1.pairs, None, tf1, pair_of_query=pq, num_max_contacts=1,
+                                     statistics=True)
+
+    prop()
+    plain()
+    t_start = time.perf_counter()
+    prop()
+    t_prop = time.perf_counter() - t_start
+    t_start = time.perf_counter()
+    plain()
+    t_plain = time.perf_counter() - t_start
+    f, p = res["f"], res["p"]
+    out = {"workload": f"{n} C1 poses, fronts propagated to nearby poses, num_max_contacts=1", "queries": n,
+           "front_entries": int(base["front"].shape[0]), "front_build_s": build_s,
+           "propagate_ms": t_prop * 1e3, "value": n / t_prop, "unit": "queries/s",
+           "plain_collide_ms": t_plain * 1e3, "timing": "host wall clock, host inputs",
+           "same_verdicts_as_plain": bool(np.array_equal(f["counts"] > 0, p["counts"] > 0)),
+           "bv_tests_propagate": int(f["num_bv_tests"].sum()), "bv_tests_plain": int(p["num_bv_tests"].sum())}
+    chk = np.sort(rng.choice(n, size=min(50, n), replace=False))
+    om = {}
+    ok = True
+    for k in chk:
+        a, b = w1.pairs[pq[k]]
+        for m in (a, b):
+            if m not in om:
+                om[m] = O.Mesh(*w1.meshes[m])
+        c, fr, nbv, _ = O.collide_front(om[a], om[b], tf1[k], front=fronts[k], num_max_contacts=1)
+        lo, hi = f["contact_offsets"][k], f["contact_offsets"][k + 1]
+        ok &= bool(np.array_equal(f["contacts"][lo:hi], c) and np.array_equal(f["fronts"][k], fr)
+                   and f["num_bv_tests"][k] == nbv)
+    out["oracle_checked_queries"] = int(chk.size)
+    out["exact_vs_oracle"] = ok
     return out
 
 
@@ -889,7 +1021,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the motion-checking request loop")
     ap.add_argument("--no-tune", action="store_true", help="keep the default collide knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the distance and convex-pair batches")
-    ap.add_argument("--only", default="all", choices=["all", "c0", "distance", "shapes", "refit", "contacts", "ccd", "serving"],
+    ap.add_argument("--only", default="all", choices=["all", "c0", "distance", "shapes", "refit", "contacts", "ccd", "front",
+                                                      "serving"],
                     help="run one section alone (profiling); the full line needs 'all'")
     ap.add_argument("--tune-sample", type=int, default=131072, help="queries the autotuner times each setting on")
     ap.add_argument("--serve-objects", type=int, default=0, help="scene objects (0 = the seeded logU draw)")

@@ -241,10 +241,13 @@ __global__ void __launch_bounds__(128) k_msr_tests(MeshShapeLaunch L, const int3
 // stage-1 hits count at once, undecided leaves run the FP64 GJK in this thread -- at
 // most kSerialGjk of them; the pair's further undecided leaves are deferred to one
 // thread each (k_msr_deferred) and the pair is recounted after them (k_msr_recount).
-// The count is min(max_contacts, intersecting leaves) either way; the serial part keeps
-// the early stop for the usual pair whose first undecided leaf intersects, the deferral
-// bounds the tail of a pair with many near misses.
-constexpr int kSerialGjk = 4;
+// The count is min(max_contacts, intersecting leaves) either way.  The serial part would
+// keep the early stop for a pair whose first undecided leaf intersects, but one FP64 GJK
+// per thread leaves most lanes of a warp idle at GB300's FP64 rate; deferring every
+// undecided leaf (one full warp of GJKs at a time) measured faster on the motion-checking
+// server (256-request burst 2,099 -> 2,405 requests/s, 16-request burst's mesh-shape
+// phase 71 -> 56 ms for budgets 4 -> 0), so the budget is 0.
+constexpr int kSerialGjk = 0;
 
 // Lists the pair's contacts c0..c-1: its first intersecting leaves of this round in
 // DFS order, as (pair, rank, triangle) records.
