@@ -706,6 +706,45 @@ def _run_refit(args, stream, flush):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": t.shape[0] / dt, "unit": "triangles/s", "cores": 1, "kind": "port",
                                "sample": "one refit of the same mesh (FCL's refit is sequential)"}
+    out["build"] = _run_build(args, v, t)
+    return out
+
+
+def _run_build(args, v, t):
+    """BVHModel construction (beginModel / addSubModel / endModel, FCL's PCA fit and MEAN
+    split) of the same mesh on the GPU (fclgpu_mesh_create_on_device, host arrays in,
+    wall clock including the upload) against the host build of the same library, and the
+    GPU rebuild of endReplaceModel(refit = false); the trees are compared node for node.
+    CPU baseline = the oracle's build (one thread; FCL's build is sequential)."""
+    from fcl_gb300 import api
+    api.BVHModel.from_arrays(v, t, build="device")  # warm-up
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        d = api.BVHModel.from_arrays(v, t, build="device")
+        ts.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    h = api.BVHModel.from_arrays(v, t)
+    host_s = time.perf_counter() - t0
+    same = all(np.array_equal(a.view(np.uint64), b.view(np.uint64)) if a.dtype == np.float64 else np.array_equal(a, b)
+               for a, b in zip(h.get_nodes(), d.get_nodes()))
+    rng = np.random.default_rng(12)
+    nv = v + rng.normal(0, 0.01, v.shape)
+    t0 = time.perf_counter()
+    d.replace_vertices(nv, refit=False)
+    rebuild_s = time.perf_counter() - t0
+    dev_s = float(np.median(ts))
+    out = {"workload": f"OBBRSS build of the {t.shape[0]}-triangle mesh", "triangles": int(t.shape[0]),
+           "ms_per_build": dev_s * 1e3, "value": t.shape[0] / dev_s, "unit": "triangles/s",
+           "host_build_ms": host_s * 1e3, "rebuild_ms": rebuild_s * 1e3, "timing": "host wall clock",
+           "identical_to_host_build": bool(same)}
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        t0 = time.perf_counter()
+        O.Mesh(v, t)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": t.shape[0] / dt, "unit": "triangles/s", "cores": 1, "kind": "port",
+                               "sample": "one build of the same mesh"}
     return out
 
 

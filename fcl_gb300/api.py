@@ -32,14 +32,18 @@ def _prec(p) -> int:
 
 
 class BVHModel:
-    """BVHModel<OBBRSS<double>>: triangles + vertices, BVH built by endModel()."""
+    """BVHModel<OBBRSS<double>>: triangles + vertices, BVH built by endModel() on the host
+    (build="host") or on the GPU (build="device"; the same tree node for node)."""
 
-    def __init__(self):
+    def __init__(self, build: str = "host"):
         self._verts: list[np.ndarray] = []
         self._tris: list[np.ndarray] = []
         self._nv = 0
         self.handle = None
         self.build_state = "empty"
+        if build not in ("host", "device"):
+            raise N.FclGpuError(N.FCLGPU_ERR_INVALID_ARGUMENT, "BVHModel", "build is 'host' or 'device'")
+        self.build = build
 
     # geometry/bvh/BVH_model-inl.h:207-248
     def beginModel(self, num_tris: int = 0, num_vertices: int = 0) -> int:
@@ -73,8 +77,13 @@ class BVHModel:
         self.vertices = np.ascontiguousarray(V)
         self.tri_indices = np.ascontiguousarray(T, dtype=np.int32)
         h = C.c_void_p()
-        N.check(N.lib().fclgpu_mesh_create(self.vertices.ctypes.data, V.shape[0], self.tri_indices.ctypes.data,
-                                           T.shape[0], C.byref(h)), "fclgpu_mesh_create")
+        if self.build == "device":
+            N.check(N.lib().fclgpu_mesh_create_on_device(self.vertices.ctypes.data, V.shape[0],
+                                                         self.tri_indices.ctypes.data, T.shape[0], C.byref(h), None),
+                    "fclgpu_mesh_create_on_device")
+        else:
+            N.check(N.lib().fclgpu_mesh_create(self.vertices.ctypes.data, V.shape[0], self.tri_indices.ctypes.data,
+                                               T.shape[0], C.byref(h)), "fclgpu_mesh_create")
         self.handle = h
         self.build_state = "processed"
         return 0
@@ -104,27 +113,30 @@ class BVHModel:
         return 0
 
     def endUpdateModel(self, refit: bool = True, bottomup: bool = True) -> int:
-        """The default (refit = True, bottomup = True) is the GPU bottom-up refit; a
-        rebuild or a top-down refit is not on the GPU path."""
+        """Bottom-up only (the top-down refit is not on the GPU path): refit = True refits
+        the tree on the GPU; refit = False rebuilds it on the GPU and then refits it over
+        both frames, as FCL does."""
         if self.build_state != "update_begun":
             return -8
-        if not (refit and bottomup):
+        if not bottomup:
             raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "endUpdateModel", "only the bottom-up refit")
         V = np.concatenate(self._upd) if self._upd else np.zeros((0, 3))
         if V.shape[0] != self.num_vertices:
             return -7  # BVH_ERR_INCORRECT_DATA
-        self.update_vertices(V)
+        self.update_vertices(V, refit=refit)
         return 0
 
-    def update_vertices(self, vertices, stream=None) -> None:
-        """beginUpdateModel + updateVertex for all vertices + endUpdateModel() at once:
+    def update_vertices(self, vertices, stream=None, refit: bool = True) -> None:
+        """beginUpdateModel + updateVertex for all vertices + endUpdateModel(refit) at once:
         numpy (host) or a CUDA torch tensor (device), (nv, 3) float64."""
         if hasattr(vertices, "data_ptr"):
-            N.check(N.lib().fclgpu_mesh_update_device(self.handle, vertices.data_ptr(), vertices.shape[0],
-                                                      stream), "fclgpu_mesh_update_device")
+            N.check(N.lib().fclgpu_mesh_update_model_device(self.handle, vertices.data_ptr(), vertices.shape[0],
+                                                            int(bool(refit)), stream),
+                    "fclgpu_mesh_update_model_device")
         else:
             V = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
-            N.check(N.lib().fclgpu_mesh_update(self.handle, V.ctypes.data, V.shape[0], stream), "fclgpu_mesh_update")
+            N.check(N.lib().fclgpu_mesh_update_model(self.handle, V.ctypes.data, V.shape[0], int(bool(refit)), stream),
+                    "fclgpu_mesh_update_model")
             self.vertices = V
         self.build_state = "updated"
 
@@ -152,34 +164,34 @@ class BVHModel:
         return 0
 
     def endReplaceModel(self, refit: bool = True, bottomup: bool = True) -> int:
-        """The default (refit = True, bottomup = True) is the GPU bottom-up refit without a
-        previous frame; a rebuild or a top-down refit is not on the GPU path."""
+        """Bottom-up only: refit = True refits the tree on the GPU without a previous frame;
+        refit = False rebuilds it on the GPU (buildTree)."""
         if self.build_state != "replace_begun":
             return -8
-        if not (refit and bottomup):
+        if not bottomup:
             raise N.FclGpuError(N.FCLGPU_ERR_UNSUPPORTED, "endReplaceModel", "only the bottom-up refit")
         V = np.concatenate(self._upd) if self._upd else np.zeros((0, 3))
         if V.shape[0] != self.num_vertices:
             return -7  # BVH_ERR_INCORRECT_DATA
-        self.replace_vertices(V)
+        self.replace_vertices(V, refit=refit)
         return 0
 
-    def replace_vertices(self, vertices, stream=None) -> None:
-        """beginReplaceModel + replaceVertex for all vertices + endReplaceModel() at once:
-        numpy (host) or a CUDA torch tensor (device), (nv, 3) float64."""
+    def replace_vertices(self, vertices, stream=None, refit: bool = True) -> None:
+        """beginReplaceModel + replaceVertex for all vertices + endReplaceModel(refit) at
+        once: numpy (host) or a CUDA torch tensor (device), (nv, 3) float64."""
         if hasattr(vertices, "data_ptr"):
-            N.check(N.lib().fclgpu_mesh_replace_device(self.handle, vertices.data_ptr(), vertices.shape[0], 1,
-                                                       stream), "fclgpu_mesh_replace_device")
+            N.check(N.lib().fclgpu_mesh_replace_device(self.handle, vertices.data_ptr(), vertices.shape[0],
+                                                       int(bool(refit)), stream), "fclgpu_mesh_replace_device")
         else:
             V = np.ascontiguousarray(vertices, dtype=np.float64).reshape(-1, 3)
-            N.check(N.lib().fclgpu_mesh_replace(self.handle, V.ctypes.data, V.shape[0], 1, stream),
+            N.check(N.lib().fclgpu_mesh_replace(self.handle, V.ctypes.data, V.shape[0], int(bool(refit)), stream),
                     "fclgpu_mesh_replace")
             self.vertices = V
         self.build_state = "processed"
 
     @classmethod
-    def from_arrays(cls, vertices, triangles) -> "BVHModel":
-        m = cls()
+    def from_arrays(cls, vertices, triangles, build: str = "host") -> "BVHModel":
+        m = cls(build=build)
         m.beginModel()
         m.addSubModel(vertices, triangles)
         m.endModel()

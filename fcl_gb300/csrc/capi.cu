@@ -24,6 +24,7 @@ using namespace fclgpu;
 namespace fclgpu {
 void set_error_detail(const std::string& what);
 }
+int repack_mesh(fclgpu_mesh m, cudaStream_t s);  // mesh_refit.cu
 
 namespace {
 
@@ -522,13 +523,128 @@ int fclgpu_get_collide_tuning(int32_t* budget, int32_t* leaf_batch_steps, int32_
   return FCLGPU_OK;
 }
 
-int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out) {
+}  // extern "C"
+
+namespace {
+// BVHModel::computeLocalAABB (geometry/bvh/BVH_model-inl.h:1080-1100) and the first vertex
+void set_local_aabb(fclgpu_mesh_s* m, const double* verts, int64_t nv) {
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = std::numeric_limits<double>::max();
+    hi[k] = -std::numeric_limits<double>::max();
+  }
+  for (int64_t i = 0; i < nv; ++i)
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], verts[3 * i + k]);
+      hi[k] = std::max(hi[k], verts[3 * i + k]);
+    }
+  double c[3], r = 0;
+  for (int k = 0; k < 3; ++k) c[k] = (lo[k] + hi[k]) * 0.5;
+  for (int64_t i = 0; i < nv; ++i) {
+    const double dx = c[0] - verts[3 * i], dy = c[1] - verts[3 * i + 1], dz = c[2] - verts[3 * i + 2];
+    const double q = (dx * dx + dy * dy) + dz * dz;
+    if (q > r) r = q;
+  }
+  for (int k = 0; k < 3; ++k) {
+    m->aabb_local[k] = lo[k];
+    m->aabb_local[3 + k] = hi[k];
+    m->aabb_center[k] = c[k];
+    m->first_vertex[k] = verts[k];
+  }
+  m->aabb_radius = std::sqrt(r);
+}
+
+int check_model(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out) {
   if (!out) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "out is null");
   *out = nullptr;
   if (nv <= 0 || nt <= 0 || !verts || !tris) return fail(FCLGPU_ERR_EMPTY_MODEL, "empty model");
   if (nt > (1 << 29)) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "too many triangles");
   for (int64_t i = 0; i < 3 * nt; ++i)
     if (tris[i] < 0 || tris[i] >= nv) return fail(FCLGPU_ERR_INVALID_ARGUMENT, "triangle index out of range");
+  return FCLGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int fclgpu_mesh_create_on_device(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out,
+                                 void* stream) {
+  int rc = check_model(verts, nv, tris, nt, out);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  rc = ensure_init();
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  fclgpu_mesh_s* m = new fclgpu_mesh_s();
+  const size_t nn = 2 * (size_t)nt - 1;
+  auto alloc = [&](void** p, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess) m->allocations.push_back(*p);
+    return e;
+  };
+  void *p_n64, *p_r64, *p_v64, *p_t, *p_n32, *p_s64, *p_r32, *p_t32, *p_lv;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = alloc(&p_n64, sizeof(NodeD) * nn);
+  if (e == cudaSuccess) e = alloc(&p_r64, sizeof(RssD) * nn);
+  if (e == cudaSuccess) e = alloc(&p_v64, sizeof(double) * 3 * nv);
+  if (e == cudaSuccess) e = alloc(&p_t, sizeof(int32_t) * 3 * nt);
+  if (e == cudaSuccess) e = alloc(&p_n32, sizeof(float) * 16 * nn);
+  if (e == cudaSuccess) e = alloc(&p_s64, sizeof(double) * nn);
+  if (e == cudaSuccess) e = alloc(&p_r32, sizeof(float) * 20 * nn);
+  if (e == cudaSuccess) e = alloc(&p_t32, sizeof(float) * 12 * nt);
+  if (e == cudaSuccess) e = alloc(&p_lv, sizeof(int32_t) * std::max<size_t>(nn / 2, 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(p_v64, verts, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(p_t, tris, sizeof(int32_t) * 3 * nt, cudaMemcpyHostToDevice, s);
+  int maxd = 0;
+  std::vector<int64_t> off;
+  if (e == cudaSuccess)
+    e = build_bvh_device((const double*)p_v64, (const int32_t*)p_t, (int)nt, (NodeD*)p_n64, (RssD*)p_r64, off,
+                         (int32_t*)p_lv, &maxd, s);
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(s);
+    for (void* p : m->allocations) cudaFree(p);
+    delete m;
+    return cuda_fail(e, "device build");
+  }
+  DevMesh& d = m->dev;
+  d.nodes64 = (const NodeD*)p_n64;
+  d.rss64 = (const RssD*)p_r64;
+  d.verts64 = (const double*)p_v64;
+  d.tris = (const int32_t*)p_t;
+  d.nodes32 = p_n32;
+  d.size64 = (const double*)p_s64;
+  d.rss32 = p_r32;
+  d.tri32 = p_t32;
+  d.n_nodes = (int32_t)nn;
+  d.n_tris = (int32_t)nt;
+  d.n_verts = (int32_t)nv;
+  d.max_depth = maxd;
+  d.refitted = 0;
+  d.pad2 = 0;
+  m->levels = (int32_t*)p_lv;
+  m->level_off = off;
+  rc = repack_mesh(m, s);
+  if (rc) {
+    for (void* p : m->allocations) cudaFree(p);
+    delete m;
+    return rc;
+  }
+  set_local_aabb(m, verts, nv);
+  m->info.num_vertices = nv;
+  m->info.num_tris = nt;
+  m->info.num_nodes = (int64_t)nn;
+  m->info.max_depth = maxd;
+  m->info.reserved = 0;
+  m->info.device_bytes = (int64_t)(nn * (sizeof(NodeD) + sizeof(RssD) + 64 + 8 + 80) + nv * 24 + nt * (12 + 48));
+  *out = m;
+  return FCLGPU_OK;
+}
+
+int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt, fclgpu_mesh* out) {
+  {
+    const int rc0 = check_model(verts, nv, tris, nt, out);
+    if (rc0) return rc0;
+  }
   // the host build runs outside the lock so several meshes can be built in parallel
   HostBVH bvh;
   if (build_obbrss(verts, nv, tris, nt, bvh) != 0) return fail(FCLGPU_ERR_EMPTY_MODEL, "empty model");
@@ -582,32 +698,7 @@ int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int
   d.rmax = pk.rmax * (1.0 + 1e-12);
   d.refitted = 0;
   d.pad2 = 0;
-  {
-    double lo[3], hi[3];
-    for (int k = 0; k < 3; ++k) {
-      lo[k] = std::numeric_limits<double>::max();
-      hi[k] = -std::numeric_limits<double>::max();
-    }
-    for (int64_t i = 0; i < nv; ++i)
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], verts[3 * i + k]);
-        hi[k] = std::max(hi[k], verts[3 * i + k]);
-      }
-    double c[3], r = 0;
-    for (int k = 0; k < 3; ++k) c[k] = (lo[k] + hi[k]) * 0.5;
-    for (int64_t i = 0; i < nv; ++i) {
-      const double dx = c[0] - verts[3 * i], dy = c[1] - verts[3 * i + 1], dz = c[2] - verts[3 * i + 2];
-      const double q = (dx * dx + dy * dy) + dz * dz;
-      if (q > r) r = q;
-    }
-    for (int k = 0; k < 3; ++k) {
-      m->aabb_local[k] = lo[k];
-      m->aabb_local[3 + k] = hi[k];
-      m->aabb_center[k] = c[k];
-      m->first_vertex[k] = verts[k];
-    }
-    m->aabb_radius = std::sqrt(r);
-  }
+  set_local_aabb(m, verts, nv);
   {
     // internal nodes by depth, for the level-by-level refit
     std::vector<int32_t> depth(nn, 0);

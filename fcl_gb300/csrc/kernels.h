@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "fclgpu_types.h"
 
 namespace fclgpu {
@@ -213,6 +215,13 @@ struct FrontLaunch {
 };
 cudaError_t launch_collide_front(const FrontLaunch& L, int precision, int stack_entries, bool fill, cudaStream_t s);
 cudaError_t launch_front_lengths(const int32_t* nseg, int64_t n, int32_t* len, cudaStream_t s);
+
+// Device construction of an OBBRSS tree (bvh_build_device.cu), bit-identical to the host
+// build: V (3 doubles per vertex) and T (3 int32 per triangle) on the device; writes the
+// 2 nt - 1 nodes and RSS volumes, the internal node ids by depth (level_ids, nt - 1
+// entries, offsets in level_off) and the depth of the deepest leaf.  Synchronises s.
+cudaError_t build_bvh_device(const double* V, const int32_t* T, int nt, NodeD* nodes, RssD* rss,
+                             std::vector<int64_t>& level_off, int32_t* level_ids, int* max_depth, cudaStream_t s);
 
 extern int64_t g_kernel_launches;
 extern double g_last_shape_ms;

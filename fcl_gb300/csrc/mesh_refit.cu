@@ -131,43 +131,19 @@ int refit_cuda(cudaError_t e, const char* where) {
   return e == cudaErrorMemoryAllocation ? FCLGPU_ERR_OUT_OF_MEMORY : FCLGPU_ERR_CUDA;
 }
 
-// verts: device pointer with the new positions (3 doubles per vertex).  replace = false:
-// update (the current frame becomes the previous one, leaves fit both frames); true:
-// replace (FCL drops the previous frame, leaves fit the new triangle alone).
-int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool replace) {
+}  // namespace
+
+// The FP32 store (nodes, sizes, RSS, triangles) from the FP64 nodes and vertices, and the
+// magnitude bounds the FP32 filters use.  Synchronises s.
+int repack_mesh(fclgpu_mesh m, cudaStream_t s) {
   DevMesh& d = m->dev;
-  const size_t vbytes = sizeof(double) * 3 * (size_t)d.n_verts;
-  cudaError_t e = cudaSuccess;
-  if (!m->prev_verts) {
-    e = cudaMalloc(&m->prev_verts, vbytes);
-    if (e != cudaSuccess) return refit_cuda(e, "previous-frame vertices");
-    m->allocations.push_back(m->prev_verts);
-  }
+  cudaError_t e;
   if (!m->bounds) {
-    e = cudaMalloc(&m->bounds, 4 * sizeof(unsigned long long));
-    if (e != cudaSuccess) return refit_cuda(e, "refit bounds");
+    if ((e = cudaMalloc(&m->bounds, 4 * sizeof(unsigned long long)))) return refit_cuda(e, "refit bounds");
     m->allocations.push_back(m->bounds);
   }
-  double* cur = const_cast<double*>(d.verts64);
-  // beginUpdateModel: the current frame becomes the previous one; updateVertex: the new
-  // positions become the current frame
-  if (!replace && (e = cudaMemcpyAsync(m->prev_verts, cur, vbytes, cudaMemcpyDeviceToDevice, s)))
-    return refit_cuda(e, "frames");
-  if ((e = cudaMemcpyAsync(cur, verts, vbytes, cudaMemcpyDeviceToDevice, s))) return refit_cuda(e, "frames");
   if ((e = cudaMemsetAsync(m->bounds, 0, 4 * sizeof(unsigned long long), s))) return refit_cuda(e, "bounds");
-  NodeD* nodes = const_cast<NodeD*>(d.nodes64);
-  RssD* rss = const_cast<RssD*>(d.rss64);
-  k_refit_leaves<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, replace ? nullptr : (const double*)m->prev_verts,
-                                                           nodes, rss);
-  ++g_kernel_launches;
-  for (size_t l = m->level_off.size() - 1; l-- > 0;) {  // deepest level first
-    const int64_t a = m->level_off[l], b = m->level_off[l + 1];
-    if (b > a) {
-      k_refit_level<<<grid_for(b - a, 128), 128, 0, s>>>(m->levels + a, (int)(b - a), nodes, rss);
-      ++g_kernel_launches;
-    }
-  }
-  k_refit_pack<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, nodes, rss, (float4*)d.nodes32,
+  k_refit_pack<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, d.nodes64, d.rss64, (float4*)d.nodes32,
                                                           const_cast<double*>(d.size64), (float4*)d.rss32,
                                                           (unsigned long long*)m->bounds);
   k_refit_tris<<<grid_for(std::max(d.n_tris, 3 * d.n_verts), 128), 128, 0, s>>>(d, (float4*)d.tri32,
@@ -183,8 +159,59 @@ int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool r
   d.vmax = bd[0] * (1.0 + 1e-12);
   d.cmax = bd[1] * (1.0 + 1e-12);
   d.rmax = bd[2] * (1.0 + 1e-12);
-  d.refitted = 1;
   m->info.max_abs_coord = bd[0];
+  return FCLGPU_OK;
+}
+
+namespace {
+
+// verts: device pointer with the new positions (3 doubles per vertex).  replace = false:
+// update (the current frame becomes the previous one, leaves fit both frames); true:
+// replace (FCL drops the previous frame, leaves fit the new triangle alone).  rebuild:
+// endUpdateModel / endReplaceModel with refit = false (BVH_model-inl.h:594-620, 703-734):
+// buildTree on the new vertices (the device build, bvh_build_device.cu), followed for an
+// update by the bottom-up refit over both frames, as FCL does.
+int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool replace, bool rebuild) {
+  DevMesh& d = m->dev;
+  const size_t vbytes = sizeof(double) * 3 * (size_t)d.n_verts;
+  cudaError_t e = cudaSuccess;
+  if (!m->prev_verts) {
+    e = cudaMalloc(&m->prev_verts, vbytes);
+    if (e != cudaSuccess) return refit_cuda(e, "previous-frame vertices");
+    m->allocations.push_back(m->prev_verts);
+  }
+  double* cur = const_cast<double*>(d.verts64);
+  // beginUpdateModel: the current frame becomes the previous one; updateVertex: the new
+  // positions become the current frame
+  if (!replace && (e = cudaMemcpyAsync(m->prev_verts, cur, vbytes, cudaMemcpyDeviceToDevice, s)))
+    return refit_cuda(e, "frames");
+  if ((e = cudaMemcpyAsync(cur, verts, vbytes, cudaMemcpyDeviceToDevice, s))) return refit_cuda(e, "frames");
+  NodeD* nodes = const_cast<NodeD*>(d.nodes64);
+  RssD* rss = const_cast<RssD*>(d.rss64);
+  if (rebuild) {
+    int maxd = 0;
+    std::vector<int64_t> off;
+    if ((e = build_bvh_device(cur, d.tris, d.n_tris, nodes, rss, off, m->levels, &maxd, s)))
+      return refit_cuda(e, "device build");
+    m->level_off = off;
+    d.max_depth = maxd;
+    m->info.max_depth = maxd;
+  }
+  if (!(rebuild && replace)) {
+    k_refit_leaves<<<grid_for(d.n_nodes, 128), 128, 0, s>>>(d, replace ? nullptr : (const double*)m->prev_verts,
+                                                             nodes, rss);
+    ++g_kernel_launches;
+    for (size_t l = m->level_off.size() - 1; l-- > 0;) {  // deepest level first
+      const int64_t a = m->level_off[l], b = m->level_off[l + 1];
+      if (b > a) {
+        k_refit_level<<<grid_for(b - a, 128), 128, 0, s>>>(m->levels + a, (int)(b - a), nodes, rss);
+        ++g_kernel_launches;
+      }
+    }
+  }
+  int rc = repack_mesh(m, s);
+  if (rc) return rc;
+  d.refitted = (rebuild && replace) ? 0 : 1;  // a fresh build's volumes contain their geometry
   if ((e = cudaMemcpyAsync(m->first_vertex, cur, 3 * sizeof(double), cudaMemcpyDeviceToHost, s)) ||
       (e = cudaStreamSynchronize(s)))
     return refit_cuda(e, "refit");
@@ -196,15 +223,17 @@ int refit_from_device(fclgpu_mesh m, const double* verts, cudaStream_t s, bool r
 extern "C" {
 
 namespace {
-int move_vertices_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace) {
+int move_vertices_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace,
+                         bool rebuild = false) {
   if (!mesh || !verts) return refit_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   if (nv != mesh->dev.n_verts)
     return refit_fail(FCLGPU_ERR_INCORRECT_DATA, "the updated model must have the same number of vertices");
   std::lock_guard<std::mutex> lk(g_refit_mu);
-  return refit_from_device(mesh, verts, (cudaStream_t)stream, replace);
+  return refit_from_device(mesh, verts, (cudaStream_t)stream, replace, rebuild);
 }
 
-int move_vertices_host(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace) {
+int move_vertices_host(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream, bool replace,
+                       bool rebuild = false) {
   if (!mesh || !verts) return refit_fail(FCLGPU_ERR_INVALID_ARGUMENT, "null argument");
   if (nv != mesh->dev.n_verts)
     return refit_fail(FCLGPU_ERR_INCORRECT_DATA, "the updated model must have the same number of vertices");
@@ -215,7 +244,7 @@ int move_vertices_host(fclgpu_mesh mesh, const double* verts, int64_t nv, void* 
   cudaError_t e = cudaMalloc(&staging, vbytes);
   if (e != cudaSuccess) return refit_cuda(e, "staging");
   e = cudaMemcpyAsync(staging, verts, vbytes, cudaMemcpyHostToDevice, s);
-  int rc = e == cudaSuccess ? refit_from_device(mesh, staging, s, replace) : refit_cuda(e, "h2d");
+  int rc = e == cudaSuccess ? refit_from_device(mesh, staging, s, replace, rebuild) : refit_cuda(e, "h2d");
   cudaStreamSynchronize(s);
   cudaFree(staging);
   return rc;
@@ -231,13 +260,19 @@ int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* 
 }
 
 int fclgpu_mesh_replace_device(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
-  if (!refit) return refit_fail(FCLGPU_ERR_UNSUPPORTED, "endReplaceModel(refit = false) rebuilds on the host");
-  return move_vertices_device(mesh, verts, nv, stream, true);
+  return move_vertices_device(mesh, verts, nv, stream, true, refit == 0);
 }
 
 int fclgpu_mesh_replace(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
-  if (!refit) return refit_fail(FCLGPU_ERR_UNSUPPORTED, "endReplaceModel(refit = false) rebuilds on the host");
-  return move_vertices_host(mesh, verts, nv, stream, true);
+  return move_vertices_host(mesh, verts, nv, stream, true, refit == 0);
+}
+
+int fclgpu_mesh_update_model_device(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
+  return move_vertices_device(mesh, verts, nv, stream, false, refit == 0);
+}
+
+int fclgpu_mesh_update_model(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit, void* stream) {
+  return move_vertices_host(mesh, verts, nv, stream, false, refit == 0);
 }
 
 }  // extern "C"

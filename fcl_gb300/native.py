@@ -176,6 +176,9 @@ _SIGS = {
     "fclgpu_last_error_detail": (C.c_char_p, []),
     "fclgpu_init": (C.c_int, [C.c_int]),
     "fclgpu_mesh_create": (C.c_int, [_VP, C.c_int64, _VP, C.c_int64, C.POINTER(C.c_void_p)]),
+    "fclgpu_mesh_create_on_device": (C.c_int, [_VP, C.c_int64, _VP, C.c_int64, C.POINTER(C.c_void_p), _VP]),
+    "fclgpu_mesh_update_model": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP]),
+    "fclgpu_mesh_update_model_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP]),
     "fclgpu_mesh_destroy": (C.c_int, [_VP]),
     "fclgpu_mesh_get_info": (C.c_int, [_VP, C.POINTER(MeshInfo)]),
     "fclgpu_mesh_get_nodes": (C.c_int, [_VP, _VP, _VP]),

@@ -90,9 +90,14 @@ typedef struct {
 
 /* Builds the OBBRSS BVH on the host (FCL's top-down PCA fit, MEAN split) from
  * nv vertices (3 doubles each) and nt triangles (3 int32 each) and uploads a
- * device mirror (FP64 nodes and vertices, packed FP32 nodes and triangles). */
+ * device mirror (FP64 nodes and vertices, packed FP32 nodes and triangles).
+ * fclgpu_mesh_create_on_device builds the same tree on the GPU (node for node
+ * bit-identical: the same sums in the same order, FCL's node ids) from host arrays;
+ * it synchronises `stream`. */
 FCLGPU_API int fclgpu_mesh_create(const double* verts, int64_t nv, const int32_t* tris, int64_t nt,
                                   fclgpu_mesh* out);
+FCLGPU_API int fclgpu_mesh_create_on_device(const double* verts, int64_t nv, const int32_t* tris, int64_t nt,
+                                            fclgpu_mesh* out, void* stream);
 FCLGPU_API int fclgpu_mesh_destroy(fclgpu_mesh mesh);
 FCLGPU_API int fclgpu_mesh_get_info(fclgpu_mesh mesh, fclgpu_mesh_info* info);
 /* Copies the FP64 BVH back to the host: per node 30 doubles (obb.axis row-major 9,
@@ -111,13 +116,22 @@ FCLGPU_API int fclgpu_mesh_get_nodes(fclgpu_mesh mesh, double* nodes30, int32_t*
  * vertex.  Synchronises the stream. */
 FCLGPU_API int fclgpu_mesh_update(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
 FCLGPU_API int fclgpu_mesh_update_device(fclgpu_mesh mesh, const double* verts, int64_t nv, void* stream);
+/* endUpdateModel(refit, bottomup = true) (BVH_model-inl.h:703-734): refit != 0 is
+ * fclgpu_mesh_update; refit = 0 rebuilds the tree on the new vertices on the GPU
+ * (buildTree, as fclgpu_mesh_create_on_device) and then refits it bottom-up over both
+ * frames, as FCL does.  Synchronises the stream. */
+FCLGPU_API int fclgpu_mesh_update_model(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit,
+                                        void* stream);
+FCLGPU_API int fclgpu_mesh_update_model_device(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit,
+                                               void* stream);
 
 /* Replaces the mesh's vertices: BVHModel::beginReplaceModel + replaceVertex (all
  * vertices, in order) + endReplaceModel(refit, bottomup = true) (BVH_model-inl.h:521-620,
  * 961-1027).  FCL drops the previous frame here, so each leaf is refitted to its new
  * triangle alone (fit3 of OBB and RSS), the internal nodes as in fclgpu_mesh_update; a
- * later update uses these vertices as its previous frame.  refit = 0 (rebuild the tree)
- * returns FCLGPU_ERR_UNSUPPORTED: create a new mesh instead.  Synchronises the stream. */
+ * later update uses these vertices as its previous frame.  refit = 0 rebuilds the tree on
+ * the new vertices on the GPU (buildTree, BVH_model-inl.h:612-615).  Synchronises the
+ * stream. */
 FCLGPU_API int fclgpu_mesh_replace(fclgpu_mesh mesh, const double* verts, int64_t nv, int32_t refit,
                                    void* stream);
 FCLGPU_API int fclgpu_mesh_replace_device(fclgpu_mesh mesh, const double* verts, int64_t nv,

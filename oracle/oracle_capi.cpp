@@ -83,6 +83,23 @@ void orc_mesh_replace(void* h, const double* verts) {
   replace_refit_bottomup(*m, nv);
 }
 
+// endUpdateModel(refit = false) / endReplaceModel(refit = false) (BVH_model-inl.h:594-620,
+// 703-734): buildTree on the new vertices; an update then refits bottom-up over both frames.
+void orc_mesh_rebuild(void* h, const double* verts, int update) {
+  Mesh* m = static_cast<Mesh*>(h);
+  std::vector<V3> nv(m->verts.size());
+  for (size_t i = 0; i < nv.size(); ++i) nv[i] = mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
+  Mesh built = *m;
+  built.verts = nv;
+  build_bvh(built);
+  m->nodes = built.nodes;
+  m->prim_idx = built.prim_idx;
+  if (update)
+    update_refit_bottomup(*m, nv);  // previous frame: the vertices before the call
+  else
+    m->verts = nv;
+}
+
 int orc_mesh_num_nodes(void* h) { return (int)static_cast<Mesh*>(h)->nodes.size(); }
 
 // Per node: obb.axis (9, row-major), obb.To (3), obb.extent (3), rss.axis (9),

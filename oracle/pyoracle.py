@@ -40,6 +40,7 @@ def lib():
         L.orc_mesh_get_nodes.argtypes = [C.c_void_p, _dp, _ip]
         L.orc_mesh_update.argtypes = [C.c_void_p, _dp]
         L.orc_mesh_replace.argtypes = [C.c_void_p, _dp]
+        L.orc_mesh_rebuild.argtypes = [C.c_void_p, _dp, C.c_int]
         L.orc_collide_batch.restype = C.c_int64
         L.orc_collide_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, _dp, _dp, C.c_int64, C.c_int,
                                         _i64p, _i64p, _i64p, _ip, C.c_int64]
@@ -114,6 +115,15 @@ class Mesh:
         v = np.ascontiguousarray(verts, dtype=np.float64)
         assert v.shape == self.verts.shape
         lib().orc_mesh_replace(self.h, _d(v))
+        self.verts = v
+
+    def rebuild(self, verts: np.ndarray, update: bool) -> None:
+        """endUpdateModel(refit = false) (update) / endReplaceModel(refit = false):
+        the tree rebuilt on the new vertices, then (update) the bottom-up refit over both
+        frames."""
+        v = np.ascontiguousarray(verts, dtype=np.float64)
+        assert v.shape == self.verts.shape
+        lib().orc_mesh_rebuild(self.h, _d(v), int(update))
         self.verts = v
 
     def nodes(self):

@@ -103,8 +103,10 @@ def test_replace_model_bit_exact(gpu_lib):
     g.update_vertices(v2)
     o.update(v2)
     assert np.array_equal(g.get_nodes()[0].view(np.uint64), o.nodes()[0].view(np.uint64))
+    # the top-down refit stays off the GPU path; refit = False rebuilds
+    # (tests/test_gpu_build.py)
     with pytest.raises(N.FclGpuError) as e:
         assert g.beginReplaceModel() == 0
         g.replaceSubModel(v1)
-        g.endReplaceModel(refit=False)
+        g.endReplaceModel(bottomup=False)
     assert e.value.code == N.FCLGPU_ERR_UNSUPPORTED
