@@ -32,14 +32,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "queries/s batched FP32+FP64-recheck vs plain GPU (exact hits); p50/p99 request ms"
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the collide round kernel
-# per C1 step, from ncu on two small cases of the same workload (5 % and 20 % of the
-# poses, the 128-register variant the autotuner picks): 83.36 GB at 55,143 queries and
-# 211.44 GB at 220,586.  Traffic grows less than in proportion to the queries (the poses
-# of one mesh pair share its tree in L2), so a full step is priced by the straight line
-# through the two points, a + b * queries.
-C1_TRAFFIC_A = 40.663e9
-C1_TRAFFIC_B = 774190.0  # bytes per query
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the collide kernel (all
+# rounds in one cooperative launch) per C1 step, from ncu on two small cases of the same
+# workload (5 % and 20 % of the poses, the 128-register variant the autotuner picks; mean
+# of 5 steps each): 82.94 GB at 55,143 queries and 212.52 GB at 220,586.  Traffic grows less
+# than in proportion to the queries (the poses of one mesh pair share its tree in L2), so a
+# full step is priced by the straight line through the two points, a + b * queries.
+C1_TRAFFIC_A = 39.75e9
+C1_TRAFFIC_B = 783226.0  # bytes per query
 C1_TRAFFIC_VARIANT = 1
 UNIT = "queries/s"
 WORKLOAD = "c1_exhaustive_contacts_64pairs_500-200k_tris"
@@ -984,7 +984,7 @@ def run_gpu(args):
     traffic = C1_TRAFFIC_A + C1_TRAFFIC_B * n if (default_workload and variant == C1_TRAFFIC_VARIANT) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "peak_kind": peak_kind,
-            "kernel": "k_collide_round_wb (FP32 + FP64 recheck), all rounds of one step",
+            "kernel": "k_collide_persist (FP32 + FP64 recheck, warp-batched leaves), all rounds of one step",
             "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg_bytes,
             "traffic_source": "small-case ncu captures (5 % and 20 % of the poses), linear in the queries",
             "dram_gbs_estimated": None if traffic is None else traffic / (k_ms / 1000.0) / 1e9}
