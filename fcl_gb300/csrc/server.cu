@@ -24,8 +24,10 @@ namespace fclgpu {
 namespace {
 
 constexpr int kMaxLinks = 64;
-// waypoints of one request per step: a request that collides early stops after its
-// first chunk, and long requests share the step with the others
+// waypoints of one request per step: the first chunk is short and each next one twice
+// as long up to kRequestChunk, so a request that collides early stops having checked few
+// waypoints past its contact, and long requests share the step with the others
+constexpr int kFirstChunk = 8;
 constexpr int kRequestChunk = 64;
 
 struct RobotDev {
@@ -114,6 +116,7 @@ struct Request {
   std::vector<double> q;
   int32_t next_wp = 0;  // next waypoint to schedule
   int32_t done_wp = 0;
+  int32_t chunk = kFirstChunk;  // waypoints of its next chunk
   fclgpu_motion_result res;
   Clock::time_point submit;
   bool started = false;
@@ -333,8 +336,9 @@ void worker_loop(fclgpu_server_s* s) {
         if (left <= 0) break;
         const int64_t share = std::max<int64_t>(1, left / (int64_t)remaining);
         --remaining;
-        const int32_t n = (int32_t)std::min<int64_t>(std::min<int64_t>(share, kRequestChunk), r->K - r->next_wp);
+        const int32_t n = (int32_t)std::min<int64_t>(std::min<int64_t>(share, r->chunk), r->K - r->next_wp);
         if (n <= 0) continue;
+        r->chunk = std::min(2 * r->chunk, kRequestChunk);
         chunks.push_back(Chunk{r, r->next_wp, r->next_wp + n});
         r->next_wp += n;
         left -= n;
