@@ -357,6 +357,82 @@ __global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const in
   }
 }
 
+// Collide counts without a contact list: FCL's count is min(max_contacts, intersecting
+// leaves), whatever order the leaves are met in, so one warp works a pair, testing up to
+// 32 of its frontier nodes (a LIFO stack in shared memory) and leaves at a time, and stops
+// at max_contacts or once the pair's group is full.  With pops of 32 and pushes of at most
+// 64 per step the stack stays below 32 (depth + 2) entries.
+constexpr int kMsWarps = 4;
+constexpr int kMsFront = 2048;
+constexpr int kMsWarpMaxDepth = kMsFront / 32 - 4;
+
+__global__ void __launch_bounds__(32 * kMsWarps) k_ms_count_warp(MeshShapeLaunch L) {
+  __shared__ int32_t front[kMsWarps][kMsFront];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long i = (long long)blockIdx.x * kMsWarps + w;
+  if (i >= L.n) return;
+  const unsigned full = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1u;
+  PairGeom g;
+  pair_geom(L, i, g);
+  ShapeBV bv;
+  if (L.bv_src)
+    bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
+  else
+    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
+  ShapeBV32 b32;
+  make_shape_bv32(g.Rm, g.tm, bv, g.m, b32);
+  const int M = L.max_contacts;
+  if (lane == 0) front[w][0] = 0;
+  int size = 1, count = 0;
+  __syncwarp();
+  while (size > 0 && count < M) {
+    if (L.group) {
+      unsigned long long gc = 0;
+      if (lane == 0) gc = *(volatile unsigned long long*)&L.group_count[L.group[i]];
+      gc = __shfl_sync(full, gc, 0);
+      if (gc >= (unsigned long long)L.group_max) break;  // the query has its contacts
+    }
+    const int take = size < 32 ? size : 32;
+    const int b = lane < take ? front[w][size - 1 - lane] : -1;
+    size -= take;
+    __syncwarp();
+    bool ov = false;
+    int child = 0;
+    if (b >= 0) ov = shape_node_overlap(g.m, g.Rm, g.tm, bv, b32, b, &child);
+    const bool inner = ov && child >= 0;
+    const unsigned pm = __ballot_sync(full, inner);
+    if (size + 2 * __popc(pm) > kMsFront) {  // not reached for trees within kMsWarpMaxDepth
+      if (lane == 0) atomicOr(L.status, 1u);  // reported as a stack overflow
+      break;
+    }
+    if (inner) {
+      const int pos = size + 2 * __popc(pm & lt);
+      front[w][pos] = child + 1;
+      front[w][pos + 1] = child;
+    }
+    size += 2 * __popc(pm);
+    bool hit = false;
+    if (ov && child < 0) {
+      double P[9];
+      load_tri_local(g.m, -(child + 1), P);
+      int h = shape_triangle_stage1(g.A, g.Rs, g.ts, P, g.Rm, g.tm);
+      if (h == 1) {
+        SimplexVert V[kSimplexSlots];
+        h = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V) ? 2 : 0;
+      }
+      hit = h == 2;
+    }
+    const int nh = __popc(__ballot_sync(full, hit));
+    if (nh) {
+      count += nh;
+      if (L.group && lane == 0) atomicAdd(&L.group_count[L.group[i]], (unsigned long long)nh);
+    }
+    __syncwarp();
+  }
+  if (lane == 0) L.counts[i] = count < M ? count : M;
+}
+
 // tris[offsets[pair] + rank] = triangle for every record
 __global__ void k_msr_scatter(const int4* rec, const unsigned long long* nrec, const int64_t* offsets, int32_t* tris) {
   const long long n = (long long)*nrec;
@@ -566,6 +642,11 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
   const cudaError_t ep = upload_solver_params(s);
   if (ep != cudaSuccess) return ep;
   std::lock_guard<std::mutex> lk(g_split_mu);
+  if (L.mode == 0 && !L.list_offsets && stack_entries <= kMsWarpMaxDepth) {  // counts only
+    k_ms_count_warp<<<(unsigned)((L.n + kMsWarps - 1) / kMsWarps), 32 * kMsWarps, 0, s>>>(L);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+  }
   return L.mode == 0 ? run_collide_rounds(L, stack_entries, s, g_split_ms)
                      : run_distance_split(L, stack_entries, s, g_split_ms);
 }

@@ -26,9 +26,9 @@ namespace {
 constexpr int kMaxLinks = 64;
 // waypoints of one request per step: the first chunk is short and each next one twice
 // as long up to kRequestChunk, so a request that collides early stops having checked few
-// waypoints past its contact, and long requests share the step with the others
+// waypoints past its contact, and a long contact-free request needs few steps
 constexpr int kFirstChunk = 8;
-constexpr int kRequestChunk = 64;
+constexpr int kRequestChunk = 512;
 
 struct RobotDev {
   int32_t L;
