@@ -1062,7 +1062,11 @@ class DynamicAABBTreeCollisionManager:
         out["node_visits"] = res.total_node_visits
         return out
 
-    def distance_batch(self, refs, tf, nearest_points: bool = True, precision: str = "fp32", stream=None):
+    def distance_batch(self, refs, tf, nearest_points: bool = True, precision: str = "fp32", stream=None,
+                       witnesses: bool = True):
+        """manager.distance(obj, cdata, DefaultDistanceFunction) per query: min_distance,
+        object, ids and nearest_points; witnesses=False asks for the distances and objects
+        alone (the mesh-shape pairs then skip their triangle ids and points)."""
         req = N.BpDistanceRequest(int(nearest_points), _prec(precision))
         if _is_torch(tf):
             import torch
@@ -1085,7 +1089,10 @@ class DynamicAABBTreeCollisionManager:
             out = dict(min_distance=np.zeros(n), object=np.zeros(n, np.int32), ids=np.zeros((n, 2), np.int32),
                        nearest_points=np.zeros((n, 2, 3)))
             res = N.BpDistanceResult(out["min_distance"].ctypes.data, out["object"].ctypes.data,
-                                     out["ids"].ctypes.data, out["nearest_points"].ctypes.data, 0, 0)
+                                     out["ids"].ctypes.data if witnesses else None,
+                                     out["nearest_points"].ctypes.data if witnesses else None, 0, 0)
+            if not witnesses:
+                del out["ids"], out["nearest_points"]
             N.check(N.lib().fclgpu_broadphase_distance(self.handle, refs.ctypes.data, n, tf.ctypes.data,
                                                        C.byref(req), C.byref(res), stream),
                     "fclgpu_broadphase_distance")

@@ -281,7 +281,7 @@ int list_kind(int64_t total, int32_t want, BpCounters* dctr, int64_t* nlist, cud
 // g_bs.x_ltris) and index[slot] = its list position (g_bs.x_index).
 int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQueryView& Q, int64_t total, int mode,
               int64_t max_contacts, BpCounters* dctr, cudaStream_t s, const int32_t* qdone = nullptr,
-              bool lists = false) {
+              bool lists = false, bool witness = true) {
   int64_t nl = 0;
   RCB(list_kind(total, 2, dctr, &nl, s, qdone));
   g_last_mixed = nl;
@@ -335,6 +335,12 @@ int run_mixed(const fclgpu_broadphase_s* bp, const BpSceneView& S, const BpQuery
   L.dist = g_bs.m_dist.as<double>();
   L.tri = g_bs.x_tri.as<int32_t>();
   L.pts = g_bs.m_pts.as<double>();
+  if (mode == 1 && !witness) {  // values only: the triangle ids and points stay unset
+    CKB(cudaMemsetAsync(g_bs.x_tri.p, 0xff, 4 * nl, s), "mixed scratch");
+    CKB(cudaMemsetAsync(g_bs.m_pts.p, 0, 48 * nl, s), "mixed scratch");
+    L.tri = nullptr;
+    L.pts = nullptr;
+  }
   L.nbv = nullptr;
   L.nleaf = nullptr;
   L.status = &dctr->status;
@@ -625,7 +631,9 @@ int distance_core(fclgpu_broadphase_s* bp, const BpQueryView& Q, const fclgpu_br
     CKB(launch_bp_shape_narrow(S, Q, pairs, total, g_bs.kind.as<int32_t>(), PAIR_DISTANCE, nullptr, dist, pts, s),
         "shape narrowphase");
     pc.tick(1);
-    RCB(run_mixed(bp, S, Q, total, 1, 0, dctr, s));
+    // the per-pair triangle and points matter only for ids or nearest points
+    const bool witness = res->ids || (req->enable_nearest_points && res->nearest_points);
+    RCB(run_mixed(bp, S, Q, total, 1, 0, dctr, s, nullptr, false, witness));
     g_phase[1][6] += (double)g_last_mixed;
     pc.tick(2);
     int64_t nl = 0;

@@ -433,6 +433,102 @@ __global__ void __launch_bounds__(32 * kMsWarps) k_ms_count_warp(MeshShapeLaunch
   if (lane == 0) L.counts[i] = count < M ? count : M;
 }
 
+// Distance values without witnesses: FCL's traversal reports the smallest distance of
+// the leaves it visits, and a leaf it prunes lies in a volume at least as far as its
+// running minimum, so the value is the minimum over the mesh's triangles (as for the
+// split form, up to a triangle whose FP64 distance falls below its node's FP64 bound by
+// rounding).  One warp per pair: a LIFO frontier of (node, lower bound) in shared memory,
+// up to 32 entries a step, entries at or beyond the current minimum dropped (FCL's
+// canStop).  The triangle and witness points are not produced (the caller asked for
+// neither).
+constexpr int kMdWarps = 2;
+constexpr int kMdFront = 1024;
+constexpr int kMdWarpMaxDepth = kMdFront / 32 - 4;
+
+__global__ void __launch_bounds__(32 * kMdWarps) k_ms_dist_warp(MeshShapeLaunch L) {
+  __shared__ int32_t fnode[kMdWarps][kMdFront];
+  __shared__ double flb[kMdWarps][kMdFront];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long i = (long long)blockIdx.x * kMdWarps + w;
+  if (i >= L.n) return;
+  const unsigned full = 0xffffffffu;
+  const unsigned lt = (1u << lane) - 1u;
+  PairGeom g;
+  pair_geom(L, i, g);
+  ShapeBV bv;
+  if (L.bv_src)
+    bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
+  else
+    shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
+  M3<double> Ab;
+  for (int k = 0; k < 9; ++k) Ab.m[k] = bv.obb.axis[k];
+  const D3v Tob = v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]);
+  auto bvd = [&](int b) {  // as mesh_shape_collect_distance's node bound
+    const RssD& rs = g.m.rss64[b];
+    M3<double> A2;
+    for (int k = 0; k < 9; ++k) A2.m[k] = rs.axis[k];
+    return rss_distance<double>(g.Rm, g.tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l,
+                                rs.r);
+  };
+  double ub = DBL_MAX;
+  if (lane == 0) {
+    fnode[w][0] = 0;
+    flb[w][0] = -1.0;
+  }
+  int size = 1;
+  __syncwarp();
+  while (size > 0) {
+    const int take = size < 32 ? size : 32;
+    int b = -1;
+    double lb = 0.0;
+    if (lane < take) {
+      b = fnode[w][size - 1 - lane];
+      lb = flb[w][size - 1 - lane];
+    }
+    size -= take;
+    __syncwarp();
+    if (b >= 0 && lb >= ub) b = -1;  // cannot lower the minimum
+    int child = 0;
+    if (b >= 0) child = g.m.nodes64[b].child;
+    const bool inner = b >= 0 && child >= 0;
+    double l1 = 0.0, l2 = 0.0;
+    if (inner) {
+      l1 = bvd(child);
+      l2 = bvd(child + 1);
+    }
+    const bool p1 = inner && l1 < ub, p2 = inner && l2 < ub;
+    const unsigned m1 = __ballot_sync(full, p1), m2 = __ballot_sync(full, p2);
+    const int np = __popc(m1) + __popc(m2);
+    if (size + np > kMdFront) {  // not reached for trees within kMdWarpMaxDepth
+      if (lane == 0) atomicOr(L.status, 1u);
+      break;
+    }
+    int pos = size + __popc(m1 & lt) + __popc(m2 & lt);
+    if (p2) {  // the farther-ordered child below, the nearer popped first: order is free here
+      fnode[w][pos] = child + 1;
+      flb[w][pos] = l2;
+      ++pos;
+    }
+    if (p1) {
+      fnode[w][pos] = child;
+      flb[w][pos] = l1;
+    }
+    size += np;
+    double d = DBL_MAX;
+    if (b >= 0 && child < 0) {
+      double P[9];
+      load_tri_local(g.m, -(child + 1), P);
+      SimplexVert V[kSimplexSlots];
+      D3v ps, pt;
+      shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+    }
+    for (int off = 16; off > 0; off >>= 1) d = fmin(d, __shfl_xor_sync(full, d, off));
+    if (d < ub) ub = d;
+    __syncwarp();
+  }
+  if (lane == 0) L.dist[i] = ub;
+}
+
 // tris[offsets[pair] + rank] = triangle for every record
 __global__ void k_msr_scatter(const int4* rec, const unsigned long long* nrec, const int64_t* offsets, int32_t* tris) {
   const long long n = (long long)*nrec;
@@ -644,6 +740,11 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
   std::lock_guard<std::mutex> lk(g_split_mu);
   if (L.mode == 0 && !L.list_offsets && stack_entries <= kMsWarpMaxDepth) {  // counts only
     k_ms_count_warp<<<(unsigned)((L.n + kMsWarps - 1) / kMsWarps), 32 * kMsWarps, 0, s>>>(L);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+  }
+  if (L.mode == 1 && !L.tri && !L.pts && stack_entries <= kMdWarpMaxDepth) {  // distance values only
+    k_ms_dist_warp<<<(unsigned)((L.n + kMdWarps - 1) / kMdWarps), 32 * kMdWarps, 0, s>>>(L);
     ++g_kernel_launches;
     return cudaGetLastError();
   }

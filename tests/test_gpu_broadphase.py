@@ -245,3 +245,28 @@ def test_broadphase_manager_against_manager(gpu_lib):
     q = np.repeat(np.arange(qgid.shape[0]), c)
     assert [(ct.o1, ct.o2, ct.b1, ct.b2) for ct in res.contacts] == \
         [(int(a), int(b), int(d), int(e)) for (a, d, e), b in zip(trip, q)]
+
+
+def test_distance_values_without_witnesses(gpu_lib):
+    """Distances asked for without ids or nearest points (the motion server's clearance
+    pass): the mesh-shape pairs take their values from one warp per pair; the minimum
+    distances and nearest objects equal the full call's."""
+    shapes = W.random_shapes(64, 71)
+    vt = [W.perturbed_ellipsoid(f, r, 0.01, 72 + k) for k, (f, r) in
+          enumerate([(5, (0.6, 0.4, 0.3)), (7, (0.5, 0.5, 0.5)), (4, (0.8, 0.3, 0.3))])]
+    meshes = [api.BVHModel.from_arrays(v, t) for v, t in vt]
+    ss = api.ShapeSet.from_workload(shapes)
+    rng = np.random.default_rng(73)
+    n, nq = 800, 600
+    kind = (rng.uniform(size=n) < 0.4).astype(np.int32)
+    refs = np.stack([kind, np.where(kind == 1, rng.integers(0, 3, size=n), rng.integers(0, 64, size=n))], 1)
+    mgr = api.DynamicAABBTreeCollisionManager(ss, meshes)
+    mgr.registerObjects(refs.astype(np.int32), W.random_poses(n, 0.0, 16.0, 74))
+    qk = (rng.uniform(size=nq) < 0.5).astype(np.int32)
+    qrefs = np.stack([qk, np.where(qk == 1, rng.integers(0, 3, size=nq), rng.integers(0, 64, size=nq))], 1)
+    qtf = W.random_poses(nq, 0.0, 16.0, 75)
+    full = mgr.distance_batch(qrefs.astype(np.int32), qtf)
+    vals = mgr.distance_batch(qrefs.astype(np.int32), qtf, witnesses=False)
+    assert np.array_equal(vals["min_distance"], full["min_distance"])
+    assert np.array_equal(vals["object"], full["object"])
+    assert (full["min_distance"] > 0).sum() > 100
