@@ -256,6 +256,8 @@ def run_serving(args):
         # broadphase wall-clock phases over the Poisson run (fclgpu_broadphase_last_phase_ms):
         # setup + candidates, shape pairs, mesh-shape pairs, mesh-mesh pairs, reduction
         "phases_ms": {"collide": [round(x, 1) for x in ph[0:5]], "distance": [round(x, 1) for x in ph[8:13]]},
+        # candidates, mesh-shape pairs and mesh-mesh pairs evaluated in those phases
+        "phase_pairs": {"collide": [int(x) for x in ph[5:8]], "distance": [int(x) for x in ph[13:16]]},
         "scene_setup_s": setup_s, "clocks": cs.summary(),
     }
     if not args.no_cpu:

@@ -748,8 +748,11 @@ int fclgpu_broadphase_distance(fclgpu_broadphase bp, const fclgpu_geometry_ref* 
   CKB(pts.ensure(48 * nq), "staging");
   CKB(cudaMemcpyAsync(refs.p, queries, 8 * nq, cudaMemcpyHostToDevice, s), "h2d");
   CKB(cudaMemcpyAsync(tfd.p, tf, 96 * nq, cudaMemcpyHostToDevice, s), "h2d");
-  fclgpu_broadphase_distance_result dr = {d.as<double>(), ob.as<int32_t>(), ids.as<int32_t>(), pts.as<double>(), 0,
-                                          0};
+  // witnesses staged only when the caller asked for them (without, the mesh-shape
+  // pairs take the value-only path)
+  const bool want_pts = res->nearest_points && req->enable_nearest_points;
+  fclgpu_broadphase_distance_result dr = {d.as<double>(), ob.as<int32_t>(), res->ids ? ids.as<int32_t>() : nullptr,
+                                          want_pts ? pts.as<double>() : nullptr, 0, 0};
   int rc = fclgpu_broadphase_distance_device(bp, refs.as<fclgpu_geometry_ref>(), nq, tfd.as<double>(), req, &dr,
                                              stream);
   if (rc == FCLGPU_OK) {

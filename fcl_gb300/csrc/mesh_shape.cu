@@ -1,6 +1,7 @@
 // Batched BVHModel<OBBRSS> x convex shape collide / distance (one pair per thread) and
 // its C ABI (fclgpu_mesh_shape_batch*).
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <algorithm>
 #include <mutex>
@@ -365,8 +366,11 @@ __global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const in
 constexpr int kMsWarps = 4;
 constexpr int kMsFront = 2048;
 constexpr int kMsWarpMaxDepth = kMsFront / 32 - 4;
+#ifndef FCLG_MS_MINB
+#define FCLG_MS_MINB 1
+#endif
 
-__global__ void __launch_bounds__(32 * kMsWarps) k_ms_count_warp(MeshShapeLaunch L) {
+__global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(MeshShapeLaunch L) {
   __shared__ int32_t front[kMsWarps][kMsFront];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long i = (long long)blockIdx.x * kMsWarps + w;
@@ -433,100 +437,437 @@ __global__ void __launch_bounds__(32 * kMsWarps) k_ms_count_warp(MeshShapeLaunch
   if (lane == 0) L.counts[i] = count < M ? count : M;
 }
 
-// Distance values without witnesses: FCL's traversal reports the smallest distance of
-// the leaves it visits, and a leaf it prunes lies in a volume at least as far as its
-// running minimum, so the value is the minimum over the mesh's triangles (as for the
-// split form, up to a triangle whose FP64 distance falls below its node's FP64 bound by
-// rounding).  One warp per pair: a LIFO frontier of (node, lower bound) in shared memory,
-// up to 32 entries a step, entries at or beyond the current minimum dropped (FCL's
-// canStop).  The triangle and witness points are not produced (the caller asked for
-// neither).
+// Mesh-shape distance, one warp per pair.  FCL's traversal (distanceRecurse with
+// triangle 0 as the seed, mesh_shape_distance_traversal_node-inl.h) reports the first
+// leaf in its visit order with the smallest distance it meets, and prunes a subtree
+// whose bound is at least its running minimum; so its distance is the minimum over the
+// mesh's triangles (up to a triangle whose FP64 distance falls below its node's FP64
+// bound by rounding), and its triangle is the first of the triangles at that minimum
+// in its depth-first order, whatever order they are found in here.
+//
+// The warp keeps a stack of (node, bound, path) in shared memory and takes up to 32
+// entries a step; the children it adds are sorted by bound (a bitonic network over the
+// warp) and pushed nearest on top, so the nearest leaves come first.  Bounds are FP32
+// lower bounds with a derived error (below): a node is dropped, and a leaf's FP64
+// distance skipped, only when its bound exceeds the running minimum by more than
+// m64 = 2^-36 S (S the pair's coordinate scale), which covers FCL's FP64 volumes
+// containing their triangles up to rounding and its FP64 distances being within
+// rounding of the exact ones.  So every triangle whose FP64 distance can reach the
+// minimum -- including every triangle tied at it -- is evaluated with FCL's FP64
+// shapeTriangleDistance.  Of tied triangles the first in FCL's order wins: triangle 0
+// (the seed) first, otherwise the one on the side FCL enters first at the two leaves'
+// deepest common node (FCL's FP64 bounds of that node's children, the nearer first,
+// the second child on d2 < d1).  A pair leaves this path, for k_ms_dist_serial to run
+// FCL's own traversal, when a triangle's distance is <= 0 (touching or intersecting,
+// where FCL's first-met rule decides the value) or when its mesh was refitted (FCL's
+// merged volumes then need not bound their triangles).
+//
+// Node bound along a direction n (mesh frame; any n != 0 gives a valid bound):
+//   dist(shape, RSS) >= (min_shape n.x - max_RSS n.y) / |n|,
+//   max_RSS n.y = n.To + l0 max(0, n.a0) + l1 max(0, n.a1) + r|n|,
+//   min_shape n.x = n.t - h_A(-Rrel^T n)   (h_A the shape's support function),
+// with (Rrel, t) the shape's pose in the mesh frame and the RSS data FCL's FP64 values
+// rounded to FP32.  Forward error (u = 2^-24, no fused multiply-adds): 3-term dot
+// products of rounded inputs err by 4.1u ||n||_1 times the input's magnitude (|To| <=
+// rmax, |t_i| <= T, unit axes); the clamped axis terms by 6.2u ||n||_1 l; r|n| by 4.1u
+// ||n||_1 r; the rotated direction by 4.1u ||n||_1 per component, moving the support
+// value by at most sqrt(3) that times the shape's radius rho, and the support value
+// itself by under 10u ||n||_1 rho; the six final additions by 6u ||n||_1 times the sum
+// of the magnitudes.  Together under 24u ||n||_1 (rmax + T + rho + l0 + l1 + r); the
+// bound subtracts 32u ||n||_1 (...) (times 1.01 for its own rounding) and scales the
+// quotient by 1 - 8u (the division and |n|).  Two directions are tried: from the RSS
+// rectangle's point nearest to the shape's origin to that origin, and the separating
+// direction of the best triangle so far (its FP32 GJK direction).  Leaf bound: FP32
+// GJK on (shape, triangle) to convergence, then the support gap along its direction
+// with the error bound of gjk32.cuh (under 40u ||D||_1 S; 64u is subtracted).
 constexpr int kMdWarps = 2;
 constexpr int kMdFront = 1024;
 constexpr int kMdWarpMaxDepth = kMdFront / 32 - 4;
+#ifndef FCLG_MD_MINB
+#define FCLG_MD_MINB 1
+#endif
 
-__global__ void __launch_bounds__(32 * kMdWarps) k_ms_dist_warp(MeshShapeLaunch L) {
+// one compare-exchange network sorting 64 entries held two per lane (entry e = lane +
+// 32 * slot) by (key, node), ascending; pay travels with its entry
+__device__ __forceinline__ bool md_less(float ka, int na, float kb, int nb) {
+  return ka < kb || (ka == kb && na < nb);
+}
+__device__ __forceinline__ void md_sort64(float& k0, int& n0, unsigned& p0, float& k1, int& n1, unsigned& p1,
+                                          int lane) {
+  const unsigned full = 0xffffffffu;
+#pragma unroll
+  for (int k = 2; k <= 64; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 32) {  // partner in the other slot of the same lane (k == 64: ascending)
+        if (md_less(k1, n1, k0, n0)) {
+          const float tk = k0;
+          const int tn = n0;
+          const unsigned tp = p0;
+          k0 = k1;
+          n0 = n1;
+          p0 = p1;
+          k1 = tk;
+          n1 = tn;
+          p1 = tp;
+        }
+        continue;
+      }
+#pragma unroll
+      for (int slot = 0; slot < 2; ++slot) {
+        float& kk = slot ? k1 : k0;
+        int& nn = slot ? n1 : n0;
+        unsigned& pp = slot ? p1 : p0;
+        const int e = lane + 32 * slot;
+        const float pk = __shfl_xor_sync(full, kk, j);
+        const int pn = __shfl_xor_sync(full, nn, j);
+        const unsigned ppay = __shfl_xor_sync(full, pp, j);
+        const bool up = (e & k) == 0;
+        const bool lower = (e & j) == 0;
+        const bool p_first = md_less(pk, pn, kk, nn);  // the partner orders before this entry
+        // the lower position keeps the first of the two in the sort direction
+        const bool take = lower ? (up ? p_first : !p_first) : (up ? !p_first : p_first);
+        if (take) {
+          kk = pk;
+          nn = pn;
+          pp = ppay;
+        }
+      }
+    }
+  }
+}
+
+// path of a node below the root: one bit per level from bit 31 down (0 = first child,
+// 1 = second), then a marker bit
+__device__ __forceinline__ unsigned md_child_path(unsigned path, int which) {
+  const int m = __ffs(path) - 1;
+  return (path & ~(1u << m)) | ((unsigned)which << m) | (1u << (m - 1));
+}
+
+struct MdPair {
+  float Rr[9];   // the shape's rotation in the mesh frame (row-major)
+  G3f tr;        // the shape's origin in the mesh frame
+  float rho;     // the shape's radius bound
+  float base;    // rmax + T + rho of the node error bound
+};
+
+// certified lower bound of the distance between the shape and node b's RSS along n
+__device__ __forceinline__ float md_node_lb(const float4* rss32, int b, const ShapeRef& A, const MdPair& q, G3f n,
+                                            float l0, float l1, float r, G3f To, G3f a0, G3f a1) {
+  const float nn = sqrtf(gdot(n, n));
+  if (!(nn > 0.f)) return -CUDART_INF_F;
+  const float n1 = (fabsf(n.x) + fabsf(n.y)) + fabsf(n.z);
+  const float hR = ((gdot(n, To) + l0 * fmaxf(0.f, gdot(n, a0))) + l1 * fmaxf(0.f, gdot(n, a1))) + r * nn;
+  const G3f uA = rot32T(q.Rr, n);
+  const G3f mu = g3f(-uA.x, -uA.y, -uA.z);
+  const float hA = gdot(mu, support32(A, mu));
+  const float gap = (gdot(n, q.tr) - hA) - hR;
+  const float E = 1.90734863e-06f * n1 * ((q.base + l0) + (l1 + r)) * 1.01f;  // 32u
+  const float g = gap - E;
+  if (!(g > 0.f)) return -CUDART_INF_F;
+  return g * (1.f - 4.76837158e-07f) / nn;  // 1 - 8u
+}
+
+__device__ __forceinline__ float md_node_bound(const float4* rss32, int b, const ShapeRef& A, const MdPair& q,
+                                               bool have_dir, G3f dir) {
+  const float4 c0 = __ldg(rss32 + 5 * (long long)b), c1 = __ldg(rss32 + 5 * (long long)b + 1);
+  const float4 x0 = __ldg(rss32 + 5 * (long long)b + 2), x1 = __ldg(rss32 + 5 * (long long)b + 3);
+  const float4 x2 = __ldg(rss32 + 5 * (long long)b + 4);
+  const G3f To = g3f(c0.x, c0.y, c0.z), a0 = g3f(x0.x, x0.y, x0.z), a1 = g3f(x1.x, x1.y, x1.z);
+  const float r = c0.w, l0 = c1.x, l1 = c1.y;
+  // from the rectangle's point nearest to the shape's origin
+  const G3f d = q.tr - To;
+  const float s = fminf(fmaxf(gdot(d, a0), 0.f), l0), t = fminf(fmaxf(gdot(d, a1), 0.f), l1);
+  G3f n = d - a0 * s - a1 * t;
+  if (!(gdot(n, n) > 1e-12f * (gdot(d, d) + 1e-30f))) {
+    const G3f a2 = g3f(x2.x, x2.y, x2.z);
+    n = gdot(d, a2) >= 0.f ? a2 : g3f(-a2.x, -a2.y, -a2.z);
+  }
+  float lb = md_node_lb(rss32, b, A, q, n, l0, l1, r, To, a0, a1);
+  if (have_dir) lb = fmaxf(lb, md_node_lb(rss32, b, A, q, dir, l0, l1, r, To, a0, a1));
+  return lb;
+}
+
+// certified lower bound of the shape-triangle distance: FP32 GJK to convergence, then
+// the support gap along its direction (the certificate of gjk32.cuh); dirA = that
+// direction in the shape's frame
+__device__ __forceinline__ float md_leaf_lb(const ShapeRef& A, const Pose32& pa, const ShapeRef& B, const Pose32& pb,
+                                            const Mink32& mk0, float S0, G3f& dirA) {
+  Mink32 mk = mk0;
+  mk.b = B;
+  const float S = S0 + shape_radius32(B);
+  G3f v;
+  if (gjk32(mk, CUDART_INF_F, v, S) != G32_SEPARATED) return -CUDART_INF_F;
+  const G3f D = rot32(pa.R, v);
+  const float n1 = (fabsf(D.x) + fabsf(D.y)) + fabsf(D.z);
+  const float nn = sqrtf(gdot(D, D));
+  if (!(nn > 0.f)) return -CUDART_INF_F;
+  const G3f uA = rot32T(pa.R, g3f(-D.x, -D.y, -D.z)), uB = rot32T(pb.R, D);
+  const float hA = gdot(uA, support32(A, uA)), hB = gdot(uB, support32(B, uB));
+  const G3f ta = g3f(pa.t[0], pa.t[1], pa.t[2]), tb = g3f(pb.t[0], pb.t[1], pb.t[2]);
+  const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
+  const float g = gap - 3.81469727e-06f * S * n1;  // 64u ||D||_1 S
+  if (!(g > 0.f)) return -CUDART_INF_F;
+  dirA = v;
+  return g * (1.f - 4.76837158e-07f) / nn;
+}
+
+template <bool WIT>
+__global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(MeshShapeLaunch L) {
   __shared__ int32_t fnode[kMdWarps][kMdFront];
-  __shared__ double flb[kMdWarps][kMdFront];
+  __shared__ float flb[kMdWarps][kMdFront];
+  __shared__ unsigned fpath[kMdWarps][kMdFront];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long i = (long long)blockIdx.x * kMdWarps + w;
   if (i >= L.n) return;
   const unsigned full = 0xffffffffu;
-  const unsigned lt = (1u << lane) - 1u;
   PairGeom g;
   pair_geom(L, i, g);
-  ShapeBV bv;
+  if (g.m.refitted) {  // FCL's traversal order decides: k_ms_dist_serial
+    if (lane == 0) L.dist[i] = CUDART_NAN;
+    return;
+  }
+  const float4* rss32 = static_cast<const float4*>(g.m.rss32);
+  MdPair q;
+  {
+    const M3<double> Rrel = mulT(g.Rm, g.Rs);
+    const D3v trel = mulTv(g.Rm, g.ts - g.tm);
+    for (int k = 0; k < 9; ++k) q.Rr[k] = (float)Rrel.m[k];
+    q.tr = g3f((float)trel.x, (float)trel.y, (float)trel.z);
+    q.rho = shape_radius32(g.A);
+    const float T = fmaxf(fabsf(q.tr.x), fmaxf(fabsf(q.tr.y), fabsf(q.tr.z)));
+    q.base = ((float)g.m.rmax * 1.0001f + T * 1.0001f) + q.rho;
+  }
+  Pose32 pa, pb;
+  pose32(g.Rs, g.ts, pa);
+  pose32(g.Rm, g.tm, pb);
+  Mink32 mk0;
+  {
+    ShapeRef B0 = g.A;  // replaced per leaf
+    make_mink32(g.A, pa, B0, pb, mk0);
+  }
+  const float S0 = 1.f + q.rho + fmaxf(fabsf(pa.t[0]), fmaxf(fabsf(pa.t[1]), fabsf(pa.t[2]))) +
+                   fmaxf(fabsf(pb.t[0]), fmaxf(fabsf(pb.t[1]), fabsf(pb.t[2])));
+  const double m64 = ldexp(1.0 + (double)q.rho + fmax(fabs(g.ts.x), fmax(fabs(g.ts.y), fabs(g.ts.z))) +
+                               fmax(fabs(g.tm.x), fmax(fabs(g.tm.y), fabs(g.tm.z))) + g.m.vmax + g.m.rmax,
+                           -36);
+  const bool sphere = g.A.s.type == SHAPE_SPHERE;
+  ShapeBV bv;  // FCL's model2_bv, for its FP64 bounds when two triangles tie
   if (L.bv_src)
     bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
   else
     shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
-  M3<double> Ab;
-  for (int k = 0; k < 9; ++k) Ab.m[k] = bv.obb.axis[k];
-  const D3v Tob = v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]);
-  auto bvd = [&](int b) {  // as mesh_shape_collect_distance's node bound
+  auto bvd = [&](int b) {  // as mesh_shape_distance's node bound
     const RssD& rs = g.m.rss64[b];
-    M3<double> A2;
-    for (int k = 0; k < 9; ++k) A2.m[k] = rs.axis[k];
-    return rss_distance<double>(g.Rm, g.tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l,
-                                rs.r);
+    M3<double> A2, Ab;
+    for (int k = 0; k < 9; ++k) {
+      A2.m[k] = rs.axis[k];
+      Ab.m[k] = bv.obb.axis[k];
+    }
+    return rss_distance<double>(g.Rm, g.tm, Ab, v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]), bv.rl, bv.rr, A2,
+                                v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
+  };
+  // true when leaf (pa, ka) comes before leaf (pb_, kb) in FCL's order
+  auto fcl_first = [&](int prim_a, unsigned ka, int prim_b, unsigned kb) {
+    if (prim_a == 0) return true;
+    if (prim_b == 0) return false;
+    const int lca = __clz(ka ^ kb);
+    int x = 0;
+    for (int t = 0; t < lca; ++t) x = g.m.nodes64[x].child + (int)((ka >> (31 - t)) & 1u);
+    const int c = g.m.nodes64[x].child;
+    const double d1 = bvd(c), d2 = bvd(c + 1);
+    const bool a_second = ((ka >> (31 - lca)) & 1u) != 0;
+    return a_second == (d2 < d1);
   };
   double ub = DBL_MAX;
+  int best = -1;
+  unsigned best_path = 0;
+  bool have_dir = false;
+  G3f dir = g3f(0.f, 0.f, 0.f);
+  bool serial = false;
   if (lane == 0) {
     fnode[w][0] = 0;
-    flb[w][0] = -1.0;
+    flb[w][0] = -CUDART_INF_F;
+    fpath[w][0] = 0x80000000u;
   }
   int size = 1;
   __syncwarp();
   while (size > 0) {
     const int take = size < 32 ? size : 32;
     int b = -1;
-    double lb = 0.0;
+    float lb = 0.f;
+    unsigned path = 0;
     if (lane < take) {
       b = fnode[w][size - 1 - lane];
       lb = flb[w][size - 1 - lane];
+      path = fpath[w][size - 1 - lane];
     }
     size -= take;
     __syncwarp();
-    if (b >= 0 && lb >= ub) b = -1;  // cannot lower the minimum
+    if (b >= 0 && (double)lb > ub + m64) b = -1;  // no triangle below can reach the minimum
     int child = 0;
     if (b >= 0) child = g.m.nodes64[b].child;
     const bool inner = b >= 0 && child >= 0;
-    double l1 = 0.0, l2 = 0.0;
+    float k0 = CUDART_INF_F, k1 = CUDART_INF_F;  // the children to push (sorted below); infinity = none
+    int n0 = -1, n1 = -1;
+    unsigned p0 = 0, p1 = 0;
     if (inner) {
-      l1 = bvd(child);
-      l2 = bvd(child + 1);
+      const float l1 = md_node_bound(rss32, child, g.A, q, have_dir, dir);
+      const float l2 = md_node_bound(rss32, child + 1, g.A, q, have_dir, dir);
+      if ((double)l1 <= ub + m64) {
+        k0 = l1;
+        n0 = child;
+        p0 = md_child_path(path, 0);
+      }
+      if ((double)l2 <= ub + m64) {
+        k1 = l2;
+        n1 = child + 1;
+        p1 = md_child_path(path, 1);
+      }
     }
-    const bool p1 = inner && l1 < ub, p2 = inner && l2 < ub;
-    const unsigned m1 = __ballot_sync(full, p1), m2 = __ballot_sync(full, p2);
-    const int np = __popc(m1) + __popc(m2);
+    double d = DBL_MAX;
+    bool has_dir = false;
+    G3f ldir = g3f(0.f, 0.f, 0.f);
+    if (b >= 0 && child < 0) {
+      double P[9];
+      load_tri_local(g.m, -(child + 1), P);
+      bool eval = true;
+      if (!sphere) {
+        const float lbl = md_leaf_lb(g.A, pa, triangle_ref(P), pb, mk0, S0, ldir);
+        has_dir = lbl > -CUDART_INF_F;
+        eval = !((double)lbl > ub + m64);
+      }
+      if (eval) {
+        SimplexVert V[kSimplexSlots];
+        D3v ps, pt;
+        shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+        if (!(d > 0.0)) serial = true;
+      }
+    }
+    if (__any_sync(full, serial)) {
+      serial = true;
+      break;
+    }
+    // the step's smallest distance; of equal ones FCL's first
+    double dm = d;
+    for (int off = 16; off > 0; off >>= 1) dm = fmin(dm, __shfl_xor_sync(full, dm, off));
+    if (dm < DBL_MAX && dm <= ub) {
+      unsigned at = __ballot_sync(full, d == dm);
+      const int prim = -(child + 1);
+      int win = -1;
+      if (dm < ub) {
+        win = __ffs(at) - 1;
+        at &= at - 1;
+        best = __shfl_sync(full, prim, win);
+        best_path = __shfl_sync(full, path, win);
+        ub = dm;
+      }
+      if (WIT) {
+        while (at) {  // ties: keep the first in FCL's order
+          const int l = __ffs(at) - 1;
+          at &= at - 1;
+          const int pl = __shfl_sync(full, prim, l);
+          const unsigned kl = __shfl_sync(full, path, l);
+          if (fcl_first(pl, kl, best, best_path)) {
+            best = pl;
+            best_path = kl;
+            win = l;
+          }
+        }
+      }
+      if (win >= 0) {  // the separating direction of the new best, for the node bounds
+        const bool hd = __shfl_sync(full, has_dir, win);
+        const float dx = __shfl_sync(full, ldir.x, win), dy = __shfl_sync(full, ldir.y, win),
+                    dz = __shfl_sync(full, ldir.z, win);
+        if (hd) {
+          dir = rot32(q.Rr, g3f(dx, dy, dz));
+          have_dir = true;
+        }
+      }
+    }
+    // push the children nearest on top; those no longer within reach stay out
+    if ((double)k0 > ub + m64) n0 = -1, k0 = CUDART_INF_F;
+    if ((double)k1 > ub + m64) n1 = -1, k1 = CUDART_INF_F;
+    const int np = __popc(__ballot_sync(full, n0 >= 0)) + __popc(__ballot_sync(full, n1 >= 0));
+    if (np == 0) continue;
     if (size + np > kMdFront) {  // not reached for trees within kMdWarpMaxDepth
       if (lane == 0) atomicOr(L.status, 1u);
       break;
     }
-    int pos = size + __popc(m1 & lt) + __popc(m2 & lt);
-    if (p2) {  // the farther-ordered child below, the nearer popped first: order is free here
-      fnode[w][pos] = child + 1;
-      flb[w][pos] = l2;
-      ++pos;
+    md_sort64(k0, n0, p0, k1, n1, p1, lane);
+    // ascending order: entry e (valid for e < np) goes to size + np - 1 - e
+    if (lane < np) {
+      fnode[w][size + np - 1 - lane] = n0;
+      flb[w][size + np - 1 - lane] = k0;
+      fpath[w][size + np - 1 - lane] = p0;
     }
-    if (p1) {
-      fnode[w][pos] = child;
-      flb[w][pos] = l1;
+    if (lane + 32 < np) {
+      fnode[w][size + np - 33 - lane] = n1;
+      flb[w][size + np - 33 - lane] = k1;
+      fpath[w][size + np - 33 - lane] = p1;
     }
     size += np;
-    double d = DBL_MAX;
-    if (b >= 0 && child < 0) {
-      double P[9];
-      load_tri_local(g.m, -(child + 1), P);
-      SimplexVert V[kSimplexSlots];
-      D3v ps, pt;
-      shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
-    }
-    for (int off = 16; off > 0; off >>= 1) d = fmin(d, __shfl_xor_sync(full, d, off));
-    if (d < ub) ub = d;
     __syncwarp();
   }
-  if (lane == 0) L.dist[i] = ub;
+  if (serial) {
+    if (lane == 0) L.dist[i] = CUDART_NAN;
+    return;
+  }
+  if (lane == 0) {
+    L.dist[i] = ub;
+    if (WIT) {
+      D3v ps = v3(0.0, 0.0, 0.0), pt = ps;
+      if (best >= 0) {
+        double P[9];
+        load_tri_local(g.m, best, P);
+        SimplexVert V[kSimplexSlots];
+        double d;
+        shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+      }
+      if (L.tri) L.tri[i] = best;
+      if (L.pts) {
+        double* p = L.pts + 6 * i;
+        p[0] = pt.x;
+        p[1] = pt.y;
+        p[2] = pt.z;
+        p[3] = ps.x;
+        p[4] = ps.y;
+        p[5] = ps.z;
+      }
+    }
+  }
+}
+
+// FCL's traversal, one thread per pair, for the pairs the order-free forms hand over
+// (distance NaN) and the pairs with a refitted mesh
+template <int STACK>
+__global__ void __launch_bounds__(128) k_ms_dist_serial(MeshShapeLaunch L) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += stride) {
+    if (!isnan(L.dist[i]) && !L.meshes[L.mesh_idx[i]].refitted) continue;
+    PairGeom g;
+    pair_geom(L, i, g);
+    MeshShapeOut o;
+    o.count = 0;
+    o.tri = -1;
+    o.dist = 0;
+    o.pmesh = o.pshape = v3(0.0, 0.0, 0.0);
+    o.nbv = o.nleaf = 0;
+    o.status = 0;
+    mesh_shape_distance<STACK>(g.m, g.Rm, g.tm, g.A, g.Rs, g.ts, o);
+    if (o.status) atomicOr(L.status, 1u);
+    L.dist[i] = o.dist;
+    if (L.tri) L.tri[i] = o.tri;
+    if (L.pts) {
+      double* p = L.pts + 6 * i;
+      p[0] = o.pmesh.x;
+      p[1] = o.pmesh.y;
+      p[2] = o.pmesh.z;
+      p[3] = o.pshape.x;
+      p[4] = o.pshape.y;
+      p[5] = o.pshape.z;
+    }
+  }
 }
 
 // tris[offsets[pair] + rank] = triangle for every record
@@ -743,13 +1084,26 @@ cudaError_t run_mesh_shape_split(const MeshShapeLaunch& L, int stack_entries, cu
     ++g_kernel_launches;
     return cudaGetLastError();
   }
-  if (L.mode == 1 && !L.tri && !L.pts && stack_entries <= kMdWarpMaxDepth) {  // distance values only
-    k_ms_dist_warp<<<(unsigned)((L.n + kMdWarps - 1) / kMdWarps), 32 * kMdWarps, 0, s>>>(L);
-    ++g_kernel_launches;
+  if (L.mode == 1 && stack_entries <= kMdWarpMaxDepth) {  // distance: warp per pair, then the handed-over pairs
+    const unsigned blocks = (unsigned)((L.n + kMdWarps - 1) / kMdWarps);
+    if (L.tri || L.pts)
+      k_ms_dist_warp<true><<<blocks, 32 * kMdWarps, 0, s>>>(L);
+    else
+      k_ms_dist_warp<false><<<blocks, 32 * kMdWarps, 0, s>>>(L);
+    k_ms_dist_serial<64><<<(unsigned)std::min<long long>((L.n + 127) / 128, 152 * 32), 128, 0, s>>>(L);
+    g_kernel_launches += 2;
     return cudaGetLastError();
   }
-  return L.mode == 0 ? run_collide_rounds(L, stack_entries, s, g_split_ms)
-                     : run_distance_split(L, stack_entries, s, g_split_ms);
+  if (L.mode == 0) return run_collide_rounds(L, stack_entries, s, g_split_ms);
+  const cudaError_t e = run_distance_split(L, stack_entries, s, g_split_ms);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)std::min<long long>((L.n + 127) / 128, 152 * 32);
+  if (stack_entries <= 64)
+    k_ms_dist_serial<64><<<grid, 128, 0, s>>>(L);
+  else
+    k_ms_dist_serial<256><<<grid, 128, 0, s>>>(L);
+  ++g_kernel_launches;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mesh_shape(const MeshShapeLaunch& L, int stack_entries, cudaStream_t s) {

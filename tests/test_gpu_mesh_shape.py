@@ -94,6 +94,40 @@ def test_broadphase_mixed_scene_matches_oracle(gpu_lib):
     assert np.all(np.abs(d["min_distance"][sep] - r) <= np.maximum(1e-6 * np.abs(r), 1e-9))
 
 
+def test_mesh_shape_distance_ties_and_refit_match_oracle(gpu_lib):
+    """Shapes just outside mesh vertices: spheres there are nearest to a vertex shared by
+    several triangles, whose FP64 distances tie exactly, and FCL reports the first of
+    them in its traversal order.  Then the same poses after a vertex update (refitted
+    volumes).  Distance, triangle and witness points equal the oracle's."""
+    v, t = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, 31)
+    mesh, om = api.BVHModel.from_arrays(v, t), P.Mesh(v, t)
+    shapes = W.random_shapes(64, 32)
+    ss, G = api.ShapeSet.from_workload(shapes), P.Geoms(shapes)
+    rng = np.random.default_rng(33)
+    n = 1500
+    spheres = np.flatnonzero(shapes.type == W.SPHERE)
+    sidx = np.where(rng.uniform(size=n) < 0.7, rng.choice(spheres, size=n),
+                    rng.integers(0, 64, size=n)).astype(np.int32)
+    k = rng.integers(0, v.shape[0], size=n)
+    u = v[k] - v.mean(axis=0)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    reach = np.where(shapes.type[sidx] == W.SPHERE, shapes.params[sidx, 0], 0.6)
+    tfs = W.random_poses(n, 0.0, 0.0, 34)
+    tfs[:, :, 3] = v[k] + u * (reach + rng.uniform(0.002, 0.3, size=n))[:, None]
+    tfm = W.identity_poses(n)
+    midx = np.zeros(n, np.int32)
+    for step in range(2):
+        g = api.mesh_shape_batch([mesh], ss, midx, sidx, tfm, tfs, mode="distance")
+        o = P.mesh_shape_distance(om, G, sidx, tfm, tfs, nthreads=8)
+        np.testing.assert_array_equal(g["min_distance"], o["dist"])
+        np.testing.assert_array_equal(g["tri"], o["tri"])
+        np.testing.assert_array_equal(g["nearest_points"], o["pts"])
+        assert (o["dist"] > 0).mean() > 0.8
+        v1 = v + rng.normal(0, 0.004, v.shape)
+        mesh.update_vertices(v1)
+        om.update(v1)
+
+
 @pytest.mark.parametrize("seed", [2])
 def test_mesh_shape_split_form_matches_oracle(gpu_lib, seed):
     # without statistics the leaf tests run one per thread; results stay the oracle's
