@@ -104,9 +104,124 @@ FCLG_HD G3f support32(const ShapeRef& sh, const G3f& d) {
   return g3f(0.f, 0.f, 0.f);
 }
 
+// A shape's support data rounded to FP32 once: the same values support32 rounds from
+// the FP64 parameters on every call, so supports (and every decision built on them)
+// are identical; leaf loops that take many supports of one shape or triangle use it
+// to keep FP64 conversions out of the FP32 iteration.
+struct Shape32 {
+  int type, n;
+  float h0, h1;       // box: half sides x, y (h2 z); round shapes: radius, half height
+  float h2;
+  const float4* v32;  // convex: FP32 vertices, or null
+  const double* v64;  // convex without FP32 vertices: the FP64 pool
+  float tv[9];        // triangle vertices
+};
+FCLG_HD void shape32(const ShapeRef& sh, Shape32& o) {
+  const DevShape& s = sh.s;
+  o.type = s.type;
+  o.n = s.vcnt;
+  o.h0 = o.h1 = o.h2 = 0.f;
+  o.v32 = nullptr;
+  o.v64 = nullptr;
+  switch (s.type) {
+    case SHAPE_BOX:
+      o.h0 = (float)(s.p[0] * 0.5);
+      o.h1 = (float)(s.p[1] * 0.5);
+      o.h2 = (float)(s.p[2] * 0.5);
+      break;
+    case SHAPE_SPHERE:
+      o.h0 = (float)s.p[0];
+      break;
+    case SHAPE_CAPSULE:
+    case SHAPE_CYLINDER:
+    case SHAPE_CONE:
+      o.h0 = (float)s.p[0];
+      o.h1 = (float)(s.p[1] * 0.5);
+      break;
+    case SHAPE_CONVEX:
+      o.v32 = convex_v32(sh);
+      o.v64 = sh.verts + 3 * (long long)s.voff;
+      break;
+    default: {  // triangle
+      const double* V = sh.verts + 3 * (long long)s.voff;
+      o.n = 3;
+      for (int k = 0; k < 9; ++k) o.tv[k] = (float)V[k];
+    }
+  }
+}
+FCLG_HD G3f support32(const Shape32& s, const G3f& d) {
+  switch (s.type) {
+    case SHAPE_BOX:
+      return g3f(d.x > 0 ? s.h0 : -s.h0, d.y > 0 ? s.h1 : -s.h1, d.z > 0 ? s.h2 : -s.h2);
+    case SHAPE_SPHERE: {
+      const float n = sqrtf(gdot(d, d));
+      return n > 0 ? d * (s.h0 / n) : g3f(0.f, 0.f, 0.f);
+    }
+    case SHAPE_CAPSULE: {
+      const float n = sqrtf(gdot(d, d));
+      const G3f r = n > 0 ? d * (s.h0 / n) : g3f(0.f, 0.f, 0.f);
+      return g3f(r.x, r.y, r.z + (d.z > 0 ? s.h1 : -s.h1));
+    }
+    case SHAPE_CYLINDER: {
+      const float zd = sqrtf(d.x * d.x + d.y * d.y);
+      const float hz = d.z > 0 ? s.h1 : -s.h1;
+      if (zd == 0.f) return g3f(0.f, 0.f, hz);
+      const float k = s.h0 / zd;
+      return g3f(d.x * k, d.y * k, hz);
+    }
+    case SHAPE_CONE: {
+      const float r = s.h0, hh = s.h1;
+      const float zd = sqrtf(d.x * d.x + d.y * d.y);
+      const G3f rim = zd > 0 ? g3f(d.x * (r / zd), d.y * (r / zd), -hh) : g3f(0.f, 0.f, -hh);
+      return (d.z * hh > gdot(d, rim)) ? g3f(0.f, 0.f, hh) : rim;
+    }
+    case SHAPE_CONVEX: {
+      if (s.v32) {
+        G3f best = g3f(s.v32[0].x, s.v32[0].y, s.v32[0].z);
+        float bd = gdot(d, best);
+        for (int i = 1; i < s.n; ++i) {
+          const G3f p = g3f(s.v32[i].x, s.v32[i].y, s.v32[i].z);
+          const float t = gdot(d, p);
+          if (t > bd) {
+            bd = t;
+            best = p;
+          }
+        }
+        return best;
+      }
+      const double* V = s.v64;
+      G3f best = g3f((float)V[0], (float)V[1], (float)V[2]);
+      float bd = gdot(d, best);
+      for (int i = 1; i < s.n; ++i) {
+        const G3f p = g3f((float)V[3 * i], (float)V[3 * i + 1], (float)V[3 * i + 2]);
+        const float t = gdot(d, p);
+        if (t > bd) {
+          bd = t;
+          best = p;
+        }
+      }
+      return best;
+    }
+    default: {  // triangle
+      G3f best = g3f(s.tv[0], s.tv[1], s.tv[2]);
+      float bd = gdot(d, best);
+      for (int i = 1; i < 3; ++i) {
+        const G3f p = g3f(s.tv[3 * i], s.tv[3 * i + 1], s.tv[3 * i + 2]);
+        const float t = gdot(d, p);
+        if (t > bd) {
+          bd = t;
+          best = p;
+        }
+      }
+      return best;
+    }
+  }
+}
+
 // A and B as posed: Minkowski difference A - B in A's frame
-struct Mink32 {
-  ShapeRef a, b;
+template <class SH>
+struct Mink32T {
+  SH a, b;
   float R1[9];  // A-frame direction -> B-frame direction (R_B^T R_A)
   float R0[9];  // B-frame point -> A frame (R_A^T R_B)
   G3f t0;        // (A^-1 B) translation
@@ -121,6 +236,8 @@ struct Mink32 {
     return pa - wb;
   }
 };
+using Mink32 = Mink32T<ShapeRef>;
+using Mink32P = Mink32T<Shape32>;
 
 
 // closest point to the origin on the triangle W[0..3) (Ericson 5.1.5 with p = origin);
@@ -238,7 +355,8 @@ enum : int { G32_SEPARATED = 0, G32_UNKNOWN = 1 };
 
 // Stops at the first direction v whose support gap v.w exceeds target |v| (or when the
 // distance estimate converges, relative 2^-16); G32_SEPARATED when v.w > 0 at the end.
-FCLG_HD int gjk32(const Mink32& m, float target, G3f& v_out, float scale) {
+template <class MK>
+FCLG_HD int gjk32(const MK& m, float target, G3f& v_out, float scale) {
   G3f W[4];
   int n = 0;
   G3f v = m.sup(g3f(1.f, 0.f, 0.f));
@@ -306,7 +424,8 @@ FCLG_HD G3f rot32T(const float* R, const G3f& v) {
 }
 
 // the Minkowski difference of A and B posed by a and b, in A's frame, in FP32
-FCLG_HD void make_mink32(const ShapeRef& A, const Pose32& a, const ShapeRef& B, const Pose32& b, Mink32& m) {
+template <class SH>
+FCLG_HD void make_mink32(const SH& A, const Pose32& a, const SH& B, const Pose32& b, Mink32T<SH>& m) {
   m.a = A;
   m.b = B;
   for (int i = 0; i < 3; ++i)
@@ -319,8 +438,9 @@ FCLG_HD void make_mink32(const ShapeRef& A, const Pose32& a, const ShapeRef& B, 
 }
 
 // the FP32 certificate along the world direction D = Ra dA
-FCLG_HD bool certify_separated32(const ShapeRef& A, const Pose32& a, const ShapeRef& B, const Pose32& b,
-                                 const G3f& dA, float S) {
+template <class SH>
+FCLG_HD bool certify_separated32(const SH& A, const Pose32& a, const SH& B, const Pose32& b, const G3f& dA, float S,
+                                 float tol) {
   const G3f D = rot32(a.R, dA);
   const float n1 = (fabsf(D.x) + fabsf(D.y)) + fabsf(D.z);
   if (!(n1 > 0.f)) return false;
@@ -328,9 +448,9 @@ FCLG_HD bool certify_separated32(const ShapeRef& A, const Pose32& a, const Shape
   const float hA = gdot(uA, support32(A, uA)), hB = gdot(uB, support32(B, uB));
   const G3f ta = g3f(a.t[0], a.t[1], a.t[2]), tb = g3f(b.t[0], b.t[1], b.t[2]);
   const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
-  // 64u ||D||_1 S, plus the GJK tolerance: FCL's GJK ends Inside once its ray is
-  // shorter than gjk_tolerance, so a certified pair is also farther apart than that
-  const float tol = (float)solver_params().gjk_tolerance * 1.01f;
+  // 64u ||D||_1 S, plus the GJK tolerance (tol = 1.01 gjk_tolerance): FCL's GJK ends
+  // Inside once its ray is shorter than gjk_tolerance, so a certified pair is also
+  // farther apart than that
   return gap > (3.81469727e-06f * S + tol) * n1;
 }
 
@@ -350,7 +470,76 @@ FCLG_HD bool certified_disjoint(const ShapeRef& A, const M3<double>& Ra, const D
   G3f v;
   // a direction whose gap clears the certificate's threshold with room to spare
   if (gjk32(m, 1.32e-5f * S, v, S) != G32_SEPARATED) return false;
-  return certify_separated32(A, a, B, b, v, S);
+  return certify_separated32(A, a, B, b, v, S, (float)solver_params().gjk_tolerance * 1.01f);
+}
+
+// One posed shape against many triangles of one posed mesh: certified_disjoint and a
+// certified distance lower bound with the per-pair work done once (poses, the shape's
+// FP32 supports, the relative rotations) and every triangle's supports rounded once.
+// Same values, hence the same decisions, as the per-call forms.
+struct LeafCert32 {
+  Mink32P m;  // m.a: the shape; m.b: the current triangle
+  Pose32 a, b;
+  float s1;   // 1 + the shape's radius
+  float ta, tb;
+  float tol;  // 1.01 gjk_tolerance
+};
+FCLG_HD void leaf_cert_init(const ShapeRef& A, const M3<double>& Ra, const D3v& ta, const M3<double>& Rb,
+                            const D3v& tb, LeafCert32& c) {
+  pose32(Ra, ta, c.a);
+  pose32(Rb, tb, c.b);
+  Shape32 A32;
+  shape32(A, A32);
+  c.m.b = A32;  // replaced per triangle
+  make_mink32(A32, c.a, A32, c.b, c.m);
+  c.s1 = 1.f + shape_radius32(A);
+  c.ta = fmaxf(fabsf(c.a.t[0]), fmaxf(fabsf(c.a.t[1]), fabsf(c.a.t[2])));
+  c.tb = fmaxf(fabsf(c.b.t[0]), fmaxf(fabsf(c.b.t[1]), fabsf(c.b.t[2])));
+  c.tol = (float)solver_params().gjk_tolerance * 1.01f;
+}
+// the triangle P (mesh frame, FP64) becomes c.m.b; returns the scale S of certified_disjoint
+FCLG_HD float leaf_cert_triangle(LeafCert32& c, const double* P) {
+  Shape32& t = c.m.b;
+  t.type = SHAPE_TRIANGLE;
+  t.n = 3;
+  float r = 0.f;
+  for (int i = 0; i < 3; ++i) {
+    t.tv[3 * i] = (float)P[3 * i];
+    t.tv[3 * i + 1] = (float)P[3 * i + 1];
+    t.tv[3 * i + 2] = (float)P[3 * i + 2];
+    r = fmaxf(r, (fabsf(t.tv[3 * i]) + fabsf(t.tv[3 * i + 1])) + fabsf(t.tv[3 * i + 2]));
+  }
+  return ((c.s1 + r * 1.0001f) + c.ta) + c.tb;
+}
+// == certified_disjoint(A, Ra, ta, triangle_ref(P), Rb, tb)
+FCLG_HD bool leaf_cert_disjoint(LeafCert32& c, const double* P) {
+  const float S = leaf_cert_triangle(c, P);
+  if (!(S < 1e30f)) return false;
+  G3f v;
+  if (gjk32(c.m, 1.32e-5f * S, v, S) != G32_SEPARATED) return false;
+  return certify_separated32(c.m.a, c.a, c.m.b, c.b, v, S, c.tol);
+}
+// A lower bound of the exact shape-triangle distance (-infinity when none): FP32 GJK to
+// convergence, then the support gap along its direction D with the certificate's error
+// bound (under 40u ||D||_1 S; 64u is subtracted), divided by |D| and scaled by 1 - 8u
+// for the division and the norm; dirA = the direction in the shape's frame.
+FCLG_HD float leaf_cert_lb(LeafCert32& c, const double* P, G3f& dirA) {
+  const float S = leaf_cert_triangle(c, P);
+  if (!(S < 1e30f)) return -INFINITY;
+  G3f v;
+  if (gjk32(c.m, INFINITY, v, S) != G32_SEPARATED) return -INFINITY;
+  const G3f D = rot32(c.a.R, v);
+  const float n1 = (fabsf(D.x) + fabsf(D.y)) + fabsf(D.z);
+  const float nn = sqrtf(gdot(D, D));
+  if (!(nn > 0.f)) return -INFINITY;
+  const G3f uA = rot32T(c.a.R, g3f(-D.x, -D.y, -D.z)), uB = rot32T(c.b.R, D);
+  const float hA = gdot(uA, support32(c.m.a, uA)), hB = gdot(uB, support32(c.m.b, uB));
+  const G3f ta = g3f(c.a.t[0], c.a.t[1], c.a.t[2]), tb = g3f(c.b.t[0], c.b.t[1], c.b.t[2]);
+  const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
+  const float g = gap - 3.81469727e-06f * S * n1;
+  if (!(g > 0.f)) return -INFINITY;
+  dirA = v;
+  return g * (1.f - 4.76837158e-07f) / nn;
 }
 
 }  // namespace fclgpu

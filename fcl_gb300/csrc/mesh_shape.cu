@@ -386,6 +386,8 @@ __global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(M
     shape_obbrss(g.A.s, g.A.verts, g.Rs, g.ts, bv);
   ShapeBV32 b32;
   make_shape_bv32(g.Rm, g.tm, bv, g.m, b32);
+  LeafCert32 cert;
+  if (g.A.s.type != SHAPE_SPHERE) leaf_cert_init(g.A, g.Rs, g.ts, g.Rm, g.tm, cert);
   const int M = L.max_contacts;
   if (lane == 0) front[w][0] = 0;
   int size = 1, count = 0;
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(M
     if (ov && child < 0) {
       double P[9];
       load_tri_local(g.m, -(child + 1), P);
-      int h = shape_triangle_stage1(g.A, g.Rs, g.ts, P, g.Rm, g.tm);
+      int h = shape_triangle_stage1(cert, g.A, g.ts, P, g.Rm, g.tm);
       if (h == 1) {
         SimplexVert V[kSimplexSlots];
         h = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V) ? 2 : 0;
@@ -588,30 +590,6 @@ __device__ __forceinline__ float md_node_bound(const float4* rss32, int b, const
   return lb;
 }
 
-// certified lower bound of the shape-triangle distance: FP32 GJK to convergence, then
-// the support gap along its direction (the certificate of gjk32.cuh); dirA = that
-// direction in the shape's frame
-__device__ __forceinline__ float md_leaf_lb(const ShapeRef& A, const Pose32& pa, const ShapeRef& B, const Pose32& pb,
-                                            const Mink32& mk0, float S0, G3f& dirA) {
-  Mink32 mk = mk0;
-  mk.b = B;
-  const float S = S0 + shape_radius32(B);
-  G3f v;
-  if (gjk32(mk, CUDART_INF_F, v, S) != G32_SEPARATED) return -CUDART_INF_F;
-  const G3f D = rot32(pa.R, v);
-  const float n1 = (fabsf(D.x) + fabsf(D.y)) + fabsf(D.z);
-  const float nn = sqrtf(gdot(D, D));
-  if (!(nn > 0.f)) return -CUDART_INF_F;
-  const G3f uA = rot32T(pa.R, g3f(-D.x, -D.y, -D.z)), uB = rot32T(pb.R, D);
-  const float hA = gdot(uA, support32(A, uA)), hB = gdot(uB, support32(B, uB));
-  const G3f ta = g3f(pa.t[0], pa.t[1], pa.t[2]), tb = g3f(pb.t[0], pb.t[1], pb.t[2]);
-  const float gap = (gdot(D, ta) - hA) - (gdot(D, tb) + hB);
-  const float g = gap - 3.81469727e-06f * S * n1;  // 64u ||D||_1 S
-  if (!(g > 0.f)) return -CUDART_INF_F;
-  dirA = v;
-  return g * (1.f - 4.76837158e-07f) / nn;
-}
-
 template <bool WIT>
 __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(MeshShapeLaunch L) {
   __shared__ int32_t fnode[kMdWarps][kMdFront];
@@ -638,20 +616,12 @@ __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(Me
     const float T = fmaxf(fabsf(q.tr.x), fmaxf(fabsf(q.tr.y), fabsf(q.tr.z)));
     q.base = ((float)g.m.rmax * 1.0001f + T * 1.0001f) + q.rho;
   }
-  Pose32 pa, pb;
-  pose32(g.Rs, g.ts, pa);
-  pose32(g.Rm, g.tm, pb);
-  Mink32 mk0;
-  {
-    ShapeRef B0 = g.A;  // replaced per leaf
-    make_mink32(g.A, pa, B0, pb, mk0);
-  }
-  const float S0 = 1.f + q.rho + fmaxf(fabsf(pa.t[0]), fmaxf(fabsf(pa.t[1]), fabsf(pa.t[2]))) +
-                   fmaxf(fabsf(pb.t[0]), fmaxf(fabsf(pb.t[1]), fabsf(pb.t[2])));
+  const bool sphere = g.A.s.type == SHAPE_SPHERE;
+  LeafCert32 cert;
+  if (!sphere) leaf_cert_init(g.A, g.Rs, g.ts, g.Rm, g.tm, cert);
   const double m64 = ldexp(1.0 + (double)q.rho + fmax(fabs(g.ts.x), fmax(fabs(g.ts.y), fabs(g.ts.z))) +
                                fmax(fabs(g.tm.x), fmax(fabs(g.tm.y), fabs(g.tm.z))) + g.m.vmax + g.m.rmax,
                            -36);
-  const bool sphere = g.A.s.type == SHAPE_SPHERE;
   ShapeBV bv;  // FCL's model2_bv, for its FP64 bounds when two triangles tie
   if (L.bv_src)
     bv = static_cast<const ShapeBV*>(L.bv_table)[L.bv_src[i]];
@@ -733,7 +703,7 @@ __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(Me
       load_tri_local(g.m, -(child + 1), P);
       bool eval = true;
       if (!sphere) {
-        const float lbl = md_leaf_lb(g.A, pa, triangle_ref(P), pb, mk0, S0, ldir);
+        const float lbl = leaf_cert_lb(cert, P, ldir);
         has_dir = lbl > -CUDART_INF_F;
         eval = !((double)lbl > ub + m64);
       }

@@ -635,7 +635,19 @@ FCLG_HD int shape_triangle_stage1(const ShapeRef& A, const M3<double>& Rs, const
     return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 2
                                                                                                           : 0;
   }
-  return certified_disjoint(A, Rs, ts, triangle_ref(P), Rm, tm) ? 0 : 1;
+  LeafCert32 c;
+  leaf_cert_init(A, Rs, ts, Rm, tm, c);
+  return leaf_cert_disjoint(c, P) ? 0 : 1;
+}
+// the same with the pair's certificate data prepared once (leaf_cert_init(A, Rs, ts, Rm, tm))
+FCLG_HD int shape_triangle_stage1(LeafCert32& c, const ShapeRef& A, const D3v& ts, const double* P,
+                                  const M3<double>& Rm, const D3v& tm) {
+  if (A.s.type == SHAPE_SPHERE) {
+    const D3v P1 = v3(P[0], P[1], P[2]), P2 = v3(P[3], P[4], P[5]), P3 = v3(P[6], P[7], P[8]);
+    return sphere_triangle_intersect(A.s.p[0], ts, mulv(Rm, P1) + tm, mulv(Rm, P2) + tm, mulv(Rm, P3) + tm) ? 2
+                                                                                                          : 0;
+  }
+  return leaf_cert_disjoint(c, P) ? 0 : 1;
 }
 // The contact MeshShapeCollisionTraversalNodeOBBRSS::leafTesting records with
 // enable_contact (mesh_shape_collision_traversal_node-inl.h:233-244): shapeTriangleIntersect
