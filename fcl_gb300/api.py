@@ -1073,11 +1073,13 @@ class DynamicAABBTreeCollisionManager:
             dev = tf.device
             n = tf.shape[0]
             out = dict(min_distance=torch.empty(n, dtype=torch.float64, device=dev),
-                       object=torch.empty(n, dtype=torch.int32, device=dev),
-                       ids=torch.empty((n, 2), dtype=torch.int32, device=dev),
-                       nearest_points=torch.zeros((n, 2, 3), dtype=torch.float64, device=dev))
-            res = N.BpDistanceResult(out["min_distance"].data_ptr(), out["object"].data_ptr(), out["ids"].data_ptr(),
-                                     out["nearest_points"].data_ptr(), 0, 0)
+                       object=torch.empty(n, dtype=torch.int32, device=dev))
+            if witnesses:
+                out["ids"] = torch.empty((n, 2), dtype=torch.int32, device=dev)
+                out["nearest_points"] = torch.zeros((n, 2, 3), dtype=torch.float64, device=dev)
+            res = N.BpDistanceResult(out["min_distance"].data_ptr(), out["object"].data_ptr(),
+                                     out["ids"].data_ptr() if witnesses else None,
+                                     out["nearest_points"].data_ptr() if witnesses else None, 0, 0)
             s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
             N.check(N.lib().fclgpu_broadphase_distance_device(self.handle, refs.data_ptr(), n, tf.data_ptr(),
                                                               C.byref(req), C.byref(res), s),
