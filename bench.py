@@ -233,10 +233,13 @@ def run_serving(args):
     rate = args.serve_rate if args.serve_rate > 0 else 0.5 * burst["requests_per_s"]
     ph = (C.c_double * 16)()
     api.N.lib().fclgpu_broadphase_last_phase_ms(ph)  # reset the phase clocks
+    st0 = srv.stats()
     with ClockSampler(0) as cs:
         load = SV.run_poisson(srv, reqs[nb:], rate, seed=6)
     api.N.lib().fclgpu_broadphase_last_phase_ms(ph)
-    st = srv.stats()
+    st1 = srv.stats()
+    # the engine's counters over the Poisson run alone
+    st = {k: st1[k] - st0[k] for k in st1 if k != "max_step_waypoints"}
     srv.close()
     out = {
         "workload": f"scene of {w.n} objects (primitives and 500-5000-tri icospheres, 25% meshes) in a 20^3 box; "
@@ -251,8 +254,8 @@ def run_serving(args):
         "latency_p50_second_half_ms": load["latency_second_half_p50_ms"],
         "p50_ms": load["p50_ms"], "p99_ms": load["p99_ms"], "mean_ms": load["mean_ms"], "max_ms": load["max_ms"],
         "waypoints": int(sum(r.q.shape[0] for r in reqs[nb:])),
-        "engine": {k: st[k] for k in ("steps", "waypoints", "queries", "candidates", "busy_ms",
-                                      "max_step_waypoints")},
+        "engine": {k: st[k] for k in ("steps", "waypoints", "queries", "candidates", "busy_ms", "collide_ms",
+                                      "distance_ms")},
         # broadphase wall-clock phases over the Poisson run (fclgpu_broadphase_last_phase_ms):
         # setup + candidates, shape pairs, mesh-shape pairs, mesh-mesh pairs, reduction
         "phases_ms": {"collide": [round(x, 1) for x in ph[0:5]], "distance": [round(x, 1) for x in ph[8:13]]},

@@ -844,9 +844,11 @@ def _collide_batch_torch(meshes, hs, pairs, tf1, tf2, pair_of_query, req, statis
 
 
 def distance_batch(meshes, pairs, tf1, tf2, pair_of_query=None, nearest_points=True, precision="fp32",
-                   margins=None, statistics=False, stream=None):
+                   margins=None, statistics=False, stream=None, ids=True):
     """Batched fcl::distance.  Returns min_distance, ids (n,2), nearest_points (n,2,3)
-    world frame, optional within_margin (distance <= margin) and statistics."""
+    world frame, optional within_margin (distance <= margin) and statistics.  ids=False
+    with nearest_points=False asks for the distances alone."""
+    want_ids = bool(ids)
     pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
     req = N.DistanceRequest(int(bool(nearest_points)), _prec(precision), int(bool(statistics)), 0)
     hs = _handles(meshes)
@@ -855,11 +857,12 @@ def distance_batch(meshes, pairs, tf1, tf2, pair_of_query=None, nearest_points=T
         dev = tf2.device
         n = tf2.shape[0]
         d = torch.empty(n, dtype=torch.float64, device=dev)
-        ids = torch.empty((n, 2), dtype=torch.int32, device=dev)
+        ids = torch.empty((n, 2), dtype=torch.int32, device=dev) if want_ids else None
         pts = torch.zeros((n, 2, 3), dtype=torch.float64, device=dev) if nearest_points else None
         within = torch.empty(n, dtype=torch.int32, device=dev) if margins is not None else None
         st = [torch.zeros(n, dtype=torch.int64, device=dev) for _ in range(3)] if statistics else [None] * 3
-        res = N.DistanceResult(d.data_ptr(), ids.data_ptr(), None if pts is None else pts.data_ptr(),
+        res = N.DistanceResult(d.data_ptr(), None if ids is None else ids.data_ptr(),
+                               None if pts is None else pts.data_ptr(),
                                None if margins is None else margins.data_ptr(),
                                None if within is None else within.data_ptr(),
                                *(None if a is None else a.data_ptr() for a in st))
@@ -876,18 +879,21 @@ def distance_batch(meshes, pairs, tf1, tf2, pair_of_query=None, nearest_points=T
         pq = None if pair_of_query is None else np.ascontiguousarray(pair_of_query, np.int32)
         mg = None if margins is None else np.ascontiguousarray(margins, np.float64)
         d = np.empty(n, np.float64)
-        ids = np.empty((n, 2), np.int32)
+        ids = np.empty((n, 2), np.int32) if want_ids else None
         pts = np.zeros((n, 2, 3), np.float64) if nearest_points else None
         within = np.empty(n, np.int32) if margins is not None else None
         st = [np.zeros(n, np.int64) for _ in range(3)] if statistics else [None] * 3
-        res = N.DistanceResult(d.ctypes.data, ids.ctypes.data, None if pts is None else pts.ctypes.data,
+        res = N.DistanceResult(d.ctypes.data, None if ids is None else ids.ctypes.data,
+                               None if pts is None else pts.ctypes.data,
                                None if mg is None else mg.ctypes.data, None if within is None else within.ctypes.data,
                                *(None if a is None else a.ctypes.data for a in st))
         N.check(N.lib().fclgpu_distance_batch(
             hs, len(meshes), pairs.ctypes.data, pairs.shape[0], n, None if pq is None else pq.ctypes.data,
             None if tf1a is None else tf1a.ctypes.data, tf2.ctypes.data, C.byref(req), C.byref(res), stream),
             "fclgpu_distance_batch")
-    out = {"min_distance": d, "ids": ids}
+    out = {"min_distance": d}
+    if want_ids:
+        out["ids"] = ids
     if nearest_points:
         out["nearest_points"] = pts
     if margins is not None:

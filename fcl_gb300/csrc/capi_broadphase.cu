@@ -649,9 +649,16 @@ int distance_core(fclgpu_broadphase_s* bp, const BpQueryView& Q, const fclgpu_br
       CKB(launch_bp_gather_mesh(S, Q, pairs, g_bs.list.as<int64_t>(), nl, bp->nm, g_bs.m_pair.as<int32_t>(),
                                 g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), s),
           "mesh gather");
-      fclgpu_distance_request mr = {1, req->precision, 0, 0};
-      fclgpu_distance_result mres = {g_bs.m_dist.as<double>(), g_bs.m_ids.as<int32_t>(), g_bs.m_pts.as<double>(),
-                                     nullptr, nullptr, nullptr, nullptr, nullptr};
+      // without witnesses the mesh pairs report their distances alone (ids and points
+      // of the scatter below stay unset)
+      fclgpu_distance_request mr = {witness ? 1 : 0, req->precision, 0, 0};
+      fclgpu_distance_result mres = {g_bs.m_dist.as<double>(), witness ? g_bs.m_ids.as<int32_t>() : nullptr,
+                                     witness ? g_bs.m_pts.as<double>() : nullptr, nullptr, nullptr, nullptr, nullptr,
+                                     nullptr};
+      if (!witness) {
+        CKB(cudaMemsetAsync(g_bs.m_ids.p, 0xff, 8 * nl, s), "mesh scratch");
+        CKB(cudaMemsetAsync(g_bs.m_pts.p, 0, 48 * nl, s), "mesh scratch");
+      }
       const int rc = fclgpu_distance_batch_device(bp->meshes.data(), bp->nm, bp->mesh_pairs.data(),
                                                   bp->nm * bp->nm, nl, g_bs.m_pair.as<int32_t>(),
                                                   g_bs.m_tf1.as<double>(), g_bs.m_tf2.as<double>(), &mr, &mres,

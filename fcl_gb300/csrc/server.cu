@@ -230,6 +230,7 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
       cudaMemcpyAsync(s->d_bases, s->h_bases, 96 * chunks.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       launch_robot_fk(robot_dev(s), W, s->d_q, s->d_slot, s->d_bases, s->d_qtf, s->d_qrefs, st) != cudaSuccess)
     return FCLGPU_ERR_CUDA;
+  const auto tc0 = Clock::now();
   fclgpu_broadphase_collide_request creq = {1, s->cfg.precision, 0};
   fclgpu_broadphase_collide_result cres = {s->d_nc, nullptr, nullptr, 0, 0};
   int rc = fclgpu_broadphase_collide_device(s->scene, reinterpret_cast<const fclgpu_geometry_ref*>(s->d_qrefs), nq,
@@ -239,6 +240,7 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
   if (cudaMemcpyAsync(s->h_nc, s->d_nc, 8 * nq, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return FCLGPU_ERR_CUDA;
+  const auto tc1 = Clock::now();
   // first colliding waypoint (and its smallest link) per request
   w = 0;
   for (const Chunk& ch : chunks) {
@@ -261,6 +263,7 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
         for (int64_t qi = w * L; qi < (w + n) * L; ++qi) s->h_fidx[nfree++] = (int32_t)qi;
       w += n;
     }
+    const auto td0 = Clock::now();
     if (nfree > 0) {
       if (cudaMemcpyAsync(s->d_fmap, s->h_fidx, 4 * nfree, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return FCLGPU_ERR_CUDA;
@@ -279,6 +282,7 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
           cudaStreamSynchronize(st) != cudaSuccess)
         return FCLGPU_ERR_CUDA;
     }
+    s->stats.distance_ms += ms_between(td0, Clock::now());
     // clearance: minimum over the contact-free queries (ties: smallest waypoint, then
     // link); 0 at the first contact
     int64_t f = 0;
@@ -311,6 +315,7 @@ int run_step(fclgpu_server_s* s, const std::vector<Chunk>& chunks, int64_t W) {
   s->cand_per_query = 0.5 * s->cand_per_query + 0.5 * std::max(1.0, (double)cand / (double)std::max<int64_t>(nq, 1));
   s->stats.queries += nq;
   s->stats.candidates += cand;
+  s->stats.collide_ms += ms_between(tc0, tc1);
   return FCLGPU_OK;
 }
 

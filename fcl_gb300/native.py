@@ -143,7 +143,8 @@ class MotionResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("waypoints", C.c_int64), ("queries", C.c_int64), ("candidates", C.c_int64),
-                ("busy_ms", C.c_double), ("max_step_waypoints", C.c_int64)]
+                ("busy_ms", C.c_double), ("max_step_waypoints", C.c_int64), ("collide_ms", C.c_double),
+                ("distance_ms", C.c_double)]
 
 
 class MeshShapeRequest(C.Structure):

@@ -779,6 +779,8 @@ typedef struct {
   int64_t candidates;
   double busy_ms;          /* wall time spent in steps */
   int64_t max_step_waypoints;
+  double collide_ms;       /* of busy_ms: the broadphase collide calls and their read-back */
+  double distance_ms;      /* of busy_ms: the clearance pass (gather, distance, read-back) */
 } fclgpu_server_stats;
 
 typedef struct fclgpu_server_s* fclgpu_server;

@@ -208,6 +208,42 @@ def test_distance_fp32_tf1_and_fixture(gpu_lib, golden):
     _dist_check(out, d, pts)
 
 
+def test_distance_values_alone_match_oracle(gpu_lib):
+    """ids=False, nearest_points=False: one warp per query (certified FP32 bounds, FP64
+    triDistance near the best) -- the distances equal the full call's bit for bit and
+    the oracle's up to one FP64 rounding, for separated multi-pair poses, for touching
+    and intersecting poses, and after a vertex update (refitted volumes: the FP64
+    form)."""
+    w = W.config2(total_poses=3000, n_pairs=6, tri_hi=30000, seed=7)
+    ms = _meshes(w)
+    full = api.distance_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, nearest_points=True,
+                              precision="fp32")
+    vals = api.distance_batch(ms, w.pairs, None, w.tf2, pair_of_query=w.pair, nearest_points=False, ids=False,
+                              precision="fp32")
+    assert "ids" not in vals
+    np.testing.assert_array_equal(vals["min_distance"], full["min_distance"])
+    om = [O.Mesh(v, t) for v, t in w.meshes]
+    for p in range(w.pairs.shape[0]):
+        idx = np.nonzero(w.pair == p)[0]
+        dd, _, _, _, _ = O.distance_batch(om[w.pairs[p, 0]], om[w.pairs[p, 1]], w.tf2[idx], nearest=False,
+                                          nthreads=8)
+        # the smallest FP64 triDistance over all triangle pairs; FCL's may be the same
+        # distance through another pair (a shared vertex), rounded differently
+        np.testing.assert_allclose(vals["min_distance"][idx], dd, rtol=4e-16, atol=0)
+    w0 = W.config0(n_poses=600, seed=8)
+    m0 = _meshes(w0)
+    a = O.Mesh(*w0.meshes[0]); b = O.Mesh(*w0.meshes[1])
+    for step in range(2):
+        v0 = api.distance_batch(m0, w0.pairs, None, w0.tf2, nearest_points=False, ids=False, precision="fp32")
+        d0, _, _, _, _ = O.distance_batch(a, b, w0.tf2, nearest=False, nthreads=8)
+        np.testing.assert_allclose(v0["min_distance"], d0, rtol=4e-16, atol=0)
+        if step == 0:
+            assert (d0 == 0).any() and (d0 > 0).any()
+            v1 = w0.meshes[1][0] + np.random.default_rng(9).normal(0, 0.003, w0.meshes[1][0].shape)
+            m0[1].update_vertices(v1)
+            b.update(v1)
+
+
 def test_distance_rejects_out_of_range_pair_index(gpu_lib):
     """A pair index outside the pair table is not read: the device entry point skips
     that query, sets the status word and returns FCLGPU_ERR_DEVICE_STATUS; the other
