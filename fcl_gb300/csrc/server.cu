@@ -24,10 +24,11 @@ namespace fclgpu {
 namespace {
 
 constexpr int kMaxLinks = 64;
-// waypoints of one request per step: the first chunk is short and each next one twice
-// as long up to kRequestChunk, so a request that collides early stops having checked few
-// waypoints past its contact, and a long contact-free request needs few steps
-constexpr int kFirstChunk = 8;
+// waypoints of one request per step: the first chunk is one waypoint and each next one
+// twice as long up to kRequestChunk, so a request checks at most about twice the
+// waypoints up to its first contact (in a cluttered scene most requests collide at
+// their first waypoints), and a long contact-free request needs few steps
+constexpr int kFirstChunk = 1;
 constexpr int kRequestChunk = 512;
 
 struct RobotDev {
