@@ -326,9 +326,12 @@ typedef struct {
   int32_t reserved;
 } fclgpu_distance_request;
 
-/* min_distance[n] always; ids[2n] (b1,b2); nearest_points[6n] (world frame, p1 then
- * p2) when requested; optional margins[n] + within_margin[n] give the tolerance
- * check distance <= margin (int32 0/1). */
+/* min_distance[n] always; ids[2n] (b1,b2) and nearest_points[6n] (world frame, p1 then
+ * p2) when given (nearest_points also needs enable_nearest_points); optional margins[n]
+ * + within_margin[n] give the tolerance check distance <= margin (int32 0/1).  With
+ * FCLGPU_FP32_RECHECK and none of ids, nearest points, margins or statistics, batches
+ * of up to 65,536 queries take the distances alone one warp per query (the same
+ * values). */
 typedef struct {
   double* min_distance;
   int32_t* ids;
