@@ -247,7 +247,7 @@ def run_serving(args):
         "objects": w.n, "links": w.robot.n_links,
         "capacity_requests_per_s": burst["requests_per_s"],
         "capacity_measure": "the same requests submitted at once",
-        "arrival_rate_per_s": rate, "requests": load["requests"],
+        "arrival_rate_per_s": rate, "offered_rate_per_s": load["offered_rate_per_s"], "requests": load["requests"],
         "throughput_requests_per_s": load["throughput_requests_per_s"],
         "sustained_requests_per_s": load["sustained_requests_per_s"],
         "latency_p50_first_half_ms": load["latency_first_half_p50_ms"],

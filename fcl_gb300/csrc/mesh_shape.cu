@@ -425,7 +425,15 @@ __global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(M
       int h = shape_triangle_stage1(cert, g.A, g.ts, P, g.Rm, g.tm);
       if (h == 1) {
         SimplexVert V[kSimplexSlots];
-        h = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V) ? 2 : 0;
+        if (L.group)  // a long GJK gives up once the query has its contacts from other pairs
+          h = shape_triangle_gjk64_until(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, [&] {
+                return *(volatile unsigned long long*)&L.group_count[L.group[i]] >=
+                       (unsigned long long)L.group_max;
+              })
+                  ? 2
+                  : 0;
+        else
+          h = shape_triangle_gjk64(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V) ? 2 : 0;
       }
       hit = h == 2;
     }

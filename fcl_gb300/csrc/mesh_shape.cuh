@@ -685,6 +685,22 @@ FCLG_HD bool shape_triangle_gjk64(const ShapeRef& A, const M3<double>& Rs, const
   return g.evaluate(d3neg(v3(1.0, 0.0, 0.0)), sp.gjk_max_iterations) == GJK_INSIDE;
 }
 
+// shape_triangle_gjk64 that gives up (false) once stop() reports that the answer is no
+// longer needed (asked every 8 GJK iterations); otherwise the same result
+template <class Stop>
+FCLG_HD bool shape_triangle_gjk64_until(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
+                                        const M3<double>& Rm, const D3v& tm, SimplexVert* V, Stop stop) {
+  GjkState g;
+  make_minkowski(A, Rs, ts, triangle_ref(P), Rm, tm, g.shape);
+  const SolverParams sp = solver_params();
+  g.V = V;
+  g.tolerance = sp.gjk_tolerance;
+  g.begin(d3neg(v3(1.0, 0.0, 0.0)), sp.gjk_max_iterations);
+  for (int it = 1; !g.step(); ++it)
+    if ((it & 7) == 0 && stop()) return false;
+  return g.finish() == GJK_INSIDE;
+}
+
 // shapeTriangleDistance; ps on the shape, pt on the triangle, in FCL's frames
 FCLG_HD bool shape_triangle_distance(const ShapeRef& A, const M3<double>& Rs, const D3v& ts, const double* P,
                                      const M3<double>& Rm, const D3v& tm, SimplexVert* V, double& d, D3v& ps,

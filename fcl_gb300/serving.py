@@ -31,6 +31,7 @@ def run_poisson(server, requests, rate: float, seed: int = 0) -> dict:
     ids: list = [None] * len(requests)
     ready = [threading.Event() for _ in requests]
     results: list = [None] * len(requests)
+    submit_at = np.zeros(len(requests))
     t0 = time.perf_counter()
 
     def submitter():
@@ -38,16 +39,15 @@ def run_poisson(server, requests, rate: float, seed: int = 0) -> dict:
             delay = arrivals[i] - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
+            submit_at[i] = time.perf_counter() - t0
             ids[i] = server.submit(r.base, r.q)
             ready[i].set()
 
     th = threading.Thread(target=submitter)
     th.start()
-    done_at = np.zeros(len(requests))
     for i in range(len(requests)):
         ready[i].wait()
         results[i] = server.wait(ids[i])
-        done_at[i] = time.perf_counter() - t0
     th.join()
     t_end = time.perf_counter()
     lat = np.array([r["latency_ms"] for r in results])
@@ -55,15 +55,19 @@ def run_poisson(server, requests, rate: float, seed: int = 0) -> dict:
     # steady state: completions per second over the middle 60 % of the arrival window
     # (the first 20 % fill the pipeline, the drain after the last arrival is excluded); a
     # server that keeps up completes requests at the arrival rate there, and its latency
-    # does not grow with the arrival index
+    # does not grow with the arrival index.  A request completes at its submission plus
+    # the latency the server measured (submit -> result), not when this thread, which
+    # collects the results in submission order, gets to it.
     T = float(arrivals[-1])
     lo_t, hi_t = 0.2 * T, 0.8 * T
-    done_in = int(np.count_nonzero((done_at >= lo_t) & (done_at < hi_t)))
+    completed = submit_at + lat / 1e3
+    done_in = int(np.count_nonzero((completed >= lo_t) & (completed < hi_t)))
     half = len(requests) // 2
     return {
         "requests": len(requests),
         "arrival_rate_per_s": rate,
         "offered_seconds": T,
+        "offered_rate_per_s": (len(requests) - 1) / float(submit_at[-1] - submit_at[0]) if len(requests) > 1 else float("nan"),
         "seconds": t_end - t0,
         "throughput_requests_per_s": len(requests) / (t_end - t0),
         "sustained_requests_per_s": done_in / (hi_t - lo_t) if hi_t > lo_t else float("nan"),
