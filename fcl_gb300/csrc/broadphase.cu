@@ -707,11 +707,21 @@ __global__ void __launch_bounds__(128) k_bp_shape_bvs(BpSceneView S, BpQueryView
   for (long long src = (long long)blockIdx.x * blockDim.x + threadIdx.x; src < n; src += stride) {
     if (!need[src]) continue;
     const bool is_q = src < Q.nq;
-    const GeomRec& g = S.geoms[is_q ? Q.gid[src] : S.gid[src - Q.nq]];
+    const long long o = src - Q.nq;
+    ShapeBV* cache = static_cast<ShapeBV*>(S.bv_cache);
+    if (!is_q && S.bv_ok && S.bv_ok[o]) {  // a scene object keeps its pose between updates
+      table[src] = cache[o];
+      continue;
+    }
+    const GeomRec& g = S.geoms[is_q ? Q.gid[src] : S.gid[o]];
     M3<double> R;
     D3v t;
-    load_tf(is_q ? Q.tf + 12 * src : S.tf + 12 * (src - Q.nq), R, t);
+    load_tf(is_q ? Q.tf + 12 * src : S.tf + 12 * o, R, t);
     shape_obbrss(S.shapes[g.index], S.sverts, R, t, table[src]);
+    if (!is_q && S.bv_ok) {
+      cache[o] = table[src];
+      S.bv_ok[o] = 1;
+    }
   }
 }
 

@@ -56,6 +56,11 @@ struct BpSceneView {
   const double* tf;      // 12 per object
   const double* aabb64;  // 6 per object (min, max), FCL's CollisionObject::getAABB()
   const BpNode* nodes;
+  // shape BVs of the scene's objects at their current poses (ShapeBV records), fitted
+  // at their first mesh-shape pair after a pose update: bv_ok[o] != 0 once bv_cache[o]
+  // holds object o's; both null = no cache
+  void* bv_cache = nullptr;
+  int32_t* bv_ok = nullptr;
 };
 
 // ---------------------------------------------------------------- build ----

@@ -37,6 +37,8 @@ struct fclgpu_broadphase_s {
   void* build_scratch = nullptr;
   DevMesh* dmeshes = nullptr;  // device table of the meshes, for mesh-shape pairs
   int max_depth = 0;
+  void* sbv = nullptr;         // the objects' shape BVs at their current poses (ShapeBV)
+  int32_t* sbv_ok = nullptr;   // per object: sbv holds its BV (reset by every pose update)
 };
 
 namespace {
@@ -190,12 +192,15 @@ BpSceneView scene_view(const fclgpu_broadphase_s* bp) {
   S.tf = bp->tf;
   S.aabb64 = bp->aabb64;
   S.nodes = bp->nodes;
+  S.bv_cache = bp->sbv;
+  S.bv_ok = bp->sbv_ok;
   return S;
 }
 
 // AABBs + tree for the current poses
 int rebuild(fclgpu_broadphase_s* bp, cudaStream_t s) {
   if (bp->n == 0) return FCLGPU_OK;
+  if (bp->sbv_ok) CKB(cudaMemsetAsync(bp->sbv_ok, 0, 4 * (size_t)bp->n, s), "shape BV cache");
   CKB(launch_world_aabbs(bp->geoms, bp->n, bp->gid, bp->tf, bp->aabb64, bp->aabb32, s), "world aabbs");
   if (bp->n >= 2) {
     CKB(launch_lbvh_build(bp->n, bp->aabb32, bp->nodes, bp->build_scratch, s), "lbvh build");
@@ -209,7 +214,7 @@ int rebuild(fclgpu_broadphase_s* bp, cudaStream_t s) {
 
 void free_bp(fclgpu_broadphase_s* bp) {
   for (void* p : {(void*)bp->geoms, (void*)bp->gid, (void*)bp->tf, (void*)bp->aabb64, (void*)bp->aabb32,
-                  (void*)bp->nodes, bp->build_scratch, (void*)bp->dmeshes})
+                  (void*)bp->nodes, bp->build_scratch, (void*)bp->dmeshes, bp->sbv, (void*)bp->sbv_ok})
     if (p) cudaFree(p);
   delete bp;
 }
@@ -448,6 +453,8 @@ int fclgpu_broadphase_create(fclgpu_shapeset shapes, const fclgpu_mesh* meshes, 
   if (e == cudaSuccess) e = cudaMalloc(&bp->aabb32, 24 * n);
   if (e == cudaSuccess) e = cudaMalloc(&bp->nodes, sizeof(BpNode) * n);
   if (e == cudaSuccess) e = cudaMalloc(&bp->build_scratch, bp_build_scratch_bytes((int64_t)n));
+  if (e == cudaSuccess && shapes) e = cudaMalloc(&bp->sbv, sizeof(ShapeBV) * n);
+  if (e == cudaSuccess && shapes) e = cudaMalloc(&bp->sbv_ok, 4 * n);
   if (e == cudaSuccess && !geoms.empty())
     e = cudaMemcpy(bp->geoms, geoms.data(), sizeof(GeomRec) * geoms.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && num_objects > 0) e = cudaMemcpy(bp->gid, gid.data(), 4 * n, cudaMemcpyHostToDevice);

@@ -78,20 +78,26 @@ def test_broadphase_mixed_scene_matches_oracle(gpu_lib):
     G = P.Geoms(shapes, om)
     gid = np.where(refs[:, 0] == 1, 64 + refs[:, 1], refs[:, 1]).astype(np.int32)
     qgid = np.where(qrefs[:, 0] == 1, 64 + qrefs[:, 1], qrefs[:, 1]).astype(np.int32)
-    S = P.Scene(G, gid, tf)
-    np.testing.assert_array_equal(mgr.getAABBs(), G.world_aabbs(gid, tf))
-    for M in (1, 100000):
-        o = S.collide(qgid, qtf, max_contacts=M, use_tree=True, nthreads=8)
-        for ex in (False, True):
-            g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M, exhaustive=ex)
-            np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
-    assert (g["num_contacts"] > 0).any()
-    d = mgr.distance_batch(qrefs, qtf)
-    o = S.distance(qgid, qtf, use_tree=True, nthreads=8)
-    np.testing.assert_array_equal(d["min_distance"] <= 0, o["dist"] <= 0)
-    sep = o["dist"] > 0
-    r = o["dist"][sep]
-    assert np.all(np.abs(d["min_distance"][sep] - r) <= np.maximum(1e-6 * np.abs(r), 1e-9))
+    # twice: the second time after moving every object (the scene objects' shape BVs are
+    # kept between calls and must be refitted after an update)
+    for rep in range(2):
+        if rep == 1:
+            tf = W.random_poses(n, 0.0, 8.0, 25)
+            mgr.update(tf)
+        S = P.Scene(G, gid, tf)
+        np.testing.assert_array_equal(mgr.getAABBs(), G.world_aabbs(gid, tf))
+        for M in (1, 100000):
+            o = S.collide(qgid, qtf, max_contacts=M, use_tree=True, nthreads=8)
+            for ex in (False, True):
+                g = mgr.collide_batch(qrefs, qtf, num_max_contacts=M, exhaustive=ex)
+                np.testing.assert_array_equal(g["num_contacts"], o["num_contacts"])
+        assert (g["num_contacts"] > 0).any()
+        d = mgr.distance_batch(qrefs, qtf)
+        o = S.distance(qgid, qtf, use_tree=True, nthreads=8)
+        np.testing.assert_array_equal(d["min_distance"] <= 0, o["dist"] <= 0)
+        sep = o["dist"] > 0
+        r = o["dist"][sep]
+        assert np.all(np.abs(d["min_distance"][sep] - r) <= np.maximum(1e-6 * np.abs(r), 1e-9))
 
 
 def test_mesh_shape_distance_ties_and_refit_match_oracle(gpu_lib):
