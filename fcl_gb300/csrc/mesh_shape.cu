@@ -499,11 +499,12 @@ constexpr int kMdWarpMaxDepth = kMdFront / 32 - 4;
 
 // one compare-exchange network sorting 64 entries held two per lane (entry e = lane +
 // 32 * slot) by (key, node), ascending; pay travels with its entry
-__device__ __forceinline__ bool md_less(float ka, int na, float kb, int nb) {
+template <class K>
+__device__ __forceinline__ bool md_less(K ka, int na, K kb, int nb) {
   return ka < kb || (ka == kb && na < nb);
 }
-__device__ __forceinline__ void md_sort64(float& k0, int& n0, unsigned& p0, float& k1, int& n1, unsigned& p1,
-                                          int lane) {
+template <class K>
+__device__ __forceinline__ void md_sort64(K& k0, int& n0, unsigned& p0, K& k1, int& n1, unsigned& p1, int lane) {
   const unsigned full = 0xffffffffu;
 #pragma unroll
   for (int k = 2; k <= 64; k <<= 1) {
@@ -511,7 +512,7 @@ __device__ __forceinline__ void md_sort64(float& k0, int& n0, unsigned& p0, floa
     for (int j = k >> 1; j > 0; j >>= 1) {
       if (j == 32) {  // partner in the other slot of the same lane (k == 64: ascending)
         if (md_less(k1, n1, k0, n0)) {
-          const float tk = k0;
+          const K tk = k0;
           const int tn = n0;
           const unsigned tp = p0;
           k0 = k1;
@@ -525,11 +526,11 @@ __device__ __forceinline__ void md_sort64(float& k0, int& n0, unsigned& p0, floa
       }
 #pragma unroll
       for (int slot = 0; slot < 2; ++slot) {
-        float& kk = slot ? k1 : k0;
+        K& kk = slot ? k1 : k0;
         int& nn = slot ? n1 : n0;
         unsigned& pp = slot ? p1 : p0;
         const int e = lane + 32 * slot;
-        const float pk = __shfl_xor_sync(full, kk, j);
+        const K pk = __shfl_xor_sync(full, kk, j);
         const int pn = __shfl_xor_sync(full, nn, j);
         const unsigned ppay = __shfl_xor_sync(full, pp, j);
         const bool up = (e & k) == 0;
@@ -788,8 +789,136 @@ __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(Me
     __syncwarp();
   }
   if (serial) {
-    if (lane == 0) L.dist[i] = CUDART_NAN;
-    return;
+    // A triangle at distance <= 0.  FCL's traversal then ends at the first intersecting
+    // triangle (-1) it meets: bounds are >= 0, so nothing passes canStop after it.  That
+    // is the first intersecting triangle in its depth-first order (children ordered by
+    // its FP64 bounds, the second first on d2 < d1) whenever every volume on that
+    // triangle's path has the FP64 bound 0 (an intersecting triangle's volumes overlap
+    // the shape's, and FCL's RSS distance clamps at 0) and no triangle before it is at
+    // distance exactly 0 (the running minimum then stays above 0, so those volumes pass
+    // canStop).  The warp searches the volumes whose certified FP32 bound is within m64
+    // of 0 in that order, 32 at a time (stack sorted by order path, earliest on top),
+    // drops every volume after the best intersecting triangle found, and hands the pair
+    // to FCL's serial traversal when a condition fails (a triangle at exactly 0, a
+    // positive bound on the winner's path, triangle 0 at 0).
+    bool cm_ok = true;
+    int cbest = -1;
+    {
+      double d0 = 0.0;
+      if (lane == 0) {
+        double P[9];
+        load_tri_local(g.m, 0, P);
+        SimplexVert V[kSimplexSlots];
+        D3v ps, pt;
+        shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d0, ps, pt);
+      }
+      d0 = __shfl_sync(full, d0, 0);
+      if (d0 < 0.0)
+        cbest = 0;  // FCL's seed intersects: its result at once
+      else if (d0 == 0.0)
+        cm_ok = false;
+    }
+    if (cm_ok && cbest < 0) {
+      // order path: bits from 31 down (0 = the child FCL enters first), a marker bit after
+      // them, bit 0 = every FP64 bound on the path so far is 0
+      unsigned best_key = 0xffffffffu;
+      bool best_zero = false;
+      __syncwarp();
+      if (lane == 0) {
+        fnode[w][0] = 0;
+        fpath[w][0] = 0x80000000u | 1u;
+      }
+      int csize = 1;
+      __syncwarp();
+      while (csize > 0) {
+        const int take = csize < 32 ? csize : 32;
+        int b = -1;
+        unsigned key = 0;
+        if (lane < take) {
+          b = fnode[w][csize - 1 - lane];
+          key = fpath[w][csize - 1 - lane];
+        }
+        csize -= take;
+        __syncwarp();
+        if (b >= 0 && (key & ~31u) > (best_key & ~31u)) b = -1;  // after the best in FCL's order
+        int child = 0;
+        if (b >= 0) child = g.m.nodes64[b].child;
+        const bool inner = b >= 0 && child >= 0;
+        unsigned k0 = 0xffffffffu, k1 = 0xffffffffu;
+        int n0 = -1, n1 = -1;
+        unsigned p0 = 0, p1 = 0;
+        if (inner) {
+          const float l1 = md_node_bound(rss32, child, g.A, q, false, dir);
+          const float l2 = md_node_bound(rss32, child + 1, g.A, q, false, dir);
+          const double d1 = bvd(child), d2 = bvd(child + 1);
+          const unsigned second_first = d2 < d1 ? 1u : 0u;
+          const unsigned base = key & ~31u, zero = key & 1u;
+          if ((double)l1 <= m64) {
+            k0 = md_child_path(base, (int)second_first) | (zero & (d1 == 0.0 ? 1u : 0u));
+            n0 = child;
+          }
+          if ((double)l2 <= m64) {
+            k1 = md_child_path(base, (int)(second_first ^ 1u)) | (zero & (d2 == 0.0 ? 1u : 0u));
+            n1 = child + 1;
+          }
+        }
+        double d = 1.0;
+        if (b >= 0 && child < 0) {
+          double P[9];
+          load_tri_local(g.m, -(child + 1), P);
+          bool eval = true;
+          if (!sphere) {
+            G3f dd;
+            eval = !((double)leaf_cert_lb(cert, P, dd) > m64);
+          }
+          if (eval) {
+            SimplexVert V[kSimplexSlots];
+            D3v ps, pt;
+            shape_triangle_distance(g.A, g.Rs, g.ts, P, g.Rm, g.tm, V, d, ps, pt);
+            if (d == 0.0) cm_ok = false;
+          }
+        }
+        if (__any_sync(full, !cm_ok)) {
+          cm_ok = false;
+          break;
+        }
+        // the earliest intersecting triangle of the step
+        unsigned kc = d < 0.0 ? (key & ~31u) : 0xffffffffu;
+        for (int off = 16; off > 0; off >>= 1) kc = min(kc, __shfl_xor_sync(full, kc, off));
+        if (kc < (best_key & ~31u)) {
+          const int l = __ffs(__ballot_sync(full, d < 0.0 && (key & ~31u) == kc)) - 1;
+          cbest = __shfl_sync(full, -(child + 1), l);
+          best_key = __shfl_sync(full, key, l);
+          best_zero = (best_key & 1u) != 0;
+        }
+        if ((k0 & ~31u) > (best_key & ~31u)) n0 = -1, k0 = 0xffffffffu;
+        if ((k1 & ~31u) > (best_key & ~31u)) n1 = -1, k1 = 0xffffffffu;
+        const int np = __popc(__ballot_sync(full, n0 >= 0)) + __popc(__ballot_sync(full, n1 >= 0));
+        if (np == 0) continue;
+        if (csize + np > kMdFront) {
+          cm_ok = false;
+          break;
+        }
+        md_sort64(k0, n0, p0, k1, n1, p1, lane);
+        if (lane < np) {
+          fnode[w][csize + np - 1 - lane] = n0;
+          fpath[w][csize + np - 1 - lane] = k0;
+        }
+        if (lane + 32 < np) {
+          fnode[w][csize + np - 33 - lane] = n1;
+          fpath[w][csize + np - 33 - lane] = k1;
+        }
+        csize += np;
+        __syncwarp();
+      }
+      if (cbest < 0 || !best_zero) cm_ok = false;
+    }
+    if (!cm_ok) {
+      if (lane == 0) L.dist[i] = CUDART_NAN;
+      return;
+    }
+    ub = -1.0;
+    best = cbest;
   }
   if (lane == 0) {
     L.dist[i] = ub;
