@@ -467,29 +467,18 @@ __global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(M
 // shapeTriangleDistance.  Of tied triangles the first in FCL's order wins: triangle 0
 // (the seed) first, otherwise the one on the side FCL enters first at the two leaves'
 // deepest common node (FCL's FP64 bounds of that node's children, the nearer first,
-// the second child on d2 < d1).  A pair leaves this path, for k_ms_dist_serial to run
-// FCL's own traversal, when a triangle's distance is <= 0 (touching or intersecting,
-// where FCL's first-met rule decides the value) or when its mesh was refitted (FCL's
-// merged volumes then need not bound their triangles).
+// the second child on d2 < d1).  A triangle at distance <= 0 (touching or
+// intersecting, where FCL's first-met rule decides the value) switches the pair to the
+// search described below the main loop; a pair whose mesh was refitted (FCL's merged
+// volumes then need not bound their triangles), or where that search's conditions
+// fail, is handed to k_ms_dist_serial, which runs FCL's own traversal.
 //
-// Node bound along a direction n (mesh frame; any n != 0 gives a valid bound):
-//   dist(shape, RSS) >= (min_shape n.x - max_RSS n.y) / |n|,
-//   max_RSS n.y = n.To + l0 max(0, n.a0) + l1 max(0, n.a1) + r|n|,
-//   min_shape n.x = n.t - h_A(-Rrel^T n)   (h_A the shape's support function),
-// with (Rrel, t) the shape's pose in the mesh frame and the RSS data FCL's FP64 values
-// rounded to FP32.  Forward error (u = 2^-24, no fused multiply-adds): 3-term dot
-// products of rounded inputs err by 4.1u ||n||_1 times the input's magnitude (|To| <=
-// rmax, |t_i| <= T, unit axes); the clamped axis terms by 6.2u ||n||_1 l; r|n| by 4.1u
-// ||n||_1 r; the rotated direction by 4.1u ||n||_1 per component, moving the support
-// value by at most sqrt(3) that times the shape's radius rho, and the support value
-// itself by under 10u ||n||_1 rho; the six final additions by 6u ||n||_1 times the sum
-// of the magnitudes.  Together under 24u ||n||_1 (rmax + T + rho + l0 + l1 + r); the
-// bound subtracts 32u ||n||_1 (...) (times 1.01 for its own rounding) and scales the
-// quotient by 1 - 8u (the division and |n|).  Two directions are tried: from the RSS
-// rectangle's point nearest to the shape's origin to that origin, and the separating
-// direction of the best triangle so far (its FP32 GJK direction).  Leaf bound: FP32
-// GJK on (shape, triangle) to convergence, then the support gap along its direction
-// with the error bound of gjk32.cuh (under 40u ||D||_1 S; 64u is subtracted).
+// Node bounds: md_node_bound (mesh_shape.cuh, with its error derivation), along two
+// directions: from the RSS rectangle's point nearest to the shape's origin to that
+// origin, and the separating direction of the best triangle so far (its FP32 GJK
+// direction).  Leaf bound: leaf_cert_lb (gjk32.cuh): FP32 GJK on (shape, triangle) to
+// convergence, then the support gap along its direction (under 40u ||D||_1 S of error;
+// 64u is subtracted).
 constexpr int kMdWarps = 2;
 constexpr int kMdFront = 1024;
 constexpr int kMdWarpMaxDepth = kMdFront / 32 - 4;
@@ -555,50 +544,6 @@ __device__ __forceinline__ unsigned md_child_path(unsigned path, int which) {
   return (path & ~(1u << m)) | ((unsigned)which << m) | (1u << (m - 1));
 }
 
-struct MdPair {
-  float Rr[9];   // the shape's rotation in the mesh frame (row-major)
-  G3f tr;        // the shape's origin in the mesh frame
-  float rho;     // the shape's radius bound
-  float base;    // rmax + T + rho of the node error bound
-};
-
-// certified lower bound of the distance between the shape and node b's RSS along n
-__device__ __forceinline__ float md_node_lb(const float4* rss32, int b, const ShapeRef& A, const MdPair& q, G3f n,
-                                            float l0, float l1, float r, G3f To, G3f a0, G3f a1) {
-  const float nn = sqrtf(gdot(n, n));
-  if (!(nn > 0.f)) return -CUDART_INF_F;
-  const float n1 = (fabsf(n.x) + fabsf(n.y)) + fabsf(n.z);
-  const float hR = ((gdot(n, To) + l0 * fmaxf(0.f, gdot(n, a0))) + l1 * fmaxf(0.f, gdot(n, a1))) + r * nn;
-  const G3f uA = rot32T(q.Rr, n);
-  const G3f mu = g3f(-uA.x, -uA.y, -uA.z);
-  const float hA = gdot(mu, support32(A, mu));
-  const float gap = (gdot(n, q.tr) - hA) - hR;
-  const float E = 1.90734863e-06f * n1 * ((q.base + l0) + (l1 + r)) * 1.01f;  // 32u
-  const float g = gap - E;
-  if (!(g > 0.f)) return -CUDART_INF_F;
-  return g * (1.f - 4.76837158e-07f) / nn;  // 1 - 8u
-}
-
-__device__ __forceinline__ float md_node_bound(const float4* rss32, int b, const ShapeRef& A, const MdPair& q,
-                                               bool have_dir, G3f dir) {
-  const float4 c0 = __ldg(rss32 + 5 * (long long)b), c1 = __ldg(rss32 + 5 * (long long)b + 1);
-  const float4 x0 = __ldg(rss32 + 5 * (long long)b + 2), x1 = __ldg(rss32 + 5 * (long long)b + 3);
-  const float4 x2 = __ldg(rss32 + 5 * (long long)b + 4);
-  const G3f To = g3f(c0.x, c0.y, c0.z), a0 = g3f(x0.x, x0.y, x0.z), a1 = g3f(x1.x, x1.y, x1.z);
-  const float r = c0.w, l0 = c1.x, l1 = c1.y;
-  // from the rectangle's point nearest to the shape's origin
-  const G3f d = q.tr - To;
-  const float s = fminf(fmaxf(gdot(d, a0), 0.f), l0), t = fminf(fmaxf(gdot(d, a1), 0.f), l1);
-  G3f n = d - a0 * s - a1 * t;
-  if (!(gdot(n, n) > 1e-12f * (gdot(d, d) + 1e-30f))) {
-    const G3f a2 = g3f(x2.x, x2.y, x2.z);
-    n = gdot(d, a2) >= 0.f ? a2 : g3f(-a2.x, -a2.y, -a2.z);
-  }
-  float lb = md_node_lb(rss32, b, A, q, n, l0, l1, r, To, a0, a1);
-  if (have_dir) lb = fmaxf(lb, md_node_lb(rss32, b, A, q, dir, l0, l1, r, To, a0, a1));
-  return lb;
-}
-
 template <bool WIT>
 __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(MeshShapeLaunch L) {
   __shared__ int32_t fnode[kMdWarps][kMdFront];
@@ -616,15 +561,7 @@ __global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(Me
   }
   const float4* rss32 = static_cast<const float4*>(g.m.rss32);
   MdPair q;
-  {
-    const M3<double> Rrel = mulT(g.Rm, g.Rs);
-    const D3v trel = mulTv(g.Rm, g.ts - g.tm);
-    for (int k = 0; k < 9; ++k) q.Rr[k] = (float)Rrel.m[k];
-    q.tr = g3f((float)trel.x, (float)trel.y, (float)trel.z);
-    q.rho = shape_radius32(g.A);
-    const float T = fmaxf(fabsf(q.tr.x), fmaxf(fabsf(q.tr.y), fabsf(q.tr.z)));
-    q.base = ((float)g.m.rmax * 1.0001f + T * 1.0001f) + q.rho;
-  }
+  md_pair(g.m, g.A, g.Rm, g.tm, g.Rs, g.ts, q);
   const bool sphere = g.A.s.type == SHAPE_SPHERE;
   LeafCert32 cert;
   if (!sphere) leaf_cert_init(g.A, g.Rs, g.ts, g.Rm, g.tm, cert);

@@ -823,6 +823,73 @@ FCLG_HD bool shape_node_overlap(const DevMesh& m, const M3<double>& Rm, const D3
   return r == F_TRUE;
 }
 
+// Certified FP32 lower bound of the distance between a posed shape and a mesh node's
+// RSS (the node bound of the warp mesh-shape distance).  Along a direction n (mesh
+// frame; any n != 0 gives a valid bound):
+//   dist(shape, RSS) >= (min_shape n.x - max_RSS n.y) / |n|,
+//   max_RSS n.y = n.To + l0 max(0, n.a0) + l1 max(0, n.a1) + r|n|,
+//   min_shape n.x = n.t - h_A(-Rrel^T n)   (h_A the shape's support function),
+// with (Rrel, t) the shape's pose in the mesh frame and the RSS data FCL's FP64 values
+// rounded to FP32.  Forward error (u = 2^-24, no fused multiply-adds): 3-term dot
+// products of rounded inputs err by 4.1u ||n||_1 times the input's magnitude (|To| <=
+// rmax, |t_i| <= T, unit axes); the clamped axis terms by 6.2u ||n||_1 l; r|n| by 4.1u
+// ||n||_1 r; the rotated direction by 4.1u ||n||_1 per component, moving the support
+// value by at most sqrt(3) that times the shape's radius rho, and the support value
+// itself by under 10u ||n||_1 rho; the six final additions by 6u ||n||_1 times the sum
+// of the magnitudes.  Together under 24u ||n||_1 (rmax + T + rho + l0 + l1 + r); the
+// bound subtracts 32u ||n||_1 (...) (times 1.01 for its own rounding) and scales the
+// quotient by 1 - 8u (the division and |n|).
+struct MdPair {
+  float Rr[9];  // the shape's rotation in the mesh frame (row-major)
+  G3f tr;       // the shape's origin in the mesh frame
+  float rho;    // the shape's radius bound
+  float base;   // rmax + T + rho of the node error bound
+};
+FCLG_HD void md_pair(const DevMesh& m, const ShapeRef& A, const M3<double>& Rm, const D3v& tm, const M3<double>& Rs,
+                     const D3v& ts, MdPair& q) {
+  const M3<double> Rrel = mulT(Rm, Rs);
+  const D3v trel = mulTv(Rm, ts - tm);
+  for (int k = 0; k < 9; ++k) q.Rr[k] = (float)Rrel.m[k];
+  q.tr = g3f((float)trel.x, (float)trel.y, (float)trel.z);
+  q.rho = shape_radius32(A);
+  const float T = fmaxf(fabsf(q.tr.x), fmaxf(fabsf(q.tr.y), fabsf(q.tr.z)));
+  q.base = ((float)m.rmax * 1.0001f + T * 1.0001f) + q.rho;
+}
+FCLG_HD float md_node_lb(const ShapeRef& A, const MdPair& q, G3f n, float l0, float l1, float r, G3f To, G3f a0,
+                         G3f a1) {
+  const float nn = sqrtf(gdot(n, n));
+  if (!(nn > 0.f)) return -INFINITY;
+  const float n1 = (fabsf(n.x) + fabsf(n.y)) + fabsf(n.z);
+  const float hR = ((gdot(n, To) + l0 * fmaxf(0.f, gdot(n, a0))) + l1 * fmaxf(0.f, gdot(n, a1))) + r * nn;
+  const G3f uA = rot32T(q.Rr, n);
+  const G3f mu = g3f(-uA.x, -uA.y, -uA.z);
+  const float hA = gdot(mu, support32(A, mu));
+  const float gap = (gdot(n, q.tr) - hA) - hR;
+  const float E = 1.90734863e-06f * n1 * ((q.base + l0) + (l1 + r)) * 1.01f;  // 32u
+  const float g = gap - E;
+  if (!(g > 0.f)) return -INFINITY;
+  return g * (1.f - 4.76837158e-07f) / nn;  // 1 - 8u
+}
+// The larger of the bounds along two directions: from the RSS rectangle's point nearest
+// to the shape's origin to that origin, and dir when have_dir.
+FCLG_HD float md_node_bound(const float4* rss32, int b, const ShapeRef& A, const MdPair& q, bool have_dir, G3f dir) {
+  const float4 c0 = FCLG_LDG(rss32 + 5 * (long long)b), c1 = FCLG_LDG(rss32 + 5 * (long long)b + 1);
+  const float4 x0 = FCLG_LDG(rss32 + 5 * (long long)b + 2), x1 = FCLG_LDG(rss32 + 5 * (long long)b + 3);
+  const float4 x2 = FCLG_LDG(rss32 + 5 * (long long)b + 4);
+  const G3f To = g3f(c0.x, c0.y, c0.z), a0 = g3f(x0.x, x0.y, x0.z), a1 = g3f(x1.x, x1.y, x1.z);
+  const float r = c0.w, l0 = c1.x, l1 = c1.y;
+  const G3f d = q.tr - To;
+  const float s = fminf(fmaxf(gdot(d, a0), 0.f), l0), t = fminf(fmaxf(gdot(d, a1), 0.f), l1);
+  G3f n = d - a0 * s - a1 * t;
+  if (!(gdot(n, n) > 1e-12f * (gdot(d, d) + 1e-30f))) {
+    const G3f a2 = g3f(x2.x, x2.y, x2.z);
+    n = gdot(d, a2) >= 0.f ? a2 : g3f(-a2.x, -a2.y, -a2.z);
+  }
+  float lb = md_node_lb(A, q, n, l0, l1, r, To, a0, a1);
+  if (have_dir) lb = fmaxf(lb, md_node_lb(A, q, dir, l0, l1, r, To, a0, a1));
+  return lb;
+}
+
 // Resumable collide DFS of one pair over an explicit stack (stack[0..sp), capacity cap):
 // visits nodes in FCL's order and emits overlapping leaves until max_emit leaves have
 // been emitted, max_visits nodes have been tested or the stack is empty.  Returns the

@@ -12,6 +12,7 @@
 #include "shape_pair.cuh"
 #include "tri_contact.cuh"
 #include "motion.cuh"
+#include "mesh_shape.cuh"
 
 using namespace fclgpu;
 
@@ -317,25 +318,20 @@ int64_t emu_collide(int prec, const double* v1, int64_t nv1, const int32_t* t1, 
 
 }  // extern "C"
 
-extern "C" {
-
-// Host run of the device shape-pair query (shape_pair.cuh) over n pairs.
-void emu_shape_batch(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
-                     const double* verts, int64_t n, const int* ia, const int* ib, const double* tf1,
-                     const double* tf2, int* hit, double* normal, double* point, double* depth, double* dist,
-                     double* p1, double* p2, int* status) {
-  // the pool as fclgpu_shapeset_create lays it out: FP64 vertices, then the FP32
-  // float4 copy the convex supports filter with
+// The shape registry as fclgpu_shapeset_create lays it out: the FP64 vertex pool, then
+// the FP32 float4 copy the convex supports filter with; convex radii in p[0].
+void make_shapes(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                 const double* verts, std::vector<double>& pool, std::vector<DevShape>& sh) {
   int64_t nv = 0;
   for (int i = 0; i < ns; ++i)
     if (type[i] == SHAPE_CONVEX) nv = std::max<int64_t>(nv, (int64_t)voff[i] + vcnt[i]);
   const int64_t off32 = (3 * nv + 1) & ~int64_t(1);
-  std::vector<double> pool(off32 + 2 * nv + 2, 0.0);
+  pool.assign(off32 + 2 * nv + 2, 0.0);
   std::copy(verts, verts + 3 * nv, pool.begin());
   float* v32 = reinterpret_cast<float*>(pool.data() + off32);
   for (int64_t k = 0; k < nv; ++k)
     for (int c = 0; c < 3; ++c) v32[4 * k + c] = (float)verts[3 * k + c];
-  std::vector<DevShape> sh(ns);
+  sh.assign(ns, DevShape());
   for (int i = 0; i < ns; ++i) {
     sh[i].type = type[i];
     sh[i].voff = voff[i];
@@ -351,6 +347,18 @@ void emu_shape_batch(int ns, const int* type, const double* params, const int* v
       sh[i].p[0] = r * (1.0 + 1e-6);
     }
   }
+}
+
+extern "C" {
+
+// Host run of the device shape-pair query (shape_pair.cuh) over n pairs.
+void emu_shape_batch(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                     const double* verts, int64_t n, const int* ia, const int* ib, const double* tf1,
+                     const double* tf2, int* hit, double* normal, double* point, double* depth, double* dist,
+                     double* p1, double* p2, int* status) {
+  std::vector<double> pool;
+  std::vector<DevShape> sh;
+  make_shapes(ns, type, params, voff, vcnt, verts, pool, sh);
   for (int64_t q = 0; q < n; ++q) {
     PairOut o;
     shape_pair_query(sh[ia[q]], sh[ib[q]], pool.data(), tf1 + 12 * q, tf2 + 12 * q, o);
@@ -399,6 +407,77 @@ void emu_tri_contact_batch(int64_t n, const double* P, const double* Qm, int* co
 // translation, 1 linear, 2 screw.
 void emu_motion(int type, int64_t n, const double* beg, const double* end, const double* t, double* out) {
   for (int64_t i = 0; i < n; ++i) motion_at(type, beg + 12 * i, end + 12 * i, t[i], out + 12 * i);
+}
+
+// The certified FP32 bounds of the mesh-shape distance kernel (md_node_bound and
+// leaf_cert_lb) checked against FCL's FP64 shapeTriangleDistance on the host: for every
+// pair and every node, the node bound (along the nearest-point direction, and along
+// the pair's direction dirs[3 * i]) must not exceed the smallest FP64 distance of the
+// triangles below it by more than m64, and each triangle's bound not its own distance.
+// Returns the number of violations; *checked receives the number of comparisons made
+// and *positive how many bounds were above 0 (a bound that is never positive tests
+// nothing).
+int64_t emu_ms_bounds(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                      const double* verts, const double* mv, int64_t nv, const int32_t* mt, int64_t nt, int64_t n,
+                      const int32_t* sidx, const double* tfm, const double* tfs, const float* dirs, int64_t* checked,
+                      int64_t* positive) {
+  std::vector<double> pool;
+  std::vector<DevShape> sh;
+  make_shapes(ns, type, params, voff, vcnt, verts, pool, sh);
+  HostMesh hm;
+  make_mesh(mv, nv, mt, nt, hm);
+  const DevMesh& m = hm.view;
+  const float4* rss32 = static_cast<const float4*>(m.rss32);
+  int64_t bad = 0, nchk = 0, npos = 0;
+  std::vector<double> dmin(m.n_nodes);
+  for (int64_t i = 0; i < n; ++i) {
+    ShapeRef A;
+    A.s = sh[sidx[i]];
+    A.verts = pool.data();
+    M3<double> Rm, Rs;
+    D3v tm, ts;
+    load_tf(tfm + 12 * i, Rm, tm);
+    load_tf(tfs + 12 * i, Rs, ts);
+    MdPair q;
+    md_pair(m, A, Rm, tm, Rs, ts, q);
+    LeafCert32 cert;
+    leaf_cert_init(A, Rs, ts, Rm, tm, cert);
+    const double m64 = std::ldexp(1.0 + (double)q.rho + std::max(std::fabs(ts.x), std::max(std::fabs(ts.y), std::fabs(ts.z))) +
+                                      std::max(std::fabs(tm.x), std::max(std::fabs(tm.y), std::fabs(tm.z))) + m.vmax + m.rmax,
+                                  -36);
+    const G3f dir = g3f(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+    // children are stored after their parent: a reverse sweep sees them first
+    for (int b = m.n_nodes - 1; b >= 0; --b) {
+      const int c = m.nodes64[b].child;
+      if (c < 0) {
+        double P[9];
+        load_tri_local(m, -(c + 1), P);
+        SimplexVert V[kSimplexSlots];
+        D3v ps, pt;
+        double d;
+        shape_triangle_distance(A, Rs, ts, P, Rm, tm, V, d, ps, pt);
+        dmin[b] = d > 0.0 ? d : 0.0;
+        if (A.s.type != SHAPE_SPHERE && d > 0.0) {
+          G3f dd;
+          const float lb = leaf_cert_lb(cert, P, dd);
+          ++nchk;
+          if (lb > 0.f) ++npos;
+          if ((double)lb > d + m64) ++bad;
+        }
+      } else {
+        dmin[b] = std::min(dmin[c], dmin[c + 1]);
+      }
+      for (int k = 0; k < 2; ++k) {
+        const float lb = md_node_bound(rss32, b, A, q, k == 1, dir);
+        ++nchk;
+        if (lb > 0.f) ++npos;
+        if ((double)lb > dmin[b] + m64) ++bad;
+      }
+    }
+  }
+  *checked = nchk;
+  *positive = npos;
+  return bad;
 }
 
 }  // extern "C"

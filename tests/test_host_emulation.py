@@ -171,3 +171,34 @@ def test_certified_fp32_distance_separated_pairs():
         od, opts, ed, epts, _ = _cert_vs_oracle(a, b, w.tf2[idx])
         assert np.array_equal(ed, od)
         assert np.abs(epts - opts).max() <= 1e-12
+
+
+def test_mesh_shape_certified_bounds_hold():
+    """The FP32 lower bounds of the warp mesh-shape distance (node: support gap of the
+    shape against the node's RSS along two directions; triangle: the FP32 GJK
+    certificate's gap) never exceed FCL's FP64 shapeTriangleDistance of the triangles
+    below them (by more than m64), for every shape type, near and far poses and
+    arbitrary directions -- the property that lets the kernel skip volumes and
+    triangles.  Host build of the device functions."""
+    import ctypes as C
+    v, t = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, 41)
+    shapes = W.random_shapes(48, 42)
+    rng = np.random.default_rng(43)
+    n = 160
+    sidx = rng.integers(0, 48, size=n).astype(np.int32)
+    tfm = W.random_poses(n, -0.2, 0.2, 44)
+    tfs = W.random_poses(n, -1.6, 1.6, 45)
+    dirs = rng.normal(size=(n, 3)).astype(np.float32)
+    chk, pos = C.c_int64(), C.c_int64()
+    # the arrays are kept alive for the call
+    arrs = [np.ascontiguousarray(a, dt) for a, dt in
+            ((shapes.type, np.int32), (shapes.params, np.float64), (shapes.voff, np.int32), (shapes.vcnt, np.int32),
+             (shapes.verts, np.float64), (v, np.float64), (t, np.int32), (sidx, np.int32), (tfm, np.float64),
+             (tfs, np.float64), (dirs, np.float32))]
+    ty, pa, vo, vc, sv, mv, mt, si, tm, ts, dr = [C.c_void_p(a.ctypes.data) for a in arrs]
+    lib = emul.lib()
+    lib.emu_ms_bounds.restype = C.c_int64
+    bad = lib.emu_ms_bounds(C.c_int(48), ty, pa, vo, vc, sv, mv, C.c_int64(v.shape[0]), mt, C.c_int64(t.shape[0]),
+                            C.c_int64(n), si, tm, ts, dr, C.byref(chk), C.byref(pos))
+    assert bad == 0
+    assert chk.value > 100000 and pos.value > chk.value // 10
