@@ -480,4 +480,41 @@ int64_t emu_ms_bounds(int ns, const int* type, const double* params, const int* 
   return bad;
 }
 
+// The prepared leaf certificate (LeafCert32: poses and shape supports rounded once per
+// pair) against the per-call certified_disjoint on n (shape, triangle) pairs of one
+// posed mesh: returns the number of pairs where the two disagree; *disjoint receives
+// how many the certificate proved disjoint.
+int64_t emu_leaf_cert(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                      const double* verts, const double* mv, int64_t nv, const int32_t* mt, int64_t nt, int64_t n,
+                      const int32_t* sidx, const double* tfm, const double* tfs, int64_t* disjoint) {
+  std::vector<double> pool;
+  std::vector<DevShape> sh;
+  make_shapes(ns, type, params, voff, vcnt, verts, pool, sh);
+  HostMesh hm;
+  make_mesh(mv, nv, mt, nt, hm);
+  const DevMesh& m = hm.view;
+  int64_t diff = 0, dis = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    ShapeRef A;
+    A.s = sh[sidx[i]];
+    A.verts = pool.data();
+    M3<double> Rm, Rs;
+    D3v tm, ts;
+    load_tf(tfm + 12 * i, Rm, tm);
+    load_tf(tfs + 12 * i, Rs, ts);
+    LeafCert32 c;
+    leaf_cert_init(A, Rs, ts, Rm, tm, c);
+    for (int p = 0; p < m.n_tris; ++p) {
+      double P[9];
+      load_tri_local(m, p, P);
+      const bool a = leaf_cert_disjoint(c, P);
+      const bool b = certified_disjoint(A, Rs, ts, triangle_ref(P), Rm, tm);
+      diff += a != b;
+      dis += a;
+    }
+  }
+  *disjoint = dis;
+  return diff;
+}
+
 }  // extern "C"

@@ -202,3 +202,30 @@ def test_mesh_shape_certified_bounds_hold():
                             C.c_int64(n), si, tm, ts, dr, C.byref(chk), C.byref(pos))
     assert bad == 0
     assert chk.value > 100000 and pos.value > chk.value // 10
+
+
+def test_prepared_leaf_certificate_equals_per_call_form():
+    """LeafCert32 (poses, relative rotations and the shape's supports rounded to FP32 once
+    per pair, each triangle's vertices once) decides exactly as certified_disjoint, which
+    rounds them on every support call: every (shape, triangle) pair of 60 posed shapes of
+    every type against a 720-triangle mesh."""
+    import ctypes as C
+    v, t = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, 51)
+    shapes = W.random_shapes(48, 52)
+    rng = np.random.default_rng(53)
+    n = 60
+    sidx = rng.integers(0, 48, size=n).astype(np.int32)
+    tfm = W.random_poses(n, -0.2, 0.2, 54)
+    tfs = W.random_poses(n, -1.2, 1.2, 55)
+    arrs = [np.ascontiguousarray(a, dt) for a, dt in
+            ((shapes.type, np.int32), (shapes.params, np.float64), (shapes.voff, np.int32), (shapes.vcnt, np.int32),
+             (shapes.verts, np.float64), (v, np.float64), (t, np.int32), (sidx, np.int32), (tfm, np.float64),
+             (tfs, np.float64))]
+    ty, pa, vo, vc, sv, mv, mt, si, tm, ts = [C.c_void_p(a.ctypes.data) for a in arrs]
+    dis = C.c_int64()
+    lib = emul.lib()
+    lib.emu_leaf_cert.restype = C.c_int64
+    diff = lib.emu_leaf_cert(C.c_int(48), ty, pa, vo, vc, sv, mv, C.c_int64(v.shape[0]), mt, C.c_int64(t.shape[0]),
+                             C.c_int64(n), si, tm, ts, C.byref(dis))
+    assert diff == 0
+    assert 0 < dis.value < n * t.shape[0]
