@@ -47,3 +47,20 @@ def test_header_is_plain_c(tmp_path):
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
                         "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_fcl_binding_compiles():
+    """The binding a maintainer would add inside FCL (tests/native/fcl_shim_check.cpp:
+    fcl::collide with and without contact geometry, fcl::continuousCollide, a broadphase
+    manager's collide forms) compiles against include/fclgpu.h with stand-ins for the
+    FCL types it touches."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        import pytest
+        pytest.skip("no C++ compiler")
+    src = os.path.join(ROOT, "tests", "native", "fcl_shim_check.cpp")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
