@@ -366,11 +366,9 @@ __global__ void __launch_bounds__(128) k_msr_recount(MeshShapeLaunch L, const in
 constexpr int kMsWarps = 4;
 constexpr int kMsFront = 2048;
 constexpr int kMsWarpMaxDepth = kMsFront / 32 - 4;
-#ifndef FCLG_MS_MINB
-#define FCLG_MS_MINB 1
-#endif
+// (register caps of 168 and 128 for more resident warps were measured slower: spills)
 
-__global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(MeshShapeLaunch L) {
+__global__ void __launch_bounds__(32 * kMsWarps) k_ms_count_warp(MeshShapeLaunch L) {
   __shared__ int32_t front[kMsWarps][kMsFront];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long i = (long long)blockIdx.x * kMsWarps + w;
@@ -482,9 +480,6 @@ __global__ void __launch_bounds__(32 * kMsWarps, FCLG_MS_MINB) k_ms_count_warp(M
 constexpr int kMdWarps = 2;
 constexpr int kMdFront = 1024;
 constexpr int kMdWarpMaxDepth = kMdFront / 32 - 4;
-#ifndef FCLG_MD_MINB
-#define FCLG_MD_MINB 1
-#endif
 
 // one compare-exchange network sorting 64 entries held two per lane (entry e = lane +
 // 32 * slot) by (key, node), ascending; pay travels with its entry
@@ -545,7 +540,7 @@ __device__ __forceinline__ unsigned md_child_path(unsigned path, int which) {
 }
 
 template <bool WIT>
-__global__ void __launch_bounds__(32 * kMdWarps, FCLG_MD_MINB) k_ms_dist_warp(MeshShapeLaunch L) {
+__global__ void __launch_bounds__(32 * kMdWarps) k_ms_dist_warp(MeshShapeLaunch L) {
   __shared__ int32_t fnode[kMdWarps][kMdFront];
   __shared__ float flb[kMdWarps][kMdFront];
   __shared__ unsigned fpath[kMdWarps][kMdFront];
