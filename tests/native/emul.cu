@@ -517,4 +517,89 @@ int64_t emu_leaf_cert(int ns, const int* type, const double* params, const int* 
   return diff;
 }
 
+// The rule the warp mesh-shape distance applies to a pair with an intersecting triangle,
+// run on the host over the whole tree: FCL's seed triangle 0 first, then the first
+// triangle at distance < 0 in FCL's depth-first order (children ordered by its FP64
+// bounds, the second first on d2 < d1), provided every bound on that triangle's path is
+// exactly 0 and no triangle before it is at distance exactly 0.  tri[i] = the rule's
+// triangle, or -1 where it does not apply (no intersecting triangle, or a condition
+// fails: the kernel then runs FCL's serial traversal); dist[i] = that triangle's FP64
+// distance.
+void emu_ms_contact_rule(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                         const double* verts, const double* mv, int64_t nv, const int32_t* mt, int64_t nt, int64_t n,
+                         const int32_t* sidx, const double* tfm, const double* tfs, int32_t* tri, double* dist) {
+  std::vector<double> pool;
+  std::vector<DevShape> sh;
+  make_shapes(ns, type, params, voff, vcnt, verts, pool, sh);
+  HostMesh hm;
+  make_mesh(mv, nv, mt, nt, hm);
+  const DevMesh& m = hm.view;
+  for (int64_t i = 0; i < n; ++i) {
+    ShapeRef A;
+    A.s = sh[sidx[i]];
+    A.verts = pool.data();
+    M3<double> Rm, Rs;
+    D3v tm, ts;
+    load_tf(tfm + 12 * i, Rm, tm);
+    load_tf(tfs + 12 * i, Rs, ts);
+    ShapeBV bv;
+    shape_obbrss(A.s, A.verts, Rs, ts, bv);
+    M3<double> Ab;
+    for (int k = 0; k < 9; ++k) Ab.m[k] = bv.obb.axis[k];
+    const D3v Tob = v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]);
+    auto bvd = [&](int b) {
+      const RssD& rs = m.rss64[b];
+      M3<double> A2;
+      for (int k = 0; k < 9; ++k) A2.m[k] = rs.axis[k];
+      return rss_distance<double>(Rm, tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
+    };
+    auto leaf_d = [&](int prim) {
+      double P[9];
+      load_tri_local(m, prim, P);
+      SimplexVert V[kSimplexSlots];
+      D3v ps, pt;
+      double d;
+      shape_triangle_distance(A, Rs, ts, P, Rm, tm, V, d, ps, pt);
+      return d;
+    };
+    tri[i] = -1;
+    dist[i] = 0.0;
+    const double d0 = leaf_d(0);
+    if (d0 < 0.0) {
+      tri[i] = 0;
+      dist[i] = d0;
+      continue;
+    }
+    if (d0 == 0.0) continue;
+    // depth-first in FCL's order: (node, all bounds on its path are 0)
+    std::vector<std::pair<int, bool>> stack{{0, true}};
+    bool zero_before = false;
+    while (!stack.empty()) {
+      const auto [b, zero] = stack.back();
+      stack.pop_back();
+      const int c = m.nodes64[b].child;
+      if (c < 0) {
+        const double d = leaf_d(-(c + 1));
+        if (d == 0.0) zero_before = true;
+        if (d < 0.0) {
+          if (zero && !zero_before) {
+            tri[i] = -(c + 1);
+            dist[i] = d;
+          }
+          break;
+        }
+        continue;
+      }
+      const double d1 = bvd(c), d2 = bvd(c + 1);
+      if (d2 < d1) {  // c + 1 first: pushed last
+        stack.push_back({c, zero && d1 == 0.0});
+        stack.push_back({c + 1, zero && d2 == 0.0});
+      } else {
+        stack.push_back({c + 1, zero && d2 == 0.0});
+        stack.push_back({c, zero && d1 == 0.0});
+      }
+    }
+  }
+}
+
 }  // extern "C"
