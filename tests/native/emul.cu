@@ -602,4 +602,96 @@ void emu_ms_contact_rule(int ns, const int* type, const double* params, const in
   }
 }
 
+// The rule the warp mesh-shape distance applies to a pair without an intersecting
+// triangle, run on the host over every triangle: the distance is the smallest FP64
+// shapeTriangleDistance, and of the triangles at that distance FCL's first -- triangle 0
+// (the seed) if it is one, otherwise the one on the side FCL enters first at their
+// deepest common node (children ordered by its FP64 bounds, the second first on
+// d2 < d1).  tri[i] = -1 where some triangle is at distance <= 0; ties[i] = the number
+// of triangles at the minimum.
+void emu_ms_min_rule(int ns, const int* type, const double* params, const int* voff, const int* vcnt,
+                     const double* verts, const double* mv, int64_t nv, const int32_t* mt, int64_t nt, int64_t n,
+                     const int32_t* sidx, const double* tfm, const double* tfs, int32_t* tri, double* dist,
+                     int32_t* ties) {
+  std::vector<double> pool;
+  std::vector<DevShape> sh;
+  make_shapes(ns, type, params, voff, vcnt, verts, pool, sh);
+  HostMesh hm;
+  make_mesh(mv, nv, mt, nt, hm);
+  const DevMesh& m = hm.view;
+  // parent of every node (children are allocated after their parent)
+  std::vector<int> parent(m.n_nodes, -1), leaf_of(m.n_tris, -1);
+  for (int b = 0; b < m.n_nodes; ++b) {
+    const int c = m.nodes64[b].child;
+    if (c >= 0) {
+      parent[c] = b;
+      parent[c + 1] = b;
+    } else {
+      leaf_of[-(c + 1)] = b;
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    ShapeRef A;
+    A.s = sh[sidx[i]];
+    A.verts = pool.data();
+    M3<double> Rm, Rs;
+    D3v tm, ts;
+    load_tf(tfm + 12 * i, Rm, tm);
+    load_tf(tfs + 12 * i, Rs, ts);
+    ShapeBV bv;
+    shape_obbrss(A.s, A.verts, Rs, ts, bv);
+    M3<double> Ab;
+    for (int k = 0; k < 9; ++k) Ab.m[k] = bv.obb.axis[k];
+    const D3v Tob = v3(bv.rTo[0], bv.rTo[1], bv.rTo[2]);
+    auto bvd = [&](int b) {
+      const RssD& rs = m.rss64[b];
+      M3<double> A2;
+      for (int k = 0; k < 9; ++k) A2.m[k] = rs.axis[k];
+      return rss_distance<double>(Rm, tm, Ab, Tob, bv.rl, bv.rr, A2, v3(rs.To[0], rs.To[1], rs.To[2]), rs.l, rs.r);
+    };
+    double best = DBL_MAX;
+    std::vector<int> at;
+    bool contact = false;
+    for (int p = 0; p < m.n_tris; ++p) {
+      double P[9];
+      load_tri_local(m, p, P);
+      SimplexVert V[kSimplexSlots];
+      D3v ps, pt;
+      double d;
+      shape_triangle_distance(A, Rs, ts, P, Rm, tm, V, d, ps, pt);
+      if (!(d > 0.0)) contact = true;
+      if (d < best) {
+        best = d;
+        at.assign(1, p);
+      } else if (d == best) {
+        at.push_back(p);
+      }
+    }
+    ties[i] = (int32_t)at.size();
+    dist[i] = best;
+    tri[i] = -1;
+    if (contact) continue;
+    // FCL's first of the tied triangles
+    auto path = [&](int p) {
+      std::vector<int> up;
+      for (int b = leaf_of[p]; b >= 0; b = parent[b]) up.push_back(b);
+      return std::vector<int>(up.rbegin(), up.rend());  // root first
+    };
+    auto first = [&](int a, int b) {
+      if (a == 0) return a;
+      if (b == 0) return b;
+      const std::vector<int> pa = path(a), pb = path(b);
+      size_t k = 0;
+      while (pa[k + 1] == pb[k + 1]) ++k;  // pa[k] is the deepest common node
+      const int c = m.nodes64[pa[k]].child;
+      const bool second_first = bvd(c + 1) < bvd(c);
+      const bool a_second = pa[k + 1] == c + 1;
+      return a_second == second_first ? a : b;
+    };
+    int w = at[0];
+    for (size_t j = 1; j < at.size(); ++j) w = first(w, at[j]);
+    tri[i] = w;
+  }
+}
+
 }  // extern "C"

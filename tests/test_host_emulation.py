@@ -261,3 +261,42 @@ def test_intersecting_pair_rule_matches_oracle():
     np.testing.assert_array_equal(o["dist"][applies], dist[applies])
     neg = o["dist"] < 0
     assert neg.sum() > 50 and applies[neg].mean() > 0.9
+
+
+def test_separated_pair_min_and_tie_rule_matches_oracle():
+    """The warp mesh-shape distance's rule for a pair without an intersecting triangle --
+    the smallest FP64 distance over all triangles, and of the triangles tied at it FCL's
+    first (the seed triangle 0, else the side FCL enters first at their deepest common
+    node) -- gives the oracle's distance and triangle.  Shapes just outside mesh vertices,
+    so that many minima are shared by several triangles."""
+    import ctypes as C
+    v, t = W.perturbed_ellipsoid(6, (0.8, 0.6, 0.5), 0.01, 31)
+    shapes = W.random_shapes(64, 32)
+    rng = np.random.default_rng(33)
+    n = 400
+    spheres = np.flatnonzero(shapes.type == W.SPHERE)
+    sidx = np.where(rng.uniform(size=n) < 0.6, rng.choice(spheres, size=n),
+                    rng.integers(0, 64, size=n)).astype(np.int32)
+    k = rng.integers(0, v.shape[0], size=n)
+    u = v[k] - v.mean(axis=0)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    reach = np.where(shapes.type[sidx] == W.SPHERE, shapes.params[sidx, 0], 0.6)
+    tfs = W.random_poses(n, 0.0, 0.0, 34)
+    tfs[:, :, 3] = v[k] + u * (reach + rng.uniform(0.002, 0.3, size=n))[:, None]
+    tfm = W.identity_poses(n)
+    arrs = [np.ascontiguousarray(a, dt) for a, dt in
+            ((shapes.type, np.int32), (shapes.params, np.float64), (shapes.voff, np.int32), (shapes.vcnt, np.int32),
+             (shapes.verts, np.float64), (v, np.float64), (t, np.int32), (sidx, np.int32), (tfm, np.float64),
+             (tfs, np.float64))]
+    ty, pa, vo, vc, sv, mv, mt, si, tm, ts = [C.c_void_p(a.ctypes.data) for a in arrs]
+    tri = np.empty(n, np.int32)
+    dist = np.empty(n)
+    ties = np.empty(n, np.int32)
+    emul.lib().emu_ms_min_rule(C.c_int(64), ty, pa, vo, vc, sv, mv, C.c_int64(v.shape[0]), mt,
+                               C.c_int64(t.shape[0]), C.c_int64(n), si, tm, ts, C.c_void_p(tri.ctypes.data),
+                               C.c_void_p(dist.ctypes.data), C.c_void_p(ties.ctypes.data))
+    o = O.mesh_shape_distance(O.Mesh(v, t), O.Geoms(shapes), sidx, tfm, tfs, nthreads=8)
+    applies = tri >= 0
+    assert applies.mean() > 0.9 and (ties[applies] > 1).sum() > 50
+    np.testing.assert_array_equal(o["tri"][applies], tri[applies])
+    np.testing.assert_array_equal(o["dist"][applies], dist[applies])
