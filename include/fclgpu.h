@@ -485,9 +485,11 @@ FCLGPU_API int fclgpu_last_shape_kernel_time(double* ms);
  * mesh_shape_collision_traversal_node-inl.h and mesh_shape_distance_traversal_node-inl.h):
  * the shape's OBBRSS is fitted to its bound vertices, the mesh BVH is traversed against
  * it, and the leaves run shapeTriangleIntersect / shapeTriangleDistance (sphere-triangle
- * closed forms, GJK/EPA otherwise).  FP64.  Pair i: meshes[mesh_idx[i]] at tf_mesh[i]
- * and shape shape_idx[i] of the set at tf_shape[i].  (fcl::collide(shape, mesh) is the
- * same call: FCL swaps the arguments.) */
+ * closed forms, GJK/EPA otherwise).  Results are FCL's FP64 ones: FP32 filters and
+ * certified FP32 bounds only skip volumes and triangles that cannot change them, and
+ * every deciding test runs in FP64.  Pair i: meshes[mesh_idx[i]] at tf_mesh[i] and
+ * shape shape_idx[i] of the set at tf_shape[i].  (fcl::collide(shape, mesh) is the same
+ * call: FCL swaps the arguments.) */
 enum { FCLGPU_MESH_SHAPE_COLLIDE = 0, FCLGPU_MESH_SHAPE_DISTANCE = 1 };
 
 typedef struct {
