@@ -16,9 +16,13 @@
 // and matrix products sum left to right, ((x0 + x1) + x2); no fused multiply-add
 // (this file is compiled with -ffp-contract=off).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <limits>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "bvh_build.h"
@@ -45,58 +49,128 @@ class Builder {
     (void)nv;
   }
 
+  // Node ids are FCL's: a node's children are the pair (num_bvs, num_bvs + 1) taken when
+  // the node is split, in depth-first order, so a node split with `base` as num_bvs
+  // gives its left subtree base + 2 and its right subtree base + 2 * (left primitives)
+  // (a subtree of k primitives takes 2 (k - 1) ids).  Subtrees are therefore
+  // independent: large meshes split their upper levels into tasks run on several host
+  // threads, with the same ids, the same partitions and so the same tree.
   void run(HostBVH& out) {
     const int n_nodes = 2 * nt_ - 1;
     out.nodes.assign(n_nodes, NodeD());
     out.rss.assign(n_nodes, RssD());
     prim_.resize(nt_);
     for (int i = 0; i < nt_; ++i) prim_[i] = (uint32_t)i;
-    int next_id = 1;
-    int max_depth = 0;
-    struct Task {
-      int id, first, count, depth;
-    };
-    std::vector<Task> todo;
-    todo.push_back({0, 0, nt_, 0});
-    while (!todo.empty()) {
-      Task tk = todo.back();
-      todo.pop_back();
-      max_depth = std::max(max_depth, tk.depth);
-      NodeD& nd = out.nodes[tk.id];
-      RssD& rs = out.rss[tk.id];
-      uint32_t* span = prim_.data() + tk.first;
-      fit(span, tk.count, nd, rs);
-      for (int k = 0; k < 9; ++k) rs.axis[k] = nd.axis[k];  // BVFitter<OBBRSS>: rss.axis = obb.axis
-      if (tk.count == 1) {
-        nd.child = -((int)span[0] + 1);
-        continue;
-      }
-      const D3 axis0 = colk(nd.axis, 0);
-      const double split = mean_split_value(span, tk.count, axis0);
-      nd.child = next_id;
-      next_id += 2;
-      int left = 0;
-      for (int i = 0; i < tk.count; ++i) {
-        const int32_t* t = T_ + 3 * (int64_t)span[i];
-        const double* p1 = V_ + 3 * (int64_t)t[0];
-        const double* p2 = V_ + 3 * (int64_t)t[1];
-        const double* p3 = V_ + 3 * (int64_t)t[2];
-        D3 c = d3(((p1[0] + p2[0]) + p3[0]) / 3.0, ((p1[1] + p2[1]) + p3[1]) / 3.0,
-                  ((p1[2] + p2[2]) + p3[2]) / 3.0);
-        if (!(dotd(axis0, c) > split)) {
-          std::swap(span[i], span[left]);
-          ++left;
-        }
-      }
-      if (left == 0 || left == tk.count) left = tk.count / 2;
-      // depth-first: left subtree is completed before the right one starts
-      todo.push_back({nd.child + 1, tk.first + left, tk.count - left, tk.depth + 1});
-      todo.push_back({nd.child, tk.first, left, tk.depth + 1});
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int workers = nt_ >= kParallelMin ? (int)std::min(16u, std::max(1u, hw)) : 1;
+    if (workers <= 1) {
+      std::vector<double> proj;
+      out.max_depth = subtree(Task{0, 0, nt_, 0, 1}, out, proj);
+      return;
     }
+    // shared task stack: tasks of at least kTaskMin primitives are split here and
+    // their children queued; smaller ones run as whole subtrees
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<Task> tasks{Task{0, 0, nt_, 0, 1}};
+    int outstanding = 1, max_depth = 0;
+    auto worker = [&]() {
+      std::vector<double> proj;
+      int local_depth = 0;
+      for (;;) {
+        Task tk;
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv.wait(lk, [&] { return !tasks.empty() || outstanding == 0; });
+          if (tasks.empty()) break;
+          tk = tasks.back();
+          tasks.pop_back();
+        }
+        Task kids[2];
+        int nkids = 0;
+        if (tk.count >= kTaskMin) {
+          local_depth = std::max(local_depth, node(tk, out, proj, kids, nkids));
+        } else {
+          local_depth = std::max(local_depth, subtree(tk, out, proj));
+        }
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          for (int k = 0; k < nkids; ++k) tasks.push_back(kids[k]);
+          outstanding += nkids - 1;
+        }
+        cv.notify_all();
+      }
+      std::lock_guard<std::mutex> lk(mu);
+      max_depth = std::max(max_depth, local_depth);
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < workers; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
     out.max_depth = max_depth;
   }
 
  private:
+  static constexpr int kParallelMin = 16384;  // meshes below this build on one thread
+  static constexpr int kTaskMin = 4096;       // tasks this large are split into two tasks
+
+  struct Task {
+    int id, first, count, depth;
+    int base;  // FCL's num_bvs when this node is split
+  };
+
+  // Fits node tk and, unless it is a leaf, splits its primitives (FCL's mean split with
+  // its in-place partition) and returns its two children as tasks (kids, nkids).
+  // Returns the node's depth.
+  int node(const Task& tk, HostBVH& out, std::vector<double>& proj, Task* kids, int& nkids) {
+    nkids = 0;
+    NodeD& nd = out.nodes[tk.id];
+    RssD& rs = out.rss[tk.id];
+    uint32_t* span = prim_.data() + tk.first;
+    fit(span, tk.count, nd, rs, proj);
+    for (int k = 0; k < 9; ++k) rs.axis[k] = nd.axis[k];  // BVFitter<OBBRSS>: rss.axis = obb.axis
+    if (tk.count == 1) {
+      nd.child = -((int)span[0] + 1);
+      return tk.depth;
+    }
+    const D3 axis0 = colk(nd.axis, 0);
+    const double split = mean_split_value(span, tk.count, axis0);
+    nd.child = tk.base;
+    int left = 0;
+    for (int i = 0; i < tk.count; ++i) {
+      const int32_t* t = T_ + 3 * (int64_t)span[i];
+      const double* p1 = V_ + 3 * (int64_t)t[0];
+      const double* p2 = V_ + 3 * (int64_t)t[1];
+      const double* p3 = V_ + 3 * (int64_t)t[2];
+      D3 c = d3(((p1[0] + p2[0]) + p3[0]) / 3.0, ((p1[1] + p2[1]) + p3[1]) / 3.0,
+                ((p1[2] + p2[2]) + p3[2]) / 3.0);
+      if (!(dotd(axis0, c) > split)) {
+        std::swap(span[i], span[left]);
+        ++left;
+      }
+    }
+    if (left == 0 || left == tk.count) left = tk.count / 2;
+    // right first: a LIFO runs the left subtree first, as FCL's recursion does
+    kids[0] = Task{nd.child + 1, tk.first + left, tk.count - left, tk.depth + 1, tk.base + 2 * left};
+    kids[1] = Task{nd.child, tk.first, left, tk.depth + 1, tk.base + 2};
+    nkids = 2;
+    return tk.depth;
+  }
+
+  // The whole subtree of tk on this thread; returns its largest depth.
+  int subtree(const Task& root, HostBVH& out, std::vector<double>& proj) {
+    int max_depth = 0;
+    std::vector<Task> todo{root};
+    while (!todo.empty()) {
+      const Task tk = todo.back();
+      todo.pop_back();
+      Task kids[2];
+      int nkids = 0;
+      max_depth = std::max(max_depth, node(tk, out, proj, kids, nkids));
+      for (int k = 0; k < nkids; ++k) todo.push_back(kids[k]);
+    }
+    return max_depth;
+  }
+
   const double* vtx(int32_t id) const { return V_ + 3 * (int64_t)id; }
 
   double mean_split_value(const uint32_t* span, int n, const D3& sv) const {
@@ -111,7 +185,7 @@ class Builder {
     return (c0 * sv.x + c1 * sv.y + c2 * sv.z) / (3 * n);
   }
 
-  void fit(const uint32_t* span, int n, NodeD& nd, RssD& rs) {
+  void fit(const uint32_t* span, int n, NodeD& nd, RssD& rs, std::vector<double>& proj_) {
     // --- covariance of the 3n vertices
     double s1x = 0, s1y = 0, s1z = 0;
     double sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
@@ -358,7 +432,6 @@ class Builder {
   const int32_t* T_;
   int nt_;
   std::vector<uint32_t> prim_;
-  std::vector<double> proj_;
 };
 
 inline float f32(double x) { return (float)x; }

@@ -16,7 +16,7 @@ def build() -> str:
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     cmd = ["nvcc", "-gencode=arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-fmad=false",
            "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", CSRC, "-shared",
-           "-x", "cu", srcs[0], "-x", "c++", srcs[1], "-o", OUT]
+           "-x", "cu", srcs[0], "-x", "c++", srcs[1], "-o", OUT, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("emulation build failed:\n" + r.stdout + r.stderr)

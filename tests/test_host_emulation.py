@@ -20,6 +20,18 @@ def test_bvh_build_bit_exact(freq, seed):
     assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
 
 
+@pytest.mark.parametrize("freq,seed", [(32, 4), (56, 5)])
+def test_bvh_build_bit_exact_parallel(freq, seed):
+    """Meshes of 20,480 and 62,720 triangles: the upper levels are built as tasks on
+    several host threads, with FCL's node ids fixed in advance; the tree is still the
+    oracle's bit for bit."""
+    v, t = W.perturbed_ellipsoid(freq, (1.0, 0.7, 0.5), 0.01, seed)
+    on, ofc = O.Mesh(v, t).nodes()
+    en, efc, _ = emul.build(v, t)
+    assert np.array_equal(ofc, efc)
+    assert np.array_equal(on.view(np.uint64), en.view(np.uint64))
+
+
 def test_bvh_build_bit_exact_reference_meshes(golden):
     for k in ("env", "rob"):
         on, ofc = O.Mesh(golden[k + "_v"], golden[k + "_t"]).nodes()
